@@ -1,0 +1,308 @@
+"""ctypes mirror of include/avbd_cuda.h and numpy-backed world buffers.
+
+`World` owns numpy arrays for every field of `avbd_world` and exposes a
+ctypes struct whose pointers reference them, so the same object can be handed
+to the CUDA backend (`libavbd_gb300.so`) and to the f64 oracle used by the
+tests. Field order and types must match include/avbd_cuda.h exactly.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import math
+
+import numpy as np
+
+AVBD_OK = 0
+AVBD_ERR_ARG = -1
+AVBD_ERR_CAPACITY = -2
+AVBD_ERR_CUDA = -3
+AVBD_ERR_TIMEOUT = -4
+AVBD_ERR_NAN = -5
+AVBD_ERR_STATE = -6
+
+SHAPE_BOX = 0
+SHAPE_SPHERE = 1
+
+ORDER_REFERENCE = 0
+ORDER_EXPLICIT = 1
+ORDER_PRIORITY = 2
+
+MAX_CONTACTS = 8
+MAX_COLORS = 64
+
+_d = C.POINTER(C.c_double)
+_i = C.POINTER(C.c_int32)
+_u = C.POINTER(C.c_uint32)
+
+
+class Params(C.Structure):
+    _fields_ = [
+        ("dt", C.c_double), ("gravity", C.c_double),
+        ("iterations", C.c_int32), ("post_stabilize", C.c_int32),
+        ("beta_lin", C.c_double), ("beta_ang", C.c_double),
+        ("alpha", C.c_double), ("gamma", C.c_double),
+        ("penalty_min", C.c_double), ("penalty_max", C.c_double),
+        ("collision_margin", C.c_double), ("stick_threshold", C.c_double),
+        ("rotated_inertia", C.c_int32), ("spring_stiffness_ramp", C.c_int32),
+        ("spring_geometric_stiffness", C.c_int32), ("cached_contact_jacobians", C.c_int32),
+        ("broadphase", C.c_int32), ("hash_threshold", C.c_int32),
+        ("body_order", C.c_int32), ("reserved0", C.c_int32),
+        ("fp64_ratio_threshold", C.c_double),
+        ("max_pairs_per_body", C.c_int32), ("max_adjacency", C.c_int32),
+        ("lanes_per_body", C.c_int32), ("blocks_per_sm", C.c_int32),
+    ]
+
+
+def default_params(**overrides) -> Params:
+    """`Solver.defaultParams()` (src/physics/solver.js:92-236)."""
+    p = Params()
+    p.dt = 1.0 / 60.0
+    p.gravity = -10.0
+    p.iterations = 10
+    p.post_stabilize = 0
+    p.beta_lin = 1e4
+    p.beta_ang = 100.0
+    p.alpha = 0.95
+    p.gamma = 0.999
+    p.penalty_min = 1.0
+    p.penalty_max = 1e10
+    p.collision_margin = 0.01
+    p.stick_threshold = 1e-5
+    p.rotated_inertia = 1
+    p.spring_stiffness_ramp = 0
+    p.spring_geometric_stiffness = 1
+    p.cached_contact_jacobians = 1
+    p.broadphase = 0
+    p.hash_threshold = 150
+    p.body_order = ORDER_REFERENCE
+    p.fp64_ratio_threshold = 1e5
+    for k, v in overrides.items():
+        if not hasattr(p, k):
+            raise AttributeError(k)
+        setattr(p, k, v)
+    return p
+
+
+class BodySoA(C.Structure):
+    _fields_ = [("count", C.c_int32), ("shape", _i), ("size", _d), ("mass", _d), ("moment", _d),
+                ("radius", _d), ("friction", _d), ("pos", _d), ("quat", _d), ("vel", _d),
+                ("omega", _d), ("prev_vel", _d)]
+
+
+class JointSoA(C.Structure):
+    _fields_ = [("count", C.c_int32), ("body_a", _i), ("body_b", _i), ("r_a", _d), ("r_b", _d),
+                ("stiffness_lin", _d), ("stiffness_ang", _d), ("fracture", _d),
+                ("penalty_lin", _d), ("penalty_ang", _d), ("lambda_lin", _d), ("lambda_ang", _d),
+                ("broken", _i), ("order", _i)]
+
+
+class SpringSoA(C.Structure):
+    _fields_ = [("count", C.c_int32), ("body_a", _i), ("body_b", _i), ("r_a", _d), ("r_b", _d),
+                ("stiffness", _d), ("rest", _d), ("tear_strain", _d), ("penalty", _d),
+                ("peak_strain", _d), ("broken", _i), ("order", _i)]
+
+
+class ManifoldSoA(C.Structure):
+    _fields_ = [("count", C.c_int32), ("capacity", C.c_int32), ("body_a", _i), ("body_b", _i),
+                ("num_contacts", _i), ("basis", _d), ("friction", _d), ("feature", _u),
+                ("r_a", _d), ("r_b", _d), ("c0", _d), ("penalty", _d), ("lambda_", _d),
+                ("stick", _i), ("order", _i)]
+
+
+class WorldC(C.Structure):
+    _fields_ = [("bodies", BodySoA), ("joints", JointSoA), ("springs", SpringSoA),
+                ("manifolds", ManifoldSoA), ("num_scenes", C.c_int32), ("scene_start", _i)]
+
+
+class Stats(C.Structure):
+    _fields_ = [("bodies", C.c_int64), ("manifolds", C.c_int64), ("contacts", C.c_int64),
+                ("candidate_pairs", C.c_int64), ("joints_broken", C.c_int64),
+                ("springs_broken", C.c_int64), ("colors", C.c_int32), ("fp64_bodies", C.c_int32),
+                ("overflow", C.c_uint32), ("steps", C.c_int32),
+                ("max_constraint_error", C.c_double), ("max_lambda", C.c_double),
+                ("max_penalty", C.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class Profile(C.Structure):
+    _fields_ = [("broadphase_ms", C.c_double), ("narrowphase_ms", C.c_double),
+                ("prepare_ms", C.c_double), ("coloring_ms", C.c_double),
+                ("solve_ms", C.c_double), ("step_ms", C.c_double)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+def _ptr(a: np.ndarray | None, kind):
+    if a is None:
+        return C.cast(None, kind)
+    assert a.flags["C_CONTIGUOUS"]
+    return a.ctypes.data_as(kind)
+
+
+class World:
+    """numpy SoA of a world (one scene or a batch of scenes)."""
+
+    BODY_F = ("size", "mass", "moment", "radius", "friction", "pos", "quat", "vel", "omega", "prev_vel")
+
+    def __init__(self, n_bodies: int, n_joints: int = 0, n_springs: int = 0, manifold_capacity: int = 0,
+                 scene_start=None):
+        n, j, s, m = n_bodies, n_joints, n_springs, manifold_capacity
+        self.shape = np.zeros(n, np.int32)
+        self.size = np.ones((n, 3))
+        self.mass = np.zeros(n)
+        self.moment = np.zeros((n, 3))
+        self.radius = np.zeros(n)
+        self.friction = np.zeros(n)
+        self.pos = np.zeros((n, 3))
+        self.quat = np.zeros((n, 4))
+        self.quat[:, 3] = 1.0
+        self.vel = np.zeros((n, 3))
+        self.omega = np.zeros((n, 3))
+        self.prev_vel = np.zeros((n, 3))
+        # joints
+        self.j_body_a = np.zeros(j, np.int32)
+        self.j_body_b = np.zeros(j, np.int32)
+        self.j_r_a = np.zeros((j, 3))
+        self.j_r_b = np.zeros((j, 3))
+        self.j_stiffness_lin = np.full(j, math.inf)
+        self.j_stiffness_ang = np.zeros(j)
+        self.j_fracture = np.full(j, math.inf)
+        self.j_penalty_lin = np.zeros((j, 3))
+        self.j_penalty_ang = np.zeros((j, 3))
+        self.j_lambda_lin = np.zeros((j, 3))
+        self.j_lambda_ang = np.zeros((j, 3))
+        self.j_broken = np.zeros(j, np.int32)
+        self.j_order = np.arange(j, dtype=np.int32)
+        # springs
+        self.s_body_a = np.zeros(s, np.int32)
+        self.s_body_b = np.zeros(s, np.int32)
+        self.s_r_a = np.zeros((s, 3))
+        self.s_r_b = np.zeros((s, 3))
+        self.s_stiffness = np.zeros(s)
+        self.s_rest = np.zeros(s)
+        self.s_tear_strain = np.full(s, math.inf)
+        self.s_penalty = np.zeros(s)
+        self.s_peak_strain = np.zeros(s)
+        self.s_broken = np.zeros(s, np.int32)
+        self.s_order = np.arange(j, j + s, dtype=np.int32)
+        # manifolds
+        self.m_count = 0
+        self._alloc_manifolds(m)
+        if scene_start is None:
+            scene_start = [0, n]
+        self.scene_start = np.asarray(scene_start, np.int32)
+        self._c = None
+
+    def _alloc_manifolds(self, m: int):
+        K = MAX_CONTACTS
+        self.m_capacity = m
+        self.m_body_a = np.zeros(m, np.int32)
+        self.m_body_b = np.zeros(m, np.int32)
+        self.m_num_contacts = np.zeros(m, np.int32)
+        self.m_basis = np.zeros((m, 9))
+        self.m_friction = np.zeros(m)
+        self.m_feature = np.zeros((m, K), np.uint32)
+        self.m_r_a = np.zeros((m, K, 3))
+        self.m_r_b = np.zeros((m, K, 3))
+        self.m_c0 = np.zeros((m, K, 3))
+        self.m_penalty = np.zeros((m, K, 3))
+        self.m_lambda = np.zeros((m, K, 3))
+        self.m_stick = np.zeros((m, K), np.int32)
+        self.m_order = np.zeros(m, np.int32)
+        self._c = None
+
+    def ensure_manifold_capacity(self, m: int):
+        if m > self.m_capacity:
+            self._alloc_manifolds(m)
+
+    @property
+    def n_bodies(self):
+        return len(self.mass)
+
+    @property
+    def n_joints(self):
+        return len(self.j_body_a)
+
+    @property
+    def n_springs(self):
+        return len(self.s_body_a)
+
+    @property
+    def num_scenes(self):
+        return len(self.scene_start) - 1
+
+    def c(self, with_manifolds: bool = True) -> WorldC:
+        """The ctypes view. Rebuilt on every call so array replacement is safe."""
+        w = WorldC()
+        b = w.bodies
+        b.count = self.n_bodies
+        b.shape = _ptr(self.shape, _i)
+        for f in self.BODY_F:
+            setattr(b, f, _ptr(getattr(self, f), _d))
+        j = w.joints
+        j.count = self.n_joints
+        j.body_a, j.body_b = _ptr(self.j_body_a, _i), _ptr(self.j_body_b, _i)
+        for f in ("r_a", "r_b", "stiffness_lin", "stiffness_ang", "fracture", "penalty_lin",
+                  "penalty_ang", "lambda_lin", "lambda_ang"):
+            setattr(j, f, _ptr(getattr(self, "j_" + f), _d))
+        j.broken, j.order = _ptr(self.j_broken, _i), _ptr(self.j_order, _i)
+        s = w.springs
+        s.count = self.n_springs
+        s.body_a, s.body_b = _ptr(self.s_body_a, _i), _ptr(self.s_body_b, _i)
+        for f in ("r_a", "r_b", "stiffness", "rest", "tear_strain", "penalty", "peak_strain"):
+            setattr(s, f, _ptr(getattr(self, "s_" + f), _d))
+        s.broken, s.order = _ptr(self.s_broken, _i), _ptr(self.s_order, _i)
+        m = w.manifolds
+        m.count = self.m_count if with_manifolds else 0
+        m.capacity = self.m_capacity if with_manifolds else 0
+        if with_manifolds:
+            m.body_a, m.body_b = _ptr(self.m_body_a, _i), _ptr(self.m_body_b, _i)
+            m.num_contacts = _ptr(self.m_num_contacts, _i)
+            m.basis, m.friction = _ptr(self.m_basis, _d), _ptr(self.m_friction, _d)
+            m.feature = _ptr(self.m_feature, _u)
+            m.r_a, m.r_b, m.c0 = _ptr(self.m_r_a, _d), _ptr(self.m_r_b, _d), _ptr(self.m_c0, _d)
+            m.penalty, m.lambda_ = _ptr(self.m_penalty, _d), _ptr(self.m_lambda, _d)
+            m.stick, m.order = _ptr(self.m_stick, _i), _ptr(self.m_order, _i)
+        w.num_scenes = self.num_scenes
+        w.scene_start = _ptr(self.scene_start, _i)
+        self._c = w
+        return w
+
+    def copy(self) -> "World":
+        import copy as _copy
+        out = _copy.copy(self)
+        for k, v in self.__dict__.items():
+            if isinstance(v, np.ndarray):
+                setattr(out, k, v.copy())
+        out._c = None
+        return out
+
+    def round_to_device(self) -> "World":
+        """A copy whose dynamic state is exactly representable on the device.
+
+        The CUDA backend keeps positions in f64 and orientations, velocities,
+        penalties, multipliers and contact anchors in f32. Feeding this copy to
+        both the oracle and the device makes their inputs identical.
+        """
+        w = self.copy()
+        f32 = lambda a: a.astype(np.float32).astype(np.float64)
+        w.quat = f32(w.quat)
+        w.vel = f32(w.vel)
+        w.omega = f32(w.omega)
+        w.prev_vel = f32(w.prev_vel)
+        for k in ("j_penalty_lin", "j_penalty_ang", "s_penalty", "m_r_a", "m_r_b", "m_penalty",
+                  "m_lambda"):
+            setattr(w, k, f32(getattr(w, k)))
+        return w
+
+    def manifold_dict(self):
+        """Live manifolds keyed by (A, B) -> (num_contacts, features tuple)."""
+        out = {}
+        for m in range(self.m_count):
+            n = int(self.m_num_contacts[m])
+            out[(int(self.m_body_a[m]), int(self.m_body_b[m]))] = (
+                n, tuple(int(x) for x in self.m_feature[m, :n]))
+        return out

@@ -1,0 +1,285 @@
+/*
+ * avbd_cuda.h - C ABI of the GB300 AVBD world-step backend.
+ *
+ * This library is a third backend for the AVBD sandbox's scene graph, next to
+ * the f64 CPU engine (`Solver.step()`, src/physics/solver.js:307-493) and the
+ * WebGPU engine (`GpuBackend`, src/physics/gpu/backend.js:243). The scene graph
+ * (bodies, joints, springs, contact manifolds) crosses this boundary as
+ * structure-of-arrays of plain doubles and ints owned by the caller; the
+ * context owns all device memory and retains no caller pointer after a call
+ * returns.
+ *
+ * Conventions (from src/math/maths.js:14-22):
+ *   vec3  = 3 doubles [x, y, z]
+ *   quat  = 4 doubles [x, y, z, w], w the scalar part
+ *   mat3  = 9 doubles, row-major
+ *   gravity acts on world z (Z-up)
+ *
+ * Every function returns an int status: AVBD_OK (0) or a negative AVBD_ERR_*.
+ * No exception crosses the ABI. `avbd_last_error` gives the text of the most
+ * recent failure on a context.
+ *
+ * Threading: a context is NOT thread-safe; distinct contexts are independent.
+ * `avbd_step` is asynchronous on the context's CUDA stream; every read
+ * synchronises that stream first.
+ */
+#ifndef AVBD_CUDA_H
+#define AVBD_CUDA_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+/* ---- status codes ------------------------------------------------------ */
+#define AVBD_OK 0
+#define AVBD_ERR_ARG (-1)      /* bad argument or inconsistent scene data     */
+#define AVBD_ERR_CAPACITY (-2) /* a device arena overflowed; the step was redone
+                                  after regrowing, or could not be             */
+#define AVBD_ERR_CUDA (-3)     /* a CUDA runtime call failed                  */
+#define AVBD_ERR_TIMEOUT (-4)  /* a bounded device-side wait gave up          */
+#define AVBD_ERR_NAN (-5)      /* a non-finite body state was produced/given  */
+#define AVBD_ERR_STATE (-6)    /* call made in the wrong state (e.g. no pack) */
+
+/* ---- body shapes (src/physics/rigid.js:32, :125) ------------------------ */
+#define AVBD_SHAPE_BOX 0
+#define AVBD_SHAPE_SPHERE 1
+
+/* ---- body visit order of the primal sweep (src/physics/solver.js:419-422) */
+#define AVBD_ORDER_REFERENCE 0 /* newest body first (oracle only)            */
+#define AVBD_ORDER_EXPLICIT 1  /* caller-supplied order (the bodyOrder hook)  */
+#define AVBD_ORDER_PRIORITY 2  /* colour order of the integer-priority greedy
+                                  colouring of this step's constraint graph:
+                                  the GPU schedule                            */
+
+/* ---- overflow bits reported in avbd_stats.overflow ---------------------- */
+#define AVBD_OVF_CELLS 0x1u      /* hash-grid insertions                     */
+#define AVBD_OVF_PAIRS 0x2u      /* candidate pairs per body / in total      */
+#define AVBD_OVF_ADJ 0x4u        /* per-body constraint adjacency            */
+#define AVBD_OVF_COLORS 0x8u     /* more than AVBD_MAX_COLORS colours        */
+#define AVBD_OVF_TIMEOUT 0x10u   /* bounded grid barrier gave up             */
+
+#define AVBD_MAX_CONTACTS 8 /* contacts per manifold (src/physics/collide.js:22) */
+#define AVBD_MAX_COLORS 64  /* colours the device colouring can encode       */
+
+/*
+ * Solver parameters. Field meanings and defaults follow
+ * `Solver.defaultParams()` (src/physics/solver.js:92-236); the GPU-only fields
+ * at the end have no counterpart there.
+ */
+typedef struct avbd_params {
+  double dt;               /* 1/60                                          */
+  double gravity;          /* -10, acts on world z                          */
+  int32_t iterations;      /* 10                                            */
+  int32_t post_stabilize;  /* 0                                             */
+  double beta_lin;         /* 1e4                                           */
+  double beta_ang;         /* 100                                           */
+  double alpha;            /* 0.95                                          */
+  double gamma;            /* 0.999                                         */
+  double penalty_min;      /* 1                                             */
+  double penalty_max;      /* 1e10                                          */
+  double collision_margin; /* 0.01                                          */
+  double stick_threshold;  /* 1e-5                                          */
+  int32_t rotated_inertia;           /* 1                                   */
+  int32_t spring_stiffness_ramp;     /* 0                                   */
+  int32_t spring_geometric_stiffness;/* 1                                   */
+  int32_t cached_contact_jacobians;  /* 1                                   */
+  int32_t broadphase;      /* oracle only: 0 auto, 1 hash, 2 brute force     */
+  int32_t hash_threshold;  /* oracle only: 150                              */
+  int32_t body_order;      /* AVBD_ORDER_*; the CUDA backend always uses
+                              AVBD_ORDER_PRIORITY                           */
+  int32_t reserved0;
+  /* GPU precision policy. A body whose largest constraint stiffness divided
+     by its inertial stiffness m/dt^2 exceeds this ratio is assembled and
+     factored in FP64; everything else runs in FP32. <= 0 disables FP64.    */
+  double fp64_ratio_threshold;
+  /* GPU capacity policy (0 = automatic). */
+  int32_t max_pairs_per_body; /* candidate partners with a lower index      */
+  int32_t max_adjacency;      /* constraints incident to one dynamic body   */
+  int32_t lanes_per_body;     /* 0 = autotuned; else 1, 2, 4, 8 or 16       */
+  int32_t blocks_per_sm;      /* 0 = autotuned                              */
+} avbd_params;
+
+/*
+ * Bodies, `Rigid` (src/physics/rigid.js:29-133). Static shape/material fields
+ * are inputs of avbd_pack; pos/quat/vel/omega/prev_vel are the dynamic state
+ * read and written by avbd_read_state / avbd_write_state.
+ */
+typedef struct avbd_body_soa {
+  int32_t count;
+  int32_t *shape;     /* AVBD_SHAPE_*                                        */
+  double *size;       /* 3 per body: full widths                             */
+  double *mass;       /* 0 makes the body static                             */
+  double *moment;     /* 3 per body: body-frame principal moments            */
+  double *radius;     /* bounding radius; a sphere's own radius              */
+  double *friction;   /* combined pairwise as sqrt(fa*fb)                    */
+  double *pos;        /* 3 per body                                          */
+  double *quat;       /* 4 per body                                          */
+  double *vel;        /* 3 per body                                          */
+  double *omega;      /* 3 per body                                          */
+  double *prev_vel;   /* 3 per body                                          */
+} avbd_body_soa;
+
+/* Ball-socket joints, `Joint` (src/physics/joint.js:74-113). */
+typedef struct avbd_joint_soa {
+  int32_t count;
+  int32_t *body_a;        /* -1: r_a is a fixed world anchor                 */
+  int32_t *body_b;
+  double *r_a;            /* 3 per joint                                     */
+  double *r_b;            /* 3 per joint                                     */
+  double *stiffness_lin;  /* INFINITY = hard                                 */
+  double *stiffness_ang;  /* 0 disables the angular rows                     */
+  double *fracture;       /* threshold on |lambda_ang|; INFINITY = none      */
+  double *penalty_lin;    /* state, 3 per joint                              */
+  double *penalty_ang;    /* state, 3 per joint                              */
+  double *lambda_lin;     /* state, 3 per joint                              */
+  double *lambda_ang;     /* state, 3 per joint                              */
+  int32_t *broken;        /* state                                           */
+  int32_t *order;         /* optional: position in the global force list     */
+} avbd_joint_soa;
+
+/* Distance springs, `Spring` (src/physics/spring.js:414-444). */
+typedef struct avbd_spring_soa {
+  int32_t count;
+  int32_t *body_a;
+  int32_t *body_b;
+  double *r_a;            /* 3 per spring                                    */
+  double *r_b;            /* 3 per spring                                    */
+  double *stiffness;
+  double *rest;           /* >= 0 (the caller resolves "current length")     */
+  double *tear_strain;    /* INFINITY = never tears                          */
+  double *penalty;        /* state                                           */
+  double *peak_strain;    /* state                                           */
+  int32_t *broken;        /* state                                           */
+  int32_t *order;         /* optional: position in the global force list     */
+} avbd_spring_soa;
+
+/*
+ * Persistent contact manifolds, `Manifold` + `Contact`
+ * (src/physics/manifold.js:33-69, :164-189). Body A has the HIGHER index of
+ * the pair (the broad phase visits (i, j) with j < i,
+ * src/physics/broadphase.js:13-16). Contact arrays hold AVBD_MAX_CONTACTS
+ * slots per manifold. On read, `count` returns the number of live manifolds
+ * and at most `capacity` are written.
+ */
+typedef struct avbd_manifold_soa {
+  int32_t count;
+  int32_t capacity;
+  int32_t *body_a;
+  int32_t *body_b;
+  int32_t *num_contacts;
+  double *basis;          /* 9 per manifold; row 0 = normal B->A            */
+  double *friction;
+  uint32_t *feature;      /* 8 per manifold                                  */
+  double *r_a;            /* 8*3 per manifold, body-A local                  */
+  double *r_b;            /* 8*3 per manifold, body-B local                  */
+  double *c0;             /* 8*3 per manifold, C*(x_t) (read only)           */
+  double *penalty;        /* 8*3 per manifold                                */
+  double *lambda;         /* 8*3 per manifold                                */
+  int32_t *stick;         /* 8 per manifold                                  */
+  int32_t *order;         /* optional: position in the global force list     */
+} avbd_manifold_soa;
+
+/*
+ * A world: one scene, or a batch of independent scenes laid end to end.
+ * Scene s owns bodies [scene_start[s], scene_start[s+1]); constraints may
+ * not cross scenes. num_scenes <= 1 with scene_start NULL means one scene.
+ */
+typedef struct avbd_world {
+  avbd_body_soa bodies;
+  avbd_joint_soa joints;
+  avbd_spring_soa springs;
+  avbd_manifold_soa manifolds; /* count 0 on pack = no warm-start contacts   */
+  int32_t num_scenes;
+  int32_t *scene_start;        /* num_scenes + 1 entries                     */
+} avbd_world;
+
+/* Diagnostics, `Solver.stats` (src/physics/solver.js:77-89, :495-528). */
+typedef struct avbd_stats {
+  int64_t bodies;
+  int64_t manifolds;
+  int64_t contacts;
+  int64_t candidate_pairs;
+  int64_t joints_broken;
+  int64_t springs_broken;
+  int32_t colors;
+  int32_t fp64_bodies;
+  uint32_t overflow;       /* AVBD_OVF_* bits seen since the last pack       */
+  int32_t steps;           /* steps taken since the last pack                */
+  double max_constraint_error;
+  double max_lambda;
+  double max_penalty;
+} avbd_stats;
+
+/* Per-phase device times of the last step, ms (src/physics/gpu/backend.js:58). */
+typedef struct avbd_profile {
+  double broadphase_ms;
+  double narrowphase_ms;
+  double prepare_ms;
+  double coloring_ms;
+  double solve_ms;
+  double step_ms;
+} avbd_profile;
+
+typedef struct avbd_ctx avbd_ctx;
+
+/* Defaults of Solver.defaultParams() (src/physics/solver.js:92-236). */
+void avbd_default_params(avbd_params *out);
+
+/* Replaces `new GpuBackend()` + `init()` (src/physics/gpu/backend.js:243,337-450). */
+int avbd_create(const avbd_params *params, avbd_ctx **out);
+
+/* Replaces `destroyBuffers()` (src/physics/gpu/backend.js:471). */
+int avbd_destroy(avbd_ctx *ctx);
+
+/* Replaces the topology half of `pack(solver)` (src/physics/gpu/backend.js:662-1301):
+   uploads shapes, constraints and state; sizes every arena. */
+int avbd_pack(avbd_ctx *ctx, const avbd_world *world);
+
+/* Replaces `step(solver)` (src/physics/gpu/backend.js:1393-1620). Asynchronous. */
+int avbd_step(avbd_ctx *ctx, int32_t n_steps);
+
+/* Replaces `idle()` (src/physics/gpu/backend.js:1804). Waits for queued steps and
+   reports device-side errors (overflow, timeout). */
+int avbd_synchronize(avbd_ctx *ctx);
+
+/* Replaces `readState()` / `syncToCPU(solver)` (src/physics/gpu/backend.js:1984-2039,
+   2154): body state, joint and spring state, and (when the manifold arrays are
+   non-NULL) the live manifolds in pair order. Fields left NULL are skipped. */
+int avbd_read_state(avbd_ctx *ctx, avbd_world *out);
+
+/* CPU-authoritative handover back to the device: overwrite the dynamic state
+   (bodies, joint/spring state and, if count > 0, the warm-start manifolds) of
+   an already-packed world with the same topology. */
+int avbd_write_state(avbd_ctx *ctx, const avbd_world *world);
+
+/* Replaces `readColoring()` (src/physics/gpu/backend.js:2053): colour of every
+   body in the last step (-1 for static bodies) and the number of colours. */
+int avbd_read_coloring(avbd_ctx *ctx, int32_t *color_of, int32_t *num_colors);
+
+/* Candidate pairs of the last broad phase (body A index, body B index), pair
+   order; `count` returns the total, at most `capacity` written. */
+int avbd_read_pairs(avbd_ctx *ctx, int32_t *body_a, int32_t *body_b,
+                    int64_t capacity, int64_t *count);
+
+/* Replaces `lastStats` (src/physics/gpu/backend.js:309, 1650-1680). */
+int avbd_read_stats(avbd_ctx *ctx, avbd_stats *out);
+
+/* Replaces `setProfiling(on)` / `lastProfile` (src/physics/gpu/backend.js:1836-1897).
+   When on, each step records per-phase CUDA events (adds a sync per step). */
+int avbd_set_profiling(avbd_ctx *ctx, int32_t on);
+int avbd_read_profile(avbd_ctx *ctx, avbd_profile *out);
+
+/* Number of device kernels launched since the last pack. */
+int avbd_kernel_launches(avbd_ctx *ctx, int64_t *out);
+
+/* Text of the last error on this context (or of the last failed create when
+   ctx is NULL). Never NULL. */
+const char *avbd_last_error(const avbd_ctx *ctx);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* AVBD_CUDA_H */

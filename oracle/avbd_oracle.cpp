@@ -1,0 +1,2033 @@
+/*
+ * ORACLE - test infrastructure only. Not part of the product.
+ *
+ * A C++17 f64 restatement of the AVBD sandbox's CPU engine, the reference
+ * `Solver.step()` path:
+ *   src/math/maths.js            vec3 / mat3 / quat / solve6
+ *   src/physics/rigid.js         mass properties, world moment, constrainedTo
+ *   src/physics/collide.js       box-box SAT + clipping, sphere-sphere, sphere-OBB
+ *   src/physics/manifold.js      persistent manifolds, warm start, contact rows
+ *   src/physics/joint.js         ball socket + angular rows + fracture
+ *   src/physics/spring.js        distance spring + Eq. 17 geometric stiffness + tear
+ *   src/physics/broadphase.js    spatial hash (brute-force order) / brute force
+ *   src/physics/coloring.js      greedy index-order colouring
+ *   src/physics/gpu/layout.js:50-57  lowbias32 colour priority
+ *   src/physics/solver.js        Algorithm 1 (`step`, :307-493)
+ *
+ * It is the checker for the CUDA backend: tests, __graft_entry__.smoke() and
+ * bench.py's CPU-baseline leg load it; nothing in the product links it.
+ *
+ * Floating-point operation order follows the reference line by line (it must
+ * be compiled with -ffp-contract=off and without -ffast-math) so that it is a
+ * faithful f64 restatement. Parity against the JavaScript engine itself cannot
+ * be run in this build environment (there is no JavaScript runtime); the
+ * oracle is pinned instead by the reference's closed-form tests
+ * (test/analytic.mjs, test/fixtures.mjs, test/spheres.mjs), ported in tests/.
+ */
+
+#include "../include/avbd_cuda.h"
+
+#include <algorithm>
+#include <cmath>
+#include <cstdint>
+#include <cstring>
+#include <limits>
+#include <string>
+#include <vector>
+
+namespace orc {
+
+static const double INF = std::numeric_limits<double>::infinity();
+static const double NaN = std::numeric_limits<double>::quiet_NaN();
+
+// ---------------------------------------------------------------------------
+// Scalar helpers with JavaScript semantics (src/math/maths.js:34-44)
+// ---------------------------------------------------------------------------
+
+// Math.min / Math.max: NaN propagates, -0 < +0.
+static inline double js_min(double a, double b) {
+  if (a != a || b != b) return NaN;
+  if (a < b) return a;
+  if (b < a) return b;
+  if (a == 0 && b == 0) return (std::signbit(a) || std::signbit(b)) ? -0.0 : 0.0;
+  return a;
+}
+static inline double js_max(double a, double b) {
+  if (a != a || b != b) return NaN;
+  if (a > b) return a;
+  if (b > a) return b;
+  if (a == 0 && b == 0) return (!std::signbit(a) || !std::signbit(b)) ? 0.0 : -0.0;
+  return a;
+}
+static inline double sign(double x) { return x < 0 ? -1 : x > 0 ? 1 : 0; }
+// clamp(x, a, b) = Math.max(a, Math.min(b, x))  (maths.js:38-40)
+static inline double clamp(double x, double a, double b) { return js_max(a, js_min(b, x)); }
+static inline bool is_finite(double x) { return std::isfinite(x); }
+
+// ---------------------------------------------------------------------------
+// vec3 (maths.js:50-193)
+// ---------------------------------------------------------------------------
+static inline void v3_set(double *o, double x, double y, double z) { o[0] = x; o[1] = y; o[2] = z; }
+static inline void v3_copy(double *o, const double *a) { o[0] = a[0]; o[1] = a[1]; o[2] = a[2]; }
+static inline void v3_zero(double *o) { o[0] = 0; o[1] = 0; o[2] = 0; }
+static inline void v3_add(double *o, const double *a, const double *b) {
+  o[0] = a[0] + b[0]; o[1] = a[1] + b[1]; o[2] = a[2] + b[2];
+}
+static inline void v3_sub(double *o, const double *a, const double *b) {
+  o[0] = a[0] - b[0]; o[1] = a[1] - b[1]; o[2] = a[2] - b[2];
+}
+static inline void v3_scale(double *o, const double *a, double s) {
+  o[0] = a[0] * s; o[1] = a[1] * s; o[2] = a[2] * s;
+}
+static inline void v3_div(double *o, const double *a, double s) {
+  o[0] = a[0] / s; o[1] = a[1] / s; o[2] = a[2] / s;
+}
+static inline void v3_add_scaled(double *o, const double *a, double s) {
+  o[0] += a[0] * s; o[1] += a[1] * s; o[2] += a[2] * s;
+}
+static inline void v3_negate(double *o, const double *a) { o[0] = -a[0]; o[1] = -a[1]; o[2] = -a[2]; }
+static inline double v3_dot(const double *a, const double *b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
+static inline double v3_len_sq(const double *a) { return a[0] * a[0] + a[1] * a[1] + a[2] * a[2]; }
+static inline double v3_len(const double *a) { return std::sqrt(a[0] * a[0] + a[1] * a[1] + a[2] * a[2]); }
+static inline void v3_cross(double *o, const double *a, const double *b) {
+  const double ax = a[0], ay = a[1], az = a[2], bx = b[0], by = b[1], bz = b[2];
+  o[0] = ay * bz - az * by;
+  o[1] = az * bx - ax * bz;
+  o[2] = ax * by - ay * bx;
+}
+static inline void v3_abs(double *o, const double *a) {
+  o[0] = std::fabs(a[0]); o[1] = std::fabs(a[1]); o[2] = std::fabs(a[2]);
+}
+static inline void v3_min_scalar(double *o, const double *a, double s) {
+  o[0] = js_min(a[0], s); o[1] = js_min(a[1], s); o[2] = js_min(a[2], s);
+}
+static inline void v3_clamp_scalar(double *o, const double *a, double lo, double hi) {
+  o[0] = clamp(a[0], lo, hi); o[1] = clamp(a[1], lo, hi); o[2] = clamp(a[2], lo, hi);
+}
+
+// ---------------------------------------------------------------------------
+// mat3, row-major (maths.js:199-435)
+// ---------------------------------------------------------------------------
+static inline void m3_zero(double *o) { for (int i = 0; i < 9; i++) o[i] = 0; }
+static inline void m3_copy(double *o, const double *a) { for (int i = 0; i < 9; i++) o[i] = a[i]; }
+static inline void m3_diagonal(double *o, double a, double b, double c) {
+  o[0] = a; o[1] = 0; o[2] = 0; o[3] = 0; o[4] = b; o[5] = 0; o[6] = 0; o[7] = 0; o[8] = c;
+}
+static inline void m3_add_into(double *o, const double *a) { for (int i = 0; i < 9; i++) o[i] += a[i]; }
+static inline void m3_scale(double *o, const double *a, double s) { for (int i = 0; i < 9; i++) o[i] = a[i] * s; }
+static inline void m3_div(double *o, const double *a, double s) { for (int i = 0; i < 9; i++) o[i] = a[i] / s; }
+static inline void m3_negate(double *o, const double *a) { for (int i = 0; i < 9; i++) o[i] = -a[i]; }
+static inline void m3_get_row(double *o, const double *a, int r) { o[0] = a[r * 3]; o[1] = a[r * 3 + 1]; o[2] = a[r * 3 + 2]; }
+static inline void m3_mul_vec(double *o, const double *a, const double *v) {
+  const double x = v[0], y = v[1], z = v[2];
+  o[0] = a[0] * x + a[1] * y + a[2] * z;
+  o[1] = a[3] * x + a[4] * y + a[5] * z;
+  o[2] = a[6] * x + a[7] * y + a[8] * z;
+}
+static inline void m3_mul(double *o, const double *a, const double *b) {
+  const double a0 = a[0], a1 = a[1], a2 = a[2], a3 = a[3], a4 = a[4], a5 = a[5], a6 = a[6], a7 = a[7], a8 = a[8];
+  const double b0 = b[0], b1 = b[1], b2 = b[2], b3 = b[3], b4 = b[4], b5 = b[5], b6 = b[6], b7 = b[7], b8 = b[8];
+  o[0] = a0 * b0 + a1 * b3 + a2 * b6;
+  o[1] = a0 * b1 + a1 * b4 + a2 * b7;
+  o[2] = a0 * b2 + a1 * b5 + a2 * b8;
+  o[3] = a3 * b0 + a4 * b3 + a5 * b6;
+  o[4] = a3 * b1 + a4 * b4 + a5 * b7;
+  o[5] = a3 * b2 + a4 * b5 + a5 * b8;
+  o[6] = a6 * b0 + a7 * b3 + a8 * b6;
+  o[7] = a6 * b1 + a7 * b4 + a8 * b7;
+  o[8] = a6 * b2 + a7 * b5 + a8 * b8;
+}
+static inline void m3_mul_diag_right(double *o, const double *a, double d0, double d1, double d2) {
+  o[0] = a[0] * d0; o[1] = a[1] * d1; o[2] = a[2] * d2;
+  o[3] = a[3] * d0; o[4] = a[4] * d1; o[5] = a[5] * d2;
+  o[6] = a[6] * d0; o[7] = a[7] * d1; o[8] = a[8] * d2;
+}
+static inline void m3_transpose(double *o, const double *a) {
+  const double a1 = a[1], a2 = a[2], a5 = a[5];
+  o[0] = a[0]; o[4] = a[4]; o[8] = a[8];
+  o[1] = a[3]; o[3] = a1;
+  o[2] = a[6]; o[6] = a2;
+  o[5] = a[7]; o[7] = a5;
+}
+static inline void m3_outer(double *o, const double *a, const double *b) {
+  o[0] = a[0] * b[0]; o[1] = a[0] * b[1]; o[2] = a[0] * b[2];
+  o[3] = a[1] * b[0]; o[4] = a[1] * b[1]; o[5] = a[1] * b[2];
+  o[6] = a[2] * b[0]; o[7] = a[2] * b[1]; o[8] = a[2] * b[2];
+}
+static inline void m3_skew(double *o, const double *r) {
+  const double rx = r[0], ry = r[1], rz = r[2];
+  o[0] = 0; o[1] = -rz; o[2] = ry;
+  o[3] = rz; o[4] = 0; o[5] = -rx;
+  o[6] = -ry; o[7] = rx; o[8] = 0;
+}
+static inline void m3_diagonalize(double *o, const double *m) {
+  const double c0 = std::sqrt(m[0] * m[0] + m[3] * m[3] + m[6] * m[6]);
+  const double c1 = std::sqrt(m[1] * m[1] + m[4] * m[4] + m[7] * m[7]);
+  const double c2 = std::sqrt(m[2] * m[2] + m[5] * m[5] + m[8] * m[8]);
+  o[0] = c0; o[1] = 0; o[2] = 0; o[3] = 0; o[4] = c1; o[5] = 0; o[6] = 0; o[7] = 0; o[8] = c2;
+}
+// maths.js:389-414
+static inline void m3_orthonormal(double *o, const double *normal) {
+  const double nx = normal[0], ny = normal[1], nz = normal[2];
+  double t1x, t1y, t1z;
+  if (std::fabs(nx) > std::fabs(nz)) { t1x = -ny; t1y = nx; t1z = 0; }
+  else { t1x = 0; t1y = -nz; t1z = ny; }
+  const double t1len = std::sqrt(t1x * t1x + t1y * t1y + t1z * t1z);
+  t1x /= t1len; t1y /= t1len; t1z /= t1len;
+  const double t2x = ny * t1z - nz * t1y;
+  const double t2y = nz * t1x - nx * t1z;
+  const double t2z = nx * t1y - ny * t1x;
+  o[0] = nx; o[1] = ny; o[2] = nz;
+  o[3] = t1x; o[4] = t1y; o[5] = t1z;
+  o[6] = t2x; o[7] = t2y; o[8] = t2z;
+}
+// maths.js:417-434
+static inline void m3_from_quat(double *o, const double *q) {
+  const double x = q[0], y = q[1], z = q[2], w = q[3];
+  const double xx = x * x, yy = y * y, zz = z * z;
+  const double xy = x * y, xz = x * z, yz = y * z;
+  const double wx = w * x, wy = w * y, wz = w * z;
+  o[0] = 1 - 2 * (yy + zz);
+  o[1] = 2 * (xy + wz);
+  o[2] = 2 * (xz - wy);
+  o[3] = 2 * (xy - wz);
+  o[4] = 1 - 2 * (xx + zz);
+  o[5] = 2 * (yz + wx);
+  o[6] = 2 * (xz + wy);
+  o[7] = 2 * (yz - wx);
+  o[8] = 1 - 2 * (xx + yy);
+}
+
+// ---------------------------------------------------------------------------
+// quat (maths.js:441-627)
+// ---------------------------------------------------------------------------
+static inline void q_copy(double *o, const double *a) { o[0] = a[0]; o[1] = a[1]; o[2] = a[2]; o[3] = a[3]; }
+static inline void q_identity(double *o) { o[0] = 0; o[1] = 0; o[2] = 0; o[3] = 1; }
+static inline void q_conjugate(double *o, const double *q) { o[0] = -q[0]; o[1] = -q[1]; o[2] = -q[2]; o[3] = q[3]; }
+// Eq. 20, maths.js:541-555
+static inline void q_subtract(double *o, const double *a, const double *b) {
+  const double lsq = b[0] * b[0] + b[1] * b[1] + b[2] * b[2] + b[3] * b[3];
+  const double ix = -b[0] / lsq, iy = -b[1] / lsq, iz = -b[2] / lsq, iw = b[3] / lsq;
+  const double ax = a[0], ay = a[1], az = a[2], aw = a[3];
+  o[0] = (aw * ix + ax * iw + ay * iz - az * iy) * 2;
+  o[1] = (aw * iy - ax * iz + ay * iw + az * ix) * 2;
+  o[2] = (aw * iz + ax * iy - ay * ix + az * iw) * 2;
+}
+// Eq. 21, maths.js:568-592 (the "0 * q" terms are kept: they fix -0 handling)
+static inline void q_integrate(double *o, const double *q, const double *dw) {
+  const double qx = q[0], qy = q[1], qz = q[2], qw = q[3];
+  const double wx = dw[0], wy = dw[1], wz = dw[2];
+  const double px = 0 * qx + wx * qw + wy * qz - wz * qy;
+  const double py = 0 * qy - wx * qz + wy * qw + wz * qx;
+  const double pz = 0 * qz + wx * qy - wy * qx + wz * qw;
+  const double pw = 0 * qw - wx * qx - wy * qy - wz * qz;
+  const double rx = qx + px * 0.5, ry = qy + py * 0.5, rz = qz + pz * 0.5, rw = qw + pw * 0.5;
+  const double len = std::sqrt(rx * rx + ry * ry + rz * rz + rw * rw);
+  o[0] = rx / len; o[1] = ry / len; o[2] = rz / len; o[3] = rw / len;
+}
+// maths.js:599-613
+static inline void q_rotate(double *o, const double *q, const double *v) {
+  const double ux = q[0], uy = q[1], uz = q[2], w = q[3];
+  const double vx = v[0], vy = v[1], vz = v[2];
+  const double tx = (uy * vz - uz * vy) * 2;
+  const double ty = (uz * vx - ux * vz) * 2;
+  const double tz = (ux * vy - uy * vx) * 2;
+  o[0] = vx + tx * w + (uy * tz - uz * ty);
+  o[1] = vy + ty * w + (uz * tx - ux * tz);
+  o[2] = vz + tz * w + (ux * ty - uy * tx);
+}
+// maths.js:621-627
+static inline void transform_point(double *o, const double *lin, const double *ang, const double *v) {
+  q_rotate(o, ang, v);
+  o[0] += lin[0]; o[1] += lin[1]; o[2] += lin[2];
+}
+
+// maths.js:660-725, unrolled LDL^T of the 6x6 block system
+static void solve6(const double *aLin, const double *aAng, const double *aCross, const double *bLin,
+                   const double *bAng, double *xLin, double *xAng) {
+  const double A11 = aLin[0];
+  const double A21 = aLin[3], A22 = aLin[4];
+  const double A31 = aLin[6], A32 = aLin[7], A33 = aLin[8];
+  const double A41 = aCross[0], A42 = aCross[1], A43 = aCross[2], A44 = aAng[0];
+  const double A51 = aCross[3], A52 = aCross[4], A53 = aCross[5], A54 = aAng[3], A55 = aAng[4];
+  const double A61 = aCross[6], A62 = aCross[7], A63 = aCross[8], A64 = aAng[6], A65 = aAng[7], A66 = aAng[8];
+
+  const double L21 = A21 / A11, L31 = A31 / A11, L41 = A41 / A11, L51 = A51 / A11, L61 = A61 / A11;
+  const double D1 = A11;
+  const double D2 = A22 - L21 * L21 * D1;
+  const double L32 = (A32 - L21 * L31 * D1) / D2;
+  const double L42 = (A42 - L21 * L41 * D1) / D2;
+  const double L52 = (A52 - L21 * L51 * D1) / D2;
+  const double L62 = (A62 - L21 * L61 * D1) / D2;
+  const double D3 = A33 - (L31 * L31 * D1 + L32 * L32 * D2);
+  const double L43 = (A43 - L31 * L41 * D1 - L32 * L42 * D2) / D3;
+  const double L53 = (A53 - L31 * L51 * D1 - L32 * L52 * D2) / D3;
+  const double L63 = (A63 - L31 * L61 * D1 - L32 * L62 * D2) / D3;
+  const double D4 = A44 - (L41 * L41 * D1 + L42 * L42 * D2 + L43 * L43 * D3);
+  const double L54 = (A54 - L41 * L51 * D1 - L42 * L52 * D2 - L43 * L53 * D3) / D4;
+  const double L64 = (A64 - L41 * L61 * D1 - L42 * L62 * D2 - L43 * L63 * D3) / D4;
+  const double D5 = A55 - (L51 * L51 * D1 + L52 * L52 * D2 + L53 * L53 * D3 + L54 * L54 * D4);
+  const double L65 = (A65 - L51 * L61 * D1 - L52 * L62 * D2 - L53 * L63 * D3 - L54 * L64 * D4) / D5;
+  const double D6 = A66 - (L61 * L61 * D1 + L62 * L62 * D2 + L63 * L63 * D3 + L64 * L64 * D4 + L65 * L65 * D5);
+
+  const double y1 = bLin[0];
+  const double y2 = bLin[1] - L21 * y1;
+  const double y3 = bLin[2] - L31 * y1 - L32 * y2;
+  const double y4 = bAng[0] - L41 * y1 - L42 * y2 - L43 * y3;
+  const double y5 = bAng[1] - L51 * y1 - L52 * y2 - L53 * y3 - L54 * y4;
+  const double y6 = bAng[2] - L61 * y1 - L62 * y2 - L63 * y3 - L64 * y4 - L65 * y5;
+
+  const double z1 = y1 / D1, z2 = y2 / D2, z3 = y3 / D3, z4 = y4 / D4, z5 = y5 / D5, z6 = y6 / D6;
+
+  xAng[2] = z6;
+  xAng[1] = z5 - L65 * xAng[2];
+  xAng[0] = z4 - L54 * xAng[1] - L64 * xAng[2];
+  xLin[2] = z3 - L43 * xAng[0] - L53 * xAng[1] - L63 * xAng[2];
+  xLin[1] = z2 - L32 * xLin[2] - L42 * xAng[0] - L52 * xAng[1] - L62 * xAng[2];
+  xLin[0] = z1 - L21 * xLin[1] - L31 * xLin[2] - L41 * xAng[0] - L51 * xAng[1] - L61 * xAng[2];
+}
+
+// lowbias32 integer hash (src/physics/gpu/layout.js:50-57)
+static inline uint32_t color_priority(uint32_t x) {
+  x ^= x >> 16;
+  x *= 0x7feb352du;
+  x ^= x >> 15;
+  x *= 0x846ca68bu;
+  x ^= x >> 16;
+  return x;
+}
+
+// ---------------------------------------------------------------------------
+// Scene graph
+// ---------------------------------------------------------------------------
+struct Solver;
+struct Force;
+
+struct Body {
+  int index = 0;
+  int shape = AVBD_SHAPE_BOX;
+  double positionLin[3] = {0, 0, 0};
+  double positionAng[4] = {0, 0, 0, 1};
+  double initialLin[3] = {0, 0, 0};
+  double initialAng[4] = {0, 0, 0, 1};
+  double inertialLin[3] = {0, 0, 0};
+  double inertialAng[4] = {0, 0, 0, 1};
+  double velocityLin[3] = {0, 0, 0};
+  double velocityAng[3] = {0, 0, 0};
+  double prevVelocityLin[3] = {0, 0, 0};
+  double size[3] = {1, 1, 1};
+  double friction = 0.5;
+  double mass = 0;
+  double moment[3] = {0, 0, 0};
+  double radius = 0;
+  std::vector<Force *> forces; // creation order; iterate in reverse
+
+  // rigid.js:228-247
+  void computeWorldMoment(double *out, bool rotated) const {
+    if (!rotated || shape == AVBD_SHAPE_SPHERE) {
+      m3_diagonal(out, moment[0], moment[1], moment[2]);
+      return;
+    }
+    double R[9], T[9];
+    m3_from_quat(R, positionAng);
+    m3_transpose(R, R);
+    m3_diagonal(T, moment[0], moment[1], moment[2]);
+    m3_mul(out, R, T);
+    m3_transpose(R, R);
+    m3_mul(out, out, R);
+  }
+  bool constrainedTo(const Body *other) const;
+};
+
+enum ForceKind { KIND_MANIFOLD = 0, KIND_JOINT = 1, KIND_SPRING = 2 };
+
+struct Force {
+  Solver *solver = nullptr;
+  Body *bodyA = nullptr;
+  Body *bodyB = nullptr;
+  ForceKind kind = KIND_MANIFOLD;
+  int id = 0; // index within its kind's array (joints / springs)
+  virtual ~Force() {}
+  virtual bool isBroken() const { return false; }
+  virtual bool initialize() { return true; }
+  virtual void updatePrimal(Body *body, double alpha, double *lhsLin, double *lhsAng, double *lhsCross,
+                            double *rhsLin, double *rhsAng) = 0;
+  virtual void updateDual(double alpha) = 0;
+  virtual double maxLambda() const { return 0; }
+  virtual double maxPenalty() const { return 0; }
+  virtual double maxConstraintError() const { return 0; }
+};
+
+// rigid.js:250-259 (a manifold has no `broken` field, which reads falsy)
+bool Body::constrainedTo(const Body *other) const {
+  for (int i = (int)forces.size() - 1; i >= 0; i--) {
+    const Force *f = forces[i];
+    if (f->isBroken()) continue;
+    if ((f->bodyA == this && f->bodyB == other) || (f->bodyA == other && f->bodyB == this)) return true;
+  }
+  return false;
+}
+
+struct Params {
+  double dt = 1.0 / 60.0, gravity = -10.0;
+  int iterations = 10;
+  double betaLin = 1e4, betaAng = 100, alpha = 0.95, gamma = 0.999;
+  bool postStabilize = false;
+  double penaltyMin = 1, penaltyMax = 1e10, collisionMargin = 0.01, stickThreshold = 1e-5;
+  bool rotatedInertia = true, springRamp = false, springGeometric = true, cachedJacobians = true;
+  int broadphase = 0, hashThreshold = 150, bodyOrderMode = AVBD_ORDER_REFERENCE;
+};
+
+// ---------------------------------------------------------------------------
+// Narrow phase (src/physics/collide.js)
+// ---------------------------------------------------------------------------
+static const int MAX_CONTACTS = 8;
+static const int MAX_POLY_VERTS = 16;
+static const double SAT_AXIS_EPSILON = 1.0e-6;
+static const double SPHERE_DISTANCE_EPSILON_SQ = 1.0e-20;
+static const double PLANE_EPSILON = 1.0e-5;
+static const double CONTACT_MERGE_DIST_SQ = 1.0e-6;
+static const int AXIS_FACE_A = 0, AXIS_FACE_B = 1, AXIS_EDGE = 2;
+
+struct Contact {
+  uint32_t feature = 0;
+  double rA[3] = {0, 0, 0}, rB[3] = {0, 0, 0};
+  double C0[3] = {0, 0, 0}, penalty[3] = {0, 0, 0}, lambda[3] = {0, 0, 0};
+  bool stick = false;
+  double C[3] = {0, 0, 0};
+  void copyFrom(const Contact &o) { *this = o; }
+  void reset() {
+    feature = 0;
+    v3_zero(penalty); v3_zero(lambda); v3_zero(C0); v3_zero(C);
+    stick = false;
+  }
+};
+
+struct OBB {
+  double center[3], half[3], axis[3][3];
+};
+
+struct SatAxis {
+  int type = 0, indexA = -1, indexB = -1;
+  double separation = 0;
+  double normalAB[3] = {0, 0, 0};
+  bool valid = false;
+};
+
+// The module-level scratch of collide.js, gathered in one object.
+struct Collider {
+  OBB boxA, boxB;
+  double frameNormal[3], frameCenter[3], frameU[3], frameV[3], frameExtentU, frameExtentV;
+  double faceExtU, faceExtV;
+  double clip0[MAX_POLY_VERTS * 3], clip1[MAX_POLY_VERTS * 3], midpoints[MAX_CONTACTS * 3];
+  int stateCount = 0;
+
+  static void makeOBB(OBB &box, const Body &b) {
+    static const double ux[3] = {1, 0, 0}, uy[3] = {0, 1, 0}, uz[3] = {0, 0, 1};
+    v3_copy(box.center, b.positionLin);
+    v3_scale(box.half, b.size, 0.5);
+    q_rotate(box.axis[0], b.positionAng, ux);
+    q_rotate(box.axis[1], b.positionAng, uy);
+    q_rotate(box.axis[2], b.positionAng, uz);
+  }
+  static double absDot(const double *a, const double *b) { return std::fabs(v3_dot(a, b)); }
+  static void supportPoint(double *out, const OBB &box, const double *dir) {
+    const double sx = v3_dot(dir, box.axis[0]) >= 0 ? 1 : -1;
+    const double sy = v3_dot(dir, box.axis[1]) >= 0 ? 1 : -1;
+    const double sz = v3_dot(dir, box.axis[2]) >= 0 ? 1 : -1;
+    v3_copy(out, box.center);
+    v3_add_scaled(out, box.axis[0], box.half[0] * sx);
+    v3_add_scaled(out, box.axis[1], box.half[1] * sy);
+    v3_add_scaled(out, box.axis[2], box.half[2] * sz);
+  }
+  void getFaceAxes(const OBB &box, int axisIndex, double *u, double *v) {
+    if (axisIndex == 0) {
+      v3_copy(u, box.axis[1]); v3_copy(v, box.axis[2]); faceExtU = box.half[1]; faceExtV = box.half[2];
+    } else if (axisIndex == 1) {
+      v3_copy(u, box.axis[0]); v3_copy(v, box.axis[2]); faceExtU = box.half[0]; faceExtV = box.half[2];
+    } else {
+      v3_copy(u, box.axis[0]); v3_copy(v, box.axis[1]); faceExtU = box.half[0]; faceExtV = box.half[1];
+    }
+  }
+  void buildFaceFrame(const OBB &box, int axisIndex, const double *outwardNormal) {
+    const double s = v3_dot(outwardNormal, box.axis[axisIndex]) >= 0 ? 1 : -1;
+    v3_scale(frameNormal, box.axis[axisIndex], s);
+    v3_copy(frameCenter, box.center);
+    v3_add_scaled(frameCenter, frameNormal, box.half[axisIndex]);
+    getFaceAxes(box, axisIndex, frameU, frameV);
+    frameExtentU = faceExtU;
+    frameExtentV = faceExtV;
+  }
+  static int chooseIncidentFaceAxis(const OBB &box, const double *referenceNormal) {
+    int axis = 0;
+    double best = -INF;
+    for (int i = 0; i < 3; i++) {
+      const double d = absDot(box.axis[i], referenceNormal);
+      if (d > best) { best = d; axis = i; }
+    }
+    return axis;
+  }
+  void buildIncidentFace(double *outVerts, const OBB &box, int axisIndex, const double *referenceNormal) {
+    double t0[3], t1[3], t2[3], t3[3];
+    const double s = v3_dot(box.axis[axisIndex], referenceNormal) > 0 ? -1 : 1;
+    v3_scale(t0, box.axis[axisIndex], s);
+    v3_copy(t1, box.center);
+    v3_add_scaled(t1, t0, box.half[axisIndex]);
+    getFaceAxes(box, axisIndex, t2, t3);
+    const double eU = faceExtU, eV = faceExtV;
+    for (int i = 0; i < 4; i++) {
+      const double su = (i == 0 || i == 3) ? 1 : -1;
+      const double sv = (i == 0 || i == 1) ? 1 : -1;
+      outVerts[i * 3 + 0] = t1[0] + t2[0] * (eU * su) + t3[0] * (eV * sv);
+      outVerts[i * 3 + 1] = t1[1] + t2[1] * (eU * su) + t3[1] * (eV * sv);
+      outVerts[i * 3 + 2] = t1[2] + t2[2] * (eU * su) + t3[2] * (eV * sv);
+    }
+  }
+  static int clipPolygonAgainstPlane(const double *inV, int inCount, const double *pn, double po, double *outV) {
+    if (inCount <= 0) return 0;
+    int outCount = 0;
+    double ax = inV[(inCount - 1) * 3 + 0], ay = inV[(inCount - 1) * 3 + 1], az = inV[(inCount - 1) * 3 + 2];
+    double da = pn[0] * ax + pn[1] * ay + pn[2] * az - po;
+    for (int i = 0; i < inCount; i++) {
+      const double bx = inV[i * 3 + 0], by = inV[i * 3 + 1], bz = inV[i * 3 + 2];
+      const double db = pn[0] * bx + pn[1] * by + pn[2] * bz - po;
+      const bool aInside = da <= PLANE_EPSILON;
+      const bool bInside = db <= PLANE_EPSILON;
+      if (aInside != bInside) {
+        double t = 0;
+        const double denom = da - db;
+        if (std::fabs(denom) > SAT_AXIS_EPSILON) t = clamp(da / denom, 0, 1);
+        if (outCount < MAX_POLY_VERTS) {
+          outV[outCount * 3 + 0] = ax + (bx - ax) * t;
+          outV[outCount * 3 + 1] = ay + (by - ay) * t;
+          outV[outCount * 3 + 2] = az + (bz - az) * t;
+          outCount++;
+        }
+      }
+      if (bInside && outCount < MAX_POLY_VERTS) {
+        outV[outCount * 3 + 0] = bx; outV[outCount * 3 + 1] = by; outV[outCount * 3 + 2] = bz;
+        outCount++;
+      }
+      ax = bx; ay = by; az = bz; da = db;
+    }
+    return outCount;
+  }
+  // collide.js:254-285
+  bool addContact(const Body &A, const Body &B, Contact *contacts, const double *xA, const double *xB, uint32_t key) {
+    const double mx = (xA[0] + xB[0]) * 0.5, my = (xA[1] + xB[1]) * 0.5, mz = (xA[2] + xB[2]) * 0.5;
+    for (int i = 0; i < stateCount; i++) {
+      const double dx = mx - midpoints[i * 3 + 0], dy = my - midpoints[i * 3 + 1], dz = mz - midpoints[i * 3 + 2];
+      if (dx * dx + dy * dy + dz * dz < CONTACT_MERGE_DIST_SQ) return false;
+    }
+    if (stateCount >= MAX_CONTACTS) return false;
+    Contact &c = contacts[stateCount];
+    c.feature = key;
+    double inv[4], t[3];
+    q_conjugate(inv, A.positionAng);
+    v3_sub(t, xA, A.positionLin);
+    q_rotate(c.rA, inv, t);
+    q_conjugate(inv, B.positionAng);
+    v3_sub(t, xB, B.positionLin);
+    q_rotate(c.rB, inv, t);
+    midpoints[stateCount * 3 + 0] = mx; midpoints[stateCount * 3 + 1] = my; midpoints[stateCount * 3 + 2] = mz;
+    stateCount++;
+    return true;
+  }
+  // collide.js:291-324
+  bool testAxis(const double *delta, const double *axis, int type, int indexA, int indexB, SatAxis &target) {
+    const double lenSq = v3_len_sq(axis);
+    if (lenSq < SAT_AXIS_EPSILON) return true;
+    const double invLen = 1.0 / std::sqrt(lenSq);
+    double n[3];
+    v3_scale(n, axis, invLen);
+    if (v3_dot(n, delta) < 0) v3_negate(n, n);
+    const double distance = std::fabs(v3_dot(delta, n));
+    const double rA = boxA.half[0] * absDot(n, boxA.axis[0]) + boxA.half[1] * absDot(n, boxA.axis[1]) +
+                      boxA.half[2] * absDot(n, boxA.axis[2]);
+    const double rB = boxB.half[0] * absDot(n, boxB.axis[0]) + boxB.half[1] * absDot(n, boxB.axis[1]) +
+                      boxB.half[2] * absDot(n, boxB.axis[2]);
+    const double separation = distance - (rA + rB);
+    if (separation > 0) return false;
+    if (!target.valid || separation > target.separation) {
+      target.valid = true;
+      target.type = type; target.indexA = indexA; target.indexB = indexB;
+      target.separation = separation;
+      v3_copy(target.normalAB, n);
+    }
+    return true;
+  }
+  static void supportEdge(const OBB &box, int axisIndex, const double *dir, double *edgeA, double *edgeB) {
+    const int axis1 = (axisIndex + 1) % 3, axis2 = (axisIndex + 2) % 3;
+    const double sign1 = v3_dot(dir, box.axis[axis1]) >= 0 ? 1 : -1;
+    const double sign2 = v3_dot(dir, box.axis[axis2]) >= 0 ? 1 : -1;
+    double t[3];
+    v3_copy(t, box.center);
+    v3_add_scaled(t, box.axis[axis1], box.half[axis1] * sign1);
+    v3_add_scaled(t, box.axis[axis2], box.half[axis2] * sign2);
+    v3_copy(edgeA, t);
+    v3_add_scaled(edgeA, box.axis[axisIndex], -box.half[axisIndex]);
+    v3_copy(edgeB, t);
+    v3_add_scaled(edgeB, box.axis[axisIndex], box.half[axisIndex]);
+  }
+  // collide.js:345-393
+  static void closestPointsOnSegments(const double *p0, const double *p1, const double *q0, const double *q1,
+                                      double *c0, double *c1) {
+    const double d1x = p1[0] - p0[0], d1y = p1[1] - p0[1], d1z = p1[2] - p0[2];
+    const double d2x = q1[0] - q0[0], d2y = q1[1] - q0[1], d2z = q1[2] - q0[2];
+    const double rx = p0[0] - q0[0], ry = p0[1] - q0[1], rz = p0[2] - q0[2];
+    const double a = d1x * d1x + d1y * d1y + d1z * d1z;
+    const double e = d2x * d2x + d2y * d2y + d2z * d2z;
+    const double f = d2x * rx + d2y * ry + d2z * rz;
+    double s = 0, t = 0;
+    if (a <= SAT_AXIS_EPSILON && e <= SAT_AXIS_EPSILON) {
+      v3_copy(c0, p0); v3_copy(c1, q0);
+      return;
+    }
+    if (a <= SAT_AXIS_EPSILON) {
+      t = clamp(f / e, 0, 1);
+    } else {
+      const double c = d1x * rx + d1y * ry + d1z * rz;
+      if (e <= SAT_AXIS_EPSILON) {
+        s = clamp(-c / a, 0, 1);
+      } else {
+        const double b = d1x * d2x + d1y * d2y + d1z * d2z;
+        const double denom = a * e - b * b;
+        if (std::fabs(denom) > SAT_AXIS_EPSILON) s = clamp((b * f - c * e) / denom, 0, 1);
+        t = (b * s + f) / e;
+        if (t < 0) { t = 0; s = clamp(-c / a, 0, 1); }
+        else if (t > 1) { t = 1; s = clamp((b - c) / a, 0, 1); }
+      }
+    }
+    c0[0] = p0[0] + d1x * s; c0[1] = p0[1] + d1y * s; c0[2] = p0[2] + d1z * s;
+    c1[0] = q0[0] + d2x * t; c1[1] = q0[1] + d2y * t; c1[2] = q0[2] + d2z * t;
+  }
+  // collide.js:403-472
+  int buildFaceManifold(const Body &A, const Body &B, bool referenceIsA, int referenceAxis, const double *normalAB,
+                        Contact *contacts) {
+    const OBB &referenceBox = referenceIsA ? boxA : boxB;
+    const OBB &incidentBox = referenceIsA ? boxB : boxA;
+    double t0[3];
+    if (referenceIsA) v3_copy(t0, normalAB);
+    else v3_negate(t0, normalAB);
+    buildFaceFrame(referenceBox, referenceAxis, t0);
+    const int incidentAxis = chooseIncidentFaceAxis(incidentBox, frameNormal);
+    buildIncidentFace(clip0, incidentBox, incidentAxis, frameNormal);
+    int count = 4;
+    double pn[3];
+    v3_copy(pn, frameU);
+    count = clipPolygonAgainstPlane(clip0, count, pn, v3_dot(pn, frameCenter) + frameExtentU, clip1);
+    if (!count) return 0;
+    v3_negate(pn, frameU);
+    count = clipPolygonAgainstPlane(clip1, count, pn, v3_dot(pn, frameCenter) + frameExtentU, clip0);
+    if (!count) return 0;
+    v3_copy(pn, frameV);
+    count = clipPolygonAgainstPlane(clip0, count, pn, v3_dot(pn, frameCenter) + frameExtentV, clip1);
+    if (!count) return 0;
+    v3_negate(pn, frameV);
+    count = clipPolygonAgainstPlane(clip1, count, pn, v3_dot(pn, frameCenter) + frameExtentV, clip0);
+    if (!count) return 0;
+
+    stateCount = 0;
+    uint32_t featurePrefix = (uint32_t)(referenceIsA ? AXIS_FACE_A : AXIS_FACE_B) << 24;
+    featurePrefix |= (uint32_t)(referenceAxis & 0xff) << 16;
+    featurePrefix |= (uint32_t)(incidentAxis & 0xff) << 8;
+    double p[3], q[3], xA[3], xB[3];
+    for (int i = 0; i < count && stateCount < MAX_CONTACTS; i++) {
+      p[0] = clip0[i * 3 + 0]; p[1] = clip0[i * 3 + 1]; p[2] = clip0[i * 3 + 2];
+      v3_sub(q, p, frameCenter);
+      const double distance = v3_dot(q, frameNormal);
+      if (distance > PLANE_EPSILON) continue;
+      v3_copy(q, p);
+      v3_add_scaled(q, frameNormal, -distance);
+      if (referenceIsA) { v3_copy(xA, q); v3_copy(xB, p); }
+      else { v3_copy(xA, p); v3_copy(xB, q); }
+      addContact(A, B, contacts, xA, xB, featurePrefix | (uint32_t)(i & 0xff));
+    }
+    if (!stateCount) {
+      double neg[3];
+      supportPoint(xA, boxA, normalAB);
+      v3_negate(neg, normalAB);
+      supportPoint(xB, boxB, neg);
+      addContact(A, B, contacts, xA, xB, featurePrefix);
+    }
+    return stateCount;
+  }
+  // collide.js:475-493
+  int buildEdgeContact(const Body &A, const Body &B, int axisA, int axisB, const double *normalAB, Contact *contacts) {
+    double neg[3], eA0[3], eA1[3], eB0[3], eB1[3], xA[3], xB[3];
+    v3_negate(neg, normalAB);
+    supportEdge(boxA, axisA, normalAB, eA0, eA1);
+    supportEdge(boxB, axisB, neg, eB0, eB1);
+    closestPointsOnSegments(eA0, eA1, eB0, eB1, xA, xB);
+    stateCount = 0;
+    const uint32_t key = ((uint32_t)AXIS_EDGE << 24) | ((uint32_t)(axisA & 0xff) << 8) | (uint32_t)(axisB & 0xff);
+    addContact(A, B, contacts, xA, xB, key);
+    if (!stateCount) {
+      supportPoint(xA, boxA, normalAB);
+      supportPoint(xB, boxB, neg);
+      addContact(A, B, contacts, xA, xB, key);
+    }
+    return stateCount;
+  }
+  // collide.js:496-520
+  int sphereSphere(const Body &A, const Body &B, Contact *contacts, double *basisOut) {
+    double delta[3], n[3], t[3], xA[3], xB[3];
+    v3_sub(delta, B.positionLin, A.positionLin);
+    const double distanceSq = v3_len_sq(delta);
+    const double radiusSum = A.radius + B.radius;
+    if (distanceSq > radiusSum * radiusSum) return 0;
+    if (distanceSq > SPHERE_DISTANCE_EPSILON_SQ) v3_scale(n, delta, 1 / std::sqrt(distanceSq));
+    else v3_set(n, 1, 0, 0);
+    v3_negate(t, n);
+    m3_orthonormal(basisOut, t);
+    v3_copy(xA, A.positionLin);
+    v3_add_scaled(xA, n, A.radius);
+    v3_copy(xB, B.positionLin);
+    v3_add_scaled(xB, n, -B.radius);
+    stateCount = 0;
+    addContact(A, B, contacts, xA, xB, 0x31000001u);
+    return stateCount;
+  }
+  // collide.js:526-600
+  int sphereBox(const Body &A, const Body &B, Contact *contacts, double *basisOut, bool sphereIsA) {
+    const Body &sphere = sphereIsA ? A : B;
+    const Body &boxBody = sphereIsA ? B : A;
+    makeOBB(boxA, boxBody);
+    double delta[3], closest[3], t3[3], n[3], t0[3], xA[3], xB[3];
+    v3_sub(delta, sphere.positionLin, boxA.center);
+    const double lx = v3_dot(delta, boxA.axis[0]);
+    const double ly = v3_dot(delta, boxA.axis[1]);
+    const double lz = v3_dot(delta, boxA.axis[2]);
+    const double cx = clamp(lx, -boxA.half[0], boxA.half[0]);
+    const double cy = clamp(ly, -boxA.half[1], boxA.half[1]);
+    const double cz = clamp(lz, -boxA.half[2], boxA.half[2]);
+    v3_copy(closest, boxA.center);
+    v3_add_scaled(closest, boxA.axis[0], cx);
+    v3_add_scaled(closest, boxA.axis[1], cy);
+    v3_add_scaled(closest, boxA.axis[2], cz);
+    v3_sub(t3, sphere.positionLin, closest);
+    const double distanceSq = v3_len_sq(t3);
+    int featureAxis = 0;
+    if (distanceSq > SPHERE_DISTANCE_EPSILON_SQ) {
+      const double distance = std::sqrt(distanceSq);
+      if (distance > sphere.radius) return 0;
+      v3_scale(n, t3, 1 / distance);
+    } else {
+      const double gx = boxA.half[0] - std::fabs(lx);
+      const double gy = boxA.half[1] - std::fabs(ly);
+      const double gz = boxA.half[2] - std::fabs(lz);
+      featureAxis = gx < gy ? (gx < gz ? 0 : 2) : (gy < gz ? 1 : 2);
+      const double local = featureAxis == 0 ? lx : featureAxis == 1 ? ly : lz;
+      const double sgn = local >= 0 ? 1 : -1;
+      v3_scale(n, boxA.axis[featureAxis], sgn);
+      const double gap = featureAxis == 0 ? gx : featureAxis == 1 ? gy : gz;
+      v3_copy(closest, sphere.positionLin);
+      v3_add_scaled(closest, n, gap);
+    }
+    v3_copy(t3, sphere.positionLin);
+    v3_add_scaled(t3, n, -sphere.radius);
+    if (sphereIsA) {
+      v3_copy(xA, t3); v3_copy(xB, closest);
+      m3_orthonormal(basisOut, n);
+    } else {
+      v3_copy(xA, closest); v3_copy(xB, t3);
+      v3_negate(t0, n);
+      m3_orthonormal(basisOut, t0);
+    }
+    stateCount = 0;
+    int sideX = lx < -boxA.half[0] ? 1 : lx > boxA.half[0] ? 2 : 0;
+    int sideY = ly < -boxA.half[1] ? 1 : ly > boxA.half[1] ? 2 : 0;
+    int sideZ = lz < -boxA.half[2] ? 1 : lz > boxA.half[2] ? 2 : 0;
+    if ((sideX | sideY | sideZ) == 0) {
+      const double local = featureAxis == 0 ? lx : featureAxis == 1 ? ly : lz;
+      const int side = local >= 0 ? 2 : 1;
+      if (featureAxis == 0) sideX = side;
+      else if (featureAxis == 1) sideY = side;
+      else sideZ = side;
+    }
+    const uint32_t region = (uint32_t)(sideX | (sideY << 2) | (sideZ << 4));
+    const uint32_t feature = 0x32000000u | (region << 2) | (sphereIsA ? 1u : 2u);
+    addContact(A, B, contacts, xA, xB, feature);
+    return stateCount;
+  }
+  // collide.js:612-685
+  int collide(const Body &A, const Body &B, Contact *contacts, double *basisOut) {
+    const bool sA = A.shape == AVBD_SHAPE_SPHERE, sB = B.shape == AVBD_SHAPE_SPHERE;
+    if (sA && sB) return sphereSphere(A, B, contacts, basisOut);
+    if (sA || sB) return sphereBox(A, B, contacts, basisOut, sA);
+    makeOBB(boxA, A);
+    makeOBB(boxB, B);
+    double delta[3], axis[3], t0[3];
+    v3_sub(delta, boxB.center, boxA.center);
+    SatAxis bestFace, bestEdge, best;
+    bestFace.separation = -INF; bestFace.valid = false;
+    bestEdge.separation = -INF; bestEdge.valid = false;
+    for (int i = 0; i < 3; i++)
+      if (!testAxis(delta, boxA.axis[i], AXIS_FACE_A, i, -1, bestFace)) return 0;
+    for (int i = 0; i < 3; i++)
+      if (!testAxis(delta, boxB.axis[i], AXIS_FACE_B, -1, i, bestFace)) return 0;
+    for (int i = 0; i < 3; i++)
+      for (int j = 0; j < 3; j++) {
+        v3_cross(axis, boxA.axis[i], boxB.axis[j]);
+        if (!testAxis(delta, axis, AXIS_EDGE, i, j, bestEdge)) return 0;
+      }
+    if (!bestFace.valid) return 0;
+    best = bestFace;
+    if (bestEdge.valid) {
+      const double edgeRelTol = 0.95, edgeAbsTol = 0.01;
+      if (edgeRelTol * bestEdge.separation > bestFace.separation + edgeAbsTol) best = bestEdge;
+    }
+    v3_negate(t0, best.normalAB);
+    m3_orthonormal(basisOut, t0);
+    if (best.type == AXIS_EDGE) return buildEdgeContact(A, B, best.indexA, best.indexB, best.normalAB, contacts);
+    if (best.type == AXIS_FACE_A) return buildFaceManifold(A, B, true, best.indexA, best.normalAB, contacts);
+    return buildFaceManifold(A, B, false, best.indexB, best.normalAB, contacts);
+  }
+};
+
+// ---------------------------------------------------------------------------
+// Solver state
+// ---------------------------------------------------------------------------
+struct Solver {
+  Params p;
+  std::vector<Body *> bodies;
+  std::vector<Force *> forces;
+  std::vector<int32_t> bodyOrder;   // explicit order (AVBD_ORDER_EXPLICIT)
+  std::vector<int32_t> lastColorOf; // priority colouring of the last step
+  int lastNumColors = 0;
+  std::vector<int64_t> lastPairs;   // manifolds initialised in the last step, (A<<32)|B
+  Collider collider;
+  std::vector<Force *> graveyard;   // removed forces, freed with the solver
+  ~Solver();
+};
+
+// ---------------------------------------------------------------------------
+// Manifold (src/physics/manifold.js)
+// ---------------------------------------------------------------------------
+static void transportComponents(double *out, const double *value, const double *oldB, const double *newB) {
+  const double x = value[0], y = value[1], z = value[2];
+  double r3[3];
+  for (int r = 0; r < 3; r++) {
+    const int n = r * 3;
+    r3[r] = x * (newB[n] * oldB[0] + newB[n + 1] * oldB[1] + newB[n + 2] * oldB[2]) +
+            y * (newB[n] * oldB[3] + newB[n + 1] * oldB[4] + newB[n + 2] * oldB[5]) +
+            z * (newB[n] * oldB[6] + newB[n + 1] * oldB[7] + newB[n + 2] * oldB[8]);
+    out[r] = r3[r];
+  }
+}
+static void transportPenalty(double *out, const double *value, const double *oldB, const double *newB) {
+  const double x = value[0], y = value[1], z = value[2];
+  for (int r = 0; r < 3; r++) {
+    const int n = r * 3;
+    const double dx = newB[n] * oldB[0] + newB[n + 1] * oldB[1] + newB[n + 2] * oldB[2];
+    const double dy = newB[n] * oldB[3] + newB[n + 1] * oldB[4] + newB[n + 2] * oldB[5];
+    const double dz = newB[n] * oldB[6] + newB[n + 1] * oldB[7] + newB[n + 2] * oldB[8];
+    out[r] = x * dx * dx + y * dy * dy + z * dz * dz;
+  }
+}
+
+struct Manifold : Force {
+  Contact contacts[MAX_CONTACTS];
+  Contact newContacts[MAX_CONTACTS];
+  double basis[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  int numContacts = 0;
+  double friction = 0;
+  double jacobians[MAX_CONTACTS * 18];
+  bool jacobiansValid = false;
+  // _beginPass scratch
+  double dqALin[3], dqAAng[3], dqBLin[3], dqBAng[3], jALin[9], jBLin[9], jAAng[9], jBAng[9];
+  double K[9], Cv[3], F[3];
+
+  Manifold() { kind = KIND_MANIFOLD; }
+
+  // manifold.js:214-318
+  bool initialize() override {
+    Body &A = *bodyA, &B = *bodyB;
+    jacobiansValid = false;
+    const bool hasSphere = A.shape == AVBD_SHAPE_SPHERE || B.shape == AVBD_SHAPE_SPHERE;
+    const bool hadContacts = numContacts > 0;
+    double oldBasis[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    if (hasSphere && hadContacts) m3_copy(oldBasis, basis);
+    friction = std::sqrt(A.friction * B.friction);
+    for (int i = 0; i < MAX_CONTACTS; i++) newContacts[i].reset();
+    const int newNum = solver->collider.collide(A, B, newContacts, basis);
+    const bool basisCompatible =
+        !hasSphere || !hadContacts || (oldBasis[0] * basis[0] + oldBasis[1] * basis[1] + oldBasis[2] * basis[2]) > 0.85;
+    for (int i = 0; i < newNum; i++) {
+      for (int j = 0; j < numContacts; j++) {
+        if (basisCompatible && newContacts[i].feature == contacts[j].feature) {
+          double nrA[3], nrB[3];
+          v3_copy(nrA, newContacts[i].rA);
+          v3_copy(nrB, newContacts[i].rB);
+          newContacts[i].copyFrom(contacts[j]);
+          if (hasSphere) {
+            transportComponents(newContacts[i].lambda, newContacts[i].lambda, oldBasis, basis);
+            transportPenalty(newContacts[i].penalty, newContacts[i].penalty, oldBasis, basis);
+          }
+          if (!contacts[j].stick || hasSphere) {
+            v3_copy(newContacts[i].rA, nrA);
+            v3_copy(newContacts[i].rB, nrB);
+          }
+          break;
+        }
+      }
+    }
+    numContacts = newNum;
+    for (int i = 0; i < newNum; i++) contacts[i].copyFrom(newContacts[i]);
+    const Params &P = solver->p;
+    for (int i = 0; i < numContacts; i++) {
+      Contact &c = contacts[i];
+      double xA[3], xB[3], d[3];
+      transform_point(xA, A.positionLin, A.positionAng, c.rA);
+      transform_point(xB, B.positionLin, B.positionAng, c.rB);
+      v3_sub(d, xA, xB);
+      m3_mul_vec(c.C0, basis, d);
+      c.C0[0] += P.collisionMargin;
+      if (!P.postStabilize) {
+        v3_scale(c.lambda, c.lambda, P.alpha);
+        v3_scale(c.lambda, c.lambda, P.gamma);
+      }
+      v3_scale(c.penalty, c.penalty, P.gamma);
+      v3_clamp_scalar(c.penalty, c.penalty, P.penaltyMin, P.penaltyMax);
+    }
+    return numContacts > 0;
+  }
+
+  // manifold.js:325-350
+  static void angularBlocks(const double *rAW, const double *rBW, const double *jALin, const double *jBLin,
+                            double *jAAng, double *jBAng) {
+    double row[3], acc[3];
+    for (int r = 0; r < 3; r++) {
+      m3_get_row(row, jALin, r);
+      v3_cross(acc, rAW, row);
+      jAAng[r * 3 + 0] = acc[0]; jAAng[r * 3 + 1] = acc[1]; jAAng[r * 3 + 2] = acc[2];
+      m3_get_row(row, jBLin, r);
+      v3_cross(acc, rBW, row);
+      jBAng[r * 3 + 0] = acc[0]; jBAng[r * 3 + 1] = acc[1]; jBAng[r * 3 + 2] = acc[2];
+    }
+  }
+  void beginPass() {
+    Body &A = *bodyA, &B = *bodyB;
+    v3_sub(dqALin, A.positionLin, A.initialLin);
+    q_subtract(dqAAng, A.positionAng, A.initialAng);
+    v3_sub(dqBLin, B.positionLin, B.initialLin);
+    q_subtract(dqBAng, B.positionAng, B.initialAng);
+    m3_copy(jALin, basis);
+    m3_negate(jBLin, basis);
+    if (solver->p.cachedJacobians && !jacobiansValid) {
+      for (int i = 0; i < numContacts; i++) {
+        double rAW[3], rBW[3];
+        q_rotate(rAW, A.initialAng, contacts[i].rA);
+        q_rotate(rBW, B.initialAng, contacts[i].rB);
+        angularBlocks(rAW, rBW, jALin, jBLin, jAAng, jBAng);
+        std::memcpy(&jacobians[i * 18], jAAng, sizeof(double) * 9);
+        std::memcpy(&jacobians[i * 18 + 9], jBAng, sizeof(double) * 9);
+      }
+      jacobiansValid = true;
+    }
+  }
+  // manifold.js:358-409
+  bool evaluate(int i, double alpha) {
+    Contact &c = contacts[i];
+    if (solver->p.cachedJacobians) {
+      for (int k = 0; k < 9; k++) { jAAng[k] = jacobians[i * 18 + k]; jBAng[k] = jacobians[i * 18 + 9 + k]; }
+    } else {
+      double rAW[3], rBW[3];
+      q_rotate(rAW, bodyA->positionAng, c.rA);
+      q_rotate(rBW, bodyB->positionAng, c.rB);
+      angularBlocks(rAW, rBW, jALin, jBLin, jAAng, jBAng);
+    }
+    m3_diagonal(K, c.penalty[0], c.penalty[1], c.penalty[2]);
+    double acc[3];
+    v3_scale(Cv, c.C0, 1 - alpha);
+    m3_mul_vec(acc, jALin, dqALin); v3_add(Cv, Cv, acc);
+    m3_mul_vec(acc, jBLin, dqBLin); v3_add(Cv, Cv, acc);
+    m3_mul_vec(acc, jAAng, dqAAng); v3_add(Cv, Cv, acc);
+    m3_mul_vec(acc, jBAng, dqBAng); v3_add(Cv, Cv, acc);
+    m3_mul_vec(F, K, Cv);
+    v3_add(F, F, c.lambda);
+    F[0] = js_min(F[0], 0);
+    const double bounds = std::fabs(F[0]) * friction;
+    const double frictionScale = std::sqrt(F[1] * F[1] + F[2] * F[2]);
+    if (frictionScale > bounds && frictionScale > 0) {
+      F[1] *= bounds / frictionScale;
+      F[2] *= bounds / frictionScale;
+    }
+    return frictionScale <= bounds;
+  }
+  // manifold.js:411-445
+  void updatePrimal(Body *body, double alpha, double *lhsLin, double *lhsAng, double *lhsCross, double *rhsLin,
+                    double *rhsAng) override {
+    const bool isA = body == bodyA;
+    beginPass();
+    double jLinT[9], jAngT[9], jAngTk[9], m0[9], acc[3];
+    for (int i = 0; i < numContacts; i++) {
+      Contact &c = contacts[i];
+      evaluate(i, alpha);
+      const double *jLin = isA ? jALin : jBLin;
+      const double *jAng = isA ? jAAng : jBAng;
+      m3_transpose(jLinT, jLin);
+      m3_transpose(jAngT, jAng);
+      m3_mul_diag_right(jAngTk, jAngT, c.penalty[0], c.penalty[1], c.penalty[2]);
+      m3_mul_diag_right(m0, jLinT, c.penalty[0], c.penalty[1], c.penalty[2]);
+      m3_mul(m0, m0, jLin);
+      m3_add_into(lhsLin, m0);
+      m3_mul(m0, jAngTk, jAng);
+      m3_add_into(lhsAng, m0);
+      m3_mul(m0, jAngTk, jLin);
+      m3_add_into(lhsCross, m0);
+      m3_mul_vec(acc, jLinT, F);
+      v3_add(rhsLin, rhsLin, acc);
+      m3_mul_vec(acc, jAngT, F);
+      v3_add(rhsAng, rhsAng, acc);
+    }
+  }
+  // manifold.js:447-491
+  void updateDual(double alpha) override {
+    const Params &P = solver->p;
+    beginPass();
+    for (int i = 0; i < numContacts; i++) {
+      Contact &c = contacts[i];
+      const bool within = evaluate(i, alpha);
+      v3_copy(c.lambda, F);
+      v3_copy(c.C, Cv);
+      if (F[0] < 0) c.penalty[0] = js_min(c.penalty[0] + P.betaLin * std::fabs(Cv[0]), P.penaltyMax);
+      if (within) {
+        c.penalty[1] = js_min(c.penalty[1] + P.betaLin * std::fabs(Cv[1]), P.penaltyMax);
+        c.penalty[2] = js_min(c.penalty[2] + P.betaLin * std::fabs(Cv[2]), P.penaltyMax);
+        c.stick = std::sqrt(Cv[1] * Cv[1] + Cv[2] * Cv[2]) < P.stickThreshold;
+      } else if (bodyA->shape == AVBD_SHAPE_SPHERE || bodyB->shape == AVBD_SHAPE_SPHERE) {
+        c.stick = false;
+      }
+    }
+  }
+  double maxLambda() const override {
+    double m = 0;
+    for (int i = 0; i < numContacts; i++) {
+      const double *l = contacts[i].lambda;
+      m = js_max(m, js_max(std::fabs(l[0]), js_max(std::fabs(l[1]), std::fabs(l[2]))));
+    }
+    return m;
+  }
+  double maxPenalty() const override {
+    double m = 0;
+    for (int i = 0; i < numContacts; i++) {
+      const double *p = contacts[i].penalty;
+      m = js_max(m, js_max(p[0], js_max(p[1], p[2])));
+    }
+    return m;
+  }
+  double maxConstraintError() const override {
+    double m = 0;
+    for (int i = 0; i < numContacts; i++) m = js_max(m, js_max(0, -contacts[i].C[0]));
+    return m;
+  }
+};
+
+// ---------------------------------------------------------------------------
+// Joint (src/physics/joint.js)
+// ---------------------------------------------------------------------------
+static void geometricStiffnessBallSocket(double *out, int k, const double *v) {
+  m3_diagonal(out, -v[k], -v[k], -v[k]);
+  out[0 * 3 + k] += v[0];
+  out[1 * 3 + k] += v[1];
+  out[2 * 3 + k] += v[2];
+}
+
+struct Joint : Force {
+  double rA[3], rB[3];
+  double stiffnessLin = INF, stiffnessAng = 0, fracture = INF;
+  bool broken = false;
+  double C0Lin[3] = {0, 0, 0}, C0Ang[3] = {0, 0, 0};
+  double penaltyLin[3] = {0, 0, 0}, penaltyAng[3] = {0, 0, 0};
+  double lambdaLin[3] = {0, 0, 0}, lambdaAng[3] = {0, 0, 0};
+  double CLin[3] = {0, 0, 0}, CAng[3] = {0, 0, 0};
+  double torqueArm = 0;
+
+  Joint() { kind = KIND_JOINT; }
+  bool isBroken() const override { return broken; }
+  void setup() { // joint.js:108-112
+    const double *sA = bodyA ? bodyA->size : nullptr;
+    const double sx = (sA ? sA[0] : 0) + bodyB->size[0];
+    const double sy = (sA ? sA[1] : 0) + bodyB->size[1];
+    const double sz = (sA ? sA[2] : 0) + bodyB->size[2];
+    torqueArm = sx * sx + sy * sy + sz * sz;
+  }
+  void evalLinear(double *out) const {
+    double pA[3], pB[3];
+    if (bodyA) transform_point(pA, bodyA->positionLin, bodyA->positionAng, rA);
+    else v3_copy(pA, rA);
+    transform_point(pB, bodyB->positionLin, bodyB->positionAng, rB);
+    v3_sub(out, pA, pB);
+  }
+  void evalAngular(double *out) const {
+    static const double identity[4] = {0, 0, 0, 1};
+    q_subtract(out, bodyA ? bodyA->positionAng : identity, bodyB->positionAng);
+    v3_scale(out, out, torqueArm);
+  }
+  // joint.js:131-160
+  bool initialize() override {
+    const Params &P = solver->p;
+    evalLinear(C0Lin);
+    evalAngular(C0Ang);
+    if (!P.postStabilize) {
+      v3_scale(lambdaLin, lambdaLin, P.alpha); v3_scale(lambdaLin, lambdaLin, P.gamma);
+      v3_scale(lambdaAng, lambdaAng, P.alpha); v3_scale(lambdaAng, lambdaAng, P.gamma);
+    }
+    v3_scale(penaltyLin, penaltyLin, P.gamma);
+    v3_clamp_scalar(penaltyLin, penaltyLin, P.penaltyMin, P.penaltyMax);
+    v3_scale(penaltyAng, penaltyAng, P.gamma);
+    v3_clamp_scalar(penaltyAng, penaltyAng, P.penaltyMin, P.penaltyMax);
+    v3_min_scalar(penaltyLin, penaltyLin, stiffnessLin);
+    v3_min_scalar(penaltyAng, penaltyAng, stiffnessAng);
+    return !broken;
+  }
+  // joint.js:162-253
+  void updatePrimal(Body *body, double alpha, double *lhsLin, double *lhsAng, double *lhsCross, double *rhsLin,
+                    double *rhsAng) override {
+    const bool isA = body == bodyA;
+    double K[9], C[3], F[3], rW[3], r[3], jLin[9], jAng[9], jLinT[9], jAngT[9], jAngTk[9], m0[9], H[9], G[9], acc[3];
+    if (v3_len_sq(penaltyLin) > 0) {
+      m3_diagonal(K, penaltyLin[0], penaltyLin[1], penaltyLin[2]);
+      evalLinear(C);
+      if (stiffnessLin == INF) v3_add_scaled(C, C0Lin, -alpha);
+      m3_mul_vec(F, K, C);
+      v3_add(F, F, lambdaLin);
+      if (isA) {
+        m3_diagonal(jLin, 1, 1, 1);
+        q_rotate(rW, bodyA->positionAng, rA);
+        v3_negate(r, rW);
+        m3_skew(jAng, r);
+        v3_copy(r, rW);
+      } else {
+        m3_diagonal(jLin, -1, -1, -1);
+        q_rotate(rW, bodyB->positionAng, rB);
+        m3_skew(jAng, rW);
+        v3_negate(r, rW);
+      }
+      const double k0 = penaltyLin[0], k1 = penaltyLin[1], k2 = penaltyLin[2];
+      m3_transpose(jLinT, jLin);
+      m3_transpose(jAngT, jAng);
+      m3_mul_diag_right(jAngTk, jAngT, k0, k1, k2);
+      m3_mul_diag_right(m0, jLinT, k0, k1, k2);
+      m3_mul(m0, m0, jLin);
+      m3_add_into(lhsLin, m0);
+      m3_mul(m0, jAngTk, jAng);
+      m3_add_into(lhsAng, m0);
+      m3_mul(m0, jAngTk, jLin);
+      m3_add_into(lhsCross, m0);
+      m3_zero(H);
+      for (int k = 0; k < 3; k++) {
+        geometricStiffnessBallSocket(G, k, r);
+        m3_scale(G, G, F[k]);
+        m3_add_into(H, G);
+      }
+      m3_diagonalize(G, H);
+      m3_add_into(lhsAng, G);
+      m3_mul_vec(acc, jLinT, F);
+      v3_add(rhsLin, rhsLin, acc);
+      m3_mul_vec(acc, jAngT, F);
+      v3_add(rhsAng, rhsAng, acc);
+    }
+    if (v3_len_sq(penaltyAng) > 0) {
+      m3_diagonal(K, penaltyAng[0], penaltyAng[1], penaltyAng[2]);
+      evalAngular(C);
+      if (stiffnessAng == INF) v3_add_scaled(C, C0Ang, -alpha);
+      m3_mul_vec(F, K, C);
+      v3_add(F, F, lambdaAng);
+      const double s = isA ? torqueArm : -torqueArm;
+      m3_diagonal(jAng, s, s, s);
+      m3_transpose(jAngT, jAng);
+      m3_mul(m0, jAngT, K);
+      m3_mul(m0, m0, jAng);
+      m3_add_into(lhsAng, m0);
+      m3_mul_vec(acc, jAngT, F);
+      v3_add(rhsAng, rhsAng, acc);
+    }
+  }
+  // joint.js:255-317
+  void updateDual(double alpha) override {
+    const Params &P = solver->p;
+    double K[9], C[3], F[3], acc[3];
+    if (v3_len_sq(penaltyLin) > 0) {
+      m3_diagonal(K, penaltyLin[0], penaltyLin[1], penaltyLin[2]);
+      evalLinear(C);
+      if (stiffnessLin == INF) {
+        v3_add_scaled(C, C0Lin, -alpha);
+        m3_mul_vec(F, K, C);
+        v3_add(lambdaLin, F, lambdaLin);
+      }
+      v3_copy(CLin, C);
+      v3_abs(acc, C);
+      v3_scale(acc, acc, P.betaLin);
+      v3_add(penaltyLin, penaltyLin, acc);
+      v3_min_scalar(penaltyLin, penaltyLin, js_min(stiffnessLin, P.penaltyMax));
+    }
+    if (v3_len_sq(penaltyAng) > 0) {
+      m3_diagonal(K, penaltyAng[0], penaltyAng[1], penaltyAng[2]);
+      evalAngular(C);
+      if (stiffnessAng == INF) {
+        v3_add_scaled(C, C0Ang, -alpha);
+        m3_mul_vec(F, K, C);
+        v3_add(lambdaAng, F, lambdaAng);
+      }
+      v3_copy(CAng, C);
+      v3_abs(acc, C);
+      v3_scale(acc, acc, P.betaAng);
+      v3_add(penaltyAng, penaltyAng, acc);
+      v3_min_scalar(penaltyAng, penaltyAng, js_min(stiffnessAng, P.penaltyMax));
+    }
+    if (v3_len_sq(lambdaAng) > fracture * fracture) {
+      v3_zero(penaltyLin); v3_zero(penaltyAng); v3_zero(lambdaLin); v3_zero(lambdaAng);
+      broken = true;
+    }
+  }
+  double maxLambda() const override { return std::sqrt(js_max(v3_len_sq(lambdaLin), v3_len_sq(lambdaAng))); }
+  double maxPenalty() const override {
+    double m = penaltyLin[0];
+    m = js_max(m, penaltyLin[1]); m = js_max(m, penaltyLin[2]);
+    m = js_max(m, penaltyAng[0]); m = js_max(m, penaltyAng[1]); m = js_max(m, penaltyAng[2]);
+    return m;
+  }
+  double maxConstraintError() const override { return std::sqrt(v3_len_sq(CLin)); }
+};
+
+// ---------------------------------------------------------------------------
+// Spring (src/physics/spring.js)
+// ---------------------------------------------------------------------------
+struct Spring : Force {
+  double rA[3], rB[3];
+  double stiffness = 0, rest = 0, penalty = 0, C = 0;
+  double tearStrain = INF;
+  bool broken = false;
+  double peakStrain = 0;
+  // _evaluate scratch (module-level in spring.js)
+  double d[3], n[3], rW[3];
+
+  Spring() { kind = KIND_SPRING; }
+  bool isBroken() const override { return broken; }
+  bool rampEnabled() const { return solver->p.springRamp; }
+  bool geometricEnabled() const { return solver->p.springGeometric; }
+
+  double evaluate() { // spring.js:447-458
+    double pA[3], pB[3];
+    transform_point(pA, bodyA->positionLin, bodyA->positionAng, rA);
+    transform_point(pB, bodyB->positionLin, bodyB->positionAng, rB);
+    v3_sub(d, pA, pB);
+    const double dLen = v3_len(d);
+    if (dLen <= 1.0e-6) return NaN;
+    v3_div(n, d, dLen);
+    return dLen - rest;
+  }
+  bool updateTearing(double Cv) { // spring.js:461-470
+    if (rest <= 1.0e-6) return false;
+    const double strain = js_max(0, Cv / rest);
+    peakStrain = js_max(peakStrain, strain);
+    if (strain <= tearStrain) return false;
+    broken = true;
+    penalty = 0;
+    C = 0;
+    return true;
+  }
+  bool initialize() override { // spring.js:472-507
+    if (broken) { penalty = 0; C = 0; return true; }
+    if (is_finite(tearStrain)) {
+      const double Cv = evaluate();
+      if (!(Cv != Cv)) {
+        C = Cv;
+        if (updateTearing(Cv)) return true;
+      }
+    }
+    const Params &P = solver->p;
+    if (!rampEnabled()) {
+      penalty = stiffness;
+      return stiffness > 0;
+    }
+    penalty = clamp(penalty * P.gamma, P.penaltyMin, P.penaltyMax);
+    penalty = js_min(penalty, stiffness);
+    return stiffness > 0;
+  }
+  void updatePrimal(Body *body, double alpha, double *lhsLin, double *lhsAng, double *lhsCross, double *rhsLin,
+                    double *rhsAng) override { // spring.js:509-553
+    (void)alpha;
+    (void)lhsCross;
+    if (broken) return;
+    const double Cv = evaluate();
+    if (Cv != Cv) return;
+    const bool isA = body == bodyA;
+    const double k = penalty;
+    const double f = k * Cv;
+    double jLin[3], jAng[3], m0[9];
+    if (isA) {
+      q_rotate(rW, bodyA->positionAng, rA);
+      v3_copy(jLin, n);
+      v3_cross(jAng, rW, n);
+    } else {
+      q_rotate(rW, bodyB->positionAng, rB);
+      v3_negate(jLin, n);
+      v3_cross(jAng, rW, n);
+      v3_negate(jAng, jAng);
+    }
+    m3_outer(m0, jLin, jLin); m3_scale(m0, m0, k); m3_add_into(lhsLin, m0);
+    m3_outer(m0, jAng, jAng); m3_scale(m0, m0, k); m3_add_into(lhsAng, m0);
+    m3_outer(m0, jAng, jLin); m3_scale(m0, m0, k); m3_add_into(lhsCross, m0);
+    v3_add_scaled(rhsLin, jLin, f);
+    v3_add_scaled(rhsAng, jAng, f);
+    if (geometricEnabled()) stampGeometricStiffness(isA, f, lhsLin, lhsAng);
+    C = Cv;
+  }
+  void stampGeometricStiffness(bool isA, double f, double *lhsLin, double *lhsAng) { // spring.js:564-616
+    const double dLen = v3_len(d);
+    const double s = isA ? 1 : -1;
+    double P[9], S[9], Gll[9], Gla[9], Gal[9], Gaa[9], m0[9];
+    m3_outer(P, n, n);
+    m3_negate(P, P);
+    P[0] += 1; P[4] += 1; P[8] += 1;
+    m3_div(P, P, dLen);
+    m3_skew(S, rW);
+    m3_copy(Gll, P);
+    m3_mul(Gla, P, S);
+    m3_negate(Gla, Gla);
+    m3_mul(Gal, S, P);
+    m3_mul(Gaa, S, P);
+    m3_mul(Gaa, Gaa, S);
+    m3_negate(Gaa, Gaa);
+    const double ndotr = v3_dot(n, rW);
+    m3_outer(m0, rW, n);
+    m0[0] -= ndotr; m0[4] -= ndotr; m0[8] -= ndotr;
+    m3_scale(m0, m0, s);
+    m3_add_into(Gaa, m0);
+    const double af = std::fabs(f);
+    for (int c = 0; c < 3; c++) {
+      const double a0 = Gll[c], a1 = Gll[3 + c], a2 = Gll[6 + c];
+      const double a3 = Gal[c], a4 = Gal[3 + c], a5 = Gal[6 + c];
+      const double g = std::sqrt(a0 * a0 + a1 * a1 + a2 * a2 + a3 * a3 + a4 * a4 + a5 * a5) * af;
+      lhsLin[c * 3 + c] += g;
+    }
+    for (int c = 0; c < 3; c++) {
+      const double a0 = Gla[c], a1 = Gla[3 + c], a2 = Gla[6 + c];
+      const double a3 = Gaa[c], a4 = Gaa[3 + c], a5 = Gaa[6 + c];
+      const double g = std::sqrt(a0 * a0 + a1 * a1 + a2 * a2 + a3 * a3 + a4 * a4 + a5 * a5) * af;
+      lhsAng[c * 3 + c] += g;
+    }
+  }
+  void updateDual(double alpha) override { // spring.js:618-634
+    (void)alpha;
+    if (broken) return;
+    const double Cv = evaluate();
+    if (Cv != Cv) return;
+    C = Cv;
+    if (is_finite(tearStrain) && updateTearing(Cv)) return;
+    if (!rampEnabled()) return;
+    const Params &P = solver->p;
+    penalty = js_min(penalty + P.betaLin * std::fabs(Cv), js_min(stiffness, P.penaltyMax));
+  }
+  double maxLambda() const override { return broken ? 0 : std::fabs(penalty * C); }
+  double maxPenalty() const override { return broken ? 0 : penalty; }
+  double maxConstraintError() const override { return broken ? 0 : std::fabs(C); }
+};
+
+Solver::~Solver() {
+  for (Body *b : bodies) delete b;
+  for (Force *f : forces) delete f;
+  for (Force *f : graveyard) delete f;
+}
+
+// ---------------------------------------------------------------------------
+// Broad phase (src/physics/broadphase.js)
+// ---------------------------------------------------------------------------
+static inline uint32_t hash_cell(int64_t x, int64_t y, int64_t z) { // broadphase.js:231-233
+  const uint32_t hx = (uint32_t)(x * 73856093LL), hy = (uint32_t)(y * 19349663LL), hz = (uint32_t)(z * 83492791LL);
+  return hx ^ hy ^ hz;
+}
+
+template <class Visit>
+static void for_each_pair_hash(const std::vector<Body *> &bodies, Visit &&visit) { // broadphase.js:47-215
+  const int n = (int)bodies.size();
+  if (n < 2) return;
+  double radiusSum = 0;
+  for (int i = 0; i < n; i++) radiusSum += bodies[i]->radius;
+  const double meanRadius = radiusSum / n;
+  const double largeThreshold = js_max(meanRadius * 8, 1e-6);
+  const double inv = 1 / js_max(meanRadius * 2, 1e-4);
+  std::vector<int32_t> large;
+  int64_t insertions = 0;
+  for (int i = 0; i < n; i++) {
+    const Body &b = *bodies[i];
+    if (b.radius > largeThreshold) { large.push_back(i); continue; }
+    const double r = b.radius;
+    const double *p = b.positionLin;
+    const int64_t nx = (int64_t)std::floor((p[0] + r) * inv) - (int64_t)std::floor((p[0] - r) * inv) + 1;
+    const int64_t ny = (int64_t)std::floor((p[1] + r) * inv) - (int64_t)std::floor((p[1] - r) * inv) + 1;
+    const int64_t nz = (int64_t)std::floor((p[2] + r) * inv) - (int64_t)std::floor((p[2] - r) * inv) + 1;
+    insertions += nx * ny * nz;
+  }
+  int64_t tableSize = 64;
+  while (tableSize < insertions * 2) tableSize *= 2;
+  const uint32_t mask = (uint32_t)(tableSize - 1);
+  std::vector<int32_t> counts(tableSize, 0), starts(tableSize, 0), scatter(tableSize, 0);
+  std::vector<int32_t> entries(std::max<int64_t>(insertions, 1));
+  std::vector<int32_t> lastSeen(n, -1);
+  auto cell_range = [&](const Body &b, int64_t *lo, int64_t *hi) {
+    const double r = b.radius;
+    const double *p = b.positionLin;
+    for (int a = 0; a < 3; a++) {
+      lo[a] = (int64_t)std::floor((p[a] - r) * inv);
+      hi[a] = (int64_t)std::floor((p[a] + r) * inv);
+    }
+  };
+  for (int i = 0; i < n; i++) {
+    const Body &b = *bodies[i];
+    if (b.radius > largeThreshold) continue;
+    int64_t lo[3], hi[3];
+    cell_range(b, lo, hi);
+    for (int64_t x = lo[0]; x <= hi[0]; x++)
+      for (int64_t y = lo[1]; y <= hi[1]; y++)
+        for (int64_t z = lo[2]; z <= hi[2]; z++) counts[hash_cell(x, y, z) & mask]++;
+  }
+  int32_t running = 0;
+  for (int64_t c = 0; c < tableSize; c++) {
+    starts[c] = running;
+    scatter[c] = running;
+    running += counts[c];
+  }
+  for (int i = 0; i < n; i++) {
+    const Body &b = *bodies[i];
+    if (b.radius > largeThreshold) continue;
+    int64_t lo[3], hi[3];
+    cell_range(b, lo, hi);
+    for (int64_t x = lo[0]; x <= hi[0]; x++)
+      for (int64_t y = lo[1]; y <= hi[1]; y++)
+        for (int64_t z = lo[2]; z <= hi[2]; z++) entries[scatter[hash_cell(x, y, z) & mask]++] = i;
+  }
+  std::vector<int32_t> candidates;
+  candidates.reserve(256);
+  for (int i = n - 1; i >= 1; i--) {
+    Body *bodyA = bodies[i];
+    if (bodyA->radius > largeThreshold) {
+      for (int j = i - 1; j >= 0; j--) visit(bodyA, bodies[j]);
+      continue;
+    }
+    candidates.clear();
+    for (int32_t j : large) {
+      if (j < i && lastSeen[j] != i) { lastSeen[j] = i; candidates.push_back(j); }
+    }
+    int64_t lo[3], hi[3];
+    cell_range(*bodyA, lo, hi);
+    for (int64_t x = lo[0]; x <= hi[0]; x++)
+      for (int64_t y = lo[1]; y <= hi[1]; y++)
+        for (int64_t z = lo[2]; z <= hi[2]; z++) {
+          const uint32_t b = hash_cell(x, y, z) & mask;
+          const int32_t start = starts[b], end = start + counts[b];
+          for (int32_t k = start; k < end; k++) {
+            const int32_t j = entries[k];
+            if (j < i && lastSeen[j] != i) { lastSeen[j] = i; candidates.push_back(j); }
+          }
+        }
+    // descending index order (the reference uses an insertion sort)
+    std::sort(candidates.begin(), candidates.end(), [](int32_t a, int32_t b) { return a > b; });
+    for (int32_t j : candidates) visit(bodyA, bodies[j]);
+  }
+}
+
+template <class Visit>
+static void for_each_pair_brute(const std::vector<Body *> &bodies, Visit &&visit) { // broadphase.js:236-243
+  for (int i = (int)bodies.size() - 1; i >= 1; i--)
+    for (int j = i - 1; j >= 0; j--) visit(bodies[i], bodies[j]);
+}
+
+// ---------------------------------------------------------------------------
+// Colouring
+// ---------------------------------------------------------------------------
+// Dynamic-dynamic edges of the current force list (after force init).
+static void constraint_edges(const Solver &s, std::vector<std::vector<int32_t>> &adj) {
+  const int n = (int)s.bodies.size();
+  adj.assign(n, {});
+  for (const Force *f : s.forces) {
+    if (!f->bodyA || !f->bodyB) continue;
+    if (f->isBroken()) continue;
+    if (f->bodyA->mass <= 0 || f->bodyB->mass <= 0) continue;
+    adj[f->bodyA->index].push_back(f->bodyB->index);
+    adj[f->bodyB->index].push_back(f->bodyA->index);
+  }
+}
+
+// Greedy colouring in integer-priority order: a body takes the smallest colour
+// not used by its neighbours that precede it in (lowbias32(local index), index)
+// order. Statics get -1. This is the fixed point of the reference GPU's Jacobi
+// colouring (src/physics/gpu/shaders.js:1558-1656).
+static int priority_coloring(const Solver &s, std::vector<int32_t> &colorOf) {
+  const int n = (int)s.bodies.size();
+  std::vector<std::vector<int32_t>> adj;
+  constraint_edges(s, adj);
+  std::vector<int32_t> order;
+  order.reserve(n);
+  for (int i = 0; i < n; i++)
+    if (s.bodies[i]->mass > 0) order.push_back(i);
+  std::sort(order.begin(), order.end(), [](int32_t a, int32_t b) {
+    const uint32_t pa = color_priority((uint32_t)a), pb = color_priority((uint32_t)b);
+    return pa < pb || (pa == pb && a < b);
+  });
+  colorOf.assign(n, -1);
+  int numColors = 0;
+  std::vector<int32_t> usedStamp(n + 1, -1);
+  int stamp = 0;
+  for (int32_t i : order) {
+    stamp++;
+    for (int32_t j : adj[i]) {
+      const int32_t c = colorOf[j];
+      if (c >= 0) usedStamp[c] = stamp;
+    }
+    int c = 0;
+    while (c < numColors && usedStamp[c] == stamp) c++;
+    if (c == numColors) numColors++;
+    colorOf[i] = c;
+  }
+  return numColors;
+}
+
+// Coloring.build (src/physics/coloring.js:43-118): greedy in index order.
+static int index_coloring(const Solver &s, std::vector<int32_t> &colorOf) {
+  const int n = (int)s.bodies.size();
+  std::vector<std::vector<int32_t>> adj(n);
+  for (const Force *f : s.forces) {
+    if (!f->bodyA || !f->bodyB) continue;
+    adj[f->bodyA->index].push_back(f->bodyB->index);
+    adj[f->bodyB->index].push_back(f->bodyA->index);
+  }
+  colorOf.assign(n, -1);
+  std::vector<int32_t> used(n + 1, -1);
+  int stamp = 0, numColors = 0;
+  for (int i = 0; i < n; i++) {
+    if (s.bodies[i]->mass <= 0) continue;
+    stamp++;
+    for (int32_t j : adj[i]) {
+      const int32_t c = colorOf[j];
+      if (c >= 0) used[c] = stamp;
+    }
+    int c = 0;
+    while (c < numColors && used[c] == stamp) c++;
+    if (c == numColors) numColors++;
+    colorOf[i] = c;
+  }
+  return numColors;
+}
+
+// ---------------------------------------------------------------------------
+// Algorithm 1 (src/physics/solver.js:307-493)
+// ---------------------------------------------------------------------------
+static void step(Solver &s) {
+  const double dt = s.p.dt;
+  std::vector<Body *> &bodies = s.bodies;
+  const Params &P = s.p;
+
+  // 1. broad phase
+  std::vector<Force *> created;
+  auto visit = [&](Body *A, Body *B) {
+    const double dx = A->positionLin[0] - B->positionLin[0];
+    const double dy = A->positionLin[1] - B->positionLin[1];
+    const double dz = A->positionLin[2] - B->positionLin[2];
+    const double r = A->radius + B->radius;
+    if (dx * dx + dy * dy + dz * dz <= r * r && !A->constrainedTo(B)) {
+      if (A->mass > 0 || B->mass > 0) {
+        Manifold *m = new Manifold();
+        m->solver = &s;
+        m->bodyA = A;
+        m->bodyB = B;
+        s.forces.push_back(m);
+        A->forces.push_back(m);
+        B->forces.push_back(m);
+      }
+    }
+  };
+  const bool useHash = P.broadphase == 1 || (P.broadphase == 0 && (int)bodies.size() > P.hashThreshold);
+  if (useHash) for_each_pair_hash(bodies, visit);
+  else for_each_pair_brute(bodies, visit);
+
+  s.lastPairs.clear();
+  for (Force *f : s.forces)
+    if (f->kind == KIND_MANIFOLD)
+      s.lastPairs.push_back(((int64_t)f->bodyA->index << 32) | (int64_t)f->bodyB->index);
+  std::sort(s.lastPairs.begin(), s.lastPairs.end());
+
+  // 2. force initialisation and warm start
+  {
+    std::vector<Force *> &forces = s.forces;
+    size_t write = 0;
+    for (size_t i = 0; i < forces.size(); i++) {
+      Force *f = forces[i];
+      if (f->initialize()) {
+        forces[write++] = f;
+      } else {
+        for (Body *b : {f->bodyA, f->bodyB}) {
+          if (!b) continue;
+          auto it = std::find(b->forces.begin(), b->forces.end(), f);
+          if (it != b->forces.end()) b->forces.erase(it);
+        }
+        s.graveyard.push_back(f);
+      }
+    }
+    forces.resize(write);
+  }
+
+  // 3. body initialisation (Eq. 2 + adaptive guess)
+  double gravityVec[3] = {0, 0, P.gravity};
+  for (Body *b : bodies) {
+    double tmp[3];
+    v3_copy(b->inertialLin, b->positionLin);
+    v3_add_scaled(b->inertialLin, b->velocityLin, dt);
+    if (b->mass > 0) v3_add_scaled(b->inertialLin, gravityVec, dt * dt);
+    v3_scale(tmp, b->velocityAng, dt);
+    q_integrate(b->inertialAng, b->positionAng, tmp);
+    const double accelZ = (b->velocityLin[2] - b->prevVelocityLin[2]) / dt;
+    const double accelExt = accelZ * sign(P.gravity);
+    double accelWeight = clamp(accelExt / std::fabs(P.gravity), 0.0, 1.0);
+    if (!is_finite(accelWeight)) accelWeight = 0.0;
+    v3_copy(b->initialLin, b->positionLin);
+    q_copy(b->initialAng, b->positionAng);
+    if (b->mass > 0) {
+      v3_add_scaled(b->positionLin, b->velocityLin, dt);
+      v3_add_scaled(b->positionLin, gravityVec, accelWeight * dt * dt);
+      v3_scale(tmp, b->velocityAng, dt);
+      q_integrate(b->positionAng, b->positionAng, tmp);
+    }
+  }
+
+  // visit order of the primal sweep
+  std::vector<int32_t> order;
+  const std::vector<int32_t> *orderPtr = nullptr;
+  if (P.bodyOrderMode == AVBD_ORDER_EXPLICIT && !s.bodyOrder.empty()) {
+    orderPtr = &s.bodyOrder;
+  } else if (P.bodyOrderMode == AVBD_ORDER_PRIORITY) {
+    s.lastNumColors = priority_coloring(s, s.lastColorOf);
+    for (int c = 0; c < s.lastNumColors; c++)
+      for (int i = 0; i < (int)bodies.size(); i++)
+        if (s.lastColorOf[i] == c) order.push_back(i);
+    orderPtr = &order;
+  }
+
+  // 4. main loop
+  const double dt2 = dt * dt;
+  const int totalIterations = P.iterations + (P.postStabilize ? 1 : 0);
+  std::vector<Force *> &forces = s.forces;
+  for (int it = 0; it < totalIterations; it++) {
+    const double alpha = P.postStabilize ? (it < P.iterations ? 1.0 : 0.0) : P.alpha;
+    const int sweep = orderPtr ? (int)orderPtr->size() : (int)bodies.size();
+    for (int si = 0; si < sweep; si++) {
+      Body *b = orderPtr ? bodies[(*orderPtr)[si]] : bodies[bodies.size() - 1 - si];
+      if (b->mass <= 0) continue;
+      double MLin[9], MAng[9], lhsLin[9], lhsAng[9], lhsCross[9], rhsLin[3], rhsAng[3], tmp[3], dq[3], dxLin[3],
+          dxAng[3];
+      m3_diagonal(MLin, b->mass, b->mass, b->mass);
+      b->computeWorldMoment(MAng, P.rotatedInertia);
+      m3_div(lhsLin, MLin, dt2);
+      m3_div(lhsAng, MAng, dt2);
+      m3_zero(lhsCross);
+      v3_sub(tmp, b->positionLin, b->inertialLin);
+      m3_mul_vec(rhsLin, lhsLin, tmp);
+      q_subtract(dq, b->positionAng, b->inertialAng);
+      m3_mul_vec(rhsAng, lhsAng, dq);
+      for (int k = (int)b->forces.size() - 1; k >= 0; k--)
+        b->forces[k]->updatePrimal(b, alpha, lhsLin, lhsAng, lhsCross, rhsLin, rhsAng);
+      v3_negate(rhsLin, rhsLin);
+      v3_negate(rhsAng, rhsAng);
+      solve6(lhsLin, lhsAng, lhsCross, rhsLin, rhsAng, dxLin, dxAng);
+      v3_add(b->positionLin, b->positionLin, dxLin);
+      q_integrate(b->positionAng, b->positionAng, dxAng);
+    }
+    if (it < P.iterations)
+      for (int i = (int)forces.size() - 1; i >= 0; i--) forces[i]->updateDual(alpha);
+    if (it == P.iterations - 1) {
+      for (Body *b : bodies) {
+        v3_copy(b->prevVelocityLin, b->velocityLin);
+        if (b->mass > 0) {
+          v3_sub(b->velocityLin, b->positionLin, b->initialLin);
+          v3_div(b->velocityLin, b->velocityLin, dt);
+          q_subtract(b->velocityAng, b->positionAng, b->initialAng);
+          v3_div(b->velocityAng, b->velocityAng, dt);
+        }
+      }
+    }
+  }
+}
+
+} // namespace orc
+
+// ===========================================================================
+// C ABI for the tests (ctypes). Shares avbd_world with the CUDA backend.
+// ===========================================================================
+using namespace orc;
+
+struct orc_solver {
+  Solver s;
+  std::string err;
+};
+
+static void params_from(Params &p, const avbd_params *a) {
+  p.dt = a->dt; p.gravity = a->gravity; p.iterations = a->iterations; p.postStabilize = a->post_stabilize != 0;
+  p.betaLin = a->beta_lin; p.betaAng = a->beta_ang; p.alpha = a->alpha; p.gamma = a->gamma;
+  p.penaltyMin = a->penalty_min; p.penaltyMax = a->penalty_max; p.collisionMargin = a->collision_margin;
+  p.stickThreshold = a->stick_threshold; p.rotatedInertia = a->rotated_inertia != 0;
+  p.springRamp = a->spring_stiffness_ramp != 0; p.springGeometric = a->spring_geometric_stiffness != 0;
+  p.cachedJacobians = a->cached_contact_jacobians != 0; p.broadphase = a->broadphase;
+  p.hashThreshold = a->hash_threshold; p.bodyOrderMode = a->body_order;
+}
+
+extern "C" {
+
+void orc_default_params(avbd_params *o) {
+  std::memset(o, 0, sizeof(*o));
+  o->dt = 1.0 / 60.0; o->gravity = -10.0; o->iterations = 10; o->post_stabilize = 0;
+  o->beta_lin = 1e4; o->beta_ang = 100; o->alpha = 0.95; o->gamma = 0.999;
+  o->penalty_min = 1; o->penalty_max = 1e10; o->collision_margin = 0.01; o->stick_threshold = 1e-5;
+  o->rotated_inertia = 1; o->spring_stiffness_ramp = 0; o->spring_geometric_stiffness = 1;
+  o->cached_contact_jacobians = 1; o->broadphase = 0; o->hash_threshold = 150;
+  o->body_order = AVBD_ORDER_REFERENCE; o->fp64_ratio_threshold = 0;
+}
+
+orc_solver *orc_create(const avbd_params *params) {
+  orc_solver *o = new orc_solver();
+  params_from(o->s.p, params);
+  return o;
+}
+
+void orc_destroy(orc_solver *o) { delete o; }
+
+int orc_set_params(orc_solver *o, const avbd_params *params) {
+  params_from(o->s.p, params);
+  return AVBD_OK;
+}
+
+const char *orc_last_error(const orc_solver *o) { return o ? o->err.c_str() : ""; }
+
+static void load_manifolds(orc_solver *o, const avbd_manifold_soa &M, std::vector<std::pair<int, Force *>> &ordered,
+                           int base) {
+  Solver &s = o->s;
+  for (int m = 0; m < M.count; m++) {
+    Manifold *f = new Manifold();
+    f->solver = &s;
+    f->bodyA = s.bodies[M.body_a[m]];
+    f->bodyB = s.bodies[M.body_b[m]];
+    f->numContacts = M.num_contacts[m];
+    if (M.basis) for (int k = 0; k < 9; k++) f->basis[k] = M.basis[m * 9 + k];
+    f->friction = M.friction ? M.friction[m] : 0;
+    for (int i = 0; i < MAX_CONTACTS; i++) {
+      Contact &c = f->contacts[i];
+      const int slot = m * MAX_CONTACTS + i;
+      c.feature = M.feature ? M.feature[slot] : 0;
+      for (int k = 0; k < 3; k++) {
+        c.rA[k] = M.r_a ? M.r_a[slot * 3 + k] : 0;
+        c.rB[k] = M.r_b ? M.r_b[slot * 3 + k] : 0;
+        c.penalty[k] = M.penalty ? M.penalty[slot * 3 + k] : 0;
+        c.lambda[k] = M.lambda ? M.lambda[slot * 3 + k] : 0;
+        c.C0[k] = M.c0 ? M.c0[slot * 3 + k] : 0;
+      }
+      c.stick = M.stick ? M.stick[slot] != 0 : false;
+    }
+    ordered.push_back({M.order ? M.order[m] : base + m, f});
+  }
+}
+
+// Build the scene graph. Forces are ordered by their `order` fields when given,
+// else joints, then springs, then manifolds, each in array order.
+int orc_load(orc_solver *o, const avbd_world *w) {
+  Solver &s = o->s;
+  for (Body *b : s.bodies) delete b;
+  for (Force *f : s.forces) delete f;
+  s.bodies.clear();
+  s.forces.clear();
+  const avbd_body_soa &B = w->bodies;
+  for (int i = 0; i < B.count; i++) {
+    Body *b = new Body();
+    b->index = i;
+    b->shape = B.shape ? B.shape[i] : AVBD_SHAPE_BOX;
+    for (int k = 0; k < 3; k++) {
+      b->size[k] = B.size[i * 3 + k];
+      b->moment[k] = B.moment[i * 3 + k];
+      b->positionLin[k] = B.pos[i * 3 + k];
+      b->initialLin[k] = B.pos[i * 3 + k];
+      b->velocityLin[k] = B.vel ? B.vel[i * 3 + k] : 0;
+      b->velocityAng[k] = B.omega ? B.omega[i * 3 + k] : 0;
+      b->prevVelocityLin[k] = B.prev_vel ? B.prev_vel[i * 3 + k] : b->velocityLin[k];
+    }
+    for (int k = 0; k < 4; k++) b->positionAng[k] = B.quat ? B.quat[i * 4 + k] : (k == 3 ? 1 : 0);
+    q_copy(b->initialAng, b->positionAng);
+    b->mass = B.mass[i];
+    b->radius = B.radius[i];
+    b->friction = B.friction[i];
+    s.bodies.push_back(b);
+  }
+  std::vector<std::pair<int, Force *>> ordered;
+  const avbd_joint_soa &J = w->joints;
+  for (int j = 0; j < J.count; j++) {
+    Joint *f = new Joint();
+    f->solver = &s;
+    f->id = j;
+    f->bodyA = J.body_a[j] < 0 ? nullptr : s.bodies[J.body_a[j]];
+    f->bodyB = s.bodies[J.body_b[j]];
+    for (int k = 0; k < 3; k++) {
+      f->rA[k] = J.r_a[j * 3 + k];
+      f->rB[k] = J.r_b[j * 3 + k];
+      f->penaltyLin[k] = J.penalty_lin ? J.penalty_lin[j * 3 + k] : 0;
+      f->penaltyAng[k] = J.penalty_ang ? J.penalty_ang[j * 3 + k] : 0;
+      f->lambdaLin[k] = J.lambda_lin ? J.lambda_lin[j * 3 + k] : 0;
+      f->lambdaAng[k] = J.lambda_ang ? J.lambda_ang[j * 3 + k] : 0;
+    }
+    f->stiffnessLin = J.stiffness_lin[j];
+    f->stiffnessAng = J.stiffness_ang[j];
+    f->fracture = J.fracture[j];
+    f->broken = J.broken ? J.broken[j] != 0 : false;
+    f->setup();
+    ordered.push_back({J.order ? J.order[j] : j, f});
+  }
+  const avbd_spring_soa &S = w->springs;
+  for (int j = 0; j < S.count; j++) {
+    Spring *f = new Spring();
+    f->solver = &s;
+    f->id = j;
+    f->bodyA = s.bodies[S.body_a[j]];
+    f->bodyB = s.bodies[S.body_b[j]];
+    for (int k = 0; k < 3; k++) {
+      f->rA[k] = S.r_a[j * 3 + k];
+      f->rB[k] = S.r_b[j * 3 + k];
+    }
+    f->stiffness = S.stiffness[j];
+    f->rest = S.rest[j];
+    f->tearStrain = S.tear_strain ? S.tear_strain[j] : INF;
+    f->penalty = S.penalty ? S.penalty[j] : 0;
+    f->peakStrain = S.peak_strain ? S.peak_strain[j] : 0;
+    f->broken = S.broken ? S.broken[j] != 0 : false;
+    ordered.push_back({S.order ? S.order[j] : J.count + j, f});
+  }
+  load_manifolds(o, w->manifolds, ordered, J.count + S.count);
+  std::stable_sort(ordered.begin(), ordered.end(),
+                   [](const std::pair<int, Force *> &a, const std::pair<int, Force *> &b) { return a.first < b.first; });
+  for (auto &e : ordered) {
+    Force *f = e.second;
+    s.forces.push_back(f);
+    if (f->bodyA) f->bodyA->forces.push_back(f);
+    if (f->bodyB) f->bodyB->forces.push_back(f);
+  }
+  return AVBD_OK;
+}
+
+int orc_set_body_order(orc_solver *o, const int32_t *order, int32_t n) {
+  o->s.bodyOrder.assign(order, order + n);
+  return AVBD_OK;
+}
+
+int orc_step(orc_solver *o, int32_t n) {
+  for (int i = 0; i < n; i++) step(o->s);
+  return AVBD_OK;
+}
+
+// Writes body state, joint/spring state (by id) and, when pointers are given,
+// the manifolds in force-list order (count = number of manifolds).
+int orc_read_state(orc_solver *o, avbd_world *w) {
+  Solver &s = o->s;
+  avbd_body_soa &B = w->bodies;
+  const int n = std::min<int>(B.count, (int)s.bodies.size());
+  for (int i = 0; i < n; i++) {
+    const Body *b = s.bodies[i];
+    for (int k = 0; k < 3; k++) {
+      if (B.pos) B.pos[i * 3 + k] = b->positionLin[k];
+      if (B.vel) B.vel[i * 3 + k] = b->velocityLin[k];
+      if (B.omega) B.omega[i * 3 + k] = b->velocityAng[k];
+      if (B.prev_vel) B.prev_vel[i * 3 + k] = b->prevVelocityLin[k];
+    }
+    if (B.quat) for (int k = 0; k < 4; k++) B.quat[i * 4 + k] = b->positionAng[k];
+  }
+  avbd_manifold_soa &M = w->manifolds;
+  int m = 0, pos = 0;
+  for (const Force *f : s.forces) {
+    if (f->kind == KIND_JOINT) {
+      const Joint *j = static_cast<const Joint *>(f);
+      avbd_joint_soa &J = w->joints;
+      if (j->id < J.count) {
+        for (int k = 0; k < 3; k++) {
+          if (J.penalty_lin) J.penalty_lin[j->id * 3 + k] = j->penaltyLin[k];
+          if (J.penalty_ang) J.penalty_ang[j->id * 3 + k] = j->penaltyAng[k];
+          if (J.lambda_lin) J.lambda_lin[j->id * 3 + k] = j->lambdaLin[k];
+          if (J.lambda_ang) J.lambda_ang[j->id * 3 + k] = j->lambdaAng[k];
+        }
+        if (J.broken) J.broken[j->id] = j->broken ? 1 : 0;
+        if (J.order) J.order[j->id] = pos;
+      }
+    } else if (f->kind == KIND_SPRING) {
+      const Spring *sp = static_cast<const Spring *>(f);
+      avbd_spring_soa &S = w->springs;
+      if (sp->id < S.count) {
+        if (S.penalty) S.penalty[sp->id] = sp->penalty;
+        if (S.peak_strain) S.peak_strain[sp->id] = sp->peakStrain;
+        if (S.broken) S.broken[sp->id] = sp->broken ? 1 : 0;
+        if (S.order) S.order[sp->id] = pos;
+      }
+    } else {
+      const Manifold *mf = static_cast<const Manifold *>(f);
+      if (m < M.capacity) {
+        if (M.body_a) M.body_a[m] = mf->bodyA->index;
+        if (M.body_b) M.body_b[m] = mf->bodyB->index;
+        if (M.num_contacts) M.num_contacts[m] = mf->numContacts;
+        if (M.basis) for (int k = 0; k < 9; k++) M.basis[m * 9 + k] = mf->basis[k];
+        if (M.friction) M.friction[m] = mf->friction;
+        for (int i = 0; i < MAX_CONTACTS; i++) {
+          const Contact &c = mf->contacts[i];
+          const int slot = m * MAX_CONTACTS + i;
+          if (M.feature) M.feature[slot] = i < mf->numContacts ? c.feature : 0;
+          for (int k = 0; k < 3; k++) {
+            const bool live = i < mf->numContacts;
+            if (M.r_a) M.r_a[slot * 3 + k] = live ? c.rA[k] : 0;
+            if (M.r_b) M.r_b[slot * 3 + k] = live ? c.rB[k] : 0;
+            if (M.c0) M.c0[slot * 3 + k] = live ? c.C0[k] : 0;
+            if (M.penalty) M.penalty[slot * 3 + k] = live ? c.penalty[k] : 0;
+            if (M.lambda) M.lambda[slot * 3 + k] = live ? c.lambda[k] : 0;
+          }
+          if (M.stick) M.stick[slot] = (i < mf->numContacts && c.stick) ? 1 : 0;
+        }
+        if (M.order) M.order[m] = pos;
+      }
+      m++;
+    }
+    pos++;
+  }
+  M.count = m;
+  // Broken joints left the force list (joint.js:159 returns !broken); report
+  // their final state too.
+  for (const Force *f : s.graveyard) {
+    if (f->kind != KIND_JOINT) continue;
+    const Joint *j = static_cast<const Joint *>(f);
+    avbd_joint_soa &J = w->joints;
+    if (j->id >= J.count) continue;
+    for (int k = 0; k < 3; k++) {
+      if (J.penalty_lin) J.penalty_lin[j->id * 3 + k] = j->penaltyLin[k];
+      if (J.penalty_ang) J.penalty_ang[j->id * 3 + k] = j->penaltyAng[k];
+      if (J.lambda_lin) J.lambda_lin[j->id * 3 + k] = j->lambdaLin[k];
+      if (J.lambda_ang) J.lambda_ang[j->id * 3 + k] = j->lambdaAng[k];
+    }
+    if (J.broken) J.broken[j->id] = j->broken ? 1 : 0;
+    if (J.order) J.order[j->id] = -1;
+  }
+  return AVBD_OK;
+}
+
+// Joints/springs that were removed from the force list (broken joints) keep
+// the state they had when removed; report them via this accessor.
+int orc_num_forces(orc_solver *o, int32_t *joints, int32_t *springs, int32_t *manifolds) {
+  int j = 0, sp = 0, m = 0;
+  for (const Force *f : o->s.forces) {
+    if (f->kind == KIND_JOINT) j++;
+    else if (f->kind == KIND_SPRING) sp++;
+    else m++;
+  }
+  *joints = j; *springs = sp; *manifolds = m;
+  return AVBD_OK;
+}
+
+int orc_read_coloring(orc_solver *o, int32_t *color_of, int32_t *num_colors) {
+  const Solver &s = o->s;
+  for (size_t i = 0; i < s.bodies.size(); i++) color_of[i] = i < s.lastColorOf.size() ? s.lastColorOf[i] : -1;
+  *num_colors = s.lastNumColors;
+  return AVBD_OK;
+}
+
+// Colourings of the CURRENT force list, without stepping.
+int orc_priority_coloring(orc_solver *o, int32_t *color_of, int32_t *num_colors) {
+  std::vector<int32_t> c;
+  *num_colors = priority_coloring(o->s, c);
+  std::memcpy(color_of, c.data(), c.size() * sizeof(int32_t));
+  return AVBD_OK;
+}
+int orc_index_coloring(orc_solver *o, int32_t *color_of, int32_t *num_colors) {
+  std::vector<int32_t> c;
+  *num_colors = index_coloring(o->s, c);
+  std::memcpy(color_of, c.data(), c.size() * sizeof(int32_t));
+  return AVBD_OK;
+}
+
+// Pairs whose manifolds were initialised in the last step (new and persisting),
+// sorted by (A, B); A is the higher index.
+int orc_read_pairs(orc_solver *o, int32_t *a, int32_t *b, int64_t capacity, int64_t *count) {
+  const std::vector<int64_t> &p = o->s.lastPairs;
+  *count = (int64_t)p.size();
+  for (int64_t i = 0; i < (int64_t)p.size() && i < capacity; i++) {
+    a[i] = (int32_t)(p[i] >> 32);
+    b[i] = (int32_t)(p[i] & 0xffffffff);
+  }
+  return AVBD_OK;
+}
+
+int orc_stats(orc_solver *o, avbd_stats *st) {
+  const Solver &s = o->s;
+  std::memset(st, 0, sizeof(*st));
+  st->bodies = (int64_t)s.bodies.size();
+  double maxErr = 0, maxL = 0, maxP = 0;
+  for (const Force *f : s.forces) {
+    if (f->kind == KIND_MANIFOLD) {
+      st->manifolds++;
+      st->contacts += static_cast<const Manifold *>(f)->numContacts;
+    }
+    maxErr = js_max(maxErr, f->maxConstraintError());
+    maxL = js_max(maxL, f->maxLambda());
+    maxP = js_max(maxP, f->maxPenalty());
+    if (f->kind == KIND_SPRING && static_cast<const Spring *>(f)->broken) st->springs_broken++;
+  }
+  for (const Force *f : s.graveyard)
+    if (f->kind == KIND_JOINT && static_cast<const Joint *>(f)->broken) st->joints_broken++;
+  st->candidate_pairs = (int64_t)s.lastPairs.size();
+  st->colors = s.lastNumColors;
+  st->max_constraint_error = maxErr;
+  st->max_lambda = maxL;
+  st->max_penalty = maxP;
+  return AVBD_OK;
+}
+
+// Broken joints leave the force list; read their final state here.
+int orc_read_joint(orc_solver *o, int32_t id, double *penalty_lin, double *lambda_ang, int32_t *broken) {
+  auto scan = [&](const std::vector<Force *> &list) -> bool {
+    for (const Force *f : list)
+      if (f->kind == KIND_JOINT && f->id == id) {
+        const Joint *j = static_cast<const Joint *>(f);
+        for (int k = 0; k < 3; k++) { penalty_lin[k] = j->penaltyLin[k]; lambda_ang[k] = j->lambdaAng[k]; }
+        *broken = j->broken ? 1 : 0;
+        return true;
+      }
+    return false;
+  };
+  if (scan(o->s.forces) || scan(o->s.graveyard)) return AVBD_OK;
+  return AVBD_ERR_ARG;
+}
+
+// World-space inertia of body i (rigid.js:228-247).
+int orc_world_moment(orc_solver *o, int32_t i, int32_t rotated, double *out9) {
+  o->s.bodies[i]->computeWorldMoment(out9, rotated != 0);
+  return AVBD_OK;
+}
+
+// Direct narrow-phase call on bodies a and b of the loaded scene
+// (collide.js:612): contact count, basis, features and body-local anchors.
+int orc_collide(orc_solver *o, int32_t a, int32_t b, double *basis9, uint32_t *features8, double *rA24,
+                double *rB24) {
+  Contact c[MAX_CONTACTS];
+  for (auto &x : c) x.reset();
+  double basis[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  const int n = o->s.collider.collide(*o->s.bodies[a], *o->s.bodies[b], c, basis);
+  for (int k = 0; k < 9; k++) basis9[k] = basis[k];
+  for (int i = 0; i < MAX_CONTACTS; i++) {
+    features8[i] = c[i].feature;
+    for (int k = 0; k < 3; k++) { rA24[i * 3 + k] = c[i].rA[k]; rB24[i * 3 + k] = c[i].rB[k]; }
+  }
+  return n;
+}
+
+// Math primitives, exposed for golden-vector tests of the restatement.
+void orc_solve6(const double *aLin, const double *aAng, const double *aCross, const double *bLin,
+                const double *bAng, double *xLin, double *xAng) {
+  solve6(aLin, aAng, aCross, bLin, bAng, xLin, xAng);
+}
+void orc_quat_subtract(double *out3, const double *a, const double *b) { q_subtract(out3, a, b); }
+void orc_quat_integrate(double *out4, const double *q, const double *dw) { q_integrate(out4, q, dw); }
+void orc_quat_rotate(double *out3, const double *q, const double *v) { q_rotate(out3, q, v); }
+void orc_orthonormal(double *out9, const double *n) { m3_orthonormal(out9, n); }
+uint32_t orc_color_priority(uint32_t i) { return color_priority(i); }
+
+} // extern "C"
