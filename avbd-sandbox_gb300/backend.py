@@ -1,0 +1,166 @@
+"""Host-side mirror of the reference `GpuBackend` (src/physics/gpu/backend.js:243),
+bound to the CUDA library through its C ABI (include/avbd_cuda.h).
+
+Method names follow the reference so its call sites read the same:
+  pack(world)          backend.js:662   topology + state upload
+  step(n)              backend.js:1393  asynchronous device step(s)
+  idle()               backend.js:1804  wait; raise on device-side errors
+  read_state()         backend.js:2154  body/joint/spring (+ manifold) state
+  sync_to_cpu(world)   backend.js:1984  write device state into a host world
+  write_state(world)   CPU-authoritative handover back to the device
+  read_coloring()      backend.js:2053
+  last_stats           backend.js:309
+  set_profiling(on) / last_profile      backend.js:1836-1897
+
+There is no CPU fallback: when the CUDA library is missing or no GPU is
+present, construction raises.
+"""
+from __future__ import annotations
+
+import ctypes as C
+import os
+
+import numpy as np
+
+from . import abi
+
+HERE = os.path.dirname(os.path.abspath(__file__))
+LIB_PATH = os.path.join(HERE, "libavbd_gb300.so")
+
+_lib = None
+
+
+def load_library(path: str = LIB_PATH):
+    """dlopen the CUDA backend. Raises if it has not been built."""
+    global _lib
+    if _lib is not None:
+        return _lib
+    if not os.path.exists(path):
+        raise RuntimeError(f"CUDA extension not built: {path} is missing (run __graft_entry__.build())")
+    L = C.CDLL(path)
+    vp = C.c_void_p
+    L.avbd_default_params.argtypes = [vp]
+    L.avbd_default_params.restype = None
+    L.avbd_create.argtypes = [vp, C.POINTER(vp)]
+    L.avbd_destroy.argtypes = [vp]
+    for name in ("avbd_pack", "avbd_read_state", "avbd_write_state", "avbd_read_stats", "avbd_read_profile",
+                 "avbd_kernel_launches"):
+        getattr(L, name).argtypes = [vp, vp]
+    L.avbd_step.argtypes = [vp, C.c_int32]
+    L.avbd_synchronize.argtypes = [vp]
+    L.avbd_set_profiling.argtypes = [vp, C.c_int32]
+    L.avbd_read_coloring.argtypes = [vp, vp, vp]
+    L.avbd_read_pairs.argtypes = [vp, vp, vp, C.c_int64, vp]
+    L.avbd_last_error.argtypes = [vp]
+    L.avbd_last_error.restype = C.c_char_p
+    for name in ("avbd_create", "avbd_destroy", "avbd_pack", "avbd_step", "avbd_synchronize", "avbd_read_state",
+                 "avbd_write_state", "avbd_read_coloring", "avbd_read_pairs", "avbd_read_stats",
+                 "avbd_set_profiling", "avbd_read_profile", "avbd_kernel_launches"):
+        getattr(L, name).restype = C.c_int
+    _lib = L
+    return L
+
+
+class AvbdError(RuntimeError):
+    def __init__(self, code, msg):
+        super().__init__(f"avbd error {code}: {msg}")
+        self.code = code
+
+
+class GpuBackend:
+    def __init__(self, params: abi.Params | None = None, **overrides):
+        self.L = load_library()
+        if params is None:
+            params = abi.Params()
+            self.L.avbd_default_params(C.byref(params))
+        for k, v in overrides.items():
+            setattr(params, k, v)
+        self.params = params
+        h = C.c_void_p()
+        rc = self.L.avbd_create(C.byref(params), C.byref(h))
+        if rc != abi.AVBD_OK:
+            raise AvbdError(rc, self.L.avbd_last_error(None).decode())
+        self.h = h
+        self.world = None
+
+    def _check(self, rc):
+        if rc != abi.AVBD_OK:
+            raise AvbdError(rc, self.L.avbd_last_error(self.h).decode())
+
+    def destroy(self):
+        if getattr(self, "h", None):
+            self.L.avbd_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.destroy()
+        except Exception:
+            pass
+
+    # --- reference interface -------------------------------------------------
+    def pack(self, world: abi.World):
+        self.world = world.copy()
+        wc = self.world.c()
+        self._check(self.L.avbd_pack(self.h, C.byref(wc)))
+
+    def step(self, n: int = 1):
+        self._check(self.L.avbd_step(self.h, n))
+
+    def idle(self):
+        self._check(self.L.avbd_synchronize(self.h))
+
+    def read_state(self, manifolds: bool = False) -> abi.World:
+        w = self.world.copy()
+        if manifolds:
+            st = self.last_stats
+            w.ensure_manifold_capacity(max(int(st["manifolds"]), 1))
+        wc = w.c(with_manifolds=manifolds)
+        self._check(self.L.avbd_read_state(self.h, C.byref(wc)))
+        w.m_count = wc.manifolds.count if manifolds else 0
+        return w
+
+    def sync_to_cpu(self, world: abi.World):
+        wc = world.c(with_manifolds=False)
+        self._check(self.L.avbd_read_state(self.h, C.byref(wc)))
+
+    def write_state(self, world: abi.World):
+        wc = world.c()
+        self._check(self.L.avbd_write_state(self.h, C.byref(wc)))
+
+    def read_coloring(self):
+        n = self.world.n_bodies
+        c = np.zeros(n, np.int32)
+        k = C.c_int32()
+        self._check(self.L.avbd_read_coloring(self.h, c.ctypes.data_as(C.c_void_p), C.byref(k)))
+        return c, k.value
+
+    def read_pairs(self):
+        cnt = C.c_int64()
+        self._check(self.L.avbd_read_pairs(self.h, None, None, 0, C.byref(cnt)))
+        a = np.zeros(max(cnt.value, 1), np.int32)
+        b = np.zeros(max(cnt.value, 1), np.int32)
+        self._check(self.L.avbd_read_pairs(self.h, a.ctypes.data_as(C.c_void_p), b.ctypes.data_as(C.c_void_p),
+                                           cnt.value, C.byref(cnt)))
+        return a[:cnt.value], b[:cnt.value]
+
+    @property
+    def last_stats(self) -> dict:
+        st = abi.Stats()
+        self._check(self.L.avbd_read_stats(self.h, C.byref(st)))
+        return st.as_dict()
+
+    def set_profiling(self, on: bool):
+        self._check(self.L.avbd_set_profiling(self.h, 1 if on else 0))
+
+    @property
+    def last_profile(self) -> dict:
+        p = abi.Profile()
+        self._check(self.L.avbd_read_profile(self.h, C.byref(p)))
+        return p.as_dict()
+
+    @property
+    def kernel_launches(self) -> int:
+        v = C.c_int64()
+        self._check(self.L.avbd_kernel_launches(self.h, C.byref(v)))
+        return v.value

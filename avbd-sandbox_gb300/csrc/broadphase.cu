@@ -1,0 +1,344 @@
+// broadphase.cu - candidate pairs of one step, in pair-key order.
+//
+// Semantics (src/physics/solver.js:316-336, src/physics/broadphase.js:47-215):
+// a pair (A, B), A the higher body index, is a candidate when
+//   |p_A - p_B|^2 <= (r_A + r_B)^2            (f64, no FMA: this unit is built
+//                                              with --fmad=false)
+//   and not both bodies are static
+//   and no live joint or spring connects them (Rigid.constrainedTo, rigid.js:250)
+// or when the pair already holds a live manifold from the previous step.
+// Bodies of different scenes of a batch never pair.
+//
+// Structure (GB300-first rather than the reference's linked lists):
+//   1. every non-large body inserts its bounding-sphere AABB cells into a
+//      hash grid (per-scene cell = 2 x mean radius, as the reference's hash);
+//      counting sort by cell hash: count, exclusive scan, scatter
+//   2. per body A: count partners B < A (grid neighbours found once, in the
+//      minimum-corner cell of the two AABBs; large bodies of the scene; old
+//      manifold partners), exclusive scan of the counts
+//   3. per body A: write its partners into its segment and sort the segment,
+//      giving a globally sorted candidate key array without a global sort
+//   4. per candidate: index of the same pair in the previous step's manifolds
+#include <cub/cub.cuh>
+
+#include "avbd_device.cuh"
+
+namespace avbd {
+namespace {
+
+__device__ __forceinline__ uint32_t cell_hash(int x, int y, int z, int scene) {
+  uint32_t h = (uint32_t)x * 73856093u ^ (uint32_t)y * 19349663u ^ (uint32_t)z * 83492791u;
+  h ^= (uint32_t)scene * 2654435761u;
+  h ^= h >> 15;
+  h *= 0x2c1b3c6du;
+  h ^= h >> 12;
+  return h;
+}
+
+__device__ __forceinline__ bool is_large(const World &w, int i) { return (w.b.flags0[i] & kBodyLarge) != 0; }
+
+// The `visit` predicate of solver.js:316-329 for A = bodies[a], B = bodies[b], b < a.
+__device__ bool accept(const World &w, int a, int b) {
+  const double ma = w.b.massD[a].x, mb = w.b.massD[b].x;
+  if (!(ma > 0 || mb > 0)) return false;
+  const D4 pa = w.b.pos[a], pb = w.b.pos[b];
+  const double dx = pa.x - pb.x, dy = pa.y - pb.y, dz = pa.z - pb.z;
+  const double r = w.b.size[a].w + w.b.size[b].w;
+  if (!(dx * dx + dy * dy + dz * dz <= r * r)) return false;
+  // constrainedTo: a live joint or spring between them
+  for (int k = w.g.cStart[a]; k < w.g.cStart[a + 1]; k++) {
+    const uint32_t ref = w.g.cRef[k];
+    const uint32_t type = ref >> 30, idx = (ref >> 1) & 0x1fffffffu;
+    int2 ab;
+    int st;
+    if (type == kRefJoint) {
+      ab = w.j.bodies[idx];
+      st = w.j.state[idx];
+    } else {
+      ab = w.s.bodies[idx];
+      st = w.s.state[idx];
+    }
+    if (st != 0) continue;
+    if ((ab.x == a && ab.y == b) || (ab.x == b && ab.y == a)) return false;
+  }
+  return true;
+}
+
+// Cell range of body i's padded bounding-sphere AABB. The extent is bounded
+// (kMaxSpan cells per axis) so that no loop over cells can run away; a body
+// that needs more, or has a non-finite position, gets an empty range and
+// raises an error flag instead.
+constexpr int kMaxSpan = 64;
+__device__ void cell_range(const World &w, int i, int4 &lo, int4 &hi) {
+  const int s = w.b.scene[i];
+  const double inv = w.g.invCell[s];
+  const D4 p = w.b.pos[i];
+  // The grid only has to return a superset of the accepted pairs: pad the
+  // bounding sphere so rounding in the cell arithmetic can never drop one.
+  const double r = w.b.size[i].w * (1.0 + 1e-7) + 1e-9;
+  const double v[6] = {(p.x - r) * inv, (p.y - r) * inv, (p.z - r) * inv,
+                       (p.x + r) * inv, (p.y + r) * inv, (p.z + r) * inv};
+  bool ok = true;
+  for (int k = 0; k < 6; k++) ok = ok && isfinite(v[k]) && fabs(v[k]) < 1.0e9;
+  if (ok) {
+    lo = make_int4((int)floor(v[0]), (int)floor(v[1]), (int)floor(v[2]), s);
+    hi = make_int4((int)floor(v[3]), (int)floor(v[4]), (int)floor(v[5]), s);
+    if (hi.x - lo.x >= kMaxSpan || hi.y - lo.y >= kMaxSpan || hi.z - lo.z >= kMaxSpan) ok = false;
+  }
+  if (!ok) {
+    if (!(w.b.flags0[i] & kBodyLarge)) atomicOr(&w.ctl->flags, isfinite(p.x + p.y + p.z) ? kOvfCells : kErrNaN);
+    lo = make_int4(0, 0, 0, s);
+    hi = make_int4(-1, -1, -1, s);
+  }
+}
+
+__global__ void cells_kernel(World w) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < w.b.n; i += gridDim.x * blockDim.x) {
+    int4 lo, hi;
+    cell_range(w, i, lo, hi);
+    w.g.cellLo[i] = lo;
+    w.g.cellHi[i] = hi;
+    if (is_large(w, i)) continue;
+    for (int x = lo.x; x <= hi.x; x++)
+      for (int y = lo.y; y <= hi.y; y++)
+        for (int z = lo.z; z <= hi.z; z++) atomicAdd(&w.g.tableCount[cell_hash(x, y, z, lo.w) & w.g.tableMask], 1);
+  }
+}
+
+__global__ void scatter_kernel(World w) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < w.b.n; i += gridDim.x * blockDim.x) {
+    if (is_large(w, i)) continue;
+    const int4 lo = w.g.cellLo[i], hi = w.g.cellHi[i];
+    for (int x = lo.x; x <= hi.x; x++)
+      for (int y = lo.y; y <= hi.y; y++)
+        for (int z = lo.z; z <= hi.z; z++) {
+          const int at = atomicAdd(&w.g.tableCursor[cell_hash(x, y, z, lo.w) & w.g.tableMask], 1);
+          if (at < w.g.entryCap) w.g.entries[at] = i;
+          else atomicOr(&w.ctl->flags, kOvfCells);
+        }
+  }
+}
+
+// Range of body a's manifolds in the previous step (keys sorted, A-major).
+__device__ void prev_range(const World &w, int a, int prevCount, int &first, int &last) {
+  const uint64_t lo = (uint64_t)(uint32_t)a << 32;
+  int l = 0, h = prevCount;
+  while (l < h) {
+    const int m = (l + h) >> 1;
+    if (w.prev.key[m] < lo) l = m + 1;
+    else h = m;
+  }
+  first = l;
+  last = l;
+  while (last < prevCount && (int)(w.prev.key[last] >> 32) == a) last++;
+}
+
+// Enumerate the candidate partners b < a of a non-large body a, calling f(b).
+template <class F>
+__device__ void partners_small(const World &w, int a, int prevCount, F &&f) {
+  const int4 lo = w.g.cellLo[a], hi = w.g.cellHi[a];
+  const int s = lo.w;
+  for (int k = w.g.largeStart[s]; k < w.g.largeStart[s + 1]; k++) {
+    const int b = w.g.largeList[k];
+    if (b < a && accept(w, a, b)) f(b);
+  }
+  for (int x = lo.x; x <= hi.x; x++)
+    for (int y = lo.y; y <= hi.y; y++)
+      for (int z = lo.z; z <= hi.z; z++) {
+        const uint32_t bucket = cell_hash(x, y, z, s) & w.g.tableMask;
+        const int beg = w.g.tableStart[bucket];
+        int end = beg + w.g.tableCount[bucket];
+        if (end > w.g.entryCap) end = w.g.entryCap;
+        for (int k = beg; k < end; k++) {
+          const int b = w.g.entries[k];
+          if (b >= a) continue;
+          const int4 bl = w.g.cellLo[b], bh = w.g.cellHi[b];
+          if (bl.w != s) continue;
+          // the pair is found once: in the minimum corner of the AABB overlap
+          if (max(lo.x, bl.x) != x || max(lo.y, bl.y) != y || max(lo.z, bl.z) != z) continue;
+          if (x > bh.x || y > bh.y || z > bh.z) continue;
+          if (accept(w, a, b)) f(b);
+        }
+      }
+  int first, last;
+  prev_range(w, a, prevCount, first, last);
+  for (int m = first; m < last; m++) {
+    if (w.prev.count[m] <= 0) continue;
+    const int b = (int)(w.prev.key[m] & 0xffffffffu);
+    if (!accept(w, a, b)) f(b);  // accepted ones were counted above
+  }
+}
+
+__global__ void count_kernel(World w) {
+  const int prevCount = w.ctl->prevCandidates;
+  for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < w.b.n; a += gridDim.x * blockDim.x) {
+    if (is_large(w, a)) continue;  // large_count_kernel
+    int c = 0;
+    partners_small(w, a, prevCount, [&](int) { c++; });
+    w.g.pairCount[a] = c;
+  }
+}
+
+// One block per large body: every body b < a of its scene is tested.
+__global__ void large_count_kernel(World w, int numLarge) {
+  const int prevCount = w.ctl->prevCandidates;
+  for (int li = blockIdx.x; li < numLarge; li += gridDim.x) {
+    const int a = w.g.largeList[li];
+    const int s = w.g.cellLo[a].w;
+    int c = 0;
+    for (int b = w.g.sceneStart[s] + threadIdx.x; b < a; b += blockDim.x) c += accept(w, a, b) ? 1 : 0;
+    typedef cub::BlockReduce<int, 256> R;
+    __shared__ typename R::TempStorage tmp;
+    int total = R(tmp).Sum(c);
+    if (threadIdx.x == 0) {
+      int first, last;
+      prev_range(w, a, prevCount, first, last);
+      for (int m = first; m < last; m++)
+        if (w.prev.count[m] > 0 && !accept(w, a, (int)(w.prev.key[m] & 0xffffffffu))) total++;
+      w.g.pairCount[a] = total;
+    }
+    __syncthreads();
+  }
+}
+
+__device__ void sort_segment(uint64_t *k, int n) {
+  for (int i = 1; i < n; i++) {
+    const uint64_t v = k[i];
+    int j = i - 1;
+    while (j >= 0 && k[j] > v) {
+      k[j + 1] = k[j];
+      j--;
+    }
+    k[j + 1] = v;
+  }
+}
+
+__global__ void write_kernel(World w) {
+  const int prevCount = w.ctl->prevCandidates;
+  const int cap = w.g.candCap;
+  for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < w.b.n; a += gridDim.x * blockDim.x) {
+    if (is_large(w, a)) continue;
+    const int beg = w.g.pairStart[a];
+    const int n = w.g.pairStart[a + 1] - beg;
+    if (beg + n > cap) {
+      atomicOr(&w.ctl->flags, kOvfPairs);
+      continue;
+    }
+    int c = 0;
+    uint64_t *seg = w.g.candKey + beg;
+    const uint64_t hiKey = (uint64_t)(uint32_t)a << 32;
+    partners_small(w, a, prevCount, [&](int b) {
+      if (c < n) seg[c] = hiKey | (uint32_t)b;
+      c++;
+    });
+    sort_segment(seg, n);
+  }
+}
+
+__global__ void large_write_kernel(World w, int numLarge) {
+  const int prevCount = w.ctl->prevCandidates;
+  const int cap = w.g.candCap;
+  typedef cub::BlockScan<int, 256> S;
+  __shared__ typename S::TempStorage tmp;
+  __shared__ int base;
+  for (int li = blockIdx.x; li < numLarge; li += gridDim.x) {
+    const int a = w.g.largeList[li];
+    const int s = w.g.cellLo[a].w;
+    const int beg = w.g.pairStart[a];
+    const int n = w.g.pairStart[a + 1] - beg;
+    if (beg + n > cap) {
+      if (threadIdx.x == 0) atomicOr(&w.ctl->flags, kOvfPairs);
+      continue;
+    }
+    uint64_t *seg = w.g.candKey + beg;
+    const uint64_t hiKey = (uint64_t)(uint32_t)a << 32;
+    if (threadIdx.x == 0) base = 0;
+    __syncthreads();
+    const int s0 = w.g.sceneStart[s];
+    for (int b0 = s0; b0 < a; b0 += blockDim.x) {
+      const int b = b0 + threadIdx.x;
+      const int ok = (b < a && accept(w, a, b)) ? 1 : 0;
+      int pos, tot;
+      S(tmp).ExclusiveSum(ok, pos, tot);
+      if (ok && base + pos < n) seg[base + pos] = hiKey | (uint32_t)b;
+      __syncthreads();
+      if (threadIdx.x == 0) base += tot;
+      __syncthreads();
+    }
+    if (threadIdx.x == 0) {
+      int c = base;
+      int first, last;
+      prev_range(w, a, prevCount, first, last);
+      bool extra = false;
+      for (int m = first; m < last; m++) {
+        const int b = (int)(w.prev.key[m] & 0xffffffffu);
+        if (w.prev.count[m] > 0 && !accept(w, a, b)) {
+          if (c < n) seg[c] = hiKey | (uint32_t)b;
+          c++;
+          extra = true;
+        }
+      }
+      if (extra) sort_segment(seg, n);
+    }
+    __syncthreads();
+  }
+}
+
+__global__ void finish_kernel(World w) {
+  int total = w.g.pairStart[w.b.n];
+  if (total > w.g.candCap) {
+    atomicOr(&w.ctl->flags, kOvfPairs);
+    total = w.g.candCap;
+  }
+  w.ctl->numCandidates = total;
+}
+
+__global__ void prev_index_kernel(World w) {
+  const int total = w.ctl->numCandidates;
+  const int prevCount = w.ctl->prevCandidates;
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < total; c += gridDim.x * blockDim.x) {
+    const uint64_t k = w.g.candKey[c];
+    int l = 0, h = prevCount;
+    while (l < h) {
+      const int m = (l + h) >> 1;
+      if (w.prev.key[m] < k) l = m + 1;
+      else h = m;
+    }
+    w.g.candPrev[c] = (l < prevCount && w.prev.key[l] == k && w.prev.count[l] > 0) ? l : -1;
+    w.cur.key[c] = k;
+  }
+}
+
+}  // namespace
+
+size_t broadphase_temp_bytes(int n, int tableSize) {
+  size_t a = 0, b = 0;
+  cub::DeviceScan::ExclusiveSum(nullptr, a, (int *)nullptr, (int *)nullptr, tableSize);
+  cub::DeviceScan::ExclusiveSum(nullptr, b, (int *)nullptr, (int *)nullptr, n + 1);
+  return a > b ? a : b;
+}
+
+void launch_broadphase_impl(const World &w, int numLarge, void *temp, size_t tempBytes, cudaStream_t st,
+                            int smCount) {
+  const int T = (int)w.g.tableMask + 1;
+  const int n = w.b.n;
+  const int blocks = smCount * 4;
+  cudaMemsetAsync(w.g.tableCount, 0, sizeof(int) * T, st);
+  cells_kernel<<<blocks, 256, 0, st>>>(w);
+  size_t tb = tempBytes;
+  cub::DeviceScan::ExclusiveSum(temp, tb, w.g.tableCount, w.g.tableStart, T, st);
+  cudaMemcpyAsync(w.g.tableCursor, w.g.tableStart, sizeof(int) * T, cudaMemcpyDeviceToDevice, st);
+  scatter_kernel<<<blocks, 256, 0, st>>>(w);
+  // pairCount[n] = 0 so the scan over n + 1 entries yields the total at [n]
+  cudaMemsetAsync(w.g.pairCount + n, 0, sizeof(int), st);
+  count_kernel<<<blocks, 128, 0, st>>>(w);
+  if (numLarge > 0) large_count_kernel<<<numLarge < 1024 ? numLarge : 1024, 256, 0, st>>>(w, numLarge);
+  tb = tempBytes;
+  cub::DeviceScan::ExclusiveSum(temp, tb, w.g.pairCount, w.g.pairStart, n + 1, st);
+  write_kernel<<<blocks, 128, 0, st>>>(w);
+  if (numLarge > 0) large_write_kernel<<<numLarge < 1024 ? numLarge : 1024, 256, 0, st>>>(w, numLarge);
+  finish_kernel<<<1, 1, 0, st>>>(w);
+  prev_index_kernel<<<blocks, 256, 0, st>>>(w);
+}
+
+}  // namespace avbd

@@ -1,0 +1,858 @@
+// host.cu - the C ABI of include/avbd_cuda.h: context, pack, step orchestration,
+// state readback. Replaces `GpuBackend` (src/physics/gpu/backend.js:243-2226).
+//
+// One context = one CUDA stream on the current device. A step is a fixed
+// launch sequence with all sizes resident on the device (no host round trip):
+//   broadphase (hash grid + candidate keys) -> narrowphase (f64 exact) ->
+//   prepare (forces, bodies, adjacency) -> colouring (cooperative) ->
+//   solve (cooperative persistent: iterations x colours, fused dual,
+//   velocity) -> commit (x_{t+1} = x_t + delta in f64)
+// Manifold arenas are double-buffered and swapped on the host after each step.
+#include <algorithm>
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/avbd_cuda.h"
+#include "avbd_device.cuh"
+
+using namespace avbd;
+
+namespace {
+
+const char *g_create_error = "";
+std::string g_create_error_buf;
+
+struct DevBuf {
+  void *p = nullptr;
+  size_t bytes = 0;
+};
+
+}  // namespace
+
+struct avbd_ctx {
+  avbd_params params{};
+  cudaStream_t stream = nullptr;
+  int device = 0;
+  int smCount = 0;
+  std::string err;
+  bool packed = false;
+  bool profiling = false;
+  int64_t launches = 0;
+  int steps = 0;
+  std::vector<void *> allocs;
+
+  // sizes
+  int n = 0, nj = 0, ns = 0, numScenes = 1, numLarge = 0;
+  int candCap = 0, entryCap = 0, tableSize = 0, adjCap = 0, colorBlocks = 0;
+  int lanes = 8, blocksPerSm = 1;
+  size_t bpTempBytes = 0, svTempBytes = 0;
+  void *bpTemp = nullptr, *svTemp = nullptr;
+  double *statsOut = nullptr;
+  World w{};
+  Manifolds mA{}, mB{};
+  int curIsA = 1;
+  avbd_profile prof{};
+  cudaEvent_t ev[8]{};
+};
+
+namespace {
+
+int fail(avbd_ctx *c, int code, const char *fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof(buf), fmt, ap);
+  va_end(ap);
+  if (c) c->err = buf;
+  return code;
+}
+
+#define CK(call)                                                                                   \
+  do {                                                                                             \
+    cudaError_t e_ = (call);                                                                       \
+    if (e_ != cudaSuccess) return fail(ctx, AVBD_ERR_CUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
+  } while (0)
+
+template <class T>
+int dalloc(avbd_ctx *ctx, T **p, size_t count) {
+  void *q = nullptr;
+  const size_t bytes = std::max<size_t>(count, 1) * sizeof(T);
+  cudaError_t e = cudaMalloc(&q, bytes);
+  if (e != cudaSuccess) return fail(ctx, AVBD_ERR_CUDA, "cudaMalloc(%zu): %s", bytes, cudaGetErrorString(e));
+  cudaMemset(q, 0, bytes);
+  ctx->allocs.push_back(q);
+  *p = static_cast<T *>(q);
+  return AVBD_OK;
+}
+
+template <class T>
+int upload(avbd_ctx *ctx, T **p, const std::vector<T> &h) {
+  int rc = dalloc(ctx, p, h.size());
+  if (rc) return rc;
+  if (!h.empty()) CK(cudaMemcpy(*p, h.data(), h.size() * sizeof(T), cudaMemcpyHostToDevice));
+  return AVBD_OK;
+}
+
+void free_all(avbd_ctx *ctx) {
+  for (void *p : ctx->allocs) cudaFree(p);
+  ctx->allocs.clear();
+  ctx->packed = false;
+}
+
+int alloc_manifolds(avbd_ctx *ctx, Manifolds &m, int cap) {
+  int rc = 0;
+  m.cap = cap;
+  const size_t S = (size_t)cap * kMaxContacts;
+  if ((rc = dalloc(ctx, &m.key, cap)) || (rc = dalloc(ctx, &m.count, cap)) || (rc = dalloc(ctx, &m.basis0, cap)) ||
+      (rc = dalloc(ctx, &m.basis1, cap)) || (rc = dalloc(ctx, &m.basis2, cap)) ||
+      (rc = dalloc(ctx, &m.basisD, (size_t)cap * 9)) || (rc = dalloc(ctx, &m.feat, S)) ||
+      (rc = dalloc(ctx, &m.rA, S)) || (rc = dalloc(ctx, &m.rB, S)) || (rc = dalloc(ctx, &m.cA, S)) ||
+      (rc = dalloc(ctx, &m.cB, S)) || (rc = dalloc(ctx, &m.cK, S)) || (rc = dalloc(ctx, &m.cL, S)))
+    return rc;
+  return AVBD_OK;
+}
+
+inline uint32_t priority_of(uint32_t local) { return color_priority(local); }
+
+bool finite3(const double *p) { return std::isfinite(p[0]) && std::isfinite(p[1]) && std::isfinite(p[2]); }
+
+void set_world_manifolds(avbd_ctx *ctx) {
+  ctx->w.cur = ctx->curIsA ? ctx->mA : ctx->mB;
+  ctx->w.prev = ctx->curIsA ? ctx->mB : ctx->mA;
+}
+
+int record(avbd_ctx *ctx, int k) {
+  if (ctx->profiling) CK(cudaEventRecord(ctx->ev[k], ctx->stream));
+  return AVBD_OK;
+}
+
+// Upload the dynamic state (bodies, joints, springs, and manifolds when
+// given) of `world` into already-sized arenas.
+int write_state(avbd_ctx *ctx, const avbd_world *world) {
+  const avbd_body_soa &B = world->bodies;
+  const int n = ctx->n;
+  std::vector<D4> pos(n);
+  std::vector<float4> quat(n), vel(n), omg(n), pv(n);
+  for (int i = 0; i < n; i++) {
+    const double *p = &B.pos[i * 3];
+    if (!finite3(p)) return fail(ctx, AVBD_ERR_NAN, "body %d: non-finite position", i);
+    pos[i] = mkd4(p[0], p[1], p[2], 0.0);
+    const double *q = B.quat ? &B.quat[i * 4] : nullptr;
+    quat[i] = q ? make_float4((float)q[0], (float)q[1], (float)q[2], (float)q[3]) : make_float4(0, 0, 0, 1);
+    auto v3 = [&](const double *a) { return a ? make_float4((float)a[i * 3], (float)a[i * 3 + 1], (float)a[i * 3 + 2], 0.f)
+                                              : make_float4(0, 0, 0, 0); };
+    vel[i] = v3(B.vel);
+    omg[i] = v3(B.omega);
+    pv[i] = B.prev_vel ? v3(B.prev_vel) : vel[i];
+  }
+  World &w = ctx->w;
+  CK(cudaMemcpy(w.b.pos, pos.data(), n * sizeof(D4), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(w.b.quat, quat.data(), n * sizeof(float4), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(w.b.vel, vel.data(), n * sizeof(float4), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(w.b.omega, omg.data(), n * sizeof(float4), cudaMemcpyHostToDevice));
+  CK(cudaMemcpy(w.b.prevVel, pv.data(), n * sizeof(float4), cudaMemcpyHostToDevice));
+
+  const avbd_joint_soa &J = world->joints;
+  if (ctx->nj) {
+    std::vector<float4> kl(ctx->nj), ka(ctx->nj);
+    std::vector<D4> ll(ctx->nj), la(ctx->nj);
+    std::vector<int> st(ctx->nj);
+    for (int j = 0; j < ctx->nj; j++) {
+      auto f = [&](const double *a) { return a ? make_float4((float)a[j * 3], (float)a[j * 3 + 1], (float)a[j * 3 + 2], 0.f)
+                                               : make_float4(0, 0, 0, 0); };
+      auto d = [&](const double *a) { return a ? mkd4(a[j * 3], a[j * 3 + 1], a[j * 3 + 2], 0.0)
+                                               : mkd4(0, 0, 0, 0); };
+      kl[j] = f(J.penalty_lin);
+      ka[j] = f(J.penalty_ang);
+      ll[j] = d(J.lambda_lin);
+      la[j] = d(J.lambda_ang);
+      st[j] = (J.broken && J.broken[j]) ? (kBroken | kRemoved) : 0;
+    }
+    CK(cudaMemcpy(w.j.penLin, kl.data(), ctx->nj * sizeof(float4), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(w.j.penAng, ka.data(), ctx->nj * sizeof(float4), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(w.j.lamLin, ll.data(), ctx->nj * sizeof(D4), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(w.j.lamAng, la.data(), ctx->nj * sizeof(D4), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(w.j.state, st.data(), ctx->nj * sizeof(int), cudaMemcpyHostToDevice));
+  }
+  const avbd_spring_soa &S = world->springs;
+  if (ctx->ns) {
+    std::vector<float> pen(ctx->ns);
+    std::vector<double> peak(ctx->ns);
+    std::vector<int> st(ctx->ns);
+    for (int s = 0; s < ctx->ns; s++) {
+      pen[s] = S.penalty ? (float)S.penalty[s] : 0.f;
+      peak[s] = S.peak_strain ? S.peak_strain[s] : 0.0;
+      st[s] = (S.broken && S.broken[s]) ? kBroken : 0;
+    }
+    CK(cudaMemcpy(w.s.penalty, pen.data(), ctx->ns * sizeof(float), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(w.s.peak, peak.data(), ctx->ns * sizeof(double), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(w.s.state, st.data(), ctx->ns * sizeof(int), cudaMemcpyHostToDevice));
+  }
+
+  // warm-start manifolds -> the "previous step" arena, sorted by pair key
+  const avbd_manifold_soa &M = world->manifolds;
+  int live = 0;
+  Manifolds &pm = ctx->curIsA ? ctx->mB : ctx->mA;
+  if (M.count > 0) {
+    if (M.count > ctx->candCap) return fail(ctx, AVBD_ERR_CAPACITY, "%d manifolds exceed capacity %d", M.count, ctx->candCap);
+    std::vector<int> idx;
+    for (int m = 0; m < M.count; m++) {
+      const int a = M.body_a[m], b = M.body_b[m];
+      if (a <= b || a >= n || b < 0) return fail(ctx, AVBD_ERR_ARG, "manifold %d: body_a must exceed body_b", m);
+      if (M.num_contacts[m] > 0) idx.push_back(m);
+    }
+    std::sort(idx.begin(), idx.end(), [&](int x, int y) {
+      return ((uint64_t)M.body_a[x] << 32 | (uint32_t)M.body_b[x]) < ((uint64_t)M.body_a[y] << 32 | (uint32_t)M.body_b[y]);
+    });
+    live = (int)idx.size();
+    const size_t K = kMaxContacts;
+    std::vector<uint64_t> key(live);
+    std::vector<int> cnt(live);
+    std::vector<double> basisD((size_t)live * 9);
+    std::vector<uint32_t> feat(live * K, 0);
+    std::vector<float4> rA(live * K), rB(live * K), cK(live * K), cL(live * K);
+    for (int t = 0; t < live; t++) {
+      const int m = idx[t];
+      key[t] = (uint64_t)M.body_a[m] << 32 | (uint32_t)M.body_b[m];
+      cnt[t] = std::min(M.num_contacts[m], (int)K);
+      for (int k = 0; k < 9; k++) basisD[t * 9 + k] = M.basis ? M.basis[m * 9 + k] : 0.0;
+      for (size_t s = 0; s < K; s++) {
+        const size_t src = (size_t)m * K + s, dst = (size_t)t * K + s;
+        feat[dst] = M.feature ? M.feature[src] : 0u;
+        auto f3 = [&](const double *a, float wv) {
+          return a ? make_float4((float)a[src * 3], (float)a[src * 3 + 1], (float)a[src * 3 + 2], wv) : make_float4(0, 0, 0, wv);
+        };
+        rA[dst] = f3(M.r_a, 0.f);
+        rB[dst] = f3(M.r_b, 0.f);
+        cK[dst] = f3(M.penalty, 0.f);
+        cL[dst] = f3(M.lambda, (M.stick && M.stick[src]) ? 1.f : 0.f);
+      }
+    }
+    CK(cudaMemcpy(pm.key, key.data(), live * sizeof(uint64_t), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(pm.count, cnt.data(), live * sizeof(int), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(pm.basisD, basisD.data(), basisD.size() * sizeof(double), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(pm.feat, feat.data(), feat.size() * sizeof(uint32_t), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(pm.rA, rA.data(), rA.size() * sizeof(float4), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(pm.rB, rB.data(), rB.size() * sizeof(float4), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(pm.cK, cK.data(), cK.size() * sizeof(float4), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(pm.cL, cL.data(), cL.size() * sizeof(float4), cudaMemcpyHostToDevice));
+  }
+  Control c{};
+  CK(cudaMemcpy(&c, w.ctl, sizeof(Control), cudaMemcpyDeviceToHost));
+  c.prevCandidates = live;
+  c.numCandidates = 0;
+  CK(cudaMemcpy(w.ctl, &c, sizeof(Control), cudaMemcpyHostToDevice));
+  return AVBD_OK;
+}
+
+int one_step(avbd_ctx *ctx) {
+  World &w = ctx->w;
+  set_world_manifolds(ctx);
+  cudaStream_t st = ctx->stream;
+  // per-step counters: numCandidates .. adjTotal
+  CK(cudaMemsetAsync(&w.ctl->numCandidates, 0, sizeof(int) * 7, st));
+  int rc;
+  if ((rc = record(ctx, 0))) return rc;
+  launch_broadphase_impl(w, ctx->numLarge, ctx->bpTemp, ctx->bpTempBytes, st, ctx->smCount);
+  ctx->launches += 9 + (ctx->numLarge > 0 ? 2 : 0);
+  if ((rc = record(ctx, 1))) return rc;
+  launch_narrowphase(w, st, ctx->smCount);
+  ctx->launches += 1;
+  if ((rc = record(ctx, 2))) return rc;
+  launch_prepare(w, ctx->svTemp, ctx->svTempBytes, st, ctx->smCount);
+  ctx->launches += 6;
+  if ((rc = record(ctx, 3))) return rc;
+  CK(launch_coloring(w, st, ctx->smCount));
+  ctx->launches += 1;
+  if ((rc = record(ctx, 4))) return rc;
+  CK(launch_solve(w, ctx->lanes, ctx->blocksPerSm, st, ctx->smCount));
+  ctx->launches += 1;
+  launch_commit(w, st, ctx->smCount);
+  ctx->launches += 1;
+  // this step's candidates become next step's previous manifolds
+  CK(cudaMemcpyAsync(&w.ctl->prevCandidates, &w.ctl->numCandidates, sizeof(int), cudaMemcpyDeviceToDevice, st));
+  if ((rc = record(ctx, 5))) return rc;
+  CK(cudaGetLastError());
+  ctx->curIsA ^= 1;
+  ctx->steps++;
+  if (ctx->profiling) {
+    CK(cudaEventSynchronize(ctx->ev[5]));
+    float t[5];
+    for (int k = 0; k < 5; k++) cudaEventElapsedTime(&t[k], ctx->ev[k], ctx->ev[k + 1]);
+    ctx->prof.broadphase_ms = t[0];
+    ctx->prof.narrowphase_ms = t[1];
+    ctx->prof.prepare_ms = t[2];
+    ctx->prof.coloring_ms = t[3];
+    ctx->prof.solve_ms = t[4];
+    float tot = 0;
+    cudaEventElapsedTime(&tot, ctx->ev[0], ctx->ev[5]);
+    ctx->prof.step_ms = tot;
+  }
+  return AVBD_OK;
+}
+
+int check_flags(avbd_ctx *ctx) {
+  Control c{};
+  CK(cudaMemcpy(&c, ctx->w.ctl, sizeof(Control), cudaMemcpyDeviceToHost));
+  if (c.flags & kOvfTimeout) return fail(ctx, AVBD_ERR_TIMEOUT, "a device grid barrier timed out");
+  if (c.flags & (kOvfCells | kOvfPairs | kOvfAdj | kOvfColors)) {
+    // grow the arenas that overflowed for the next pack; this state is invalid
+    if (c.flags & kOvfPairs) ctx->params.max_pairs_per_body = std::max(ctx->params.max_pairs_per_body, 16) * 2;
+    if (c.flags & kOvfAdj) ctx->params.max_adjacency = std::max(ctx->params.max_adjacency, 2) * 2;
+    if (c.flags & kOvfCells) ctx->params.reserved0 = std::max(ctx->params.reserved0, 1) * 2;
+    return fail(ctx, AVBD_ERR_CAPACITY, "device arena overflow (flags 0x%x); capacities grown, repack to retry",
+                c.flags);
+  }
+  if (c.flags & kErrNaN) return fail(ctx, AVBD_ERR_NAN, "non-finite body state produced");
+  return AVBD_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+void avbd_default_params(avbd_params *o) {
+  std::memset(o, 0, sizeof(*o));
+  o->dt = 1.0 / 60.0;
+  o->gravity = -10.0;
+  o->iterations = 10;
+  o->beta_lin = 1e4;
+  o->beta_ang = 100;
+  o->alpha = 0.95;
+  o->gamma = 0.999;
+  o->penalty_min = 1;
+  o->penalty_max = 1e10;
+  o->collision_margin = 0.01;
+  o->stick_threshold = 1e-5;
+  o->rotated_inertia = 1;
+  o->spring_geometric_stiffness = 1;
+  o->cached_contact_jacobians = 1;
+  o->hash_threshold = 150;
+  o->body_order = AVBD_ORDER_PRIORITY;
+  o->fp64_ratio_threshold = 1e5;
+}
+
+int avbd_create(const avbd_params *params, avbd_ctx **out) {
+  if (!params || !out) {
+    g_create_error = "avbd_create: NULL argument";
+    return AVBD_ERR_ARG;
+  }
+  if (!(params->dt > 0) || params->iterations < 0) {
+    g_create_error = "avbd_create: dt must be > 0 and iterations >= 0";
+    return AVBD_ERR_ARG;
+  }
+  avbd_ctx *ctx = new avbd_ctx();
+  ctx->params = *params;
+  cudaError_t e = cudaGetDevice(&ctx->device);
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&ctx->smCount, cudaDevAttrMultiProcessorCount, ctx->device);
+  int coop = 0;
+  if (e == cudaSuccess) e = cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, ctx->device);
+  if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
+  for (int k = 0; k < 8 && e == cudaSuccess; k++) e = cudaEventCreate(&ctx->ev[k]);
+  if (e != cudaSuccess || !coop) {
+    g_create_error_buf = std::string("avbd_create: ") + (e != cudaSuccess ? cudaGetErrorString(e)
+                                                                          : "device lacks cooperative launch");
+    g_create_error = g_create_error_buf.c_str();
+    delete ctx;
+    return AVBD_ERR_CUDA;
+  }
+  *out = ctx;
+  return AVBD_OK;
+}
+
+int avbd_destroy(avbd_ctx *ctx) {
+  if (!ctx) return AVBD_OK;
+  cudaStreamSynchronize(ctx->stream);
+  free_all(ctx);
+  for (auto &e : ctx->ev)
+    if (e) cudaEventDestroy(e);
+  if (ctx->stream) cudaStreamDestroy(ctx->stream);
+  delete ctx;
+  return AVBD_OK;
+}
+
+int avbd_pack(avbd_ctx *ctx, const avbd_world *world) {
+  if (!ctx || !world) return fail(ctx, AVBD_ERR_ARG, "avbd_pack: NULL argument");
+  const avbd_body_soa &B = world->bodies;
+  const int n = B.count;
+  if (n <= 0 || !B.size || !B.mass || !B.moment || !B.radius || !B.friction || !B.pos)
+    return fail(ctx, AVBD_ERR_ARG, "avbd_pack: bodies need count > 0 and size/mass/moment/radius/friction/pos");
+  cudaStreamSynchronize(ctx->stream);
+  free_all(ctx);
+  ctx->n = n;
+  ctx->nj = world->joints.count;
+  ctx->ns = world->springs.count;
+  // scenes
+  std::vector<int> sceneStart;
+  if (world->num_scenes > 1 && world->scene_start) {
+    sceneStart.assign(world->scene_start, world->scene_start + world->num_scenes + 1);
+  } else {
+    sceneStart = {0, n};
+  }
+  const int S = (int)sceneStart.size() - 1;
+  if (sceneStart.front() != 0 || sceneStart.back() != n)
+    return fail(ctx, AVBD_ERR_ARG, "avbd_pack: scene_start must run from 0 to the body count");
+  for (int s = 0; s < S; s++)
+    if (sceneStart[s + 1] < sceneStart[s]) return fail(ctx, AVBD_ERR_ARG, "avbd_pack: scene_start not monotone");
+  ctx->numScenes = S;
+  std::vector<int> scene(n);
+  for (int s = 0; s < S; s++)
+    for (int i = sceneStart[s]; i < sceneStart[s + 1]; i++) scene[i] = s;
+
+  // static body tables
+  std::vector<D4> size(n), massD(n);
+  std::vector<float4> massF(n);
+  std::vector<double> friction(n), invCell(S);
+  std::vector<int> flags0(n);
+  std::vector<uint32_t> prio(n);
+  std::vector<std::vector<int>> large(S);
+  for (int s = 0; s < S; s++) {
+    // cell size and "large" threshold from the mean radius (broadphase.js:52-59)
+    double sum = 0;
+    const int cnt = sceneStart[s + 1] - sceneStart[s];
+    for (int i = sceneStart[s]; i < sceneStart[s + 1]; i++) sum += B.radius[i];
+    const double mean = cnt ? sum / cnt : 1.0;
+    const double thr = std::max(mean * 8, 1e-6);
+    invCell[s] = 1 / std::max(mean * 2, 1e-4);
+    for (int i = sceneStart[s]; i < sceneStart[s + 1]; i++) {
+      const int shape = B.shape ? B.shape[i] : AVBD_SHAPE_BOX;
+      if (!(B.mass[i] >= 0) || !std::isfinite(B.mass[i]))
+        return fail(ctx, AVBD_ERR_ARG, "body %d: mass must be finite and >= 0", i);
+      size[i] = mkd4(B.size[i * 3], B.size[i * 3 + 1], B.size[i * 3 + 2], B.radius[i]);
+      massD[i] = mkd4(B.mass[i], B.moment[i * 3], B.moment[i * 3 + 1], B.moment[i * 3 + 2]);
+      massF[i] = make_float4((float)B.mass[i], (float)B.moment[i * 3], (float)B.moment[i * 3 + 1],
+                             (float)B.moment[i * 3 + 2]);
+      friction[i] = B.friction[i];
+      int f = 0;
+      if (B.mass[i] > 0) f |= kBodyDynamic;
+      if (shape == AVBD_SHAPE_SPHERE) f |= kBodySphere;
+      if (B.radius[i] > thr) {
+        f |= kBodyLarge;
+        large[s].push_back(i);
+      }
+      flags0[i] = f;
+      prio[i] = priority_of((uint32_t)(i - sceneStart[s]));
+    }
+  }
+  std::vector<int> largeStart(S + 1, 0), largeList;
+  for (int s = 0; s < S; s++) {
+    largeStart[s] = (int)largeList.size();
+    largeList.insert(largeList.end(), large[s].begin(), large[s].end());
+  }
+  largeStart[S] = (int)largeList.size();
+  ctx->numLarge = (int)largeList.size();
+
+  // joints / springs
+  const avbd_joint_soa &J = world->joints;
+  const avbd_spring_soa &SP = world->springs;
+  std::vector<int2> jb(ctx->nj), sb(ctx->ns);
+  std::vector<D4> jrA(ctx->nj), jrB(ctx->nj), jst(ctx->nj), srA(ctx->ns), srB(ctx->ns), sprm(ctx->ns);
+  std::vector<float4> jrAf(ctx->nj), jrBf(ctx->nj), srAf(ctx->ns), srBf(ctx->ns);
+  std::vector<std::vector<uint32_t>> refs(n);
+  for (int j = 0; j < ctx->nj; j++) {
+    const int a = J.body_a[j], b = J.body_b[j];
+    if (b < 0 || b >= n || a >= n || a == b) return fail(ctx, AVBD_ERR_ARG, "joint %d: bad body indices", j);
+    if (a >= 0 && scene[a] != scene[b]) return fail(ctx, AVBD_ERR_ARG, "joint %d crosses scenes", j);
+    jb[j] = make_int2(a, b);
+    jrA[j] = mkd4(J.r_a[j * 3], J.r_a[j * 3 + 1], J.r_a[j * 3 + 2], 0);
+    jrB[j] = mkd4(J.r_b[j * 3], J.r_b[j * 3 + 1], J.r_b[j * 3 + 2], 0);
+    jrAf[j] = make_float4((float)jrA[j].x, (float)jrA[j].y, (float)jrA[j].z, 0);
+    jrBf[j] = make_float4((float)jrB[j].x, (float)jrB[j].y, (float)jrB[j].z, 0);
+    // torqueArm = |size_A + size_B|^2 (joint.js:108-112)
+    const double sx = (a >= 0 ? B.size[a * 3] : 0) + B.size[b * 3];
+    const double sy = (a >= 0 ? B.size[a * 3 + 1] : 0) + B.size[b * 3 + 1];
+    const double sz = (a >= 0 ? B.size[a * 3 + 2] : 0) + B.size[b * 3 + 2];
+    jst[j] = mkd4(J.stiffness_lin[j], J.stiffness_ang[j], J.fracture[j], sx * sx + sy * sy + sz * sz);
+    if (a >= 0) refs[a].push_back(make_ref(kRefJoint, j, 0));
+    refs[b].push_back(make_ref(kRefJoint, j, 1));
+  }
+  for (int s = 0; s < ctx->ns; s++) {
+    const int a = SP.body_a[s], b = SP.body_b[s];
+    if (a < 0 || b < 0 || a >= n || b >= n || a == b) return fail(ctx, AVBD_ERR_ARG, "spring %d: bad body indices", s);
+    if (scene[a] != scene[b]) return fail(ctx, AVBD_ERR_ARG, "spring %d crosses scenes", s);
+    if (!(SP.rest[s] >= 0)) return fail(ctx, AVBD_ERR_ARG, "spring %d: rest length must be resolved (>= 0)", s);
+    sb[s] = make_int2(a, b);
+    srA[s] = mkd4(SP.r_a[s * 3], SP.r_a[s * 3 + 1], SP.r_a[s * 3 + 2], 0);
+    srB[s] = mkd4(SP.r_b[s * 3], SP.r_b[s * 3 + 1], SP.r_b[s * 3 + 2], 0);
+    srAf[s] = make_float4((float)srA[s].x, (float)srA[s].y, (float)srA[s].z, 0);
+    srBf[s] = make_float4((float)srB[s].x, (float)srB[s].y, (float)srB[s].z, 0);
+    sprm[s] = mkd4(SP.stiffness[s], SP.rest[s], SP.tear_strain ? SP.tear_strain[s] : INFINITY, 0);
+    refs[a].push_back(make_ref(kRefSpring, s, 0));
+    refs[b].push_back(make_ref(kRefSpring, s, 1));
+  }
+  std::vector<int> cStart(n + 1, 0);
+  std::vector<uint32_t> cRef;
+  for (int i = 0; i < n; i++) {
+    cStart[i] = (int)cRef.size();
+    cRef.insert(cRef.end(), refs[i].begin(), refs[i].end());
+  }
+  cStart[n] = (int)cRef.size();
+
+  // capacities
+  long long insertions = 0;
+  for (int i = 0; i < n; i++) {
+    if (flags0[i] & kBodyLarge) continue;
+    const double r = B.radius[i] * (1.0 + 1e-7) + 1e-9, inv = invCell[scene[i]];
+    long long c = 1;
+    for (int k = 0; k < 3; k++) {
+      const double p = B.pos[i * 3 + k];
+      c *= (long long)std::floor((p + r) * inv) - (long long)std::floor((p - r) * inv) + 1;
+    }
+    insertions += c;
+  }
+  const int pairsPerBody = std::max(ctx->params.max_pairs_per_body, 12);
+  const int cellFactor = std::max(ctx->params.reserved0, 1);
+  ctx->candCap = (int)std::min<long long>((long long)n * pairsPerBody + 4096 + world->manifolds.count, 0x3fffffff);
+  ctx->entryCap = (int)std::min<long long>(insertions * 2 * cellFactor + 4096, 0x3fffffff);
+  ctx->tableSize = 1024;
+  while (ctx->tableSize < ctx->entryCap * 2) ctx->tableSize *= 2;
+  ctx->adjCap = (int)std::min<long long>(2LL * ctx->candCap * std::max(ctx->params.max_adjacency, 1) / 1, 0x3fffffff);
+
+  World &w = ctx->w;
+  w = World{};
+  const avbd_params &P = ctx->params;
+  w.p = SolverParams{P.dt, P.gravity, P.iterations, P.post_stabilize, P.beta_lin, P.beta_ang, P.alpha, P.gamma,
+                     P.penalty_min, P.penalty_max, P.collision_margin, P.stick_threshold, P.rotated_inertia,
+                     P.spring_stiffness_ramp, P.spring_geometric_stiffness, P.cached_contact_jacobians,
+                     P.fp64_ratio_threshold};
+  int rc = 0;
+  D4 *sizeP, *massDP;
+  float4 *massFP;
+  double *fricP, *invCellP;
+  int *flags0P, *sceneP, *sceneStartP, *largeStartP, *largeListP, *cStartP;
+  uint32_t *prioP, *cRefP;
+  if ((rc = upload(ctx, &sizeP, size)) || (rc = upload(ctx, &massDP, massD)) || (rc = upload(ctx, &massFP, massF)) ||
+      (rc = upload(ctx, &fricP, friction)) || (rc = upload(ctx, &flags0P, flags0)) || (rc = upload(ctx, &sceneP, scene)) ||
+      (rc = upload(ctx, &prioP, prio)) || (rc = upload(ctx, &invCellP, invCell)) ||
+      (rc = upload(ctx, &sceneStartP, sceneStart)) || (rc = upload(ctx, &largeStartP, largeStart)) ||
+      (rc = upload(ctx, &largeListP, largeList)) || (rc = upload(ctx, &cStartP, cStart)) || (rc = upload(ctx, &cRefP, cRef)))
+    return rc;
+  w.b.n = n;
+  w.b.size = sizeP; w.b.massD = massDP; w.b.massF = massFP; w.b.friction = fricP; w.b.flags0 = flags0P;
+  w.b.scene = sceneP; w.b.priority = prioP;
+  if ((rc = dalloc(ctx, &w.b.pos, n)) || (rc = dalloc(ctx, &w.b.quat, n)) || (rc = dalloc(ctx, &w.b.vel, n)) ||
+      (rc = dalloc(ctx, &w.b.omega, n)) || (rc = dalloc(ctx, &w.b.prevVel, n)) || (rc = dalloc(ctx, &w.b.quatT, n)) ||
+      (rc = dalloc(ctx, &w.b.dp, n)) || (rc = dalloc(ctx, &w.b.yLin, n)) || (rc = dalloc(ctx, &w.b.yAng, n)) ||
+      (rc = dalloc(ctx, &w.b.dpD, n)) || (rc = dalloc(ctx, &w.b.quatD, n)) || (rc = dalloc(ctx, &w.b.flags, n)) ||
+      (rc = dalloc(ctx, &w.b.color, n)))
+    return rc;
+  // joints
+  w.j.n = ctx->nj;
+  {
+    int2 *jbP; D4 *a, *b, *c; float4 *af, *bf;
+    if ((rc = upload(ctx, &jbP, jb)) || (rc = upload(ctx, &a, jrA)) || (rc = upload(ctx, &b, jrB)) ||
+        (rc = upload(ctx, &c, jst)) || (rc = upload(ctx, &af, jrAf)) || (rc = upload(ctx, &bf, jrBf)))
+      return rc;
+    w.j.bodies = jbP; w.j.rAD = a; w.j.rBD = b; w.j.stiff = c; w.j.rAF = af; w.j.rBF = bf;
+    if ((rc = dalloc(ctx, &w.j.penLin, ctx->nj)) || (rc = dalloc(ctx, &w.j.penAng, ctx->nj)) ||
+        (rc = dalloc(ctx, &w.j.lamLin, ctx->nj)) || (rc = dalloc(ctx, &w.j.lamAng, ctx->nj)) ||
+        (rc = dalloc(ctx, &w.j.c0Lin, ctx->nj)) || (rc = dalloc(ctx, &w.j.c0Ang, ctx->nj)) ||
+        (rc = dalloc(ctx, &w.j.dpt, ctx->nj)) || (rc = dalloc(ctx, &w.j.dptD, ctx->nj)) ||
+        (rc = dalloc(ctx, &w.j.state, ctx->nj)))
+      return rc;
+  }
+  w.s.n = ctx->ns;
+  {
+    int2 *sbP; D4 *a, *b, *c; float4 *af, *bf;
+    if ((rc = upload(ctx, &sbP, sb)) || (rc = upload(ctx, &a, srA)) || (rc = upload(ctx, &b, srB)) ||
+        (rc = upload(ctx, &c, sprm)) || (rc = upload(ctx, &af, srAf)) || (rc = upload(ctx, &bf, srBf)))
+      return rc;
+    w.s.bodies = sbP; w.s.rAD = a; w.s.rBD = b; w.s.prm = c; w.s.rAF = af; w.s.rBF = bf;
+    if ((rc = dalloc(ctx, &w.s.penalty, ctx->ns)) || (rc = dalloc(ctx, &w.s.peak, ctx->ns)) ||
+        (rc = dalloc(ctx, &w.s.state, ctx->ns)) || (rc = dalloc(ctx, &w.s.dpt, ctx->ns)) ||
+        (rc = dalloc(ctx, &w.s.dptD, ctx->ns)))
+      return rc;
+  }
+  // grid
+  w.g.numScenes = S;
+  w.g.sceneStart = sceneStartP; w.g.invCell = invCellP; w.g.largeStart = largeStartP; w.g.largeList = largeListP;
+  w.g.cStart = cStartP; w.g.cRef = cRefP;
+  w.g.tableMask = (unsigned)(ctx->tableSize - 1);
+  w.g.entryCap = ctx->entryCap;
+  w.g.candCap = ctx->candCap;
+  if ((rc = dalloc(ctx, &w.g.cellLo, n)) || (rc = dalloc(ctx, &w.g.cellHi, n)) ||
+      (rc = dalloc(ctx, &w.g.tableCount, ctx->tableSize)) || (rc = dalloc(ctx, &w.g.tableStart, ctx->tableSize)) ||
+      (rc = dalloc(ctx, &w.g.tableCursor, ctx->tableSize)) || (rc = dalloc(ctx, &w.g.entries, ctx->entryCap)) ||
+      (rc = dalloc(ctx, &w.g.pairCount, n + 1)) || (rc = dalloc(ctx, &w.g.pairStart, n + 1)) ||
+      (rc = dalloc(ctx, &w.g.candKey, ctx->candCap)) || (rc = dalloc(ctx, &w.g.candPrev, ctx->candCap)))
+    return rc;
+  // adjacency + colouring
+  w.a.cap = ctx->adjCap;
+  ctx->colorBlocks = std::max(1, coloring_grid(ctx->smCount));
+  if ((rc = dalloc(ctx, &w.a.start, n + 1)) || (rc = dalloc(ctx, &w.a.count, n + 1)) ||
+      (rc = dalloc(ctx, &w.a.cursor, n + 1)) || (rc = dalloc(ctx, &w.a.entry, ctx->adjCap)) ||
+      (rc = dalloc(ctx, &w.a.colorStart, kMaxColors + 1)) || (rc = dalloc(ctx, &w.a.colorBodies, n)) ||
+      (rc = dalloc(ctx, &w.a.blockHist, (size_t)ctx->colorBlocks * kMaxColors)))
+    return rc;
+  // manifolds (double-buffered)
+  if ((rc = alloc_manifolds(ctx, ctx->mA, ctx->candCap)) || (rc = alloc_manifolds(ctx, ctx->mB, ctx->candCap))) return rc;
+  ctx->curIsA = 1;
+  set_world_manifolds(ctx);
+  if ((rc = dalloc(ctx, &w.ctl, 1)) || (rc = dalloc(ctx, &ctx->statsOut, 3))) return rc;
+  // scratch of the scans
+  ctx->bpTempBytes = broadphase_temp_bytes(n, ctx->tableSize);
+  ctx->svTempBytes = solver_temp_bytes(n);
+  if ((rc = dalloc(ctx, (char **)&ctx->bpTemp, ctx->bpTempBytes)) || (rc = dalloc(ctx, (char **)&ctx->svTemp, ctx->svTempBytes)))
+    return rc;
+  // launch shape of the persistent solve
+  const int maxPerSm = solve_max_blocks_per_sm(ctx->lanes);
+  ctx->lanes = P.lanes_per_body > 0 ? P.lanes_per_body : 8;
+  if (ctx->lanes != 1 && ctx->lanes != 2 && ctx->lanes != 4 && ctx->lanes != 8 && ctx->lanes != 16 && ctx->lanes != 32)
+    return fail(ctx, AVBD_ERR_ARG, "lanes_per_body must be a power of two <= 32");
+  ctx->blocksPerSm = P.blocks_per_sm > 0 ? std::min(P.blocks_per_sm, maxPerSm) : maxPerSm;
+  if (ctx->blocksPerSm < 1) return fail(ctx, AVBD_ERR_CUDA, "solve kernel cannot be made resident");
+  // colours start at 0 for dynamic bodies
+  CK(cudaMemset(w.b.color, 0, sizeof(int) * n));
+  ctx->packed = true;
+  ctx->steps = 0;
+  ctx->launches = 0;
+  rc = write_state(ctx, world);
+  if (rc) return rc;
+  CK(cudaDeviceSynchronize());
+  return AVBD_OK;
+}
+
+int avbd_step(avbd_ctx *ctx, int32_t n_steps) {
+  if (!ctx) return AVBD_ERR_ARG;
+  if (!ctx->packed) return fail(ctx, AVBD_ERR_STATE, "avbd_step before avbd_pack");
+  for (int s = 0; s < n_steps; s++) {
+    int rc = one_step(ctx);
+    if (rc) return rc;
+  }
+  return AVBD_OK;
+}
+
+int avbd_synchronize(avbd_ctx *ctx) {
+  if (!ctx) return AVBD_ERR_ARG;
+  CK(cudaStreamSynchronize(ctx->stream));
+  if (!ctx->packed) return AVBD_OK;
+  return check_flags(ctx);
+}
+
+int avbd_read_state(avbd_ctx *ctx, avbd_world *out) {
+  if (!ctx || !out) return AVBD_ERR_ARG;
+  if (!ctx->packed) return fail(ctx, AVBD_ERR_STATE, "avbd_read_state before avbd_pack");
+  CK(cudaStreamSynchronize(ctx->stream));
+  const World &w = ctx->w;
+  const int n = ctx->n;
+  avbd_body_soa &B = out->bodies;
+  if (B.count < n) return fail(ctx, AVBD_ERR_ARG, "avbd_read_state: body arrays hold %d < %d", B.count, n);
+  std::vector<D4> pos(n);
+  std::vector<float4> q(n), v(n), om(n), pv(n);
+  CK(cudaMemcpy(pos.data(), w.b.pos, n * sizeof(D4), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(q.data(), w.b.quat, n * sizeof(float4), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(v.data(), w.b.vel, n * sizeof(float4), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(om.data(), w.b.omega, n * sizeof(float4), cudaMemcpyDeviceToHost));
+  CK(cudaMemcpy(pv.data(), w.b.prevVel, n * sizeof(float4), cudaMemcpyDeviceToHost));
+  for (int i = 0; i < n; i++) {
+    if (B.pos) { B.pos[i * 3] = pos[i].x; B.pos[i * 3 + 1] = pos[i].y; B.pos[i * 3 + 2] = pos[i].z; }
+    if (B.quat) { B.quat[i * 4] = q[i].x; B.quat[i * 4 + 1] = q[i].y; B.quat[i * 4 + 2] = q[i].z; B.quat[i * 4 + 3] = q[i].w; }
+    if (B.vel) { B.vel[i * 3] = v[i].x; B.vel[i * 3 + 1] = v[i].y; B.vel[i * 3 + 2] = v[i].z; }
+    if (B.omega) { B.omega[i * 3] = om[i].x; B.omega[i * 3 + 1] = om[i].y; B.omega[i * 3 + 2] = om[i].z; }
+    if (B.prev_vel) { B.prev_vel[i * 3] = pv[i].x; B.prev_vel[i * 3 + 1] = pv[i].y; B.prev_vel[i * 3 + 2] = pv[i].z; }
+  }
+  avbd_joint_soa &J = out->joints;
+  if (ctx->nj && J.count >= ctx->nj) {
+    std::vector<float4> kl(ctx->nj), ka(ctx->nj);
+    std::vector<D4> ll(ctx->nj), la(ctx->nj);
+    std::vector<int> st(ctx->nj);
+    CK(cudaMemcpy(kl.data(), w.j.penLin, ctx->nj * sizeof(float4), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(ka.data(), w.j.penAng, ctx->nj * sizeof(float4), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(ll.data(), w.j.lamLin, ctx->nj * sizeof(D4), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(la.data(), w.j.lamAng, ctx->nj * sizeof(D4), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(st.data(), w.j.state, ctx->nj * sizeof(int), cudaMemcpyDeviceToHost));
+    for (int j = 0; j < ctx->nj; j++) {
+      const float kv[6] = {kl[j].x, kl[j].y, kl[j].z, ka[j].x, ka[j].y, ka[j].z};
+      const double lv[6] = {ll[j].x, ll[j].y, ll[j].z, la[j].x, la[j].y, la[j].z};
+      for (int k = 0; k < 3; k++) {
+        if (J.penalty_lin) J.penalty_lin[j * 3 + k] = kv[k];
+        if (J.penalty_ang) J.penalty_ang[j * 3 + k] = kv[3 + k];
+        if (J.lambda_lin) J.lambda_lin[j * 3 + k] = lv[k];
+        if (J.lambda_ang) J.lambda_ang[j * 3 + k] = lv[3 + k];
+      }
+      if (J.broken) J.broken[j] = (st[j] & kBroken) ? 1 : 0;
+    }
+  }
+  avbd_spring_soa &SP = out->springs;
+  if (ctx->ns && SP.count >= ctx->ns) {
+    std::vector<float> pen(ctx->ns);
+    std::vector<double> peak(ctx->ns);
+    std::vector<int> st(ctx->ns);
+    CK(cudaMemcpy(pen.data(), w.s.penalty, ctx->ns * sizeof(float), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(peak.data(), w.s.peak, ctx->ns * sizeof(double), cudaMemcpyDeviceToHost));
+    CK(cudaMemcpy(st.data(), w.s.state, ctx->ns * sizeof(int), cudaMemcpyDeviceToHost));
+    for (int s = 0; s < ctx->ns; s++) {
+      if (SP.penalty) SP.penalty[s] = pen[s];
+      if (SP.peak_strain) SP.peak_strain[s] = peak[s];
+      if (SP.broken) SP.broken[s] = (st[s] & kBroken) ? 1 : 0;
+    }
+  }
+  // manifolds of the last step (now the "previous" arena)
+  avbd_manifold_soa &M = out->manifolds;
+  if (M.body_a || M.num_contacts) {
+    Control c{};
+    CK(cudaMemcpy(&c, w.ctl, sizeof(Control), cudaMemcpyDeviceToHost));
+    const int total = c.prevCandidates;
+    const Manifolds &pm = ctx->curIsA ? ctx->mB : ctx->mA;
+    std::vector<uint64_t> key(total);
+    std::vector<int> cnt(total);
+    if (total) {
+      CK(cudaMemcpy(key.data(), pm.key, total * sizeof(uint64_t), cudaMemcpyDeviceToHost));
+      CK(cudaMemcpy(cnt.data(), pm.count, total * sizeof(int), cudaMemcpyDeviceToHost));
+    }
+    std::vector<int> live;
+    for (int m = 0; m < total; m++)
+      if (cnt[m] > 0) live.push_back(m);
+    M.count = (int)live.size();
+    const int wrote = std::min<int>(M.count, M.capacity);
+    const size_t K = kMaxContacts;
+    std::vector<double> basisD((size_t)total * 9);
+    std::vector<float4> b0(total);
+    std::vector<uint32_t> feat((size_t)total * K);
+    std::vector<float4> rA(total * K), rB(total * K), cA(total * K), cB(total * K), cK(total * K), cL(total * K);
+    if (total) {
+      CK(cudaMemcpy(basisD.data(), pm.basisD, basisD.size() * sizeof(double), cudaMemcpyDeviceToHost));
+      CK(cudaMemcpy(b0.data(), pm.basis0, total * sizeof(float4), cudaMemcpyDeviceToHost));
+      CK(cudaMemcpy(feat.data(), pm.feat, feat.size() * sizeof(uint32_t), cudaMemcpyDeviceToHost));
+      CK(cudaMemcpy(rA.data(), pm.rA, rA.size() * sizeof(float4), cudaMemcpyDeviceToHost));
+      CK(cudaMemcpy(rB.data(), pm.rB, rB.size() * sizeof(float4), cudaMemcpyDeviceToHost));
+      CK(cudaMemcpy(cA.data(), pm.cA, cA.size() * sizeof(float4), cudaMemcpyDeviceToHost));
+      CK(cudaMemcpy(cB.data(), pm.cB, cB.size() * sizeof(float4), cudaMemcpyDeviceToHost));
+      CK(cudaMemcpy(cK.data(), pm.cK, cK.size() * sizeof(float4), cudaMemcpyDeviceToHost));
+      CK(cudaMemcpy(cL.data(), pm.cL, cL.size() * sizeof(float4), cudaMemcpyDeviceToHost));
+    }
+    for (int t = 0; t < wrote; t++) {
+      const int m = live[t];
+      if (M.body_a) M.body_a[t] = (int)(key[m] >> 32);
+      if (M.body_b) M.body_b[t] = (int)(key[m] & 0xffffffffu);
+      if (M.num_contacts) M.num_contacts[t] = cnt[m];
+      if (M.basis) for (int k = 0; k < 9; k++) M.basis[t * 9 + k] = basisD[(size_t)m * 9 + k];
+      if (M.friction) M.friction[t] = b0[m].w;
+      for (size_t s = 0; s < K; s++) {
+        const size_t d = (size_t)t * K + s, src = (size_t)m * K + s;
+        const bool on = (int)s < cnt[m];
+        if (M.feature) M.feature[d] = on ? feat[src] : 0u;
+        const float4 v[5] = {rA[src], rB[src], make_float4(cA[src].w, cB[src].w, cK[src].w, 0), cK[src], cL[src]};
+        double *dst[5] = {M.r_a, M.r_b, M.c0, M.penalty, M.lambda};
+        for (int f = 0; f < 5; f++)
+          if (dst[f]) {
+            dst[f][d * 3] = on ? v[f].x : 0;
+            dst[f][d * 3 + 1] = on ? v[f].y : 0;
+            dst[f][d * 3 + 2] = on ? v[f].z : 0;
+          }
+        if (M.stick) M.stick[d] = (on && cL[src].w != 0.f) ? 1 : 0;
+      }
+      if (M.order) M.order[t] = t;
+    }
+  }
+  return AVBD_OK;
+}
+
+int avbd_write_state(avbd_ctx *ctx, const avbd_world *world) {
+  if (!ctx || !world) return AVBD_ERR_ARG;
+  if (!ctx->packed) return fail(ctx, AVBD_ERR_STATE, "avbd_write_state before avbd_pack");
+  if (world->bodies.count != ctx->n || world->joints.count != ctx->nj || world->springs.count != ctx->ns)
+    return fail(ctx, AVBD_ERR_ARG, "avbd_write_state: topology differs from the packed world");
+  CK(cudaStreamSynchronize(ctx->stream));
+  return write_state(ctx, world);
+}
+
+int avbd_read_coloring(avbd_ctx *ctx, int32_t *color_of, int32_t *num_colors) {
+  if (!ctx || !ctx->packed) return fail(ctx, AVBD_ERR_STATE, "avbd_read_coloring before avbd_pack");
+  CK(cudaStreamSynchronize(ctx->stream));
+  if (color_of) CK(cudaMemcpy(color_of, ctx->w.b.color, ctx->n * sizeof(int), cudaMemcpyDeviceToHost));
+  Control c{};
+  CK(cudaMemcpy(&c, ctx->w.ctl, sizeof(Control), cudaMemcpyDeviceToHost));
+  if (num_colors) *num_colors = c.numColors;
+  return AVBD_OK;
+}
+
+int avbd_read_pairs(avbd_ctx *ctx, int32_t *body_a, int32_t *body_b, int64_t capacity, int64_t *count) {
+  if (!ctx || !ctx->packed) return fail(ctx, AVBD_ERR_STATE, "avbd_read_pairs before avbd_pack");
+  CK(cudaStreamSynchronize(ctx->stream));
+  Control c{};
+  CK(cudaMemcpy(&c, ctx->w.ctl, sizeof(Control), cudaMemcpyDeviceToHost));
+  const int total = c.prevCandidates;
+  if (count) *count = total;
+  const int k = (int)std::min<int64_t>(total, capacity);
+  if (k > 0) {
+    const Manifolds &pm = ctx->curIsA ? ctx->mB : ctx->mA;
+    std::vector<uint64_t> key(k);
+    CK(cudaMemcpy(key.data(), pm.key, k * sizeof(uint64_t), cudaMemcpyDeviceToHost));
+    for (int i = 0; i < k; i++) {
+      if (body_a) body_a[i] = (int)(key[i] >> 32);
+      if (body_b) body_b[i] = (int)(key[i] & 0xffffffffu);
+    }
+  }
+  return AVBD_OK;
+}
+
+int avbd_read_stats(avbd_ctx *ctx, avbd_stats *out) {
+  if (!ctx || !out) return AVBD_ERR_ARG;
+  std::memset(out, 0, sizeof(*out));
+  if (!ctx->packed) return AVBD_OK;
+  const World &w = ctx->w;
+  World sw = w;
+  const Manifolds &pm = ctx->curIsA ? ctx->mB : ctx->mA;
+  sw.cur = pm;
+  Control c{};
+  CK(cudaStreamSynchronize(ctx->stream));
+  CK(cudaMemcpy(&c, w.ctl, sizeof(Control), cudaMemcpyDeviceToHost));
+  // the stats kernel reads numCandidates: point it at the last step's count
+  Control tmp = c;
+  tmp.numCandidates = c.prevCandidates;
+  CK(cudaMemcpy(w.ctl, &tmp, sizeof(Control), cudaMemcpyHostToDevice));
+  launch_stats(sw, ctx->statsOut, ctx->stream, ctx->smCount);
+  double st3[3];
+  CK(cudaMemcpyAsync(st3, ctx->statsOut, sizeof(st3), cudaMemcpyDeviceToHost, ctx->stream));
+  CK(cudaStreamSynchronize(ctx->stream));
+  CK(cudaMemcpy(w.ctl, &c, sizeof(Control), cudaMemcpyHostToDevice));
+  out->bodies = ctx->n;
+  out->manifolds = c.liveManifolds;
+  out->contacts = c.liveContacts;
+  out->candidate_pairs = c.prevCandidates;
+  out->colors = c.numColors;
+  out->fp64_bodies = c.fp64Bodies;
+  out->overflow = c.flags;
+  out->steps = ctx->steps;
+  out->max_constraint_error = st3[0];
+  out->max_lambda = st3[1];
+  out->max_penalty = st3[2];
+  if (ctx->nj) {
+    std::vector<int> st(ctx->nj);
+    CK(cudaMemcpy(st.data(), w.j.state, ctx->nj * sizeof(int), cudaMemcpyDeviceToHost));
+    for (int s : st) out->joints_broken += (s & kBroken) ? 1 : 0;
+  }
+  if (ctx->ns) {
+    std::vector<int> st(ctx->ns);
+    CK(cudaMemcpy(st.data(), w.s.state, ctx->ns * sizeof(int), cudaMemcpyDeviceToHost));
+    for (int s : st) out->springs_broken += (s & kBroken) ? 1 : 0;
+  }
+  return AVBD_OK;
+}
+
+int avbd_set_profiling(avbd_ctx *ctx, int32_t on) {
+  if (!ctx) return AVBD_ERR_ARG;
+  ctx->profiling = on != 0;
+  return AVBD_OK;
+}
+
+int avbd_read_profile(avbd_ctx *ctx, avbd_profile *out) {
+  if (!ctx || !out) return AVBD_ERR_ARG;
+  *out = ctx->prof;
+  return AVBD_OK;
+}
+
+int avbd_kernel_launches(avbd_ctx *ctx, int64_t *out) {
+  if (!ctx || !out) return AVBD_ERR_ARG;
+  *out = ctx->launches;
+  return AVBD_OK;
+}
+
+const char *avbd_last_error(const avbd_ctx *ctx) { return ctx ? ctx->err.c_str() : g_create_error; }
+
+}  // extern "C"

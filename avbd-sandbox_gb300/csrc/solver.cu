@@ -1,0 +1,1213 @@
+// solver.cu - per-step preparation, constraint adjacency, integer-priority
+// colouring and the persistent primal/dual solve of one AVBD step.
+//
+// Reference path (src/physics/solver.js:340-489):
+//   force init   manifold.js:214-318 (narrowphase.cu), joint.js:131-160,
+//                spring.js:472-507                      -> prepare_forces_kernel
+//   body init    solver.js:366-401 (Eq. 2 + adaptive guess) -> prepare_bodies_kernel
+//   primal       solver.js:418-458, manifold.js:411-445, joint.js:162-253,
+//                spring.js:509-616, maths.js:660-725    -> solve_kernel
+//   dual         manifold.js:447-491, joint.js:255-317, spring.js:618-634
+//   velocity     solver.js:476-488 (BDF1)
+//
+// GB300 design:
+//   * the primal and dual iterations of a step are ONE cooperative persistent
+//     kernel; colour phases are separated by a bounded grid barrier
+//   * a group of `G` lanes assembles one body's 6x6 system (each lane takes a
+//     share of the incident constraints), reduces it with warp shuffles and
+//     every lane solves the LDL^T in registers
+//   * the dual update of a constraint is fused into the primal phase of its
+//     endpoint with the larger colour: both endpoints are final for the
+//     iteration at that moment, so this equals the reference's separate
+//     dual sweep (solver.js:466-470) without another barrier per iteration
+//   * positions are iterated as delta = x - x_t in f32 (x_t in f64), so the
+//     f32 rounding is relative to the step's displacement, not to |x|
+//   * bodies whose constraint stiffness dwarfs their inertia (k / (m/dt^2)
+//     above a threshold) are assembled and factored in f64 from f64 shadows
+#include <cooperative_groups.h>
+#include <cub/cub.cuh>
+
+#include "avbd_device.cuh"
+
+namespace avbd {
+namespace {
+
+constexpr int kSolveBlock = 256;
+constexpr long long kSpinLimit = 20000000;  // ~1-2 s of polling at most
+
+// ---------------------------------------------------------------------------
+// Bounded grid barrier (all blocks are co-resident: cooperative launch).
+// Returns false when the wait gave up or another block reported a timeout;
+// the caller must then return.
+// ---------------------------------------------------------------------------
+__device__ bool grid_barrier(Control *ctl) {
+  __shared__ int ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    ok = 1;
+    volatile unsigned *gen = &ctl->barrierGen;
+    const unsigned g = *gen;
+    __threadfence();
+    const unsigned arrived = atomicAdd(&ctl->barrierCount, 1u) + 1u;
+    if (arrived == gridDim.x) {
+      ctl->barrierCount = 0;
+      __threadfence();
+      atomicAdd(&ctl->barrierGen, 1u);
+    } else {
+      long long spins = 0;
+      while (*gen == g) {
+        if (++spins > kSpinLimit) {
+          atomicOr(&ctl->flags, kOvfTimeout);
+          break;
+        }
+        __nanosleep(64);
+      }
+    }
+    __threadfence();
+    if (*((volatile unsigned *)&ctl->flags) & kOvfTimeout) ok = 0;
+  }
+  __syncthreads();
+  return ok != 0;
+}
+
+// ---------------------------------------------------------------------------
+// Preparation
+// ---------------------------------------------------------------------------
+__device__ inline double jsmin(double a, double b) { return a < b ? a : (b < a ? b : a); }
+__device__ inline double jsmax(double a, double b) { return a > b ? a : (b > a ? b : a); }
+__device__ inline double clampd(double x, double a, double b) { return x != x ? x : jsmax(a, jsmin(b, x)); }
+
+__device__ inline Q4<double> body_q_t(const World &w, int i) {
+  const float4 q = w.b.quat[i];
+  return Q4<double>{q.x, q.y, q.z, q.w};
+}
+
+// joint.js:131-160 / spring.js:472-507, plus the f64 offsets p_A(t) - p_B(t).
+__global__ void prepare_forces_kernel(World w) {
+  const SolverParams &P = w.p;
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x, stride = gridDim.x * blockDim.x;
+  for (int j = tid; j < w.j.n; j += stride) {
+    int st = w.j.state[j];
+    if (st & kBroken) st |= kRemoved;  // Joint.initialize returns !broken
+    w.j.state[j] = st;
+    if (st) continue;
+    const int2 ab = w.j.bodies[j];
+    const D4 rA = w.j.rAD[j], rB = w.j.rBD[j], sf = w.j.stiff[j];
+    const Q4<double> qB = body_q_t(w, ab.y);
+    const D4 pB = w.b.pos[ab.y];
+    V3<double> pa, dpt;
+    Q4<double> qA{0, 0, 0, 1};
+    if (ab.x >= 0) {
+      qA = body_q_t(w, ab.x);
+      const D4 p = w.b.pos[ab.x];
+      const V3<double> r = qrotate(qA, V3<double>{rA.x, rA.y, rA.z});
+      pa = V3<double>{r.x + p.x, r.y + p.y, r.z + p.z};
+      dpt = V3<double>{p.x - pB.x, p.y - pB.y, p.z - pB.z};
+    } else {
+      pa = V3<double>{rA.x, rA.y, rA.z};
+      dpt = V3<double>{rA.x - pB.x, rA.y - pB.y, rA.z - pB.z};
+    }
+    const V3<double> rb = qrotate(qB, V3<double>{rB.x, rB.y, rB.z});
+    const V3<double> pb{rb.x + pB.x, rb.y + pB.y, rb.z + pB.z};
+    const V3<double> c0l = pa - pb;
+    const V3<double> c0a = qsub(qA, qB) * sf.w;
+    w.j.c0Lin[j] = make_float4((float)c0l.x, (float)c0l.y, (float)c0l.z, 0.f);
+    w.j.c0Ang[j] = make_float4((float)c0a.x, (float)c0a.y, (float)c0a.z, 0.f);
+    w.j.dpt[j] = make_float4((float)dpt.x, (float)dpt.y, (float)dpt.z, 0.f);
+    w.j.dptD[j] = mkd4(dpt.x, dpt.y, dpt.z, 0.0);
+    D4 ll = w.j.lamLin[j], la = w.j.lamAng[j];
+    if (!P.postStabilize) {
+      ll.x = ll.x * P.alpha * P.gamma; ll.y = ll.y * P.alpha * P.gamma; ll.z = ll.z * P.alpha * P.gamma;
+      la.x = la.x * P.alpha * P.gamma; la.y = la.y * P.alpha * P.gamma; la.z = la.z * P.alpha * P.gamma;
+    }
+    w.j.lamLin[j] = ll;
+    w.j.lamAng[j] = la;
+    float4 kl = w.j.penLin[j], ka = w.j.penAng[j];
+    auto warm = [&](float k, double cap) {
+      return (float)jsmin(clampd((double)k * P.gamma, P.penaltyMin, P.penaltyMax), cap);
+    };
+    kl = make_float4(warm(kl.x, sf.x), warm(kl.y, sf.x), warm(kl.z, sf.x), 0.f);
+    ka = make_float4(warm(ka.x, sf.y), warm(ka.y, sf.y), warm(ka.z, sf.y), 0.f);
+    w.j.penLin[j] = kl;
+    w.j.penAng[j] = ka;
+  }
+  for (int s = tid; s < w.s.n; s += stride) {
+    int st = w.s.state[s];
+    if (st & kRemoved) continue;
+    const int2 ab = w.s.bodies[s];
+    const D4 prm = w.s.prm[s];
+    const D4 pA = w.b.pos[ab.x], pB = w.b.pos[ab.y];
+    const V3<double> dpt{pA.x - pB.x, pA.y - pB.y, pA.z - pB.z};
+    w.s.dpt[s] = make_float4((float)dpt.x, (float)dpt.y, (float)dpt.z, 0.f);
+    w.s.dptD[s] = mkd4(dpt.x, dpt.y, dpt.z, 0.0);
+    if (st & kBroken) {
+      w.s.penalty[s] = 0.f;
+      continue;
+    }
+    if (isfinite(prm.z)) {  // tear check at x_t (spring.js:484-490)
+      const D4 rA = w.s.rAD[s], rB = w.s.rBD[s];
+      const V3<double> ra = qrotate(body_q_t(w, ab.x), V3<double>{rA.x, rA.y, rA.z});
+      const V3<double> rb = qrotate(body_q_t(w, ab.y), V3<double>{rB.x, rB.y, rB.z});
+      const V3<double> d{(ra.x + pA.x) - (rb.x + pB.x), (ra.y + pA.y) - (rb.y + pB.y),
+                         (ra.z + pA.z) - (rb.z + pB.z)};
+      const double len = sqrt(d.x * d.x + d.y * d.y + d.z * d.z);
+      if (len > 1.0e-6 && prm.y > 1.0e-6) {
+        const double strain = jsmax(0.0, (len - prm.y) / prm.y);
+        w.s.peak[s] = jsmax(w.s.peak[s], strain);
+        if (strain > prm.z) {
+          w.s.state[s] = st | kBroken;
+          w.s.penalty[s] = 0.f;
+          continue;
+        }
+      }
+    }
+    if (!P.springRamp) {
+      w.s.penalty[s] = (float)prm.x;
+    } else {
+      double k = clampd((double)w.s.penalty[s] * P.gamma, P.penaltyMin, P.penaltyMax);
+      w.s.penalty[s] = (float)jsmin(k, prm.x);
+    }
+    if (!(prm.x > 0)) w.s.state[s] = st | kRemoved;
+  }
+}
+
+// solver.js:369-401, in delta form.
+__global__ void prepare_bodies_kernel(World w) {
+  const SolverParams &P = w.p;
+  const double dt = P.dt, g = P.gravity;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < w.b.n; i += gridDim.x * blockDim.x) {
+    const float4 qf = w.b.quat[i], vf = w.b.vel[i], wf = w.b.omega[i], pv = w.b.prevVel[i];
+    const double mass = w.b.massD[i].x;
+    const Q4<double> q{qf.x, qf.y, qf.z, qf.w};
+    const V3<double> wdt{(double)wf.x * dt, (double)wf.y * dt, (double)wf.z * dt};
+    V3<double> y{(double)vf.x * dt, (double)vf.y * dt, (double)vf.z * dt};
+    if (mass > 0) y.z += g * (dt * dt);
+    const Q4<double> qy = qintegrate(q, wdt);
+    const double accelZ = ((double)vf.z - (double)pv.z) / dt;
+    const double sgn = g < 0 ? -1.0 : (g > 0 ? 1.0 : 0.0);
+    double weight = clampd(accelZ * sgn / fabs(g), 0.0, 1.0);
+    if (!isfinite(weight)) weight = 0.0;
+    w.b.quatT[i] = qf;
+    w.b.yLin[i] = make_float4((float)y.x, (float)y.y, (float)y.z, 0.f);
+    w.b.yAng[i] = make_float4((float)qy.x, (float)qy.y, (float)qy.z, (float)qy.w);
+    int fl = w.b.flags0[i];
+    if (mass > 0) {
+      V3<double> d{(double)vf.x * dt, (double)vf.y * dt, (double)vf.z * dt};
+      d.z += g * (weight * dt * dt);
+      w.b.dp[i] = make_float4((float)d.x, (float)d.y, (float)d.z, 0.f);
+      w.b.dpD[i] = mkd4(d.x, d.y, d.z, 0.0);
+      w.b.quat[i] = make_float4((float)qy.x, (float)qy.y, (float)qy.z, (float)qy.w);
+      w.b.quatD[i] = mkd4(qy.x, qy.y, qy.z, qy.w);
+    } else {
+      w.b.dp[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+      w.b.dpD[i] = mkd4(0.0, 0.0, 0.0, 0.0);
+      w.b.quatD[i] = mkd4(q.x, q.y, q.z, q.w);
+    }
+    w.b.flags[i] = fl;
+    w.a.count[i] = 0;
+  }
+}
+
+// Live manifolds of this step: count the incident ones of every dynamic body.
+__global__ void adj_count_kernel(World w) {
+  const int total = w.ctl->numCandidates;
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < total; c += gridDim.x * blockDim.x) {
+    const int n = w.cur.count[c];
+    if (n <= 0) continue;
+    const uint64_t k = w.cur.key[c];
+    const int a = (int)(k >> 32), b = (int)(k & 0xffffffffu);
+    if (w.b.flags0[a] & kBodyDynamic) atomicAdd(&w.a.count[a], 1);
+    if (w.b.flags0[b] & kBodyDynamic) atomicAdd(&w.a.count[b], 1);
+    atomicAdd(&w.ctl->liveManifolds, 1);
+    atomicAdd(&w.ctl->liveContacts, n);
+  }
+}
+
+__global__ void adj_fill_kernel(World w) {
+  const int total = w.ctl->numCandidates;
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < total; c += gridDim.x * blockDim.x) {
+    if (w.cur.count[c] <= 0) continue;
+    const uint64_t k = w.cur.key[c];
+    const int a = (int)(k >> 32), b = (int)(k & 0xffffffffu);
+    if (w.b.flags0[a] & kBodyDynamic) {
+      const int at = atomicAdd(&w.a.cursor[a], 1);
+      if (at < w.a.cap) w.a.entry[at] = ((uint32_t)c << 1) | 0u;
+      else atomicOr(&w.ctl->flags, kOvfAdj);
+    }
+    if (w.b.flags0[b] & kBodyDynamic) {
+      const int at = atomicAdd(&w.a.cursor[b], 1);
+      if (at < w.a.cap) w.a.entry[at] = ((uint32_t)c << 1) | 1u;
+      else atomicOr(&w.ctl->flags, kOvfAdj);
+    }
+  }
+}
+
+// Sort each body's manifold list (determinism) and decide its precision.
+__global__ void adj_sort_kernel(World w) {
+  const double dt2 = w.p.dt * w.p.dt;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < w.b.n; i += gridDim.x * blockDim.x) {
+    int fl = w.b.flags[i];
+    if (!(fl & kBodyDynamic)) continue;
+    int beg = w.a.start[i], end = w.a.start[i + 1];
+    if (end > w.a.cap) end = w.a.cap;
+    uint32_t *e = w.a.entry;
+    for (int x = beg + 1; x < end; x++) {
+      const uint32_t v = e[x];
+      int y = x - 1;
+      while (y >= beg && e[y] > v) {
+        e[y + 1] = e[y];
+        y--;
+      }
+      e[y + 1] = v;
+    }
+    if (w.p.fp64Ratio > 0) {
+      double kmax = 0;
+      for (int k = w.g.cStart[i]; k < w.g.cStart[i + 1]; k++) {
+        const uint32_t ref = w.g.cRef[k];
+        const uint32_t type = ref >> 30, idx = (ref >> 1) & 0x1fffffffu;
+        if (type == kRefJoint) {
+          if (w.j.state[idx]) continue;
+          const float4 kl = w.j.penLin[idx];
+          const double hard = isinf(w.j.stiff[idx].x) ? w.p.penaltyMax : 0.0;
+          kmax = fmax(kmax, fmax(fmax((double)kl.x, (double)kl.y), fmax((double)kl.z, hard)));
+        } else {
+          if (w.s.state[idx]) continue;
+          kmax = fmax(kmax, (double)w.s.penalty[idx]);
+        }
+      }
+      const double inertial = w.b.massD[i].x / dt2;
+      if (kmax > w.p.fp64Ratio * inertial) {
+        fl |= kBodyFp64;
+        atomicAdd(&w.ctl->fp64Bodies, 1);
+      }
+    }
+    w.b.flags[i] = fl;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Colouring: greedy in (lowbias32(local index), index) order, computed as the
+// fixed point of in-place Jacobi rounds seeded with the previous step's
+// colours (the reference GPU's incremental colouring,
+// src/physics/gpu/shaders.js:1558-1656, run to convergence so that the result
+// is exactly the sequential greedy colouring in priority order). Then a
+// stable counting sort lists each colour's bodies in index order.
+// ---------------------------------------------------------------------------
+__device__ inline bool precedes(const World &w, int j, int i) {
+  const uint32_t pj = w.b.priority[j], pi = w.b.priority[i];
+  return pj < pi || (pj == pi && j < i);
+}
+
+template <class F>
+__device__ inline void for_each_neighbor(const World &w, int i, F &&f) {
+  int end = w.a.start[i + 1];
+  if (end > w.a.cap) end = w.a.cap;
+  for (int k = w.a.start[i]; k < end; k++) {
+    const uint32_t e = w.a.entry[k];
+    const int c = (int)(e >> 1);
+    const uint64_t key = w.cur.key[c];
+    const int other = (e & 1u) ? (int)(key >> 32) : (int)(key & 0xffffffffu);
+    if (w.b.flags0[other] & kBodyDynamic) f(other);
+  }
+  for (int k = w.g.cStart[i]; k < w.g.cStart[i + 1]; k++) {
+    const uint32_t ref = w.g.cRef[k];
+    const uint32_t type = ref >> 30, idx = (ref >> 1) & 0x1fffffffu, side = ref & 1u;
+    int2 ab;
+    if (type == kRefJoint) {
+      if (w.j.state[idx]) continue;
+      ab = w.j.bodies[idx];
+    } else {
+      if (w.s.state[idx]) continue;
+      ab = w.s.bodies[idx];
+    }
+    const int other = side ? ab.x : ab.y;
+    if (other >= 0 && (w.b.flags0[other] & kBodyDynamic)) f(other);
+  }
+}
+
+__global__ void __launch_bounds__(256) coloring_kernel(World w) {
+  Control *ctl = w.ctl;
+  const int n = w.b.n;
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x, stride = gridDim.x * blockDim.x;
+  volatile int *color = w.b.color;
+  // seed: previous colours (statics -1, new dynamic bodies 0)
+  for (int i = tid; i < n; i += stride) {
+    if (!(w.b.flags0[i] & kBodyDynamic)) color[i] = -1;
+    else if (color[i] < 0 || color[i] >= kMaxColors) color[i] = 0;
+  }
+  // "changed" flags, triple-buffered: round r sets flag r % 3 and clears the
+  // flag of round r + 1, which no block can still be reading (it was last
+  // read in round r - 2, before the barriers of round r - 1).
+  if (tid == 0) ctl->pad[1] = 0;
+  int round = 0;
+  for (;; round++) {
+    if (tid == 0) ctl->pad[1 + (round + 1) % 3] = 0;
+    if (!grid_barrier(ctl)) return;
+    int changed = 0;
+    for (int i = tid; i < n; i += stride) {
+      if (!(w.b.flags0[i] & kBodyDynamic)) continue;
+      unsigned long long used = 0ull;
+      for_each_neighbor(w, i, [&](int j) {
+        if (precedes(w, j, i)) {
+          const int c = color[j];
+          if (c >= 0 && c < kMaxColors) used |= 1ull << c;
+        }
+      });
+      int c = __ffsll((long long)~used) - 1;
+      if (c < 0) {
+        c = kMaxColors - 1;
+        atomicOr(&ctl->flags, kOvfColors);
+      }
+      if (c != color[i]) {
+        color[i] = c;
+        changed = 1;
+      }
+    }
+    if (changed) atomicOr(&ctl->pad[1 + round % 3], 1);
+    if (!grid_barrier(ctl)) return;
+    const int any = *((volatile int *)&ctl->pad[1 + round % 3]);
+    if (!any) break;
+    if (round > 4096) {
+      if (tid == 0) atomicOr(&ctl->flags, kOvfColors);
+      break;
+    }
+  }
+  // --- stable counting sort by colour (per-block chunk of body indices) ---
+  __shared__ int hist[kMaxColors];
+  __shared__ int base[kMaxColors];
+  __shared__ int warpCnt[8][kMaxColors];
+  const int chunk = (n + gridDim.x - 1) / gridDim.x;
+  const int b0 = blockIdx.x * chunk, b1 = min(n, b0 + chunk);
+  for (int c = threadIdx.x; c < kMaxColors; c += blockDim.x) hist[c] = 0;
+  __syncthreads();
+  for (int i = b0 + threadIdx.x; i < b1; i += blockDim.x) {
+    const int c = color[i];
+    if (c >= 0) atomicAdd(&hist[c], 1);
+  }
+  __syncthreads();
+  for (int c = threadIdx.x; c < kMaxColors; c += blockDim.x) w.a.blockHist[blockIdx.x * kMaxColors + c] = hist[c];
+  if (!grid_barrier(ctl)) return;
+  if (blockIdx.x == 0) {
+    __shared__ int totals[kMaxColors];
+    if (threadIdx.x < kMaxColors) {
+      const int c = threadIdx.x;
+      int run = 0;
+      for (int b = 0; b < (int)gridDim.x; b++) {
+        const int h = w.a.blockHist[b * kMaxColors + c];
+        w.a.blockHist[b * kMaxColors + c] = run;
+        run += h;
+      }
+      totals[c] = run;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      int run = 0, used = 0;
+      for (int c = 0; c < kMaxColors; c++) {
+        w.a.colorStart[c] = run;
+        run += totals[c];
+        if (totals[c] > 0) used = c + 1;
+      }
+      w.a.colorStart[kMaxColors] = run;
+      ctl->numColors = used;
+    }
+  }
+  if (!grid_barrier(ctl)) return;
+  for (int c = threadIdx.x; c < kMaxColors; c += blockDim.x)
+    base[c] = w.a.colorStart[c] + w.a.blockHist[blockIdx.x * kMaxColors + c];
+  __syncthreads();
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  for (int t0 = b0; t0 < b1; t0 += blockDim.x) {
+    for (int c = threadIdx.x; c < 8 * kMaxColors; c += blockDim.x) (&warpCnt[0][0])[c] = 0;
+    __syncthreads();
+    const int i = t0 + threadIdx.x;
+    const int c = (i < b1) ? color[i] : -1;
+    const unsigned m = __match_any_sync(0xffffffffu, c);
+    const int rankInWarp = __popc(m & ((1u << lane) - 1u));
+    if (c >= 0 && rankInWarp == 0) warpCnt[warp][c] = __popc(m);
+    __syncthreads();
+    if (c >= 0) {
+      int r = base[c] + rankInWarp;
+      for (int q = 0; q < warp; q++) r += warpCnt[q][c];
+      w.a.colorBodies[r] = i;
+    }
+    __syncthreads();
+    for (int cc = threadIdx.x; cc < kMaxColors; cc += blockDim.x) {
+      int s = 0;
+      for (int q = 0; q < 8; q++) s += warpCnt[q][cc];
+      base[cc] += s;
+    }
+    __syncthreads();
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Per-body assembly and solve
+// ---------------------------------------------------------------------------
+template <class T>
+struct Sys {  // lower triangles of the three 3x3 blocks + right-hand side
+  T l[6];  // aLin: 00 10 11 20 21 22
+  T a[6];  // aAng: same layout
+  T c[9];  // aCross row-major (rows: angular dof, cols: linear dof)
+  T bl[3], ba[3];
+};
+
+template <class T>
+__device__ inline void zero(Sys<T> &s) {
+#pragma unroll
+  for (int k = 0; k < 6; k++) s.l[k] = s.a[k] = T(0);
+#pragma unroll
+  for (int k = 0; k < 9; k++) s.c[k] = T(0);
+#pragma unroll
+  for (int k = 0; k < 3; k++) s.bl[k] = s.ba[k] = T(0);
+}
+
+template <class T>
+__device__ inline T shfl_xor(T v, int m, unsigned mask, int width) {
+  return __shfl_xor_sync(mask, v, m, width);
+}
+
+template <class T>
+__device__ inline void group_reduce(Sys<T> &s, unsigned mask, int G) {
+  for (int m = G >> 1; m > 0; m >>= 1) {
+#pragma unroll
+    for (int k = 0; k < 6; k++) {
+      s.l[k] += shfl_xor(s.l[k], m, mask, G);
+      s.a[k] += shfl_xor(s.a[k], m, mask, G);
+    }
+#pragma unroll
+    for (int k = 0; k < 9; k++) s.c[k] += shfl_xor(s.c[k], m, mask, G);
+#pragma unroll
+    for (int k = 0; k < 3; k++) {
+      s.bl[k] += shfl_xor(s.bl[k], m, mask, G);
+      s.ba[k] += shfl_xor(s.ba[k], m, mask, G);
+    }
+  }
+}
+
+// sym 3x3 lower index
+__device__ inline constexpr int L(int r, int c) { return r >= c ? (r * (r + 1)) / 2 + c : (c * (c + 1)) / 2 + r; }
+
+// H_lin += k n n^T ; H_ang += k a a^T ; H_cross += k a n^T ; b += f_lin, f_ang
+template <class T>
+__device__ inline void stamp_row(Sys<T> &s, T k, V3<T> n, V3<T> a) {
+  const T nn[3] = {n.x, n.y, n.z}, aa[3] = {a.x, a.y, a.z};
+#pragma unroll
+  for (int r = 0; r < 3; r++)
+#pragma unroll
+    for (int c = 0; c <= r; c++) {
+      s.l[L(r, c)] += k * nn[r] * nn[c];
+      s.a[L(r, c)] += k * aa[r] * aa[c];
+    }
+#pragma unroll
+  for (int r = 0; r < 3; r++)
+#pragma unroll
+    for (int c = 0; c < 3; c++) s.c[r * 3 + c] += k * aa[r] * nn[c];
+}
+
+// maths.js:660-725, unrolled LDL^T (lower storage).
+template <class T>
+__device__ inline void ldlt_solve(const Sys<T> &s, T bl0, T bl1, T bl2, T ba0, T ba1, T ba2, V3<T> &xl, V3<T> &xa) {
+  const T A11 = s.l[0], A21 = s.l[1], A22 = s.l[2], A31 = s.l[3], A32 = s.l[4], A33 = s.l[5];
+  const T A41 = s.c[0], A42 = s.c[1], A43 = s.c[2], A44 = s.a[0];
+  const T A51 = s.c[3], A52 = s.c[4], A53 = s.c[5], A54 = s.a[1], A55 = s.a[2];
+  const T A61 = s.c[6], A62 = s.c[7], A63 = s.c[8], A64 = s.a[3], A65 = s.a[4], A66 = s.a[5];
+  const T L21 = A21 / A11, L31 = A31 / A11, L41 = A41 / A11, L51 = A51 / A11, L61 = A61 / A11;
+  const T D1 = A11;
+  const T D2 = A22 - L21 * L21 * D1;
+  const T L32 = (A32 - L21 * L31 * D1) / D2;
+  const T L42 = (A42 - L21 * L41 * D1) / D2;
+  const T L52 = (A52 - L21 * L51 * D1) / D2;
+  const T L62 = (A62 - L21 * L61 * D1) / D2;
+  const T D3 = A33 - (L31 * L31 * D1 + L32 * L32 * D2);
+  const T L43 = (A43 - L31 * L41 * D1 - L32 * L42 * D2) / D3;
+  const T L53 = (A53 - L31 * L51 * D1 - L32 * L52 * D2) / D3;
+  const T L63 = (A63 - L31 * L61 * D1 - L32 * L62 * D2) / D3;
+  const T D4 = A44 - (L41 * L41 * D1 + L42 * L42 * D2 + L43 * L43 * D3);
+  const T L54 = (A54 - L41 * L51 * D1 - L42 * L52 * D2 - L43 * L53 * D3) / D4;
+  const T L64 = (A64 - L41 * L61 * D1 - L42 * L62 * D2 - L43 * L63 * D3) / D4;
+  const T D5 = A55 - (L51 * L51 * D1 + L52 * L52 * D2 + L53 * L53 * D3 + L54 * L54 * D4);
+  const T L65 = (A65 - L51 * L61 * D1 - L52 * L62 * D2 - L53 * L63 * D3 - L54 * L64 * D4) / D5;
+  const T D6 = A66 - (L61 * L61 * D1 + L62 * L62 * D2 + L63 * L63 * D3 + L64 * L64 * D4 + L65 * L65 * D5);
+  const T y1 = bl0;
+  const T y2 = bl1 - L21 * y1;
+  const T y3 = bl2 - L31 * y1 - L32 * y2;
+  const T y4 = ba0 - L41 * y1 - L42 * y2 - L43 * y3;
+  const T y5 = ba1 - L51 * y1 - L52 * y2 - L53 * y3 - L54 * y4;
+  const T y6 = ba2 - L61 * y1 - L62 * y2 - L63 * y3 - L64 * y4 - L65 * y5;
+  const T z1 = y1 / D1, z2 = y2 / D2, z3 = y3 / D3, z4 = y4 / D4, z5 = y5 / D5, z6 = y6 / D6;
+  xa.z = z6;
+  xa.y = z5 - L65 * xa.z;
+  xa.x = z4 - L54 * xa.y - L64 * xa.z;
+  xl.z = z3 - L43 * xa.x - L53 * xa.y - L63 * xa.z;
+  xl.y = z2 - L32 * xl.z - L42 * xa.x - L52 * xa.y - L62 * xa.z;
+  xl.x = z1 - L21 * xl.y - L31 * xl.z - L41 * xa.x - L51 * xa.y - L61 * xa.z;
+}
+
+template <class T>
+struct BState {
+  V3<T> dp;    // p - p_t
+  Q4<T> q;     // current orientation
+  V3<T> dang;  // qsub(q, q_t)
+};
+
+template <class T>
+__device__ inline BState<T> load_state(const World &w, int i) {
+  BState<T> s;
+  const float4 qt = ld(&w.b.quatT[i]);
+  const Q4<T> qT{(T)qt.x, (T)qt.y, (T)qt.z, (T)qt.w};
+  if (sizeof(T) == 8 && (ld(&w.b.flags[i]) & kBodyFp64)) {
+    const D4 d = ldcg(&w.b.dpD[i]), q = ldcg(&w.b.quatD[i]);
+    s.dp = V3<T>{(T)d.x, (T)d.y, (T)d.z};
+    s.q = Q4<T>{(T)q.x, (T)q.y, (T)q.z, (T)q.w};
+  } else {
+    const float4 d = ldcg(&w.b.dp[i]), q = ldcg(&w.b.quat[i]);
+    s.dp = V3<T>{(T)d.x, (T)d.y, (T)d.z};
+    s.q = Q4<T>{(T)q.x, (T)q.y, (T)q.z, (T)q.w};
+  }
+  s.dang = qsub(s.q, qT);
+  return s;
+}
+
+template <class T>
+struct ContactEval {
+  V3<T> C, F;
+  bool within;
+};
+
+// manifold.js:358-409 in delta form: C = (1 - alpha) C0 + n_r . (dx_A - dx_B),
+// dx = delta + dtheta x r_world(x_t).
+template <class T>
+__device__ inline ContactEval<T> eval_contact(const V3<T> n[3], T mu, float4 cA, float4 cB, float4 cK, float4 cL,
+                                              const BState<T> &A, const BState<T> &B, T alpha) {
+  const V3<T> rA{(T)cA.x, (T)cA.y, (T)cA.z}, rB{(T)cB.x, (T)cB.y, (T)cB.z};
+  const V3<T> u = (A.dp + cross(A.dang, rA)) - (B.dp + cross(B.dang, rB));
+  ContactEval<T> e;
+  const T om = T(1) - alpha;
+  e.C.x = om * (T)cA.w + dot(n[0], u);
+  e.C.y = om * (T)cB.w + dot(n[1], u);
+  e.C.z = om * (T)cK.w + dot(n[2], u);
+  e.F.x = (T)cK.x * e.C.x + (T)cL.x;
+  e.F.y = (T)cK.y * e.C.y + (T)cL.y;
+  e.F.z = (T)cK.z * e.C.z + (T)cL.z;
+  e.F.x = e.F.x < T(0) ? e.F.x : T(0);
+  const T bounds = fabs(e.F.x) * mu;
+  const T fs = sqrt(e.F.y * e.F.y + e.F.z * e.F.z);
+  if (fs > bounds && fs > T(0)) {
+    e.F.y *= bounds / fs;
+    e.F.z *= bounds / fs;
+  }
+  e.within = fs <= bounds;
+  return e;
+}
+
+template <class T>
+__device__ inline void manifold_rows(const World &w, int m, V3<T> n[3], T &mu, int &cnt) {
+  const float4 b0 = ld(&w.cur.basis0[m]), b1 = ld(&w.cur.basis1[m]), b2 = ld(&w.cur.basis2[m]);
+  n[0] = V3<T>{(T)b0.x, (T)b0.y, (T)b0.z};
+  n[1] = V3<T>{(T)b1.x, (T)b1.y, (T)b1.z};
+  n[2] = V3<T>{(T)b2.x, (T)b2.y, (T)b2.z};
+  mu = (T)b0.w;
+  cnt = ld(&w.cur.count[m]);
+}
+
+template <class T>
+__device__ void contact_primal(const World &w, int m, int side, const BState<T> &self, T alpha, Sys<T> &s) {
+  V3<T> n[3];
+  T mu;
+  int cnt;
+  manifold_rows(w, m, n, mu, cnt);
+  const uint64_t key = ld(&w.cur.key[m]);
+  const int other = side ? (int)(key >> 32) : (int)(key & 0xffffffffu);
+  const BState<T> o = load_state<T>(w, other);
+  const BState<T> &A = side ? o : self;
+  const BState<T> &B = side ? self : o;
+  const T sgn = side ? T(-1) : T(1);
+  for (int k = 0; k < cnt; k++) {
+    const int slot = m * kMaxContacts + k;
+    const float4 cA = ld(&w.cur.cA[slot]), cB = ld(&w.cur.cB[slot]);
+    const float4 cK = __ldcg(&w.cur.cK[slot]), cL = __ldcg(&w.cur.cL[slot]);
+    const ContactEval<T> e = eval_contact(n, mu, cA, cB, cK, cL, A, B, alpha);
+    const V3<T> r = side ? V3<T>{(T)cB.x, (T)cB.y, (T)cB.z} : V3<T>{(T)cA.x, (T)cA.y, (T)cA.z};
+    const T kk[3] = {(T)cK.x, (T)cK.y, (T)cK.z};
+    const T ff[3] = {e.F.x, e.F.y, e.F.z};
+#pragma unroll
+    for (int row = 0; row < 3; row++) {
+      const V3<T> a = cross(r, n[row]);
+      stamp_row(s, kk[row], n[row], a);
+      const T f = sgn * ff[row];
+      s.bl[0] += f * n[row].x; s.bl[1] += f * n[row].y; s.bl[2] += f * n[row].z;
+      s.ba[0] += f * a.x; s.ba[1] += f * a.y; s.ba[2] += f * a.z;
+    }
+  }
+}
+
+template <class T>
+__device__ void contact_dual(const World &w, int m, int side, const BState<T> &self, T alpha) {
+  V3<T> n[3];
+  T mu;
+  int cnt;
+  manifold_rows(w, m, n, mu, cnt);
+  const uint64_t key = ld(&w.cur.key[m]);
+  const int ia = (int)(key >> 32), ib = (int)(key & 0xffffffffu);
+  const BState<T> o = load_state<T>(w, side ? ia : ib);
+  const BState<T> &A = side ? o : self;
+  const BState<T> &B = side ? self : o;
+  const bool sphere = ((ld(&w.b.flags0[ia]) | ld(&w.b.flags0[ib])) & kBodySphere) != 0;
+  const T beta = (T)w.p.betaLin, kmax = (T)w.p.penaltyMax, thr = (T)w.p.stickThreshold;
+  for (int k = 0; k < cnt; k++) {
+    const int slot = m * kMaxContacts + k;
+    const float4 cA = ld(&w.cur.cA[slot]), cB = ld(&w.cur.cB[slot]);
+    float4 cK = __ldcg(&w.cur.cK[slot]), cL = __ldcg(&w.cur.cL[slot]);
+    const ContactEval<T> e = eval_contact(n, mu, cA, cB, cK, cL, A, B, alpha);
+    float stick = cL.w;
+    if (e.F.x < T(0)) cK.x = (float)fmin((T)cK.x + beta * fabs(e.C.x), kmax);
+    if (e.within) {
+      cK.y = (float)fmin((T)cK.y + beta * fabs(e.C.y), kmax);
+      cK.z = (float)fmin((T)cK.z + beta * fabs(e.C.z), kmax);
+      stick = sqrt(e.C.y * e.C.y + e.C.z * e.C.z) < thr ? 1.f : 0.f;
+    } else if (sphere) {
+      stick = 0.f;
+    }
+    __stcg(&w.cur.cK[slot], cK);
+    __stcg(&w.cur.cL[slot], make_float4((float)e.F.x, (float)e.F.y, (float)e.F.z, stick));
+  }
+}
+
+// Joint geometry at the current iterate (joint.js:115-129), delta form.
+template <class T>
+struct JointGeo {
+  V3<T> Clin, Cang;
+  V3<T> rAw, rBw;
+};
+
+template <class T>
+__device__ inline JointGeo<T> joint_geo(const World &w, int j, int2 ab, const BState<T> &A, const BState<T> &B,
+                                        bool hasA) {
+  JointGeo<T> g;
+  V3<T> dpt;
+  if (sizeof(T) == 8) {
+    const D4 d = ld(&w.j.dptD[j]);
+    dpt = V3<T>{(T)d.x, (T)d.y, (T)d.z};
+  } else {
+    const float4 d = ld(&w.j.dpt[j]);
+    dpt = V3<T>{(T)d.x, (T)d.y, (T)d.z};
+  }
+  const float4 ra = ld(&w.j.rAF[j]), rb = ld(&w.j.rBF[j]);
+  const D4 raD = ld(&w.j.rAD[j]), rbD = ld(&w.j.rBD[j]);
+  const V3<T> rAl = sizeof(T) == 8 ? V3<T>{(T)raD.x, (T)raD.y, (T)raD.z} : V3<T>{(T)ra.x, (T)ra.y, (T)ra.z};
+  const V3<T> rBl = sizeof(T) == 8 ? V3<T>{(T)rbD.x, (T)rbD.y, (T)rbD.z} : V3<T>{(T)rb.x, (T)rb.y, (T)rb.z};
+  g.rBw = qrotate(B.q, rBl);
+  if (hasA) {
+    g.rAw = qrotate(A.q, rAl);
+    g.Clin = ((dpt + (A.dp - B.dp)) + g.rAw) - g.rBw;
+  } else {
+    g.rAw = V3<T>{0, 0, 0};
+    g.Clin = (dpt - B.dp) - g.rBw;
+  }
+  const Q4<T> qA = hasA ? A.q : Q4<T>{0, 0, 0, 1};
+  g.Cang = qsub(qA, B.q) * (T)ld(&w.j.stiff[j]).w;
+  return g;
+}
+
+template <class T>
+__device__ void joint_primal(const World &w, int j, int side, const BState<T> &self, T alpha, Sys<T> &s) {
+  if (__ldcg(&w.j.state[j])) return;
+  const int2 ab = ld(&w.j.bodies[j]);
+  const bool hasA = ab.x >= 0;
+  BState<T> o;
+  if (side == 0) o = load_state<T>(w, ab.y);
+  else if (hasA) o = load_state<T>(w, ab.x);
+  const BState<T> &A = side ? o : self;
+  const BState<T> &B = side ? self : o;
+  const JointGeo<T> g = joint_geo(w, j, ab, A, B, hasA);
+  const D4 sf = ld(&w.j.stiff[j]);
+  const float4 kl = __ldcg(&w.j.penLin[j]);
+  if (kl.x * kl.x + kl.y * kl.y + kl.z * kl.z > 0.f) {
+    const D4 lam = ldcg(&w.j.lamLin[j]);
+    const float4 c0 = ld(&w.j.c0Lin[j]);
+    V3<T> C = g.Clin;
+    if (isinf(sf.x)) C = C - V3<T>{(T)c0.x, (T)c0.y, (T)c0.z} * alpha;
+    const T K[3] = {(T)kl.x, (T)kl.y, (T)kl.z};
+    const T F[3] = {K[0] * C.x + (T)lam.x, K[1] * C.y + (T)lam.y, K[2] * C.z + (T)lam.z};
+    // A: jLin = I, jAng = skew(-rAw), r = rAw ; B: jLin = -I, jAng = skew(rBw), r = -rBw
+    const V3<T> v = side ? g.rBw : -g.rAw;
+    const V3<T> r = side ? -g.rBw : g.rAw;
+    const T sl = side ? T(-1) : T(1);
+    // skew(v) rows: [0,-vz,vy],[vz,0,-vx],[-vy,vx,0]
+    const T S[9] = {T(0), -v.z, v.y, v.z, T(0), -v.x, -v.y, v.x, T(0)};
+#pragma unroll
+    for (int rr = 0; rr < 3; rr++) s.l[L(rr, rr)] += K[rr];
+    // jAng^T K jAng  and  jAng^T K jLin = sl * (S^T K)
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+#pragma unroll
+      for (int b = 0; b <= a; b++) {
+        T acc = T(0);
+#pragma unroll
+        for (int q = 0; q < 3; q++) acc += S[q * 3 + a] * K[q] * S[q * 3 + b];
+        s.a[L(a, b)] += acc;
+      }
+#pragma unroll
+      for (int b = 0; b < 3; b++) s.c[a * 3 + b] += sl * S[b * 3 + a] * K[b];
+    }
+    // geometric stiffness (joint.js:214-221): H = -(F.r) I + r F^T, column-norm lumped
+    const T fr = F[0] * r.x + F[1] * r.y + F[2] * r.z;
+    const T rv[3] = {r.x, r.y, r.z};
+#pragma unroll
+    for (int col = 0; col < 3; col++) {
+      T n2 = T(0);
+#pragma unroll
+      for (int row = 0; row < 3; row++) {
+        const T h = (row == col ? -fr : T(0)) + rv[row] * F[col];
+        n2 += h * h;
+      }
+      s.a[L(col, col)] += sqrt(n2);
+    }
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+      s.bl[a] += sl * F[a];
+      s.ba[a] += S[0 * 3 + a] * F[0] + S[1 * 3 + a] * F[1] + S[2 * 3 + a] * F[2];
+    }
+  }
+  const float4 ka = __ldcg(&w.j.penAng[j]);
+  if (ka.x * ka.x + ka.y * ka.y + ka.z * ka.z > 0.f) {
+    const D4 lam = ldcg(&w.j.lamAng[j]);
+    const float4 c0 = ld(&w.j.c0Ang[j]);
+    V3<T> C = g.Cang;
+    if (isinf(sf.y)) C = C - V3<T>{(T)c0.x, (T)c0.y, (T)c0.z} * alpha;
+    const T st = side ? -(T)sf.w : (T)sf.w;
+    const T K[3] = {(T)ka.x, (T)ka.y, (T)ka.z};
+    const T F[3] = {K[0] * C.x + (T)lam.x, K[1] * C.y + (T)lam.y, K[2] * C.z + (T)lam.z};
+#pragma unroll
+    for (int a = 0; a < 3; a++) {
+      s.a[L(a, a)] += st * K[a] * st;
+      s.ba[a] += st * F[a];
+    }
+  }
+}
+
+template <class T>
+__device__ void joint_dual(const World &w, int j, int side, const BState<T> &self, T alpha) {
+  if (__ldcg(&w.j.state[j])) return;
+  const int2 ab = ld(&w.j.bodies[j]);
+  const bool hasA = ab.x >= 0;
+  BState<T> o;
+  if (side == 0) o = load_state<T>(w, ab.y);
+  else if (hasA) o = load_state<T>(w, ab.x);
+  const BState<T> &A = side ? o : self;
+  const BState<T> &B = side ? self : o;
+  const JointGeo<T> g = joint_geo(w, j, ab, A, B, hasA);
+  const D4 sf = ld(&w.j.stiff[j]);
+  const double kmax = w.p.penaltyMax;
+  float4 kl = __ldcg(&w.j.penLin[j]);
+  D4 ll = ldcg(&w.j.lamLin[j]);
+  if (kl.x * kl.x + kl.y * kl.y + kl.z * kl.z > 0.f) {
+    V3<T> C = g.Clin;
+    if (isinf(sf.x)) {
+      const float4 c0 = ld(&w.j.c0Lin[j]);
+      C = C - V3<T>{(T)c0.x, (T)c0.y, (T)c0.z} * alpha;
+      ll.x = (double)kl.x * (double)C.x + ll.x;
+      ll.y = (double)kl.y * (double)C.y + ll.y;
+      ll.z = (double)kl.z * (double)C.z + ll.z;
+    }
+    const double cap = fmin(sf.x, kmax);
+    kl.x = (float)fmin((double)kl.x + w.p.betaLin * fabs((double)C.x), cap);
+    kl.y = (float)fmin((double)kl.y + w.p.betaLin * fabs((double)C.y), cap);
+    kl.z = (float)fmin((double)kl.z + w.p.betaLin * fabs((double)C.z), cap);
+  }
+  float4 ka = __ldcg(&w.j.penAng[j]);
+  D4 la = ldcg(&w.j.lamAng[j]);
+  if (ka.x * ka.x + ka.y * ka.y + ka.z * ka.z > 0.f) {
+    V3<T> C = g.Cang;
+    if (isinf(sf.y)) {
+      const float4 c0 = ld(&w.j.c0Ang[j]);
+      C = C - V3<T>{(T)c0.x, (T)c0.y, (T)c0.z} * alpha;
+      la.x = (double)ka.x * (double)C.x + la.x;
+      la.y = (double)ka.y * (double)C.y + la.y;
+      la.z = (double)ka.z * (double)C.z + la.z;
+    }
+    const double cap = fmin(sf.y, kmax);
+    ka.x = (float)fmin((double)ka.x + w.p.betaAng * fabs((double)C.x), cap);
+    ka.y = (float)fmin((double)ka.y + w.p.betaAng * fabs((double)C.y), cap);
+    ka.z = (float)fmin((double)ka.z + w.p.betaAng * fabs((double)C.z), cap);
+  }
+  // fracture on |lambda_ang| (joint.js:307-316)
+  if (la.x * la.x + la.y * la.y + la.z * la.z > sf.z * sf.z) {
+    kl = make_float4(0.f, 0.f, 0.f, 0.f);
+    ka = kl;
+    ll = mkd4(0, 0, 0, 0);
+    la = ll;
+    __stcg(&w.j.state[j], kBroken);
+  }
+  __stcg(&w.j.penLin[j], kl);
+  __stcg(&w.j.penAng[j], ka);
+  stcg(&w.j.lamLin[j], ll);
+  stcg(&w.j.lamAng[j], la);
+}
+
+// spring.js:447-458: d, |d| and C at the current iterate.
+template <class T>
+__device__ inline bool spring_eval(const World &w, int sIdx, const BState<T> &A, const BState<T> &B, V3<T> &d,
+                                   T &len, V3<T> &rAw, V3<T> &rBw) {
+  V3<T> dpt, rAl, rBl;
+  if (sizeof(T) == 8) {
+    const D4 x = ld(&w.s.dptD[sIdx]), a = ld(&w.s.rAD[sIdx]), b = ld(&w.s.rBD[sIdx]);
+    dpt = V3<T>{(T)x.x, (T)x.y, (T)x.z};
+    rAl = V3<T>{(T)a.x, (T)a.y, (T)a.z};
+    rBl = V3<T>{(T)b.x, (T)b.y, (T)b.z};
+  } else {
+    const float4 x = ld(&w.s.dpt[sIdx]), a = ld(&w.s.rAF[sIdx]), b = ld(&w.s.rBF[sIdx]);
+    dpt = V3<T>{(T)x.x, (T)x.y, (T)x.z};
+    rAl = V3<T>{(T)a.x, (T)a.y, (T)a.z};
+    rBl = V3<T>{(T)b.x, (T)b.y, (T)b.z};
+  }
+  rAw = qrotate(A.q, rAl);
+  rBw = qrotate(B.q, rBl);
+  d = ((dpt + (A.dp - B.dp)) + rAw) - rBw;
+  len = sqrt(dot(d, d));
+  return len > T(1.0e-6);
+}
+
+template <class T>
+__device__ void spring_primal(const World &w, int sIdx, int side, const BState<T> &self, Sys<T> &s) {
+  if (__ldcg(&w.s.state[sIdx])) return;
+  const int2 ab = ld(&w.s.bodies[sIdx]);
+  const BState<T> o = load_state<T>(w, side ? ab.x : ab.y);
+  const BState<T> &A = side ? o : self;
+  const BState<T> &B = side ? self : o;
+  V3<T> d, rAw, rBw;
+  T len;
+  if (!spring_eval(w, sIdx, A, B, d, len, rAw, rBw)) return;
+  const T rest = (T)ld(&w.s.prm[sIdx]).y;
+  const T k = (T)__ldcg(&w.s.penalty[sIdx]);
+  const V3<T> n = d * (T(1) / len);
+  const T C = len - rest;
+  const T f = k * C;
+  const V3<T> rW = side ? rBw : rAw;
+  const V3<T> jl = side ? -n : n;
+  const V3<T> ja = side ? -cross(rW, n) : cross(rW, n);
+  stamp_row(s, k, jl, ja);
+  s.bl[0] += f * jl.x; s.bl[1] += f * jl.y; s.bl[2] += f * jl.z;
+  s.ba[0] += f * ja.x; s.ba[1] += f * ja.y; s.ba[2] += f * ja.z;
+  if (w.p.springGeometric) {  // spring.js:564-616
+    const T sg = side ? T(-1) : T(1);
+    const T nv[3] = {n.x, n.y, n.z}, rv[3] = {rW.x, rW.y, rW.z};
+    T P[9], Sk[9];
+#pragma unroll
+    for (int a = 0; a < 3; a++)
+#pragma unroll
+      for (int b = 0; b < 3; b++) P[a * 3 + b] = ((a == b ? T(1) : T(0)) - nv[a] * nv[b]) / len;
+    Sk[0] = 0; Sk[1] = -rW.z; Sk[2] = rW.y;
+    Sk[3] = rW.z; Sk[4] = 0; Sk[5] = -rW.x;
+    Sk[6] = -rW.y; Sk[7] = rW.x; Sk[8] = 0;
+    T SP[9], PS[9];
+#pragma unroll
+    for (int a = 0; a < 3; a++)
+#pragma unroll
+      for (int b = 0; b < 3; b++) {
+        SP[a * 3 + b] = Sk[a * 3] * P[b] + Sk[a * 3 + 1] * P[3 + b] + Sk[a * 3 + 2] * P[6 + b];
+        PS[a * 3 + b] = P[a * 3] * Sk[b] + P[a * 3 + 1] * Sk[3 + b] + P[a * 3 + 2] * Sk[6 + b];
+      }
+    const T ndr = dot(n, rW);
+    const T af = fabs(f);
+#pragma unroll
+    for (int c = 0; c < 3; c++) {
+      // linear column: Gll = P, Gal = S P
+      T n2 = T(0);
+#pragma unroll
+      for (int r = 0; r < 3; r++) n2 += P[r * 3 + c] * P[r * 3 + c] + SP[r * 3 + c] * SP[r * 3 + c];
+      s.l[L(c, c)] += sqrt(n2) * af;
+      // angular column: Gla = -P S, Gaa = -S P S + sg(-(n.r) I + r n^T)
+      T m2 = T(0);
+#pragma unroll
+      for (int r = 0; r < 3; r++) {
+        const T gla = -PS[r * 3 + c];
+        const T sps = SP[r * 3] * Sk[c] + SP[r * 3 + 1] * Sk[3 + c] + SP[r * 3 + 2] * Sk[6 + c];
+        const T gaa = -sps + sg * ((r == c ? -ndr : T(0)) + rv[r] * nv[c]);
+        m2 += gla * gla + gaa * gaa;
+      }
+      s.a[L(c, c)] += sqrt(m2) * af;
+    }
+  }
+}
+
+template <class T>
+__device__ void spring_dual(const World &w, int sIdx, int side, const BState<T> &self) {
+  if (__ldcg(&w.s.state[sIdx])) return;
+  const int2 ab = ld(&w.s.bodies[sIdx]);
+  const BState<T> o = load_state<T>(w, side ? ab.x : ab.y);
+  const BState<T> &A = side ? o : self;
+  const BState<T> &B = side ? self : o;
+  V3<T> d, rAw, rBw;
+  T len;
+  if (!spring_eval(w, sIdx, A, B, d, len, rAw, rBw)) return;
+  const D4 prm = ld(&w.s.prm[sIdx]);
+  const double C = (double)len - prm.y;
+  if (isfinite(prm.z) && prm.y > 1.0e-6) {  // spring.js:461-470
+    const double strain = fmax(0.0, C / prm.y);
+    double peak = __ldcg(&w.s.peak[sIdx]);
+    if (strain > peak) __stcg(&w.s.peak[sIdx], strain);
+    if (strain > prm.z) {
+      __stcg(&w.s.state[sIdx], kBroken);
+      __stcg(&w.s.penalty[sIdx], 0.f);
+      return;
+    }
+  }
+  if (!w.p.springRamp) return;
+  const double k = __ldcg(&w.s.penalty[sIdx]);
+  __stcg(&w.s.penalty[sIdx], (float)fmin(k + w.p.betaLin * fabs(C), fmin(prm.x, w.p.penaltyMax)));
+}
+
+// Owner of a constraint's dual update: its endpoint with the larger colour
+// (static endpoints have colour -1).
+__device__ inline bool owns(int myColor, int otherColor) { return myColor > otherColor; }
+
+template <class T>
+__device__ void solve_body(const World &w, int i, int lane, int G, unsigned mask, T alpha, bool dual, bool velocity) {
+  const SolverParams &P = w.p;
+  const T dt = (T)P.dt, dt2 = (T)(P.dt * P.dt);
+  BState<T> self = load_state<T>(w, i);
+  const int mStart = ld(&w.a.start[i]);
+  int mEnd = ld(&w.a.start[i + 1]);
+  if (mEnd > w.a.cap) mEnd = w.a.cap;
+  const int cStart = ld(&w.g.cStart[i]), cEnd = ld(&w.g.cStart[i + 1]);
+  const int nm = mEnd - mStart, total = nm + (cEnd - cStart);
+
+  Sys<T> s;
+  zero(s);
+  if (lane == 0) {  // inertial terms (solver.js:425-439)
+    const D4 md = ld(&w.b.massD[i]);
+    const T m = (T)md.x;
+    const T ml = m / dt2;
+    s.l[0] = ml; s.l[2] = ml; s.l[5] = ml;
+    const float4 y = ld(&w.b.yLin[i]), qy = ld(&w.b.yAng[i]);
+    const V3<T> dy = self.dp - V3<T>{(T)y.x, (T)y.y, (T)y.z};
+    s.bl[0] = ml * dy.x; s.bl[1] = ml * dy.y; s.bl[2] = ml * dy.z;
+    // world moment R I R^T (rigid.js:228-247), / dt^2
+    T M[9];
+    const bool iso = !P.rotatedInertia || (ld(&w.b.flags0[i]) & kBodySphere);
+    const T I0 = (T)md.y, I1 = (T)md.z, I2 = (T)md.w;
+    if (iso) {
+      M[0] = I0; M[1] = 0; M[2] = 0; M[3] = 0; M[4] = I1; M[5] = 0; M[6] = 0; M[7] = 0; M[8] = I2;
+    } else {
+      const Q4<T> q = self.q;
+      const T xx = q.x * q.x, yy = q.y * q.y, zz = q.z * q.z, xy = q.x * q.y, xz = q.x * q.z, yz = q.y * q.z;
+      const T wx = q.w * q.x, wy = q.w * q.y, wz = q.w * q.z;
+      const T R[9] = {T(1) - T(2) * (yy + zz), T(2) * (xy - wz), T(2) * (xz + wy),
+                      T(2) * (xy + wz), T(1) - T(2) * (xx + zz), T(2) * (yz - wx),
+                      T(2) * (xz - wy), T(2) * (yz + wx), T(1) - T(2) * (xx + yy)};
+#pragma unroll
+      for (int a = 0; a < 3; a++)
+#pragma unroll
+        for (int b = 0; b < 3; b++) M[a * 3 + b] = R[a * 3] * I0 * R[b * 3] + R[a * 3 + 1] * I1 * R[b * 3 + 1] +
+                                                  R[a * 3 + 2] * I2 * R[b * 3 + 2];
+    }
+    const V3<T> dq = qsub(self.q, Q4<T>{(T)qy.x, (T)qy.y, (T)qy.z, (T)qy.w});
+#pragma unroll
+    for (int a = 0; a < 3; a++)
+#pragma unroll
+      for (int b = 0; b <= a; b++) s.a[L(a, b)] = M[a * 3 + b] / dt2;
+    s.ba[0] = (M[0] * dq.x + M[1] * dq.y + M[2] * dq.z) / dt2;
+    s.ba[1] = (M[3] * dq.x + M[4] * dq.y + M[5] * dq.z) / dt2;
+    s.ba[2] = (M[6] * dq.x + M[7] * dq.y + M[8] * dq.z) / dt2;
+  }
+  for (int e = lane; e < total; e += G) {
+    if (e < nm) {
+      const uint32_t ent = ld(&w.a.entry[mStart + e]);
+      contact_primal<T>(w, (int)(ent >> 1), (int)(ent & 1u), self, alpha, s);
+    } else {
+      const uint32_t ref = ld(&w.g.cRef[cStart + e - nm]);
+      const uint32_t type = ref >> 30, idx = (ref >> 1) & 0x1fffffffu, side = ref & 1u;
+      if (type == kRefJoint) joint_primal<T>(w, (int)idx, (int)side, self, alpha, s);
+      else spring_primal<T>(w, (int)idx, (int)side, self, s);
+    }
+  }
+  group_reduce(s, mask, G);
+  V3<T> xl, xa;
+  ldlt_solve(s, -s.bl[0], -s.bl[1], -s.bl[2], -s.ba[0], -s.ba[1], -s.ba[2], xl, xa);
+  self.dp = self.dp + xl;
+  self.q = qintegrate(self.q, xa);
+  {
+    const float4 qt = ld(&w.b.quatT[i]);
+    self.dang = qsub(self.q, Q4<T>{(T)qt.x, (T)qt.y, (T)qt.z, (T)qt.w});
+  }
+  if (lane == 0) {
+    __stcg(&w.b.dp[i], make_float4((float)self.dp.x, (float)self.dp.y, (float)self.dp.z, 0.f));
+    __stcg(&w.b.quat[i], make_float4((float)self.q.x, (float)self.q.y, (float)self.q.z, (float)self.q.w));
+    if (sizeof(T) == 8) {
+      stcg(&w.b.dpD[i], mkd4((double)self.dp.x, (double)self.dp.y, (double)self.dp.z, 0.0));
+      stcg(&w.b.quatD[i], mkd4((double)self.q.x, (double)self.q.y, (double)self.q.z, (double)self.q.w));
+    }
+    if (velocity) {  // BDF1 (solver.js:476-488)
+      const float4 v = ld(&w.b.vel[i]);
+      w.b.prevVel[i] = v;
+      const V3<T> vn = self.dp * (T(1) / dt);
+      w.b.vel[i] = make_float4((float)(self.dp.x / dt), (float)(self.dp.y / dt), (float)(self.dp.z / dt), 0.f);
+      (void)vn;
+      w.b.omega[i] = make_float4((float)(self.dang.x / dt), (float)(self.dang.y / dt), (float)(self.dang.z / dt), 0.f);
+    }
+  }
+  if (!dual) return;
+  const int myColor = ld(&w.b.color[i]);
+  for (int e = lane; e < total; e += G) {
+    if (e < nm) {
+      const uint32_t ent = ld(&w.a.entry[mStart + e]);
+      const int m = (int)(ent >> 1), side = (int)(ent & 1u);
+      const uint64_t key = ld(&w.cur.key[m]);
+      const int other = side ? (int)(key >> 32) : (int)(key & 0xffffffffu);
+      if (owns(myColor, ld(&w.b.color[other]))) contact_dual<T>(w, m, side, self, alpha);
+    } else {
+      const uint32_t ref = ld(&w.g.cRef[cStart + e - nm]);
+      const uint32_t type = ref >> 30, idx = (ref >> 1) & 0x1fffffffu, side = ref & 1u;
+      const int2 ab = type == kRefJoint ? ld(&w.j.bodies[idx]) : ld(&w.s.bodies[idx]);
+      const int other = side ? ab.x : ab.y;
+      const int oc = other >= 0 ? ld(&w.b.color[other]) : -1;
+      if (!owns(myColor, oc)) continue;
+      if (type == kRefJoint) joint_dual<T>(w, (int)idx, (int)side, self, alpha);
+      else spring_dual<T>(w, (int)idx, (int)side, self);
+    }
+  }
+}
+
+__global__ void __launch_bounds__(kSolveBlock) solve_kernel(World w, int G) {
+  const SolverParams &P = w.p;
+  Control *ctl = w.ctl;
+  const int numColors = *((volatile int *)&ctl->numColors);
+  const int lane = threadIdx.x & (G - 1);
+  const int warpLane = threadIdx.x & 31;
+  const unsigned mask = (G == 32 ? 0xffffffffu : (((1u << G) - 1u) << (warpLane & ~(G - 1))));
+  const int group = (blockIdx.x * blockDim.x + threadIdx.x) / G;
+  const int groups = (gridDim.x * blockDim.x) / G;
+  const int total = P.iterations + (P.postStabilize ? 1 : 0);
+  for (int it = 0; it < total; it++) {
+    const double alpha = P.postStabilize ? (it < P.iterations ? 1.0 : 0.0) : P.alpha;
+    const bool dual = it < P.iterations;
+    const bool vel = it == P.iterations - 1;
+    for (int c = 0; c < numColors; c++) {
+      const int beg = ld(&w.a.colorStart[c]), end = ld(&w.a.colorStart[c + 1]);
+      for (int k = beg + group; k < end; k += groups) {
+        const int i = ld(&w.a.colorBodies[k]);
+        if (ld(&w.b.flags[i]) & kBodyFp64) solve_body<double>(w, i, lane, G, mask, alpha, dual, vel);
+        else solve_body<float>(w, i, lane, G, mask, (float)alpha, dual, vel);
+      }
+      if (!grid_barrier(ctl)) return;
+    }
+  }
+}
+
+// x_{t+1} = x_t + delta (f64); statics: prevVel <- vel (solver.js:479).
+__global__ void commit_kernel(World w) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < w.b.n; i += gridDim.x * blockDim.x) {
+    const int fl = w.b.flags[i];
+    if (!(fl & kBodyDynamic)) {
+      w.b.prevVel[i] = w.b.vel[i];
+      continue;
+    }
+    D4 p = w.b.pos[i];
+    double dx, dy, dz;
+    if (fl & kBodyFp64) {
+      const D4 d = w.b.dpD[i];
+      dx = d.x; dy = d.y; dz = d.z;
+    } else {
+      const float4 d = w.b.dp[i];
+      dx = d.x; dy = d.y; dz = d.z;
+    }
+    p.x += dx; p.y += dy; p.z += dz;
+    const float4 q = w.b.quat[i];
+    if (!isfinite(p.x + p.y + p.z) || !isfinite(q.x + q.y + q.z + q.w)) atomicOr(&w.ctl->flags, kErrNaN);
+    w.b.pos[i] = p;
+  }
+}
+
+__global__ void stats_kernel(World w, double *out) {
+  // out[0] max penetration, out[1] max |lambda|, out[2] max penalty (contacts + joints + springs)
+  double e = 0, l = 0, k = 0;
+  const int total = w.ctl->numCandidates;
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < total; c += gridDim.x * blockDim.x) {
+    const int n = w.cur.count[c];
+    for (int s = 0; s < n; s++) {
+      const float4 kk = w.cur.cK[c * kMaxContacts + s], ll = w.cur.cL[c * kMaxContacts + s];
+      l = fmax(l, fmax(fabs((double)ll.x), fmax(fabs((double)ll.y), fabs((double)ll.z))));
+      k = fmax(k, fmax((double)kk.x, fmax((double)kk.y, (double)kk.z)));
+    }
+  }
+  for (int j = blockIdx.x * blockDim.x + threadIdx.x; j < w.j.n; j += gridDim.x * blockDim.x) {
+    if (w.j.state[j] & kRemoved) continue;
+    const D4 a = w.j.lamLin[j], b = w.j.lamAng[j];
+    l = fmax(l, sqrt(fmax(a.x * a.x + a.y * a.y + a.z * a.z, b.x * b.x + b.y * b.y + b.z * b.z)));
+    const float4 p = w.j.penLin[j], q = w.j.penAng[j];
+    k = fmax(k, fmax(fmax((double)p.x, fmax((double)p.y, (double)p.z)), fmax((double)q.x, fmax((double)q.y, (double)q.z))));
+  }
+  typedef cub::BlockReduce<double, 256> R;
+  __shared__ typename R::TempStorage t0, t1, t2;
+  const double me = R(t0).Reduce(e, ::cuda::maximum<>{});
+  const double ml = R(t1).Reduce(l, ::cuda::maximum<>{});
+  const double mk = R(t2).Reduce(k, ::cuda::maximum<>{});
+  if (threadIdx.x == 0) {
+    // non-negative doubles order like their bit patterns
+    atomicMax(reinterpret_cast<unsigned long long *>(&out[0]), __double_as_longlong(me));
+    atomicMax(reinterpret_cast<unsigned long long *>(&out[1]), __double_as_longlong(ml));
+    atomicMax(reinterpret_cast<unsigned long long *>(&out[2]), __double_as_longlong(mk));
+  }
+}
+
+}  // namespace
+
+size_t solver_temp_bytes(int n) {
+  size_t a = 0;
+  cub::DeviceScan::ExclusiveSum(nullptr, a, (int *)nullptr, (int *)nullptr, n + 1);
+  return a;
+}
+
+void launch_prepare(const World &w, void *temp, size_t tempBytes, cudaStream_t st, int smCount) {
+  const int blocks = smCount * 4;
+  prepare_forces_kernel<<<blocks, 256, 0, st>>>(w);
+  prepare_bodies_kernel<<<blocks, 256, 0, st>>>(w);
+  cudaMemsetAsync(w.a.count + w.b.n, 0, sizeof(int), st);
+  adj_count_kernel<<<blocks, 256, 0, st>>>(w);
+  size_t tb = tempBytes;
+  cub::DeviceScan::ExclusiveSum(temp, tb, w.a.count, w.a.start, w.b.n + 1, st);
+  cudaMemcpyAsync(w.a.cursor, w.a.start, sizeof(int) * w.b.n, cudaMemcpyDeviceToDevice, st);
+  adj_fill_kernel<<<blocks, 256, 0, st>>>(w);
+  adj_sort_kernel<<<blocks, 256, 0, st>>>(w);
+}
+
+static int coloring_blocks(int smCount) {
+  int perSm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, coloring_kernel, 256, 0);
+  if (perSm > 2) perSm = 2;
+  return perSm * smCount;
+}
+
+int coloring_grid(int smCount) { return coloring_blocks(smCount); }
+
+cudaError_t launch_coloring(const World &w, cudaStream_t st, int smCount) {
+  World arg = w;
+  void *args[] = {&arg};
+  return cudaLaunchCooperativeKernel((void *)coloring_kernel, dim3(coloring_blocks(smCount)), dim3(256), args, 0,
+                                     st);
+}
+
+int solve_max_blocks_per_sm(int lanesPerBody) {
+  (void)lanesPerBody;
+  int perSm = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, solve_kernel, kSolveBlock, 0);
+  return perSm;
+}
+
+cudaError_t launch_solve(const World &w, int lanesPerBody, int blocksPerSm, cudaStream_t st, int smCount) {
+  World arg = w;
+  int G = lanesPerBody;
+  void *args[] = {&arg, &G};
+  return cudaLaunchCooperativeKernel((void *)solve_kernel, dim3(blocksPerSm * smCount), dim3(kSolveBlock), args, 0,
+                                     st);
+}
+
+void launch_commit(const World &w, cudaStream_t st, int smCount) { commit_kernel<<<smCount * 4, 256, 0, st>>>(w); }
+
+void launch_stats(const World &w, double *out3, cudaStream_t st, int smCount) {
+  cudaMemsetAsync(out3, 0, sizeof(double) * 3, st);
+  stats_kernel<<<smCount * 2, 256, 0, st>>>(w, out3);
+}
+
+}  // namespace avbd
