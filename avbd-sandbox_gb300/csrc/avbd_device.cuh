@@ -149,7 +149,7 @@ struct Grid {
   int4 *cellLo, *cellHi;     // per body, w = scene
   unsigned tableMask;
   int *tableCount, *tableStart, *tableCursor;
-  int *entries;
+  int4 *entries;  // (body, cell x, cell y, cell z)
   int entryCap;
   int *pairCount, *pairStart;  // per body, pairStart has n + 1 entries
   uint64_t *candKey;

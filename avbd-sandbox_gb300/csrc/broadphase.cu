@@ -113,7 +113,7 @@ __global__ void scatter_kernel(World w) {
       for (int y = lo.y; y <= hi.y; y++)
         for (int z = lo.z; z <= hi.z; z++) {
           const int at = atomicAdd(&w.g.tableCursor[cell_hash(x, y, z, lo.w) & w.g.tableMask], 1);
-          if (at < w.g.entryCap) w.g.entries[at] = i;
+          if (at < w.g.entryCap) w.g.entries[at] = make_int4(i, x, y, z);
           else atomicOr(&w.ctl->flags, kOvfCells);
         }
   }
@@ -150,8 +150,10 @@ __device__ void partners_small(const World &w, int a, int prevCount, F &&f) {
         int end = beg + w.g.tableCount[bucket];
         if (end > w.g.entryCap) end = w.g.entryCap;
         for (int k = beg; k < end; k++) {
-          const int b = w.g.entries[k];
-          if (b >= a) continue;
+          // entries carry their cell: other cells hashing to this bucket are skipped
+          const int4 ent = w.g.entries[k];
+          const int b = ent.x;
+          if (b >= a || ent.y != x || ent.z != y || ent.w != z) continue;
           const int4 bl = w.g.cellLo[b], bh = w.g.cellHi[b];
           if (bl.w != s) continue;
           // the pair is found once: in the minimum corner of the AABB overlap

@@ -57,6 +57,9 @@ struct avbd_ctx {
   int curIsA = 1;
   avbd_profile prof{};
   cudaEvent_t ev[8]{};
+  // pinned staging of the per-step body state (upload / readback)
+  D4 *hPos = nullptr;
+  float4 *hQuat = nullptr, *hVel = nullptr, *hOmega = nullptr, *hPrev = nullptr;
 };
 
 namespace {
@@ -100,6 +103,11 @@ int upload(avbd_ctx *ctx, T **p, const std::vector<T> &h) {
 void free_all(avbd_ctx *ctx) {
   for (void *p : ctx->allocs) cudaFree(p);
   ctx->allocs.clear();
+  void *pinned[5] = {ctx->hPos, ctx->hQuat, ctx->hVel, ctx->hOmega, ctx->hPrev};
+  for (void *p : pinned)
+    if (p) cudaFreeHost(p);
+  ctx->hPos = nullptr;
+  ctx->hQuat = ctx->hVel = ctx->hOmega = ctx->hPrev = nullptr;
   ctx->packed = false;
 }
 
@@ -132,29 +140,29 @@ int record(avbd_ctx *ctx, int k) {
 
 // Upload the dynamic state (bodies, joints, springs, and manifolds when
 // given) of `world` into already-sized arenas.
-int write_state(avbd_ctx *ctx, const avbd_world *world) {
+int write_state(avbd_ctx *ctx, const avbd_world *world, bool keepManifolds) {
   const avbd_body_soa &B = world->bodies;
   const int n = ctx->n;
-  std::vector<D4> pos(n);
-  std::vector<float4> quat(n), vel(n), omg(n), pv(n);
   for (int i = 0; i < n; i++) {
     const double *p = &B.pos[i * 3];
     if (!finite3(p)) return fail(ctx, AVBD_ERR_NAN, "body %d: non-finite position", i);
-    pos[i] = mkd4(p[0], p[1], p[2], 0.0);
+    ctx->hPos[i] = mkd4(p[0], p[1], p[2], 0.0);
     const double *q = B.quat ? &B.quat[i * 4] : nullptr;
-    quat[i] = q ? make_float4((float)q[0], (float)q[1], (float)q[2], (float)q[3]) : make_float4(0, 0, 0, 1);
+    ctx->hQuat[i] = q ? make_float4((float)q[0], (float)q[1], (float)q[2], (float)q[3]) : make_float4(0, 0, 0, 1);
     auto v3 = [&](const double *a) { return a ? make_float4((float)a[i * 3], (float)a[i * 3 + 1], (float)a[i * 3 + 2], 0.f)
                                               : make_float4(0, 0, 0, 0); };
-    vel[i] = v3(B.vel);
-    omg[i] = v3(B.omega);
-    pv[i] = B.prev_vel ? v3(B.prev_vel) : vel[i];
+    ctx->hVel[i] = v3(B.vel);
+    ctx->hOmega[i] = v3(B.omega);
+    ctx->hPrev[i] = B.prev_vel ? v3(B.prev_vel) : ctx->hVel[i];
   }
   World &w = ctx->w;
-  CK(cudaMemcpy(w.b.pos, pos.data(), n * sizeof(D4), cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(w.b.quat, quat.data(), n * sizeof(float4), cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(w.b.vel, vel.data(), n * sizeof(float4), cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(w.b.omega, omg.data(), n * sizeof(float4), cudaMemcpyHostToDevice));
-  CK(cudaMemcpy(w.b.prevVel, pv.data(), n * sizeof(float4), cudaMemcpyHostToDevice));
+  cudaStream_t st = ctx->stream;
+  CK(cudaMemcpyAsync(w.b.pos, ctx->hPos, n * sizeof(D4), cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(w.b.quat, ctx->hQuat, n * sizeof(float4), cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(w.b.vel, ctx->hVel, n * sizeof(float4), cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(w.b.omega, ctx->hOmega, n * sizeof(float4), cudaMemcpyHostToDevice, st));
+  CK(cudaMemcpyAsync(w.b.prevVel, ctx->hPrev, n * sizeof(float4), cudaMemcpyHostToDevice, st));
+  CK(cudaStreamSynchronize(st));
 
   const avbd_joint_soa &J = world->joints;
   if (ctx->nj) {
@@ -241,11 +249,13 @@ int write_state(avbd_ctx *ctx, const avbd_world *world) {
     CK(cudaMemcpy(pm.cK, cK.data(), cK.size() * sizeof(float4), cudaMemcpyHostToDevice));
     CK(cudaMemcpy(pm.cL, cL.data(), cL.size() * sizeof(float4), cudaMemcpyHostToDevice));
   }
-  Control c{};
-  CK(cudaMemcpy(&c, w.ctl, sizeof(Control), cudaMemcpyDeviceToHost));
-  c.prevCandidates = live;
-  c.numCandidates = 0;
-  CK(cudaMemcpy(w.ctl, &c, sizeof(Control), cudaMemcpyHostToDevice));
+  if (M.count > 0 || !keepManifolds) {
+    Control c{};
+    CK(cudaMemcpy(&c, w.ctl, sizeof(Control), cudaMemcpyDeviceToHost));
+    c.prevCandidates = live;
+    c.numCandidates = 0;
+    CK(cudaMemcpy(w.ctl, &c, sizeof(Control), cudaMemcpyHostToDevice));
+  }
   return AVBD_OK;
 }
 
@@ -258,29 +268,30 @@ int one_step(avbd_ctx *ctx) {
   int rc;
   if ((rc = record(ctx, 0))) return rc;
   launch_broadphase_impl(w, ctx->numLarge, ctx->bpTemp, ctx->bpTempBytes, st, ctx->smCount);
-  ctx->launches += 9 + (ctx->numLarge > 0 ? 2 : 0);
+  ctx->launches += 6 + (ctx->numLarge > 0 ? 2 : 0);  // own kernels (the two scans are library code)
   if ((rc = record(ctx, 1))) return rc;
   launch_narrowphase(w, st, ctx->smCount);
   ctx->launches += 1;
   if ((rc = record(ctx, 2))) return rc;
   launch_prepare(w, ctx->svTemp, ctx->svTempBytes, st, ctx->smCount);
-  ctx->launches += 6;
+  ctx->launches += 5;
   if ((rc = record(ctx, 3))) return rc;
   CK(launch_coloring(w, st, ctx->smCount));
   ctx->launches += 1;
   if ((rc = record(ctx, 4))) return rc;
   CK(launch_solve(w, ctx->lanes, ctx->blocksPerSm, st, ctx->smCount));
   ctx->launches += 1;
+  if ((rc = record(ctx, 5))) return rc;
   launch_commit(w, st, ctx->smCount);
   ctx->launches += 1;
   // this step's candidates become next step's previous manifolds
   CK(cudaMemcpyAsync(&w.ctl->prevCandidates, &w.ctl->numCandidates, sizeof(int), cudaMemcpyDeviceToDevice, st));
-  if ((rc = record(ctx, 5))) return rc;
+  if ((rc = record(ctx, 6))) return rc;
   CK(cudaGetLastError());
   ctx->curIsA ^= 1;
   ctx->steps++;
   if (ctx->profiling) {
-    CK(cudaEventSynchronize(ctx->ev[5]));
+    CK(cudaEventSynchronize(ctx->ev[6]));
     float t[5];
     for (int k = 0; k < 5; k++) cudaEventElapsedTime(&t[k], ctx->ev[k], ctx->ev[k + 1]);
     ctx->prof.broadphase_ms = t[0];
@@ -289,7 +300,7 @@ int one_step(avbd_ctx *ctx) {
     ctx->prof.coloring_ms = t[3];
     ctx->prof.solve_ms = t[4];
     float tot = 0;
-    cudaEventElapsedTime(&tot, ctx->ev[0], ctx->ev[5]);
+    cudaEventElapsedTime(&tot, ctx->ev[0], ctx->ev[6]);
     ctx->prof.step_ms = tot;
   }
   return AVBD_OK;
@@ -607,10 +618,15 @@ int avbd_pack(avbd_ctx *ctx, const avbd_world *world) {
   if (ctx->blocksPerSm < 1) return fail(ctx, AVBD_ERR_CUDA, "solve kernel cannot be made resident");
   // colours start at 0 for dynamic bodies
   CK(cudaMemset(w.b.color, 0, sizeof(int) * n));
+  CK(cudaMallocHost((void **)&ctx->hPos, sizeof(D4) * n));
+  CK(cudaMallocHost((void **)&ctx->hQuat, sizeof(float4) * n));
+  CK(cudaMallocHost((void **)&ctx->hVel, sizeof(float4) * n));
+  CK(cudaMallocHost((void **)&ctx->hOmega, sizeof(float4) * n));
+  CK(cudaMallocHost((void **)&ctx->hPrev, sizeof(float4) * n));
   ctx->packed = true;
   ctx->steps = 0;
   ctx->launches = 0;
-  rc = write_state(ctx, world);
+  rc = write_state(ctx, world, false);
   if (rc) return rc;
   CK(cudaDeviceSynchronize());
   return AVBD_OK;
@@ -641,13 +657,15 @@ int avbd_read_state(avbd_ctx *ctx, avbd_world *out) {
   const int n = ctx->n;
   avbd_body_soa &B = out->bodies;
   if (B.count < n) return fail(ctx, AVBD_ERR_ARG, "avbd_read_state: body arrays hold %d < %d", B.count, n);
-  std::vector<D4> pos(n);
-  std::vector<float4> q(n), v(n), om(n), pv(n);
-  CK(cudaMemcpy(pos.data(), w.b.pos, n * sizeof(D4), cudaMemcpyDeviceToHost));
-  CK(cudaMemcpy(q.data(), w.b.quat, n * sizeof(float4), cudaMemcpyDeviceToHost));
-  CK(cudaMemcpy(v.data(), w.b.vel, n * sizeof(float4), cudaMemcpyDeviceToHost));
-  CK(cudaMemcpy(om.data(), w.b.omega, n * sizeof(float4), cudaMemcpyDeviceToHost));
-  CK(cudaMemcpy(pv.data(), w.b.prevVel, n * sizeof(float4), cudaMemcpyDeviceToHost));
+  cudaStream_t st = ctx->stream;
+  CK(cudaMemcpyAsync(ctx->hPos, w.b.pos, n * sizeof(D4), cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(ctx->hQuat, w.b.quat, n * sizeof(float4), cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(ctx->hVel, w.b.vel, n * sizeof(float4), cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(ctx->hOmega, w.b.omega, n * sizeof(float4), cudaMemcpyDeviceToHost, st));
+  CK(cudaMemcpyAsync(ctx->hPrev, w.b.prevVel, n * sizeof(float4), cudaMemcpyDeviceToHost, st));
+  CK(cudaStreamSynchronize(st));
+  const D4 *pos = ctx->hPos;
+  const float4 *q = ctx->hQuat, *v = ctx->hVel, *om = ctx->hOmega, *pv = ctx->hPrev;
   for (int i = 0; i < n; i++) {
     if (B.pos) { B.pos[i * 3] = pos[i].x; B.pos[i * 3 + 1] = pos[i].y; B.pos[i * 3 + 2] = pos[i].z; }
     if (B.quat) { B.quat[i * 4] = q[i].x; B.quat[i * 4 + 1] = q[i].y; B.quat[i * 4 + 2] = q[i].z; B.quat[i * 4 + 3] = q[i].w; }
@@ -758,7 +776,7 @@ int avbd_write_state(avbd_ctx *ctx, const avbd_world *world) {
   if (world->bodies.count != ctx->n || world->joints.count != ctx->nj || world->springs.count != ctx->ns)
     return fail(ctx, AVBD_ERR_ARG, "avbd_write_state: topology differs from the packed world");
   CK(cudaStreamSynchronize(ctx->stream));
-  return write_state(ctx, world);
+  return write_state(ctx, world, true);
 }
 
 int avbd_read_coloring(avbd_ctx *ctx, int32_t *color_of, int32_t *num_colors) {

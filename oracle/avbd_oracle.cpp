@@ -797,7 +797,8 @@ struct Solver {
   int lastNumColors = 0;
   std::vector<int64_t> lastPairs;   // manifolds initialised in the last step, (A<<32)|B
   Collider collider;
-  std::vector<Force *> graveyard;   // removed forces, freed with the solver
+  std::vector<Force *> graveyard;   // removed joints/springs, freed with the solver
+  std::vector<Force *> manifoldPool;  // recycled manifolds (solver.js:68-73)
   ~Solver();
 };
 
@@ -1331,6 +1332,7 @@ Solver::~Solver() {
   for (Body *b : bodies) delete b;
   for (Force *f : forces) delete f;
   for (Force *f : graveyard) delete f;
+  for (Force *f : manifoldPool) delete f;
 }
 
 // ---------------------------------------------------------------------------
@@ -1530,7 +1532,17 @@ static void step(Solver &s) {
     const double r = A->radius + B->radius;
     if (dx * dx + dy * dy + dz * dz <= r * r && !A->constrainedTo(B)) {
       if (A->mass > 0 || B->mass > 0) {
-        Manifold *m = new Manifold();
+        // Manifold.reinit (manifold.js:201-212) on a pooled manifold, or a new one
+        Manifold *m;
+        if (!s.manifoldPool.empty()) {
+          m = static_cast<Manifold *>(s.manifoldPool.back());
+          s.manifoldPool.pop_back();
+          m->numContacts = 0;
+          m->friction = 0;
+          for (int i = 0; i < MAX_CONTACTS; i++) m->contacts[i].reset();
+        } else {
+          m = new Manifold();
+        }
         m->solver = &s;
         m->bodyA = A;
         m->bodyB = B;
@@ -1564,7 +1576,8 @@ static void step(Solver &s) {
           auto it = std::find(b->forces.begin(), b->forces.end(), f);
           if (it != b->forces.end()) b->forces.erase(it);
         }
-        s.graveyard.push_back(f);
+        if (f->kind == KIND_MANIFOLD) s.manifoldPool.push_back(f);
+        else s.graveyard.push_back(f);
       }
     }
     forces.resize(write);
