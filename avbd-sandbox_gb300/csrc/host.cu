@@ -60,6 +60,10 @@ struct avbd_ctx {
   // pinned staging of the per-step body state (upload / readback)
   D4 *hPos = nullptr;
   float4 *hQuat = nullptr, *hVel = nullptr, *hOmega = nullptr, *hPrev = nullptr;
+  // candidate count of the latest completed step (pinned, written by the stream)
+  int *hCand = nullptr;
+  std::vector<void *> growable;  // arenas sized by the candidate capacity
+  int64_t regrows = 0;
 };
 
 namespace {
@@ -93,6 +97,15 @@ int dalloc(avbd_ctx *ctx, T **p, size_t count) {
 }
 
 template <class T>
+int galloc(avbd_ctx *ctx, T **p, size_t count) {
+  int rc = dalloc(ctx, p, count);
+  if (rc) return rc;
+  ctx->allocs.pop_back();
+  ctx->growable.push_back(*p);
+  return AVBD_OK;
+}
+
+template <class T>
 int upload(avbd_ctx *ctx, T **p, const std::vector<T> &h) {
   int rc = dalloc(ctx, p, h.size());
   if (rc) return rc;
@@ -103,6 +116,10 @@ int upload(avbd_ctx *ctx, T **p, const std::vector<T> &h) {
 void free_all(avbd_ctx *ctx) {
   for (void *p : ctx->allocs) cudaFree(p);
   ctx->allocs.clear();
+  for (void *p : ctx->growable) cudaFree(p);
+  ctx->growable.clear();
+  if (ctx->hCand) cudaFreeHost(ctx->hCand);
+  ctx->hCand = nullptr;
   void *pinned[5] = {ctx->hPos, ctx->hQuat, ctx->hVel, ctx->hOmega, ctx->hPrev};
   for (void *p : pinned)
     if (p) cudaFreeHost(p);
@@ -111,16 +128,79 @@ void free_all(avbd_ctx *ctx) {
   ctx->packed = false;
 }
 
+void set_world_manifolds(avbd_ctx *ctx) {
+  ctx->w.cur = ctx->curIsA ? ctx->mA : ctx->mB;
+  ctx->w.prev = ctx->curIsA ? ctx->mB : ctx->mA;
+}
+
 int alloc_manifolds(avbd_ctx *ctx, Manifolds &m, int cap) {
   int rc = 0;
   m.cap = cap;
   const size_t S = (size_t)cap * kMaxContacts;
-  if ((rc = dalloc(ctx, &m.key, cap)) || (rc = dalloc(ctx, &m.count, cap)) || (rc = dalloc(ctx, &m.basis0, cap)) ||
-      (rc = dalloc(ctx, &m.basis1, cap)) || (rc = dalloc(ctx, &m.basis2, cap)) ||
-      (rc = dalloc(ctx, &m.basisD, (size_t)cap * 9)) || (rc = dalloc(ctx, &m.feat, S)) ||
-      (rc = dalloc(ctx, &m.rA, S)) || (rc = dalloc(ctx, &m.rB, S)) || (rc = dalloc(ctx, &m.cA, S)) ||
-      (rc = dalloc(ctx, &m.cB, S)) || (rc = dalloc(ctx, &m.cK, S)) || (rc = dalloc(ctx, &m.cL, S)))
+  if ((rc = galloc(ctx, &m.key, cap)) || (rc = galloc(ctx, &m.count, cap)) || (rc = galloc(ctx, &m.basis0, cap)) ||
+      (rc = galloc(ctx, &m.basis1, cap)) || (rc = galloc(ctx, &m.basis2, cap)) ||
+      (rc = galloc(ctx, &m.basisD, (size_t)cap * 9)) || (rc = galloc(ctx, &m.feat, S)) ||
+      (rc = galloc(ctx, &m.rA, S)) || (rc = galloc(ctx, &m.rB, S)) || (rc = galloc(ctx, &m.cA, S)) ||
+      (rc = galloc(ctx, &m.cB, S)) || (rc = galloc(ctx, &m.cK, S)) || (rc = galloc(ctx, &m.cL, S)))
     return rc;
+  return AVBD_OK;
+}
+
+// Arenas whose size follows the candidate capacity: both manifold buffers,
+// the candidate keys and the per-body adjacency.
+int alloc_candidate_arenas(avbd_ctx *ctx, int cap) {
+  int rc;
+  World &w = ctx->w;
+  ctx->candCap = cap;
+  ctx->adjCap = (int)std::min<long long>(2LL * cap, 0x3fffffff);
+  w.g.candCap = cap;
+  w.a.cap = ctx->adjCap;
+  if ((rc = alloc_manifolds(ctx, ctx->mA, cap)) || (rc = alloc_manifolds(ctx, ctx->mB, cap)) ||
+      (rc = galloc(ctx, &w.g.candKey, cap)) || (rc = galloc(ctx, &w.g.candPrev, cap)) ||
+      (rc = galloc(ctx, &w.a.entry, ctx->adjCap)))
+    return rc;
+  return AVBD_OK;
+}
+
+// Overflow-driven regrow (src/physics/gpu/backend.js:1683-1739), done ahead
+// of the overflow: when the last completed step used more than 70% of the
+// candidate capacity, the arenas double and the previous step's manifolds
+// (the warm-start state) move into the new ones.
+int maybe_regrow(avbd_ctx *ctx) {
+  const int last = *((volatile int *)ctx->hCand);
+  if (last * 10LL <= ctx->candCap * 7LL) return AVBD_OK;
+  CK(cudaStreamSynchronize(ctx->stream));
+  Control c{};
+  CK(cudaMemcpy(&c, ctx->w.ctl, sizeof(Control), cudaMemcpyDeviceToHost));
+  const int keep = c.prevCandidates;
+  const Manifolds old = ctx->curIsA ? ctx->mB : ctx->mA;  // last step's arena
+  std::vector<void *> oldBufs;
+  oldBufs.swap(ctx->growable);
+  const int cap = (int)std::min<long long>(std::max<long long>(2LL * ctx->candCap, 2LL * last), 0x3fffffff);
+  int rc = alloc_candidate_arenas(ctx, cap);
+  if (rc) {
+    for (void *p : oldBufs) cudaFree(p);
+    return rc;
+  }
+  ctx->curIsA = 1;  // the new "previous" arena is mB
+  Manifolds &pm = ctx->mB;
+  const size_t K = kMaxContacts;
+  if (keep > 0) {
+    CK(cudaMemcpy(pm.key, old.key, keep * sizeof(uint64_t), cudaMemcpyDeviceToDevice));
+    CK(cudaMemcpy(pm.count, old.count, keep * sizeof(int), cudaMemcpyDeviceToDevice));
+    CK(cudaMemcpy(pm.basis0, old.basis0, keep * sizeof(float4), cudaMemcpyDeviceToDevice));
+    CK(cudaMemcpy(pm.basis1, old.basis1, keep * sizeof(float4), cudaMemcpyDeviceToDevice));
+    CK(cudaMemcpy(pm.basis2, old.basis2, keep * sizeof(float4), cudaMemcpyDeviceToDevice));
+    CK(cudaMemcpy(pm.basisD, old.basisD, keep * 9 * sizeof(double), cudaMemcpyDeviceToDevice));
+    CK(cudaMemcpy(pm.feat, old.feat, keep * K * sizeof(uint32_t), cudaMemcpyDeviceToDevice));
+    float4 *dst[6] = {pm.rA, pm.rB, pm.cA, pm.cB, pm.cK, pm.cL};
+    float4 *src[6] = {old.rA, old.rB, old.cA, old.cB, old.cK, old.cL};
+    for (int k = 0; k < 6; k++) CK(cudaMemcpy(dst[k], src[k], keep * K * sizeof(float4), cudaMemcpyDeviceToDevice));
+  }
+  CK(cudaDeviceSynchronize());
+  for (void *p : oldBufs) cudaFree(p);
+  set_world_manifolds(ctx);
+  ctx->regrows++;
   return AVBD_OK;
 }
 
@@ -128,10 +208,6 @@ inline uint32_t priority_of(uint32_t local) { return color_priority(local); }
 
 bool finite3(const double *p) { return std::isfinite(p[0]) && std::isfinite(p[1]) && std::isfinite(p[2]); }
 
-void set_world_manifolds(avbd_ctx *ctx) {
-  ctx->w.cur = ctx->curIsA ? ctx->mA : ctx->mB;
-  ctx->w.prev = ctx->curIsA ? ctx->mB : ctx->mA;
-}
 
 int record(avbd_ctx *ctx, int k) {
   if (ctx->profiling) CK(cudaEventRecord(ctx->ev[k], ctx->stream));
@@ -260,6 +336,8 @@ int write_state(avbd_ctx *ctx, const avbd_world *world, bool keepManifolds) {
 }
 
 int one_step(avbd_ctx *ctx) {
+  int rg = maybe_regrow(ctx);
+  if (rg) return rg;
   World &w = ctx->w;
   set_world_manifolds(ctx);
   cudaStream_t st = ctx->stream;
@@ -286,6 +364,7 @@ int one_step(avbd_ctx *ctx) {
   ctx->launches += 1;
   // this step's candidates become next step's previous manifolds
   CK(cudaMemcpyAsync(&w.ctl->prevCandidates, &w.ctl->numCandidates, sizeof(int), cudaMemcpyDeviceToDevice, st));
+  CK(cudaMemcpyAsync(ctx->hCand, &w.ctl->numCandidates, sizeof(int), cudaMemcpyDeviceToHost, st));
   if ((rc = record(ctx, 6))) return rc;
   CK(cudaGetLastError());
   ctx->curIsA ^= 1;
@@ -515,13 +594,12 @@ int avbd_pack(avbd_ctx *ctx, const avbd_world *world) {
     }
     insertions += c;
   }
-  const int pairsPerBody = std::max(ctx->params.max_pairs_per_body, 12);
+  const int pairsPerBody = ctx->params.max_pairs_per_body > 0 ? ctx->params.max_pairs_per_body : 16;
   const int cellFactor = std::max(ctx->params.reserved0, 1);
-  ctx->candCap = (int)std::min<long long>((long long)n * pairsPerBody + 4096 + world->manifolds.count, 0x3fffffff);
+  ctx->candCap = (int)std::min<long long>((long long)n * pairsPerBody + 256 + world->manifolds.count, 0x3fffffff);
   ctx->entryCap = (int)std::min<long long>(insertions * 2 * cellFactor + 4096, 0x3fffffff);
   ctx->tableSize = 1024;
   while (ctx->tableSize < ctx->entryCap * 2) ctx->tableSize *= 2;
-  ctx->adjCap = (int)std::min<long long>(2LL * ctx->candCap * std::max(ctx->params.max_adjacency, 1) / 1, 0x3fffffff);
 
   World &w = ctx->w;
   w = World{};
@@ -588,19 +666,20 @@ int avbd_pack(avbd_ctx *ctx, const avbd_world *world) {
   if ((rc = dalloc(ctx, &w.g.cellLo, n)) || (rc = dalloc(ctx, &w.g.cellHi, n)) ||
       (rc = dalloc(ctx, &w.g.tableCount, ctx->tableSize)) || (rc = dalloc(ctx, &w.g.tableStart, ctx->tableSize)) ||
       (rc = dalloc(ctx, &w.g.tableCursor, ctx->tableSize)) || (rc = dalloc(ctx, &w.g.entries, ctx->entryCap)) ||
-      (rc = dalloc(ctx, &w.g.pairCount, n + 1)) || (rc = dalloc(ctx, &w.g.pairStart, n + 1)) ||
-      (rc = dalloc(ctx, &w.g.candKey, ctx->candCap)) || (rc = dalloc(ctx, &w.g.candPrev, ctx->candCap)))
+      (rc = dalloc(ctx, &w.g.pairCount, n + 1)) || (rc = dalloc(ctx, &w.g.pairStart, n + 1)))
     return rc;
   // adjacency + colouring
   w.a.cap = ctx->adjCap;
   ctx->colorBlocks = std::max(1, coloring_grid(ctx->smCount));
   if ((rc = dalloc(ctx, &w.a.start, n + 1)) || (rc = dalloc(ctx, &w.a.count, n + 1)) ||
-      (rc = dalloc(ctx, &w.a.cursor, n + 1)) || (rc = dalloc(ctx, &w.a.entry, ctx->adjCap)) ||
+      (rc = dalloc(ctx, &w.a.cursor, n + 1)) ||
       (rc = dalloc(ctx, &w.a.colorStart, kMaxColors + 1)) || (rc = dalloc(ctx, &w.a.colorBodies, n)) ||
       (rc = dalloc(ctx, &w.a.blockHist, (size_t)ctx->colorBlocks * kMaxColors)))
     return rc;
-  // manifolds (double-buffered)
-  if ((rc = alloc_manifolds(ctx, ctx->mA, ctx->candCap)) || (rc = alloc_manifolds(ctx, ctx->mB, ctx->candCap))) return rc;
+  // manifolds (double-buffered), candidate keys, adjacency
+  if ((rc = alloc_candidate_arenas(ctx, ctx->candCap))) return rc;
+  CK(cudaMallocHost((void **)&ctx->hCand, sizeof(int)));
+  *ctx->hCand = 0;
   ctx->curIsA = 1;
   set_world_manifolds(ctx);
   if ((rc = dalloc(ctx, &w.ctl, 1)) || (rc = dalloc(ctx, &ctx->statsOut, 3))) return rc;

@@ -169,3 +169,21 @@ def test_determinism(abi, scenes, backend_mod):
         gpu.idle()
         outs.append(gpu.read_state().pos.copy())
     assert np.array_equal(outs[0], outs[1])
+
+
+def test_arena_regrow_preserves_results(abi, scenes, backend_mod):
+    """Overflow-driven regrow (src/physics/gpu/backend.js:1683-1739): with a
+    candidate arena sized just above the first step's need, the library grows
+    it ahead of overflow, carries the warm-start manifolds over, and the
+    trajectory is bit-identical to a run with ample capacity."""
+    s = scenes.pyramid(layers=10)
+    outs = []
+    for cap in (0, 9):
+        params = abi.default_params(**s.params, body_order=abi.ORDER_PRIORITY, max_pairs_per_body=cap)
+        gpu = backend_mod.GpuBackend(params)
+        gpu.pack(s.world())
+        gpu.step(40)
+        gpu.idle()
+        assert gpu.last_stats["overflow"] == 0
+        outs.append(gpu.read_state().pos.copy())
+    assert np.array_equal(outs[0], outs[1])
