@@ -1069,7 +1069,15 @@ __device__ void solve_body(const World &w, int i, int lane, int G, unsigned mask
   }
 }
 
-__global__ void __launch_bounds__(kSolveBlock) solve_kernel(World w, int G) {
+// The FP64 path is kept out of line so that its register demand (and any
+// spills under the 2-blocks-per-SM bound) stays in the rare FP64 bodies
+// instead of lowering the occupancy of the FP32 path.
+__device__ __noinline__ void solve_body_f64(const World &w, int i, int lane, int G, unsigned mask, double alpha,
+                                            bool dual, bool velocity) {
+  solve_body<double>(w, i, lane, G, mask, alpha, dual, velocity);
+}
+
+__global__ void __launch_bounds__(kSolveBlock, 2) solve_kernel(World w, int G) {
   const SolverParams &P = w.p;
   Control *ctl = w.ctl;
   const int numColors = *((volatile int *)&ctl->numColors);
@@ -1087,7 +1095,7 @@ __global__ void __launch_bounds__(kSolveBlock) solve_kernel(World w, int G) {
       const int beg = ld(&w.a.colorStart[c]), end = ld(&w.a.colorStart[c + 1]);
       for (int k = beg + group; k < end; k += groups) {
         const int i = ld(&w.a.colorBodies[k]);
-        if (ld(&w.b.flags[i]) & kBodyFp64) solve_body<double>(w, i, lane, G, mask, alpha, dual, vel);
+        if (ld(&w.b.flags[i]) & kBodyFp64) solve_body_f64(w, i, lane, G, mask, alpha, dual, vel);
         else solve_body<float>(w, i, lane, G, mask, (float)alpha, dual, vel);
       }
       if (!grid_barrier(ctl)) return;
