@@ -166,6 +166,12 @@ struct Adjacency {
   int *cursor;  // n
   uint32_t *entry;  // (manifold << 1) | side
   int cap;
+  // per-contact adjacency of dynamic bodies: (slot << 1 | side, other body),
+  // slot = manifold * 8 + contact; in manifold order, then contact order
+  int *cstart;   // n + 1
+  int *ccount;   // n
+  int2 *centry;
+  int ccap;
   int *colorStart;   // kMaxColors + 1
   int *colorBodies;  // dynamic bodies sorted by (colour, index)
   int *blockHist;    // colouring counting sort scratch

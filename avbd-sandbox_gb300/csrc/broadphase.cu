@@ -171,16 +171,6 @@ __device__ void partners_small(const World &w, int a, int prevCount, F &&f) {
   }
 }
 
-__global__ void count_kernel(World w) {
-  const int prevCount = w.ctl->prevCandidates;
-  for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < w.b.n; a += gridDim.x * blockDim.x) {
-    if (is_large(w, a)) continue;  // large_count_kernel
-    int c = 0;
-    partners_small(w, a, prevCount, [&](int) { c++; });
-    w.g.pairCount[a] = c;
-  }
-}
-
 // One block per large body: every body b < a of its scene is tested.
 __global__ void large_count_kernel(World w, int numLarge) {
   const int prevCount = w.ctl->prevCandidates;
@@ -215,25 +205,112 @@ __device__ void sort_segment(uint64_t *k, int n) {
   }
 }
 
-__global__ void write_kernel(World w) {
+// Warp-cooperative enumeration of the partners b < a of a non-large body a:
+// lanes split its cells (and its old manifolds and the scene's large bodies),
+// calling f(b) on the lane that finds b. Each partner is found exactly once.
+template <class F>
+__device__ void warp_partners(const World &w, int a, int prevCount, int lane, F &&f) {
+  const int4 lo = w.g.cellLo[a], hi = w.g.cellHi[a];
+  const int s = lo.w;
+  for (int k = w.g.largeStart[s] + lane; k < w.g.largeStart[s + 1]; k += 32) {
+    const int b = w.g.largeList[k];
+    if (b < a && accept(w, a, b)) f(b);
+  }
+  const int nx = hi.x - lo.x + 1, ny = hi.y - lo.y + 1, nz = hi.z - lo.z + 1;
+  const int ncell = (nx > 0 && ny > 0 && nz > 0) ? nx * ny * nz : 0;
+  for (int ci = lane; ci < ncell; ci += 32) {
+    const int x = lo.x + ci / (ny * nz), y = lo.y + (ci / nz) % ny, z = lo.z + ci % nz;
+    const uint32_t bucket = cell_hash(x, y, z, s) & w.g.tableMask;
+    const int beg = w.g.tableStart[bucket];
+    int end = beg + w.g.tableCount[bucket];
+    if (end > w.g.entryCap) end = w.g.entryCap;
+    for (int k = beg; k < end; k++) {
+      // entries carry their cell: other cells hashing to this bucket are skipped
+      const int4 ent = w.g.entries[k];
+      const int b = ent.x;
+      if (b >= a || ent.y != x || ent.z != y || ent.w != z) continue;
+      const int4 bl = w.g.cellLo[b], bh = w.g.cellHi[b];
+      if (bl.w != s) continue;
+      // the pair is found once: in the minimum corner of the AABB overlap
+      if (max(lo.x, bl.x) != x || max(lo.y, bl.y) != y || max(lo.z, bl.z) != z) continue;
+      if (x > bh.x || y > bh.y || z > bh.z) continue;
+      if (accept(w, a, b)) f(b);
+    }
+  }
+  int first = 0, last = 0;
+  if (lane == 0) prev_range(w, a, prevCount, first, last);
+  first = __shfl_sync(0xffffffffu, first, 0);
+  last = __shfl_sync(0xffffffffu, last, 0);
+  for (int m = first + lane; m < last; m += 32) {
+    if (w.prev.count[m] <= 0) continue;
+    const int b = (int)(w.prev.key[m] & 0xffffffffu);
+    if (!accept(w, a, b)) f(b);  // accepted ones were found above
+  }
+}
+
+constexpr int kWarpsPerBlock = 8;
+constexpr int kSegCap = 128;  // partners sorted in shared memory; longer lists take the serial path
+
+__global__ void __launch_bounds__(256) count_kernel(World w) {
+  const int prevCount = w.ctl->prevCandidates;
+  const int lane = threadIdx.x & 31;
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, warps = (gridDim.x * blockDim.x) >> 5;
+  for (int a = warp; a < w.b.n; a += warps) {
+    if (is_large(w, a)) continue;  // large_count_kernel
+    int c = 0;
+    warp_partners(w, a, prevCount, lane, [&](int) { c++; });
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
+    if (lane == 0) w.g.pairCount[a] = c;
+  }
+}
+
+__global__ void __launch_bounds__(256) write_kernel(World w) {
+  __shared__ uint32_t buf[kWarpsPerBlock][kSegCap];
+  __shared__ int fill[kWarpsPerBlock];
   const int prevCount = w.ctl->prevCandidates;
   const int cap = w.g.candCap;
-  for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < w.b.n; a += gridDim.x * blockDim.x) {
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, warps = (gridDim.x * blockDim.x) >> 5;
+  for (int a = warp; a < w.b.n; a += warps) {
     if (is_large(w, a)) continue;
     const int beg = w.g.pairStart[a];
     const int n = w.g.pairStart[a + 1] - beg;
     if (beg + n > cap) {
-      atomicOr(&w.ctl->flags, kOvfPairs);
+      if (lane == 0) atomicOr(&w.ctl->flags, kOvfPairs);
       continue;
     }
-    int c = 0;
+    if (n == 0) continue;
     uint64_t *seg = w.g.candKey + beg;
     const uint64_t hiKey = (uint64_t)(uint32_t)a << 32;
-    partners_small(w, a, prevCount, [&](int b) {
-      if (c < n) seg[c] = hiKey | (uint32_t)b;
-      c++;
+    if (n > kSegCap) {  // rare: serial write + sort on lane 0
+      if (lane == 0) {
+        int c = 0;
+        partners_small(w, a, prevCount, [&](int b) {
+          if (c < n) seg[c] = hiKey | (uint32_t)b;
+          c++;
+        });
+        sort_segment(seg, n);
+      }
+      __syncwarp();
+      continue;
+    }
+    if (lane == 0) fill[wib] = 0;
+    __syncwarp();
+    warp_partners(w, a, prevCount, lane, [&](int b) {
+      const int at = atomicAdd(&fill[wib], 1);
+      if (at < kSegCap) buf[wib][at] = (uint32_t)b;
     });
-    sort_segment(seg, n);
+    __syncwarp();
+    const int m = min(fill[wib], n);
+    // rank sort (partners are distinct): element i goes to #{j : b_j < b_i}
+    for (int i = lane; i < m; i += 32) {
+      const uint32_t v = buf[wib][i];
+      int r = 0;
+      for (int j = 0; j < m; j++) r += buf[wib][j] < v ? 1 : 0;
+      seg[r] = hiKey | v;
+    }
+    __syncwarp();
   }
 }
 
@@ -333,11 +410,12 @@ void launch_broadphase_impl(const World &w, int numLarge, void *temp, size_t tem
   scatter_kernel<<<blocks, 256, 0, st>>>(w);
   // pairCount[n] = 0 so the scan over n + 1 entries yields the total at [n]
   cudaMemsetAsync(w.g.pairCount + n, 0, sizeof(int), st);
-  count_kernel<<<blocks, 128, 0, st>>>(w);
+  const int warpBlocks = (int)std::min<long long>(((long long)n + 7) / 8, (long long)smCount * 32);
+  count_kernel<<<warpBlocks, 256, 0, st>>>(w);
   if (numLarge > 0) large_count_kernel<<<numLarge < 1024 ? numLarge : 1024, 256, 0, st>>>(w, numLarge);
   tb = tempBytes;
   cub::DeviceScan::ExclusiveSum(temp, tb, w.g.pairCount, w.g.pairStart, n + 1, st);
-  write_kernel<<<blocks, 128, 0, st>>>(w);
+  write_kernel<<<warpBlocks, 256, 0, st>>>(w);
   if (numLarge > 0) large_write_kernel<<<numLarge < 1024 ? numLarge : 1024, 256, 0, st>>>(w, numLarge);
   finish_kernel<<<1, 1, 0, st>>>(w);
   prev_index_kernel<<<blocks, 256, 0, st>>>(w);

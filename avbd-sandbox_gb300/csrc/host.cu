@@ -64,6 +64,11 @@ struct avbd_ctx {
   int *hCand = nullptr;
   std::vector<void *> growable;  // arenas sized by the candidate capacity
   int64_t regrows = 0;
+  // The host runs at most kRunAhead steps ahead of the device, so the
+  // candidate count the regrow check reads is at most that many steps old.
+  static constexpr int kRunAhead = 4;
+  cudaEvent_t stepEv[8]{};
+  int64_t stepSeq = 0;
 };
 
 namespace {
@@ -155,9 +160,10 @@ int alloc_candidate_arenas(avbd_ctx *ctx, int cap) {
   ctx->adjCap = (int)std::min<long long>(2LL * cap, 0x3fffffff);
   w.g.candCap = cap;
   w.a.cap = ctx->adjCap;
+  w.a.ccap = (int)std::min<long long>(2LL * kMaxContacts * cap, 0x7fffffff);
   if ((rc = alloc_manifolds(ctx, ctx->mA, cap)) || (rc = alloc_manifolds(ctx, ctx->mB, cap)) ||
       (rc = galloc(ctx, &w.g.candKey, cap)) || (rc = galloc(ctx, &w.g.candPrev, cap)) ||
-      (rc = galloc(ctx, &w.a.entry, ctx->adjCap)))
+      (rc = galloc(ctx, &w.a.entry, ctx->adjCap)) || (rc = galloc(ctx, &w.a.centry, w.a.ccap)))
     return rc;
   return AVBD_OK;
 }
@@ -336,6 +342,8 @@ int write_state(avbd_ctx *ctx, const avbd_world *world, bool keepManifolds) {
 }
 
 int one_step(avbd_ctx *ctx) {
+  if (ctx->stepSeq >= avbd_ctx::kRunAhead)
+    CK(cudaEventSynchronize(ctx->stepEv[(ctx->stepSeq - avbd_ctx::kRunAhead) % 8]));
   int rg = maybe_regrow(ctx);
   if (rg) return rg;
   World &w = ctx->w;
@@ -366,6 +374,8 @@ int one_step(avbd_ctx *ctx) {
   CK(cudaMemcpyAsync(&w.ctl->prevCandidates, &w.ctl->numCandidates, sizeof(int), cudaMemcpyDeviceToDevice, st));
   CK(cudaMemcpyAsync(ctx->hCand, &w.ctl->numCandidates, sizeof(int), cudaMemcpyDeviceToHost, st));
   if ((rc = record(ctx, 6))) return rc;
+  CK(cudaEventRecord(ctx->stepEv[ctx->stepSeq % 8], st));
+  ctx->stepSeq++;
   CK(cudaGetLastError());
   ctx->curIsA ^= 1;
   ctx->steps++;
@@ -443,6 +453,7 @@ int avbd_create(const avbd_params *params, avbd_ctx **out) {
   if (e == cudaSuccess) e = cudaDeviceGetAttribute(&coop, cudaDevAttrCooperativeLaunch, ctx->device);
   if (e == cudaSuccess) e = cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking);
   for (int k = 0; k < 8 && e == cudaSuccess; k++) e = cudaEventCreate(&ctx->ev[k]);
+  for (int k = 0; k < 8 && e == cudaSuccess; k++) e = cudaEventCreateWithFlags(&ctx->stepEv[k], cudaEventDisableTiming);
   if (e != cudaSuccess || !coop) {
     g_create_error_buf = std::string("avbd_create: ") + (e != cudaSuccess ? cudaGetErrorString(e)
                                                                           : "device lacks cooperative launch");
@@ -459,6 +470,8 @@ int avbd_destroy(avbd_ctx *ctx) {
   cudaStreamSynchronize(ctx->stream);
   free_all(ctx);
   for (auto &e : ctx->ev)
+    if (e) cudaEventDestroy(e);
+  for (auto &e : ctx->stepEv)
     if (e) cudaEventDestroy(e);
   if (ctx->stream) cudaStreamDestroy(ctx->stream);
   delete ctx;
@@ -672,7 +685,8 @@ int avbd_pack(avbd_ctx *ctx, const avbd_world *world) {
   w.a.cap = ctx->adjCap;
   ctx->colorBlocks = std::max(1, coloring_grid(ctx->smCount));
   if ((rc = dalloc(ctx, &w.a.start, n + 1)) || (rc = dalloc(ctx, &w.a.count, n + 1)) ||
-      (rc = dalloc(ctx, &w.a.cursor, n + 1)) ||
+      (rc = dalloc(ctx, &w.a.cursor, n + 1)) || (rc = dalloc(ctx, &w.a.cstart, n + 1)) ||
+      (rc = dalloc(ctx, &w.a.ccount, n + 1)) ||
       (rc = dalloc(ctx, &w.a.colorStart, kMaxColors + 1)) || (rc = dalloc(ctx, &w.a.colorBodies, n)) ||
       (rc = dalloc(ctx, &w.a.blockHist, (size_t)ctx->colorBlocks * kMaxColors)))
     return rc;
@@ -690,7 +704,7 @@ int avbd_pack(avbd_ctx *ctx, const avbd_world *world) {
     return rc;
   // launch shape of the persistent solve
   const int maxPerSm = solve_max_blocks_per_sm(ctx->lanes);
-  ctx->lanes = P.lanes_per_body > 0 ? P.lanes_per_body : 8;
+  ctx->lanes = P.lanes_per_body > 0 ? P.lanes_per_body : 16;
   if (ctx->lanes != 1 && ctx->lanes != 2 && ctx->lanes != 4 && ctx->lanes != 8 && ctx->lanes != 16 && ctx->lanes != 32)
     return fail(ctx, AVBD_ERR_ARG, "lanes_per_body must be a power of two <= 32");
   ctx->blocksPerSm = P.blocks_per_sm > 0 ? std::min(P.blocks_per_sm, maxPerSm) : maxPerSm;
@@ -703,6 +717,7 @@ int avbd_pack(avbd_ctx *ctx, const avbd_world *world) {
   CK(cudaMallocHost((void **)&ctx->hOmega, sizeof(float4) * n));
   CK(cudaMallocHost((void **)&ctx->hPrev, sizeof(float4) * n));
   ctx->packed = true;
+  ctx->stepSeq = 0;
   ctx->steps = 0;
   ctx->launches = 0;
   rc = write_state(ctx, world, false);

@@ -205,6 +205,7 @@ __global__ void prepare_bodies_kernel(World w) {
     }
     w.b.flags[i] = fl;
     w.a.count[i] = 0;
+    w.a.ccount[i] = 0;
   }
 }
 
@@ -216,8 +217,14 @@ __global__ void adj_count_kernel(World w) {
     if (n <= 0) continue;
     const uint64_t k = w.cur.key[c];
     const int a = (int)(k >> 32), b = (int)(k & 0xffffffffu);
-    if (w.b.flags0[a] & kBodyDynamic) atomicAdd(&w.a.count[a], 1);
-    if (w.b.flags0[b] & kBodyDynamic) atomicAdd(&w.a.count[b], 1);
+    if (w.b.flags0[a] & kBodyDynamic) {
+      atomicAdd(&w.a.count[a], 1);
+      atomicAdd(&w.a.ccount[a], n);
+    }
+    if (w.b.flags0[b] & kBodyDynamic) {
+      atomicAdd(&w.a.count[b], 1);
+      atomicAdd(&w.a.ccount[b], n);
+    }
     atomicAdd(&w.ctl->liveManifolds, 1);
     atomicAdd(&w.ctl->liveContacts, n);
   }
@@ -259,6 +266,20 @@ __global__ void adj_sort_kernel(World w) {
         y--;
       }
       e[y + 1] = v;
+    }
+    // per-contact adjacency, in manifold order then contact order
+    {
+      int at = w.a.cstart[i];
+      const int cend = min(w.a.cstart[i + 1], w.a.ccap);
+      for (int x = beg; x < end; x++) {
+        const uint32_t v = e[x];
+        const int m = (int)(v >> 1), side = (int)(v & 1u);
+        const uint64_t key = w.cur.key[m];
+        const int other = side ? (int)(key >> 32) : (int)(key & 0xffffffffu);
+        const int cnt = w.cur.count[m];
+        for (int k = 0; k < cnt && at < cend; k++, at++)
+          w.a.centry[at] = make_int2(((m * kMaxContacts + k) << 1) | side, other);
+      }
     }
     if (w.p.fp64Ratio > 0) {
       double kmax = 0;
@@ -555,6 +576,8 @@ __device__ inline BState<T> load_state(const World &w, int i) {
   BState<T> s;
   const float4 qt = ld(&w.b.quatT[i]);
   const Q4<T> qT{(T)qt.x, (T)qt.y, (T)qt.z, (T)qt.w};
+  // only the FP64 path consults the precision flag (FP64 bodies keep their
+  // iterate in f64 shadows); the FP32 path issues its loads at once
   if (sizeof(T) == 8 && (ld(&w.b.flags[i]) & kBodyFp64)) {
     const D4 d = ldcg(&w.b.dpD[i]), q = ldcg(&w.b.quatD[i]);
     s.dp = V3<T>{(T)d.x, (T)d.y, (T)d.z};
@@ -610,67 +633,62 @@ __device__ inline void manifold_rows(const World &w, int m, V3<T> n[3], T &mu, i
   cnt = ld(&w.cur.count[m]);
 }
 
+// One contact of the body's per-contact adjacency: slot = manifold * 8 + k.
 template <class T>
-__device__ void contact_primal(const World &w, int m, int side, const BState<T> &self, T alpha, Sys<T> &s) {
+__device__ void contact_primal(const World &w, int slot, int side, int other, const BState<T> &self, T alpha,
+                               Sys<T> &s) {
+  const int m = slot >> 3;
   V3<T> n[3];
   T mu;
   int cnt;
   manifold_rows(w, m, n, mu, cnt);
-  const uint64_t key = ld(&w.cur.key[m]);
-  const int other = side ? (int)(key >> 32) : (int)(key & 0xffffffffu);
+  const float4 cA = ld(&w.cur.cA[slot]), cB = ld(&w.cur.cB[slot]);
+  const float4 cK = __ldcg(&w.cur.cK[slot]), cL = __ldcg(&w.cur.cL[slot]);
   const BState<T> o = load_state<T>(w, other);
   const BState<T> &A = side ? o : self;
   const BState<T> &B = side ? self : o;
   const T sgn = side ? T(-1) : T(1);
-  for (int k = 0; k < cnt; k++) {
-    const int slot = m * kMaxContacts + k;
-    const float4 cA = ld(&w.cur.cA[slot]), cB = ld(&w.cur.cB[slot]);
-    const float4 cK = __ldcg(&w.cur.cK[slot]), cL = __ldcg(&w.cur.cL[slot]);
-    const ContactEval<T> e = eval_contact(n, mu, cA, cB, cK, cL, A, B, alpha);
-    const V3<T> r = side ? V3<T>{(T)cB.x, (T)cB.y, (T)cB.z} : V3<T>{(T)cA.x, (T)cA.y, (T)cA.z};
-    const T kk[3] = {(T)cK.x, (T)cK.y, (T)cK.z};
-    const T ff[3] = {e.F.x, e.F.y, e.F.z};
+  const ContactEval<T> e = eval_contact(n, mu, cA, cB, cK, cL, A, B, alpha);
+  const V3<T> r = side ? V3<T>{(T)cB.x, (T)cB.y, (T)cB.z} : V3<T>{(T)cA.x, (T)cA.y, (T)cA.z};
+  const T kk[3] = {(T)cK.x, (T)cK.y, (T)cK.z};
+  const T ff[3] = {e.F.x, e.F.y, e.F.z};
 #pragma unroll
-    for (int row = 0; row < 3; row++) {
-      const V3<T> a = cross(r, n[row]);
-      stamp_row(s, kk[row], n[row], a);
-      const T f = sgn * ff[row];
-      s.bl[0] += f * n[row].x; s.bl[1] += f * n[row].y; s.bl[2] += f * n[row].z;
-      s.ba[0] += f * a.x; s.ba[1] += f * a.y; s.ba[2] += f * a.z;
-    }
+  for (int row = 0; row < 3; row++) {
+    const V3<T> a = cross(r, n[row]);
+    stamp_row(s, kk[row], n[row], a);
+    const T f = sgn * ff[row];
+    s.bl[0] += f * n[row].x; s.bl[1] += f * n[row].y; s.bl[2] += f * n[row].z;
+    s.ba[0] += f * a.x; s.ba[1] += f * a.y; s.ba[2] += f * a.z;
   }
 }
 
 template <class T>
-__device__ void contact_dual(const World &w, int m, int side, const BState<T> &self, T alpha) {
+__device__ void contact_dual(const World &w, int slot, int side, int other, const BState<T> &self, T alpha,
+                             bool sphere) {
+  const int m = slot >> 3;
   V3<T> n[3];
   T mu;
   int cnt;
   manifold_rows(w, m, n, mu, cnt);
-  const uint64_t key = ld(&w.cur.key[m]);
-  const int ia = (int)(key >> 32), ib = (int)(key & 0xffffffffu);
-  const BState<T> o = load_state<T>(w, side ? ia : ib);
+  const float4 cA = ld(&w.cur.cA[slot]), cB = ld(&w.cur.cB[slot]);
+  float4 cK = __ldcg(&w.cur.cK[slot]);
+  const float4 cL = __ldcg(&w.cur.cL[slot]);
+  const BState<T> o = load_state<T>(w, other);
   const BState<T> &A = side ? o : self;
   const BState<T> &B = side ? self : o;
-  const bool sphere = ((ld(&w.b.flags0[ia]) | ld(&w.b.flags0[ib])) & kBodySphere) != 0;
   const T beta = (T)w.p.betaLin, kmax = (T)w.p.penaltyMax, thr = (T)w.p.stickThreshold;
-  for (int k = 0; k < cnt; k++) {
-    const int slot = m * kMaxContacts + k;
-    const float4 cA = ld(&w.cur.cA[slot]), cB = ld(&w.cur.cB[slot]);
-    float4 cK = __ldcg(&w.cur.cK[slot]), cL = __ldcg(&w.cur.cL[slot]);
-    const ContactEval<T> e = eval_contact(n, mu, cA, cB, cK, cL, A, B, alpha);
-    float stick = cL.w;
-    if (e.F.x < T(0)) cK.x = (float)fmin((T)cK.x + beta * fabs(e.C.x), kmax);
-    if (e.within) {
-      cK.y = (float)fmin((T)cK.y + beta * fabs(e.C.y), kmax);
-      cK.z = (float)fmin((T)cK.z + beta * fabs(e.C.z), kmax);
-      stick = sqrt(e.C.y * e.C.y + e.C.z * e.C.z) < thr ? 1.f : 0.f;
-    } else if (sphere) {
-      stick = 0.f;
-    }
-    __stcg(&w.cur.cK[slot], cK);
-    __stcg(&w.cur.cL[slot], make_float4((float)e.F.x, (float)e.F.y, (float)e.F.z, stick));
+  const ContactEval<T> e = eval_contact(n, mu, cA, cB, cK, cL, A, B, alpha);
+  float stick = cL.w;
+  if (e.F.x < T(0)) cK.x = (float)fmin((T)cK.x + beta * fabs(e.C.x), kmax);
+  if (e.within) {
+    cK.y = (float)fmin((T)cK.y + beta * fabs(e.C.y), kmax);
+    cK.z = (float)fmin((T)cK.z + beta * fabs(e.C.z), kmax);
+    stick = sqrt(e.C.y * e.C.y + e.C.z * e.C.z) < thr ? 1.f : 0.f;
+  } else if (sphere) {
+    stick = 0.f;
   }
+  __stcg(&w.cur.cK[slot], cK);
+  __stcg(&w.cur.cL[slot], make_float4((float)e.F.x, (float)e.F.y, (float)e.F.z, stick));
 }
 
 // Joint geometry at the current iterate (joint.js:115-129), delta form.
@@ -967,11 +985,11 @@ __device__ void solve_body(const World &w, int i, int lane, int G, unsigned mask
   const SolverParams &P = w.p;
   const T dt = (T)P.dt, dt2 = (T)(P.dt * P.dt);
   BState<T> self = load_state<T>(w, i);
-  const int mStart = ld(&w.a.start[i]);
-  int mEnd = ld(&w.a.start[i + 1]);
-  if (mEnd > w.a.cap) mEnd = w.a.cap;
+  const int cb = ld(&w.a.cstart[i]);
+  int ce = ld(&w.a.cstart[i + 1]);
+  if (ce > w.a.ccap) ce = w.a.ccap;
   const int cStart = ld(&w.g.cStart[i]), cEnd = ld(&w.g.cStart[i + 1]);
-  const int nm = mEnd - mStart, total = nm + (cEnd - cStart);
+  const int nm = ce - cb, total = nm + (cEnd - cStart);
 
   Sys<T> s;
   zero(s);
@@ -1013,8 +1031,8 @@ __device__ void solve_body(const World &w, int i, int lane, int G, unsigned mask
   }
   for (int e = lane; e < total; e += G) {
     if (e < nm) {
-      const uint32_t ent = ld(&w.a.entry[mStart + e]);
-      contact_primal<T>(w, (int)(ent >> 1), (int)(ent & 1u), self, alpha, s);
+      const int2 ent = ld(&w.a.centry[cb + e]);
+      contact_primal<T>(w, ent.x >> 1, ent.x & 1, ent.y, self, alpha, s);
     } else {
       const uint32_t ref = ld(&w.g.cRef[cStart + e - nm]);
       const uint32_t type = ref >> 30, idx = (ref >> 1) & 0x1fffffffu, side = ref & 1u;
@@ -1049,13 +1067,14 @@ __device__ void solve_body(const World &w, int i, int lane, int G, unsigned mask
   }
   if (!dual) return;
   const int myColor = ld(&w.b.color[i]);
+  const bool selfSphere = (ld(&w.b.flags0[i]) & kBodySphere) != 0;
   for (int e = lane; e < total; e += G) {
     if (e < nm) {
-      const uint32_t ent = ld(&w.a.entry[mStart + e]);
-      const int m = (int)(ent >> 1), side = (int)(ent & 1u);
-      const uint64_t key = ld(&w.cur.key[m]);
-      const int other = side ? (int)(key >> 32) : (int)(key & 0xffffffffu);
-      if (owns(myColor, ld(&w.b.color[other]))) contact_dual<T>(w, m, side, self, alpha);
+      const int2 ent = ld(&w.a.centry[cb + e]);
+      if (owns(myColor, ld(&w.b.color[ent.y]))) {
+        const bool sphere = selfSphere || (ld(&w.b.flags0[ent.y]) & kBodySphere) != 0;
+        contact_dual<T>(w, ent.x >> 1, ent.x & 1, ent.y, self, alpha, sphere);
+      }
     } else {
       const uint32_t ref = ld(&w.g.cRef[cStart + e - nm]);
       const uint32_t type = ref >> 30, idx = (ref >> 1) & 0x1fffffffu, side = ref & 1u;
@@ -1172,9 +1191,12 @@ void launch_prepare(const World &w, void *temp, size_t tempBytes, cudaStream_t s
   prepare_forces_kernel<<<blocks, 256, 0, st>>>(w);
   prepare_bodies_kernel<<<blocks, 256, 0, st>>>(w);
   cudaMemsetAsync(w.a.count + w.b.n, 0, sizeof(int), st);
+  cudaMemsetAsync(w.a.ccount + w.b.n, 0, sizeof(int), st);
   adj_count_kernel<<<blocks, 256, 0, st>>>(w);
   size_t tb = tempBytes;
   cub::DeviceScan::ExclusiveSum(temp, tb, w.a.count, w.a.start, w.b.n + 1, st);
+  tb = tempBytes;
+  cub::DeviceScan::ExclusiveSum(temp, tb, w.a.ccount, w.a.cstart, w.b.n + 1, st);
   cudaMemcpyAsync(w.a.cursor, w.a.start, sizeof(int) * w.b.n, cudaMemcpyDeviceToDevice, st);
   adj_fill_kernel<<<blocks, 256, 0, st>>>(w);
   adj_sort_kernel<<<blocks, 256, 0, st>>>(w);
