@@ -140,6 +140,14 @@ struct Springs {
   D4 *dptD;
 };
 
+// One hash-grid insertion: the body's exact broad-phase inputs travel with
+// it, so the sphere test needs no further loads. b2 = (body << 1) | dynamic.
+struct __align__(16) Entry {
+  double x, y, z, r;
+  int b2, cx, cy, cz;
+};
+constexpr int kPairScratch = 64;
+
 struct Grid {
   int numScenes;
   const int *sceneStart;     // numScenes + 1
@@ -149,8 +157,10 @@ struct Grid {
   int4 *cellLo, *cellHi;     // per body, w = scene
   unsigned tableMask;
   int *tableCount, *tableStart, *tableCursor;
-  int4 *entries;  // (body, cell x, cell y, cell z)
+  struct Entry *entries;
   int entryCap;
+  uint32_t *scratch;  // per body: sorted lower-index partners (kPairScratch each)
+  int hasConstraints; // any joint or spring in the world
   int *pairCount, *pairStart;  // per body, pairStart has n + 1 entries
   uint64_t *candKey;
   int *candPrev;

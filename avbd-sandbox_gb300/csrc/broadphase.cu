@@ -113,7 +113,14 @@ __global__ void scatter_kernel(World w) {
       for (int y = lo.y; y <= hi.y; y++)
         for (int z = lo.z; z <= hi.z; z++) {
           const int at = atomicAdd(&w.g.tableCursor[cell_hash(x, y, z, lo.w) & w.g.tableMask], 1);
-          if (at < w.g.entryCap) w.g.entries[at] = make_int4(i, x, y, z);
+          if (at < w.g.entryCap) {
+            const D4 p = w.b.pos[i];
+            Entry e;
+            e.x = p.x; e.y = p.y; e.z = p.z; e.r = w.b.size[i].w;
+            e.b2 = (i << 1) | ((w.b.flags0[i] & kBodyDynamic) ? 1 : 0);
+            e.cx = x; e.cy = y; e.cz = z;
+            w.g.entries[at] = e;
+          }
           else atomicOr(&w.ctl->flags, kOvfCells);
         }
   }
@@ -151,14 +158,13 @@ __device__ void partners_small(const World &w, int a, int prevCount, F &&f) {
         if (end > w.g.entryCap) end = w.g.entryCap;
         for (int k = beg; k < end; k++) {
           // entries carry their cell: other cells hashing to this bucket are skipped
-          const int4 ent = w.g.entries[k];
-          const int b = ent.x;
-          if (b >= a || ent.y != x || ent.z != y || ent.w != z) continue;
-          const int4 bl = w.g.cellLo[b], bh = w.g.cellHi[b];
+          const Entry &ent = w.g.entries[k];
+          const int b = ent.b2 >> 1;
+          if (b >= a || ent.cx != x || ent.cy != y || ent.cz != z) continue;
+          const int4 bl = w.g.cellLo[b];
           if (bl.w != s) continue;
           // the pair is found once: in the minimum corner of the AABB overlap
           if (max(lo.x, bl.x) != x || max(lo.y, bl.y) != y || max(lo.z, bl.z) != z) continue;
-          if (x > bh.x || y > bh.y || z > bh.z) continue;
           if (accept(w, a, b)) f(b);
         }
       }
@@ -205,17 +211,37 @@ __device__ void sort_segment(uint64_t *k, int n) {
   }
 }
 
+// A's exact broad-phase inputs, held in registers during its walk.
+struct BodyA {
+  int a, s;
+  int4 lo, hi;
+  double x, y, z, r;
+  bool dyn;
+};
+
+// The `visit` predicate (solver.js:316-329) against a grid entry.
+__device__ __forceinline__ bool accept_entry(const World &w, const BodyA &A, const Entry &e) {
+  if (!(A.dyn || (e.b2 & 1))) return false;
+  const double dx = A.x - e.x, dy = A.y - e.y, dz = A.z - e.z;
+  const double r = A.r + e.r;
+  if (!(dx * dx + dy * dy + dz * dz <= r * r)) return false;
+  return !w.g.hasConstraints || accept(w, A.a, e.b2 >> 1);
+}
+
 // Warp-cooperative enumeration of the partners b < a of a non-large body a:
 // lanes split its cells (and its old manifolds and the scene's large bodies),
-// calling f(b) on the lane that finds b. Each partner is found exactly once.
+// calling f(b) on the lane that finds b. Each partner is found exactly once:
+// grid pairs in the minimum corner cell of the two AABBs; old manifolds only
+// when the sphere test rejects them; large bodies from the scene's list.
 template <class F>
-__device__ void warp_partners(const World &w, int a, int prevCount, int lane, F &&f) {
-  const int4 lo = w.g.cellLo[a], hi = w.g.cellHi[a];
-  const int s = lo.w;
+__device__ void warp_partners(const World &w, const BodyA &A, int prevCount, int lane, F &&f) {
+  const int a = A.a, s = A.s;
   for (int k = w.g.largeStart[s] + lane; k < w.g.largeStart[s + 1]; k += 32) {
     const int b = w.g.largeList[k];
     if (b < a && accept(w, a, b)) f(b);
   }
+  const int4 lo = A.lo, hi = A.hi;
+  const double inv = w.g.invCell[s];
   const int nx = hi.x - lo.x + 1, ny = hi.y - lo.y + 1, nz = hi.z - lo.z + 1;
   const int ncell = (nx > 0 && ny > 0 && nz > 0) ? nx * ny * nz : 0;
   for (int ci = lane; ci < ncell; ci += 32) {
@@ -225,16 +251,18 @@ __device__ void warp_partners(const World &w, int a, int prevCount, int lane, F 
     int end = beg + w.g.tableCount[bucket];
     if (end > w.g.entryCap) end = w.g.entryCap;
     for (int k = beg; k < end; k++) {
+      const Entry e = w.g.entries[k];
+      const int b = e.b2 >> 1;
       // entries carry their cell: other cells hashing to this bucket are skipped
-      const int4 ent = w.g.entries[k];
-      const int b = ent.x;
-      if (b >= a || ent.y != x || ent.z != y || ent.w != z) continue;
-      const int4 bl = w.g.cellLo[b], bh = w.g.cellHi[b];
-      if (bl.w != s) continue;
+      if (b >= a || e.cx != x || e.cy != y || e.cz != z) continue;
+      // B's cell range, recomputed exactly as the insertion computed it
+      const double rb = e.r * (1.0 + 1e-7) + 1e-9;
+      const int blx = (int)floor((e.x - rb) * inv), bly = (int)floor((e.y - rb) * inv),
+                blz = (int)floor((e.z - rb) * inv);
       // the pair is found once: in the minimum corner of the AABB overlap
-      if (max(lo.x, bl.x) != x || max(lo.y, bl.y) != y || max(lo.z, bl.z) != z) continue;
-      if (x > bh.x || y > bh.y || z > bh.z) continue;
-      if (accept(w, a, b)) f(b);
+      if (max(lo.x, blx) != x || max(lo.y, bly) != y || max(lo.z, blz) != z) continue;
+      if (w.g.numScenes > 1 && w.b.scene[b] != s) continue;  // another scene's cell, same bucket
+      if (accept_entry(w, A, e)) f(b);
     }
   }
   int first = 0, last = 0;
@@ -248,69 +276,85 @@ __device__ void warp_partners(const World &w, int a, int prevCount, int lane, F 
   }
 }
 
-constexpr int kWarpsPerBlock = 8;
-constexpr int kSegCap = 128;  // partners sorted in shared memory; longer lists take the serial path
+__device__ BodyA body_a(const World &w, int a) {
+  BodyA A;
+  A.a = a;
+  A.lo = w.g.cellLo[a];
+  A.hi = w.g.cellHi[a];
+  A.s = A.lo.w;
+  const D4 p = w.b.pos[a];
+  A.x = p.x; A.y = p.y; A.z = p.z;
+  A.r = w.b.size[a].w;
+  A.dyn = (w.b.flags0[a] & kBodyDynamic) != 0;
+  return A;
+}
 
-__global__ void __launch_bounds__(256) count_kernel(World w) {
+constexpr int kWarpsPerBlock = 8;
+
+// One pass per non-large body: count its partners and, when they fit, leave
+// them sorted in its scratch row for the copy after the scan.
+__global__ void __launch_bounds__(256) pairs_kernel(World w) {
+  __shared__ uint32_t buf[kWarpsPerBlock][kPairScratch];
+  __shared__ int fill[kWarpsPerBlock];
   const int prevCount = w.ctl->prevCandidates;
-  const int lane = threadIdx.x & 31;
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, warps = (gridDim.x * blockDim.x) >> 5;
   for (int a = warp; a < w.b.n; a += warps) {
     if (is_large(w, a)) continue;  // large_count_kernel
-    int c = 0;
-    warp_partners(w, a, prevCount, lane, [&](int) { c++; });
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) c += __shfl_xor_sync(0xffffffffu, c, o);
-    if (lane == 0) w.g.pairCount[a] = c;
+    const BodyA A = body_a(w, a);
+    if (lane == 0) fill[wib] = 0;
+    __syncwarp();
+    warp_partners(w, A, prevCount, lane, [&](int b) {
+      const int at = atomicAdd(&fill[wib], 1);
+      if (at < kPairScratch) buf[wib][at] = (uint32_t)b;
+    });
+    __syncwarp();
+    const int n = fill[wib];
+    if (lane == 0) w.g.pairCount[a] = n;
+    if (n <= kPairScratch) {
+      // rank sort (partners are distinct): element i goes to #{j : b_j < b_i}
+      uint32_t *row = w.g.scratch + (size_t)a * kPairScratch;
+      for (int i = lane; i < n; i += 32) {
+        const uint32_t v = buf[wib][i];
+        int r = 0;
+        for (int j = 0; j < n; j++) r += buf[wib][j] < v ? 1 : 0;
+        row[r] = v;
+      }
+    }
+    __syncwarp();
   }
 }
 
-__global__ void __launch_bounds__(256) write_kernel(World w) {
-  __shared__ uint32_t buf[kWarpsPerBlock][kSegCap];
-  __shared__ int fill[kWarpsPerBlock];
+// Copy each body's sorted partners into its segment of the key array; the
+// rare bodies with more than kPairScratch partners are enumerated again
+// serially and sorted in place.
+__global__ void __launch_bounds__(256) copy_kernel(World w) {
   const int prevCount = w.ctl->prevCandidates;
   const int cap = w.g.candCap;
-  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
+  const int lane = threadIdx.x & 31;
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, warps = (gridDim.x * blockDim.x) >> 5;
   for (int a = warp; a < w.b.n; a += warps) {
     if (is_large(w, a)) continue;
     const int beg = w.g.pairStart[a];
     const int n = w.g.pairStart[a + 1] - beg;
+    if (n == 0) continue;
     if (beg + n > cap) {
       if (lane == 0) atomicOr(&w.ctl->flags, kOvfPairs);
       continue;
     }
-    if (n == 0) continue;
     uint64_t *seg = w.g.candKey + beg;
     const uint64_t hiKey = (uint64_t)(uint32_t)a << 32;
-    if (n > kSegCap) {  // rare: serial write + sort on lane 0
-      if (lane == 0) {
-        int c = 0;
-        partners_small(w, a, prevCount, [&](int b) {
-          if (c < n) seg[c] = hiKey | (uint32_t)b;
-          c++;
-        });
-        sort_segment(seg, n);
-      }
-      __syncwarp();
-      continue;
+    if (n <= kPairScratch) {
+      const uint32_t *row = w.g.scratch + (size_t)a * kPairScratch;
+      for (int i = lane; i < n; i += 32) seg[i] = hiKey | row[i];
+    } else if (lane == 0) {
+      int c = 0;
+      partners_small(w, a, prevCount, [&](int b) {
+        if (c < n) seg[c] = hiKey | (uint32_t)b;
+        c++;
+      });
+      sort_segment(seg, n);
     }
-    if (lane == 0) fill[wib] = 0;
-    __syncwarp();
-    warp_partners(w, a, prevCount, lane, [&](int b) {
-      const int at = atomicAdd(&fill[wib], 1);
-      if (at < kSegCap) buf[wib][at] = (uint32_t)b;
-    });
-    __syncwarp();
-    const int m = min(fill[wib], n);
-    // rank sort (partners are distinct): element i goes to #{j : b_j < b_i}
-    for (int i = lane; i < m; i += 32) {
-      const uint32_t v = buf[wib][i];
-      int r = 0;
-      for (int j = 0; j < m; j++) r += buf[wib][j] < v ? 1 : 0;
-      seg[r] = hiKey | v;
-    }
-    __syncwarp();
   }
 }
 
@@ -411,11 +455,11 @@ void launch_broadphase_impl(const World &w, int numLarge, void *temp, size_t tem
   // pairCount[n] = 0 so the scan over n + 1 entries yields the total at [n]
   cudaMemsetAsync(w.g.pairCount + n, 0, sizeof(int), st);
   const int warpBlocks = (int)std::min<long long>(((long long)n + 7) / 8, (long long)smCount * 32);
-  count_kernel<<<warpBlocks, 256, 0, st>>>(w);
+  pairs_kernel<<<warpBlocks, 256, 0, st>>>(w);
   if (numLarge > 0) large_count_kernel<<<numLarge < 1024 ? numLarge : 1024, 256, 0, st>>>(w, numLarge);
   tb = tempBytes;
   cub::DeviceScan::ExclusiveSum(temp, tb, w.g.pairCount, w.g.pairStart, n + 1, st);
-  write_kernel<<<warpBlocks, 256, 0, st>>>(w);
+  copy_kernel<<<warpBlocks, 256, 0, st>>>(w);
   if (numLarge > 0) large_write_kernel<<<numLarge < 1024 ? numLarge : 1024, 256, 0, st>>>(w, numLarge);
   finish_kernel<<<1, 1, 0, st>>>(w);
   prev_index_kernel<<<blocks, 256, 0, st>>>(w);

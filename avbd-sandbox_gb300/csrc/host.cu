@@ -679,8 +679,10 @@ int avbd_pack(avbd_ctx *ctx, const avbd_world *world) {
   if ((rc = dalloc(ctx, &w.g.cellLo, n)) || (rc = dalloc(ctx, &w.g.cellHi, n)) ||
       (rc = dalloc(ctx, &w.g.tableCount, ctx->tableSize)) || (rc = dalloc(ctx, &w.g.tableStart, ctx->tableSize)) ||
       (rc = dalloc(ctx, &w.g.tableCursor, ctx->tableSize)) || (rc = dalloc(ctx, &w.g.entries, ctx->entryCap)) ||
-      (rc = dalloc(ctx, &w.g.pairCount, n + 1)) || (rc = dalloc(ctx, &w.g.pairStart, n + 1)))
+      (rc = dalloc(ctx, &w.g.pairCount, n + 1)) || (rc = dalloc(ctx, &w.g.pairStart, n + 1)) ||
+      (rc = dalloc(ctx, &w.g.scratch, (size_t)n * kPairScratch)))
     return rc;
+  w.g.hasConstraints = (ctx->nj + ctx->ns) > 0 ? 1 : 0;
   // adjacency + colouring
   w.a.cap = ctx->adjCap;
   ctx->colorBlocks = std::max(1, coloring_grid(ctx->smCount));

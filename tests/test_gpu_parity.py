@@ -132,30 +132,33 @@ def test_short_horizon_drift(abi, scenes, backend_mod, name):
 
 
 def test_batched_scenes_match_individual_oracles(abi, scenes, backend_mod):
+    """A batch of unrelated scenes in one world steps exactly like each scene
+    alone: same colouring as each scene's own oracle, body states within the
+    reference harness's per-step schedule (src/app/gputest.js:91-96)."""
     parts = [scenes.cube_stack(n=6, seed=3), scenes.parity_scenes()[2], scenes.spheres_scene(),
              scenes.random_pile(40, seed=7)]
-    for p in parts:
-        p.params = dict(gravity=-9.81, iterations=10)
     params = abi.default_params(gravity=-9.81, iterations=10, body_order=abi.ORDER_PRIORITY)
     worlds = [p.world().round_to_device() for p in parts]
     batch = scenes.batch_worlds(worlds)
     gpu = backend_mod.GpuBackend(params)
     gpu.pack(batch)
-    gpu.step(3)
-    gpu.idle()
-    got = gpu.read_state()
-    gc, _ = gpu.read_coloring()
-    start = 0
-    for w in worlds:
-        ref = Oracle(params, w)
-        ref.step(3)
-        want = ref.state()
-        n = w.n_bodies
-        dyn = want.mass > 0
-        assert np.max(np.abs(got.pos[start:start + n][dyn] - want.pos[dyn])) < 1e-4
-        oc, _ = ref.coloring()
-        assert np.array_equal(gc[start:start + n], oc)
-        start += n
+    refs = [Oracle(params, w) for w in worlds]
+    for step, tol in enumerate([3e-4, 1e-3, 4e-3]):
+        gpu.step(1)
+        gpu.idle()
+        got = gpu.read_state()
+        gc, _ = gpu.read_coloring()
+        start = 0
+        for w, ref in zip(worlds, refs):
+            ref.step(1)
+            want = ref.state()
+            n = w.n_bodies
+            dyn = want.mass > 0
+            err = np.abs(got.pos[start:start + n][dyn] - want.pos[dyn]) / np.maximum(1.0, np.abs(want.pos[dyn]))
+            assert err.max() <= tol, (step, float(err.max()))
+            oc, _ = ref.coloring()
+            assert np.array_equal(gc[start:start + n], oc)
+            start += n
 
 
 def test_determinism(abi, scenes, backend_mod):
