@@ -50,6 +50,7 @@ class Params(C.Structure):
         ("fp64_ratio_threshold", C.c_double),
         ("max_pairs_per_body", C.c_int32), ("max_adjacency", C.c_int32),
         ("lanes_per_body", C.c_int32), ("blocks_per_sm", C.c_int32),
+        ("schedule", C.c_int32), ("grid_factor", C.c_int32),
     ]
 
 
@@ -76,6 +77,7 @@ def default_params(**overrides) -> Params:
     p.hash_threshold = 150
     p.body_order = ORDER_REFERENCE
     p.fp64_ratio_threshold = 1e5
+    p.schedule = 1
     for k, v in overrides.items():
         if not hasattr(p, k):
             raise AttributeError(k)

@@ -57,6 +57,7 @@ struct SolverParams {
   double betaLin, betaAng, alpha, gamma, penaltyMin, penaltyMax, margin, stickThreshold;
   int rotatedInertia, springRamp, springGeometric, cachedJacobians;
   double fp64Ratio;
+  int schedule;  // 0: colour phases + grid barrier, 1: dependency wavefront
 };
 
 // Device scalars shared by all kernels of a step.
@@ -97,6 +98,7 @@ struct Bodies {
   D4 *dpD, *quatD;  // f64 shadows (FP64 bodies)
   int *flags;     // per-step flags (static bits | kBodyFp64)
   int *color;     // colour, -1 for static bodies
+  int *progress;  // iterations completed in the current step (wavefront schedule)
 };
 
 struct Manifolds {

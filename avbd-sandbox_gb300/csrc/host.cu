@@ -403,7 +403,7 @@ int check_flags(avbd_ctx *ctx) {
     // grow the arenas that overflowed for the next pack; this state is invalid
     if (c.flags & kOvfPairs) ctx->params.max_pairs_per_body = std::max(ctx->params.max_pairs_per_body, 16) * 2;
     if (c.flags & kOvfAdj) ctx->params.max_adjacency = std::max(ctx->params.max_adjacency, 2) * 2;
-    if (c.flags & kOvfCells) ctx->params.reserved0 = std::max(ctx->params.reserved0, 1) * 2;
+    if (c.flags & kOvfCells) ctx->params.grid_factor = std::max(ctx->params.grid_factor, 1) * 2;
     return fail(ctx, AVBD_ERR_CAPACITY, "device arena overflow (flags 0x%x); capacities grown, repack to retry",
                 c.flags);
   }
@@ -434,6 +434,7 @@ void avbd_default_params(avbd_params *o) {
   o->hash_threshold = 150;
   o->body_order = AVBD_ORDER_PRIORITY;
   o->fp64_ratio_threshold = 1e5;
+  o->schedule = 1;
 }
 
 int avbd_create(const avbd_params *params, avbd_ctx **out) {
@@ -608,7 +609,7 @@ int avbd_pack(avbd_ctx *ctx, const avbd_world *world) {
     insertions += c;
   }
   const int pairsPerBody = ctx->params.max_pairs_per_body > 0 ? ctx->params.max_pairs_per_body : 16;
-  const int cellFactor = std::max(ctx->params.reserved0, 1);
+  const int cellFactor = std::max(ctx->params.grid_factor, 1);
   ctx->candCap = (int)std::min<long long>((long long)n * pairsPerBody + 256 + world->manifolds.count, 0x3fffffff);
   ctx->entryCap = (int)std::min<long long>(insertions * 2 * cellFactor + 4096, 0x3fffffff);
   ctx->tableSize = 1024;
@@ -620,7 +621,7 @@ int avbd_pack(avbd_ctx *ctx, const avbd_world *world) {
   w.p = SolverParams{P.dt, P.gravity, P.iterations, P.post_stabilize, P.beta_lin, P.beta_ang, P.alpha, P.gamma,
                      P.penalty_min, P.penalty_max, P.collision_margin, P.stick_threshold, P.rotated_inertia,
                      P.spring_stiffness_ramp, P.spring_geometric_stiffness, P.cached_contact_jacobians,
-                     P.fp64_ratio_threshold};
+                     P.fp64_ratio_threshold, P.schedule == 1 ? 1 : 0};
   int rc = 0;
   D4 *sizeP, *massDP;
   float4 *massFP;
@@ -640,7 +641,7 @@ int avbd_pack(avbd_ctx *ctx, const avbd_world *world) {
       (rc = dalloc(ctx, &w.b.omega, n)) || (rc = dalloc(ctx, &w.b.prevVel, n)) || (rc = dalloc(ctx, &w.b.quatT, n)) ||
       (rc = dalloc(ctx, &w.b.dp, n)) || (rc = dalloc(ctx, &w.b.yLin, n)) || (rc = dalloc(ctx, &w.b.yAng, n)) ||
       (rc = dalloc(ctx, &w.b.dpD, n)) || (rc = dalloc(ctx, &w.b.quatD, n)) || (rc = dalloc(ctx, &w.b.flags, n)) ||
-      (rc = dalloc(ctx, &w.b.color, n)))
+      (rc = dalloc(ctx, &w.b.color, n)) || (rc = dalloc(ctx, &w.b.progress, n)))
     return rc;
   // joints
   w.j.n = ctx->nj;

@@ -206,6 +206,7 @@ __global__ void prepare_bodies_kernel(World w) {
     w.b.flags[i] = fl;
     w.a.count[i] = 0;
     w.a.ccount[i] = 0;
+    w.b.progress[i] = 0;
   }
 }
 
@@ -1122,6 +1123,92 @@ __global__ void __launch_bounds__(kSolveBlock, 2) solve_kernel(World w, int G) {
   }
 }
 
+// ---------------------------------------------------------------------------
+// Dependency-driven wavefront schedule. Body i may run iteration t once every
+// neighbour of lower colour has completed iteration t and every neighbour of
+// higher colour has completed iteration t - 1: exactly the order of the colour
+// phases, without a grid-wide barrier between them. Each group walks its
+// bodies in increasing (iteration, colour) order, so the earliest unfinished
+// body always has its inputs ready and the schedule cannot deadlock while all
+// blocks are resident (cooperative launch). Every wait is bounded.
+// ---------------------------------------------------------------------------
+__device__ inline int ld_acquire(const int *p) {
+  int v;
+  asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ inline void st_release(int *p, int v) {
+  asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+constexpr long long kWaitLimit = 4000000;  // polls per body, about a second
+
+__device__ bool wait_neighbors(const World &w, int i, int it, int lane, int G, unsigned mask) {
+  const int myColor = ld(&w.b.color[i]);
+  const int cb = ld(&w.a.cstart[i]);
+  int ce = ld(&w.a.cstart[i + 1]);
+  if (ce > w.a.ccap) ce = w.a.ccap;
+  const int jb = ld(&w.g.cStart[i]), je = ld(&w.g.cStart[i + 1]);
+  const int nm = ce - cb, total = nm + (je - jb);
+  long long polls = 0;
+  for (int e = lane; e < total; e += G) {
+    int other;
+    if (e < nm) {
+      other = ld(&w.a.centry[cb + e]).y;
+    } else {
+      const uint32_t ref = ld(&w.g.cRef[jb + e - nm]);
+      const uint32_t type = ref >> 30, idx = (ref >> 1) & 0x1fffffffu, side = ref & 1u;
+      const int2 ab = type == kRefJoint ? ld(&w.j.bodies[idx]) : ld(&w.s.bodies[idx]);
+      other = side ? ab.x : ab.y;
+      if (other < 0) continue;
+    }
+    if (!(ld(&w.b.flags0[other]) & kBodyDynamic)) continue;
+    const int oc = ld(&w.b.color[other]);
+    const int need = oc < myColor ? it + 1 : it;
+    while (ld_acquire(&w.b.progress[other]) < need) {
+      if (++polls > kWaitLimit || (*((volatile unsigned *)&w.ctl->flags) & kOvfTimeout)) {
+        atomicOr(&w.ctl->flags, kOvfTimeout);
+        polls = -1;
+        break;
+      }
+      __nanosleep(32);
+    }
+    if (polls < 0) break;
+  }
+  return __all_sync(mask, polls >= 0);
+}
+
+__global__ void __launch_bounds__(kSolveBlock, 2) wave_kernel(World w, int G) {
+  const SolverParams &P = w.p;
+  Control *ctl = w.ctl;
+  const int numColors = *((volatile int *)&ctl->numColors);
+  const int lane = threadIdx.x & (G - 1);
+  const int warpLane = threadIdx.x & 31;
+  const unsigned mask = (G == 32 ? 0xffffffffu : (((1u << G) - 1u) << (warpLane & ~(G - 1))));
+  // groups interleaved across blocks, so a thin colour still spreads over all SMs
+  const int groupsPerBlock = blockDim.x / G;
+  const int group = (threadIdx.x / G) * gridDim.x + blockIdx.x;
+  const int groups = groupsPerBlock * gridDim.x;
+  const int total = P.iterations + (P.postStabilize ? 1 : 0);
+  for (int it = 0; it < total; it++) {
+    const double alpha = P.postStabilize ? (it < P.iterations ? 1.0 : 0.0) : P.alpha;
+    const bool dual = it < P.iterations;
+    const bool vel = it == P.iterations - 1;
+    for (int c = 0; c < numColors; c++) {
+      const int beg = ld(&w.a.colorStart[c]), end = ld(&w.a.colorStart[c + 1]);
+      for (int k = beg + group; k < end; k += groups) {
+        const int i = ld(&w.a.colorBodies[k]);
+        if (!wait_neighbors(w, i, it, lane, G, mask)) return;
+        if (ld(&w.b.flags[i]) & kBodyFp64) solve_body_f64(w, i, lane, G, mask, alpha, dual, vel);
+        else solve_body<float>(w, i, lane, G, mask, (float)alpha, dual, vel);
+        __threadfence();
+        __syncwarp(mask);
+        if (lane == 0) st_release(&w.b.progress[i], it + 1);
+      }
+    }
+  }
+}
+
 // x_{t+1} = x_t + delta (f64); statics: prevVel <- vel (solver.js:479).
 __global__ void commit_kernel(World w) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < w.b.n; i += gridDim.x * blockDim.x) {
@@ -1220,17 +1307,18 @@ cudaError_t launch_coloring(const World &w, cudaStream_t st, int smCount) {
 
 int solve_max_blocks_per_sm(int lanesPerBody) {
   (void)lanesPerBody;
-  int perSm = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, solve_kernel, kSolveBlock, 0);
-  return perSm;
+  int a = 0, b = 0;
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, solve_kernel, kSolveBlock, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, wave_kernel, kSolveBlock, 0);
+  return a < b ? a : b;
 }
 
 cudaError_t launch_solve(const World &w, int lanesPerBody, int blocksPerSm, cudaStream_t st, int smCount) {
   World arg = w;
   int G = lanesPerBody;
   void *args[] = {&arg, &G};
-  return cudaLaunchCooperativeKernel((void *)solve_kernel, dim3(blocksPerSm * smCount), dim3(kSolveBlock), args, 0,
-                                     st);
+  const void *fn = w.p.schedule == 1 ? (const void *)wave_kernel : (const void *)solve_kernel;
+  return cudaLaunchCooperativeKernel(fn, dim3(blocksPerSm * smCount), dim3(kSolveBlock), args, 0, st);
 }
 
 void launch_commit(const World &w, cudaStream_t st, int smCount) { commit_kernel<<<smCount * 4, 256, 0, st>>>(w); }

@@ -97,8 +97,13 @@ typedef struct avbd_params {
   /* GPU capacity policy (0 = automatic). */
   int32_t max_pairs_per_body; /* candidate partners with a lower index      */
   int32_t max_adjacency;      /* constraints incident to one dynamic body   */
-  int32_t lanes_per_body;     /* 0 = autotuned; else 1, 2, 4, 8 or 16       */
-  int32_t blocks_per_sm;      /* 0 = autotuned                              */
+  int32_t lanes_per_body;     /* 0 = automatic; else 1, 2, 4, 8, 16 or 32   */
+  int32_t blocks_per_sm;      /* 0 = automatic                              */
+  /* Schedule of the primal/dual iterations on the device:
+     0 = colour phases separated by a grid barrier,
+     1 = dependency wavefront (each body waits only for its neighbours). */
+  int32_t schedule;
+  int32_t grid_factor;        /* hash-grid arena multiplier (0 = 1)         */
 } avbd_params;
 
 /*

@@ -1695,7 +1695,7 @@ void orc_default_params(avbd_params *o) {
   o->penalty_min = 1; o->penalty_max = 1e10; o->collision_margin = 0.01; o->stick_threshold = 1e-5;
   o->rotated_inertia = 1; o->spring_stiffness_ramp = 0; o->spring_geometric_stiffness = 1;
   o->cached_contact_jacobians = 1; o->broadphase = 0; o->hash_threshold = 150;
-  o->body_order = AVBD_ORDER_REFERENCE; o->fp64_ratio_threshold = 0;
+  o->body_order = AVBD_ORDER_REFERENCE; o->fp64_ratio_threshold = 0; o->schedule = 1;
 }
 
 orc_solver *orc_create(const avbd_params *params) {
