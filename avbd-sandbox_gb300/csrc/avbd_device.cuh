@@ -186,6 +186,7 @@ struct Adjacency {
   int ccap;
   int *colorStart;   // kMaxColors + 1
   int *colorBodies;  // dynamic bodies sorted by (colour, index)
+  int4 *colorRec;    // per colour position: body, contact range begin, end, 0
   int *blockHist;    // colouring counting sort scratch
 };
 
@@ -247,7 +248,13 @@ __host__ __device__ inline V3<T> cross(V3<T> a, V3<T> b) {
 template <class T>
 __host__ __device__ inline V3<T> qsub(Q4<T> a, Q4<T> b) {
   const T lsq = b.x * b.x + b.y * b.y + b.z * b.z + b.w * b.w;
-  const T ix = -b.x / lsq, iy = -b.y / lsq, iz = -b.z / lsq, iw = b.w / lsq;
+  T ix, iy, iz, iw;
+  if constexpr (sizeof(T) == 4) {  // FP32 solver path: one reciprocal
+    const T r = T(1) / lsq;
+    ix = -b.x * r; iy = -b.y * r; iz = -b.z * r; iw = b.w * r;
+  } else {
+    ix = -b.x / lsq; iy = -b.y / lsq; iz = -b.z / lsq; iw = b.w / lsq;
+  }
   V3<T> o;
   o.x = (a.w * ix + a.x * iw + a.y * iz - a.z * iy) * T(2);
   o.y = (a.w * iy - a.x * iz + a.y * iw + a.z * ix) * T(2);
@@ -262,8 +269,13 @@ __host__ __device__ inline Q4<T> qintegrate(Q4<T> q, V3<T> w) {
   const T pz = w.x * q.y - w.y * q.x + w.z * q.w;
   const T pw = -w.x * q.x - w.y * q.y - w.z * q.z;
   const T rx = q.x + px * T(0.5), ry = q.y + py * T(0.5), rz = q.z + pz * T(0.5), rw = q.w + pw * T(0.5);
-  const T len = sqrt(rx * rx + ry * ry + rz * rz + rw * rw);
-  return Q4<T>{rx / len, ry / len, rz / len, rw / len};
+  if constexpr (sizeof(T) == 4) {  // FP32 solver path: one reciprocal square root
+    const T il = rsqrtf(rx * rx + ry * ry + rz * rz + rw * rw);
+    return Q4<T>{rx * il, ry * il, rz * il, rw * il};
+  } else {
+    const T len = sqrt(rx * rx + ry * ry + rz * rz + rw * rw);
+    return Q4<T>{rx / len, ry / len, rz / len, rw / len};
+  }
 }
 // maths.js:599-613
 template <class T>

@@ -10,14 +10,17 @@
 // Bodies of different scenes of a batch never pair.
 //
 // Structure (GB300-first rather than the reference's linked lists):
-//   1. every non-large body inserts its bounding-sphere AABB cells into a
-//      hash grid (per-scene cell = 2 x mean radius, as the reference's hash);
-//      counting sort by cell hash: count, exclusive scan, scatter
-//   2. per body A: count partners B < A (grid neighbours found once, in the
-//      minimum-corner cell of the two AABBs; large bodies of the scene; old
-//      manifold partners), exclusive scan of the counts
-//   3. per body A: write its partners into its segment and sort the segment,
-//      giving a globally sorted candidate key array without a global sort
+//   1. every regular body is inserted once, in the hash-grid cell of its
+//      centre; the per-scene cell is at least twice the largest regular
+//      bounding radius, so overlapping regular bodies sit in adjacent cells.
+//      Bodies above twice the scene's 95th-percentile radius are "large" and
+//      are tested against every body of their scene. Counting sort by cell
+//      hash: count, exclusive scan, scatter.
+//   2. per body A (one warp): its 27 neighbour cells, the scene's large
+//      bodies and its old manifolds give the partners B < A; they are sorted
+//      in shared memory and parked in a per-body scratch row with their count
+//   3. exclusive scan of the counts; each body copies its sorted row into its
+//      segment: a globally sorted candidate key array without a global sort
 //   4. per candidate: index of the same pair in the previous step's manifolds
 #include <cub/cub.cuh>
 
@@ -64,65 +67,46 @@ __device__ bool accept(const World &w, int a, int b) {
   return true;
 }
 
-// Cell range of body i's padded bounding-sphere AABB. The extent is bounded
-// (kMaxSpan cells per axis) so that no loop over cells can run away; a body
-// that needs more, or has a non-finite position, gets an empty range and
-// raises an error flag instead.
-constexpr int kMaxSpan = 64;
-__device__ void cell_range(const World &w, int i, int4 &lo, int4 &hi) {
+// Centre cell of body i. Coordinates beyond +-1e9 cells or non-finite
+// positions give no cell (the body is skipped) and raise an error flag.
+__device__ bool centre_cell(const World &w, int i, int4 &c) {
   const int s = w.b.scene[i];
   const double inv = w.g.invCell[s];
   const D4 p = w.b.pos[i];
-  // The grid only has to return a superset of the accepted pairs: pad the
-  // bounding sphere so rounding in the cell arithmetic can never drop one.
-  const double r = w.b.size[i].w * (1.0 + 1e-7) + 1e-9;
-  const double v[6] = {(p.x - r) * inv, (p.y - r) * inv, (p.z - r) * inv,
-                       (p.x + r) * inv, (p.y + r) * inv, (p.z + r) * inv};
+  const double v[3] = {p.x * inv, p.y * inv, p.z * inv};
   bool ok = true;
-  for (int k = 0; k < 6; k++) ok = ok && isfinite(v[k]) && fabs(v[k]) < 1.0e9;
-  if (ok) {
-    lo = make_int4((int)floor(v[0]), (int)floor(v[1]), (int)floor(v[2]), s);
-    hi = make_int4((int)floor(v[3]), (int)floor(v[4]), (int)floor(v[5]), s);
-    if (hi.x - lo.x >= kMaxSpan || hi.y - lo.y >= kMaxSpan || hi.z - lo.z >= kMaxSpan) ok = false;
-  }
-  if (!ok) {
-    if (!(w.b.flags0[i] & kBodyLarge)) atomicOr(&w.ctl->flags, isfinite(p.x + p.y + p.z) ? kOvfCells : kErrNaN);
-    lo = make_int4(0, 0, 0, s);
-    hi = make_int4(-1, -1, -1, s);
-  }
+  for (int k = 0; k < 3; k++) ok = ok && isfinite(v[k]) && fabs(v[k]) < 1.0e9;
+  c = ok ? make_int4((int)floor(v[0]), (int)floor(v[1]), (int)floor(v[2]), s) : make_int4(0, 0, 0, s);
+  if (!ok) atomicOr(&w.ctl->flags, isfinite(p.x + p.y + p.z) ? kOvfCells : kErrNaN);
+  return ok;
 }
 
 __global__ void cells_kernel(World w) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < w.b.n; i += gridDim.x * blockDim.x) {
-    int4 lo, hi;
-    cell_range(w, i, lo, hi);
-    w.g.cellLo[i] = lo;
-    w.g.cellHi[i] = hi;
-    if (is_large(w, i)) continue;
-    for (int x = lo.x; x <= hi.x; x++)
-      for (int y = lo.y; y <= hi.y; y++)
-        for (int z = lo.z; z <= hi.z; z++) atomicAdd(&w.g.tableCount[cell_hash(x, y, z, lo.w) & w.g.tableMask], 1);
+    int4 c;
+    const bool ok = centre_cell(w, i, c);
+    c.w = ok ? c.w : -1 - c.w;  // scene, negative when the body has no cell
+    w.g.cellLo[i] = c;
+    if (!ok || is_large(w, i)) continue;
+    atomicAdd(&w.g.tableCount[cell_hash(c.x, c.y, c.z, c.w) & w.g.tableMask], 1);
   }
 }
 
 __global__ void scatter_kernel(World w) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < w.b.n; i += gridDim.x * blockDim.x) {
-    if (is_large(w, i)) continue;
-    const int4 lo = w.g.cellLo[i], hi = w.g.cellHi[i];
-    for (int x = lo.x; x <= hi.x; x++)
-      for (int y = lo.y; y <= hi.y; y++)
-        for (int z = lo.z; z <= hi.z; z++) {
-          const int at = atomicAdd(&w.g.tableCursor[cell_hash(x, y, z, lo.w) & w.g.tableMask], 1);
-          if (at < w.g.entryCap) {
-            const D4 p = w.b.pos[i];
-            Entry e;
-            e.x = p.x; e.y = p.y; e.z = p.z; e.r = w.b.size[i].w;
-            e.b2 = (i << 1) | ((w.b.flags0[i] & kBodyDynamic) ? 1 : 0);
-            e.cx = x; e.cy = y; e.cz = z;
-            w.g.entries[at] = e;
-          }
-          else atomicOr(&w.ctl->flags, kOvfCells);
-        }
+    const int4 c = w.g.cellLo[i];
+    if (c.w < 0 || is_large(w, i)) continue;
+    const int at = atomicAdd(&w.g.tableCursor[cell_hash(c.x, c.y, c.z, c.w) & w.g.tableMask], 1);
+    if (at < w.g.entryCap) {
+      const D4 p = w.b.pos[i];
+      Entry e;
+      e.x = p.x; e.y = p.y; e.z = p.z; e.r = w.b.size[i].w;
+      e.b2 = (i << 1) | ((w.b.flags0[i] & kBodyDynamic) ? 1 : 0);
+      e.cx = c.x; e.cy = c.y; e.cz = c.z;
+      w.g.entries[at] = e;
+    } else {
+      atomicOr(&w.ctl->flags, kOvfCells);
+    }
   }
 }
 
@@ -140,34 +124,31 @@ __device__ void prev_range(const World &w, int a, int prevCount, int &first, int
   while (last < prevCount && (int)(w.prev.key[last] >> 32) == a) last++;
 }
 
-// Enumerate the candidate partners b < a of a non-large body a, calling f(b).
+// Enumerate the candidate partners b < a of a non-large body a, calling f(b)
+// (serial form, for the rare bodies whose partner list exceeds the scratch row).
 template <class F>
 __device__ void partners_small(const World &w, int a, int prevCount, F &&f) {
-  const int4 lo = w.g.cellLo[a], hi = w.g.cellHi[a];
-  const int s = lo.w;
+  const int4 c = w.g.cellLo[a];
+  const int s = c.w;
+  if (s < 0) return;
   for (int k = w.g.largeStart[s]; k < w.g.largeStart[s + 1]; k++) {
     const int b = w.g.largeList[k];
     if (b < a && accept(w, a, b)) f(b);
   }
-  for (int x = lo.x; x <= hi.x; x++)
-    for (int y = lo.y; y <= hi.y; y++)
-      for (int z = lo.z; z <= hi.z; z++) {
-        const uint32_t bucket = cell_hash(x, y, z, s) & w.g.tableMask;
-        const int beg = w.g.tableStart[bucket];
-        int end = beg + w.g.tableCount[bucket];
-        if (end > w.g.entryCap) end = w.g.entryCap;
-        for (int k = beg; k < end; k++) {
-          // entries carry their cell: other cells hashing to this bucket are skipped
-          const Entry &ent = w.g.entries[k];
-          const int b = ent.b2 >> 1;
-          if (b >= a || ent.cx != x || ent.cy != y || ent.cz != z) continue;
-          const int4 bl = w.g.cellLo[b];
-          if (bl.w != s) continue;
-          // the pair is found once: in the minimum corner of the AABB overlap
-          if (max(lo.x, bl.x) != x || max(lo.y, bl.y) != y || max(lo.z, bl.z) != z) continue;
-          if (accept(w, a, b)) f(b);
-        }
-      }
+  for (int ci = 0; ci < 27; ci++) {
+    const int x = c.x + ci / 9 - 1, y = c.y + (ci / 3) % 3 - 1, z = c.z + ci % 3 - 1;
+    const uint32_t bucket = cell_hash(x, y, z, s) & w.g.tableMask;
+    const int beg = w.g.tableStart[bucket];
+    int end = beg + w.g.tableCount[bucket];
+    if (end > w.g.entryCap) end = w.g.entryCap;
+    for (int k = beg; k < end; k++) {
+      const Entry &e = w.g.entries[k];
+      const int b = e.b2 >> 1;
+      if (b >= a || e.cx != x || e.cy != y || e.cz != z) continue;
+      if (w.g.numScenes > 1 && w.b.scene[b] != s) continue;
+      if (accept(w, a, b)) f(b);
+    }
+  }
   int first, last;
   prev_range(w, a, prevCount, first, last);
   for (int m = first; m < last; m++) {
@@ -182,7 +163,7 @@ __global__ void large_count_kernel(World w, int numLarge) {
   const int prevCount = w.ctl->prevCandidates;
   for (int li = blockIdx.x; li < numLarge; li += gridDim.x) {
     const int a = w.g.largeList[li];
-    const int s = w.g.cellLo[a].w;
+    const int s = w.b.scene[a];
     int c = 0;
     for (int b = w.g.sceneStart[s] + threadIdx.x; b < a; b += blockDim.x) c += accept(w, a, b) ? 1 : 0;
     typedef cub::BlockReduce<int, 256> R;
@@ -214,7 +195,7 @@ __device__ void sort_segment(uint64_t *k, int n) {
 // A's exact broad-phase inputs, held in registers during its walk.
 struct BodyA {
   int a, s;
-  int4 lo, hi;
+  int4 c;
   double x, y, z, r;
   bool dyn;
 };
@@ -229,23 +210,20 @@ __device__ __forceinline__ bool accept_entry(const World &w, const BodyA &A, con
 }
 
 // Warp-cooperative enumeration of the partners b < a of a non-large body a:
-// lanes split its cells (and its old manifolds and the scene's large bodies),
-// calling f(b) on the lane that finds b. Each partner is found exactly once:
-// grid pairs in the minimum corner cell of the two AABBs; old manifolds only
-// when the sphere test rejects them; large bodies from the scene's list.
+// lanes take the 27 neighbour cells (and the old manifolds and the scene's
+// large bodies), calling f(b) on the lane that finds b. Each partner is
+// found exactly once: regular bodies live in exactly one cell; old manifolds
+// are added only when the sphere test rejects them.
 template <class F>
 __device__ void warp_partners(const World &w, const BodyA &A, int prevCount, int lane, F &&f) {
   const int a = A.a, s = A.s;
+  if (s < 0) return;
   for (int k = w.g.largeStart[s] + lane; k < w.g.largeStart[s + 1]; k += 32) {
     const int b = w.g.largeList[k];
     if (b < a && accept(w, a, b)) f(b);
   }
-  const int4 lo = A.lo, hi = A.hi;
-  const double inv = w.g.invCell[s];
-  const int nx = hi.x - lo.x + 1, ny = hi.y - lo.y + 1, nz = hi.z - lo.z + 1;
-  const int ncell = (nx > 0 && ny > 0 && nz > 0) ? nx * ny * nz : 0;
-  for (int ci = lane; ci < ncell; ci += 32) {
-    const int x = lo.x + ci / (ny * nz), y = lo.y + (ci / nz) % ny, z = lo.z + ci % nz;
+  if (lane < 27) {
+    const int x = A.c.x + lane / 9 - 1, y = A.c.y + (lane / 3) % 3 - 1, z = A.c.z + lane % 3 - 1;
     const uint32_t bucket = cell_hash(x, y, z, s) & w.g.tableMask;
     const int beg = w.g.tableStart[bucket];
     int end = beg + w.g.tableCount[bucket];
@@ -255,12 +233,6 @@ __device__ void warp_partners(const World &w, const BodyA &A, int prevCount, int
       const int b = e.b2 >> 1;
       // entries carry their cell: other cells hashing to this bucket are skipped
       if (b >= a || e.cx != x || e.cy != y || e.cz != z) continue;
-      // B's cell range, recomputed exactly as the insertion computed it
-      const double rb = e.r * (1.0 + 1e-7) + 1e-9;
-      const int blx = (int)floor((e.x - rb) * inv), bly = (int)floor((e.y - rb) * inv),
-                blz = (int)floor((e.z - rb) * inv);
-      // the pair is found once: in the minimum corner of the AABB overlap
-      if (max(lo.x, blx) != x || max(lo.y, bly) != y || max(lo.z, blz) != z) continue;
       if (w.g.numScenes > 1 && w.b.scene[b] != s) continue;  // another scene's cell, same bucket
       if (accept_entry(w, A, e)) f(b);
     }
@@ -279,9 +251,8 @@ __device__ void warp_partners(const World &w, const BodyA &A, int prevCount, int
 __device__ BodyA body_a(const World &w, int a) {
   BodyA A;
   A.a = a;
-  A.lo = w.g.cellLo[a];
-  A.hi = w.g.cellHi[a];
-  A.s = A.lo.w;
+  A.c = w.g.cellLo[a];
+  A.s = A.c.w;
   const D4 p = w.b.pos[a];
   A.x = p.x; A.y = p.y; A.z = p.z;
   A.r = w.b.size[a].w;
@@ -366,7 +337,7 @@ __global__ void large_write_kernel(World w, int numLarge) {
   __shared__ int base;
   for (int li = blockIdx.x; li < numLarge; li += gridDim.x) {
     const int a = w.g.largeList[li];
-    const int s = w.g.cellLo[a].w;
+    const int s = w.b.scene[a];
     const int beg = w.g.pairStart[a];
     const int n = w.g.pairStart[a + 1] - beg;
     if (beg + n > cap) {

@@ -515,17 +515,30 @@ int avbd_pack(avbd_ctx *ctx, const avbd_world *world) {
   std::vector<uint32_t> prio(n);
   std::vector<std::vector<int>> large(S);
   for (int s = 0; s < S; s++) {
-    // cell size and "large" threshold from the mean radius (broadphase.js:52-59)
-    double sum = 0;
+    // Large bodies: bounding radius above twice the scene's 95th-percentile
+    // radius (a ground box, a wrecking ball). Grid cell: twice the largest
+    // remaining radius, padded so rounding cannot separate overlapping bodies
+    // by more than one cell.
     const int cnt = sceneStart[s + 1] - sceneStart[s];
-    for (int i = sceneStart[s]; i < sceneStart[s + 1]; i++) sum += B.radius[i];
-    const double mean = cnt ? sum / cnt : 1.0;
-    const double thr = std::max(mean * 8, 1e-6);
-    invCell[s] = 1 / std::max(mean * 2, 1e-4);
+    std::vector<double> radii(B.radius + sceneStart[s], B.radius + sceneStart[s + 1]);
+    double r95 = 1.0;
+    if (cnt > 0) {
+      const size_t k = std::min<size_t>((size_t)(0.95 * (cnt - 1)), (size_t)cnt - 1);
+      std::nth_element(radii.begin(), radii.begin() + k, radii.end());
+      r95 = radii[k];
+    }
+    const double thr = 2.0 * r95;
+    double rmax = 0;
+    for (int i = sceneStart[s]; i < sceneStart[s + 1]; i++)
+      if (B.radius[i] <= thr) rmax = std::max(rmax, B.radius[i]);
+    const double cell = std::max(2.0 * rmax * (1.0 + 1e-6) + 1e-9, 1e-4);
+    invCell[s] = 1.0 / cell;
     for (int i = sceneStart[s]; i < sceneStart[s + 1]; i++) {
       const int shape = B.shape ? B.shape[i] : AVBD_SHAPE_BOX;
       if (!(B.mass[i] >= 0) || !std::isfinite(B.mass[i]))
         return fail(ctx, AVBD_ERR_ARG, "body %d: mass must be finite and >= 0", i);
+      if (!(B.radius[i] >= 0) || !std::isfinite(B.radius[i]))
+        return fail(ctx, AVBD_ERR_ARG, "body %d: radius must be finite and >= 0", i);
       size[i] = mkd4(B.size[i * 3], B.size[i * 3 + 1], B.size[i * 3 + 2], B.radius[i]);
       massD[i] = mkd4(B.mass[i], B.moment[i * 3], B.moment[i * 3 + 1], B.moment[i * 3 + 2]);
       massF[i] = make_float4((float)B.mass[i], (float)B.moment[i * 3], (float)B.moment[i * 3 + 1],
@@ -596,18 +609,10 @@ int avbd_pack(avbd_ctx *ctx, const avbd_world *world) {
   }
   cStart[n] = (int)cRef.size();
 
-  // capacities
+  // capacities: one grid insertion per regular body
   long long insertions = 0;
-  for (int i = 0; i < n; i++) {
-    if (flags0[i] & kBodyLarge) continue;
-    const double r = B.radius[i] * (1.0 + 1e-7) + 1e-9, inv = invCell[scene[i]];
-    long long c = 1;
-    for (int k = 0; k < 3; k++) {
-      const double p = B.pos[i * 3 + k];
-      c *= (long long)std::floor((p + r) * inv) - (long long)std::floor((p - r) * inv) + 1;
-    }
-    insertions += c;
-  }
+  for (int i = 0; i < n; i++)
+    if (!(flags0[i] & kBodyLarge)) insertions++;
   const int pairsPerBody = ctx->params.max_pairs_per_body > 0 ? ctx->params.max_pairs_per_body : 16;
   const int cellFactor = std::max(ctx->params.grid_factor, 1);
   ctx->candCap = (int)std::min<long long>((long long)n * pairsPerBody + 256 + world->manifolds.count, 0x3fffffff);
@@ -691,6 +696,7 @@ int avbd_pack(avbd_ctx *ctx, const avbd_world *world) {
       (rc = dalloc(ctx, &w.a.cursor, n + 1)) || (rc = dalloc(ctx, &w.a.cstart, n + 1)) ||
       (rc = dalloc(ctx, &w.a.ccount, n + 1)) ||
       (rc = dalloc(ctx, &w.a.colorStart, kMaxColors + 1)) || (rc = dalloc(ctx, &w.a.colorBodies, n)) ||
+      (rc = dalloc(ctx, &w.a.colorRec, n)) ||
       (rc = dalloc(ctx, &w.a.blockHist, (size_t)ctx->colorBlocks * kMaxColors)))
     return rc;
   // manifolds (double-buffered), candidate keys, adjacency
@@ -707,7 +713,7 @@ int avbd_pack(avbd_ctx *ctx, const avbd_world *world) {
     return rc;
   // launch shape of the persistent solve
   const int maxPerSm = solve_max_blocks_per_sm(ctx->lanes);
-  ctx->lanes = P.lanes_per_body > 0 ? P.lanes_per_body : 16;
+  ctx->lanes = P.lanes_per_body > 0 ? P.lanes_per_body : 32;
   if (ctx->lanes != 1 && ctx->lanes != 2 && ctx->lanes != 4 && ctx->lanes != 8 && ctx->lanes != 16 && ctx->lanes != 32)
     return fail(ctx, AVBD_ERR_ARG, "lanes_per_body must be a power of two <= 32");
   ctx->blocksPerSm = P.blocks_per_sm > 0 ? std::min(P.blocks_per_sm, maxPerSm) : maxPerSm;

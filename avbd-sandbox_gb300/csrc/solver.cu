@@ -451,6 +451,7 @@ __global__ void __launch_bounds__(256) coloring_kernel(World w) {
       int r = base[c] + rankInWarp;
       for (int q = 0; q < warp; q++) r += warpCnt[q][c];
       w.a.colorBodies[r] = i;
+      w.a.colorRec[r] = make_int4(i, w.a.cstart[i], min(w.a.cstart[i + 1], w.a.ccap), 0);
     }
     __syncthreads();
     for (int cc = threadIdx.x; cc < kMaxColors; cc += blockDim.x) {
@@ -474,7 +475,7 @@ struct Sys {  // lower triangles of the three 3x3 blocks + right-hand side
 };
 
 template <class T>
-__device__ inline void zero(Sys<T> &s) {
+__device__ __forceinline__ void zero(Sys<T> &s) {
 #pragma unroll
   for (int k = 0; k < 6; k++) s.l[k] = s.a[k] = T(0);
 #pragma unroll
@@ -489,7 +490,7 @@ __device__ inline T shfl_xor(T v, int m, unsigned mask, int width) {
 }
 
 template <class T>
-__device__ inline void group_reduce(Sys<T> &s, unsigned mask, int G) {
+__device__ __forceinline__ void group_reduce(Sys<T> &s, unsigned mask, int G) {
   for (int m = G >> 1; m > 0; m >>= 1) {
 #pragma unroll
     for (int k = 0; k < 6; k++) {
@@ -511,7 +512,7 @@ __device__ inline constexpr int L(int r, int c) { return r >= c ? (r * (r + 1)) 
 
 // H_lin += k n n^T ; H_ang += k a a^T ; H_cross += k a n^T ; b += f_lin, f_ang
 template <class T>
-__device__ inline void stamp_row(Sys<T> &s, T k, V3<T> n, V3<T> a) {
+__device__ __forceinline__ void stamp_row(Sys<T> &s, T k, V3<T> n, V3<T> a) {
   const T nn[3] = {n.x, n.y, n.z}, aa[3] = {a.x, a.y, a.z};
 #pragma unroll
   for (int r = 0; r < 3; r++)
@@ -528,11 +529,47 @@ __device__ inline void stamp_row(Sys<T> &s, T k, V3<T> n, V3<T> a) {
 
 // maths.js:660-725, unrolled LDL^T (lower storage).
 template <class T>
-__device__ inline void ldlt_solve(const Sys<T> &s, T bl0, T bl1, T bl2, T ba0, T ba1, T ba2, V3<T> &xl, V3<T> &xa) {
+__device__ __forceinline__ void ldlt_solve(const Sys<T> &s, T bl0, T bl1, T bl2, T ba0, T ba1, T ba2, V3<T> &xl, V3<T> &xa) {
   const T A11 = s.l[0], A21 = s.l[1], A22 = s.l[2], A31 = s.l[3], A32 = s.l[4], A33 = s.l[5];
   const T A41 = s.c[0], A42 = s.c[1], A43 = s.c[2], A44 = s.a[0];
   const T A51 = s.c[3], A52 = s.c[4], A53 = s.c[5], A54 = s.a[1], A55 = s.a[2];
   const T A61 = s.c[6], A62 = s.c[7], A63 = s.c[8], A64 = s.a[3], A65 = s.a[4], A66 = s.a[5];
+  if constexpr (sizeof(T) == 4) {
+    // FP32 path: one reciprocal per pivot instead of a division per entry
+    const T i1 = T(1) / A11;
+    const T L21 = A21 * i1, L31 = A31 * i1, L41 = A41 * i1, L51 = A51 * i1, L61 = A61 * i1;
+    const T D2 = A22 - L21 * L21 * A11;
+    const T i2 = T(1) / D2;
+    const T L32 = (A32 - L21 * L31 * A11) * i2, L42 = (A42 - L21 * L41 * A11) * i2;
+    const T L52 = (A52 - L21 * L51 * A11) * i2, L62 = (A62 - L21 * L61 * A11) * i2;
+    const T D3 = A33 - (L31 * L31 * A11 + L32 * L32 * D2);
+    const T i3 = T(1) / D3;
+    const T L43 = (A43 - L31 * L41 * A11 - L32 * L42 * D2) * i3;
+    const T L53 = (A53 - L31 * L51 * A11 - L32 * L52 * D2) * i3;
+    const T L63 = (A63 - L31 * L61 * A11 - L32 * L62 * D2) * i3;
+    const T D4 = A44 - (L41 * L41 * A11 + L42 * L42 * D2 + L43 * L43 * D3);
+    const T i4 = T(1) / D4;
+    const T L54 = (A54 - L41 * L51 * A11 - L42 * L52 * D2 - L43 * L53 * D3) * i4;
+    const T L64 = (A64 - L41 * L61 * A11 - L42 * L62 * D2 - L43 * L63 * D3) * i4;
+    const T D5 = A55 - (L51 * L51 * A11 + L52 * L52 * D2 + L53 * L53 * D3 + L54 * L54 * D4);
+    const T i5 = T(1) / D5;
+    const T L65 = (A65 - L51 * L61 * A11 - L52 * L62 * D2 - L53 * L63 * D3 - L54 * L64 * D4) * i5;
+    const T D6 = A66 - (L61 * L61 * A11 + L62 * L62 * D2 + L63 * L63 * D3 + L64 * L64 * D4 + L65 * L65 * D5);
+    const T i6 = T(1) / D6;
+    const T y1 = bl0;
+    const T y2 = bl1 - L21 * y1;
+    const T y3 = bl2 - L31 * y1 - L32 * y2;
+    const T y4 = ba0 - L41 * y1 - L42 * y2 - L43 * y3;
+    const T y5 = ba1 - L51 * y1 - L52 * y2 - L53 * y3 - L54 * y4;
+    const T y6 = ba2 - L61 * y1 - L62 * y2 - L63 * y3 - L64 * y4 - L65 * y5;
+    xa.z = y6 * i6;
+    xa.y = y5 * i5 - L65 * xa.z;
+    xa.x = y4 * i4 - L54 * xa.y - L64 * xa.z;
+    xl.z = y3 * i3 - L43 * xa.x - L53 * xa.y - L63 * xa.z;
+    xl.y = y2 * i2 - L32 * xl.z - L42 * xa.x - L52 * xa.y - L62 * xa.z;
+    xl.x = y1 * i1 - L21 * xl.y - L31 * xl.z - L41 * xa.x - L51 * xa.y - L61 * xa.z;
+    return;
+  }
   const T L21 = A21 / A11, L31 = A31 / A11, L41 = A41 / A11, L51 = A51 / A11, L61 = A61 / A11;
   const T D1 = A11;
   const T D2 = A22 - L21 * L21 * D1;
@@ -573,7 +610,7 @@ struct BState {
 };
 
 template <class T>
-__device__ inline BState<T> load_state(const World &w, int i) {
+__device__ __forceinline__ BState<T> load_state(const World &w, int i) {
   BState<T> s;
   const float4 qt = ld(&w.b.quatT[i]);
   const Q4<T> qT{(T)qt.x, (T)qt.y, (T)qt.z, (T)qt.w};
@@ -601,7 +638,7 @@ struct ContactEval {
 // manifold.js:358-409 in delta form: C = (1 - alpha) C0 + n_r . (dx_A - dx_B),
 // dx = delta + dtheta x r_world(x_t).
 template <class T>
-__device__ inline ContactEval<T> eval_contact(const V3<T> n[3], T mu, float4 cA, float4 cB, float4 cK, float4 cL,
+__device__ __forceinline__ ContactEval<T> eval_contact(const V3<T> n[3], T mu, float4 cA, float4 cB, float4 cK, float4 cL,
                                               const BState<T> &A, const BState<T> &B, T alpha) {
   const V3<T> rA{(T)cA.x, (T)cA.y, (T)cA.z}, rB{(T)cB.x, (T)cB.y, (T)cB.z};
   const V3<T> u = (A.dp + cross(A.dang, rA)) - (B.dp + cross(B.dang, rB));
@@ -625,7 +662,7 @@ __device__ inline ContactEval<T> eval_contact(const V3<T> n[3], T mu, float4 cA,
 }
 
 template <class T>
-__device__ inline void manifold_rows(const World &w, int m, V3<T> n[3], T &mu, int &cnt) {
+__device__ __forceinline__ void manifold_rows(const World &w, int m, V3<T> n[3], T &mu, int &cnt) {
   const float4 b0 = ld(&w.cur.basis0[m]), b1 = ld(&w.cur.basis1[m]), b2 = ld(&w.cur.basis2[m]);
   n[0] = V3<T>{(T)b0.x, (T)b0.y, (T)b0.z};
   n[1] = V3<T>{(T)b1.x, (T)b1.y, (T)b1.z};
@@ -634,62 +671,76 @@ __device__ inline void manifold_rows(const World &w, int m, V3<T> n[3], T &mu, i
   cnt = ld(&w.cur.count[m]);
 }
 
-// One contact of the body's per-contact adjacency: slot = manifold * 8 + k.
+// One contact of a body's per-contact adjacency (slot = manifold * 8 + k),
+// with everything its primal stamp and dual update read. Loaded once per
+// body update: the dual reuses it, since no other body writes this contact's
+// multiplier and stiffness between this body's primal and dual.
 template <class T>
-__device__ void contact_primal(const World &w, int slot, int side, int other, const BState<T> &self, T alpha,
-                               Sys<T> &s) {
-  const int m = slot >> 3;
+struct ContactData {
   V3<T> n[3];
   T mu;
+  float4 cA, cB, cK, cL;
+  BState<T> o;
+  int slot, side, otherColor;
+  bool sphere;
+};
+
+template <class T>
+__device__ __forceinline__ ContactData<T> load_contact(const World &w, int2 ent, bool selfSphere) {
+  ContactData<T> d;
+  d.slot = ent.x >> 1;
+  d.side = ent.x & 1;
+  const int other = ent.y;
   int cnt;
-  manifold_rows(w, m, n, mu, cnt);
-  const float4 cA = ld(&w.cur.cA[slot]), cB = ld(&w.cur.cB[slot]);
-  const float4 cK = __ldcg(&w.cur.cK[slot]), cL = __ldcg(&w.cur.cL[slot]);
-  const BState<T> o = load_state<T>(w, other);
-  const BState<T> &A = side ? o : self;
-  const BState<T> &B = side ? self : o;
-  const T sgn = side ? T(-1) : T(1);
-  const ContactEval<T> e = eval_contact(n, mu, cA, cB, cK, cL, A, B, alpha);
-  const V3<T> r = side ? V3<T>{(T)cB.x, (T)cB.y, (T)cB.z} : V3<T>{(T)cA.x, (T)cA.y, (T)cA.z};
-  const T kk[3] = {(T)cK.x, (T)cK.y, (T)cK.z};
+  manifold_rows(w, d.slot >> 3, d.n, d.mu, cnt);
+  d.cA = ld(&w.cur.cA[d.slot]);
+  d.cB = ld(&w.cur.cB[d.slot]);
+  d.cK = __ldcg(&w.cur.cK[d.slot]);
+  d.cL = __ldcg(&w.cur.cL[d.slot]);
+  d.o = load_state<T>(w, other);
+  d.otherColor = ld(&w.b.color[other]);
+  d.sphere = selfSphere || (ld(&w.b.flags0[other]) & kBodySphere) != 0;
+  return d;
+}
+
+template <class T>
+__device__ __forceinline__ void contact_primal(const ContactData<T> &d, const BState<T> &self, T alpha, Sys<T> &s) {
+  const BState<T> &A = d.side ? d.o : self;
+  const BState<T> &B = d.side ? self : d.o;
+  const T sgn = d.side ? T(-1) : T(1);
+  const ContactEval<T> e = eval_contact(d.n, d.mu, d.cA, d.cB, d.cK, d.cL, A, B, alpha);
+  const V3<T> r = d.side ? V3<T>{(T)d.cB.x, (T)d.cB.y, (T)d.cB.z} : V3<T>{(T)d.cA.x, (T)d.cA.y, (T)d.cA.z};
+  const T kk[3] = {(T)d.cK.x, (T)d.cK.y, (T)d.cK.z};
   const T ff[3] = {e.F.x, e.F.y, e.F.z};
 #pragma unroll
   for (int row = 0; row < 3; row++) {
-    const V3<T> a = cross(r, n[row]);
-    stamp_row(s, kk[row], n[row], a);
+    const V3<T> a = cross(r, d.n[row]);
+    stamp_row(s, kk[row], d.n[row], a);
     const T f = sgn * ff[row];
-    s.bl[0] += f * n[row].x; s.bl[1] += f * n[row].y; s.bl[2] += f * n[row].z;
+    s.bl[0] += f * d.n[row].x; s.bl[1] += f * d.n[row].y; s.bl[2] += f * d.n[row].z;
     s.ba[0] += f * a.x; s.ba[1] += f * a.y; s.ba[2] += f * a.z;
   }
 }
 
+// manifold.js:447-491 for one contact, with the body's updated state.
 template <class T>
-__device__ void contact_dual(const World &w, int slot, int side, int other, const BState<T> &self, T alpha,
-                             bool sphere) {
-  const int m = slot >> 3;
-  V3<T> n[3];
-  T mu;
-  int cnt;
-  manifold_rows(w, m, n, mu, cnt);
-  const float4 cA = ld(&w.cur.cA[slot]), cB = ld(&w.cur.cB[slot]);
-  float4 cK = __ldcg(&w.cur.cK[slot]);
-  const float4 cL = __ldcg(&w.cur.cL[slot]);
-  const BState<T> o = load_state<T>(w, other);
-  const BState<T> &A = side ? o : self;
-  const BState<T> &B = side ? self : o;
+__device__ __forceinline__ void contact_dual(const World &w, const ContactData<T> &d, const BState<T> &self, T alpha) {
+  const BState<T> &A = d.side ? d.o : self;
+  const BState<T> &B = d.side ? self : d.o;
   const T beta = (T)w.p.betaLin, kmax = (T)w.p.penaltyMax, thr = (T)w.p.stickThreshold;
-  const ContactEval<T> e = eval_contact(n, mu, cA, cB, cK, cL, A, B, alpha);
-  float stick = cL.w;
+  const ContactEval<T> e = eval_contact(d.n, d.mu, d.cA, d.cB, d.cK, d.cL, A, B, alpha);
+  float4 cK = d.cK;
+  float stick = d.cL.w;
   if (e.F.x < T(0)) cK.x = (float)fmin((T)cK.x + beta * fabs(e.C.x), kmax);
   if (e.within) {
     cK.y = (float)fmin((T)cK.y + beta * fabs(e.C.y), kmax);
     cK.z = (float)fmin((T)cK.z + beta * fabs(e.C.z), kmax);
     stick = sqrt(e.C.y * e.C.y + e.C.z * e.C.z) < thr ? 1.f : 0.f;
-  } else if (sphere) {
+  } else if (d.sphere) {
     stick = 0.f;
   }
-  __stcg(&w.cur.cK[slot], cK);
-  __stcg(&w.cur.cL[slot], make_float4((float)e.F.x, (float)e.F.y, (float)e.F.z, stick));
+  __stcg(&w.cur.cK[d.slot], cK);
+  __stcg(&w.cur.cL[d.slot], make_float4((float)e.F.x, (float)e.F.y, (float)e.F.z, stick));
 }
 
 // Joint geometry at the current iterate (joint.js:115-129), delta form.
@@ -700,7 +751,7 @@ struct JointGeo {
 };
 
 template <class T>
-__device__ inline JointGeo<T> joint_geo(const World &w, int j, int2 ab, const BState<T> &A, const BState<T> &B,
+__device__ __forceinline__ JointGeo<T> joint_geo(const World &w, int j, int2 ab, const BState<T> &A, const BState<T> &B,
                                         bool hasA) {
   JointGeo<T> g;
   V3<T> dpt;
@@ -729,7 +780,7 @@ __device__ inline JointGeo<T> joint_geo(const World &w, int j, int2 ab, const BS
 }
 
 template <class T>
-__device__ void joint_primal(const World &w, int j, int side, const BState<T> &self, T alpha, Sys<T> &s) {
+__device__ __forceinline__ void joint_primal(const World &w, int j, int side, const BState<T> &self, T alpha, Sys<T> &s) {
   if (__ldcg(&w.j.state[j])) return;
   const int2 ab = ld(&w.j.bodies[j]);
   const bool hasA = ab.x >= 0;
@@ -806,7 +857,7 @@ __device__ void joint_primal(const World &w, int j, int side, const BState<T> &s
 }
 
 template <class T>
-__device__ void joint_dual(const World &w, int j, int side, const BState<T> &self, T alpha) {
+__device__ __forceinline__ void joint_dual(const World &w, int j, int side, const BState<T> &self, T alpha) {
   if (__ldcg(&w.j.state[j])) return;
   const int2 ab = ld(&w.j.bodies[j]);
   const bool hasA = ab.x >= 0;
@@ -866,7 +917,7 @@ __device__ void joint_dual(const World &w, int j, int side, const BState<T> &sel
 
 // spring.js:447-458: d, |d| and C at the current iterate.
 template <class T>
-__device__ inline bool spring_eval(const World &w, int sIdx, const BState<T> &A, const BState<T> &B, V3<T> &d,
+__device__ __forceinline__ bool spring_eval(const World &w, int sIdx, const BState<T> &A, const BState<T> &B, V3<T> &d,
                                    T &len, V3<T> &rAw, V3<T> &rBw) {
   V3<T> dpt, rAl, rBl;
   if (sizeof(T) == 8) {
@@ -888,7 +939,7 @@ __device__ inline bool spring_eval(const World &w, int sIdx, const BState<T> &A,
 }
 
 template <class T>
-__device__ void spring_primal(const World &w, int sIdx, int side, const BState<T> &self, Sys<T> &s) {
+__device__ __forceinline__ void spring_primal(const World &w, int sIdx, int side, const BState<T> &self, Sys<T> &s) {
   if (__ldcg(&w.s.state[sIdx])) return;
   const int2 ab = ld(&w.s.bodies[sIdx]);
   const BState<T> o = load_state<T>(w, side ? ab.x : ab.y);
@@ -951,7 +1002,7 @@ __device__ void spring_primal(const World &w, int sIdx, int side, const BState<T
 }
 
 template <class T>
-__device__ void spring_dual(const World &w, int sIdx, int side, const BState<T> &self) {
+__device__ __forceinline__ void spring_dual(const World &w, int sIdx, int side, const BState<T> &self) {
   if (__ldcg(&w.s.state[sIdx])) return;
   const int2 ab = ld(&w.s.bodies[sIdx]);
   const BState<T> o = load_state<T>(w, side ? ab.x : ab.y);
@@ -981,16 +1032,66 @@ __device__ void spring_dual(const World &w, int sIdx, int side, const BState<T> 
 // (static endpoints have colour -1).
 __device__ inline bool owns(int myColor, int otherColor) { return myColor > otherColor; }
 
+// Out-of-line helpers for the less common entries of a body's update: its
+// joints and springs, and contacts beyond the first one per lane. Keeping
+// them out of line keeps the common path (one contact per lane, held in
+// registers from the primal stamp to the dual update) within the register
+// budget of two resident blocks per SM; the callee pays its own spills.
 template <class T>
-__device__ void solve_body(const World &w, int i, int lane, int G, unsigned mask, T alpha, bool dual, bool velocity) {
+__device__ __noinline__ void extra_primal(const World &w, int i, int cb, int nm, int cStart, int total, int lane,
+                                          int G, bool selfSphere, const BState<T> &self, T alpha, Sys<T> &s) {
+  for (int e = lane; e < total; e += G) {
+    if (e < nm) {
+      if (e == lane) continue;  // the lane's first contact is handled inline
+      contact_primal<T>(load_contact<T>(w, ld(&w.a.centry[cb + e]), selfSphere), self, alpha, s);
+    } else {
+      const uint32_t ref = ld(&w.g.cRef[cStart + e - nm]);
+      const uint32_t type = ref >> 30, idx = (ref >> 1) & 0x1fffffffu, side = ref & 1u;
+      if (type == kRefJoint) joint_primal<T>(w, (int)idx, (int)side, self, alpha, s);
+      else spring_primal<T>(w, (int)idx, (int)side, self, s);
+    }
+  }
+}
+
+template <class T>
+__device__ __noinline__ void extra_dual(const World &w, int i, int cb, int nm, int cStart, int total, int lane, int G,
+                                        bool selfSphere, const BState<T> &self, T alpha) {
+  const int myColor = ld(&w.b.color[i]);
+  for (int e = lane; e < total; e += G) {
+    if (e < nm) {
+      if (e == lane) continue;
+      const ContactData<T> d = load_contact<T>(w, ld(&w.a.centry[cb + e]), selfSphere);
+      if (owns(myColor, d.otherColor)) contact_dual<T>(w, d, self, alpha);
+    } else {
+      const uint32_t ref = ld(&w.g.cRef[cStart + e - nm]);
+      const uint32_t type = ref >> 30, idx = (ref >> 1) & 0x1fffffffu, side = ref & 1u;
+      const int2 ab = type == kRefJoint ? ld(&w.j.bodies[idx]) : ld(&w.s.bodies[idx]);
+      const int other = side ? ab.x : ab.y;
+      const int oc = other >= 0 ? ld(&w.b.color[other]) : -1;
+      if (!owns(myColor, oc)) continue;
+      if (type == kRefJoint) joint_dual<T>(w, (int)idx, (int)side, self, alpha);
+      else spring_dual<T>(w, (int)idx, (int)side, self);
+    }
+  }
+}
+
+// One body's update (solver.js:425-457) by a group of G lanes, followed by
+// the dual updates (manifold.js:447, joint.js:255, spring.js:618) of the
+// constraints it owns, and on the last main iteration its BDF1 velocity.
+template <class T>
+__device__ void solve_body(const World &w, int4 rec, int lane, int G, unsigned mask, T alpha, bool dual, bool velocity) {
   const SolverParams &P = w.p;
   const T dt = (T)P.dt, dt2 = (T)(P.dt * P.dt);
+  const int i = rec.x, cb = rec.y, nm = rec.z - rec.y;
+  // one round of loads: own state, constraint ranges and this lane's first contact
   BState<T> self = load_state<T>(w, i);
-  const int cb = ld(&w.a.cstart[i]);
-  int ce = ld(&w.a.cstart[i + 1]);
-  if (ce > w.a.ccap) ce = w.a.ccap;
   const int cStart = ld(&w.g.cStart[i]), cEnd = ld(&w.g.cStart[i + 1]);
-  const int nm = ce - cb, total = nm + (cEnd - cStart);
+  const int total = nm + (cEnd - cStart);
+  const bool selfSphere = (ld(&w.b.flags0[i]) & kBodySphere) != 0;
+  const bool has0 = lane < nm;
+  ContactData<T> d0;
+  if (has0) d0 = load_contact<T>(w, ld(&w.a.centry[cb + lane]), selfSphere);
+  const bool extra = total > nm || nm > G;  // joints, springs or more contacts than lanes
 
   Sys<T> s;
   zero(s);
@@ -1004,7 +1105,7 @@ __device__ void solve_body(const World &w, int i, int lane, int G, unsigned mask
     s.bl[0] = ml * dy.x; s.bl[1] = ml * dy.y; s.bl[2] = ml * dy.z;
     // world moment R I R^T (rigid.js:228-247), / dt^2
     T M[9];
-    const bool iso = !P.rotatedInertia || (ld(&w.b.flags0[i]) & kBodySphere);
+    const bool iso = !P.rotatedInertia || selfSphere;
     const T I0 = (T)md.y, I1 = (T)md.z, I2 = (T)md.w;
     if (iso) {
       M[0] = I0; M[1] = 0; M[2] = 0; M[3] = 0; M[4] = I1; M[5] = 0; M[6] = 0; M[7] = 0; M[8] = I2;
@@ -1030,17 +1131,8 @@ __device__ void solve_body(const World &w, int i, int lane, int G, unsigned mask
     s.ba[1] = (M[3] * dq.x + M[4] * dq.y + M[5] * dq.z) / dt2;
     s.ba[2] = (M[6] * dq.x + M[7] * dq.y + M[8] * dq.z) / dt2;
   }
-  for (int e = lane; e < total; e += G) {
-    if (e < nm) {
-      const int2 ent = ld(&w.a.centry[cb + e]);
-      contact_primal<T>(w, ent.x >> 1, ent.x & 1, ent.y, self, alpha, s);
-    } else {
-      const uint32_t ref = ld(&w.g.cRef[cStart + e - nm]);
-      const uint32_t type = ref >> 30, idx = (ref >> 1) & 0x1fffffffu, side = ref & 1u;
-      if (type == kRefJoint) joint_primal<T>(w, (int)idx, (int)side, self, alpha, s);
-      else spring_primal<T>(w, (int)idx, (int)side, self, s);
-    }
-  }
+  if (has0) contact_primal<T>(d0, self, alpha, s);
+  if (extra) extra_primal<T>(w, i, cb, nm, cStart, total, lane, G, selfSphere, self, alpha, s);
   group_reduce(s, mask, G);
   V3<T> xl, xa;
   ldlt_solve(s, -s.bl[0], -s.bl[1], -s.bl[2], -s.ba[0], -s.ba[1], -s.ba[2], xl, xa);
@@ -1058,43 +1150,23 @@ __device__ void solve_body(const World &w, int i, int lane, int G, unsigned mask
       stcg(&w.b.quatD[i], mkd4((double)self.q.x, (double)self.q.y, (double)self.q.z, (double)self.q.w));
     }
     if (velocity) {  // BDF1 (solver.js:476-488)
-      const float4 v = ld(&w.b.vel[i]);
-      w.b.prevVel[i] = v;
-      const V3<T> vn = self.dp * (T(1) / dt);
+      w.b.prevVel[i] = ld(&w.b.vel[i]);
       w.b.vel[i] = make_float4((float)(self.dp.x / dt), (float)(self.dp.y / dt), (float)(self.dp.z / dt), 0.f);
-      (void)vn;
       w.b.omega[i] = make_float4((float)(self.dang.x / dt), (float)(self.dang.y / dt), (float)(self.dang.z / dt), 0.f);
     }
   }
   if (!dual) return;
-  const int myColor = ld(&w.b.color[i]);
-  const bool selfSphere = (ld(&w.b.flags0[i]) & kBodySphere) != 0;
-  for (int e = lane; e < total; e += G) {
-    if (e < nm) {
-      const int2 ent = ld(&w.a.centry[cb + e]);
-      if (owns(myColor, ld(&w.b.color[ent.y]))) {
-        const bool sphere = selfSphere || (ld(&w.b.flags0[ent.y]) & kBodySphere) != 0;
-        contact_dual<T>(w, ent.x >> 1, ent.x & 1, ent.y, self, alpha, sphere);
-      }
-    } else {
-      const uint32_t ref = ld(&w.g.cRef[cStart + e - nm]);
-      const uint32_t type = ref >> 30, idx = (ref >> 1) & 0x1fffffffu, side = ref & 1u;
-      const int2 ab = type == kRefJoint ? ld(&w.j.bodies[idx]) : ld(&w.s.bodies[idx]);
-      const int other = side ? ab.x : ab.y;
-      const int oc = other >= 0 ? ld(&w.b.color[other]) : -1;
-      if (!owns(myColor, oc)) continue;
-      if (type == kRefJoint) joint_dual<T>(w, (int)idx, (int)side, self, alpha);
-      else spring_dual<T>(w, (int)idx, (int)side, self);
-    }
-  }
+  // dual updates of the constraints this body owns (it has the larger colour)
+  if (has0 && owns(ld(&w.b.color[i]), d0.otherColor)) contact_dual<T>(w, d0, self, alpha);
+  if (extra) extra_dual<T>(w, i, cb, nm, cStart, total, lane, G, selfSphere, self, alpha);
 }
 
 // The FP64 path is kept out of line so that its register demand (and any
 // spills under the 2-blocks-per-SM bound) stays in the rare FP64 bodies
 // instead of lowering the occupancy of the FP32 path.
-__device__ __noinline__ void solve_body_f64(const World &w, int i, int lane, int G, unsigned mask, double alpha,
+__device__ __noinline__ void solve_body_f64(const World &w, int4 rec, int lane, int G, unsigned mask, double alpha,
                                             bool dual, bool velocity) {
-  solve_body<double>(w, i, lane, G, mask, alpha, dual, velocity);
+  solve_body<double>(w, rec, lane, G, mask, alpha, dual, velocity);
 }
 
 __global__ void __launch_bounds__(kSolveBlock, 2) solve_kernel(World w, int G) {
@@ -1104,7 +1176,8 @@ __global__ void __launch_bounds__(kSolveBlock, 2) solve_kernel(World w, int G) {
   const int lane = threadIdx.x & (G - 1);
   const int warpLane = threadIdx.x & 31;
   const unsigned mask = (G == 32 ? 0xffffffffu : (((1u << G) - 1u) << (warpLane & ~(G - 1))));
-  const int group = (blockIdx.x * blockDim.x + threadIdx.x) / G;
+  // groups interleaved across blocks, so a thin colour still spreads over all SMs
+  const int group = (threadIdx.x / G) * gridDim.x + blockIdx.x;
   const int groups = (gridDim.x * blockDim.x) / G;
   const int total = P.iterations + (P.postStabilize ? 1 : 0);
   for (int it = 0; it < total; it++) {
@@ -1114,9 +1187,9 @@ __global__ void __launch_bounds__(kSolveBlock, 2) solve_kernel(World w, int G) {
     for (int c = 0; c < numColors; c++) {
       const int beg = ld(&w.a.colorStart[c]), end = ld(&w.a.colorStart[c + 1]);
       for (int k = beg + group; k < end; k += groups) {
-        const int i = ld(&w.a.colorBodies[k]);
-        if (ld(&w.b.flags[i]) & kBodyFp64) solve_body_f64(w, i, lane, G, mask, alpha, dual, vel);
-        else solve_body<float>(w, i, lane, G, mask, (float)alpha, dual, vel);
+        const int4 rec = ld(&w.a.colorRec[k]);
+        if (ld(&w.b.flags[rec.x]) & kBodyFp64) solve_body_f64(w, rec, lane, G, mask, alpha, dual, vel);
+        else solve_body<float>(w, rec, lane, G, mask, (float)alpha, dual, vel);
       }
       if (!grid_barrier(ctl)) return;
     }
@@ -1197,10 +1270,11 @@ __global__ void __launch_bounds__(kSolveBlock, 2) wave_kernel(World w, int G) {
     for (int c = 0; c < numColors; c++) {
       const int beg = ld(&w.a.colorStart[c]), end = ld(&w.a.colorStart[c + 1]);
       for (int k = beg + group; k < end; k += groups) {
-        const int i = ld(&w.a.colorBodies[k]);
+        const int4 rec = ld(&w.a.colorRec[k]);
+        const int i = rec.x;
         if (!wait_neighbors(w, i, it, lane, G, mask)) return;
-        if (ld(&w.b.flags[i]) & kBodyFp64) solve_body_f64(w, i, lane, G, mask, alpha, dual, vel);
-        else solve_body<float>(w, i, lane, G, mask, (float)alpha, dual, vel);
+        if (ld(&w.b.flags[i]) & kBodyFp64) solve_body_f64(w, rec, lane, G, mask, alpha, dual, vel);
+        else solve_body<float>(w, rec, lane, G, mask, (float)alpha, dual, vel);
         __threadfence();
         __syncwarp(mask);
         if (lane == 0) st_release(&w.b.progress[i], it + 1);
