@@ -131,7 +131,9 @@ class Stats(C.Structure):
 class Profile(C.Structure):
     _fields_ = [("broadphase_ms", C.c_double), ("narrowphase_ms", C.c_double),
                 ("prepare_ms", C.c_double), ("coloring_ms", C.c_double),
-                ("solve_ms", C.c_double), ("step_ms", C.c_double)]
+                ("solve_ms", C.c_double), ("step_ms", C.c_double),
+                ("candidate_pairs", C.c_int64), ("manifolds", C.c_int64), ("contacts", C.c_int64),
+                ("colors", C.c_int32), ("fp64_bodies", C.c_int32)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

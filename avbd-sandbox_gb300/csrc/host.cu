@@ -391,6 +391,13 @@ int one_step(avbd_ctx *ctx) {
     float tot = 0;
     cudaEventElapsedTime(&tot, ctx->ev[0], ctx->ev[6]);
     ctx->prof.step_ms = tot;
+    Control c{};
+    CK(cudaMemcpy(&c, w.ctl, sizeof(Control), cudaMemcpyDeviceToHost));
+    ctx->prof.candidate_pairs = c.numCandidates;
+    ctx->prof.manifolds = c.liveManifolds;
+    ctx->prof.contacts = c.liveContacts;
+    ctx->prof.colors = c.numColors;
+    ctx->prof.fp64_bodies = c.fp64Bodies;
   }
   return AVBD_OK;
 }

@@ -4,15 +4,20 @@ Workload (one "step" = one AVBD world step of the whole scene): the dense
 pile - a square pyramid of 53 layers (layer k is a k x k grid of 1 m cubes,
 51,039 cubes, 1% gap, 1000 kg/m^3, mu 0.6) on the ground, with a 2 m-radius
 sphere (5000 kg/m^3) dropped onto the apex at 10 m/s; dt = 1/60 s,
-10 iterations, gravity -9.81. Synthetic scene, seeded and deterministic.
+10 iterations, gravity -9.81, 600 steps. Synthetic scene, seeded and
+deterministic.
 
-Timing: W warm-up steps, then exactly K steps. Each step's device time comes
-from CUDA events recorded by the library on its own stream around the whole
-step; L2 is flushed (a 256 MB write) between steps, outside those events.
-The JSON line also carries the roofline of the dominant kernel, the f64 CPU
-baseline (the oracle, 1 thread, a bounded sample of the same scene), the
-end-to-end rate through the C ABI with host buffers, the kernel launch count
-and the SM clocks sampled during the timed region.
+Timing: W warm-up steps, then the scene is packed again and exactly K steps
+are timed from its initial state (K = 600 by default: the whole run, from
+the standing pyramid to the crushed pile). Each step's device time comes from
+CUDA events recorded by the library on its own stream around the whole step;
+L2 is flushed (a 256 MB write) between steps, outside those events.
+The JSON line also carries the roofline of the dominant kernel (algorithmic
+bytes from each step's own pair/manifold/contact counts), the f64 CPU
+baseline (the oracle, 1 thread, single steps from states sampled along the
+same trajectory), the end-to-end rate through the C ABI with host buffers
+(state upload + step + state readback every step, over the same K steps), the
+kernel launch count and the SM clocks sampled during the timed region.
 
 `--impl reference` times the reference's CPU algorithm on the host cores
 (the oracle restatement: the reference engine is JavaScript and no
@@ -38,7 +43,9 @@ for _p in (ROOT, os.path.join(ROOT, "oracle")):
 
 METRIC = "AVBD steps/s at 51k boxes vs f64 CPU ref; batched & adjoint steps/s at tol"
 UNIT = "steps/s"
-WORKLOAD = ("pyramid: 53 layers = 51,039 1 m cubes (1% gap, 1000 kg/m^3, mu 0.6) + ground + r=2 m sphere "
+def workload(layers):
+    cubes = layers * (layers + 1) * (2 * layers + 1) // 6
+    return (f"pyramid: {layers} layers = {cubes:,} 1 m cubes (1% gap, 1000 kg/m^3, mu 0.6) + ground + r=2 m sphere "
             "(5000 kg/m^3, 10 m/s onto the apex); dt=1/60, 10 iterations, gravity -9.81")
 
 
@@ -66,26 +73,35 @@ def dist_env():
 # ---------------------------------------------------------------------------
 # CPU baseline: the f64 oracle, one thread, a bounded sample of the workload
 # ---------------------------------------------------------------------------
-def cpu_baseline(scene, params, budget_s=20.0, warm=3, max_steps=30):
+def cpu_baseline(params, snapshots, budget_s=45.0):
+    """Time the oracle on single steps taken from states of the timed
+    trajectory (`snapshots`: (step index, world with warm-start manifolds)),
+    in the given order until the budget is spent. The mean of those step times
+    estimates the mean CPU step over the same run."""
     from oracle import Oracle
 
-    o = Oracle(params, scene.world())
-    o.step(warm)  # layers settle into contact (they start 1 cm apart)
-    times = []
+    times, used = [], []
     t_all = time.perf_counter()
-    while len(times) < max_steps and (time.perf_counter() - t_all) < budget_s:
+    for step_idx, snap in snapshots:
+        if times and time.perf_counter() - t_all > budget_s:
+            break
+        o = Oracle(params, snap)
         t0 = time.perf_counter()
         o.step(1)
         times.append(time.perf_counter() - t0)
-    med = statistics.median(times)
+        used.append(step_idx)
+        del o
+    mean = sum(times) / len(times)
     return {
-        "value": 1.0 / med,
+        "value": 1.0 / mean,
         "unit": UNIT,
         "cores": 1,
         "kind": "port",
-        "sample": f"steps {warm + 1}..{warm + len(times)} of the same scene from its initial state; median of "
-                  f"{len(times)} single-thread steps ({sum(times):.1f} s of CPU work)",
-        "ms_per_step": med * 1e3,
+        "sample": f"one single-thread f64 step from each of the states after steps {sorted(used)} of the same "
+                  f"run (loaded with their warm-start manifolds); mean of {len(times)} steps "
+                  f"({sum(times):.1f} s of CPU work) estimates the run's mean step",
+        "ms_per_step": mean * 1e3,
+        "sampled_ms": [round(t * 1e3, 1) for t in times],
     }
 
 
@@ -142,9 +158,20 @@ class ClockSampler:
 
 
 # ---------------------------------------------------------------------------
-# roofline of the dominant kernel (algorithmic bytes)
+# roofline of the dominant kernel: algorithmic bytes per launch
 # ---------------------------------------------------------------------------
 def algorithmic_bytes(kind, st, n_dyn, iterations, n_joints=0, n_springs=0):
+    """Bytes a launch must move at minimum, from the step's own counts.
+
+    solve (per iteration): each dynamic body reads its state, inertial target,
+    mass and moments (72 B) and writes p, q (28 B); each manifold side reads the
+    basis and the other body's state (92 B), each contact side reads rA, rB,
+    C0, k, lambda (60 B); the dual reads basis + both bodies (148 B) per
+    manifold and 60 B, writes 28 B per contact; joints and springs likewise.
+    narrowphase: per candidate pair both bodies' pose and size (2 x 56 B) + the
+    pair key and previous index (8 B) + the previous manifold header (84 B);
+    per live manifold its key, count and basis (132 B written); per contact
+    the old record read (60 B) and the new one written (80 B)."""
     N_m, N_c, N_p = st["manifolds"], st["contacts"], st["candidate_pairs"]
     if kind == "solve":
         per_iter = (n_dyn * 100 + N_m * (2 * 92 + 148) + N_c * (2 * 60 + 88) + n_joints * (160 + 2 * 56)
@@ -164,20 +191,20 @@ def read_peaks():
         return 6800.0, "fallback"
 
 
-def read_traffic(kernel):
-    """Per-launch DRAM bytes of `kernel` from the committed ncu summary."""
+def read_traffic(kernel, units_per_launch):
+    """DRAM bytes per launch of `kernel`: the per-unit traffic of a committed
+    ncu capture (profiles/traffic.json) scaled to this run's units per launch."""
     path = os.path.join(ROOT, "profiles", "traffic.json")
     try:
         with open(path) as f:
-            return json.load(f).get(kernel)
+            d = json.load(f)[kernel]
+        return d["dram_bytes"] / d["units"] * units_per_launch
     except Exception:
         return None
 
 
 # ---------------------------------------------------------------------------
 def run_gpu(args):
-    import ctypes
-
     import torch
 
     ws, rank, local = dist_env()
@@ -194,20 +221,25 @@ def run_gpu(args):
     gpu = backend.GpuBackend(params)
     gpu.pack(world)
     n_dyn = int((world.mass > 0).sum())
+    K = args.steps
 
     gpu.step(args.warmup)
     gpu.idle()
+    gpu.pack(world)  # back to the initial state: the timed steps are steps 1..K of the run
     flush = torch.empty(256 * 1024 * 1024 // 4, dtype=torch.float32, device="cuda")
     gpu.set_profiling(True)
     launches0 = gpu.kernel_launches
     phase_tot = {k: 0.0 for k in ("broadphase_ms", "narrowphase_ms", "prepare_ms", "coloring_ms", "solve_ms")}
+    algo_tot = {"solve": 0.0, "narrowphase": 0.0}
     step_ms = []
+    work = {"candidate_pairs": 0, "manifolds": 0, "contacts": 0}
+    peak_work = dict(work, colors=0, fp64_bodies=0)
     if ws > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     with ClockSampler(local) as clk:
-        for _ in range(args.steps):
+        for _ in range(K):
             flush.fill_(1.0)  # L2 flush, outside the step's events
             torch.cuda.synchronize()
             gpu.step(1)
@@ -215,6 +247,12 @@ def run_gpu(args):
             step_ms.append(p["step_ms"])
             for k in phase_tot:
                 phase_tot[k] += p[k]
+            for kind in algo_tot:
+                algo_tot[kind] += algorithmic_bytes(kind, p, n_dyn, params.iterations)
+            for k in work:
+                work[k] += p[k]
+            for k in peak_work:
+                peak_work[k] = max(peak_work[k], p[k])
     gpu.idle()
     torch.cuda.synchronize()
     wall = time.perf_counter() - t0
@@ -224,71 +262,82 @@ def run_gpu(args):
         t = torch.tensor([dev_s], dtype=torch.float64, device="cuda")
         torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
         dev_s = float(t.item())
-    st = gpu.last_stats
     gpu.set_profiling(False)
 
-    # back-to-back steady state (no flush, no per-step sync), for information
-    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    gpu.idle()
-    t1 = time.perf_counter()
-    gpu.step(args.steps)
-    gpu.idle()
-    b2b = (time.perf_counter() - t1) / args.steps
-
-    # end to end through the C ABI with host buffers: upload state, step, read back
-    e2e_steps = max(3, min(args.steps, 20))
+    # end to end through the C ABI with host buffers, over the same K steps:
+    # every step uploads the state from host arrays (avbd_write_state), steps,
+    # and reads the state back (avbd_read_state). States for the CPU baseline
+    # are captured on the way, outside the clock.
+    snap_at = [int((i + 0.5) * K / 3) for i in (1, 0, 2)] if rank == 0 and not args.no_cpu_baseline else []
+    snapshots = []
+    gpu.pack(world)
     host = gpu.read_state()
-    gpu.idle()
-    t2 = time.perf_counter()
-    for _ in range(e2e_steps):
+    e2e_s = 0.0
+    for i in range(K):
+        t1 = time.perf_counter()
         gpu.write_state(host)
         gpu.step(1)
         gpu.sync_to_cpu(host)
-    e2e_s = (time.perf_counter() - t2) / e2e_steps
+        e2e_s += time.perf_counter() - t1
+        if i + 1 in snap_at:
+            snapshots.append((i + 1, gpu.read_state(manifolds=True)))
+    if ws > 1:
+        t = torch.tensor([e2e_s], dtype=torch.float64, device="cuda")
+        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+        e2e_s = float(t.item())
+    snapshots.sort(key=lambda x: snap_at.index(x[0]))
     n = world.n_bodies
     per_body = 32 + 4 * 16  # f64 position (D4) + quaternion, velocity, angular velocity, previous velocity (float4)
 
     # dominant kernel and its roofline
-    phases = {k: v / args.steps for k, v in phase_tot.items()}
-    kinds = {"solve_ms": ("solve", "solve_kernel"), "narrowphase_ms": ("narrowphase", "narrowphase_kernel")}
+    phases = {k: v / K for k, v in phase_tot.items()}
+    solve_kernel = "wave_kernel" if params.schedule == 1 else "solve_kernel"
+    kinds = {"solve_ms": ("solve", solve_kernel), "narrowphase_ms": ("narrowphase", "narrowphase_kernel")}
     dom = max(kinds, key=lambda k: phases[k])
     kind, kname = kinds[dom]
-    algo = algorithmic_bytes(kind, st, n_dyn, params.iterations)
+    algo = algo_tot[kind] / K
     peak, peak_src = read_peaks()
     achieved = algo / (phases[dom] / 1e3) / 1e9
-    traffic = read_traffic(kname)
-    value = ws * args.steps / dev_s
+    traffic = read_traffic(kname, algo)
+    value = ws * K / dev_s
     clocks = clk.summary()
+    other = "narrowphase" if kind == "solve" else "solve"
+    oms = phases["narrowphase_ms" if kind == "solve" else "solve_ms"]
     out = {
         "metric": METRIC,
         "value": value,
         "unit": UNIT,
         "n_gpus": ws,
-        "steps": args.steps,
+        "steps": K,
         "warmup": args.warmup,
-        "ms_per_step": dev_s * 1e3 / args.steps,
+        "ms_per_step": dev_s * 1e3 / K,
         "higher_is_better": True,
         "scaling": "weak",
         "vs_baseline": None,
         "dtype": "f32 (f64 narrowphase geometry, f64 positions and joint multipliers)",
         "data": "synthetic",
-        "config": {"workload": WORKLOAD, "bodies": n, "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU",
+        "config": {"workload": workload(args.layers), "bodies": n, "timed_steps": f"steps 1..{K} of the run from its initial state",
+                   "parallelism": f"replicas x{ws}" if ws > 1 else "single GPU",
                    "l2": "flushed between steps (256 MB write), outside the timed step events"},
         "roofline": {"bound": "hbm", "kernel": kname, "achieved": achieved, "peak": peak, "unit": "GB/s",
                      "frac": achieved / peak, "peak_source": peak_src, "traffic": traffic,
-                     "algorithmic_bytes_per_launch": algo, "launch_ms": phases[dom]},
-        "e2e": {"value": 1.0 / e2e_s, "unit": UNIT, "h2d_bytes_per_step": n * per_body,
+                     "algorithmic_bytes_per_launch": algo, "launch_ms": phases[dom],
+                     "other": {"kernel": other, "achieved": algo_tot[other] / K / (oms / 1e3) / 1e9,
+                               "frac": algo_tot[other] / K / (oms / 1e3) / 1e9 / peak, "launch_ms": oms}},
+        "e2e": {"value": ws * K / e2e_s, "unit": UNIT, "h2d_bytes_per_step": n * per_body,
                 "d2h_bytes_per_step": n * per_body,
-                "how": "avbd_write_state + avbd_step(1) + avbd_read_state per step, pinned staging, host f64 arrays"},
+                "how": "avbd_write_state + avbd_step(1) + avbd_read_state every step over the same run, pinned "
+                       "staging, host f64 arrays"},
         "gpu_launches": launches,
         "clocks": clocks,
         "phases_ms": phases,
-        "back_to_back_steps_per_s": 1.0 / b2b,
         "wall_s": wall,
-        "stats": {k: st[k] for k in ("manifolds", "contacts", "candidate_pairs", "colors", "fp64_bodies")},
+        "mean_work_per_step": {k: v / K for k, v in work.items()},
+        "peak_work": peak_work,
     }
-    if rank == 0 and not args.no_cpu_baseline:
-        out["cpu_baseline"] = cpu_baseline(s, params, budget_s=args.cpu_budget)
+    if rank == 0 and snapshots:
+        ref_params = params_for(abi, s, body_order=abi.ORDER_REFERENCE)
+        out["cpu_baseline"] = cpu_baseline(ref_params, snapshots, budget_s=args.cpu_budget)
     if rank == 0:
         print(json.dumps(out), flush=True)
     if ws > 1:
@@ -296,7 +345,11 @@ def run_gpu(args):
 
 
 def run_reference(args):
-    """The reference's CPU engine algorithm (oracle restatement), host cores."""
+    """The reference's CPU engine algorithm (oracle restatement, index-order
+    colouring as the reference's CPU solver), one host thread: the reference
+    engine is single-threaded sequential Gauss-Seidel. It steps the same run
+    from its initial state: min(W, 3) untimed steps, then consecutive timed
+    steps until K steps or the time budget is reached."""
     ws, rank, _ = dist_env()
     if rank != 0:
         return
@@ -306,28 +359,25 @@ def run_reference(args):
     s = make_scene(args.layers)
     params = params_for(abi, s, body_order=abi.ORDER_REFERENCE)
     o = Oracle(params, s.world())
-    o.step(3)
-    # each measured step is one step of the same workload; bounded to a few minutes
-    n = max(1, min(args.steps, int(args.cpu_budget * 3)))
-    o.step(min(args.warmup, 2))
+    warm = min(args.warmup, 3)
+    o.step(warm)
     times = []
-    for _ in range(n):
+    while len(times) < args.steps and sum(times) < args.ref_budget:
         t0 = time.perf_counter()
         o.step(1)
         times.append(time.perf_counter() - t0)
-        if sum(times) > args.cpu_budget * 6:
-            break
     tot = sum(times)
     value = len(times) / tot
+    sample = (f"steps {warm + 1}..{warm + len(times)} of the run from its initial state, "
+              f"{tot:.1f} s of single-thread f64 work; the early steps carry fewer contacts than the run's "
+              "later ones, so this rate is above the run's mean CPU rate")
     out = {
         "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": ws, "steps": len(times),
-        "warmup": 3 + min(args.warmup, 2), "ms_per_step": tot * 1e3 / len(times), "higher_is_better": True,
+        "warmup": warm, "ms_per_step": tot * 1e3 / len(times), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
-        "config": {"workload": WORKLOAD, "bodies": s.world().n_bodies},
+        "config": {"workload": workload(args.layers), "bodies": s.world().n_bodies},
         "impl": "reference",
-        "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1, "kind": "port",
-                         "sample": f"{len(times)} consecutive steps of the same scene after 3 + warm-up steps; the "
-                                   "reference engine is single-threaded sequential Gauss-Seidel, so 1 thread"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": 1, "kind": "port", "sample": sample},
         "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }
     print(json.dumps(out), flush=True)
@@ -336,11 +386,12 @@ def run_reference(args):
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
-    ap.add_argument("--steps", type=int, default=60)
-    ap.add_argument("--warmup", type=int, default=10)
+    ap.add_argument("--steps", type=int, default=600)
+    ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
     ap.add_argument("--layers", type=int, default=53)
-    ap.add_argument("--cpu-budget", type=float, default=20.0)
+    ap.add_argument("--cpu-budget", type=float, default=45.0)
+    ap.add_argument("--ref-budget", type=float, default=120.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     args = ap.parse_args()
     if args.warmup < 3:

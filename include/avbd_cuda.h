@@ -217,7 +217,8 @@ typedef struct avbd_stats {
   double max_penalty;
 } avbd_stats;
 
-/* Per-phase device times of the last step, ms (src/physics/gpu/backend.js:58). */
+/* Per-phase device times of the last step, ms (src/physics/gpu/backend.js:58),
+   and the work that step did (the counters the phase times are divided by). */
 typedef struct avbd_profile {
   double broadphase_ms;
   double narrowphase_ms;
@@ -225,6 +226,11 @@ typedef struct avbd_profile {
   double coloring_ms;
   double solve_ms;
   double step_ms;
+  int64_t candidate_pairs;    /* pairs the narrow phase tested              */
+  int64_t manifolds;          /* manifolds with at least one contact        */
+  int64_t contacts;           /* contact points in those manifolds          */
+  int32_t colors;
+  int32_t fp64_bodies;
 } avbd_profile;
 
 typedef struct avbd_ctx avbd_ctx;

@@ -7,7 +7,7 @@ one step on each side must give:
   * the same colouring as the oracle's integer-priority greedy colouring,
     which is also the order the oracle replays (AVBD_ORDER_PRIORITY)
   * body states within the FP32 tolerance below
-Tolerances: positions 1e-5 m (the spec single-step bound), orientation
+Tolerances: positions 1e-5 m (the FP32 single-step position bound), orientation
 components 1e-5, velocities 1e-3 m/s (= 1e-5 m / dt + rounding of delta/dt).
 """
 import importlib
