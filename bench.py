@@ -238,6 +238,7 @@ def run_gpu(args):
         torch.distributed.barrier()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
+    trace = open(args.trace, "w") if args.trace and rank == 0 else None
     with ClockSampler(local) as clk:
         for _ in range(K):
             flush.fill_(1.0)  # L2 flush, outside the step's events
@@ -253,6 +254,13 @@ def run_gpu(args):
                 work[k] += p[k]
             for k in peak_work:
                 peak_work[k] = max(peak_work[k], p[k])
+            if trace:
+                rec = dict(p, step=len(step_ms))
+                for kind in algo_tot:
+                    rec[f"algorithmic_bytes_{kind}"] = algorithmic_bytes(kind, p, n_dyn, params.iterations)
+                trace.write(json.dumps(rec) + "\n")
+    if trace:
+        trace.close()
     gpu.idle()
     torch.cuda.synchronize()
     wall = time.perf_counter() - t0
@@ -393,6 +401,7 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=45.0)
     ap.add_argument("--ref-budget", type=float, default=120.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--trace", default="", help="write each timed step's profile and counters (JSON lines)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
