@@ -302,6 +302,24 @@ class World:
             setattr(w, k, f32(getattr(w, k)))
         return w
 
+    def to_arrays(self, prefix: str = "") -> dict:
+        """Every array of the world (and the live manifold count), for np.savez."""
+        out = {prefix + k: (v[:self.m_count] if k.startswith("m_") else v)
+               for k, v in self.__dict__.items() if isinstance(v, np.ndarray)}
+        out[prefix + "m_count"] = np.int64(self.m_count)
+        return out
+
+    @classmethod
+    def from_arrays(cls, d, prefix: str = "") -> "World":
+        w = cls(0)
+        for k in list(w.__dict__):
+            if isinstance(w.__dict__[k], np.ndarray) and prefix + k in d:
+                setattr(w, k, np.array(d[prefix + k]))
+        w.m_count = int(d[prefix + "m_count"])
+        w.m_capacity = len(w.m_body_a)
+        w._c = None
+        return w
+
     def manifold_dict(self):
         """Live manifolds keyed by (A, B) -> (num_contacts, features tuple)."""
         out = {}
