@@ -53,6 +53,8 @@ def load_library(path: str = LIB_PATH):
     L.avbd_read_pairs.argtypes = [vp, vp, vp, C.c_int64, vp]
     L.avbd_last_error.argtypes = [vp]
     L.avbd_last_error.restype = C.c_char_p
+    L.avbd_overlap_pairs_static.argtypes = [C.c_int32, vp, vp, vp, C.c_double, vp, C.c_int64, vp, vp]
+    L.avbd_overlap_pairs_static.restype = C.c_int
     for name in ("avbd_create", "avbd_destroy", "avbd_pack", "avbd_step", "avbd_synchronize", "avbd_read_state",
                  "avbd_write_state", "avbd_read_coloring", "avbd_read_pairs", "avbd_read_stats",
                  "avbd_set_profiling", "avbd_read_profile", "avbd_kernel_launches"):
@@ -164,3 +166,17 @@ class GpuBackend:
         v = C.c_int64()
         self._check(self.L.avbd_kernel_launches(self.h, C.byref(v)))
         return v.value
+
+
+STATIC_PAIRS_MAX_BODIES = 65000
+
+
+def overlap_pairs_static(n, pos, radius, dynamic, cell_size, keys, capacity, count, stream=0):
+    """avbd_overlap_pairs_static on device pointers (ints): the allocation-free
+    bounding-sphere overlap query. Results are ready when `stream` reaches the
+    end of the call; raises AvbdError on a rejected call."""
+    L = load_library()
+    rc = L.avbd_overlap_pairs_static(n, pos, radius, dynamic or None, cell_size, keys, capacity, count,
+                                     stream or None)
+    if rc != abi.AVBD_OK:
+        raise AvbdError(rc, L.avbd_last_error(None).decode())

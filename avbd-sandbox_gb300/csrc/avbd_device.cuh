@@ -346,5 +346,7 @@ cudaError_t launch_solve(const World &w, int lanesPerBody, int blocksPerSm, cuda
 int solve_max_blocks_per_sm(int lanesPerBody);
 void launch_commit(const World &w, cudaStream_t st, int smCount);
 void launch_stats(const World &w, double *out3, cudaStream_t st, int smCount);
+// Error text of a context-free ABI call (read back by avbd_last_error(NULL)).
+int set_context_free_error(int code, const char *msg);
 
 }  // namespace avbd

@@ -24,6 +24,9 @@
 //   4. per candidate: index of the same pair in the previous step's manifolds
 #include <cub/cub.cuh>
 
+#include <mutex>
+
+#include "../../include/avbd_cuda.h"
 #include "avbd_device.cuh"
 
 namespace avbd {
@@ -437,3 +440,284 @@ void launch_broadphase_impl(const World &w, int numLarge, void *temp, size_t tem
 }
 
 }  // namespace avbd
+
+// ---------------------------------------------------------------------------
+// Allocation-free overlap query (avbd_overlap_pairs_static): the kernels above
+// on caller-owned inputs and outputs, with every scratch array carved out of
+// one file-scope device array instead of allocated memory.
+// ---------------------------------------------------------------------------
+namespace avbd {
+
+static __device__ __align__(256) unsigned char g_static_scratch[AVBD_STATIC_SCRATCH_BYTES];
+
+namespace {
+
+// Where the query's arrays sit in the scratch array, for n bodies.
+struct StaticLayout {
+  size_t pos, size, massD, flags0, scene, cStart, cellLo, entries, rows, pairCount, pairStart, largeList,
+      largeStart, sceneStart, invCell, tableCount, tableStart, tableCursor, ctl, temp, tempBytes, total;
+  int tableSize;
+};
+
+StaticLayout static_layout(int n) {
+  StaticLayout L{};
+  size_t at = 0;
+  auto take = [&](size_t bytes) {
+    const size_t here = at;
+    at = (at + bytes + 255) & ~size_t(255);
+    return here;
+  };
+  const size_t m = (size_t)(n > 0 ? n : 1);
+  int T = 1024;
+  while ((size_t)T < 2 * m) T <<= 1;
+  L.tableSize = T;
+  L.pos = take(m * sizeof(D4));
+  L.size = take(m * sizeof(D4));
+  L.massD = take(m * sizeof(D4));
+  L.flags0 = take(m * sizeof(int));
+  L.scene = take(m * sizeof(int));
+  L.cStart = take((m + 1) * sizeof(int));
+  L.cellLo = take(m * sizeof(int4));
+  L.entries = take(m * sizeof(Entry));
+  L.rows = take(m * kPairScratch * sizeof(uint32_t));
+  L.pairCount = take((m + 1) * sizeof(int));
+  L.pairStart = take((m + 1) * sizeof(int));
+  L.largeList = take(m * sizeof(int));
+  L.largeStart = take(2 * sizeof(int));
+  L.sceneStart = take(2 * sizeof(int));
+  L.invCell = take(sizeof(double));
+  L.tableCount = take((size_t)T * sizeof(int));
+  L.tableStart = take((size_t)T * sizeof(int));
+  L.tableCursor = take((size_t)T * sizeof(int));
+  L.ctl = take(sizeof(Control));
+  L.tempBytes = broadphase_temp_bytes((int)m, T);
+  L.temp = take(L.tempBytes);
+  L.total = at;
+  return L;
+}
+
+// Caller inputs -> the step's body layout. Bodies whose diameter (padded as
+// the context's pack pads its cell) exceeds the cell are "large".
+__global__ void static_stage_kernel(World w, D4 *pos, D4 *size, D4 *massD, int *flags0, int *scene, int *cStart,
+                                    const double *p, const double *radius, const int32_t *dynamic, double cell) {
+  const int n = w.b.n;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const double r = radius[i];
+    const bool dyn = dynamic ? dynamic[i] != 0 : true;
+    const bool large = 2.0 * r * (1.0 + 1e-6) + 1e-9 > cell;
+    pos[i] = mkd4(p[3 * i], p[3 * i + 1], p[3 * i + 2], 0.0);
+    size[i] = mkd4(0.0, 0.0, 0.0, r);
+    massD[i] = mkd4(dyn ? 1.0 : 0.0, 0.0, 0.0, 0.0);
+    flags0[i] = (dyn ? kBodyDynamic : 0) | (large ? kBodyLarge : 0);
+    scene[i] = 0;
+    cStart[i] = 0;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) cStart[n] = 0;
+}
+
+// Large bodies in ascending index order (one block).
+__global__ void __launch_bounds__(1024) static_large_list_kernel(World w, int *largeList, int *largeStart) {
+  typedef cub::BlockScan<int, 1024> S;
+  __shared__ typename S::TempStorage tmp;
+  __shared__ int base;
+  if (threadIdx.x == 0) base = 0;
+  __syncthreads();
+  const int n = w.b.n;
+  for (int i0 = 0; i0 < n; i0 += 1024) {
+    const int i = i0 + threadIdx.x;
+    const int f = (i < n && is_large(w, i)) ? 1 : 0;
+    int at, tot;
+    S(tmp).ExclusiveSum(f, at, tot);
+    if (f) largeList[base + at] = i;
+    __syncthreads();
+    if (threadIdx.x == 0) base += tot;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) {
+    largeStart[0] = 0;
+    largeStart[1] = base;
+  }
+}
+
+// large_count_kernel / large_write_kernel with the large-body count read on
+// the device and no previous manifolds.
+__global__ void static_large_count_kernel(World w) {
+  const int numLarge = w.g.largeStart[1];
+  typedef cub::BlockReduce<int, 256> R;
+  __shared__ typename R::TempStorage tmp;
+  for (int li = blockIdx.x; li < numLarge; li += gridDim.x) {
+    const int a = w.g.largeList[li];
+    int c = 0;
+    for (int b = threadIdx.x; b < a; b += blockDim.x) c += accept(w, a, b) ? 1 : 0;
+    const int total = R(tmp).Sum(c);
+    if (threadIdx.x == 0) w.g.pairCount[a] = total;
+    __syncthreads();
+  }
+}
+
+__global__ void static_large_write_kernel(World w) {
+  const int numLarge = w.g.largeStart[1];
+  const int cap = w.g.candCap;
+  typedef cub::BlockScan<int, 256> S;
+  __shared__ typename S::TempStorage tmp;
+  __shared__ int base;
+  for (int li = blockIdx.x; li < numLarge; li += gridDim.x) {
+    const int a = w.g.largeList[li];
+    const int beg = w.g.pairStart[a];
+    const int n = w.g.pairStart[a + 1] - beg;
+    if ((long long)beg + n > cap) continue;  // count > capacity tells the caller
+    uint64_t *seg = w.g.candKey + beg;
+    const uint64_t hiKey = (uint64_t)(uint32_t)a << 32;
+    if (threadIdx.x == 0) base = 0;
+    __syncthreads();
+    for (int b0 = 0; b0 < a; b0 += blockDim.x) {
+      const int b = b0 + threadIdx.x;
+      const int ok = (b < a && accept(w, a, b)) ? 1 : 0;
+      int at, tot;
+      S(tmp).ExclusiveSum(ok, at, tot);
+      if (ok && base + at < n) seg[base + at] = hiKey | (uint32_t)b;
+      __syncthreads();
+      if (threadIdx.x == 0) base += tot;
+      __syncthreads();
+    }
+  }
+}
+
+__global__ void static_scalars_kernel(int *sceneStart, double *invCell, int n, double inv) {
+  sceneStart[0] = 0;
+  sceneStart[1] = n;
+  invCell[0] = inv;
+}
+
+__global__ void static_finish_kernel(World w, int32_t *count) {
+  count[0] = (w.ctl->flags & (kErrNaN | kOvfCells)) ? -1 : w.g.pairStart[w.b.n];
+}
+
+std::mutex g_static_mutex;
+constexpr int kMaxDevices = 64;
+void *g_static_ptr[kMaxDevices] = {};
+
+}  // namespace
+}  // namespace avbd
+
+using namespace avbd;
+
+extern "C" int avbd_overlap_pairs_static(int32_t n, const double *pos, const double *radius,
+                                         const int32_t *dynamic, double cell_size, uint64_t *keys,
+                                         int64_t capacity, int32_t *count, void *stream) {
+  char msg[256];
+  if (n < 0 || n > AVBD_STATIC_PAIRS_MAX_BODIES) {
+    snprintf(msg, sizeof(msg),
+             "avbd_overlap_pairs_static: %d bodies; the static scratch array (%u bytes) holds at most %d",
+             (int)n, (unsigned)AVBD_STATIC_SCRATCH_BYTES, AVBD_STATIC_PAIRS_MAX_BODIES);
+    return set_context_free_error(n < 0 ? AVBD_ERR_ARG : AVBD_ERR_CAPACITY, msg);
+  }
+  if (!count || (n > 0 && (!pos || !radius)) || (capacity > 0 && !keys) || capacity < 0 ||
+      capacity > 0x7fffffff || !(cell_size > 0) || !std::isfinite(cell_size))
+    return set_context_free_error(AVBD_ERR_ARG,
+                                  "avbd_overlap_pairs_static: NULL buffer, capacity outside 0..2^31-1, or "
+                                  "cell_size not finite and > 0");
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess || dev < 0 || dev >= kMaxDevices) {
+    snprintf(msg, sizeof(msg), "avbd_overlap_pairs_static: cudaGetDevice: %s",
+             e != cudaSuccess ? cudaGetErrorString(e) : "device ordinal out of range");
+    return set_context_free_error(AVBD_ERR_CUDA, msg);
+  }
+  unsigned char *base = nullptr;
+  {
+    std::lock_guard<std::mutex> lock(g_static_mutex);
+    if (!g_static_ptr[dev]) {
+      void *p = nullptr;
+      e = cudaGetSymbolAddress(&p, g_static_scratch);
+      if (e != cudaSuccess) {
+        snprintf(msg, sizeof(msg), "avbd_overlap_pairs_static: cudaGetSymbolAddress: %s", cudaGetErrorString(e));
+        return set_context_free_error(AVBD_ERR_CUDA, msg);
+      }
+      g_static_ptr[dev] = p;
+    }
+    base = (unsigned char *)g_static_ptr[dev];
+  }
+  cudaStream_t st = (cudaStream_t)stream;
+  if (n == 0) {
+    e = cudaMemsetAsync(count, 0, sizeof(int32_t), st);
+    if (e != cudaSuccess) {
+      snprintf(msg, sizeof(msg), "avbd_overlap_pairs_static: %s", cudaGetErrorString(e));
+      return set_context_free_error(AVBD_ERR_CUDA, msg);
+    }
+    return AVBD_OK;
+  }
+  const StaticLayout L = static_layout(n);
+  if (L.total > AVBD_STATIC_SCRATCH_BYTES) {
+    snprintf(msg, sizeof(msg), "avbd_overlap_pairs_static: %d bodies need %zu scratch bytes, the array holds %u",
+             (int)n, L.total, (unsigned)AVBD_STATIC_SCRATCH_BYTES);
+    return set_context_free_error(AVBD_ERR_CAPACITY, msg);
+  }
+  World w{};
+  D4 *dPos = (D4 *)(base + L.pos), *dSize = (D4 *)(base + L.size), *dMass = (D4 *)(base + L.massD);
+  int *dFlags = (int *)(base + L.flags0), *dScene = (int *)(base + L.scene), *dCStart = (int *)(base + L.cStart);
+  w.b.n = n;
+  w.b.pos = dPos;
+  w.b.size = dSize;
+  w.b.massD = dMass;
+  w.b.flags0 = dFlags;
+  w.b.scene = dScene;
+  w.g.numScenes = 1;
+  w.g.sceneStart = (const int *)(base + L.sceneStart);
+  w.g.invCell = (const double *)(base + L.invCell);
+  w.g.largeStart = (const int *)(base + L.largeStart);
+  w.g.largeList = (const int *)(base + L.largeList);
+  w.g.cellLo = (int4 *)(base + L.cellLo);
+  w.g.tableMask = (unsigned)(L.tableSize - 1);
+  w.g.tableCount = (int *)(base + L.tableCount);
+  w.g.tableStart = (int *)(base + L.tableStart);
+  w.g.tableCursor = (int *)(base + L.tableCursor);
+  w.g.entries = (Entry *)(base + L.entries);
+  w.g.entryCap = n;
+  w.g.scratch = (uint32_t *)(base + L.rows);
+  w.g.hasConstraints = 0;
+  w.g.pairCount = (int *)(base + L.pairCount);
+  w.g.pairStart = (int *)(base + L.pairStart);
+  w.g.candKey = keys;
+  w.g.candCap = (int)capacity;
+  w.g.cStart = dCStart;
+  w.ctl = (Control *)(base + L.ctl);
+
+  int smCount = 0;
+  e = cudaDeviceGetAttribute(&smCount, cudaDevAttrMultiProcessorCount, dev);
+  if (e == cudaSuccess) {
+    // zero what the kernels accumulate into; the scene table and cell size
+    const int sceneStart[2] = {0, n};
+    const double inv = 1.0 / cell_size;
+    cudaMemsetAsync(w.ctl, 0, sizeof(Control), st);
+    cudaMemsetAsync(w.g.tableCount, 0, sizeof(int) * L.tableSize, st);
+    cudaMemsetAsync(w.g.pairCount + n, 0, sizeof(int), st);
+    const int blocks = smCount * 4;
+    static_stage_kernel<<<blocks, 256, 0, st>>>(w, dPos, dSize, dMass, dFlags, dScene, dCStart, pos, radius,
+                                                dynamic, cell_size);
+    // two scalars and the inverse cell: written by a one-thread kernel so the
+    // call needs no host staging buffer
+    static_scalars_kernel<<<1, 1, 0, st>>>((int *)(base + L.sceneStart), (double *)(base + L.invCell),
+                                           sceneStart[1], inv);
+    static_large_list_kernel<<<1, 1024, 0, st>>>(w, (int *)(base + L.largeList), (int *)(base + L.largeStart));
+    cells_kernel<<<blocks, 256, 0, st>>>(w);
+    size_t tb = L.tempBytes;
+    cub::DeviceScan::ExclusiveSum(base + L.temp, tb, w.g.tableCount, w.g.tableStart, L.tableSize, st);
+    cudaMemcpyAsync(w.g.tableCursor, w.g.tableStart, sizeof(int) * L.tableSize, cudaMemcpyDeviceToDevice, st);
+    scatter_kernel<<<blocks, 256, 0, st>>>(w);
+    const int warpBlocks = (int)std::min<long long>(((long long)n + 7) / 8, (long long)smCount * 32);
+    pairs_kernel<<<warpBlocks, 256, 0, st>>>(w);
+    static_large_count_kernel<<<smCount, 256, 0, st>>>(w);
+    tb = L.tempBytes;
+    cub::DeviceScan::ExclusiveSum(base + L.temp, tb, w.g.pairCount, w.g.pairStart, n + 1, st);
+    copy_kernel<<<warpBlocks, 256, 0, st>>>(w);
+    static_large_write_kernel<<<smCount, 256, 0, st>>>(w);
+    static_finish_kernel<<<1, 1, 0, st>>>(w, count);
+    e = cudaGetLastError();
+  }
+  if (e != cudaSuccess) {
+    snprintf(msg, sizeof(msg), "avbd_overlap_pairs_static: %s", cudaGetErrorString(e));
+    return set_context_free_error(AVBD_ERR_CUDA, msg);
+  }
+  return AVBD_OK;
+}

@@ -984,3 +984,11 @@ int avbd_kernel_launches(avbd_ctx *ctx, int64_t *out) {
 const char *avbd_last_error(const avbd_ctx *ctx) { return ctx ? ctx->err.c_str() : g_create_error; }
 
 }  // extern "C"
+
+namespace avbd {
+int set_context_free_error(int code, const char *msg) {
+  g_create_error_buf = msg;
+  g_create_error = g_create_error_buf.c_str();
+  return code;
+}
+}  // namespace avbd

@@ -285,9 +285,57 @@ int avbd_read_profile(avbd_ctx *ctx, avbd_profile *out);
 /* Number of device kernels launched since the last pack. */
 int avbd_kernel_launches(avbd_ctx *ctx, int64_t *out);
 
-/* Text of the last error on this context (or of the last failed create when
-   ctx is NULL). Never NULL. */
+/* Text of the last error on this context (or, when ctx is NULL, of the last
+   failed avbd_create or context-free call). Never NULL. */
 const char *avbd_last_error(const avbd_ctx *ctx);
+
+/*
+ * Allocation-free bounding-sphere overlap query. No counterpart in the
+ * reference: it runs the broad phase's pair kernels (the same f64 sphere test
+ * and the same pair order as a step's candidate pairs) on caller-owned device
+ * buffers, without a context, and allocates nothing: no cudaMalloc, cudaFree
+ * or allocating library routine. Its scratch memory (hash grid, per-body
+ * partner rows, scan temporaries) is one file-scope __device__ array of
+ * AVBD_STATIC_SCRATCH_BYTES (32 MiB) per device.
+ *
+ * For callers that must not allocate device memory once they are running:
+ * frame loops with a fixed memory budget (cudaFree synchronises the whole
+ * device and would stall every other stream of the frame), and hosts whose
+ * device memory is reserved up front by another allocator.
+ *
+ *   n          bodies, 0..AVBD_STATIC_PAIRS_MAX_BODIES (65,000; the
+ *              reference's per-scene body cap, src/app/scenes.js:66-75);
+ *              more is rejected with AVBD_ERR_CAPACITY
+ *   pos        device, n x 3 doubles (x, y, z)
+ *   radius     device, n doubles (bounding radius, >= 0)
+ *   dynamic    device, n int32 (0 = static; NULL = all dynamic); pairs of
+ *              two static bodies are not reported
+ *   cell_size  hash-grid cell edge, > 0; bodies with 2 r above it (with a
+ *              1e-6 relative pad) are tested against every other body, the
+ *              rest through the grid. Any value gives the same pairs; about
+ *              twice the largest common radius is fastest.
+ *   keys       device, capacity uint64: (a << 32) | b for each pair a > b
+ *              with |p_a - p_b|^2 <= (r_a + r_b)^2, ascending
+ *   count      device, one int32: the number of pairs (may exceed capacity:
+ *              then keys holds an incomplete set and the call must be
+ *              repeated with a larger buffer), or -1 when a position is
+ *              non-finite or beyond 1e9 cells from the origin
+ *   stream     a cudaStream_t (NULL = the legacy default stream)
+ *
+ * The results are ready when the stream reaches the end of the call. The
+ * first call on each device looks up the scratch array's address
+ * (cudaGetSymbolAddress) with that device current; when a call may happen
+ * while its stream is being captured, make one call on that device before.
+ * All calls on a device share the one scratch array, and every call resets
+ * the parts that must start at zero: two calls whose executions overlap (on
+ * different streams, or from different host threads without ordering) race
+ * and corrupt each other's results. Order them on one stream or with events.
+ */
+#define AVBD_STATIC_PAIRS_MAX_BODIES 65000
+#define AVBD_STATIC_SCRATCH_BYTES (32u << 20)
+int avbd_overlap_pairs_static(int32_t n, const double *pos, const double *radius, const int32_t *dynamic,
+                              double cell_size, uint64_t *keys, int64_t capacity, int32_t *count,
+                              void *stream);
 
 #ifdef __cplusplus
 }
