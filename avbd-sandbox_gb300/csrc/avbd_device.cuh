@@ -148,7 +148,8 @@ struct __align__(16) Entry {
   double x, y, z, r;
   int b2, cx, cy, cz;
 };
-constexpr int kPairScratch = 64;
+constexpr int kPairScratch = 128;     // partner row of a step's broad phase
+constexpr int kStaticPairRow = 64;    // partner row of the allocation-free query
 
 struct Grid {
   int numScenes;

@@ -127,40 +127,6 @@ __device__ void prev_range(const World &w, int a, int prevCount, int &first, int
   while (last < prevCount && (int)(w.prev.key[last] >> 32) == a) last++;
 }
 
-// Enumerate the candidate partners b < a of a non-large body a, calling f(b)
-// (serial form, for the rare bodies whose partner list exceeds the scratch row).
-template <class F>
-__device__ void partners_small(const World &w, int a, int prevCount, F &&f) {
-  const int4 c = w.g.cellLo[a];
-  const int s = c.w;
-  if (s < 0) return;
-  for (int k = w.g.largeStart[s]; k < w.g.largeStart[s + 1]; k++) {
-    const int b = w.g.largeList[k];
-    if (b < a && accept(w, a, b)) f(b);
-  }
-  for (int ci = 0; ci < 27; ci++) {
-    const int x = c.x + ci / 9 - 1, y = c.y + (ci / 3) % 3 - 1, z = c.z + ci % 3 - 1;
-    const uint32_t bucket = cell_hash(x, y, z, s) & w.g.tableMask;
-    const int beg = w.g.tableStart[bucket];
-    int end = beg + w.g.tableCount[bucket];
-    if (end > w.g.entryCap) end = w.g.entryCap;
-    for (int k = beg; k < end; k++) {
-      const Entry &e = w.g.entries[k];
-      const int b = e.b2 >> 1;
-      if (b >= a || e.cx != x || e.cy != y || e.cz != z) continue;
-      if (w.g.numScenes > 1 && w.b.scene[b] != s) continue;
-      if (accept(w, a, b)) f(b);
-    }
-  }
-  int first, last;
-  prev_range(w, a, prevCount, first, last);
-  for (int m = first; m < last; m++) {
-    if (w.prev.count[m] <= 0) continue;
-    const int b = (int)(w.prev.key[m] & 0xffffffffu);
-    if (!accept(w, a, b)) f(b);  // accepted ones were counted above
-  }
-}
-
 // One block per large body: every body b < a of its scene is tested.
 __global__ void large_count_kernel(World w, int numLarge) {
   const int prevCount = w.ctl->prevCandidates;
@@ -266,9 +232,10 @@ __device__ BodyA body_a(const World &w, int a) {
 constexpr int kWarpsPerBlock = 8;
 
 // One pass per non-large body: count its partners and, when they fit, leave
-// them sorted in its scratch row for the copy after the scan.
+// them sorted in its scratch row (kRow entries) for the copy after the scan.
+template <int kRow>
 __global__ void __launch_bounds__(256) pairs_kernel(World w) {
-  __shared__ uint32_t buf[kWarpsPerBlock][kPairScratch];
+  __shared__ uint32_t buf[kWarpsPerBlock][kRow];
   __shared__ int fill[kWarpsPerBlock];
   const int prevCount = w.ctl->prevCandidates;
   const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
@@ -280,14 +247,14 @@ __global__ void __launch_bounds__(256) pairs_kernel(World w) {
     __syncwarp();
     warp_partners(w, A, prevCount, lane, [&](int b) {
       const int at = atomicAdd(&fill[wib], 1);
-      if (at < kPairScratch) buf[wib][at] = (uint32_t)b;
+      if (at < kRow) buf[wib][at] = (uint32_t)b;
     });
     __syncwarp();
     const int n = fill[wib];
     if (lane == 0) w.g.pairCount[a] = n;
-    if (n <= kPairScratch) {
+    if (n <= kRow) {
       // rank sort (partners are distinct): element i goes to #{j : b_j < b_i}
-      uint32_t *row = w.g.scratch + (size_t)a * kPairScratch;
+      uint32_t *row = w.g.scratch + (size_t)a * kRow;
       for (int i = lane; i < n; i += 32) {
         const uint32_t v = buf[wib][i];
         int r = 0;
@@ -299,13 +266,16 @@ __global__ void __launch_bounds__(256) pairs_kernel(World w) {
   }
 }
 
-// Copy each body's sorted partners into its segment of the key array; the
-// rare bodies with more than kPairScratch partners are enumerated again
-// serially and sorted in place.
+// Copy each body's sorted partners into its segment of the key array. The
+// rare bodies with more than kRow partners are enumerated again by their
+// warp straight into the segment, which the warp then sorts in place (odd-even
+// transposition: n rounds of compare-exchange on alternating pairs).
+template <int kRow>
 __global__ void __launch_bounds__(256) copy_kernel(World w) {
+  __shared__ int fill[kWarpsPerBlock];
   const int prevCount = w.ctl->prevCandidates;
   const int cap = w.g.candCap;
-  const int lane = threadIdx.x & 31;
+  const int lane = threadIdx.x & 31, wib = threadIdx.x >> 5;
   const int warp = (blockIdx.x * blockDim.x + threadIdx.x) >> 5, warps = (gridDim.x * blockDim.x) >> 5;
   for (int a = warp; a < w.b.n; a += warps) {
     if (is_large(w, a)) continue;
@@ -318,16 +288,28 @@ __global__ void __launch_bounds__(256) copy_kernel(World w) {
     }
     uint64_t *seg = w.g.candKey + beg;
     const uint64_t hiKey = (uint64_t)(uint32_t)a << 32;
-    if (n <= kPairScratch) {
-      const uint32_t *row = w.g.scratch + (size_t)a * kPairScratch;
+    if (n <= kRow) {
+      const uint32_t *row = w.g.scratch + (size_t)a * kRow;
       for (int i = lane; i < n; i += 32) seg[i] = hiKey | row[i];
-    } else if (lane == 0) {
-      int c = 0;
-      partners_small(w, a, prevCount, [&](int b) {
-        if (c < n) seg[c] = hiKey | (uint32_t)b;
-        c++;
-      });
-      sort_segment(seg, n);
+      continue;
+    }
+    if (lane == 0) fill[wib] = 0;
+    __syncwarp();
+    const BodyA A = body_a(w, a);
+    warp_partners(w, A, prevCount, lane, [&](int b) {
+      const int at = atomicAdd(&fill[wib], 1);
+      if (at < n) seg[at] = hiKey | (uint32_t)b;
+    });
+    __syncwarp();
+    for (int round = 0; round < n; round++) {
+      for (int i = 2 * lane + (round & 1); i + 1 < n; i += 64) {
+        const uint64_t x = seg[i], y = seg[i + 1];
+        if (x > y) {
+          seg[i] = y;
+          seg[i + 1] = x;
+        }
+      }
+      __syncwarp();
     }
   }
 }
@@ -429,11 +411,11 @@ void launch_broadphase_impl(const World &w, int numLarge, void *temp, size_t tem
   // pairCount[n] = 0 so the scan over n + 1 entries yields the total at [n]
   cudaMemsetAsync(w.g.pairCount + n, 0, sizeof(int), st);
   const int warpBlocks = (int)std::min<long long>(((long long)n + 7) / 8, (long long)smCount * 32);
-  pairs_kernel<<<warpBlocks, 256, 0, st>>>(w);
+  pairs_kernel<kPairScratch><<<warpBlocks, 256, 0, st>>>(w);
   if (numLarge > 0) large_count_kernel<<<numLarge < 1024 ? numLarge : 1024, 256, 0, st>>>(w, numLarge);
   tb = tempBytes;
   cub::DeviceScan::ExclusiveSum(temp, tb, w.g.pairCount, w.g.pairStart, n + 1, st);
-  copy_kernel<<<warpBlocks, 256, 0, st>>>(w);
+  copy_kernel<kPairScratch><<<warpBlocks, 256, 0, st>>>(w);
   if (numLarge > 0) large_write_kernel<<<numLarge < 1024 ? numLarge : 1024, 256, 0, st>>>(w, numLarge);
   finish_kernel<<<1, 1, 0, st>>>(w);
   prev_index_kernel<<<blocks, 256, 0, st>>>(w);
@@ -479,7 +461,7 @@ StaticLayout static_layout(int n) {
   L.cStart = take((m + 1) * sizeof(int));
   L.cellLo = take(m * sizeof(int4));
   L.entries = take(m * sizeof(Entry));
-  L.rows = take(m * kPairScratch * sizeof(uint32_t));
+  L.rows = take(m * kStaticPairRow * sizeof(uint32_t));
   L.pairCount = take((m + 1) * sizeof(int));
   L.pairStart = take((m + 1) * sizeof(int));
   L.largeList = take(m * sizeof(int));
@@ -706,11 +688,11 @@ extern "C" int avbd_overlap_pairs_static(int32_t n, const double *pos, const dou
     cudaMemcpyAsync(w.g.tableCursor, w.g.tableStart, sizeof(int) * L.tableSize, cudaMemcpyDeviceToDevice, st);
     scatter_kernel<<<blocks, 256, 0, st>>>(w);
     const int warpBlocks = (int)std::min<long long>(((long long)n + 7) / 8, (long long)smCount * 32);
-    pairs_kernel<<<warpBlocks, 256, 0, st>>>(w);
+    pairs_kernel<kStaticPairRow><<<warpBlocks, 256, 0, st>>>(w);
     static_large_count_kernel<<<smCount, 256, 0, st>>>(w);
     tb = L.tempBytes;
     cub::DeviceScan::ExclusiveSum(base + L.temp, tb, w.g.pairCount, w.g.pairStart, n + 1, st);
-    copy_kernel<<<warpBlocks, 256, 0, st>>>(w);
+    copy_kernel<kStaticPairRow><<<warpBlocks, 256, 0, st>>>(w);
     static_large_write_kernel<<<smCount, 256, 0, st>>>(w);
     static_finish_kernel<<<1, 1, 0, st>>>(w, count);
     e = cudaGetLastError();

@@ -11,9 +11,14 @@
 //   manifold.js:214-318 feature-ID merge, sphere basis transport,
 //                      C*(x_t) + margin, warm start lambda <- gamma(alpha lambda),
 //                      k <- clamp(gamma k, kmin, kmax)
-// A cheap f32 test over the six face axes rejects pairs that are separated by
-// more than its error bound before any f64 work (GB300's FP64 rate is a small
-// fraction of its FP32 rate, so the exact path only runs where it can matter).
+// Box-box SAT runs first in f32 in a frame centred on body A, each of the 15
+// axis separations with a conservative bound on its distance from the f64
+// value (GB300's FP64 rate is a small fraction of its FP32 rate). A bound
+// that cannot settle a decision - the sign of a separation, the skip of a
+// near-degenerate edge axis, the order of near-tied best axes, the edge-vs-
+// face choice - sends just those axes through the exact f64 axis test, so
+// every decision equals the f64 one. The winning axis's normal, the contact
+// basis and the clipping stay in exact f64.
 #include "avbd_device.cuh"
 
 namespace avbd {
@@ -99,6 +104,97 @@ struct NewContact {
   uint32_t feature;
   D3 rA, rB;
 };
+
+// f32 SAT of a box-box pair (collide.js:612-685), certified against the f64
+// evaluation. Per axis k (0-2 faces of A, 3-5 faces of B, 6-14 edges
+// A_i x B_j): sep[k] and a bound err[k] >= |sep_f32 - sep_f64|, derived from
+// a per-component error of the f32 box axes of at most ~32 ulp(1) and the
+// 1/len amplification of normalising an edge axis, with a 16x margin:
+//   err = 512 u S (1 + 1/len),  u = 2^-24,  S = |d|_1 + sum(hA) + sum(hB).
+// Axis states: kSkip (edge axis certainly below the length threshold, the f64
+// test skips it too), kValid (sep, err usable), kExact (undecided: the f64
+// test must run). Returns true when some axis certainly separates the boxes.
+constexpr int kSkip = 0, kValid = 1, kExact = 2;
+
+struct SatF {
+  float sep[15], err[15];
+  unsigned char state[15];
+  // the f32 boxes in A's frame: B's centre, the box axes, the half sizes
+  V3<float> d, ax[3], bx[3];
+  float ha[3], hb[3];
+};
+
+__device__ bool sat_f32(const BodyD &A, const BodyD &B, SatF &r) {
+  const Q4<float> qa{(float)A.q.x, (float)A.q.y, (float)A.q.z, (float)A.q.w};
+  const Q4<float> qb{(float)B.q.x, (float)B.q.y, (float)B.q.z, (float)B.q.w};
+  const V3<float> d{(float)(B.p.x - A.p.x), (float)(B.p.y - A.p.y), (float)(B.p.z - A.p.z)};
+  const float ha[3] = {(float)A.half.x, (float)A.half.y, (float)A.half.z};
+  const float hb[3] = {(float)B.half.x, (float)B.half.y, (float)B.half.z};
+  V3<float> ax[3], bx[3];
+  ax[0] = qrotate(qa, V3<float>{1, 0, 0});
+  ax[1] = qrotate(qa, V3<float>{0, 1, 0});
+  ax[2] = qrotate(qa, V3<float>{0, 0, 1});
+  bx[0] = qrotate(qb, V3<float>{1, 0, 0});
+  bx[1] = qrotate(qb, V3<float>{0, 1, 0});
+  bx[2] = qrotate(qb, V3<float>{0, 0, 1});
+  r.d = d;
+  for (int i = 0; i < 3; i++) {
+    r.ax[i] = ax[i];
+    r.bx[i] = bx[i];
+    r.ha[i] = ha[i];
+    r.hb[i] = hb[i];
+  }
+  const float S = fabsf(d.x) + fabsf(d.y) + fabsf(d.z) + ha[0] + ha[1] + ha[2] + hb[0] + hb[1] + hb[2];
+  constexpr float u512 = 512.0f / 16777216.0f;
+  const float eBase = u512 * S;
+  for (int k = 0; k < 15; k++) {
+    V3<float> a;
+    const bool edge = k >= 6;
+    if (k < 3) a = ax[k];
+    else if (k < 6) a = bx[k - 3];
+    else {
+      const V3<float> p = ax[(k - 6) / 3], q = bx[(k - 6) % 3];
+      a = V3<float>{p.y * q.z - p.z * q.y, p.z * q.x - p.x * q.z, p.x * q.y - p.y * q.x};
+    }
+    const float lenSq = a.x * a.x + a.y * a.y + a.z * a.z;
+    r.sep[k] = 0.f;
+    r.err[k] = 0.f;
+    if (!(lenSq == lenSq) || !(S == S) || S > 1e30f) {  // non-finite input: exact path decides
+      r.state[k] = kExact;
+      continue;
+    }
+    if (edge) {
+      // lenSq of the f32 cross product is within 1024 u len + 1e-9 of the f64 one
+      const float eLen = (1024.0f / 16777216.0f) * sqrtf(lenSq) + 1e-9f;
+      if (lenSq + eLen < (float)kSatEps) {
+        r.state[k] = kSkip;
+        continue;
+      }
+      if (lenSq - eLen < (float)kSatEps) {
+        r.state[k] = kExact;
+        continue;
+      }
+    } else if (lenSq < 0.25f) {
+      r.state[k] = kExact;
+      continue;
+    }
+    const float len = sqrtf(lenSq);
+    const V3<float> n{a.x / len, a.y / len, a.z / len};
+    const float dist = fabsf(n.x * d.x + n.y * d.y + n.z * d.z);
+    float rA = 0.f, rB = 0.f;
+    for (int i = 0; i < 3; i++) {
+      rA += ha[i] * fabsf(n.x * ax[i].x + n.y * ax[i].y + n.z * ax[i].z);
+      rB += hb[i] * fabsf(n.x * bx[i].x + n.y * bx[i].y + n.z * bx[i].z);
+    }
+    const float sep = dist - (rA + rB);
+    const float err = eBase * (1.0f + 1.0f / len);
+    if (sep - err > 0.f) return true;  // the f64 test finds this axis separating as well
+    r.sep[k] = sep;
+    r.err[k] = err;
+    r.state[k] = (sep + err > 0.f) ? kExact : kValid;
+  }
+  return false;
+}
 
 struct Collider {
   const BodyD &A, &B;
@@ -398,6 +494,277 @@ struct Collider {
     addContact(xA, xB, 0x32000000u | (region << 2) | (sphereIsA ? 1u : 2u));
     return count;
   }
+  // ---- faceManifold (collide.js:403-472) in f32, in A's frame ----------------
+  // Every f32 point carries a bound .w on its distance from the f64 point
+  // (minus A's position). Each discrete decision - clip side, intersection
+  // denominator, contact depth, merge distance - is taken only when the
+  // bound settles it; otherwise the function returns -1 and the caller runs
+  // the f64 builder. Returns the contact count when every decision was certain.
+  static constexpr float kU = 1.0f / 16777216.0f;  // unit roundoff of f32
+  static constexpr float kEA = 64.0f * kU;         // error of an f32 box axis (2-norm)
+  static constexpr float kFloor = 1e-9f;           // f64 rounding at world scale, and slack
+  __device__ static float nrm(V3<float> v) { return sqrtf(v.x * v.x + v.y * v.y + v.z * v.z); }
+  __device__ static V3<float> fsub(V3<float> a, V3<float> b) { return V3<float>{a.x - b.x, a.y - b.y, a.z - b.z}; }
+  __device__ static V3<float> fadds(V3<float> o, V3<float> a, float s) {
+    return V3<float>{o.x + a.x * s, o.y + a.y * s, o.z + a.z * s};
+  }
+  __device__ static float fdot(V3<float> a, V3<float> b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+  // clip side of a point at signed distance dd (bound e): 1 inside, 0 outside, -1 undecided
+  __device__ static int side(float dd, float e) {
+    if (dd + e <= (float)kPlaneEps) return 1;
+    if (dd - e > (float)kPlaneEps) return 0;
+    return -1;
+  }
+  // clipAgainstPlane (collide.js:202-247); -1 when a decision is undecided
+  __device__ static int clipF(const float4 *in, int n, V3<float> pn, float po, float ePo, float4 *o) {
+    if (n <= 0) return 0;
+    auto dist = [&](float4 v, float &e) {
+      const V3<float> p{v.x, v.y, v.z};
+      const float np = nrm(p);
+      const float dd = fdot(pn, p) - po;
+      e = v.w + (kEA + 3.0f * kU) * np + ePo + kU * fabsf(dd) + kFloor;
+      return dd;
+    };
+    int oc = 0;
+    float4 a = in[n - 1];
+    float ea;
+    float da = dist(a, ea);
+    int ai = side(da, ea);
+    if (ai < 0) return -1;
+    for (int i = 0; i < n; i++) {
+      const float4 b = in[i];
+      float eb;
+      const float db = dist(b, eb);
+      const int bi = side(db, eb);
+      if (bi < 0) return -1;
+      if (ai != bi) {
+        const float denom = da - db;
+        const float eDen = ea + eb + kU * fabsf(denom);
+        float t = 0.f, et = 0.f;
+        if (fabsf(denom) - eDen > (float)kSatEps) {
+          if (fabsf(denom) < 4.0f * eDen) return -1;  // keep the first-order bound valid
+          const float tr = da / denom;
+          et = 1.5f * (fabsf(db) * ea + fabsf(da) * eb) / (denom * denom) + 2.0f * kU * fabsf(tr);
+          t = fminf(fmaxf(tr, 0.f), 1.f);  // clamp is 1-Lipschitz: no decision to certify
+        } else if (!(fabsf(denom) + eDen <= (float)kSatEps)) {
+          return -1;
+        }
+        if (oc < kPolyCap) {
+          const V3<float> pa{a.x, a.y, a.z}, pb{b.x, b.y, b.z};
+          const V3<float> ab = fsub(pb, pa);
+          const V3<float> q = fadds(pa, ab, t);
+          const float e = a.w + t * (a.w + b.w) + nrm(ab) * et + 3.0f * kU * (nrm(pa) + nrm(ab)) + kFloor;
+          o[oc++] = make_float4(q.x, q.y, q.z, e);
+        }
+      }
+      if (bi && oc < kPolyCap) o[oc++] = b;
+      a = b;
+      da = db;
+      ea = eb;
+      ai = bi;
+    }
+    return oc;
+  }
+  // addContact (collide.js:254-285) on f32 points; 1 added, 0 merged or full,
+  // -1 undecided
+  __device__ int addContactF(V3<float> xA, float eA, V3<float> xB, float eB, uint32_t key, const SatF &F,
+                             float4 *midF) {
+    const V3<float> m{(xA.x + xB.x) * 0.5f, (xA.y + xB.y) * 0.5f, (xA.z + xB.z) * 0.5f};
+    const float eM = 0.5f * (eA + eB) + 2.0f * kU * nrm(m) + kFloor;
+    for (int i = 0; i < count; i++) {
+      const V3<float> dv{m.x - midF[i].x, m.y - midF[i].y, m.z - midF[i].z};
+      const float d2 = fdot(dv, dv);
+      const float ee = eM + midF[i].w;
+      const float e2 = 2.0f * nrm(dv) * ee + ee * ee + 4.0f * kU * d2 + kFloor;
+      if (d2 + e2 < (float)kMergeDistSq) return 0;
+      if (d2 - e2 < (float)kMergeDistSq) return -1;
+    }
+    if (count >= kMaxContacts) return 0;
+    const Q4<float> qa{(float)-A.q.x, (float)-A.q.y, (float)-A.q.z, (float)A.q.w};
+    const Q4<float> qb{(float)-B.q.x, (float)-B.q.y, (float)-B.q.z, (float)B.q.w};
+    const V3<float> ra = qrotate(qa, xA);
+    const V3<float> rb = qrotate(qb, fsub(xB, F.d));
+    NewContact &c = out[count];
+    c.feature = key;
+    c.rA = mk(ra.x, ra.y, ra.z);
+    c.rB = mk(rb.x, rb.y, rb.z);
+    midF[count] = make_float4(m.x, m.y, m.z, eM);
+    count++;
+    return 1;
+  }
+  __device__ int faceManifoldF(const SatF &F, bool refIsA, int refAxis, D3 nAB) {
+    const OBB &rb = refIsA ? boxA : boxB;
+    const OBB &ib = refIsA ? boxB : boxA;
+    // the orientation decisions in f64 (the reference's own expressions)
+    const D3 outward = refIsA ? nAB : neg(nAB);
+    const double s = dt3(outward, rb.ax[refAxis]) >= 0 ? 1 : -1;
+    const D3 fN64 = scl(rb.ax[refAxis], s);
+    int incAxis = 0;
+    double best = -INFINITY, dots[3];
+    for (int i = 0; i < 3; i++) {
+      dots[i] = dt3(ib.ax[i], fN64);
+      const double dd = fabs(dots[i]);
+      if (dd > best) {
+        best = dd;
+        incAxis = i;
+      }
+    }
+    const float si = dots[incAxis] > 0 ? -1.f : 1.f;
+    // the geometry in f32
+    const V3<float> zero{0.f, 0.f, 0.f};
+    const V3<float> *rAx = refIsA ? F.ax : F.bx;
+    const V3<float> *iAx = refIsA ? F.bx : F.ax;
+    const float *rH = refIsA ? F.ha : F.hb;
+    const float *iH = refIsA ? F.hb : F.ha;
+    const V3<float> rC = refIsA ? zero : F.d, iC = refIsA ? F.d : zero;
+    const float eD = kU * nrm(F.d) + kFloor;
+    const float eRC = refIsA ? 0.f : eD, eIC = refIsA ? eD : 0.f;
+    const V3<float> fN{rAx[refAxis].x * (float)s, rAx[refAxis].y * (float)s, rAx[refAxis].z * (float)s};
+    const float hR = rH[refAxis];
+    const V3<float> fC = fadds(rC, fN, hR);
+    const float eFC = eRC + kEA * hR + 3.0f * kU * (nrm(rC) + hR) + kFloor;
+    const int u0 = refAxis == 0 ? 1 : 0, v0 = refAxis == 2 ? 1 : 2;
+    const V3<float> fU = rAx[u0], fV = rAx[v0];
+    const float fEU = rH[u0], fEV = rH[v0];
+    const int u1 = incAxis == 0 ? 1 : 0, v1 = incAxis == 2 ? 1 : 2;
+    const V3<float> fn{iAx[incAxis].x * si, iAx[incAxis].y * si, iAx[incAxis].z * si};
+    const float hI = iH[incAxis], eU = iH[u1], eV = iH[v1];
+    const V3<float> fc = fadds(iC, fn, hI);
+    const float eCorner = eIC + kEA * (hI + eU + eV) + 5.0f * kU * (nrm(iC) + hI + eU + eV) + kFloor;
+    float4 P[kPolyCap], Q[kPolyCap];
+    for (int i = 0; i < 4; i++) {
+      const float su = (i == 0 || i == 3) ? 1.f : -1.f;
+      const float sv = (i == 0 || i == 1) ? 1.f : -1.f;
+      const V3<float> c = fadds(fadds(fc, iAx[u1], eU * su), iAx[v1], eV * sv);
+      P[i] = make_float4(c.x, c.y, c.z, eCorner);
+    }
+    int n = 4;
+    const float nFC = nrm(fC);
+    for (int k = 0; k < 4; k++) {
+      const V3<float> ax = k < 2 ? fU : fV;
+      const float sg = (k & 1) ? -1.f : 1.f;
+      const V3<float> pn{ax.x * sg, ax.y * sg, ax.z * sg};
+      const float ext = k < 2 ? fEU : fEV;
+      const float po = fdot(pn, fC) + ext;
+      const float ePo = kEA * nFC + eFC + 3.0f * kU * nFC + kU * (fabsf(po) + ext) + kFloor;
+      n = (k & 1) ? clipF(Q, n, pn, po, ePo, P) : clipF(P, n, pn, po, ePo, Q);
+      if (n < 0) return -1;
+      if (n == 0) return 0;
+    }
+    count = 0;
+    uint32_t prefix = (uint32_t)(refIsA ? kFaceA : kFaceB) << 24;
+    prefix |= (uint32_t)(refAxis & 0xff) << 16;
+    prefix |= (uint32_t)(incAxis & 0xff) << 8;
+    float4 midF[kMaxContacts];
+    for (int i = 0; i < n && count < kMaxContacts; i++) {
+      const V3<float> p{P[i].x, P[i].y, P[i].z};
+      const V3<float> pc = fsub(p, fC);
+      const float dist = fdot(pc, fN);
+      const float eDist = P[i].w + eFC + kEA * nrm(pc) + 4.0f * kU * (nrm(p) + nFC) + kFloor;
+      if (dist - eDist > (float)kPlaneEps) continue;
+      if (dist + eDist > (float)kPlaneEps) return -1;
+      const V3<float> proj = fadds(p, fN, -dist);
+      const float eProj = P[i].w + kEA * fabsf(dist) + eDist + 2.0f * kU * (nrm(p) + fabsf(dist)) + kFloor;
+      const int r = refIsA ? addContactF(proj, eProj, p, P[i].w, prefix | (uint32_t)(i & 0xff), F, midF)
+                           : addContactF(p, P[i].w, proj, eProj, prefix | (uint32_t)(i & 0xff), F, midF);
+      if (r < 0) return -1;
+    }
+    if (!count) return -1;  // the support-point contact is built in f64
+    return count;
+  }
+  // The exact f64 test of SAT axis k (0-2 faces of A, 3-5 faces of B, 6-14
+  // edges) into t; false when the axis separates (collide.js:291-324).
+  __device__ bool exactAxis(D3 delta, int k, Sat &t) {
+    t.valid = false;
+    t.sep = -INFINITY;
+    if (k < 3) return testAxis(delta, boxA.ax[k], kFaceA, k, -1, t);
+    if (k < 6) return testAxis(delta, boxB.ax[k - 3], kFaceB, -1, k - 3, t);
+    const int i = (k - 6) / 3, j = (k - 6) % 3;
+    return testAxis(delta, crs(boxA.ax[i], boxB.ax[j]), kEdge, i, j, t);
+  }
+  // Index of the axis in [k0, k1) the f64 SAT keeps as best (largest
+  // separation, first on ties), or -1 when none is valid. Axes whose f32 value
+  // is not certainly below the largest lower bound are evaluated exactly.
+  __device__ int bestAxis(D3 delta, SatF &r, int k0, int k1, Sat *ex) {
+    float lo = -INFINITY;
+    int any = 0;
+    for (int k = k0; k < k1; k++)
+      if (r.state[k] == kValid) {
+        lo = fmaxf(lo, r.sep[k] - r.err[k]);
+        any++;
+      }
+    if (!any) return -1;
+    int cand = 0, only = -1;
+    for (int k = k0; k < k1; k++)
+      if (r.state[k] == kValid && r.sep[k] + r.err[k] >= lo) {
+        cand++;
+        only = k;
+      }
+    if (cand == 1) return only;
+    int best = -1;
+    double bestSep = 0;
+    for (int k = k0; k < k1; k++) {
+      if (r.state[k] != kValid || r.sep[k] + r.err[k] < lo) continue;
+      if (r.err[k] > 0.f) {  // a candidate for the maximum: take its exact value
+        exactAxis(delta, k, ex[k]);
+        r.sep[k] = (float)ex[k].sep;
+        r.err[k] = 0.f;
+        if (!ex[k].valid) {
+          r.state[k] = kSkip;
+          continue;
+        }
+      }
+      if (best < 0 || ex[k].sep > bestSep) {
+        best = k;
+        bestSep = ex[k].sep;
+      }
+    }
+    return best;
+  }
+  // Box-box through the certified f32 SAT; the same result as the f64 SAT.
+  __device__ int collideBoxes(double *basis) {
+    SatF r;
+    if (sat_f32(A, B, r)) return 0;
+    makeOBB(boxA, A);
+    makeOBB(boxB, B);
+    const D3 delta = sub(boxB.c, boxA.c);
+    Sat ex[15];
+    for (int k = 0; k < 15; k++) {
+      ex[k].valid = false;
+      if (r.state[k] != kExact) continue;
+      if (!exactAxis(delta, k, ex[k])) return 0;
+      r.state[k] = ex[k].valid ? kValid : kSkip;
+      r.sep[k] = (float)ex[k].sep;
+      r.err[k] = 0.f;
+    }
+    const int kf = bestAxis(delta, r, 0, 6, ex);
+    if (kf < 0) return 0;
+    const int ke = bestAxis(delta, r, 6, 15, ex);
+    int win = kf;
+    if (ke >= 0) {
+      // edge preferred when 0.95 sepE > sepF + 0.01: certain from the f32
+      // values unless within their bounds, else on the exact values
+      const float m = 0.95f * r.sep[ke] - (r.sep[kf] + 0.01f);
+      const float em = 0.95f * r.err[ke] + r.err[kf] + 1e-6f * (fabsf(r.sep[ke]) + fabsf(r.sep[kf]) + 0.01f);
+      if (fabsf(m) <= em) {
+        if (!ex[kf].valid) exactAxis(delta, kf, ex[kf]);
+        if (!ex[ke].valid) exactAxis(delta, ke, ex[ke]);
+        win = (0.95 * ex[ke].sep > ex[kf].sep + 0.01) ? ke : kf;
+      } else {
+        win = m > 0.f ? ke : kf;
+      }
+    }
+    if (!ex[win].valid) exactAxis(delta, win, ex[win]);  // the winner's exact normal
+    const Sat &best = ex[win];
+    orthonormal(basis, neg(best.n));
+    if (best.type == kEdge) return edgeContact(best.ia, best.ib, best.n);
+    const bool refIsA = best.type == kFaceA;
+    const int refAxis = refIsA ? best.ia : best.ib;
+    const int c = faceManifoldF(r, refIsA, refAxis, best.n);
+    if (c >= 0) return c;
+    count = 0;
+    return faceManifold(refIsA, refAxis, best.n);
+  }
   // collide.js:612-685
   __device__ int collide(double *basis) {
     if (A.sphere && B.sphere) return sphereSphere(basis);
@@ -424,35 +791,6 @@ struct Collider {
     return faceManifold(false, best.ib, best.n);
   }
 };
-
-// f32 pre-test: true when a face axis of either box separates the pair by
-// more than the worst-case f32-vs-f64 disagreement of the separation value,
-// in which case the f64 test also finds a separating axis and returns no
-// contact. Only box-box pairs.
-__device__ bool clearly_separated(const BodyD &A, const BodyD &B) {
-  const Q4<float> qa{(float)A.q.x, (float)A.q.y, (float)A.q.z, (float)A.q.w};
-  const Q4<float> qb{(float)B.q.x, (float)B.q.y, (float)B.q.z, (float)B.q.w};
-  const V3<float> d{(float)(B.p.x - A.p.x), (float)(B.p.y - A.p.y), (float)(B.p.z - A.p.z)};
-  const V3<float> ha{(float)A.half.x, (float)A.half.y, (float)A.half.z};
-  const V3<float> hb{(float)B.half.x, (float)B.half.y, (float)B.half.z};
-  V3<float> ax[6];
-  ax[0] = qrotate(qa, V3<float>{1, 0, 0});
-  ax[1] = qrotate(qa, V3<float>{0, 1, 0});
-  ax[2] = qrotate(qa, V3<float>{0, 0, 1});
-  ax[3] = qrotate(qb, V3<float>{1, 0, 0});
-  ax[4] = qrotate(qb, V3<float>{0, 1, 0});
-  ax[5] = qrotate(qb, V3<float>{0, 0, 1});
-  const float scale = fabsf(d.x) + fabsf(d.y) + fabsf(d.z) + ha.x + ha.y + ha.z + hb.x + hb.y + hb.z;
-  const float tol = 1.0e-5f * scale + 1.0e-12f;
-  for (int k = 0; k < 6; k++) {
-    const V3<float> n = ax[k];
-    const float dist = fabsf(dot(d, n));
-    const float rA = ha.x * fabsf(dot(n, ax[0])) + ha.y * fabsf(dot(n, ax[1])) + ha.z * fabsf(dot(n, ax[2]));
-    const float rB = hb.x * fabsf(dot(n, ax[3])) + hb.y * fabsf(dot(n, ax[4])) + hb.z * fabsf(dot(n, ax[5]));
-    if (dist - (rA + rB) > tol) return true;
-  }
-  return false;
-}
 
 __device__ BodyD load_body(const World &w, int i) {
   BodyD b;
@@ -496,9 +834,9 @@ __global__ void __launch_bounds__(128) narrowphase_kernel(World w) {
     int num = 0;
     double basis[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
     NewContact nc[kMaxContacts];
-    if (!(!A.sphere && !B.sphere && clearly_separated(A, B))) {
+    {
       Collider col(A, B, nc);
-      num = col.collide(basis);
+      num = (A.sphere || B.sphere) ? col.collide(basis) : col.collideBoxes(basis);
     }
     w.cur.count[c] = num;
     if (num == 0) continue;
@@ -515,7 +853,58 @@ __global__ void __launch_bounds__(128) narrowphase_kernel(World w) {
     const bool compatible = !hasSphere || !hadContacts ||
                             (oldBasis[0] * basis[0] + oldBasis[1] * basis[1] + oldBasis[2] * basis[2]) > 0.85;
     const QD qA = A.q, qB = B.q;
-    for (int i = 0; i < num; i++) {
+    if (!hasSphere) {
+      // box pairs: the same merge, C*(x_t) and warm start in f32 in A's frame
+      // (xA - xB = R_A rA - R_B rB - (pB - pA)); the outputs are stored in f32.
+      const Q4<float> qa{(float)qA.x, (float)qA.y, (float)qA.z, (float)qA.w};
+      const Q4<float> qb{(float)qB.x, (float)qB.y, (float)qB.z, (float)qB.w};
+      const V3<float> dAB{(float)(B.p.x - A.p.x), (float)(B.p.y - A.p.y), (float)(B.p.z - A.p.z)};
+      float bf[9];
+      for (int k = 0; k < 9; k++) bf[k] = (float)basis[k];
+      const float alpha = (float)P.alpha, gamma = (float)P.gamma;
+      const float kmin = (float)P.penaltyMin, kmax = (float)P.penaltyMax, margin = (float)P.margin;
+      for (int i = 0; i < num; i++) {
+        V3<float> rA{(float)nc[i].rA.x, (float)nc[i].rA.y, (float)nc[i].rA.z};
+        V3<float> rB{(float)nc[i].rB.x, (float)nc[i].rB.y, (float)nc[i].rB.z};
+        float lam[3] = {0.f, 0.f, 0.f}, pen[3] = {0.f, 0.f, 0.f};
+        bool stick = false;
+        for (int j = 0; j < oldNum; j++) {
+          const int os = pi * kMaxContacts + j;
+          if (nc[i].feature == w.prev.feat[os]) {
+            const float4 ok = w.prev.cK[os], ol = w.prev.cL[os];
+            lam[0] = ol.x; lam[1] = ol.y; lam[2] = ol.z;
+            pen[0] = ok.x; pen[1] = ok.y; pen[2] = ok.z;
+            stick = ol.w != 0.0f;
+            if (stick) {
+              const float4 a = w.prev.rA[os], b = w.prev.rB[os];
+              rA = V3<float>{a.x, a.y, a.z};
+              rB = V3<float>{b.x, b.y, b.z};
+            }
+            break;
+          }
+        }
+        const V3<float> rAw = qrotate(qa, rA), rBw = qrotate(qb, rB);
+        const V3<float> dd{rAw.x - rBw.x - dAB.x, rAw.y - rBw.y - dAB.y, rAw.z - rBw.z - dAB.z};
+        float C0[3];
+        for (int k = 0; k < 3; k++) C0[k] = bf[3 * k] * dd.x + bf[3 * k + 1] * dd.y + bf[3 * k + 2] * dd.z;
+        C0[0] += margin;
+        if (!P.postStabilize)
+          for (int k = 0; k < 3; k++) lam[k] = (lam[k] * alpha) * gamma;
+        for (int k = 0; k < 3; k++) {
+          const float x = pen[k] * gamma;  // clamp(gamma k, kmin, kmax), NaN propagating
+          pen[k] = x != x ? x : fmaxf(kmin, fminf(kmax, x));
+        }
+        const int s = c * kMaxContacts + i;
+        w.cur.feat[s] = nc[i].feature;
+        w.cur.rA[s] = make_float4(rA.x, rA.y, rA.z, 0.f);
+        w.cur.rB[s] = make_float4(rB.x, rB.y, rB.z, 0.f);
+        w.cur.cA[s] = make_float4(rAw.x, rAw.y, rAw.z, C0[0]);
+        w.cur.cB[s] = make_float4(rBw.x, rBw.y, rBw.z, C0[1]);
+        w.cur.cK[s] = make_float4(pen[0], pen[1], pen[2], C0[2]);
+        w.cur.cL[s] = make_float4(lam[0], lam[1], lam[2], stick ? 1.f : 0.f);
+      }
+    }
+    for (int i = 0; i < num && hasSphere; i++) {
       D3 rA = nc[i].rA, rB = nc[i].rB;
       double lam[3] = {0, 0, 0}, pen[3] = {0, 0, 0};
       bool stick = false;

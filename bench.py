@@ -343,6 +343,8 @@ def run_gpu(args):
         "mean_work_per_step": {k: v / K for k, v in work.items()},
         "peak_work": peak_work,
     }
+    if args.batched_steps > 0:
+        out["batched"] = run_batched(abi, backend, args, flush)
     if rank == 0 and snapshots:
         ref_params = params_for(abi, s, body_order=abi.ORDER_REFERENCE)
         out["cpu_baseline"] = cpu_baseline(ref_params, snapshots, budget_s=args.cpu_budget)
@@ -350,6 +352,49 @@ def run_gpu(args):
         print(json.dumps(out), flush=True)
     if ws > 1:
         torch.distributed.destroy_process_group()
+
+
+def run_batched(abi, backend, args, flush):
+    """The batched workload: 512 independent random box piles (body counts
+    log-uniform in [64, 8192], edges U[0.3, 2] m, densities log-uniform
+    [100, 1e4] kg/m^3, mu U[0.2, 0.9], contact-free column drop), all in one
+    context: every phase of a step is one launch over all scenes. Timed like
+    the main workload (per-step device events, L2 flushed between steps)."""
+    import torch
+
+    sc = pkg().scene
+    parts = sc.pile_batch()
+    worlds = [p.world() for p in parts]
+    batch = sc.batch_worlds(worlds)
+    params = abi.default_params(gravity=-9.81, iterations=10, body_order=abi.ORDER_PRIORITY)
+    gpu = backend.GpuBackend(params)
+    gpu.pack(batch)
+    gpu.step(args.warmup)
+    gpu.idle()
+    gpu.pack(batch)
+    gpu.set_profiling(True)
+    total_ms, K = 0.0, args.batched_steps
+    phases = {k: 0.0 for k in ("broadphase_ms", "narrowphase_ms", "prepare_ms", "coloring_ms", "solve_ms")}
+    contacts = 0
+    for _ in range(K):
+        flush.fill_(1.0)
+        torch.cuda.synchronize()
+        gpu.step(1)
+        p = gpu.last_profile
+        total_ms += p["step_ms"]
+        contacts += p["contacts"]
+        for k in phases:
+            phases[k] += p[k]
+    gpu.set_profiling(False)
+    gpu.destroy()
+    n_scenes = len(parts)
+    return {
+        "value": n_scenes * K / (total_ms / 1e3), "unit": "scene-steps/s", "scenes": n_scenes,
+        "bodies": batch.n_bodies, "steps": K, "ms_per_step": total_ms / K,
+        "steps_per_s": K / (total_ms / 1e3), "mean_contacts": contacts / K,
+        "phases_ms": {k: v / K for k, v in phases.items()},
+        "workload": f"{n_scenes} random box piles ({batch.n_bodies:,} bodies) in one context, steps 1..{K}",
+    }
 
 
 def run_reference(args):
@@ -401,6 +446,7 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=45.0)
     ap.add_argument("--ref-budget", type=float, default=120.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--batched-steps", type=int, default=240, help="steps of the 512-scene batch (0: skip)")
     ap.add_argument("--trace", default="", help="write each timed step's profile and counters (JSON lines)")
     args = ap.parse_args()
     if args.warmup < 3:

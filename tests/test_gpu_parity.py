@@ -207,3 +207,61 @@ def test_schedules_agree(abi, scenes, backend_mod):
         outs.append(gpu.read_state())
     assert np.array_equal(outs[0].pos, outs[1].pos)
     assert np.array_equal(outs[0].quat, outs[1].quat)
+
+
+def box_pairs_scene(scenes, n_pairs=2400, seed=3):
+    """Isolated box pairs near contact, in five families that stress the SAT
+    and clipping decisions: random poses; exactly aligned stacks (tied face
+    axes, vertices on the clip planes); a 45-degree yaw (tied incident faces);
+    near-parallel edges around the 1e-3 rad axis-length threshold; crossed
+    45-degree edges (edge-edge contacts)."""
+    rng = np.random.default_rng(seed)
+    s = scenes.Scene("box_pairs")
+    s.params = dict(gravity=0.0, iterations=4)
+    side = int(np.ceil(np.sqrt(n_pairs)))
+    ident = (0.0, 0.0, 0.0, 1.0)
+    for i in range(n_pairs):
+        base = np.array([(i % side) * 9.0, (i // side) * 9.0, 5.0])
+        ha = rng.uniform(0.2, 1.0, 3)
+        hb = rng.uniform(0.2, 1.0, 3)
+        fam = i % 5
+        qa, qb = ident, ident
+        off = np.zeros(3)
+        if fam == 0:
+            qa = scenes.axis_angle(rng.normal(size=3), rng.uniform(0, np.pi))
+            qb = scenes.axis_angle(rng.normal(size=3), rng.uniform(0, np.pi))
+            d = rng.normal(size=3)
+            off = d / np.linalg.norm(d) * rng.uniform(0.3, 1.0) * (np.linalg.norm(ha) + np.linalg.norm(hb))
+        else:
+            pen = [0.0, 1e-3, 0.02, -1e-3][rng.integers(4)]
+            lateral = [0.0, 0.0, 0.25][rng.integers(3)] * rng.uniform(-1, 1, 2)
+            if fam == 2:
+                qb = scenes.axis_angle((0.0, 0.0, 1.0), np.pi / 4)
+            elif fam == 3:
+                eps = [1e-4, 9.99e-4, 1e-3, 1.001e-3, 1e-2][rng.integers(5)]
+                qb = scenes.axis_angle(rng.normal(size=3), eps)
+            elif fam == 4:
+                qa = scenes.axis_angle((1.0, 0.0, 0.0), np.pi / 4)
+                qb = scenes.axis_angle((0.0, 1.0, 0.0), np.pi / 4)
+                pen = pen * 0.5
+            za = ha[2] if fam != 4 else (ha[1] + ha[2]) / np.sqrt(2)
+            zb = hb[2] if fam != 4 else (hb[0] + hb[2]) / np.sqrt(2)
+            off = np.array([lateral[0], lateral[1], za + zb - pen])
+        s.box(2 * ha, 500.0, 0.5, tuple(base), quat=qa)
+        s.box(2 * hb, 500.0, 0.5, tuple(base + off), quat=qb)
+    return s
+
+
+@pytest.mark.parametrize("seed", [3, 4])
+def test_narrowphase_stress_topology(abi, scenes, backend_mod, seed):
+    """Thousands of isolated box pairs: the device's manifolds (pairs, contact
+    counts, feature IDs) equal the oracle's exactly, and so do the pairs."""
+    s = box_pairs_scene(scenes, seed=seed)
+    ref, gpu = compare_step(abi, backend_mod, s, 0)
+    oa, ob = ref.pairs()
+    ga, gb = gpu.read_pairs()
+    assert np.array_equal(oa, ga) and np.array_equal(ob, gb)
+    want = ref.state().manifold_dict()
+    got = gpu.read_state(manifolds=True).manifold_dict()
+    assert len(want) > 1000
+    assert got == want
