@@ -73,6 +73,7 @@ struct Control {
   int fp64Bodies;
   int adjTotal;
   int prevCandidates;  // candidates (= manifold slots) of the previous step
+  int npCount[3];      // narrow-phase work lists: face, edge, exact
   int pad[5];
 };
 
@@ -168,6 +169,9 @@ struct Grid {
   uint64_t *candKey;
   int *candPrev;
   int candCap;
+  // narrow-phase work lists (candidate index + winning axis), candCap each
+  int2 *npFace, *npEdge;
+  int *npExact;
   // static joint/spring adjacency (pack time)
   const int *cStart;
   const uint32_t *cRef;

@@ -163,6 +163,8 @@ int alloc_candidate_arenas(avbd_ctx *ctx, int cap) {
   w.a.ccap = (int)std::min<long long>(2LL * kMaxContacts * cap, 0x7fffffff);
   if ((rc = alloc_manifolds(ctx, ctx->mA, cap)) || (rc = alloc_manifolds(ctx, ctx->mB, cap)) ||
       (rc = galloc(ctx, &w.g.candKey, cap)) || (rc = galloc(ctx, &w.g.candPrev, cap)) ||
+      (rc = galloc(ctx, &w.g.npFace, cap)) || (rc = galloc(ctx, &w.g.npEdge, cap)) ||
+      (rc = galloc(ctx, &w.g.npExact, cap)) ||
       (rc = galloc(ctx, &w.a.entry, ctx->adjCap)) || (rc = galloc(ctx, &w.a.centry, w.a.ccap)))
     return rc;
   return AVBD_OK;
@@ -357,7 +359,7 @@ int one_step(avbd_ctx *ctx) {
   ctx->launches += 6 + (ctx->numLarge > 0 ? 2 : 0);  // own kernels (the two scans are library code)
   if ((rc = record(ctx, 1))) return rc;
   launch_narrowphase(w, st, ctx->smCount);
-  ctx->launches += 1;
+  ctx->launches += 4;
   if ((rc = record(ctx, 2))) return rc;
   launch_prepare(w, ctx->svTemp, ctx->svTempBytes, st, ctx->smCount);
   ctx->launches += 5;

@@ -105,95 +105,133 @@ struct NewContact {
   D3 rA, rB;
 };
 
-// f32 SAT of a box-box pair (collide.js:612-685), certified against the f64
-// evaluation. Per axis k (0-2 faces of A, 3-5 faces of B, 6-14 edges
-// A_i x B_j): sep[k] and a bound err[k] >= |sep_f32 - sep_f64|, derived from
-// a per-component error of the f32 box axes of at most ~32 ulp(1) and the
-// 1/len amplification of normalising an edge axis, with a 16x margin:
-//   err = 512 u S (1 + 1/len),  u = 2^-24,  S = |d|_1 + sum(hA) + sum(hB).
-// Axis states: kSkip (edge axis certainly below the length threshold, the f64
-// test skips it too), kValid (sep, err usable), kExact (undecided: the f64
-// test must run). Returns true when some axis certainly separates the boxes.
-constexpr int kSkip = 0, kValid = 1, kExact = 2;
+struct NewContactF {
+  uint32_t feature;
+  float ra[3], rb[3];
+};
 
-struct SatF {
-  float sep[15], err[15];
-  unsigned char state[15];
-  // the f32 boxes in A's frame: B's centre, the box axes, the half sizes
+// The two boxes in f32 in a frame centred on A: B's centre, the box axes and
+// the half sizes.
+struct BoxF {
   V3<float> d, ax[3], bx[3];
   float ha[3], hb[3];
 };
 
-__device__ bool sat_f32(const BodyD &A, const BodyD &B, SatF &r) {
+__device__ BoxF make_boxf(const BodyD &A, const BodyD &B) {
+  BoxF F;
   const Q4<float> qa{(float)A.q.x, (float)A.q.y, (float)A.q.z, (float)A.q.w};
   const Q4<float> qb{(float)B.q.x, (float)B.q.y, (float)B.q.z, (float)B.q.w};
-  const V3<float> d{(float)(B.p.x - A.p.x), (float)(B.p.y - A.p.y), (float)(B.p.z - A.p.z)};
-  const float ha[3] = {(float)A.half.x, (float)A.half.y, (float)A.half.z};
-  const float hb[3] = {(float)B.half.x, (float)B.half.y, (float)B.half.z};
-  V3<float> ax[3], bx[3];
-  ax[0] = qrotate(qa, V3<float>{1, 0, 0});
-  ax[1] = qrotate(qa, V3<float>{0, 1, 0});
-  ax[2] = qrotate(qa, V3<float>{0, 0, 1});
-  bx[0] = qrotate(qb, V3<float>{1, 0, 0});
-  bx[1] = qrotate(qb, V3<float>{0, 1, 0});
-  bx[2] = qrotate(qb, V3<float>{0, 0, 1});
-  r.d = d;
-  for (int i = 0; i < 3; i++) {
-    r.ax[i] = ax[i];
-    r.bx[i] = bx[i];
-    r.ha[i] = ha[i];
-    r.hb[i] = hb[i];
-  }
-  const float S = fabsf(d.x) + fabsf(d.y) + fabsf(d.z) + ha[0] + ha[1] + ha[2] + hb[0] + hb[1] + hb[2];
+  F.d = V3<float>{(float)(B.p.x - A.p.x), (float)(B.p.y - A.p.y), (float)(B.p.z - A.p.z)};
+  F.ha[0] = (float)A.half.x; F.ha[1] = (float)A.half.y; F.ha[2] = (float)A.half.z;
+  F.hb[0] = (float)B.half.x; F.hb[1] = (float)B.half.y; F.hb[2] = (float)B.half.z;
+  F.ax[0] = qrotate(qa, V3<float>{1, 0, 0});
+  F.ax[1] = qrotate(qa, V3<float>{0, 1, 0});
+  F.ax[2] = qrotate(qa, V3<float>{0, 0, 1});
+  F.bx[0] = qrotate(qb, V3<float>{1, 0, 0});
+  F.bx[1] = qrotate(qb, V3<float>{0, 1, 0});
+  F.bx[2] = qrotate(qb, V3<float>{0, 0, 1});
+  return F;
+}
+
+// Outcome of the f32 SAT of a box pair.
+constexpr int kSeparated = 0, kFaceWin = 1, kEdgeWin = 2, kUndecided = 3;
+
+// f32 SAT of a box-box pair (collide.js:612-685), certified against the f64
+// evaluation: every axis separation comes with a bound err >= |sep_f32 -
+// sep_f64|, derived from a per-component error of the f32 box axes of at
+// most ~32 ulp(1) and the 1/len amplification of normalising an edge axis,
+// with a 16x margin:
+//   err = 512 u S (1 + 1/len),  u = 2^-24,  S = |d|_1 + sum(hA) + sum(hB).
+// kSeparated when some axis certainly separates the boxes (the f64 test then
+// finds a separating axis too and returns no contact). kFaceWin / kEdgeWin
+// when no axis can separate, the best face axis (largest separation, first
+// on ties) and, if it can matter, the best edge axis are certain, and so is
+// the choice 0.95 sepE > sepF + 0.01 between them. kUndecided otherwise: the
+// exact f64 path decides.
+__device__ int classify_f32(const BoxF &F, bool &refIsA, int &axA, int &axB) {
+  const float S = fabsf(F.d.x) + fabsf(F.d.y) + fabsf(F.d.z) + F.ha[0] + F.ha[1] + F.ha[2] + F.hb[0] + F.hb[1] +
+                  F.hb[2];
+  if (!(S == S) || S > 1e30f) return kUndecided;
   constexpr float u512 = 512.0f / 16777216.0f;
   const float eBase = u512 * S;
+  bool undecided = false;
+  // best of each group so far, and the largest upper bound among the others
+  int fBest = -1, eBest = -1;
+  float fSep = 0.f, fErr = 0.f, fOther = -INFINITY, eSep = 0.f, eErr = 0.f, eOther = -INFINITY;
+#pragma unroll
   for (int k = 0; k < 15; k++) {
     V3<float> a;
     const bool edge = k >= 6;
-    if (k < 3) a = ax[k];
-    else if (k < 6) a = bx[k - 3];
+    if (k < 3) a = F.ax[k];
+    else if (k < 6) a = F.bx[k - 3];
     else {
-      const V3<float> p = ax[(k - 6) / 3], q = bx[(k - 6) % 3];
+      const V3<float> p = F.ax[(k - 6) / 3], q = F.bx[(k - 6) % 3];
       a = V3<float>{p.y * q.z - p.z * q.y, p.z * q.x - p.x * q.z, p.x * q.y - p.y * q.x};
     }
     const float lenSq = a.x * a.x + a.y * a.y + a.z * a.z;
-    r.sep[k] = 0.f;
-    r.err[k] = 0.f;
-    if (!(lenSq == lenSq) || !(S == S) || S > 1e30f) {  // non-finite input: exact path decides
-      r.state[k] = kExact;
-      continue;
-    }
     if (edge) {
       // lenSq of the f32 cross product is within 1024 u len + 1e-9 of the f64 one
       const float eLen = (1024.0f / 16777216.0f) * sqrtf(lenSq) + 1e-9f;
-      if (lenSq + eLen < (float)kSatEps) {
-        r.state[k] = kSkip;
-        continue;
-      }
+      if (lenSq + eLen < (float)kSatEps) continue;  // the f64 test skips this axis too
       if (lenSq - eLen < (float)kSatEps) {
-        r.state[k] = kExact;
+        undecided = true;
         continue;
       }
-    } else if (lenSq < 0.25f) {
-      r.state[k] = kExact;
+    } else if (!(lenSq >= 0.25f)) {
+      undecided = true;
       continue;
     }
     const float len = sqrtf(lenSq);
     const V3<float> n{a.x / len, a.y / len, a.z / len};
-    const float dist = fabsf(n.x * d.x + n.y * d.y + n.z * d.z);
+    const float dist = fabsf(n.x * F.d.x + n.y * F.d.y + n.z * F.d.z);
     float rA = 0.f, rB = 0.f;
+#pragma unroll
     for (int i = 0; i < 3; i++) {
-      rA += ha[i] * fabsf(n.x * ax[i].x + n.y * ax[i].y + n.z * ax[i].z);
-      rB += hb[i] * fabsf(n.x * bx[i].x + n.y * bx[i].y + n.z * bx[i].z);
+      rA += F.ha[i] * fabsf(n.x * F.ax[i].x + n.y * F.ax[i].y + n.z * F.ax[i].z);
+      rB += F.hb[i] * fabsf(n.x * F.bx[i].x + n.y * F.bx[i].y + n.z * F.bx[i].z);
     }
     const float sep = dist - (rA + rB);
     const float err = eBase * (1.0f + 1.0f / len);
-    if (sep - err > 0.f) return true;  // the f64 test finds this axis separating as well
-    r.sep[k] = sep;
-    r.err[k] = err;
-    r.state[k] = (sep + err > 0.f) ? kExact : kValid;
+    if (sep - err > 0.f) return kSeparated;
+    if (sep + err > 0.f) {
+      undecided = true;
+      continue;
+    }
+    if (!edge) {
+      if (fBest < 0 || sep > fSep) {
+        if (fBest >= 0) fOther = fmaxf(fOther, fSep + fErr);
+        fBest = k; fSep = sep; fErr = err;
+      } else {
+        fOther = fmaxf(fOther, sep + err);
+      }
+    } else {
+      if (eBest < 0 || sep > eSep) {
+        if (eBest >= 0) eOther = fmaxf(eOther, eSep + eErr);
+        eBest = k; eSep = sep; eErr = err;
+      } else {
+        eOther = fmaxf(eOther, sep + err);
+      }
+    }
   }
-  return false;
+  if (undecided || fBest < 0) return kUndecided;
+  const float fLo = fSep - fErr, fHi = fmaxf(fSep + fErr, fOther);
+  bool edgeWins = false;
+  if (eBest >= 0) {
+    const float eLo = eSep - eErr, eHi = fmaxf(eSep + eErr, eOther);
+    const float slack = 1e-6f * (fabsf(eSep) + fabsf(fSep) + 0.01f);
+    if (0.95f * eLo > fHi + 0.01f + slack) edgeWins = true;
+    else if (!(0.95f * eHi < fLo + 0.01f - slack)) return kUndecided;
+  }
+  if (edgeWins) {
+    if (!(eOther < eSep - eErr)) return kUndecided;  // tied edge axes
+    axA = (eBest - 6) / 3;
+    axB = (eBest - 6) % 3;
+    return kEdgeWin;
+  }
+  if (!(fOther < fSep - fErr)) return kUndecided;  // tied face axes
+  refIsA = fBest < 3;
+  axA = refIsA ? fBest : fBest - 3;
+  return kFaceWin;
 }
 
 struct Collider {
@@ -202,7 +240,6 @@ struct Collider {
   D3 fN, fC, fU, fV;
   double fEU, fEV;
   double faceExtU, faceExtV;
-  D3 clip0[kPolyCap], clip1[kPolyCap];
   D3 mid[kMaxContacts];
   int count = 0;
   NewContact *out;
@@ -351,6 +388,7 @@ struct Collider {
   }
   // collide.js:403-472
   __device__ int faceManifold(bool refIsA, int refAxis, D3 nAB) {
+    D3 clip0[kPolyCap], clip1[kPolyCap];
     const OBB &rb = refIsA ? boxA : boxB;
     const OBB &ib = refIsA ? boxB : boxA;
     const D3 outward = refIsA ? nAB : neg(nAB);
@@ -494,7 +532,53 @@ struct Collider {
     addContact(xA, xB, 0x32000000u | (region << 2) | (sphereIsA ? 1u : 2u));
     return count;
   }
-  // ---- faceManifold (collide.js:403-472) in f32, in A's frame ----------------
+  // The exact unit normal of an SAT axis, oriented from A to B, with the
+  // operations of testAxis (collide.js:291-324).
+  __device__ static D3 axisNormal(D3 axis, D3 delta) {
+    const double lenSq = axis.x * axis.x + axis.y * axis.y + axis.z * axis.z;
+    const double invLen = 1.0 / sqrt(lenSq);
+    D3 n = scl(axis, invLen);
+    if (dt3(n, delta) < 0) n = neg(n);
+    return n;
+  }
+  // collide.js:612-685
+  __device__ int collide(double *basis) {
+    if (A.sphere && B.sphere) return sphereSphere(basis);
+    if (A.sphere || B.sphere) return sphereBox(basis, A.sphere);
+    makeOBB(boxA, A);
+    makeOBB(boxB, B);
+    const D3 delta = sub(boxB.c, boxA.c);
+    Sat bf, be;
+    bf.sep = -INFINITY; bf.valid = false; bf.type = 0; bf.ia = bf.ib = -1; bf.n = mk(0, 0, 0);
+    be = bf;
+    for (int i = 0; i < 3; i++)
+      if (!testAxis(delta, boxA.ax[i], kFaceA, i, -1, bf)) return 0;
+    for (int i = 0; i < 3; i++)
+      if (!testAxis(delta, boxB.ax[i], kFaceB, -1, i, bf)) return 0;
+    for (int i = 0; i < 3; i++)
+      for (int j = 0; j < 3; j++)
+        if (!testAxis(delta, crs(boxA.ax[i], boxB.ax[j]), kEdge, i, j, be)) return 0;
+    if (!bf.valid) return 0;
+    Sat best = bf;
+    if (be.valid && 0.95 * be.sep > bf.sep + 0.01) best = be;
+    orthonormal(basis, neg(best.n));
+    if (best.type == kEdge) return edgeContact(best.ia, best.ib, best.n);
+    if (best.type == kFaceA) return faceManifold(true, best.ia, best.n);
+    return faceManifold(false, best.ib, best.n);
+  }
+};
+
+// ---- faceManifold (collide.js:403-472) in f32, in A's frame ------------------
+struct FaceF {
+  const BoxF &F;
+  Q4<float> qaInv, qbInv;  // conjugate orientations of A and B (f32)
+  NewContactF *outF;
+  int count = 0;
+  __device__ FaceF(const BoxF &f, const BodyD &A, const BodyD &B, NewContactF *o)
+      : F(f),
+        qaInv{(float)-A.q.x, (float)-A.q.y, (float)-A.q.z, (float)A.q.w},
+        qbInv{(float)-B.q.x, (float)-B.q.y, (float)-B.q.z, (float)B.q.w},
+        outF(o) {}
   // Every f32 point carries a bound .w on its distance from the f64 point
   // (minus A's position). Each discrete decision - clip side, intersection
   // denominator, contact depth, merge distance - is taken only when the
@@ -567,8 +651,7 @@ struct Collider {
   }
   // addContact (collide.js:254-285) on f32 points; 1 added, 0 merged or full,
   // -1 undecided
-  __device__ int addContactF(V3<float> xA, float eA, V3<float> xB, float eB, uint32_t key, const SatF &F,
-                             float4 *midF) {
+  __device__ int addContactF(V3<float> xA, float eA, V3<float> xB, float eB, uint32_t key, float4 *midF) {
     const V3<float> m{(xA.x + xB.x) * 0.5f, (xA.y + xB.y) * 0.5f, (xA.z + xB.z) * 0.5f};
     const float eM = 0.5f * (eA + eB) + 2.0f * kU * nrm(m) + kFloor;
     for (int i = 0; i < count; i++) {
@@ -580,29 +663,26 @@ struct Collider {
       if (d2 - e2 < (float)kMergeDistSq) return -1;
     }
     if (count >= kMaxContacts) return 0;
-    const Q4<float> qa{(float)-A.q.x, (float)-A.q.y, (float)-A.q.z, (float)A.q.w};
-    const Q4<float> qb{(float)-B.q.x, (float)-B.q.y, (float)-B.q.z, (float)B.q.w};
-    const V3<float> ra = qrotate(qa, xA);
-    const V3<float> rb = qrotate(qb, fsub(xB, F.d));
-    NewContact &c = out[count];
+    const V3<float> ra = qrotate(qaInv, xA);
+    const V3<float> rb = qrotate(qbInv, fsub(xB, F.d));
+    NewContactF &c = outF[count];
     c.feature = key;
-    c.rA = mk(ra.x, ra.y, ra.z);
-    c.rB = mk(rb.x, rb.y, rb.z);
+    c.ra[0] = ra.x; c.ra[1] = ra.y; c.ra[2] = ra.z;
+    c.rb[0] = rb.x; c.rb[1] = rb.y; c.rb[2] = rb.z;
     midF[count] = make_float4(m.x, m.y, m.z, eM);
     count++;
     return 1;
   }
-  __device__ int faceManifoldF(const SatF &F, bool refIsA, int refAxis, D3 nAB) {
-    const OBB &rb = refIsA ? boxA : boxB;
-    const OBB &ib = refIsA ? boxB : boxA;
-    // the orientation decisions in f64 (the reference's own expressions)
+  // refAx: the reference face axis in f64; ibAx: the incident box's axes in
+  // f64 (the orientation decisions use the reference's own f64 expressions).
+  __device__ int build(bool refIsA, int refAxis, D3 nAB, D3 refAx, const D3 *ibAx) {
     const D3 outward = refIsA ? nAB : neg(nAB);
-    const double s = dt3(outward, rb.ax[refAxis]) >= 0 ? 1 : -1;
-    const D3 fN64 = scl(rb.ax[refAxis], s);
+    const double s = dt3(outward, refAx) >= 0 ? 1 : -1;
+    const D3 fN64 = scl(refAx, s);
     int incAxis = 0;
     double best = -INFINITY, dots[3];
     for (int i = 0; i < 3; i++) {
-      dots[i] = dt3(ib.ax[i], fN64);
+      dots[i] = dt3(ibAx[i], fN64);
       const double dd = fabs(dots[i]);
       if (dd > best) {
         best = dd;
@@ -656,6 +736,7 @@ struct Collider {
     prefix |= (uint32_t)(refAxis & 0xff) << 16;
     prefix |= (uint32_t)(incAxis & 0xff) << 8;
     float4 midF[kMaxContacts];
+    count = 0;
     for (int i = 0; i < n && count < kMaxContacts; i++) {
       const V3<float> p{P[i].x, P[i].y, P[i].z};
       const V3<float> pc = fsub(p, fC);
@@ -665,130 +746,12 @@ struct Collider {
       if (dist + eDist > (float)kPlaneEps) return -1;
       const V3<float> proj = fadds(p, fN, -dist);
       const float eProj = P[i].w + kEA * fabsf(dist) + eDist + 2.0f * kU * (nrm(p) + fabsf(dist)) + kFloor;
-      const int r = refIsA ? addContactF(proj, eProj, p, P[i].w, prefix | (uint32_t)(i & 0xff), F, midF)
-                           : addContactF(p, P[i].w, proj, eProj, prefix | (uint32_t)(i & 0xff), F, midF);
+      const int r = refIsA ? addContactF(proj, eProj, p, P[i].w, prefix | (uint32_t)(i & 0xff), midF)
+                           : addContactF(p, P[i].w, proj, eProj, prefix | (uint32_t)(i & 0xff), midF);
       if (r < 0) return -1;
     }
     if (!count) return -1;  // the support-point contact is built in f64
     return count;
-  }
-  // The exact f64 test of SAT axis k (0-2 faces of A, 3-5 faces of B, 6-14
-  // edges) into t; false when the axis separates (collide.js:291-324).
-  __device__ bool exactAxis(D3 delta, int k, Sat &t) {
-    t.valid = false;
-    t.sep = -INFINITY;
-    if (k < 3) return testAxis(delta, boxA.ax[k], kFaceA, k, -1, t);
-    if (k < 6) return testAxis(delta, boxB.ax[k - 3], kFaceB, -1, k - 3, t);
-    const int i = (k - 6) / 3, j = (k - 6) % 3;
-    return testAxis(delta, crs(boxA.ax[i], boxB.ax[j]), kEdge, i, j, t);
-  }
-  // Index of the axis in [k0, k1) the f64 SAT keeps as best (largest
-  // separation, first on ties), or -1 when none is valid. Axes whose f32 value
-  // is not certainly below the largest lower bound are evaluated exactly.
-  __device__ int bestAxis(D3 delta, SatF &r, int k0, int k1, Sat *ex) {
-    float lo = -INFINITY;
-    int any = 0;
-    for (int k = k0; k < k1; k++)
-      if (r.state[k] == kValid) {
-        lo = fmaxf(lo, r.sep[k] - r.err[k]);
-        any++;
-      }
-    if (!any) return -1;
-    int cand = 0, only = -1;
-    for (int k = k0; k < k1; k++)
-      if (r.state[k] == kValid && r.sep[k] + r.err[k] >= lo) {
-        cand++;
-        only = k;
-      }
-    if (cand == 1) return only;
-    int best = -1;
-    double bestSep = 0;
-    for (int k = k0; k < k1; k++) {
-      if (r.state[k] != kValid || r.sep[k] + r.err[k] < lo) continue;
-      if (r.err[k] > 0.f) {  // a candidate for the maximum: take its exact value
-        exactAxis(delta, k, ex[k]);
-        r.sep[k] = (float)ex[k].sep;
-        r.err[k] = 0.f;
-        if (!ex[k].valid) {
-          r.state[k] = kSkip;
-          continue;
-        }
-      }
-      if (best < 0 || ex[k].sep > bestSep) {
-        best = k;
-        bestSep = ex[k].sep;
-      }
-    }
-    return best;
-  }
-  // Box-box through the certified f32 SAT; the same result as the f64 SAT.
-  __device__ int collideBoxes(double *basis) {
-    SatF r;
-    if (sat_f32(A, B, r)) return 0;
-    makeOBB(boxA, A);
-    makeOBB(boxB, B);
-    const D3 delta = sub(boxB.c, boxA.c);
-    Sat ex[15];
-    for (int k = 0; k < 15; k++) {
-      ex[k].valid = false;
-      if (r.state[k] != kExact) continue;
-      if (!exactAxis(delta, k, ex[k])) return 0;
-      r.state[k] = ex[k].valid ? kValid : kSkip;
-      r.sep[k] = (float)ex[k].sep;
-      r.err[k] = 0.f;
-    }
-    const int kf = bestAxis(delta, r, 0, 6, ex);
-    if (kf < 0) return 0;
-    const int ke = bestAxis(delta, r, 6, 15, ex);
-    int win = kf;
-    if (ke >= 0) {
-      // edge preferred when 0.95 sepE > sepF + 0.01: certain from the f32
-      // values unless within their bounds, else on the exact values
-      const float m = 0.95f * r.sep[ke] - (r.sep[kf] + 0.01f);
-      const float em = 0.95f * r.err[ke] + r.err[kf] + 1e-6f * (fabsf(r.sep[ke]) + fabsf(r.sep[kf]) + 0.01f);
-      if (fabsf(m) <= em) {
-        if (!ex[kf].valid) exactAxis(delta, kf, ex[kf]);
-        if (!ex[ke].valid) exactAxis(delta, ke, ex[ke]);
-        win = (0.95 * ex[ke].sep > ex[kf].sep + 0.01) ? ke : kf;
-      } else {
-        win = m > 0.f ? ke : kf;
-      }
-    }
-    if (!ex[win].valid) exactAxis(delta, win, ex[win]);  // the winner's exact normal
-    const Sat &best = ex[win];
-    orthonormal(basis, neg(best.n));
-    if (best.type == kEdge) return edgeContact(best.ia, best.ib, best.n);
-    const bool refIsA = best.type == kFaceA;
-    const int refAxis = refIsA ? best.ia : best.ib;
-    const int c = faceManifoldF(r, refIsA, refAxis, best.n);
-    if (c >= 0) return c;
-    count = 0;
-    return faceManifold(refIsA, refAxis, best.n);
-  }
-  // collide.js:612-685
-  __device__ int collide(double *basis) {
-    if (A.sphere && B.sphere) return sphereSphere(basis);
-    if (A.sphere || B.sphere) return sphereBox(basis, A.sphere);
-    makeOBB(boxA, A);
-    makeOBB(boxB, B);
-    const D3 delta = sub(boxB.c, boxA.c);
-    Sat bf, be;
-    bf.sep = -INFINITY; bf.valid = false; bf.type = 0; bf.ia = bf.ib = -1; bf.n = mk(0, 0, 0);
-    be = bf;
-    for (int i = 0; i < 3; i++)
-      if (!testAxis(delta, boxA.ax[i], kFaceA, i, -1, bf)) return 0;
-    for (int i = 0; i < 3; i++)
-      if (!testAxis(delta, boxB.ax[i], kFaceB, -1, i, bf)) return 0;
-    for (int i = 0; i < 3; i++)
-      for (int j = 0; j < 3; j++)
-        if (!testAxis(delta, crs(boxA.ax[i], boxB.ax[j]), kEdge, i, j, be)) return 0;
-    if (!bf.valid) return 0;
-    Sat best = bf;
-    if (be.valid && 0.95 * be.sep > bf.sep + 0.01) best = be;
-    orthonormal(basis, neg(best.n));
-    if (best.type == kEdge) return edgeContact(best.ia, best.ib, best.n);
-    if (best.type == kFaceA) return faceManifold(true, best.ia, best.n);
-    return faceManifold(false, best.ib, best.n);
   }
 };
 
@@ -824,144 +787,274 @@ __device__ void transport(double *lam, double *pen, const double *ob, const doub
   }
 }
 
-__global__ void __launch_bounds__(128) narrowphase_kernel(World w) {
-  const int total = *((volatile int *)&w.ctl->numCandidates);
+// ---------------------------------------------------------------------------
+// Manifold output: merge with the previous step's manifold by feature ID,
+// C*(x_t) + margin, warm start (manifold.js:214-318).
+// ---------------------------------------------------------------------------
+
+// Box pairs, in f32 in A's frame (xA - xB = R_A rA - R_B rB - (pB - pA)); the
+// outputs are stored in f32.
+__device__ void write_box_manifold(const World &w, int c, int ia, int ib, const BodyD &A, const BodyD &B,
+                                   const NewContactF *nc, int num, const double *basis) {
   const SolverParams &P = w.p;
+  w.cur.count[c] = num;
+  if (num == 0) return;
+  const int pi = w.g.candPrev[c];
+  const int oldNum = pi >= 0 ? w.prev.count[pi] : 0;
+  const Q4<float> qa{(float)A.q.x, (float)A.q.y, (float)A.q.z, (float)A.q.w};
+  const Q4<float> qb{(float)B.q.x, (float)B.q.y, (float)B.q.z, (float)B.q.w};
+  const V3<float> dAB{(float)(B.p.x - A.p.x), (float)(B.p.y - A.p.y), (float)(B.p.z - A.p.z)};
+  float bf[9];
+  for (int k = 0; k < 9; k++) bf[k] = (float)basis[k];
+  const float alpha = (float)P.alpha, gamma = (float)P.gamma;
+  const float kmin = (float)P.penaltyMin, kmax = (float)P.penaltyMax, margin = (float)P.margin;
+  for (int i = 0; i < num; i++) {
+    V3<float> rA{nc[i].ra[0], nc[i].ra[1], nc[i].ra[2]};
+    V3<float> rB{nc[i].rb[0], nc[i].rb[1], nc[i].rb[2]};
+    float lam[3] = {0.f, 0.f, 0.f}, pen[3] = {0.f, 0.f, 0.f};
+    bool stick = false;
+    for (int j = 0; j < oldNum; j++) {
+      const int os = pi * kMaxContacts + j;
+      if (nc[i].feature == w.prev.feat[os]) {
+        const float4 ok = w.prev.cK[os], ol = w.prev.cL[os];
+        lam[0] = ol.x; lam[1] = ol.y; lam[2] = ol.z;
+        pen[0] = ok.x; pen[1] = ok.y; pen[2] = ok.z;
+        stick = ol.w != 0.0f;
+        if (stick) {  // a stuck box contact keeps its anchors (manifold.js:279-282)
+          const float4 oa = w.prev.rA[os], ob = w.prev.rB[os];
+          rA = V3<float>{oa.x, oa.y, oa.z};
+          rB = V3<float>{ob.x, ob.y, ob.z};
+        }
+        break;
+      }
+    }
+    const V3<float> rAw = qrotate(qa, rA), rBw = qrotate(qb, rB);
+    const V3<float> dd{rAw.x - rBw.x - dAB.x, rAw.y - rBw.y - dAB.y, rAw.z - rBw.z - dAB.z};
+    float C0[3];
+    for (int k = 0; k < 3; k++) C0[k] = bf[3 * k] * dd.x + bf[3 * k + 1] * dd.y + bf[3 * k + 2] * dd.z;
+    C0[0] += margin;
+    if (!P.postStabilize)
+      for (int k = 0; k < 3; k++) lam[k] = (lam[k] * alpha) * gamma;
+    for (int k = 0; k < 3; k++) {
+      const float x = pen[k] * gamma;  // clamp(gamma k, kmin, kmax), NaN propagating
+      pen[k] = x != x ? x : fmaxf(kmin, fminf(kmax, x));
+    }
+    const int s = c * kMaxContacts + i;
+    w.cur.feat[s] = nc[i].feature;
+    w.cur.rA[s] = make_float4(rA.x, rA.y, rA.z, 0.f);
+    w.cur.rB[s] = make_float4(rB.x, rB.y, rB.z, 0.f);
+    w.cur.cA[s] = make_float4(rAw.x, rAw.y, rAw.z, C0[0]);
+    w.cur.cB[s] = make_float4(rBw.x, rBw.y, rBw.z, C0[1]);
+    w.cur.cK[s] = make_float4(pen[0], pen[1], pen[2], C0[2]);
+    w.cur.cL[s] = make_float4(lam[0], lam[1], lam[2], stick ? 1.f : 0.f);
+  }
+  const double friction = sqrt(w.b.friction[ia] * w.b.friction[ib]);
+  for (int k = 0; k < 9; k++) w.cur.basisD[c * 9 + k] = basis[k];
+  w.cur.basis0[c] = make_float4(bf[0], bf[1], bf[2], (float)friction);
+  w.cur.basis1[c] = make_float4(bf[3], bf[4], bf[5], 0.f);
+  w.cur.basis2[c] = make_float4(bf[6], bf[7], bf[8], 0.f);
+}
+
+// Pairs with a sphere, in f64: the basis-compatibility test and the
+// transport of lambda and k into the new basis (manifold.js:222-270).
+__device__ void write_sphere_manifold(const World &w, int c, int ia, int ib, const BodyD &A, const BodyD &B,
+                                      const NewContact *nc, int num, const double *basis) {
+  const SolverParams &P = w.p;
+  w.cur.count[c] = num;
+  if (num == 0) return;
+  const int pi = w.g.candPrev[c];
+  const int oldNum = pi >= 0 ? w.prev.count[pi] : 0;
+  double oldBasis[9];
+  if (oldNum > 0)
+    for (int k = 0; k < 9; k++) oldBasis[k] = w.prev.basisD[pi * 9 + k];
+  const double friction = sqrt(w.b.friction[ia] * w.b.friction[ib]);
+  const bool compatible =
+      oldNum == 0 || (oldBasis[0] * basis[0] + oldBasis[1] * basis[1] + oldBasis[2] * basis[2]) > 0.85;
+  const QD qA = A.q, qB = B.q;
+  for (int i = 0; i < num; i++) {
+    const D3 rA = nc[i].rA, rB = nc[i].rB;
+    double lam[3] = {0, 0, 0}, pen[3] = {0, 0, 0};
+    bool stick = false;
+    for (int j = 0; j < oldNum; j++) {
+      const int os = pi * kMaxContacts + j;
+      if (compatible && nc[i].feature == w.prev.feat[os]) {
+        const float4 ok = w.prev.cK[os], ol = w.prev.cL[os];
+        lam[0] = ol.x; lam[1] = ol.y; lam[2] = ol.z;
+        pen[0] = ok.x; pen[1] = ok.y; pen[2] = ok.z;
+        stick = ol.w != 0.0f;
+        transport(lam, pen, oldBasis, basis);
+        break;
+      }
+    }
+    // C*(x_t) and warm start (manifold.js:292-315)
+    const D3 xA = add(rot(qA, rA), A.p);
+    const D3 xB = add(rot(qB, rB), B.p);
+    const D3 d = sub(xA, xB);
+    double C0[3];
+    C0[0] = basis[0] * d.x + basis[1] * d.y + basis[2] * d.z;
+    C0[1] = basis[3] * d.x + basis[4] * d.y + basis[5] * d.z;
+    C0[2] = basis[6] * d.x + basis[7] * d.y + basis[8] * d.z;
+    C0[0] += P.margin;
+    if (!P.postStabilize) {
+      for (int k = 0; k < 3; k++) {
+        lam[k] = lam[k] * P.alpha;
+        lam[k] = lam[k] * P.gamma;
+      }
+    }
+    for (int k = 0; k < 3; k++) pen[k] = clampd(pen[k] * P.gamma, P.penaltyMin, P.penaltyMax);
+    const D3 rAw = rot(qA, rA), rBw = rot(qB, rB);
+    const int s = c * kMaxContacts + i;
+    w.cur.feat[s] = nc[i].feature;
+    w.cur.rA[s] = make_float4((float)rA.x, (float)rA.y, (float)rA.z, 0.f);
+    w.cur.rB[s] = make_float4((float)rB.x, (float)rB.y, (float)rB.z, 0.f);
+    w.cur.cA[s] = make_float4((float)rAw.x, (float)rAw.y, (float)rAw.z, (float)C0[0]);
+    w.cur.cB[s] = make_float4((float)rBw.x, (float)rBw.y, (float)rBw.z, (float)C0[1]);
+    w.cur.cK[s] = make_float4((float)pen[0], (float)pen[1], (float)pen[2], (float)C0[2]);
+    w.cur.cL[s] = make_float4((float)lam[0], (float)lam[1], (float)lam[2], stick ? 1.f : 0.f);
+  }
+  for (int k = 0; k < 9; k++) w.cur.basisD[c * 9 + k] = basis[k];
+  w.cur.basis0[c] = make_float4((float)basis[0], (float)basis[1], (float)basis[2], (float)friction);
+  w.cur.basis1[c] = make_float4((float)basis[3], (float)basis[4], (float)basis[5], 0.f);
+  w.cur.basis2[c] = make_float4((float)basis[6], (float)basis[7], (float)basis[8], 0.f);
+}
+
+// Append to one of the work lists, one atomic per coalesced group of lanes.
+__device__ __forceinline__ int push_slot(int *counter) {
+  const unsigned m = __activemask();
+  const int lane = threadIdx.x & 31;
+  const int leader = __ffs(m) - 1;
+  int base = 0;
+  if (lane == leader) base = atomicAdd(counter, __popc(m));
+  base = __shfl_sync(m, base, leader);
+  return base + __popc(m & ((1u << lane) - 1u));
+}
+
+__device__ __forceinline__ void push_exact(const World &w, int c) {
+  w.g.npExact[push_slot(&w.ctl->npCount[2])] = c;
+}
+
+// 1. Every candidate: the f32 SAT. Separated pairs get count 0; box pairs
+//    with a certain winning axis go to the face or edge list, everything
+//    else (sphere pairs, undecided box pairs) to the exact list.
+__global__ void __launch_bounds__(256) classify_kernel(World w) {
+  const int total = *((volatile int *)&w.ctl->numCandidates);
   for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < total; c += gridDim.x * blockDim.x) {
     const uint64_t key = w.g.candKey[c];
     const int ia = (int)(key >> 32), ib = (int)(key & 0xffffffffu);
     const BodyD A = load_body(w, ia), B = load_body(w, ib);
-    int num = 0;
+    if (A.sphere || B.sphere) {
+      push_exact(w, c);
+      continue;
+    }
+    bool refIsA = true;
+    int axA = 0, axB = 0;
+    const int r = classify_f32(make_boxf(A, B), refIsA, axA, axB);
+    if (r == kSeparated) {
+      w.cur.count[c] = 0;
+    } else if (r == kFaceWin) {
+      w.g.npFace[push_slot(&w.ctl->npCount[0])] = make_int2(c, (refIsA ? 4 : 0) | axA);
+    } else if (r == kEdgeWin) {
+      w.g.npEdge[push_slot(&w.ctl->npCount[1])] = make_int2(c, axA * 3 + axB);
+    } else {
+      push_exact(w, c);
+    }
+  }
+}
+
+// 2. Face manifolds: the exact normal and basis in f64, the clipping in f32
+//    with certified decisions; an undecided pair moves to the exact list.
+__global__ void __launch_bounds__(128) face_kernel(World w) {
+  const int total = *((volatile int *)&w.ctl->npCount[0]);
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
+    const int2 e = w.g.npFace[t];
+    const int c = e.x;
+    const bool refIsA = (e.y & 4) != 0;
+    const int refAxis = e.y & 3;
+    const uint64_t key = w.g.candKey[c];
+    const int ia = (int)(key >> 32), ib = (int)(key & 0xffffffffu);
+    const BodyD A = load_body(w, ia), B = load_body(w, ib);
+    // f64: the reference axis, the incident box's axes, the exact normal
+    const QD qRef = refIsA ? A.q : B.q, qInc = refIsA ? B.q : A.q;
+    const D3 e3[3] = {mk(1, 0, 0), mk(0, 1, 0), mk(0, 0, 1)};
+    const D3 refAx = rot(qRef, e3[refAxis]);
+    const D3 ibAx[3] = {rot(qInc, e3[0]), rot(qInc, e3[1]), rot(qInc, e3[2])};
+    const D3 n = Collider::axisNormal(refAx, sub(B.p, A.p));
+    double basis[9];
+    orthonormal(basis, neg(n));
+    const BoxF F = make_boxf(A, B);
+    NewContactF ncf[kMaxContacts];
+    FaceF face(F, A, B, ncf);
+    const int num = face.build(refIsA, refAxis, n, refAx, ibAx);
+    if (num < 0) {
+      push_exact(w, c);
+      continue;
+    }
+    write_box_manifold(w, c, ia, ib, A, B, ncf, num, basis);
+  }
+}
+
+// 3. Edge-edge contacts (collide.js:475-493), exact f64.
+__global__ void __launch_bounds__(128) edge_kernel(World w) {
+  const int total = *((volatile int *)&w.ctl->npCount[1]);
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
+    const int2 e = w.g.npEdge[t];
+    const int c = e.x, i = e.y / 3, j = e.y % 3;
+    const uint64_t key = w.g.candKey[c];
+    const int ia = (int)(key >> 32), ib = (int)(key & 0xffffffffu);
+    const BodyD A = load_body(w, ia), B = load_body(w, ib);
+    NewContact nc[2];
+    Collider col(A, B, nc);
+    Collider::makeOBB(col.boxA, A);
+    Collider::makeOBB(col.boxB, B);
+    const D3 delta = sub(col.boxB.c, col.boxA.c);
+    const D3 n = Collider::axisNormal(crs(col.boxA.ax[i], col.boxB.ax[j]), delta);
+    double basis[9];
+    orthonormal(basis, neg(n));
+    const int num = col.edgeContact(i, j, n);
+    NewContactF ncf[2];
+    for (int k = 0; k < num; k++) {
+      ncf[k].feature = nc[k].feature;
+      ncf[k].ra[0] = (float)nc[k].rA.x; ncf[k].ra[1] = (float)nc[k].rA.y; ncf[k].ra[2] = (float)nc[k].rA.z;
+      ncf[k].rb[0] = (float)nc[k].rB.x; ncf[k].rb[1] = (float)nc[k].rB.y; ncf[k].rb[2] = (float)nc[k].rB.z;
+    }
+    write_box_manifold(w, c, ia, ib, A, B, ncf, num, basis);
+  }
+}
+
+// 4. Sphere pairs and undecided box pairs: the whole f64 collider.
+__global__ void __launch_bounds__(128) exact_kernel(World w) {
+  const int total = *((volatile int *)&w.ctl->npCount[2]);
+  for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
+    const int c = w.g.npExact[t];
+    const uint64_t key = w.g.candKey[c];
+    const int ia = (int)(key >> 32), ib = (int)(key & 0xffffffffu);
+    const BodyD A = load_body(w, ia), B = load_body(w, ib);
     double basis[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
     NewContact nc[kMaxContacts];
-    {
-      Collider col(A, B, nc);
-      num = (A.sphere || B.sphere) ? col.collide(basis) : col.collideBoxes(basis);
+    Collider col(A, B, nc);
+    const int num = col.collide(basis);
+    if (A.sphere || B.sphere) {
+      write_sphere_manifold(w, c, ia, ib, A, B, nc, num, basis);
+      continue;
     }
-    w.cur.count[c] = num;
-    if (num == 0) continue;
-
-    // --- merge persistent state (manifold.js:214-290) ---
-    const int pi = w.g.candPrev[c];
-    const int oldNum = pi >= 0 ? w.prev.count[pi] : 0;
-    const bool hasSphere = A.sphere || B.sphere;
-    const bool hadContacts = oldNum > 0;
-    double oldBasis[9];
-    if (hasSphere && hadContacts)
-      for (int k = 0; k < 9; k++) oldBasis[k] = w.prev.basisD[pi * 9 + k];
-    const double friction = sqrt(w.b.friction[ia] * w.b.friction[ib]);
-    const bool compatible = !hasSphere || !hadContacts ||
-                            (oldBasis[0] * basis[0] + oldBasis[1] * basis[1] + oldBasis[2] * basis[2]) > 0.85;
-    const QD qA = A.q, qB = B.q;
-    if (!hasSphere) {
-      // box pairs: the same merge, C*(x_t) and warm start in f32 in A's frame
-      // (xA - xB = R_A rA - R_B rB - (pB - pA)); the outputs are stored in f32.
-      const Q4<float> qa{(float)qA.x, (float)qA.y, (float)qA.z, (float)qA.w};
-      const Q4<float> qb{(float)qB.x, (float)qB.y, (float)qB.z, (float)qB.w};
-      const V3<float> dAB{(float)(B.p.x - A.p.x), (float)(B.p.y - A.p.y), (float)(B.p.z - A.p.z)};
-      float bf[9];
-      for (int k = 0; k < 9; k++) bf[k] = (float)basis[k];
-      const float alpha = (float)P.alpha, gamma = (float)P.gamma;
-      const float kmin = (float)P.penaltyMin, kmax = (float)P.penaltyMax, margin = (float)P.margin;
-      for (int i = 0; i < num; i++) {
-        V3<float> rA{(float)nc[i].rA.x, (float)nc[i].rA.y, (float)nc[i].rA.z};
-        V3<float> rB{(float)nc[i].rB.x, (float)nc[i].rB.y, (float)nc[i].rB.z};
-        float lam[3] = {0.f, 0.f, 0.f}, pen[3] = {0.f, 0.f, 0.f};
-        bool stick = false;
-        for (int j = 0; j < oldNum; j++) {
-          const int os = pi * kMaxContacts + j;
-          if (nc[i].feature == w.prev.feat[os]) {
-            const float4 ok = w.prev.cK[os], ol = w.prev.cL[os];
-            lam[0] = ol.x; lam[1] = ol.y; lam[2] = ol.z;
-            pen[0] = ok.x; pen[1] = ok.y; pen[2] = ok.z;
-            stick = ol.w != 0.0f;
-            if (stick) {
-              const float4 a = w.prev.rA[os], b = w.prev.rB[os];
-              rA = V3<float>{a.x, a.y, a.z};
-              rB = V3<float>{b.x, b.y, b.z};
-            }
-            break;
-          }
-        }
-        const V3<float> rAw = qrotate(qa, rA), rBw = qrotate(qb, rB);
-        const V3<float> dd{rAw.x - rBw.x - dAB.x, rAw.y - rBw.y - dAB.y, rAw.z - rBw.z - dAB.z};
-        float C0[3];
-        for (int k = 0; k < 3; k++) C0[k] = bf[3 * k] * dd.x + bf[3 * k + 1] * dd.y + bf[3 * k + 2] * dd.z;
-        C0[0] += margin;
-        if (!P.postStabilize)
-          for (int k = 0; k < 3; k++) lam[k] = (lam[k] * alpha) * gamma;
-        for (int k = 0; k < 3; k++) {
-          const float x = pen[k] * gamma;  // clamp(gamma k, kmin, kmax), NaN propagating
-          pen[k] = x != x ? x : fmaxf(kmin, fminf(kmax, x));
-        }
-        const int s = c * kMaxContacts + i;
-        w.cur.feat[s] = nc[i].feature;
-        w.cur.rA[s] = make_float4(rA.x, rA.y, rA.z, 0.f);
-        w.cur.rB[s] = make_float4(rB.x, rB.y, rB.z, 0.f);
-        w.cur.cA[s] = make_float4(rAw.x, rAw.y, rAw.z, C0[0]);
-        w.cur.cB[s] = make_float4(rBw.x, rBw.y, rBw.z, C0[1]);
-        w.cur.cK[s] = make_float4(pen[0], pen[1], pen[2], C0[2]);
-        w.cur.cL[s] = make_float4(lam[0], lam[1], lam[2], stick ? 1.f : 0.f);
-      }
+    NewContactF ncf[kMaxContacts];
+    for (int k = 0; k < num; k++) {
+      ncf[k].feature = nc[k].feature;
+      ncf[k].ra[0] = (float)nc[k].rA.x; ncf[k].ra[1] = (float)nc[k].rA.y; ncf[k].ra[2] = (float)nc[k].rA.z;
+      ncf[k].rb[0] = (float)nc[k].rB.x; ncf[k].rb[1] = (float)nc[k].rB.y; ncf[k].rb[2] = (float)nc[k].rB.z;
     }
-    for (int i = 0; i < num && hasSphere; i++) {
-      D3 rA = nc[i].rA, rB = nc[i].rB;
-      double lam[3] = {0, 0, 0}, pen[3] = {0, 0, 0};
-      bool stick = false;
-      for (int j = 0; j < oldNum; j++) {
-        const int os = pi * kMaxContacts + j;
-        if (compatible && nc[i].feature == w.prev.feat[os]) {
-          const float4 ok = w.prev.cK[os], ol = w.prev.cL[os];
-          lam[0] = ol.x; lam[1] = ol.y; lam[2] = ol.z;
-          pen[0] = ok.x; pen[1] = ok.y; pen[2] = ok.z;
-          stick = ol.w != 0.0f;
-          if (hasSphere) transport(lam, pen, oldBasis, basis);
-          if (stick && !hasSphere) {
-            const float4 a = w.prev.rA[os], b = w.prev.rB[os];
-            rA = mk(a.x, a.y, a.z);
-            rB = mk(b.x, b.y, b.z);
-          }
-          break;
-        }
-      }
-      // C*(x_t) and warm start (manifold.js:292-315)
-      const D3 xA = add(rot(qA, rA), A.p);
-      const D3 xB = add(rot(qB, rB), B.p);
-      const D3 d = sub(xA, xB);
-      double C0[3];
-      C0[0] = basis[0] * d.x + basis[1] * d.y + basis[2] * d.z;
-      C0[1] = basis[3] * d.x + basis[4] * d.y + basis[5] * d.z;
-      C0[2] = basis[6] * d.x + basis[7] * d.y + basis[8] * d.z;
-      C0[0] += P.margin;
-      if (!P.postStabilize) {
-        for (int k = 0; k < 3; k++) {
-          lam[k] = lam[k] * P.alpha;
-          lam[k] = lam[k] * P.gamma;
-        }
-      }
-      for (int k = 0; k < 3; k++) pen[k] = clampd(pen[k] * P.gamma, P.penaltyMin, P.penaltyMax);
-      const D3 rAw = rot(qA, rA), rBw = rot(qB, rB);
-      const int s = c * kMaxContacts + i;
-      w.cur.feat[s] = nc[i].feature;
-      w.cur.rA[s] = make_float4((float)rA.x, (float)rA.y, (float)rA.z, 0.f);
-      w.cur.rB[s] = make_float4((float)rB.x, (float)rB.y, (float)rB.z, 0.f);
-      w.cur.cA[s] = make_float4((float)rAw.x, (float)rAw.y, (float)rAw.z, (float)C0[0]);
-      w.cur.cB[s] = make_float4((float)rBw.x, (float)rBw.y, (float)rBw.z, (float)C0[1]);
-      w.cur.cK[s] = make_float4((float)pen[0], (float)pen[1], (float)pen[2], (float)C0[2]);
-      w.cur.cL[s] = make_float4((float)lam[0], (float)lam[1], (float)lam[2], stick ? 1.f : 0.f);
-    }
-    for (int k = 0; k < 9; k++) w.cur.basisD[c * 9 + k] = basis[k];
-    w.cur.basis0[c] = make_float4((float)basis[0], (float)basis[1], (float)basis[2], (float)friction);
-    w.cur.basis1[c] = make_float4((float)basis[3], (float)basis[4], (float)basis[5], 0.f);
-    w.cur.basis2[c] = make_float4((float)basis[6], (float)basis[7], (float)basis[8], 0.f);
+    write_box_manifold(w, c, ia, ib, A, B, ncf, num, basis);
   }
 }
 
 }  // namespace
 
 void launch_narrowphase(const World &w, cudaStream_t st, int smCount) {
-  const int blocks = smCount * 8;
-  narrowphase_kernel<<<blocks, 128, 0, st>>>(w);
+  cudaMemsetAsync(w.ctl->npCount, 0, sizeof(w.ctl->npCount), st);
+  classify_kernel<<<smCount * 8, 256, 0, st>>>(w);
+  face_kernel<<<smCount * 8, 128, 0, st>>>(w);
+  edge_kernel<<<smCount * 4, 128, 0, st>>>(w);
+  exact_kernel<<<smCount * 4, 128, 0, st>>>(w);
 }
 
 }  // namespace avbd

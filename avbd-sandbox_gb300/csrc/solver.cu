@@ -1037,19 +1037,29 @@ __device__ inline bool owns(int myColor, int otherColor) { return myColor > othe
 // them out of line keeps the common path (one contact per lane, held in
 // registers from the primal stamp to the dual update) within the register
 // budget of two resident blocks per SM; the callee pays its own spills.
+// First joint/spring entry of this lane: the smallest e >= nm with e = lane (mod G).
+__device__ __forceinline__ int first_extra(int lane, int nm, int G) {
+  return lane < nm ? lane + ((nm - lane + G - 1) / G) * G : lane;
+}
+
 template <class T>
 __device__ __noinline__ void extra_primal(const World &w, int i, int cb, int nm, int cStart, int total, int lane,
                                           int G, bool selfSphere, const BState<T> &self, T alpha, Sys<T> &s) {
-  for (int e = lane; e < total; e += G) {
-    if (e < nm) {
-      if (e == lane) continue;  // the lane's first contact is handled inline
-      contact_primal<T>(load_contact<T>(w, ld(&w.a.centry[cb + e]), selfSphere), self, alpha, s);
-    } else {
-      const uint32_t ref = ld(&w.g.cRef[cStart + e - nm]);
-      const uint32_t type = ref >> 30, idx = (ref >> 1) & 0x1fffffffu, side = ref & 1u;
-      if (type == kRefJoint) joint_primal<T>(w, (int)idx, (int)side, self, alpha, s);
-      else spring_primal<T>(w, (int)idx, (int)side, self, s);
-    }
+  // contacts beyond the lane's first, two at a time so that their loads overlap
+  int e = lane + G;
+  for (; e + G < nm; e += 2 * G) {
+    const int2 ea = ld(&w.a.centry[cb + e]), eb = ld(&w.a.centry[cb + e + G]);
+    const ContactData<T> da = load_contact<T>(w, ea, selfSphere);
+    const ContactData<T> db = load_contact<T>(w, eb, selfSphere);
+    contact_primal<T>(da, self, alpha, s);
+    contact_primal<T>(db, self, alpha, s);
+  }
+  if (e < nm) contact_primal<T>(load_contact<T>(w, ld(&w.a.centry[cb + e]), selfSphere), self, alpha, s);
+  for (e = first_extra(lane, nm, G); e < total; e += G) {
+    const uint32_t ref = ld(&w.g.cRef[cStart + e - nm]);
+    const uint32_t type = ref >> 30, idx = (ref >> 1) & 0x1fffffffu, side = ref & 1u;
+    if (type == kRefJoint) joint_primal<T>(w, (int)idx, (int)side, self, alpha, s);
+    else spring_primal<T>(w, (int)idx, (int)side, self, s);
   }
 }
 
@@ -1057,21 +1067,27 @@ template <class T>
 __device__ __noinline__ void extra_dual(const World &w, int i, int cb, int nm, int cStart, int total, int lane, int G,
                                         bool selfSphere, const BState<T> &self, T alpha) {
   const int myColor = ld(&w.b.color[i]);
-  for (int e = lane; e < total; e += G) {
-    if (e < nm) {
-      if (e == lane) continue;
-      const ContactData<T> d = load_contact<T>(w, ld(&w.a.centry[cb + e]), selfSphere);
-      if (owns(myColor, d.otherColor)) contact_dual<T>(w, d, self, alpha);
-    } else {
-      const uint32_t ref = ld(&w.g.cRef[cStart + e - nm]);
-      const uint32_t type = ref >> 30, idx = (ref >> 1) & 0x1fffffffu, side = ref & 1u;
-      const int2 ab = type == kRefJoint ? ld(&w.j.bodies[idx]) : ld(&w.s.bodies[idx]);
-      const int other = side ? ab.x : ab.y;
-      const int oc = other >= 0 ? ld(&w.b.color[other]) : -1;
-      if (!owns(myColor, oc)) continue;
-      if (type == kRefJoint) joint_dual<T>(w, (int)idx, (int)side, self, alpha);
-      else spring_dual<T>(w, (int)idx, (int)side, self);
-    }
+  int e = lane + G;
+  for (; e + G < nm; e += 2 * G) {
+    const int2 ea = ld(&w.a.centry[cb + e]), eb = ld(&w.a.centry[cb + e + G]);
+    const ContactData<T> da = load_contact<T>(w, ea, selfSphere);
+    const ContactData<T> db = load_contact<T>(w, eb, selfSphere);
+    if (owns(myColor, da.otherColor)) contact_dual<T>(w, da, self, alpha);
+    if (owns(myColor, db.otherColor)) contact_dual<T>(w, db, self, alpha);
+  }
+  if (e < nm) {
+    const ContactData<T> d = load_contact<T>(w, ld(&w.a.centry[cb + e]), selfSphere);
+    if (owns(myColor, d.otherColor)) contact_dual<T>(w, d, self, alpha);
+  }
+  for (e = first_extra(lane, nm, G); e < total; e += G) {
+    const uint32_t ref = ld(&w.g.cRef[cStart + e - nm]);
+    const uint32_t type = ref >> 30, idx = (ref >> 1) & 0x1fffffffu, side = ref & 1u;
+    const int2 ab = type == kRefJoint ? ld(&w.j.bodies[idx]) : ld(&w.s.bodies[idx]);
+    const int other = side ? ab.x : ab.y;
+    const int oc = other >= 0 ? ld(&w.b.color[other]) : -1;
+    if (!owns(myColor, oc)) continue;
+    if (type == kRefJoint) joint_dual<T>(w, (int)idx, (int)side, self, alpha);
+    else spring_dual<T>(w, (int)idx, (int)side, self);
   }
 }
 
@@ -1216,18 +1232,22 @@ __device__ inline void st_release(int *p, int v) {
 
 constexpr long long kWaitLimit = 4000000;  // polls per body, about a second
 
+// The neighbours come from the body's manifold list (one entry per touching
+// body, where the per-contact list has up to eight) and its joints/springs.
 __device__ bool wait_neighbors(const World &w, int i, int it, int lane, int G, unsigned mask) {
   const int myColor = ld(&w.b.color[i]);
-  const int cb = ld(&w.a.cstart[i]);
-  int ce = ld(&w.a.cstart[i + 1]);
-  if (ce > w.a.ccap) ce = w.a.ccap;
+  const int mb = ld(&w.a.start[i]);
+  int me = ld(&w.a.start[i + 1]);
+  if (me > w.a.cap) me = w.a.cap;
   const int jb = ld(&w.g.cStart[i]), je = ld(&w.g.cStart[i + 1]);
-  const int nm = ce - cb, total = nm + (je - jb);
+  const int nm = me - mb, total = nm + (je - jb);
   long long polls = 0;
   for (int e = lane; e < total; e += G) {
     int other;
     if (e < nm) {
-      other = ld(&w.a.centry[cb + e]).y;
+      const uint32_t v = ld(&w.a.entry[mb + e]);
+      const unsigned long long key = __ldg(reinterpret_cast<const unsigned long long *>(w.cur.key) + (v >> 1));
+      other = (v & 1u) ? (int)(key >> 32) : (int)(key & 0xffffffffu);
     } else {
       const uint32_t ref = ld(&w.g.cRef[jb + e - nm]);
       const uint32_t type = ref >> 30, idx = (ref >> 1) & 0x1fffffffu, side = ref & 1u;
