@@ -94,6 +94,7 @@ struct Bodies {
   // per-step
   float4 *quatT;  // q_t
   float4 *dp;     // delta = p - p_t
+  float4 *dang;   // qsub(q, q_t) of the current iterate (f32), what neighbours read
   float4 *yLin;   // y - p_t
   float4 *yAng;   // q of the inertial prediction
   D4 *dpD, *quatD;  // f64 shadows (FP64 bodies)

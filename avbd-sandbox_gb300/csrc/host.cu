@@ -653,7 +653,7 @@ int avbd_pack(avbd_ctx *ctx, const avbd_world *world) {
   w.b.scene = sceneP; w.b.priority = prioP;
   if ((rc = dalloc(ctx, &w.b.pos, n)) || (rc = dalloc(ctx, &w.b.quat, n)) || (rc = dalloc(ctx, &w.b.vel, n)) ||
       (rc = dalloc(ctx, &w.b.omega, n)) || (rc = dalloc(ctx, &w.b.prevVel, n)) || (rc = dalloc(ctx, &w.b.quatT, n)) ||
-      (rc = dalloc(ctx, &w.b.dp, n)) || (rc = dalloc(ctx, &w.b.yLin, n)) || (rc = dalloc(ctx, &w.b.yAng, n)) ||
+      (rc = dalloc(ctx, &w.b.dp, n)) || (rc = dalloc(ctx, &w.b.dang, n)) || (rc = dalloc(ctx, &w.b.yLin, n)) || (rc = dalloc(ctx, &w.b.yAng, n)) ||
       (rc = dalloc(ctx, &w.b.dpD, n)) || (rc = dalloc(ctx, &w.b.quatD, n)) || (rc = dalloc(ctx, &w.b.flags, n)) ||
       (rc = dalloc(ctx, &w.b.color, n)) || (rc = dalloc(ctx, &w.b.progress, n)))
     return rc;

@@ -914,7 +914,7 @@ __device__ void write_sphere_manifold(const World &w, int c, int ia, int ib, con
   }
   for (int k = 0; k < 9; k++) w.cur.basisD[c * 9 + k] = basis[k];
   w.cur.basis0[c] = make_float4((float)basis[0], (float)basis[1], (float)basis[2], (float)friction);
-  w.cur.basis1[c] = make_float4((float)basis[3], (float)basis[4], (float)basis[5], 0.f);
+  w.cur.basis1[c] = make_float4((float)basis[3], (float)basis[4], (float)basis[5], 1.f);  // .w: sphere pair
   w.cur.basis2[c] = make_float4((float)basis[6], (float)basis[7], (float)basis[8], 0.f);
 }
 

@@ -32,7 +32,10 @@
 namespace avbd {
 namespace {
 
-constexpr int kSolveBlock = 256;
+constexpr int kSolveBlock = 128;   // threads of a solve block (3 blocks per SM)
+constexpr int kStageSlots = 4;     // contacts a lane stages in shared memory at a time
+constexpr int kStageVecs = 9;      // float4 per staged contact
+constexpr size_t kSolveSmem = (size_t)kSolveBlock * kStageSlots * kStageVecs * sizeof(float4);  // 73,728 B
 constexpr long long kSpinLimit = 20000000;  // ~1-2 s of polling at most
 
 // ---------------------------------------------------------------------------
@@ -203,6 +206,11 @@ __global__ void prepare_bodies_kernel(World w) {
       w.b.dpD[i] = mkd4(0.0, 0.0, 0.0, 0.0);
       w.b.quatD[i] = mkd4(q.x, q.y, q.z, q.w);
     }
+    {  // the iterate's qsub(q, q_t), as load_state<float> forms it
+      const float4 qn = w.b.quat[i];
+      const V3<float> da = qsub(Q4<float>{qn.x, qn.y, qn.z, qn.w}, Q4<float>{qf.x, qf.y, qf.z, qf.w});
+      w.b.dang[i] = make_float4(da.x, da.y, da.z, 0.f);
+    }
     w.b.flags[i] = fl;
     w.a.count[i] = 0;
     w.a.ccount[i] = 0;
@@ -279,7 +287,7 @@ __global__ void adj_sort_kernel(World w) {
         const int other = side ? (int)(key >> 32) : (int)(key & 0xffffffffu);
         const int cnt = w.cur.count[m];
         for (int k = 0; k < cnt && at < cend; k++, at++)
-          w.a.centry[at] = make_int2(((m * kMaxContacts + k) << 1) | side, other);
+          w.a.centry[at] = make_int2(((m * kMaxContacts + k) << 2) | side, other);  // owner bit set after colouring
       }
     }
     if (w.p.fp64Ratio > 0) {
@@ -392,6 +400,19 @@ __global__ void __launch_bounds__(256) coloring_kernel(World w) {
     if (round > 4096) {
       if (tid == 0) atomicOr(&ctl->flags, kOvfColors);
       break;
+    }
+  }
+  // owner bit (bit 1) of every contact entry: the endpoint with the larger
+  // colour owns the contact's dual update (a static endpoint has colour -1)
+  for (int i = tid; i < n; i += stride) {
+    if (!(w.b.flags0[i] & kBodyDynamic)) continue;
+    const int ci = color[i];
+    const int e1 = min(w.a.cstart[i + 1], w.a.ccap);
+    for (int e = w.a.cstart[i]; e < e1; e++) {
+      int2 v = w.a.centry[e];
+      const int oc = (w.b.flags0[v.y] & kBodyDynamic) ? color[v.y] : -1;
+      v.x = (v.x & ~2) | (ci > oc ? 2 : 0);
+      w.a.centry[e] = v;
     }
   }
   // --- stable counting sort by colour (per-block chunk of body indices) ---
@@ -662,13 +683,27 @@ __device__ __forceinline__ ContactEval<T> eval_contact(const V3<T> n[3], T mu, f
 }
 
 template <class T>
-__device__ __forceinline__ void manifold_rows(const World &w, int m, V3<T> n[3], T &mu, int &cnt) {
+__device__ __forceinline__ void manifold_rows(const World &w, int m, V3<T> n[3], T &mu, bool &sphere) {
   const float4 b0 = ld(&w.cur.basis0[m]), b1 = ld(&w.cur.basis1[m]), b2 = ld(&w.cur.basis2[m]);
   n[0] = V3<T>{(T)b0.x, (T)b0.y, (T)b0.z};
   n[1] = V3<T>{(T)b1.x, (T)b1.y, (T)b1.z};
   n[2] = V3<T>{(T)b2.x, (T)b2.y, (T)b2.z};
   mu = (T)b0.w;
-  cnt = ld(&w.cur.count[m]);
+  sphere = b1.w != 0.0f;  // the narrow phase marks sphere pairs here
+}
+
+// A neighbour's state as the contact rows read it: displacement and
+// qsub(q, q_t). The FP32 path reads what the neighbour published; the FP64
+// path forms it from the orientation as load_state does.
+template <class T>
+__device__ __forceinline__ BState<T> load_other(const World &w, int i) {
+  if (sizeof(T) == 8) return load_state<T>(w, i);
+  BState<T> s;
+  const float4 d = ldcg(&w.b.dp[i]), a = ldcg(&w.b.dang[i]);
+  s.dp = V3<T>{(T)d.x, (T)d.y, (T)d.z};
+  s.dang = V3<T>{(T)a.x, (T)a.y, (T)a.z};
+  s.q = Q4<T>{T(0), T(0), T(0), T(1)};  // not read by the contact rows
+  return s;
 }
 
 // One contact of a body's per-contact adjacency (slot = manifold * 8 + k),
@@ -681,25 +716,23 @@ struct ContactData {
   T mu;
   float4 cA, cB, cK, cL;
   BState<T> o;
-  int slot, side, otherColor;
+  int slot, side;
+  bool owned;  // this body owns the contact's dual update
   bool sphere;
 };
 
 template <class T>
-__device__ __forceinline__ ContactData<T> load_contact(const World &w, int2 ent, bool selfSphere) {
+__device__ __forceinline__ ContactData<T> load_contact(const World &w, int2 ent) {
   ContactData<T> d;
-  d.slot = ent.x >> 1;
+  d.slot = ent.x >> 2;
+  d.owned = (ent.x & 2) != 0;
   d.side = ent.x & 1;
-  const int other = ent.y;
-  int cnt;
-  manifold_rows(w, d.slot >> 3, d.n, d.mu, cnt);
+  manifold_rows(w, d.slot >> 3, d.n, d.mu, d.sphere);
   d.cA = ld(&w.cur.cA[d.slot]);
   d.cB = ld(&w.cur.cB[d.slot]);
   d.cK = __ldcg(&w.cur.cK[d.slot]);
   d.cL = __ldcg(&w.cur.cL[d.slot]);
-  d.o = load_state<T>(w, other);
-  d.otherColor = ld(&w.b.color[other]);
-  d.sphere = selfSphere || (ld(&w.b.flags0[other]) & kBodySphere) != 0;
+  d.o = load_other<T>(w, ent.y);
   return d;
 }
 
@@ -1044,17 +1077,17 @@ __device__ __forceinline__ int first_extra(int lane, int nm, int G) {
 
 template <class T>
 __device__ __noinline__ void extra_primal(const World &w, int i, int cb, int nm, int cStart, int total, int lane,
-                                          int G, bool selfSphere, const BState<T> &self, T alpha, Sys<T> &s) {
+                                          int G, const BState<T> &self, T alpha, Sys<T> &s) {
   // contacts beyond the lane's first, two at a time so that their loads overlap
   int e = lane + G;
   for (; e + G < nm; e += 2 * G) {
     const int2 ea = ld(&w.a.centry[cb + e]), eb = ld(&w.a.centry[cb + e + G]);
-    const ContactData<T> da = load_contact<T>(w, ea, selfSphere);
-    const ContactData<T> db = load_contact<T>(w, eb, selfSphere);
+    const ContactData<T> da = load_contact<T>(w, ea);
+    const ContactData<T> db = load_contact<T>(w, eb);
     contact_primal<T>(da, self, alpha, s);
     contact_primal<T>(db, self, alpha, s);
   }
-  if (e < nm) contact_primal<T>(load_contact<T>(w, ld(&w.a.centry[cb + e]), selfSphere), self, alpha, s);
+  if (e < nm) contact_primal<T>(load_contact<T>(w, ld(&w.a.centry[cb + e])), self, alpha, s);
   for (e = first_extra(lane, nm, G); e < total; e += G) {
     const uint32_t ref = ld(&w.g.cRef[cStart + e - nm]);
     const uint32_t type = ref >> 30, idx = (ref >> 1) & 0x1fffffffu, side = ref & 1u;
@@ -1063,23 +1096,28 @@ __device__ __noinline__ void extra_primal(const World &w, int i, int cb, int nm,
   }
 }
 
+// The dual updates of the extra entries this body owns; a contact's data is
+// loaded only when its owner bit says so.
 template <class T>
 __device__ __noinline__ void extra_dual(const World &w, int i, int cb, int nm, int cStart, int total, int lane, int G,
-                                        bool selfSphere, const BState<T> &self, T alpha) {
-  const int myColor = ld(&w.b.color[i]);
-  int e = lane + G;
-  for (; e + G < nm; e += 2 * G) {
-    const int2 ea = ld(&w.a.centry[cb + e]), eb = ld(&w.a.centry[cb + e + G]);
-    const ContactData<T> da = load_contact<T>(w, ea, selfSphere);
-    const ContactData<T> db = load_contact<T>(w, eb, selfSphere);
-    if (owns(myColor, da.otherColor)) contact_dual<T>(w, da, self, alpha);
-    if (owns(myColor, db.otherColor)) contact_dual<T>(w, db, self, alpha);
+                                        const BState<T> &self, T alpha) {
+  int pending = -1;  // an owned contact waiting for a partner, so loads go two at a time
+  for (int e = lane + G; e < nm; e += G) {
+    const int2 ent = ld(&w.a.centry[cb + e]);
+    if (!(ent.x & 2)) continue;
+    if (pending < 0) {
+      pending = e;
+      continue;
+    }
+    const ContactData<T> da = load_contact<T>(w, ld(&w.a.centry[cb + pending]));
+    const ContactData<T> db = load_contact<T>(w, ent);
+    contact_dual<T>(w, da, self, alpha);
+    contact_dual<T>(w, db, self, alpha);
+    pending = -1;
   }
-  if (e < nm) {
-    const ContactData<T> d = load_contact<T>(w, ld(&w.a.centry[cb + e]), selfSphere);
-    if (owns(myColor, d.otherColor)) contact_dual<T>(w, d, self, alpha);
-  }
-  for (e = first_extra(lane, nm, G); e < total; e += G) {
+  if (pending >= 0) contact_dual<T>(w, load_contact<T>(w, ld(&w.a.centry[cb + pending])), self, alpha);
+  const int myColor = total > nm ? ld(&w.b.color[i]) : 0;
+  for (int e = first_extra(lane, nm, G); e < total; e += G) {
     const uint32_t ref = ld(&w.g.cRef[cStart + e - nm]);
     const uint32_t type = ref >> 30, idx = (ref >> 1) & 0x1fffffffu, side = ref & 1u;
     const int2 ab = type == kRefJoint ? ld(&w.j.bodies[idx]) : ld(&w.s.bodies[idx]);
@@ -1091,13 +1129,89 @@ __device__ __noinline__ void extra_dual(const World &w, int i, int cb, int nm, i
   }
 }
 
+// Inertial terms of a body's system (solver.js:425-439), added by lane 0.
+template <class T>
+__device__ __forceinline__ void inertial_terms(const World &w, int i, const BState<T> &self, bool selfSphere,
+                                               Sys<T> &s) {
+  const SolverParams &P = w.p;
+  const T dt2 = (T)(P.dt * P.dt);
+  const D4 md = ld(&w.b.massD[i]);
+  const T m = (T)md.x;
+  const T ml = m / dt2;
+  s.l[0] = ml; s.l[2] = ml; s.l[5] = ml;
+  const float4 y = ld(&w.b.yLin[i]), qy = ld(&w.b.yAng[i]);
+  const V3<T> dy = self.dp - V3<T>{(T)y.x, (T)y.y, (T)y.z};
+  s.bl[0] = ml * dy.x; s.bl[1] = ml * dy.y; s.bl[2] = ml * dy.z;
+  // world moment R I R^T (rigid.js:228-247), / dt^2
+  T M[9];
+  const bool iso = !P.rotatedInertia || selfSphere;
+  const T I0 = (T)md.y, I1 = (T)md.z, I2 = (T)md.w;
+  if (iso) {
+    M[0] = I0; M[1] = 0; M[2] = 0; M[3] = 0; M[4] = I1; M[5] = 0; M[6] = 0; M[7] = 0; M[8] = I2;
+  } else {
+    const Q4<T> q = self.q;
+    const T xx = q.x * q.x, yy = q.y * q.y, zz = q.z * q.z, xy = q.x * q.y, xz = q.x * q.z, yz = q.y * q.z;
+    const T wx = q.w * q.x, wy = q.w * q.y, wz = q.w * q.z;
+    const T R[9] = {T(1) - T(2) * (yy + zz), T(2) * (xy - wz), T(2) * (xz + wy),
+                    T(2) * (xy + wz), T(1) - T(2) * (xx + zz), T(2) * (yz - wx),
+                    T(2) * (xz - wy), T(2) * (yz + wx), T(1) - T(2) * (xx + yy)};
+#pragma unroll
+    for (int a = 0; a < 3; a++)
+#pragma unroll
+      for (int b = 0; b < 3; b++) M[a * 3 + b] = R[a * 3] * I0 * R[b * 3] + R[a * 3 + 1] * I1 * R[b * 3 + 1] +
+                                                R[a * 3 + 2] * I2 * R[b * 3 + 2];
+  }
+  const V3<T> dq = qsub(self.q, Q4<T>{(T)qy.x, (T)qy.y, (T)qy.z, (T)qy.w});
+#pragma unroll
+  for (int a = 0; a < 3; a++)
+#pragma unroll
+    for (int b = 0; b <= a; b++) s.a[L(a, b)] = M[a * 3 + b] / dt2;
+  s.ba[0] = (M[0] * dq.x + M[1] * dq.y + M[2] * dq.z) / dt2;
+  s.ba[1] = (M[3] * dq.x + M[4] * dq.y + M[5] * dq.z) / dt2;
+  s.ba[2] = (M[6] * dq.x + M[7] * dq.y + M[8] * dq.z) / dt2;
+}
+
+// Reduce the group's partial systems, solve the 6x6 system (maths.js:660-725),
+// integrate (maths.js:568-592) and publish the new iterate; on the last main
+// iteration also the BDF1 velocity (solver.js:476-488).
+template <class T>
+__device__ __forceinline__ void finish_body(const World &w, int i, int lane, int G, unsigned mask, bool velocity,
+                                            Sys<T> &s, BState<T> &self) {
+  const T dt = (T)w.p.dt;
+  group_reduce(s, mask, G);
+  V3<T> xl, xa;
+  ldlt_solve(s, -s.bl[0], -s.bl[1], -s.bl[2], -s.ba[0], -s.ba[1], -s.ba[2], xl, xa);
+  self.dp = self.dp + xl;
+  self.q = qintegrate(self.q, xa);
+  const float4 qt = ld(&w.b.quatT[i]);
+  self.dang = qsub(self.q, Q4<T>{(T)qt.x, (T)qt.y, (T)qt.z, (T)qt.w});
+  if (lane != 0) return;
+  __stcg(&w.b.dp[i], make_float4((float)self.dp.x, (float)self.dp.y, (float)self.dp.z, 0.f));
+  __stcg(&w.b.quat[i], make_float4((float)self.q.x, (float)self.q.y, (float)self.q.z, (float)self.q.w));
+  {  // what neighbours read: qsub of the f32 orientation, as load_state<float> forms it
+    const V3<float> da =
+        sizeof(T) == 4 ? V3<float>{(float)self.dang.x, (float)self.dang.y, (float)self.dang.z}
+                       : qsub(Q4<float>{(float)self.q.x, (float)self.q.y, (float)self.q.z, (float)self.q.w},
+                              Q4<float>{qt.x, qt.y, qt.z, qt.w});
+    __stcg(&w.b.dang[i], make_float4(da.x, da.y, da.z, 0.f));
+  }
+  if (sizeof(T) == 8) {
+    stcg(&w.b.dpD[i], mkd4((double)self.dp.x, (double)self.dp.y, (double)self.dp.z, 0.0));
+    stcg(&w.b.quatD[i], mkd4((double)self.q.x, (double)self.q.y, (double)self.q.z, (double)self.q.w));
+  }
+  if (velocity) {  // BDF1 (solver.js:476-488)
+    w.b.prevVel[i] = ld(&w.b.vel[i]);
+    w.b.vel[i] = make_float4((float)(self.dp.x / dt), (float)(self.dp.y / dt), (float)(self.dp.z / dt), 0.f);
+    w.b.omega[i] = make_float4((float)(self.dang.x / dt), (float)(self.dang.y / dt), (float)(self.dang.z / dt), 0.f);
+  }
+}
+
 // One body's update (solver.js:425-457) by a group of G lanes, followed by
 // the dual updates (manifold.js:447, joint.js:255, spring.js:618) of the
 // constraints it owns, and on the last main iteration its BDF1 velocity.
+// Register form: the FP64 path.
 template <class T>
 __device__ void solve_body(const World &w, int4 rec, int lane, int G, unsigned mask, T alpha, bool dual, bool velocity) {
-  const SolverParams &P = w.p;
-  const T dt = (T)P.dt, dt2 = (T)(P.dt * P.dt);
   const int i = rec.x, cb = rec.y, nm = rec.z - rec.y;
   // one round of loads: own state, constraint ranges and this lane's first contact
   BState<T> self = load_state<T>(w, i);
@@ -1106,75 +1220,165 @@ __device__ void solve_body(const World &w, int4 rec, int lane, int G, unsigned m
   const bool selfSphere = (ld(&w.b.flags0[i]) & kBodySphere) != 0;
   const bool has0 = lane < nm;
   ContactData<T> d0;
-  if (has0) d0 = load_contact<T>(w, ld(&w.a.centry[cb + lane]), selfSphere);
+  if (has0) d0 = load_contact<T>(w, ld(&w.a.centry[cb + lane]));
   const bool extra = total > nm || nm > G;  // joints, springs or more contacts than lanes
-
   Sys<T> s;
   zero(s);
-  if (lane == 0) {  // inertial terms (solver.js:425-439)
-    const D4 md = ld(&w.b.massD[i]);
-    const T m = (T)md.x;
-    const T ml = m / dt2;
-    s.l[0] = ml; s.l[2] = ml; s.l[5] = ml;
-    const float4 y = ld(&w.b.yLin[i]), qy = ld(&w.b.yAng[i]);
-    const V3<T> dy = self.dp - V3<T>{(T)y.x, (T)y.y, (T)y.z};
-    s.bl[0] = ml * dy.x; s.bl[1] = ml * dy.y; s.bl[2] = ml * dy.z;
-    // world moment R I R^T (rigid.js:228-247), / dt^2
-    T M[9];
-    const bool iso = !P.rotatedInertia || selfSphere;
-    const T I0 = (T)md.y, I1 = (T)md.z, I2 = (T)md.w;
-    if (iso) {
-      M[0] = I0; M[1] = 0; M[2] = 0; M[3] = 0; M[4] = I1; M[5] = 0; M[6] = 0; M[7] = 0; M[8] = I2;
-    } else {
-      const Q4<T> q = self.q;
-      const T xx = q.x * q.x, yy = q.y * q.y, zz = q.z * q.z, xy = q.x * q.y, xz = q.x * q.z, yz = q.y * q.z;
-      const T wx = q.w * q.x, wy = q.w * q.y, wz = q.w * q.z;
-      const T R[9] = {T(1) - T(2) * (yy + zz), T(2) * (xy - wz), T(2) * (xz + wy),
-                      T(2) * (xy + wz), T(1) - T(2) * (xx + zz), T(2) * (yz - wx),
-                      T(2) * (xz - wy), T(2) * (yz + wx), T(1) - T(2) * (xx + yy)};
-#pragma unroll
-      for (int a = 0; a < 3; a++)
-#pragma unroll
-        for (int b = 0; b < 3; b++) M[a * 3 + b] = R[a * 3] * I0 * R[b * 3] + R[a * 3 + 1] * I1 * R[b * 3 + 1] +
-                                                  R[a * 3 + 2] * I2 * R[b * 3 + 2];
-    }
-    const V3<T> dq = qsub(self.q, Q4<T>{(T)qy.x, (T)qy.y, (T)qy.z, (T)qy.w});
-#pragma unroll
-    for (int a = 0; a < 3; a++)
-#pragma unroll
-      for (int b = 0; b <= a; b++) s.a[L(a, b)] = M[a * 3 + b] / dt2;
-    s.ba[0] = (M[0] * dq.x + M[1] * dq.y + M[2] * dq.z) / dt2;
-    s.ba[1] = (M[3] * dq.x + M[4] * dq.y + M[5] * dq.z) / dt2;
-    s.ba[2] = (M[6] * dq.x + M[7] * dq.y + M[8] * dq.z) / dt2;
-  }
+  if (lane == 0) inertial_terms<T>(w, i, self, selfSphere, s);
   if (has0) contact_primal<T>(d0, self, alpha, s);
-  if (extra) extra_primal<T>(w, i, cb, nm, cStart, total, lane, G, selfSphere, self, alpha, s);
-  group_reduce(s, mask, G);
-  V3<T> xl, xa;
-  ldlt_solve(s, -s.bl[0], -s.bl[1], -s.bl[2], -s.ba[0], -s.ba[1], -s.ba[2], xl, xa);
-  self.dp = self.dp + xl;
-  self.q = qintegrate(self.q, xa);
-  {
-    const float4 qt = ld(&w.b.quatT[i]);
-    self.dang = qsub(self.q, Q4<T>{(T)qt.x, (T)qt.y, (T)qt.z, (T)qt.w});
-  }
-  if (lane == 0) {
-    __stcg(&w.b.dp[i], make_float4((float)self.dp.x, (float)self.dp.y, (float)self.dp.z, 0.f));
-    __stcg(&w.b.quat[i], make_float4((float)self.q.x, (float)self.q.y, (float)self.q.z, (float)self.q.w));
-    if (sizeof(T) == 8) {
-      stcg(&w.b.dpD[i], mkd4((double)self.dp.x, (double)self.dp.y, (double)self.dp.z, 0.0));
-      stcg(&w.b.quatD[i], mkd4((double)self.q.x, (double)self.q.y, (double)self.q.z, (double)self.q.w));
-    }
-    if (velocity) {  // BDF1 (solver.js:476-488)
-      w.b.prevVel[i] = ld(&w.b.vel[i]);
-      w.b.vel[i] = make_float4((float)(self.dp.x / dt), (float)(self.dp.y / dt), (float)(self.dp.z / dt), 0.f);
-      w.b.omega[i] = make_float4((float)(self.dang.x / dt), (float)(self.dang.y / dt), (float)(self.dang.z / dt), 0.f);
-    }
-  }
+  if (extra) extra_primal<T>(w, i, cb, nm, cStart, total, lane, G, self, alpha, s);
+  finish_body<T>(w, i, lane, G, mask, velocity, s, self);
   if (!dual) return;
   // dual updates of the constraints this body owns (it has the larger colour)
-  if (has0 && owns(ld(&w.b.color[i]), d0.otherColor)) contact_dual<T>(w, d0, self, alpha);
-  if (extra) extra_dual<T>(w, i, cb, nm, cStart, total, lane, G, selfSphere, self, alpha);
+  if (has0 && d0.owned) contact_dual<T>(w, d0, self, alpha);
+  if (extra) extra_dual<T>(w, i, cb, nm, cStart, total, lane, G, self, alpha);
+}
+
+// ---------------------------------------------------------------------------
+// Staged form (the FP32 path). Each lane copies the data of up to
+// kStageSlots of its contacts - basis rows, the contact record, the other
+// body's displacement and rotation - into shared memory with cp.async, all
+// at once, then stamps them; a lane with no more than kStageSlots contacts
+// still holds them at the dual update, which then reads no global memory but
+// the writes. Slot (j, v) of thread t lives at stage[(j * kStageVecs + v) *
+// kSolveBlock + t], so a warp's accesses are conflict-free.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void cp_async_ca(float4 *dst, const float4 *src) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 16;" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_cg(float4 *dst, const float4 *src) {
+  const unsigned d = (unsigned)__cvta_generic_to_shared(dst);
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(d), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+// What the solve writes during the kernel (multipliers, penalties, neighbour
+// state) goes through L2 (.cg); what it only reads may also use L1 (.ca).
+__device__ __forceinline__ void stage_contact(const World &w, int2 ent, float4 *st) {
+  const int slot = ent.x >> 2, m = slot >> 3;
+  cp_async_ca(st + 0 * kSolveBlock, &w.cur.basis0[m]);
+  cp_async_ca(st + 1 * kSolveBlock, &w.cur.basis1[m]);
+  cp_async_ca(st + 2 * kSolveBlock, &w.cur.basis2[m]);
+  cp_async_ca(st + 3 * kSolveBlock, &w.cur.cA[slot]);
+  cp_async_ca(st + 4 * kSolveBlock, &w.cur.cB[slot]);
+  cp_async_cg(st + 5 * kSolveBlock, &w.cur.cK[slot]);
+  cp_async_cg(st + 6 * kSolveBlock, &w.cur.cL[slot]);
+  cp_async_cg(st + 7 * kSolveBlock, &w.b.dp[ent.y]);
+  cp_async_cg(st + 8 * kSolveBlock, &w.b.dang[ent.y]);
+}
+
+__device__ __forceinline__ ContactData<float> staged_contact(const float4 *st, int2 ent) {
+  ContactData<float> d;
+  d.slot = ent.x >> 2;
+  d.owned = (ent.x & 2) != 0;
+  d.side = ent.x & 1;
+  const float4 b0 = st[0], b1 = st[kSolveBlock], b2 = st[2 * kSolveBlock];
+  d.n[0] = V3<float>{b0.x, b0.y, b0.z};
+  d.n[1] = V3<float>{b1.x, b1.y, b1.z};
+  d.n[2] = V3<float>{b2.x, b2.y, b2.z};
+  d.mu = b0.w;
+  d.sphere = b1.w != 0.0f;
+  d.cA = st[3 * kSolveBlock];
+  d.cB = st[4 * kSolveBlock];
+  d.cK = st[5 * kSolveBlock];
+  d.cL = st[6 * kSolveBlock];
+  const float4 dp = st[7 * kSolveBlock], da = st[8 * kSolveBlock];
+  d.o.dp = V3<float>{dp.x, dp.y, dp.z};
+  d.o.dang = V3<float>{da.x, da.y, da.z};
+  d.o.q = Q4<float>{0.f, 0.f, 0.f, 1.f};  // not read by the contact rows
+  return d;
+}
+
+// Stage chunk [k0, k0 + cnt) of this lane's contacts (contact e = lane + k G).
+__device__ __forceinline__ int stage_chunk(const World &w, int cb, int lane, int G, int k0, int cnt, int2 *ent,
+                                           float4 *stage, bool ownedOnly) {
+  int staged = 0;
+#pragma unroll
+  for (int j = 0; j < kStageSlots; j++)
+    if (j < cnt) ent[j] = ld(&w.a.centry[cb + lane + (k0 + j) * G]);
+#pragma unroll
+  for (int j = 0; j < kStageSlots; j++)
+    if (j < cnt && (!ownedOnly || (ent[j].x & 2))) {
+      stage_contact(w, ent[j], stage + j * kStageVecs * kSolveBlock);
+      staged++;
+    }
+  cp_async_commit();
+  return staged;
+}
+
+// The joints and springs of a body (entries nm..total of its constraint list).
+template <class T>
+__device__ __noinline__ void constraints_primal(const World &w, int nm, int cStart, int total, int lane, int G,
+                                                const BState<T> &self, T alpha, Sys<T> &s) {
+  for (int e = first_extra(lane, nm, G); e < total; e += G) {
+    const uint32_t ref = ld(&w.g.cRef[cStart + e - nm]);
+    const uint32_t type = ref >> 30, idx = (ref >> 1) & 0x1fffffffu, side = ref & 1u;
+    if (type == kRefJoint) joint_primal<T>(w, (int)idx, (int)side, self, alpha, s);
+    else spring_primal<T>(w, (int)idx, (int)side, self, s);
+  }
+}
+
+template <class T>
+__device__ __noinline__ void constraints_dual(const World &w, int i, int nm, int cStart, int total, int lane, int G,
+                                              const BState<T> &self, T alpha) {
+  const int myColor = ld(&w.b.color[i]);
+  for (int e = first_extra(lane, nm, G); e < total; e += G) {
+    const uint32_t ref = ld(&w.g.cRef[cStart + e - nm]);
+    const uint32_t type = ref >> 30, idx = (ref >> 1) & 0x1fffffffu, side = ref & 1u;
+    const int2 ab = type == kRefJoint ? ld(&w.j.bodies[idx]) : ld(&w.s.bodies[idx]);
+    const int other = side ? ab.x : ab.y;
+    const int oc = other >= 0 ? ld(&w.b.color[other]) : -1;
+    if (!owns(myColor, oc)) continue;
+    if (type == kRefJoint) joint_dual<T>(w, (int)idx, (int)side, self, alpha);
+    else spring_dual<T>(w, (int)idx, (int)side, self);
+  }
+}
+
+__device__ void solve_body_staged(const World &w, int4 rec, int lane, int G, unsigned mask, float alpha, bool dual,
+                                  bool velocity, float4 *stage) {
+  using T = float;
+  const int i = rec.x, cb = rec.y, nm = rec.z - rec.y;
+  const int nk = lane < nm ? (nm - lane + G - 1) / G : 0;  // this lane's contacts
+  int2 ent[kStageSlots];
+  int cnt = nk < kStageSlots ? nk : kStageSlots;
+  stage_chunk(w, cb, lane, G, 0, cnt, ent, stage, false);  // in flight while the body's own data loads
+  BState<T> self = load_state<T>(w, i);
+  const int cStart = ld(&w.g.cStart[i]), cEnd = ld(&w.g.cStart[i + 1]);
+  const int total = nm + (cEnd - cStart);
+  Sys<T> s;
+  zero(s);
+  if (lane == 0) inertial_terms<T>(w, i, self, (ld(&w.b.flags0[i]) & kBodySphere) != 0, s);
+  for (int k0 = 0;;) {
+    cp_async_wait_all();
+    for (int j = 0; j < cnt; j++)
+      contact_primal<T>(staged_contact(stage + j * kStageVecs * kSolveBlock, ent[j]), self, alpha, s);
+    k0 += cnt;
+    if (k0 >= nk) break;
+    cnt = nk - k0 < kStageSlots ? nk - k0 : kStageSlots;
+    stage_chunk(w, cb, lane, G, k0, cnt, ent, stage, false);
+  }
+  if (total > nm) constraints_primal<T>(w, nm, cStart, total, lane, G, self, alpha, s);
+  finish_body<T>(w, i, lane, G, mask, velocity, s, self);
+  if (!dual) return;
+  if (nk <= kStageSlots) {
+    // every contact of this lane is still staged; the owner alone writes a
+    // contact's multiplier and penalty, and the other body is done with
+    // this iteration, so the staged values are current
+    for (int j = 0; j < cnt; j++)
+      if (ent[j].x & 2) contact_dual<T>(w, staged_contact(stage + j * kStageVecs * kSolveBlock, ent[j]), self, alpha);
+  } else {
+    for (int k0 = 0; k0 < nk; k0 += kStageSlots) {
+      const int c2 = nk - k0 < kStageSlots ? nk - k0 : kStageSlots;
+      stage_chunk(w, cb, lane, G, k0, c2, ent, stage, true);
+      cp_async_wait_all();
+      for (int j = 0; j < c2; j++)
+        if (ent[j].x & 2)
+          contact_dual<T>(w, staged_contact(stage + j * kStageVecs * kSolveBlock, ent[j]), self, alpha);
+    }
+  }
+  if (total > nm) constraints_dual<T>(w, i, nm, cStart, total, lane, G, self, alpha);
 }
 
 // The FP64 path is kept out of line so that its register demand (and any
@@ -1185,7 +1389,9 @@ __device__ __noinline__ void solve_body_f64(const World &w, int4 rec, int lane, 
   solve_body<double>(w, rec, lane, G, mask, alpha, dual, velocity);
 }
 
-__global__ void __launch_bounds__(kSolveBlock, 2) solve_kernel(World w, int G) {
+__global__ void __launch_bounds__(kSolveBlock, 3) solve_kernel(World w, int G) {
+  extern __shared__ float4 stageSm[];
+  float4 *stage = stageSm + threadIdx.x;
   const SolverParams &P = w.p;
   Control *ctl = w.ctl;
   const int numColors = *((volatile int *)&ctl->numColors);
@@ -1205,7 +1411,7 @@ __global__ void __launch_bounds__(kSolveBlock, 2) solve_kernel(World w, int G) {
       for (int k = beg + group; k < end; k += groups) {
         const int4 rec = ld(&w.a.colorRec[k]);
         if (ld(&w.b.flags[rec.x]) & kBodyFp64) solve_body_f64(w, rec, lane, G, mask, alpha, dual, vel);
-        else solve_body<float>(w, rec, lane, G, mask, (float)alpha, dual, vel);
+        else solve_body_staged(w, rec, lane, G, mask, (float)alpha, dual, vel, stage);
       }
       if (!grid_barrier(ctl)) return;
     }
@@ -1271,7 +1477,9 @@ __device__ bool wait_neighbors(const World &w, int i, int it, int lane, int G, u
   return __all_sync(mask, polls >= 0);
 }
 
-__global__ void __launch_bounds__(kSolveBlock, 2) wave_kernel(World w, int G) {
+__global__ void __launch_bounds__(kSolveBlock, 3) wave_kernel(World w, int G) {
+  extern __shared__ float4 stageSm[];
+  float4 *stage = stageSm + threadIdx.x;
   const SolverParams &P = w.p;
   Control *ctl = w.ctl;
   const int numColors = *((volatile int *)&ctl->numColors);
@@ -1293,8 +1501,9 @@ __global__ void __launch_bounds__(kSolveBlock, 2) wave_kernel(World w, int G) {
         const int4 rec = ld(&w.a.colorRec[k]);
         const int i = rec.x;
         if (!wait_neighbors(w, i, it, lane, G, mask)) return;
+        __syncwarp(mask);  // orders every lane's reads after the acquires of the others
         if (ld(&w.b.flags[i]) & kBodyFp64) solve_body_f64(w, rec, lane, G, mask, alpha, dual, vel);
-        else solve_body<float>(w, rec, lane, G, mask, (float)alpha, dual, vel);
+        else solve_body_staged(w, rec, lane, G, mask, (float)alpha, dual, vel, stage);
         __threadfence();
         __syncwarp(mask);
         if (lane == 0) st_release(&w.b.progress[i], it + 1);
@@ -1401,9 +1610,11 @@ cudaError_t launch_coloring(const World &w, cudaStream_t st, int smCount) {
 
 int solve_max_blocks_per_sm(int lanesPerBody) {
   (void)lanesPerBody;
+  cudaFuncSetAttribute(solve_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSolveSmem);
+  cudaFuncSetAttribute(wave_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSolveSmem);
   int a = 0, b = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, solve_kernel, kSolveBlock, 0);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, wave_kernel, kSolveBlock, 0);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, solve_kernel, kSolveBlock, kSolveSmem);
+  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, wave_kernel, kSolveBlock, kSolveSmem);
   return a < b ? a : b;
 }
 
@@ -1412,7 +1623,7 @@ cudaError_t launch_solve(const World &w, int lanesPerBody, int blocksPerSm, cuda
   int G = lanesPerBody;
   void *args[] = {&arg, &G};
   const void *fn = w.p.schedule == 1 ? (const void *)wave_kernel : (const void *)solve_kernel;
-  return cudaLaunchCooperativeKernel(fn, dim3(blocksPerSm * smCount), dim3(kSolveBlock), args, 0, st);
+  return cudaLaunchCooperativeKernel(fn, dim3(blocksPerSm * smCount), dim3(kSolveBlock), args, kSolveSmem, st);
 }
 
 void launch_commit(const World &w, cudaStream_t st, int smCount) { commit_kernel<<<smCount * 4, 256, 0, st>>>(w); }
