@@ -133,7 +133,9 @@ class Profile(C.Structure):
                 ("prepare_ms", C.c_double), ("coloring_ms", C.c_double),
                 ("solve_ms", C.c_double), ("step_ms", C.c_double),
                 ("candidate_pairs", C.c_int64), ("manifolds", C.c_int64), ("contacts", C.c_int64),
-                ("colors", C.c_int32), ("fp64_bodies", C.c_int32)]
+                ("colors", C.c_int32), ("fp64_bodies", C.c_int32),
+                ("np_face", C.c_int32), ("np_edge", C.c_int32), ("np_exact", C.c_int32),
+                ("reserved", C.c_int32)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

@@ -190,6 +190,8 @@ struct Adjacency {
   int *ccount;   // n
   int2 *centry;
   int ccap;
+  int *hpEntry;      // per body, within its manifold range: dynamic neighbours of higher colouring priority
+  int *hpCount;      // n
   int *colorStart;   // kMaxColors + 1
   int *colorBodies;  // dynamic bodies sorted by (colour, index)
   int4 *colorRec;    // per colour position: body, contact range begin, end, 0

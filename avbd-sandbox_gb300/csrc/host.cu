@@ -165,7 +165,8 @@ int alloc_candidate_arenas(avbd_ctx *ctx, int cap) {
       (rc = galloc(ctx, &w.g.candKey, cap)) || (rc = galloc(ctx, &w.g.candPrev, cap)) ||
       (rc = galloc(ctx, &w.g.npFace, cap)) || (rc = galloc(ctx, &w.g.npEdge, cap)) ||
       (rc = galloc(ctx, &w.g.npExact, cap)) ||
-      (rc = galloc(ctx, &w.a.entry, ctx->adjCap)) || (rc = galloc(ctx, &w.a.centry, w.a.ccap)))
+      (rc = galloc(ctx, &w.a.entry, ctx->adjCap)) || (rc = galloc(ctx, &w.a.hpEntry, ctx->adjCap)) ||
+      (rc = galloc(ctx, &w.a.centry, w.a.ccap)))
     return rc;
   return AVBD_OK;
 }
@@ -400,6 +401,9 @@ int one_step(avbd_ctx *ctx) {
     ctx->prof.contacts = c.liveContacts;
     ctx->prof.colors = c.numColors;
     ctx->prof.fp64_bodies = c.fp64Bodies;
+    ctx->prof.np_face = c.npCount[0];
+    ctx->prof.np_edge = c.npCount[1];
+    ctx->prof.np_exact = c.npCount[2];
   }
   return AVBD_OK;
 }
@@ -702,6 +706,7 @@ int avbd_pack(avbd_ctx *ctx, const avbd_world *world) {
   w.a.cap = ctx->adjCap;
   ctx->colorBlocks = std::max(1, coloring_grid(ctx->smCount));
   if ((rc = dalloc(ctx, &w.a.start, n + 1)) || (rc = dalloc(ctx, &w.a.count, n + 1)) ||
+      (rc = dalloc(ctx, &w.a.hpCount, n)) ||
       (rc = dalloc(ctx, &w.a.cursor, n + 1)) || (rc = dalloc(ctx, &w.a.cstart, n + 1)) ||
       (rc = dalloc(ctx, &w.a.ccount, n + 1)) ||
       (rc = dalloc(ctx, &w.a.colorStart, kMaxColors + 1)) || (rc = dalloc(ctx, &w.a.colorBodies, n)) ||

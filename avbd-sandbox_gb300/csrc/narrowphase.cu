@@ -134,7 +134,7 @@ __device__ BoxF make_boxf(const BodyD &A, const BodyD &B) {
 }
 
 // Outcome of the f32 SAT of a box pair.
-constexpr int kSeparated = 0, kFaceWin = 1, kEdgeWin = 2, kUndecided = 3;
+constexpr int kSeparated = 0, kFaceWin = 1, kEdgeWin = 2, kUndecided = 3, kFaceTie = 4;
 
 // f32 SAT of a box-box pair (collide.js:612-685), certified against the f64
 // evaluation: every axis separation comes with a bound err >= |sep_f32 -
@@ -146,9 +146,12 @@ constexpr int kSeparated = 0, kFaceWin = 1, kEdgeWin = 2, kUndecided = 3;
 // finds a separating axis too and returns no contact). kFaceWin / kEdgeWin
 // when no axis can separate, the best face axis (largest separation, first
 // on ties) and, if it can matter, the best edge axis are certain, and so is
-// the choice 0.95 sepE > sepF + 0.01 between them. kUndecided otherwise: the
-// exact f64 path decides.
-__device__ int classify_f32(const BoxF &F, bool &refIsA, int &axA, int &axB) {
+// the choice 0.95 sepE > sepF + 0.01 between them. kFaceTie when all of that
+// holds and a face wins, but which face is not certain: tieMask (bits 0-5:
+// faces 0-2 of A, 0-2 of B) lists the face axes that can be the largest,
+// for an exact f64 comparison of just those. kUndecided otherwise: the exact
+// f64 path decides.
+__device__ int classify_f32(const BoxF &F, bool &refIsA, int &axA, int &axB, int &tieMask) {
   const float S = fabsf(F.d.x) + fabsf(F.d.y) + fabsf(F.d.z) + F.ha[0] + F.ha[1] + F.ha[2] + F.hb[0] + F.hb[1] +
                   F.hb[2];
   if (!(S == S) || S > 1e30f) return kUndecided;
@@ -158,6 +161,9 @@ __device__ int classify_f32(const BoxF &F, bool &refIsA, int &axA, int &axB) {
   // best of each group so far, and the largest upper bound among the others
   int fBest = -1, eBest = -1;
   float fSep = 0.f, fErr = 0.f, fOther = -INFINITY, eSep = 0.f, eErr = 0.f, eOther = -INFINITY;
+  float fUp[6];  // upper bound of each face axis's separation
+#pragma unroll
+  for (int k = 0; k < 6; k++) fUp[k] = -INFINITY;
 #pragma unroll
   for (int k = 0; k < 15; k++) {
     V3<float> a;
@@ -198,6 +204,7 @@ __device__ int classify_f32(const BoxF &F, bool &refIsA, int &axA, int &axB) {
       continue;
     }
     if (!edge) {
+      fUp[k < 6 ? k : 0] = sep + err;
       if (fBest < 0 || sep > fSep) {
         if (fBest >= 0) fOther = fmaxf(fOther, fSep + fErr);
         fBest = k; fSep = sep; fErr = err;
@@ -228,7 +235,13 @@ __device__ int classify_f32(const BoxF &F, bool &refIsA, int &axA, int &axB) {
     axB = (eBest - 6) % 3;
     return kEdgeWin;
   }
-  if (!(fOther < fSep - fErr)) return kUndecided;  // tied face axes
+  if (!(fOther < fSep - fErr)) {  // tied face axes: the candidates for an exact comparison
+    tieMask = 0;
+#pragma unroll
+    for (int k = 0; k < 6; k++)
+      if (fUp[k] >= fLo) tieMask |= 1 << k;
+    return kFaceTie;
+  }
   refIsA = fBest < 3;
   axA = refIsA ? fBest : fBest - 3;
   return kFaceWin;
@@ -933,6 +946,38 @@ __device__ __forceinline__ void push_exact(const World &w, int c) {
   w.g.npExact[push_slot(&w.ctl->npCount[2])] = c;
 }
 
+// The face axis among `mask` (bits 0-5: faces of A, then of B) with the
+// largest exact separation, the first on ties: the f64 expressions of
+// testAxis (collide.js:291-324) for just those axes.
+__device__ int exact_best_face(const BodyD &A, const BodyD &B, int mask) {
+  const D3 e3[3] = {mk(1, 0, 0), mk(0, 1, 0), mk(0, 0, 1)};
+  D3 ax[3], bx[3];
+  for (int i = 0; i < 3; i++) {
+    ax[i] = rot(A.q, e3[i]);
+    bx[i] = rot(B.q, e3[i]);
+  }
+  const D3 delta = sub(B.p, A.p);
+  int best = -1;
+  double bestSep = -INFINITY;
+  for (int k = 0; k < 6; k++) {
+    if (!((mask >> k) & 1)) continue;
+    const D3 axis = k < 3 ? ax[k] : bx[k - 3];
+    const double lenSq = axis.x * axis.x + axis.y * axis.y + axis.z * axis.z;
+    const double invLen = 1.0 / sqrt(lenSq);
+    D3 n = scl(axis, invLen);
+    if (dt3(n, delta) < 0) n = neg(n);
+    const double distance = fabs(dt3(delta, n));
+    const double rA = A.half.x * fabs(dt3(n, ax[0])) + A.half.y * fabs(dt3(n, ax[1])) + A.half.z * fabs(dt3(n, ax[2]));
+    const double rB = B.half.x * fabs(dt3(n, bx[0])) + B.half.y * fabs(dt3(n, bx[1])) + B.half.z * fabs(dt3(n, bx[2]));
+    const double separation = distance - (rA + rB);
+    if (best < 0 || separation > bestSep) {
+      best = k;
+      bestSep = separation;
+    }
+  }
+  return best;
+}
+
 // 1. Every candidate: the f32 SAT. Separated pairs get count 0; box pairs
 //    with a certain winning axis go to the face or edge list, everything
 //    else (sphere pairs, undecided box pairs) to the exact list.
@@ -947,12 +992,14 @@ __global__ void __launch_bounds__(256) classify_kernel(World w) {
       continue;
     }
     bool refIsA = true;
-    int axA = 0, axB = 0;
-    const int r = classify_f32(make_boxf(A, B), refIsA, axA, axB);
+    int axA = 0, axB = 0, tieMask = 0;
+    const int r = classify_f32(make_boxf(A, B), refIsA, axA, axB, tieMask);
     if (r == kSeparated) {
       w.cur.count[c] = 0;
     } else if (r == kFaceWin) {
       w.g.npFace[push_slot(&w.ctl->npCount[0])] = make_int2(c, (refIsA ? 4 : 0) | axA);
+    } else if (r == kFaceTie) {
+      w.g.npFace[push_slot(&w.ctl->npCount[0])] = make_int2(c, tieMask << 8);
     } else if (r == kEdgeWin) {
       w.g.npEdge[push_slot(&w.ctl->npCount[1])] = make_int2(c, axA * 3 + axB);
     } else {
@@ -968,11 +1015,16 @@ __global__ void __launch_bounds__(128) face_kernel(World w) {
   for (int t = blockIdx.x * blockDim.x + threadIdx.x; t < total; t += gridDim.x * blockDim.x) {
     const int2 e = w.g.npFace[t];
     const int c = e.x;
-    const bool refIsA = (e.y & 4) != 0;
-    const int refAxis = e.y & 3;
+    bool refIsA = (e.y & 4) != 0;
+    int refAxis = e.y & 3;
     const uint64_t key = w.g.candKey[c];
     const int ia = (int)(key >> 32), ib = (int)(key & 0xffffffffu);
     const BodyD A = load_body(w, ia), B = load_body(w, ib);
+    if (e.y >> 8) {  // tied face axes: their exact separations decide (first largest wins)
+      const int k = exact_best_face(A, B, e.y >> 8);
+      refIsA = k < 3;
+      refAxis = refIsA ? k : k - 3;
+    }
     // f64: the reference axis, the incident box's axes, the exact normal
     const QD qRef = refIsA ? A.q : B.q, qInc = refIsA ? B.q : A.q;
     const D3 e3[3] = {mk(1, 0, 0), mk(0, 1, 0), mk(0, 0, 1)};

@@ -219,6 +219,11 @@ __global__ void prepare_bodies_kernel(World w) {
 }
 
 // Live manifolds of this step: count the incident ones of every dynamic body.
+__device__ inline bool precedes(const World &w, int j, int i) {
+  const uint32_t pj = w.b.priority[j], pi = w.b.priority[i];
+  return pj < pi || (pj == pi && j < i);
+}
+
 __global__ void adj_count_kernel(World w) {
   const int total = w.ctl->numCandidates;
   for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < total; c += gridDim.x * blockDim.x) {
@@ -276,10 +281,13 @@ __global__ void adj_sort_kernel(World w) {
       }
       e[y + 1] = v;
     }
-    // per-contact adjacency, in manifold order then contact order
+    // per-contact adjacency, in manifold order then contact order; and the
+    // dynamic neighbours of higher colouring priority (the only ones a
+    // colouring round reads), stored in the body's own manifold range
     {
       int at = w.a.cstart[i];
       const int cend = min(w.a.cstart[i + 1], w.a.ccap);
+      int hc = 0;
       for (int x = beg; x < end; x++) {
         const uint32_t v = e[x];
         const int m = (int)(v >> 1), side = (int)(v & 1u);
@@ -288,7 +296,9 @@ __global__ void adj_sort_kernel(World w) {
         const int cnt = w.cur.count[m];
         for (int k = 0; k < cnt && at < cend; k++, at++)
           w.a.centry[at] = make_int2(((m * kMaxContacts + k) << 2) | side, other);  // owner bit set after colouring
+        if ((w.b.flags0[other] & kBodyDynamic) && precedes(w, other, i)) w.a.hpEntry[beg + hc++] = other;
       }
+      w.a.hpCount[i] = hc;
     }
     if (w.p.fp64Ratio > 0) {
       double kmax = 0;
@@ -323,22 +333,9 @@ __global__ void adj_sort_kernel(World w) {
 // is exactly the sequential greedy colouring in priority order). Then a
 // stable counting sort lists each colour's bodies in index order.
 // ---------------------------------------------------------------------------
-__device__ inline bool precedes(const World &w, int j, int i) {
-  const uint32_t pj = w.b.priority[j], pi = w.b.priority[i];
-  return pj < pi || (pj == pi && j < i);
-}
-
+// The live joint and spring partners of body i that are dynamic.
 template <class F>
-__device__ inline void for_each_neighbor(const World &w, int i, F &&f) {
-  int end = w.a.start[i + 1];
-  if (end > w.a.cap) end = w.a.cap;
-  for (int k = w.a.start[i]; k < end; k++) {
-    const uint32_t e = w.a.entry[k];
-    const int c = (int)(e >> 1);
-    const uint64_t key = w.cur.key[c];
-    const int other = (e & 1u) ? (int)(key >> 32) : (int)(key & 0xffffffffu);
-    if (w.b.flags0[other] & kBodyDynamic) f(other);
-  }
+__device__ inline void constraint_neighbors(const World &w, int i, F &&f) {
   for (int k = w.g.cStart[i]; k < w.g.cStart[i + 1]; k++) {
     const uint32_t ref = w.g.cRef[k];
     const uint32_t type = ref >> 30, idx = (ref >> 1) & 0x1fffffffu, side = ref & 1u;
@@ -377,12 +374,18 @@ __global__ void __launch_bounds__(256) coloring_kernel(World w) {
     for (int i = tid; i < n; i += stride) {
       if (!(w.b.flags0[i] & kBodyDynamic)) continue;
       unsigned long long used = 0ull;
-      for_each_neighbor(w, i, [&](int j) {
-        if (precedes(w, j, i)) {
-          const int c = color[j];
-          if (c >= 0 && c < kMaxColors) used |= 1ull << c;
-        }
-      });
+      const int hb = w.a.start[i], hc = w.a.hpCount[i];
+      for (int k = 0; k < hc; k++) {
+        const int c = color[w.a.hpEntry[hb + k]];
+        if (c >= 0 && c < kMaxColors) used |= 1ull << c;
+      }
+      if (w.g.hasConstraints)
+        constraint_neighbors(w, i, [&](int j) {
+          if (precedes(w, j, i)) {
+            const int c = color[j];
+            if (c >= 0 && c < kMaxColors) used |= 1ull << c;
+          }
+        });
       int c = __ffsll((long long)~used) - 1;
       if (c < 0) {
         c = kMaxColors - 1;

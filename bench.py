@@ -232,8 +232,8 @@ def run_gpu(args):
     phase_tot = {k: 0.0 for k in ("broadphase_ms", "narrowphase_ms", "prepare_ms", "coloring_ms", "solve_ms")}
     algo_tot = {"solve": 0.0, "narrowphase": 0.0}
     step_ms = []
-    work = {"candidate_pairs": 0, "manifolds": 0, "contacts": 0}
-    peak_work = dict(work, colors=0, fp64_bodies=0)
+    work = {"candidate_pairs": 0, "manifolds": 0, "contacts": 0, "np_face": 0, "np_edge": 0, "np_exact": 0}
+    peak_work = {k: 0 for k in ("candidate_pairs", "manifolds", "contacts", "colors", "fp64_bodies")}
     if ws > 1:
         torch.distributed.barrier()
     torch.cuda.synchronize()

@@ -231,6 +231,12 @@ typedef struct avbd_profile {
   int64_t contacts;           /* contact points in those manifolds          */
   int32_t colors;
   int32_t fp64_bodies;
+  /* narrow-phase work split: box pairs with a certain face / edge winner
+     (f32 geometry) and pairs decided by the exact f64 collider */
+  int32_t np_face;
+  int32_t np_edge;
+  int32_t np_exact;
+  int32_t reserved;
 } avbd_profile;
 
 typedef struct avbd_ctx avbd_ctx;
