@@ -531,6 +531,51 @@ __device__ __forceinline__ void group_reduce(Sys<T> &s, unsigned mask, int G) {
   }
 }
 
+// For groups of 32 lanes: the same sums by reduce-scatter (xor distances 16,
+// 8, 4, 2, 1, the butterfly's own pairing, so every total is bitwise the
+// butterfly's) and an all-gather: 31 + 27 shuffles instead of 5 x 27.
+__device__ __forceinline__ void group_reduce32(Sys<float> &s) {
+  const int lane = threadIdx.x & 31;
+  float v[32];
+#pragma unroll
+  for (int k = 0; k < 6; k++) {
+    v[k] = s.l[k];
+    v[6 + k] = s.a[k];
+  }
+#pragma unroll
+  for (int k = 0; k < 9; k++) v[12 + k] = s.c[k];
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    v[21 + k] = s.bl[k];
+    v[24 + k] = s.ba[k];
+  }
+#pragma unroll
+  for (int k = 27; k < 32; k++) v[k] = 0.f;
+#pragma unroll
+  for (int h = 16; h > 0; h >>= 1) {
+    const bool up = (lane & h) != 0;
+#pragma unroll
+    for (int p = 0; p < h; p++) {
+      const float send = up ? v[p] : v[p + h];
+      const float keep = up ? v[p + h] : v[p];
+      v[p] = keep + __shfl_xor_sync(0xffffffffu, send, h);
+    }
+  }
+  // lane j now holds the total of value j
+#pragma unroll
+  for (int k = 0; k < 6; k++) {
+    s.l[k] = __shfl_sync(0xffffffffu, v[0], k);
+    s.a[k] = __shfl_sync(0xffffffffu, v[0], 6 + k);
+  }
+#pragma unroll
+  for (int k = 0; k < 9; k++) s.c[k] = __shfl_sync(0xffffffffu, v[0], 12 + k);
+#pragma unroll
+  for (int k = 0; k < 3; k++) {
+    s.bl[k] = __shfl_sync(0xffffffffu, v[0], 21 + k);
+    s.ba[k] = __shfl_sync(0xffffffffu, v[0], 24 + k);
+  }
+}
+
 // sym 3x3 lower index
 __device__ inline constexpr int L(int r, int c) { return r >= c ? (r * (r + 1)) / 2 + c : (c * (c + 1)) / 2 + r; }
 
@@ -1179,14 +1224,18 @@ __device__ __forceinline__ void inertial_terms(const World &w, int i, const BSta
 // iteration also the BDF1 velocity (solver.js:476-488).
 template <class T>
 __device__ __forceinline__ void finish_body(const World &w, int i, int lane, int G, unsigned mask, bool velocity,
-                                            Sys<T> &s, BState<T> &self) {
+                                            float4 qt, Sys<T> &s, BState<T> &self) {
   const T dt = (T)w.p.dt;
-  group_reduce(s, mask, G);
+  if constexpr (sizeof(T) == 4) {
+    if (G == 32) group_reduce32(s);
+    else group_reduce(s, mask, G);
+  } else {
+    group_reduce(s, mask, G);
+  }
   V3<T> xl, xa;
   ldlt_solve(s, -s.bl[0], -s.bl[1], -s.bl[2], -s.ba[0], -s.ba[1], -s.ba[2], xl, xa);
   self.dp = self.dp + xl;
   self.q = qintegrate(self.q, xa);
-  const float4 qt = ld(&w.b.quatT[i]);
   self.dang = qsub(self.q, Q4<T>{(T)qt.x, (T)qt.y, (T)qt.z, (T)qt.w});
   if (lane != 0) return;
   __stcg(&w.b.dp[i], make_float4((float)self.dp.x, (float)self.dp.y, (float)self.dp.z, 0.f));
@@ -1230,7 +1279,7 @@ __device__ void solve_body(const World &w, int4 rec, int lane, int G, unsigned m
   if (lane == 0) inertial_terms<T>(w, i, self, selfSphere, s);
   if (has0) contact_primal<T>(d0, self, alpha, s);
   if (extra) extra_primal<T>(w, i, cb, nm, cStart, total, lane, G, self, alpha, s);
-  finish_body<T>(w, i, lane, G, mask, velocity, s, self);
+  finish_body<T>(w, i, lane, G, mask, velocity, ld(&w.b.quatT[i]), s, self);
   if (!dual) return;
   // dual updates of the constraints this body owns (it has the larger colour)
   if (has0 && d0.owned) contact_dual<T>(w, d0, self, alpha);
@@ -1347,6 +1396,7 @@ __device__ void solve_body_staged(const World &w, int4 rec, int lane, int G, uns
   int2 ent[kStageSlots];
   int cnt = nk < kStageSlots ? nk : kStageSlots;
   stage_chunk(w, cb, lane, G, 0, cnt, ent, stage, false);  // in flight while the body's own data loads
+  const float4 qt = ld(&w.b.quatT[i]);
   BState<T> self = load_state<T>(w, i);
   const int cStart = ld(&w.g.cStart[i]), cEnd = ld(&w.g.cStart[i + 1]);
   const int total = nm + (cEnd - cStart);
@@ -1363,7 +1413,7 @@ __device__ void solve_body_staged(const World &w, int4 rec, int lane, int G, uns
     stage_chunk(w, cb, lane, G, k0, cnt, ent, stage, false);
   }
   if (total > nm) constraints_primal<T>(w, nm, cStart, total, lane, G, self, alpha, s);
-  finish_body<T>(w, i, lane, G, mask, velocity, s, self);
+  finish_body<T>(w, i, lane, G, mask, velocity, qt, s, self);
   if (!dual) return;
   if (nk <= kStageSlots) {
     // every contact of this lane is still staged; the owner alone writes a
@@ -1507,7 +1557,8 @@ __global__ void __launch_bounds__(kSolveBlock, 3) wave_kernel(World w, int G) {
         __syncwarp(mask);  // orders every lane's reads after the acquires of the others
         if (ld(&w.b.flags[i]) & kBodyFp64) solve_body_f64(w, rec, lane, G, mask, alpha, dual, vel);
         else solve_body_staged(w, rec, lane, G, mask, (float)alpha, dual, vel, stage);
-        __threadfence();
+        // the warp barrier orders every lane's writes before lane 0's release,
+        // which makes them visible at gpu scope to whoever acquires the flag
         __syncwarp(mask);
         if (lane == 0) st_release(&w.b.progress[i], it + 1);
       }
