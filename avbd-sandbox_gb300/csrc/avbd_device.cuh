@@ -145,9 +145,11 @@ struct Springs {
 };
 
 // One hash-grid insertion: the body's exact broad-phase inputs travel with
-// it, so the sphere test needs no further loads. b2 = (body << 1) | dynamic.
+// it, so the sphere test needs no further loads. b2 = (body << 1) | dynamic;
+// loc = f32 offset of the centre from its cell's corner, w = radius (f32).
 struct __align__(16) Entry {
   double x, y, z, r;
+  float4 loc;
   int b2, cx, cy, cz;
 };
 constexpr int kPairScratch = 128;     // partner row of a step's broad phase
@@ -159,7 +161,9 @@ struct Grid {
   const double *invCell;     // per scene
   const int *largeStart;     // per scene CSR of large bodies
   const int *largeList;
-  int4 *cellLo, *cellHi;     // per body, w = scene
+  int4 *cellLo;              // per body: centre cell, w = scene
+  float4 *loc;               // per body: f32 offset from the cell corner, w = radius
+  const float *cellF;        // per scene: cell edge (f32 of 1 / invCell)
   unsigned tableMask;
   int *tableCount, *tableStart, *tableCursor;
   struct Entry *entries;

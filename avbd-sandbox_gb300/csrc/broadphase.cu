@@ -43,14 +43,41 @@ __device__ __forceinline__ uint32_t cell_hash(int x, int y, int z, int scene) {
 
 __device__ __forceinline__ bool is_large(const World &w, int i) { return (w.b.flags0[i] & kBodyLarge) != 0; }
 
+// The sphere test in f32 from cell indices and in-cell offsets:
+// d = (cA - cB) cell + (lA - lB), so the error does not grow with the
+// distance from the origin. Returns 1 when |d|^2 <= (rA + rB)^2 certainly
+// holds in f64, 0 when it certainly fails, -1 when the f64 test must decide.
+// Bound: per component |d_f32 - d| <= 3u (|dc| + 2) cell, giving
+// |d2_f32 - d2| <= 27u Q^2 and |r2_f32 - r2| <= 7u r2, Q = (max|dc| + 2) cell;
+// 64u (Q^2 + r2) covers both with a factor of two.
+__device__ __forceinline__ int sphere_f32(int4 ca, float4 la, int cx, int cy, int cz, float4 lb, float cell) {
+  if (ca.w < 0) return -1;
+  const float ex = (float)(ca.x - cx), ey = (float)(ca.y - cy), ez = (float)(ca.z - cz);
+  const float dx = ex * cell + (la.x - lb.x), dy = ey * cell + (la.y - lb.y), dz = ez * cell + (la.z - lb.z);
+  const float d2 = dx * dx + dy * dy + dz * dz;
+  const float rs = la.w + lb.w, r2 = rs * rs;
+  const float m = fmaxf(fabsf(ex), fmaxf(fabsf(ey), fabsf(ez))) + 2.0f;
+  const float E = (64.0f / 16777216.0f) * (m * m * cell * cell + r2);
+  if (!(d2 == d2) || !(E < 1e30f)) return -1;
+  if (d2 + E < r2) return 1;
+  if (d2 - E > r2) return 0;
+  return -1;
+}
+
 // The `visit` predicate of solver.js:316-329 for A = bodies[a], B = bodies[b], b < a.
 __device__ bool accept(const World &w, int a, int b) {
   const double ma = w.b.massD[a].x, mb = w.b.massD[b].x;
   if (!(ma > 0 || mb > 0)) return false;
-  const D4 pa = w.b.pos[a], pb = w.b.pos[b];
-  const double dx = pa.x - pb.x, dy = pa.y - pb.y, dz = pa.z - pb.z;
-  const double r = w.b.size[a].w + w.b.size[b].w;
-  if (!(dx * dx + dy * dy + dz * dz <= r * r)) return false;
+  const int4 cb = w.g.cellLo[b];
+  int t = -1;
+  if (cb.w >= 0) t = sphere_f32(w.g.cellLo[a], w.g.loc[a], cb.x, cb.y, cb.z, w.g.loc[b], w.g.cellF[cb.w]);
+  if (t == 0) return false;
+  if (t < 0) {
+    const D4 pa = w.b.pos[a], pb = w.b.pos[b];
+    const double dx = pa.x - pb.x, dy = pa.y - pb.y, dz = pa.z - pb.z;
+    const double r = w.b.size[a].w + w.b.size[b].w;
+    if (!(dx * dx + dy * dy + dz * dz <= r * r)) return false;
+  }
   // constrainedTo: a live joint or spring between them
   for (int k = w.g.cStart[a]; k < w.g.cStart[a + 1]; k++) {
     const uint32_t ref = w.g.cRef[k];
@@ -88,6 +115,12 @@ __global__ void cells_kernel(World w) {
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < w.b.n; i += gridDim.x * blockDim.x) {
     int4 c;
     const bool ok = centre_cell(w, i, c);
+    if (ok) {  // f32 offset from the cell corner (cell = 1 / invCell, as the f32 test's cell)
+      const double cell = 1.0 / w.g.invCell[c.w];
+      const D4 p = w.b.pos[i];
+      w.g.loc[i] = make_float4((float)(p.x - c.x * cell), (float)(p.y - c.y * cell), (float)(p.z - c.z * cell),
+                               (float)w.b.size[i].w);
+    }
     c.w = ok ? c.w : -1 - c.w;  // scene, negative when the body has no cell
     w.g.cellLo[i] = c;
     if (!ok || is_large(w, i)) continue;
@@ -104,6 +137,7 @@ __global__ void scatter_kernel(World w) {
       const D4 p = w.b.pos[i];
       Entry e;
       e.x = p.x; e.y = p.y; e.z = p.z; e.r = w.b.size[i].w;
+      e.loc = w.g.loc[i];
       e.b2 = (i << 1) | ((w.b.flags0[i] & kBodyDynamic) ? 1 : 0);
       e.cx = c.x; e.cy = c.y; e.cz = c.z;
       w.g.entries[at] = e;
@@ -165,6 +199,8 @@ __device__ void sort_segment(uint64_t *k, int n) {
 struct BodyA {
   int a, s;
   int4 c;
+  float4 loc;
+  float cell;
   double x, y, z, r;
   bool dyn;
 };
@@ -172,9 +208,13 @@ struct BodyA {
 // The `visit` predicate (solver.js:316-329) against a grid entry.
 __device__ __forceinline__ bool accept_entry(const World &w, const BodyA &A, const Entry &e) {
   if (!(A.dyn || (e.b2 & 1))) return false;
-  const double dx = A.x - e.x, dy = A.y - e.y, dz = A.z - e.z;
-  const double r = A.r + e.r;
-  if (!(dx * dx + dy * dy + dz * dz <= r * r)) return false;
+  const int t = sphere_f32(A.c, A.loc, e.cx, e.cy, e.cz, e.loc, A.cell);
+  if (t == 0) return false;
+  if (t < 0) {
+    const double dx = A.x - e.x, dy = A.y - e.y, dz = A.z - e.z;
+    const double r = A.r + e.r;
+    if (!(dx * dx + dy * dy + dz * dz <= r * r)) return false;
+  }
   return !w.g.hasConstraints || accept(w, A.a, e.b2 >> 1);
 }
 
@@ -222,6 +262,8 @@ __device__ BodyA body_a(const World &w, int a) {
   A.a = a;
   A.c = w.g.cellLo[a];
   A.s = A.c.w;
+  A.loc = w.g.loc[a];
+  A.cell = A.s >= 0 ? w.g.cellF[A.s] : 0.f;
   const D4 p = w.b.pos[a];
   A.x = p.x; A.y = p.y; A.z = p.z;
   A.r = w.b.size[a].w;
@@ -436,7 +478,7 @@ namespace {
 
 // Where the query's arrays sit in the scratch array, for n bodies.
 struct StaticLayout {
-  size_t pos, size, massD, flags0, scene, cStart, cellLo, entries, rows, pairCount, pairStart, largeList,
+  size_t pos, size, massD, flags0, scene, cStart, cellLo, loc, cellF, entries, rows, pairCount, pairStart, largeList,
       largeStart, sceneStart, invCell, tableCount, tableStart, tableCursor, ctl, temp, tempBytes, total;
   int tableSize;
 };
@@ -460,6 +502,8 @@ StaticLayout static_layout(int n) {
   L.scene = take(m * sizeof(int));
   L.cStart = take((m + 1) * sizeof(int));
   L.cellLo = take(m * sizeof(int4));
+  L.loc = take(m * sizeof(float4));
+  L.cellF = take(sizeof(float));
   L.entries = take(m * sizeof(Entry));
   L.rows = take(m * kStaticPairRow * sizeof(uint32_t));
   L.pairCount = take((m + 1) * sizeof(int));
@@ -565,10 +609,11 @@ __global__ void static_large_write_kernel(World w) {
   }
 }
 
-__global__ void static_scalars_kernel(int *sceneStart, double *invCell, int n, double inv) {
+__global__ void static_scalars_kernel(int *sceneStart, double *invCell, float *cellF, int n, double inv) {
   sceneStart[0] = 0;
   sceneStart[1] = n;
   invCell[0] = inv;
+  cellF[0] = (float)(1.0 / inv);
 }
 
 __global__ void static_finish_kernel(World w, int32_t *count) {
@@ -650,6 +695,8 @@ extern "C" int avbd_overlap_pairs_static(int32_t n, const double *pos, const dou
   w.g.largeStart = (const int *)(base + L.largeStart);
   w.g.largeList = (const int *)(base + L.largeList);
   w.g.cellLo = (int4 *)(base + L.cellLo);
+  w.g.loc = (float4 *)(base + L.loc);
+  w.g.cellF = (const float *)(base + L.cellF);
   w.g.tableMask = (unsigned)(L.tableSize - 1);
   w.g.tableCount = (int *)(base + L.tableCount);
   w.g.tableStart = (int *)(base + L.tableStart);
@@ -680,7 +727,7 @@ extern "C" int avbd_overlap_pairs_static(int32_t n, const double *pos, const dou
     // two scalars and the inverse cell: written by a one-thread kernel so the
     // call needs no host staging buffer
     static_scalars_kernel<<<1, 1, 0, st>>>((int *)(base + L.sceneStart), (double *)(base + L.invCell),
-                                           sceneStart[1], inv);
+                                           (float *)(base + L.cellF), sceneStart[1], inv);
     static_large_list_kernel<<<1, 1024, 0, st>>>(w, (int *)(base + L.largeList), (int *)(base + L.largeStart));
     cells_kernel<<<blocks, 256, 0, st>>>(w);
     size_t tb = L.tempBytes;

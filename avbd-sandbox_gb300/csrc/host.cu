@@ -644,11 +644,14 @@ int avbd_pack(avbd_ctx *ctx, const avbd_world *world) {
   D4 *sizeP, *massDP;
   float4 *massFP;
   double *fricP, *invCellP;
+  float *cellFP;
   int *flags0P, *sceneP, *sceneStartP, *largeStartP, *largeListP, *cStartP;
   uint32_t *prioP, *cRefP;
+  std::vector<float> cellF(S);
+  for (int s = 0; s < S; s++) cellF[s] = (float)(1.0 / invCell[s]);
   if ((rc = upload(ctx, &sizeP, size)) || (rc = upload(ctx, &massDP, massD)) || (rc = upload(ctx, &massFP, massF)) ||
       (rc = upload(ctx, &fricP, friction)) || (rc = upload(ctx, &flags0P, flags0)) || (rc = upload(ctx, &sceneP, scene)) ||
-      (rc = upload(ctx, &prioP, prio)) || (rc = upload(ctx, &invCellP, invCell)) ||
+      (rc = upload(ctx, &prioP, prio)) || (rc = upload(ctx, &invCellP, invCell)) || (rc = upload(ctx, &cellFP, cellF)) ||
       (rc = upload(ctx, &sceneStartP, sceneStart)) || (rc = upload(ctx, &largeStartP, largeStart)) ||
       (rc = upload(ctx, &largeListP, largeList)) || (rc = upload(ctx, &cStartP, cStart)) || (rc = upload(ctx, &cRefP, cRef)))
     return rc;
@@ -690,12 +693,12 @@ int avbd_pack(avbd_ctx *ctx, const avbd_world *world) {
   }
   // grid
   w.g.numScenes = S;
-  w.g.sceneStart = sceneStartP; w.g.invCell = invCellP; w.g.largeStart = largeStartP; w.g.largeList = largeListP;
+  w.g.sceneStart = sceneStartP; w.g.invCell = invCellP; w.g.cellF = cellFP; w.g.largeStart = largeStartP; w.g.largeList = largeListP;
   w.g.cStart = cStartP; w.g.cRef = cRefP;
   w.g.tableMask = (unsigned)(ctx->tableSize - 1);
   w.g.entryCap = ctx->entryCap;
   w.g.candCap = ctx->candCap;
-  if ((rc = dalloc(ctx, &w.g.cellLo, n)) || (rc = dalloc(ctx, &w.g.cellHi, n)) ||
+  if ((rc = dalloc(ctx, &w.g.cellLo, n)) || (rc = dalloc(ctx, &w.g.loc, n)) ||
       (rc = dalloc(ctx, &w.g.tableCount, ctx->tableSize)) || (rc = dalloc(ctx, &w.g.tableStart, ctx->tableSize)) ||
       (rc = dalloc(ctx, &w.g.tableCursor, ctx->tableSize)) || (rc = dalloc(ctx, &w.g.entries, ctx->entryCap)) ||
       (rc = dalloc(ctx, &w.g.pairCount, n + 1)) || (rc = dalloc(ctx, &w.g.pairStart, n + 1)) ||
