@@ -211,7 +211,11 @@ def batch_worlds(worlds):
 
 def cube_stack(n=10, seed=1, beta=10.0, gravity=-9.81):
     """Ten 1 m cubes (1000 kg/m^3, mu 0.5) stacked on the ground, each with a
-    seeded +-0.01 m xy jitter and +-2 degree yaw about z."""
+    seeded +-0.01 m xy jitter and +-2 degree yaw about z. `beta` is the
+    penalty ramp of both rows; None keeps the reference's own ramps (betaLin
+    1e4, betaAng 100, src/physics/solver.js:97-104). With beta = 10 the ramp
+    cannot stiffen the contacts of 1000 kg cubes within a step and the stack
+    sinks through the ground, in the reference engine as on the device."""
     s = Scene("cube_stack")
     add_ground(s, 0.5)
     rnd = LCG(seed)
@@ -221,7 +225,9 @@ def cube_stack(n=10, seed=1, beta=10.0, gravity=-9.81):
         yaw = math.radians(rnd.uniform(-2.0, 2.0))
         k = s.box((1.0, 1.0, 1.0), 1000.0, 0.5, (jx, jy, 0.5 + i * 1.0))
         s.set_orientation(k, (0.0, 0.0, 1.0), yaw)
-    s.params = dict(gravity=gravity, iterations=10, alpha=0.95, beta_lin=beta, beta_ang=beta)
+    s.params = dict(gravity=gravity, iterations=10, alpha=0.95)
+    if beta is not None:
+        s.params.update(beta_lin=beta, beta_ang=beta)
     s.meta = dict(steps=300)
     return s
 
@@ -295,9 +301,10 @@ def heavy_chain(links=50, end_mass=26000.0, springs=100, gravity=-9.81):
     E = 3.0
     end = s.box((E, E, E), end_mass / (E * E * E), 0.5, along(links * L + E / 2), quat=q)
     s.joint(prev, end, (0.0, 0.0, -L / 2), (0.0, 0.0, E / 2))
-    # spring chain at its analytic equilibrium (the fixture of test/fixtures.mjs:62-135)
+    # spring chain at its analytic equilibrium (the fixture of test/fixtures.mjs:62-135),
+    # 150 m away: beyond the reach of the swinging chain (radius 53 m)
     g = abs(gravity)
-    anchor = s.box((0.4, 0.4, 0.4), 0.0, 0.5, (40.0, 0.0, 150.0))
+    anchor = s.box((0.4, 0.4, 0.4), 0.0, 0.5, (150.0, 0.0, 150.0))
     prev = anchor
     z = 150.0
     size = 0.1
@@ -305,11 +312,11 @@ def heavy_chain(links=50, end_mass=26000.0, springs=100, gravity=-9.81):
         k = 1e3 if i % 2 == 0 else 1e6
         ext = g * (springs - i) * 1.0 / k
         z -= 1.0 + ext
-        b = s.box((size, size, size), 1.0 / (size * size * size), 0.5, (40.0, 0.0, z))
+        b = s.box((size, size, size), 1.0 / (size * size * size), 0.5, (150.0, 0.0, z))
         s.spring(prev, b, (0.0, 0.0, 0.0), (0.0, 0.0, 0.0), k, 1.0)
         prev = b
     s.params = dict(gravity=gravity, iterations=20)
-    s.meta = dict(steps=1000, end_body=end)
+    s.meta = dict(steps=1000, end_body=end, chain_bodies=(0, end + 1))
     return s
 
 

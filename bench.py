@@ -36,6 +36,8 @@ import subprocess
 import sys
 import time
 
+import numpy as np
+
 ROOT = os.path.dirname(os.path.abspath(__file__))
 for _p in (ROOT, os.path.join(ROOT, "oracle")):
     if _p not in sys.path:
@@ -345,6 +347,8 @@ def run_gpu(args):
     }
     if args.batched_steps > 0:
         out["batched"] = run_batched(abi, backend, args, flush)
+    if rank == 0 and not args.no_accuracy:
+        out["accuracy_vs_oracle"] = run_accuracy(abi, backend)
     if rank == 0 and snapshots:
         ref_params = params_for(abi, s, body_order=abi.ORDER_REFERENCE)
         out["cpu_baseline"] = cpu_baseline(ref_params, snapshots, budget_s=args.cpu_budget)
@@ -397,6 +401,73 @@ def run_batched(abi, backend, args, flush):
     }
 
 
+def run_accuracy(abi, backend):
+    """The small configurations against the f64 oracle over their whole runs,
+    both stepping the same start state (device colouring order replayed by
+    the oracle): the 10-cube stack for 300 steps and the heavy chain (26,000:1
+    end mass, hard joints) with the 1e3/1e6 spring chain for 1000 steps; the
+    worst position error of any dynamic body and of the chain's end mass.
+    Beside each, the oracle against itself from a start nudged by 1e-7 m (one
+    body, x): these scenes are unstable or chaotic over their full length, so
+    that divergence is the yardstick for the device's long-horizon error."""
+    from oracle import Oracle
+
+    sc = pkg().scene
+    out = {}
+    cases = (("cube_stack_300 (beta 10, as configured: sinks through the ground)", sc.cube_stack()),
+             ("cube_stack_300 (reference ramps betaLin 1e4, betaAng 100)", sc.cube_stack(beta=None)),
+             ("heavy_chain_1000 (50 hard links, 26,000 kg end mass, 1e3/1e6 spring chain)", sc.heavy_chain()))
+    for name, s in cases:
+        steps = s.meta["steps"]
+        params = abi.default_params(**s.params, body_order=abi.ORDER_PRIORITY)
+        w = s.world().round_to_device()
+        gpu = backend.GpuBackend(params)
+        gpu.pack(w)
+        o = Oracle(params, w)
+        dyn = w.mass > 0
+        wn = w.copy()
+        wn.pos[int(np.argmax(dyn)), 0] += 1e-7
+        on = Oracle(params, wn)
+        self_div, self_end = 0.0, 0.0
+        worst, worst_end, worst_chain, worst_springs = 0.0, 0.0, 0.0, 0.0
+        t0 = time.perf_counter()
+        for k in range(steps):
+            gpu.step(1)
+            o.step(1)
+            on.step(1)
+            if (k + 1) % 10 == 0 or k + 1 == steps:
+                g, r, rn = gpu.read_state(), o.state(), on.state()
+                err = np.abs(g.pos[dyn] - r.pos[dyn]).max()
+                worst = max(worst, float(err))
+                self_div = max(self_div, float(np.abs(rn.pos[dyn] - r.pos[dyn]).max()))
+                if "end_body" in s.meta:
+                    e = s.meta["end_body"]
+                    self_end = max(self_end, float(np.abs(rn.pos[e] - r.pos[e]).max()))
+                if "end_body" in s.meta:
+                    e = s.meta["end_body"]
+                    c0, c1 = s.meta["chain_bodies"]
+                    worst_end = max(worst_end, float(np.abs(g.pos[e] - r.pos[e]).max()))
+                    worst_chain = max(worst_chain, float(np.abs(g.pos[c0:c1] - r.pos[c0:c1]).max()))
+                    sp = np.arange(w.n_bodies) >= c1
+                    sp &= dyn
+                    worst_springs = max(worst_springs, float(np.abs(g.pos[sp] - r.pos[sp]).max()))
+        st = gpu.last_stats
+        rec = {"steps": steps, "bodies": w.n_bodies, "max_pos_error_m": worst, "fp64_bodies": st["fp64_bodies"],
+               "final_pos_error_m": float(np.abs(gpu.read_state().pos[dyn] - o.state().pos[dyn]).max()),
+               "wall_s": time.perf_counter() - t0}
+        if "end_body" in s.meta:
+            rec["end_mass_max_error_m"] = worst_end
+            rec["chain_max_error_m"] = worst_chain
+            rec["spring_chain_max_error_m"] = worst_springs
+        rec["max_travel_m"] = float(np.abs(o.state().pos[dyn] - w.pos[dyn]).max())
+        rec["oracle_vs_oracle_nudged_1e-7m_max_error_m"] = self_div
+        if "end_body" in s.meta:
+            rec["oracle_vs_oracle_nudged_end_mass_max_error_m"] = self_end
+        out[name] = rec
+        gpu.destroy()
+    return out
+
+
 def run_reference(args):
     """The reference's CPU engine algorithm (oracle restatement, index-order
     colouring as the reference's CPU solver), one host thread: the reference
@@ -446,6 +517,7 @@ def main():
     ap.add_argument("--cpu-budget", type=float, default=45.0)
     ap.add_argument("--ref-budget", type=float, default=120.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-accuracy", action="store_true", help="skip the small-scene accuracy runs")
     ap.add_argument("--batched-steps", type=int, default=240, help="steps of the 512-scene batch (0: skip)")
     ap.add_argument("--trace", default="", help="write each timed step's profile and counters (JSON lines)")
     args = ap.parse_args()
