@@ -46,7 +46,7 @@ class Params(C.Structure):
         ("rotated_inertia", C.c_int32), ("spring_stiffness_ramp", C.c_int32),
         ("spring_geometric_stiffness", C.c_int32), ("cached_contact_jacobians", C.c_int32),
         ("broadphase", C.c_int32), ("hash_threshold", C.c_int32),
-        ("body_order", C.c_int32), ("reserved0", C.c_int32),
+        ("body_order", C.c_int32), ("wait_limit", C.c_int32),
         ("fp64_ratio_threshold", C.c_double),
         ("max_pairs_per_body", C.c_int32), ("max_adjacency", C.c_int32),
         ("lanes_per_body", C.c_int32), ("blocks_per_sm", C.c_int32),

@@ -58,6 +58,7 @@ struct SolverParams {
   int rotatedInertia, springRamp, springGeometric, cachedJacobians;
   double fp64Ratio;
   int schedule;  // 0: colour phases + grid barrier, 1: dependency wavefront
+  long long barrierLimit, waitLimit;  // polls before a grid barrier / a neighbour wait gives up
 };
 
 // Device scalars shared by all kernels of a step.

@@ -411,7 +411,8 @@ int one_step(avbd_ctx *ctx) {
 int check_flags(avbd_ctx *ctx) {
   Control c{};
   CK(cudaMemcpy(&c, ctx->w.ctl, sizeof(Control), cudaMemcpyDeviceToHost));
-  if (c.flags & kOvfTimeout) return fail(ctx, AVBD_ERR_TIMEOUT, "a device grid barrier timed out");
+  if (c.flags & kOvfTimeout)
+    return fail(ctx, AVBD_ERR_TIMEOUT, "a device wait (grid barrier or neighbour progress) gave up; repack to continue");
   if (c.flags & (kOvfCells | kOvfPairs | kOvfAdj | kOvfColors)) {
     // grow the arenas that overflowed for the next pack; this state is invalid
     if (c.flags & kOvfPairs) ctx->params.max_pairs_per_body = std::max(ctx->params.max_pairs_per_body, 16) * 2;
@@ -639,7 +640,9 @@ int avbd_pack(avbd_ctx *ctx, const avbd_world *world) {
   w.p = SolverParams{P.dt, P.gravity, P.iterations, P.post_stabilize, P.beta_lin, P.beta_ang, P.alpha, P.gamma,
                      P.penalty_min, P.penalty_max, P.collision_margin, P.stick_threshold, P.rotated_inertia,
                      P.spring_stiffness_ramp, P.spring_geometric_stiffness, P.cached_contact_jacobians,
-                     P.fp64_ratio_threshold, P.schedule == 1 ? 1 : 0};
+                     P.fp64_ratio_threshold, P.schedule == 1 ? 1 : 0,
+                     P.wait_limit > 0 ? (long long)P.wait_limit : 20000000LL,
+                     P.wait_limit > 0 ? (long long)P.wait_limit : 4000000LL};
   int rc = 0;
   D4 *sizeP, *massDP;
   float4 *massFP;

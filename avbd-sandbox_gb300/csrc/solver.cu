@@ -36,14 +36,13 @@ constexpr int kSolveBlock = 128;   // threads of a solve block (3 blocks per SM)
 constexpr int kStageSlots = 4;     // contacts a lane stages in shared memory at a time
 constexpr int kStageVecs = 9;      // float4 per staged contact
 constexpr size_t kSolveSmem = (size_t)kSolveBlock * kStageSlots * kStageVecs * sizeof(float4);  // 73,728 B
-constexpr long long kSpinLimit = 20000000;  // ~1-2 s of polling at most
 
 // ---------------------------------------------------------------------------
 // Bounded grid barrier (all blocks are co-resident: cooperative launch).
 // Returns false when the wait gave up or another block reported a timeout;
 // the caller must then return.
 // ---------------------------------------------------------------------------
-__device__ bool grid_barrier(Control *ctl) {
+__device__ bool grid_barrier(Control *ctl, long long limit) {
   __shared__ int ok;
   __syncthreads();
   if (threadIdx.x == 0) {
@@ -59,7 +58,8 @@ __device__ bool grid_barrier(Control *ctl) {
     } else {
       long long spins = 0;
       while (*gen == g) {
-        if (++spins > kSpinLimit) {
+        // give up after `limit` polls, or at once when another block gave up
+        if (++spins > limit || (*((volatile unsigned *)&ctl->flags) & kOvfTimeout)) {
           atomicOr(&ctl->flags, kOvfTimeout);
           break;
         }
@@ -369,7 +369,7 @@ __global__ void __launch_bounds__(256) coloring_kernel(World w) {
   int round = 0;
   for (;; round++) {
     if (tid == 0) ctl->pad[1 + (round + 1) % 3] = 0;
-    if (!grid_barrier(ctl)) return;
+    if (!grid_barrier(ctl, w.p.barrierLimit)) return;
     int changed = 0;
     for (int i = tid; i < n; i += stride) {
       if (!(w.b.flags0[i] & kBodyDynamic)) continue;
@@ -397,7 +397,7 @@ __global__ void __launch_bounds__(256) coloring_kernel(World w) {
       }
     }
     if (changed) atomicOr(&ctl->pad[1 + round % 3], 1);
-    if (!grid_barrier(ctl)) return;
+    if (!grid_barrier(ctl, w.p.barrierLimit)) return;
     const int any = *((volatile int *)&ctl->pad[1 + round % 3]);
     if (!any) break;
     if (round > 4096) {
@@ -432,7 +432,7 @@ __global__ void __launch_bounds__(256) coloring_kernel(World w) {
   }
   __syncthreads();
   for (int c = threadIdx.x; c < kMaxColors; c += blockDim.x) w.a.blockHist[blockIdx.x * kMaxColors + c] = hist[c];
-  if (!grid_barrier(ctl)) return;
+  if (!grid_barrier(ctl, w.p.barrierLimit)) return;
   if (blockIdx.x == 0) {
     __shared__ int totals[kMaxColors];
     if (threadIdx.x < kMaxColors) {
@@ -457,7 +457,7 @@ __global__ void __launch_bounds__(256) coloring_kernel(World w) {
       ctl->numColors = used;
     }
   }
-  if (!grid_barrier(ctl)) return;
+  if (!grid_barrier(ctl, w.p.barrierLimit)) return;
   for (int c = threadIdx.x; c < kMaxColors; c += blockDim.x)
     base[c] = w.a.colorStart[c] + w.a.blockHist[blockIdx.x * kMaxColors + c];
   __syncthreads();
@@ -1466,7 +1466,7 @@ __global__ void __launch_bounds__(kSolveBlock, 3) solve_kernel(World w, int G) {
         if (ld(&w.b.flags[rec.x]) & kBodyFp64) solve_body_f64(w, rec, lane, G, mask, alpha, dual, vel);
         else solve_body_staged(w, rec, lane, G, mask, (float)alpha, dual, vel, stage);
       }
-      if (!grid_barrier(ctl)) return;
+      if (!grid_barrier(ctl, w.p.barrierLimit)) return;
     }
   }
 }
@@ -1489,7 +1489,6 @@ __device__ inline void st_release(int *p, int v) {
   asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
 }
 
-constexpr long long kWaitLimit = 4000000;  // polls per body, about a second
 
 // The neighbours come from the body's manifold list (one entry per touching
 // body, where the per-contact list has up to eight) and its joints/springs.
@@ -1518,7 +1517,7 @@ __device__ bool wait_neighbors(const World &w, int i, int it, int lane, int G, u
     const int oc = ld(&w.b.color[other]);
     const int need = oc < myColor ? it + 1 : it;
     while (ld_acquire(&w.b.progress[other]) < need) {
-      if (++polls > kWaitLimit || (*((volatile unsigned *)&w.ctl->flags) & kOvfTimeout)) {
+      if (++polls > w.p.waitLimit || (*((volatile unsigned *)&w.ctl->flags) & kOvfTimeout)) {
         atomicOr(&w.ctl->flags, kOvfTimeout);
         polls = -1;
         break;

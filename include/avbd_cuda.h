@@ -89,7 +89,10 @@ typedef struct avbd_params {
   int32_t hash_threshold;  /* oracle only: 150                              */
   int32_t body_order;      /* AVBD_ORDER_*; the CUDA backend always uses
                               AVBD_ORDER_PRIORITY                           */
-  int32_t reserved0;
+  /* Polls before a device wait (grid barrier, neighbour progress) gives up:
+     the kernel then returns and avbd_synchronize reports AVBD_ERR_TIMEOUT;
+     the context needs avbd_pack again. 0 = default (about a second). */
+  int32_t wait_limit;
   /* GPU precision policy. A body whose largest constraint stiffness divided
      by its inertial stiffness m/dt^2 exceeds this ratio is assembled and
      factored in FP64; everything else runs in FP32. <= 0 disables FP64.    */

@@ -23,6 +23,8 @@ def load(name):
     d = np.load(os.path.join(HERE, "golden", name + ".npz"))
     p = abi.Params()
     for field, ctype in p._fields_:
+        if "p_" + field not in d:  # a field added after the fixture was written keeps its zero default
+            continue
         v = d["p_" + field]
         setattr(p, field, float(v) if ctype in (abi.C.c_double, abi.C.c_float) else int(v))
     return p, abi.World.from_arrays(d, "in_"), abi.World.from_arrays(d, "out_"), d
