@@ -128,6 +128,12 @@ class Stats(C.Structure):
         return {k: getattr(self, k) for k, _ in self._fields_}
 
 
+class DeviceViews(C.Structure):
+    _fields_ = [("body_pos", C.c_void_p), ("body_quat", C.c_void_p), ("body_count", C.c_int32),
+                ("joint_state", C.c_void_p), ("joint_count", C.c_int32),
+                ("spring_state", C.c_void_p), ("spring_count", C.c_int32)]
+
+
 class Profile(C.Structure):
     _fields_ = [("broadphase_ms", C.c_double), ("narrowphase_ms", C.c_double),
                 ("prepare_ms", C.c_double), ("coloring_ms", C.c_double),

@@ -55,6 +55,12 @@ def load_library(path: str = LIB_PATH):
     L.avbd_last_error.restype = C.c_char_p
     L.avbd_overlap_pairs_static.argtypes = [C.c_int32, vp, vp, vp, C.c_double, vp, C.c_int64, vp, vp]
     L.avbd_overlap_pairs_static.restype = C.c_int
+    L.avbd_set_coloring.argtypes = [vp, vp]
+    L.avbd_set_coloring.restype = C.c_int
+    L.avbd_update_joint_anchor.argtypes = [vp, C.c_int32, vp]
+    L.avbd_update_joint_anchor.restype = C.c_int
+    L.avbd_device_views_get.argtypes = [vp, vp]
+    L.avbd_device_views_get.restype = C.c_int
     for name in ("avbd_create", "avbd_destroy", "avbd_pack", "avbd_step", "avbd_synchronize", "avbd_read_state",
                  "avbd_write_state", "avbd_read_coloring", "avbd_read_pairs", "avbd_read_stats",
                  "avbd_set_profiling", "avbd_read_profile", "avbd_kernel_launches"):
@@ -145,6 +151,29 @@ class GpuBackend:
         self._check(self.L.avbd_read_pairs(self.h, a.ctypes.data_as(C.c_void_p), b.ctypes.data_as(C.c_void_p),
                                            cnt.value, C.byref(cnt)))
         return a[:cnt.value], b[:cnt.value]
+
+    def set_coloring(self, color_of):
+        """uploadColoring / overrideColoring (backend.js:1925): colours to use
+        from the next step on; None returns to the device's own colouring."""
+        if color_of is None:
+            self._check(self.L.avbd_set_coloring(self.h, None))
+            return
+        c = np.ascontiguousarray(color_of, dtype=np.int32)
+        assert c.shape == (self.world.n_bodies,)
+        self._check(self.L.avbd_set_coloring(self.h, c.ctypes.data_as(C.c_void_p)))
+
+    def update_joint_anchor(self, joint: int, r_a):
+        """updateJointAnchor (backend.js:1970-1978): joint's anchor on body A
+        (a world point when the joint has no body A)."""
+        a = np.ascontiguousarray(r_a, dtype=np.float64)
+        self._check(self.L.avbd_update_joint_anchor(self.h, int(joint), a.ctypes.data_as(C.c_void_p)))
+
+    def device_views(self) -> dict:
+        """getConstraintGpuState (backend.js:1950-1967): device pointers of the
+        live body poses and joint/spring state."""
+        v = abi.DeviceViews()
+        self._check(self.L.avbd_device_views_get(self.h, C.byref(v)))
+        return {k: getattr(v, k) for k, _ in v._fields_}
 
     @property
     def last_stats(self) -> dict:

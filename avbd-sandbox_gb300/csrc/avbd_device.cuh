@@ -33,6 +33,7 @@ constexpr unsigned kOvfAdj = 0x4u;
 constexpr unsigned kOvfColors = 0x8u;
 constexpr unsigned kOvfTimeout = 0x10u;
 constexpr unsigned kErrNaN = 0x100u;
+constexpr unsigned kErrColoring = 0x200u;  // an uploaded colouring was not proper (AVBD_ERR_COLORING)
 
 // Body flag bits.
 constexpr int kBodyDynamic = 0x1;
@@ -75,6 +76,7 @@ struct Control {
   int adjTotal;
   int prevCandidates;  // candidates (= manifold slots) of the previous step
   int npCount[3];      // narrow-phase work lists: face, edge, exact
+  int colorBad;        // this step's uploaded colouring has a conflict
   int pad[5];
 };
 
@@ -197,6 +199,7 @@ struct Adjacency {
   int ccap;
   int *hpEntry;      // per body, within its manifold range: dynamic neighbours of higher colouring priority
   int *hpCount;      // n
+  const int *colorOverride;  // uploaded colours (avbd_set_coloring), or null
   int *colorStart;   // kMaxColors + 1
   int *colorBodies;  // dynamic bodies sorted by (colour, index)
   int4 *colorRec;    // per colour position: body, contact range begin, end, 0
@@ -359,6 +362,7 @@ cudaError_t launch_solve(const World &w, int lanesPerBody, int blocksPerSm, cuda
 int solve_max_blocks_per_sm(int lanesPerBody);
 void launch_commit(const World &w, cudaStream_t st, int smCount);
 void launch_stats(const World &w, double *out3, cudaStream_t st, int smCount);
+cudaError_t launch_joint_anchor(const World &w, int joint, double x, double y, double z, cudaStream_t st);
 // Error text of a context-free ABI call (read back by avbd_last_error(NULL)).
 int set_context_free_error(int code, const char *msg);
 

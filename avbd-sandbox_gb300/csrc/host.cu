@@ -64,6 +64,7 @@ struct avbd_ctx {
   int *hCand = nullptr;
   std::vector<void *> growable;  // arenas sized by the candidate capacity
   int64_t regrows = 0;
+  int *colorOverride = nullptr;  // device copy of an uploaded colouring (n)
   // The host runs at most kRunAhead steps ahead of the device, so the
   // candidate count the regrow check reads is at most that many steps old.
   static constexpr int kRunAhead = 4;
@@ -422,6 +423,14 @@ int check_flags(avbd_ctx *ctx) {
                 c.flags);
   }
   if (c.flags & kErrNaN) return fail(ctx, AVBD_ERR_NAN, "non-finite body state produced");
+  if (c.flags & kErrColoring) {  // reported once: the steps used their own colouring
+    c.flags &= ~kErrColoring;
+    CK(cudaMemcpy(&ctx->w.ctl->flags, &c.flags, sizeof(unsigned), cudaMemcpyHostToDevice));
+    return fail(ctx, AVBD_ERR_ARG,
+                "the uploaded colouring gives two neighbours one colour (or a colour >= %d) in this step's "
+                "constraint graph; those steps used the device's own colouring",
+                kMaxColors);
+  }
   return AVBD_OK;
 }
 
@@ -501,6 +510,8 @@ int avbd_pack(avbd_ctx *ctx, const avbd_world *world) {
     return fail(ctx, AVBD_ERR_ARG, "avbd_pack: bodies need count > 0 and size/mass/moment/radius/friction/pos");
   cudaStreamSynchronize(ctx->stream);
   free_all(ctx);
+  ctx->colorOverride = nullptr;
+  ctx->w.a.colorOverride = nullptr;
   ctx->n = n;
   ctx->nj = world->joints.count;
   ctx->ns = world->springs.count;
@@ -991,6 +1002,47 @@ int avbd_read_profile(avbd_ctx *ctx, avbd_profile *out) {
 int avbd_kernel_launches(avbd_ctx *ctx, int64_t *out) {
   if (!ctx || !out) return AVBD_ERR_ARG;
   *out = ctx->launches;
+  return AVBD_OK;
+}
+
+int avbd_set_coloring(avbd_ctx *ctx, const int32_t *color_of) {
+  if (!ctx) return AVBD_ERR_ARG;
+  if (!ctx->packed) return fail(ctx, AVBD_ERR_STATE, "avbd_set_coloring before avbd_pack");
+  CK(cudaStreamSynchronize(ctx->stream));
+  if (!color_of) {
+    ctx->w.a.colorOverride = nullptr;
+    return AVBD_OK;
+  }
+  if (!ctx->colorOverride) {
+    int rc = dalloc(ctx, &ctx->colorOverride, ctx->n);
+    if (rc) return rc;
+  }
+  CK(cudaMemcpy(ctx->colorOverride, color_of, sizeof(int32_t) * ctx->n, cudaMemcpyHostToDevice));
+  ctx->w.a.colorOverride = ctx->colorOverride;
+  return AVBD_OK;
+}
+
+int avbd_update_joint_anchor(avbd_ctx *ctx, int32_t joint, const double r_a[3]) {
+  if (!ctx || !r_a) return AVBD_ERR_ARG;
+  if (!ctx->packed) return fail(ctx, AVBD_ERR_STATE, "avbd_update_joint_anchor before avbd_pack");
+  if (joint < 0 || joint >= ctx->nj) return fail(ctx, AVBD_ERR_ARG, "joint %d out of range (%d joints)", joint, ctx->nj);
+  if (!std::isfinite(r_a[0]) || !std::isfinite(r_a[1]) || !std::isfinite(r_a[2]))
+    return fail(ctx, AVBD_ERR_NAN, "joint %d: non-finite anchor", joint);
+  CK(launch_joint_anchor(ctx->w, joint, r_a[0], r_a[1], r_a[2], ctx->stream));
+  ctx->launches += 1;
+  return AVBD_OK;
+}
+
+int avbd_device_views_get(avbd_ctx *ctx, avbd_device_views *out) {
+  if (!ctx || !out) return AVBD_ERR_ARG;
+  if (!ctx->packed) return fail(ctx, AVBD_ERR_STATE, "avbd_device_views_get before avbd_pack");
+  out->body_pos = reinterpret_cast<const double *>(ctx->w.b.pos);
+  out->body_quat = reinterpret_cast<const float *>(ctx->w.b.quat);
+  out->body_count = ctx->n;
+  out->joint_state = ctx->w.j.state;
+  out->joint_count = ctx->nj;
+  out->spring_state = ctx->w.s.state;
+  out->spring_count = ctx->ns;
   return AVBD_OK;
 }
 

@@ -357,8 +357,34 @@ __global__ void __launch_bounds__(256) coloring_kernel(World w) {
   const int n = w.b.n;
   const int tid = blockIdx.x * blockDim.x + threadIdx.x, stride = gridDim.x * blockDim.x;
   volatile int *color = w.b.color;
+  // an uploaded colouring: taken when it is proper for this step's graph
+  bool useUploaded = false;
+  if (w.a.colorOverride) {
+    if (tid == 0) ctl->colorBad = 0;
+    for (int i = tid; i < n; i += stride)
+      color[i] = (w.b.flags0[i] & kBodyDynamic) ? w.a.colorOverride[i] : -1;
+    if (!grid_barrier(ctl, w.p.barrierLimit)) return;
+    int bad = 0;
+    for (int i = tid; i < n && !bad; i += stride) {
+      if (!(w.b.flags0[i] & kBodyDynamic)) continue;
+      const int ci = color[i];
+      if (ci < 0 || ci >= kMaxColors) {
+        bad = 1;
+        break;
+      }
+      // a conflicting edge is in the higher-priority list of one of its ends
+      const int hb = w.a.start[i], hc = w.a.hpCount[i];
+      for (int k = 0; k < hc && !bad; k++) bad = color[w.a.hpEntry[hb + k]] == ci;
+      if (w.g.hasConstraints)
+        constraint_neighbors(w, i, [&](int j) { bad |= color[j] == ci ? 1 : 0; });
+    }
+    if (bad) atomicOr(&ctl->colorBad, 1);
+    if (!grid_barrier(ctl, w.p.barrierLimit)) return;
+    useUploaded = *((volatile int *)&ctl->colorBad) == 0;
+    if (!useUploaded && tid == 0) atomicOr(&ctl->flags, kErrColoring);
+  }
   // seed: previous colours (statics -1, new dynamic bodies 0)
-  for (int i = tid; i < n; i += stride) {
+  for (int i = tid; i < n && !useUploaded; i += stride) {
     if (!(w.b.flags0[i] & kBodyDynamic)) color[i] = -1;
     else if (color[i] < 0 || color[i] >= kMaxColors) color[i] = 0;
   }
@@ -367,7 +393,7 @@ __global__ void __launch_bounds__(256) coloring_kernel(World w) {
   // read in round r - 2, before the barriers of round r - 1).
   if (tid == 0) ctl->pad[1] = 0;
   int round = 0;
-  for (;; round++) {
+  for (; !useUploaded; round++) {
     if (tid == 0) ctl->pad[1 + (round + 1) % 3] = 0;
     if (!grid_barrier(ctl, w.p.barrierLimit)) return;
     int changed = 0;
@@ -1659,6 +1685,17 @@ cudaError_t launch_coloring(const World &w, cudaStream_t st, int smCount) {
   void *args[] = {&arg};
   return cudaLaunchCooperativeKernel((void *)coloring_kernel, dim3(coloring_blocks(smCount)), dim3(256), args, 0,
                                      st);
+}
+
+// A joint's anchor on body A, set between steps (avbd_update_joint_anchor).
+static __global__ void joint_anchor_kernel(World w, int j, double x, double y, double z) {
+  const_cast<D4 *>(w.j.rAD)[j] = mkd4(x, y, z, 0.0);
+  const_cast<float4 *>(w.j.rAF)[j] = make_float4((float)x, (float)y, (float)z, 0.f);
+}
+
+cudaError_t launch_joint_anchor(const World &w, int joint, double x, double y, double z, cudaStream_t st) {
+  joint_anchor_kernel<<<1, 1, 0, st>>>(w, joint, x, y, z);
+  return cudaGetLastError();
 }
 
 int solve_max_blocks_per_sm(int lanesPerBody) {

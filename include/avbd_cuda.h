@@ -59,6 +59,7 @@ extern "C" {
 #define AVBD_OVF_ADJ 0x4u        /* per-body constraint adjacency            */
 #define AVBD_OVF_COLORS 0x8u     /* more than AVBD_MAX_COLORS colours        */
 #define AVBD_OVF_TIMEOUT 0x10u   /* bounded grid barrier gave up             */
+#define AVBD_ERR_COLORING 0x200u /* an uploaded colouring was not proper     */
 
 #define AVBD_MAX_CONTACTS 8 /* contacts per manifold (src/physics/collide.js:22) */
 #define AVBD_MAX_COLORS 64  /* colours the device colouring can encode       */
@@ -277,6 +278,37 @@ int avbd_write_state(avbd_ctx *ctx, const avbd_world *world);
 /* Replaces `readColoring()` (src/physics/gpu/backend.js:2053): colour of every
    body in the last step (-1 for static bodies) and the number of colours. */
 int avbd_read_coloring(avbd_ctx *ctx, int32_t *color_of, int32_t *num_colors);
+
+/* Replaces `uploadColoring(entries, offsets, counts)` + `overrideColoring`
+   (src/physics/gpu/backend.js:1925, 256-299): the colour of every body
+   (n int32, -1 or any value for static bodies) to use instead of the
+   device's priority colouring, from the next avbd_step on, until cleared
+   with color_of = NULL. Each step checks it against that step's constraint
+   graph; where two dynamic neighbours share a colour (or a colour is not
+   below AVBD_MAX_COLORS) the step uses its own colouring and
+   avbd_synchronize reports AVBD_ERR_ARG. Copied at the call. */
+int avbd_set_coloring(avbd_ctx *ctx, const int32_t *color_of);
+
+/* Replaces `updateJointAnchor(joint)` (src/physics/gpu/backend.js:1970-1978):
+   set joint `joint`'s anchor on body A (its world point when the joint has no
+   body A, as a drag joint) for the following steps, without a repack.
+   Ordered on the context's stream after the steps already queued. */
+int avbd_update_joint_anchor(avbd_ctx *ctx, int32_t joint, const double r_a[3]);
+
+/* Replaces `getConstraintGpuState()` (src/physics/gpu/backend.js:1950-1967):
+   where a renderer or another CUDA consumer on the same device finds the
+   live state, without a copy. Valid until the next avbd_pack or
+   avbd_destroy; read after avbd_synchronize (the stream's steps write them). */
+typedef struct avbd_device_views {
+  const double *body_pos;      /* x, y, z, unused: 4 doubles per body (x_t)   */
+  const float *body_quat;      /* x, y, z, w: 4 floats per body               */
+  int32_t body_count;
+  const int32_t *joint_state;  /* per joint: bit 0 = broken                   */
+  int32_t joint_count;
+  const int32_t *spring_state; /* per spring: bit 0 = broken                  */
+  int32_t spring_count;
+} avbd_device_views;
+int avbd_device_views_get(avbd_ctx *ctx, avbd_device_views *out);
 
 /* Candidate pairs of the last broad phase (body A index, body B index), pair
    order; `count` returns the total, at most `capacity` written. */
