@@ -65,6 +65,23 @@ def params_for(abi, s, **kw):
     return abi.default_params(**s.params, **kw)
 
 
+def slowest_rank(seconds: float, ws: int, device: str = "cuda") -> float:
+    """Replicas only: every rank steps its own copy of the workload, and the
+    job's time is the slowest rank's (all_reduce MAX; no collective when ws = 1)."""
+    if ws <= 1:
+        return seconds
+    import torch
+
+    t = torch.tensor([seconds], dtype=torch.float64, device=device)
+    torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
+    return float(t.item())
+
+
+def replica_rate(steps: int, ws: int, slowest_seconds: float) -> float:
+    """Whole-job steps/s: all ranks' steps over the slowest rank's time (weak scaling)."""
+    return ws * steps / slowest_seconds
+
+
 def dist_env():
     ws = int(os.environ.get("WORLD_SIZE", "1"))
     rank = int(os.environ.get("RANK", "0"))
@@ -267,11 +284,7 @@ def run_gpu(args):
     torch.cuda.synchronize()
     wall = time.perf_counter() - t0
     launches = gpu.kernel_launches - launches0
-    dev_s = sum(step_ms) / 1e3
-    if ws > 1:
-        t = torch.tensor([dev_s], dtype=torch.float64, device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        dev_s = float(t.item())
+    dev_s = slowest_rank(sum(step_ms) / 1e3, ws)
     gpu.set_profiling(False)
 
     # end to end through the C ABI with host buffers, over the same K steps:
@@ -291,10 +304,7 @@ def run_gpu(args):
         e2e_s += time.perf_counter() - t1
         if i + 1 in snap_at:
             snapshots.append((i + 1, gpu.read_state(manifolds=True)))
-    if ws > 1:
-        t = torch.tensor([e2e_s], dtype=torch.float64, device="cuda")
-        torch.distributed.all_reduce(t, op=torch.distributed.ReduceOp.MAX)
-        e2e_s = float(t.item())
+    e2e_s = slowest_rank(e2e_s, ws)
     snapshots.sort(key=lambda x: snap_at.index(x[0]))
     n = world.n_bodies
     per_body = 32 + 4 * 16  # f64 position (D4) + quaternion, velocity, angular velocity, previous velocity (float4)
@@ -309,7 +319,7 @@ def run_gpu(args):
     peak, peak_src = read_peaks()
     achieved = algo / (phases[dom] / 1e3) / 1e9
     traffic = read_traffic(kname, algo)
-    value = ws * K / dev_s
+    value = replica_rate(K, ws, dev_s)
     clocks = clk.summary()
     other = "narrowphase" if kind == "solve" else "solve"
     oms = phases["narrowphase_ms" if kind == "solve" else "solve_ms"]
@@ -334,7 +344,7 @@ def run_gpu(args):
                      "algorithmic_bytes_per_launch": algo, "launch_ms": phases[dom],
                      "other": {"kernel": other, "achieved": algo_tot[other] / K / (oms / 1e3) / 1e9,
                                "frac": algo_tot[other] / K / (oms / 1e3) / 1e9 / peak, "launch_ms": oms}},
-        "e2e": {"value": ws * K / e2e_s, "unit": UNIT, "h2d_bytes_per_step": n * per_body,
+        "e2e": {"value": replica_rate(K, ws, e2e_s), "unit": UNIT, "h2d_bytes_per_step": n * per_body,
                 "d2h_bytes_per_step": n * per_body,
                 "how": "avbd_write_state + avbd_step(1) + avbd_read_state every step over the same run, pinned "
                        "staging, host f64 arrays"},
