@@ -156,6 +156,7 @@ struct __align__(16) Entry {
   int b2, cx, cy, cz;
 };
 constexpr int kPairScratch = 128;     // partner row of a step's broad phase
+constexpr int kLargeChunk = 1024;     // bodies a block tests against one large body
 constexpr int kStaticPairRow = 64;    // partner row of the allocation-free query
 
 struct Grid {
@@ -164,6 +165,8 @@ struct Grid {
   const double *invCell;     // per scene
   const int *largeStart;     // per scene CSR of large bodies
   const int *largeList;
+  int *largeChunk;           // per large body, maxChunks counts / offsets of its partner chunks
+  int maxChunks;             // partner chunks of kLargeChunk bodies per large body
   int4 *cellLo;              // per body: centre cell, w = scene
   float4 *loc;               // per body: f32 offset from the cell corner, w = radius
   const float *cellF;        // per scene: cell edge (f32 of 1 / invCell)

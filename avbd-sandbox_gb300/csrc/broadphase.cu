@@ -161,26 +161,40 @@ __device__ void prev_range(const World &w, int a, int prevCount, int &first, int
   while (last < prevCount && (int)(w.prev.key[last] >> 32) == a) last++;
 }
 
-// One block per large body: every body b < a of its scene is tested.
-__global__ void large_count_kernel(World w, int numLarge) {
-  const int prevCount = w.ctl->prevCandidates;
-  for (int li = blockIdx.x; li < numLarge; li += gridDim.x) {
-    const int a = w.g.largeList[li];
-    const int s = w.b.scene[a];
-    int c = 0;
-    for (int b = w.g.sceneStart[s] + threadIdx.x; b < a; b += blockDim.x) c += accept(w, a, b) ? 1 : 0;
-    typedef cub::BlockReduce<int, 256> R;
-    __shared__ typename R::TempStorage tmp;
-    int total = R(tmp).Sum(c);
-    if (threadIdx.x == 0) {
-      int first, last;
-      prev_range(w, a, prevCount, first, last);
-      for (int m = first; m < last; m++)
-        if (w.prev.count[m] > 0 && !accept(w, a, (int)(w.prev.key[m] & 0xffffffffu))) total++;
-      w.g.pairCount[a] = total;
-    }
-    __syncthreads();
+// Large bodies: every body b < a of the scene is tested, in chunks of
+// kLargeChunk bodies, one block per (large body, chunk).
+// 1. the accepted count of each chunk
+__global__ void __launch_bounds__(256) large_count_kernel(World w) {
+  const int li = blockIdx.y, ch = blockIdx.x;
+  const int a = w.g.largeList[li];
+  const int s0 = w.g.sceneStart[w.b.scene[a]];
+  const int b0 = s0 + ch * kLargeChunk, b1 = min(a, b0 + kLargeChunk);
+  int c = 0;
+  for (int b = b0 + threadIdx.x; b < b1; b += blockDim.x) c += accept(w, a, b) ? 1 : 0;
+  typedef cub::BlockReduce<int, 256> R;
+  __shared__ typename R::TempStorage tmp;
+  const int total = R(tmp).Sum(c);
+  if (threadIdx.x == 0) w.g.largeChunk[li * w.g.maxChunks + ch] = b0 < b1 ? total : 0;
+}
+
+// 2. per large body: chunk counts -> chunk offsets, plus the old manifolds the
+//    sphere test rejects (they stay candidates); the body's partner count
+__global__ void large_total_kernel(World w) {
+  const int li = blockIdx.x;
+  if (threadIdx.x != 0) return;
+  const int a = w.g.largeList[li];
+  int *cnt = w.g.largeChunk + li * w.g.maxChunks;
+  int run = 0;
+  for (int ch = 0; ch < w.g.maxChunks; ch++) {
+    const int v = cnt[ch];
+    cnt[ch] = run;
+    run += v;
   }
+  int first, last;
+  prev_range(w, a, w.ctl->prevCandidates, first, last);
+  for (int m = first; m < last; m++)
+    if (w.prev.count[m] > 0 && !accept(w, a, (int)(w.prev.key[m] & 0xffffffffu))) run++;
+  w.g.pairCount[a] = run;
 }
 
 __device__ void sort_segment(uint64_t *k, int n) {
@@ -356,53 +370,60 @@ __global__ void __launch_bounds__(256) copy_kernel(World w) {
   }
 }
 
-__global__ void large_write_kernel(World w, int numLarge) {
-  const int prevCount = w.ctl->prevCandidates;
-  const int cap = w.g.candCap;
+// 3. each chunk writes its accepted partners at its offset, in index order
+__global__ void __launch_bounds__(256) large_write_kernel(World w) {
+  const int li = blockIdx.y, ch = blockIdx.x;
+  const int a = w.g.largeList[li];
+  const int s0 = w.g.sceneStart[w.b.scene[a]];
+  const int b0 = s0 + ch * kLargeChunk, b1 = min(a, b0 + kLargeChunk);
+  if (b0 >= b1) return;
+  const int beg = w.g.pairStart[a];
+  const int n = w.g.pairStart[a + 1] - beg;
+  if ((long long)beg + n > w.g.candCap) {
+    if (threadIdx.x == 0) atomicOr(&w.ctl->flags, kOvfPairs);
+    return;
+  }
+  uint64_t *seg = w.g.candKey + beg;
+  const uint64_t hiKey = (uint64_t)(uint32_t)a << 32;
   typedef cub::BlockScan<int, 256> S;
   __shared__ typename S::TempStorage tmp;
   __shared__ int base;
-  for (int li = blockIdx.x; li < numLarge; li += gridDim.x) {
-    const int a = w.g.largeList[li];
-    const int s = w.b.scene[a];
-    const int beg = w.g.pairStart[a];
-    const int n = w.g.pairStart[a + 1] - beg;
-    if (beg + n > cap) {
-      if (threadIdx.x == 0) atomicOr(&w.ctl->flags, kOvfPairs);
-      continue;
-    }
-    uint64_t *seg = w.g.candKey + beg;
-    const uint64_t hiKey = (uint64_t)(uint32_t)a << 32;
-    if (threadIdx.x == 0) base = 0;
+  if (threadIdx.x == 0) base = w.g.largeChunk[li * w.g.maxChunks + ch];
+  __syncthreads();
+  for (int t0 = b0; t0 < b1; t0 += blockDim.x) {
+    const int b = t0 + threadIdx.x;
+    const int ok = (b < b1 && accept(w, a, b)) ? 1 : 0;
+    int at, tot;
+    S(tmp).ExclusiveSum(ok, at, tot);
+    if (ok && base + at < n) seg[base + at] = hiKey | (uint32_t)b;
     __syncthreads();
-    const int s0 = w.g.sceneStart[s];
-    for (int b0 = s0; b0 < a; b0 += blockDim.x) {
-      const int b = b0 + threadIdx.x;
-      const int ok = (b < a && accept(w, a, b)) ? 1 : 0;
-      int pos, tot;
-      S(tmp).ExclusiveSum(ok, pos, tot);
-      if (ok && base + pos < n) seg[base + pos] = hiKey | (uint32_t)b;
-      __syncthreads();
-      if (threadIdx.x == 0) base += tot;
-      __syncthreads();
-    }
-    if (threadIdx.x == 0) {
-      int c = base;
-      int first, last;
-      prev_range(w, a, prevCount, first, last);
-      bool extra = false;
-      for (int m = first; m < last; m++) {
-        const int b = (int)(w.prev.key[m] & 0xffffffffu);
-        if (w.prev.count[m] > 0 && !accept(w, a, b)) {
-          if (c < n) seg[c] = hiKey | (uint32_t)b;
-          c++;
-          extra = true;
-        }
-      }
-      if (extra) sort_segment(seg, n);
-    }
+    if (threadIdx.x == 0) base += tot;
     __syncthreads();
   }
+}
+
+// 4. the old manifolds the sphere test rejected, appended, and the segment
+//    sorted when there are any (rare: a large body's sphere holds its scene)
+__global__ void large_extra_kernel(World w) {
+  const int li = blockIdx.x;
+  if (threadIdx.x != 0) return;
+  const int a = w.g.largeList[li];
+  const int beg = w.g.pairStart[a];
+  const int n = w.g.pairStart[a + 1] - beg;
+  if ((long long)beg + n > w.g.candCap) return;
+  uint64_t *seg = w.g.candKey + beg;
+  const uint64_t hiKey = (uint64_t)(uint32_t)a << 32;
+  int first, last;
+  prev_range(w, a, w.ctl->prevCandidates, first, last);
+  int c = n;
+  for (int m = last - 1; m >= first; m--)  // count the extras to find where they start
+    if (w.prev.count[m] > 0 && !accept(w, a, (int)(w.prev.key[m] & 0xffffffffu))) c--;
+  if (c == n) return;
+  for (int m = first; m < last; m++) {
+    const int b = (int)(w.prev.key[m] & 0xffffffffu);
+    if (w.prev.count[m] > 0 && !accept(w, a, b)) seg[c++] = hiKey | (uint32_t)b;
+  }
+  sort_segment(seg, n);
 }
 
 __global__ void finish_kernel(World w) {
@@ -454,11 +475,17 @@ void launch_broadphase_impl(const World &w, int numLarge, void *temp, size_t tem
   cudaMemsetAsync(w.g.pairCount + n, 0, sizeof(int), st);
   const int warpBlocks = (int)std::min<long long>(((long long)n + 7) / 8, (long long)smCount * 32);
   pairs_kernel<kPairScratch><<<warpBlocks, 256, 0, st>>>(w);
-  if (numLarge > 0) large_count_kernel<<<numLarge < 1024 ? numLarge : 1024, 256, 0, st>>>(w, numLarge);
+  if (numLarge > 0) {
+    large_count_kernel<<<dim3(w.g.maxChunks, numLarge), 256, 0, st>>>(w);
+    large_total_kernel<<<numLarge, 32, 0, st>>>(w);
+  }
   tb = tempBytes;
   cub::DeviceScan::ExclusiveSum(temp, tb, w.g.pairCount, w.g.pairStart, n + 1, st);
   copy_kernel<kPairScratch><<<warpBlocks, 256, 0, st>>>(w);
-  if (numLarge > 0) large_write_kernel<<<numLarge < 1024 ? numLarge : 1024, 256, 0, st>>>(w, numLarge);
+  if (numLarge > 0) {
+    large_write_kernel<<<dim3(w.g.maxChunks, numLarge), 256, 0, st>>>(w);
+    large_extra_kernel<<<numLarge, 32, 0, st>>>(w);
+  }
   finish_kernel<<<1, 1, 0, st>>>(w);
   prev_index_kernel<<<blocks, 256, 0, st>>>(w);
 }

@@ -358,7 +358,7 @@ int one_step(avbd_ctx *ctx) {
   int rc;
   if ((rc = record(ctx, 0))) return rc;
   launch_broadphase_impl(w, ctx->numLarge, ctx->bpTemp, ctx->bpTempBytes, st, ctx->smCount);
-  ctx->launches += 6 + (ctx->numLarge > 0 ? 2 : 0);  // own kernels (the two scans are library code)
+  ctx->launches += 6 + (ctx->numLarge > 0 ? 4 : 0);  // own kernels (the two scans are library code)
   if ((rc = record(ctx, 1))) return rc;
   launch_narrowphase(w, st, ctx->smCount);
   ctx->launches += 4;
@@ -367,7 +367,7 @@ int one_step(avbd_ctx *ctx) {
   ctx->launches += 5;
   if ((rc = record(ctx, 3))) return rc;
   CK(launch_coloring(w, st, ctx->smCount));
-  ctx->launches += 1;
+  ctx->launches += 1 + (w.a.colorOverride ? 2 : 0);
   if ((rc = record(ctx, 4))) return rc;
   CK(launch_solve(w, ctx->lanes, ctx->blocksPerSm, st, ctx->smCount));
   ctx->launches += 1;
@@ -587,6 +587,12 @@ int avbd_pack(avbd_ctx *ctx, const avbd_world *world) {
   }
   largeStart[S] = (int)largeList.size();
   ctx->numLarge = (int)largeList.size();
+  int maxChunks = 1;
+  for (int li = 0; li < ctx->numLarge; li++) {
+    const int a = largeList[li];
+    const int lower = a - sceneStart[scene[a]];
+    maxChunks = std::max(maxChunks, (lower + kLargeChunk - 1) / kLargeChunk);
+  }
 
   // joints / springs
   const avbd_joint_soa &J = world->joints;
@@ -708,6 +714,8 @@ int avbd_pack(avbd_ctx *ctx, const avbd_world *world) {
   // grid
   w.g.numScenes = S;
   w.g.sceneStart = sceneStartP; w.g.invCell = invCellP; w.g.cellF = cellFP; w.g.largeStart = largeStartP; w.g.largeList = largeListP;
+  w.g.maxChunks = maxChunks;
+  if ((rc = dalloc(ctx, &w.g.largeChunk, (size_t)std::max(ctx->numLarge, 1) * maxChunks))) return rc;
   w.g.cStart = cStartP; w.g.cRef = cRefP;
   w.g.tableMask = (unsigned)(ctx->tableSize - 1);
   w.g.entryCap = ctx->entryCap;

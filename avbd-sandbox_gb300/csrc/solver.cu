@@ -352,85 +352,13 @@ __device__ inline void constraint_neighbors(const World &w, int i, F &&f) {
   }
 }
 
-__global__ void __launch_bounds__(256) coloring_kernel(World w) {
+// The tail of the colouring: owner bits of the contact entries and the
+// stable counting sort by colour (cooperative: grid barriers inside).
+__device__ void coloring_finish(const World &w) {
   Control *ctl = w.ctl;
   const int n = w.b.n;
   const int tid = blockIdx.x * blockDim.x + threadIdx.x, stride = gridDim.x * blockDim.x;
   volatile int *color = w.b.color;
-  // an uploaded colouring: taken when it is proper for this step's graph
-  bool useUploaded = false;
-  if (w.a.colorOverride) {
-    if (tid == 0) ctl->colorBad = 0;
-    for (int i = tid; i < n; i += stride)
-      color[i] = (w.b.flags0[i] & kBodyDynamic) ? w.a.colorOverride[i] : -1;
-    if (!grid_barrier(ctl, w.p.barrierLimit)) return;
-    int bad = 0;
-    for (int i = tid; i < n && !bad; i += stride) {
-      if (!(w.b.flags0[i] & kBodyDynamic)) continue;
-      const int ci = color[i];
-      if (ci < 0 || ci >= kMaxColors) {
-        bad = 1;
-        break;
-      }
-      // a conflicting edge is in the higher-priority list of one of its ends
-      const int hb = w.a.start[i], hc = w.a.hpCount[i];
-      for (int k = 0; k < hc && !bad; k++) bad = color[w.a.hpEntry[hb + k]] == ci;
-      if (w.g.hasConstraints)
-        constraint_neighbors(w, i, [&](int j) { bad |= color[j] == ci ? 1 : 0; });
-    }
-    if (bad) atomicOr(&ctl->colorBad, 1);
-    if (!grid_barrier(ctl, w.p.barrierLimit)) return;
-    useUploaded = *((volatile int *)&ctl->colorBad) == 0;
-    if (!useUploaded && tid == 0) atomicOr(&ctl->flags, kErrColoring);
-  }
-  // seed: previous colours (statics -1, new dynamic bodies 0)
-  for (int i = tid; i < n && !useUploaded; i += stride) {
-    if (!(w.b.flags0[i] & kBodyDynamic)) color[i] = -1;
-    else if (color[i] < 0 || color[i] >= kMaxColors) color[i] = 0;
-  }
-  // "changed" flags, triple-buffered: round r sets flag r % 3 and clears the
-  // flag of round r + 1, which no block can still be reading (it was last
-  // read in round r - 2, before the barriers of round r - 1).
-  if (tid == 0) ctl->pad[1] = 0;
-  int round = 0;
-  for (; !useUploaded; round++) {
-    if (tid == 0) ctl->pad[1 + (round + 1) % 3] = 0;
-    if (!grid_barrier(ctl, w.p.barrierLimit)) return;
-    int changed = 0;
-    for (int i = tid; i < n; i += stride) {
-      if (!(w.b.flags0[i] & kBodyDynamic)) continue;
-      unsigned long long used = 0ull;
-      const int hb = w.a.start[i], hc = w.a.hpCount[i];
-      for (int k = 0; k < hc; k++) {
-        const int c = color[w.a.hpEntry[hb + k]];
-        if (c >= 0 && c < kMaxColors) used |= 1ull << c;
-      }
-      if (w.g.hasConstraints)
-        constraint_neighbors(w, i, [&](int j) {
-          if (precedes(w, j, i)) {
-            const int c = color[j];
-            if (c >= 0 && c < kMaxColors) used |= 1ull << c;
-          }
-        });
-      int c = __ffsll((long long)~used) - 1;
-      if (c < 0) {
-        c = kMaxColors - 1;
-        atomicOr(&ctl->flags, kOvfColors);
-      }
-      if (c != color[i]) {
-        color[i] = c;
-        changed = 1;
-      }
-    }
-    if (changed) atomicOr(&ctl->pad[1 + round % 3], 1);
-    if (!grid_barrier(ctl, w.p.barrierLimit)) return;
-    const int any = *((volatile int *)&ctl->pad[1 + round % 3]);
-    if (!any) break;
-    if (round > 4096) {
-      if (tid == 0) atomicOr(&ctl->flags, kOvfColors);
-      break;
-    }
-  }
   // owner bit (bit 1) of every contact entry: the endpoint with the larger
   // colour owns the contact's dual update (a static endpoint has colour -1)
   for (int i = tid; i < n; i += stride) {
@@ -511,6 +439,71 @@ __global__ void __launch_bounds__(256) coloring_kernel(World w) {
     }
     __syncthreads();
   }
+}
+
+__global__ void __launch_bounds__(256) coloring_kernel(World w) {
+  Control *ctl = w.ctl;
+  const int n = w.b.n;
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x, stride = gridDim.x * blockDim.x;
+  volatile int *color = w.b.color;
+  // an uploaded colouring (copied and checked by the kernels before this
+  // one) is used when proper; otherwise the priority colouring is computed
+  if (w.a.colorOverride) {
+    if (*((volatile int *)&ctl->colorBad) == 0) {
+      coloring_finish(w);
+      return;
+    }
+    if (tid == 0) atomicOr(&ctl->flags, kErrColoring);
+  }
+  // seed: previous colours (statics -1, new dynamic bodies 0)
+  for (int i = tid; i < n; i += stride) {
+    if (!(w.b.flags0[i] & kBodyDynamic)) color[i] = -1;
+    else if (color[i] < 0 || color[i] >= kMaxColors) color[i] = 0;
+  }
+  // "changed" flags, triple-buffered: round r sets flag r % 3 and clears the
+  // flag of round r + 1, which no block can still be reading (it was last
+  // read in round r - 2, before the barriers of round r - 1).
+  if (tid == 0) ctl->pad[1] = 0;
+  int round = 0;
+  for (;; round++) {
+    if (tid == 0) ctl->pad[1 + (round + 1) % 3] = 0;
+    if (!grid_barrier(ctl, w.p.barrierLimit)) return;
+    int changed = 0;
+    for (int i = tid; i < n; i += stride) {
+      if (!(w.b.flags0[i] & kBodyDynamic)) continue;
+      unsigned long long used = 0ull;
+      const int hb = w.a.start[i], hc = w.a.hpCount[i];
+      for (int k = 0; k < hc; k++) {
+        const int c = color[w.a.hpEntry[hb + k]];
+        if (c >= 0 && c < kMaxColors) used |= 1ull << c;
+      }
+      if (w.g.hasConstraints)
+        constraint_neighbors(w, i, [&](int j) {
+          if (precedes(w, j, i)) {
+            const int c = color[j];
+            if (c >= 0 && c < kMaxColors) used |= 1ull << c;
+          }
+        });
+      int c = __ffsll((long long)~used) - 1;
+      if (c < 0) {
+        c = kMaxColors - 1;
+        atomicOr(&ctl->flags, kOvfColors);
+      }
+      if (c != color[i]) {
+        color[i] = c;
+        changed = 1;
+      }
+    }
+    if (changed) atomicOr(&ctl->pad[1 + round % 3], 1);
+    if (!grid_barrier(ctl, w.p.barrierLimit)) return;
+    const int any = *((volatile int *)&ctl->pad[1 + round % 3]);
+    if (!any) break;
+    if (round > 4096) {
+      if (tid == 0) atomicOr(&ctl->flags, kOvfColors);
+      break;
+    }
+  }
+  coloring_finish(w);
 }
 
 // ---------------------------------------------------------------------------
@@ -1680,7 +1673,35 @@ static int coloring_blocks(int smCount) {
 
 int coloring_grid(int smCount) { return coloring_blocks(smCount); }
 
+// An uploaded colouring: copied, then checked against this step's graph.
+__global__ void color_copy_kernel(World w) {
+  if (blockIdx.x == 0 && threadIdx.x == 0) w.ctl->colorBad = 0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < w.b.n; i += gridDim.x * blockDim.x)
+    w.b.color[i] = (w.b.flags0[i] & kBodyDynamic) ? w.a.colorOverride[i] : -1;
+}
+
+__global__ void color_check_kernel(World w) {
+  int bad = 0;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < w.b.n && !bad; i += gridDim.x * blockDim.x) {
+    if (!(w.b.flags0[i] & kBodyDynamic)) continue;
+    const int ci = w.b.color[i];
+    if (ci < 0 || ci >= kMaxColors) {
+      bad = 1;
+      break;
+    }
+    // a conflicting edge is in the higher-priority list of one of its ends
+    const int hb = w.a.start[i], hc = w.a.hpCount[i];
+    for (int k = 0; k < hc && !bad; k++) bad = w.b.color[w.a.hpEntry[hb + k]] == ci;
+    if (w.g.hasConstraints) constraint_neighbors(w, i, [&](int j) { bad |= w.b.color[j] == ci ? 1 : 0; });
+  }
+  if (bad) atomicOr(&w.ctl->colorBad, 1);
+}
+
 cudaError_t launch_coloring(const World &w, cudaStream_t st, int smCount) {
+  if (w.a.colorOverride) {
+    color_copy_kernel<<<smCount * 4, 256, 0, st>>>(w);
+    color_check_kernel<<<smCount * 4, 256, 0, st>>>(w);
+  }
   World arg = w;
   void *args[] = {&arg};
   return cudaLaunchCooperativeKernel((void *)coloring_kernel, dim3(coloring_blocks(smCount)), dim3(256), args, 0,
