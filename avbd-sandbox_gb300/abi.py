@@ -77,7 +77,7 @@ def default_params(**overrides) -> Params:
     p.hash_threshold = 150
     p.body_order = ORDER_REFERENCE
     p.fp64_ratio_threshold = 1e5
-    p.schedule = 1
+    p.schedule = 0
     for k, v in overrides.items():
         if not hasattr(p, k):
             raise AttributeError(k)
@@ -141,7 +141,7 @@ class Profile(C.Structure):
                 ("candidate_pairs", C.c_int64), ("manifolds", C.c_int64), ("contacts", C.c_int64),
                 ("colors", C.c_int32), ("fp64_bodies", C.c_int32),
                 ("np_face", C.c_int32), ("np_edge", C.c_int32), ("np_exact", C.c_int32),
-                ("reserved", C.c_int32)]
+                ("lanes_per_body", C.c_int32)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}

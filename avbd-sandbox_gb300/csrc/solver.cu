@@ -1461,18 +1461,19 @@ __device__ __noinline__ void solve_body_f64(const World &w, int4 rec, int lane, 
   solve_body<double>(w, rec, lane, G, mask, alpha, dual, velocity);
 }
 
+// G > 0: every colour phase uses G lanes per body. G < 0: each phase picks its
+// own: 32 lanes (the lowest latency per body) unless the colour holds more
+// bodies than the grid has groups of that width, then halved while that
+// stays so, down to -G lanes (a floor the host sets from the contact sides per
+// body, so that lanes do not take on many staging chunks).
 __global__ void __launch_bounds__(kSolveBlock, 3) solve_kernel(World w, int G) {
   extern __shared__ float4 stageSm[];
   float4 *stage = stageSm + threadIdx.x;
   const SolverParams &P = w.p;
   Control *ctl = w.ctl;
   const int numColors = *((volatile int *)&ctl->numColors);
-  const int lane = threadIdx.x & (G - 1);
+  const int threads = gridDim.x * blockDim.x;
   const int warpLane = threadIdx.x & 31;
-  const unsigned mask = (G == 32 ? 0xffffffffu : (((1u << G) - 1u) << (warpLane & ~(G - 1))));
-  // groups interleaved across blocks, so a thin colour still spreads over all SMs
-  const int group = (threadIdx.x / G) * gridDim.x + blockIdx.x;
-  const int groups = (gridDim.x * blockDim.x) / G;
   const int total = P.iterations + (P.postStabilize ? 1 : 0);
   for (int it = 0; it < total; it++) {
     const double alpha = P.postStabilize ? (it < P.iterations ? 1.0 : 0.0) : P.alpha;
@@ -1480,10 +1481,20 @@ __global__ void __launch_bounds__(kSolveBlock, 3) solve_kernel(World w, int G) {
     const bool vel = it == P.iterations - 1;
     for (int c = 0; c < numColors; c++) {
       const int beg = ld(&w.a.colorStart[c]), end = ld(&w.a.colorStart[c + 1]);
+      int Gc = G;
+      if (G < 0) {
+        Gc = 32;
+        while (Gc > -G && end - beg > threads / Gc) Gc >>= 1;
+      }
+      const int lane = threadIdx.x & (Gc - 1);
+      const unsigned mask = (Gc == 32 ? 0xffffffffu : (((1u << Gc) - 1u) << (warpLane & ~(Gc - 1))));
+      // groups interleaved across blocks, so a thin colour still spreads over all SMs
+      const int group = (threadIdx.x / Gc) * gridDim.x + blockIdx.x;
+      const int groups = threads / Gc;
       for (int k = beg + group; k < end; k += groups) {
         const int4 rec = ld(&w.a.colorRec[k]);
-        if (ld(&w.b.flags[rec.x]) & kBodyFp64) solve_body_f64(w, rec, lane, G, mask, alpha, dual, vel);
-        else solve_body_staged(w, rec, lane, G, mask, (float)alpha, dual, vel, stage);
+        if (ld(&w.b.flags[rec.x]) & kBodyFp64) solve_body_f64(w, rec, lane, Gc, mask, alpha, dual, vel);
+        else solve_body_staged(w, rec, lane, Gc, mask, (float)alpha, dual, vel, stage);
       }
       if (!grid_barrier(ctl, w.p.barrierLimit)) return;
     }

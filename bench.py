@@ -251,7 +251,8 @@ def run_gpu(args):
     phase_tot = {k: 0.0 for k in ("broadphase_ms", "narrowphase_ms", "prepare_ms", "coloring_ms", "solve_ms")}
     algo_tot = {"solve": 0.0, "narrowphase": 0.0}
     step_ms = []
-    work = {"candidate_pairs": 0, "manifolds": 0, "contacts": 0, "np_face": 0, "np_edge": 0, "np_exact": 0}
+    work = {"candidate_pairs": 0, "manifolds": 0, "contacts": 0, "np_face": 0, "np_edge": 0, "np_exact": 0,
+            "lanes_per_body": 0}
     peak_work = {k: 0 for k in ("candidate_pairs", "manifolds", "contacts", "colors", "fp64_bodies")}
     if ws > 1:
         torch.distributed.barrier()
@@ -389,7 +390,7 @@ def run_batched(abi, backend, args, flush):
     gpu.set_profiling(True)
     total_ms, K = 0.0, args.batched_steps
     phases = {k: 0.0 for k in ("broadphase_ms", "narrowphase_ms", "prepare_ms", "coloring_ms", "solve_ms")}
-    contacts = 0
+    contacts = lanes = 0
     for _ in range(K):
         flush.fill_(1.0)
         torch.cuda.synchronize()
@@ -397,6 +398,7 @@ def run_batched(abi, backend, args, flush):
         p = gpu.last_profile
         total_ms += p["step_ms"]
         contacts += p["contacts"]
+        lanes += p["lanes_per_body"]
         for k in phases:
             phases[k] += p[k]
     gpu.set_profiling(False)
@@ -405,7 +407,7 @@ def run_batched(abi, backend, args, flush):
     return {
         "value": n_scenes * K / (total_ms / 1e3), "unit": "scene-steps/s", "scenes": n_scenes,
         "bodies": batch.n_bodies, "steps": K, "ms_per_step": total_ms / K,
-        "steps_per_s": K / (total_ms / 1e3), "mean_contacts": contacts / K,
+        "steps_per_s": K / (total_ms / 1e3), "mean_contacts": contacts / K, "mean_lanes_per_body": lanes / K,
         "phases_ms": {k: v / K for k, v in phases.items()},
         "workload": f"{n_scenes} random box piles ({batch.n_bodies:,} bodies) in one context, steps 1..{K}",
     }

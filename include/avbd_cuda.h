@@ -101,11 +101,17 @@ typedef struct avbd_params {
   /* GPU capacity policy (0 = automatic). */
   int32_t max_pairs_per_body; /* candidate partners with a lower index      */
   int32_t max_adjacency;      /* constraints incident to one dynamic body   */
-  int32_t lanes_per_body;     /* 0 = automatic; else 1, 2, 4, 8, 16 or 32   */
+  /* Lanes of a warp per body update: 1, 2, 4, 8, 16 or 32. 0 = automatic:
+     under schedule 0, the fewest lanes (4..32) whose 4-contact staging per
+     lane holds the mean contact sides of a body, raised towards 32 in colour
+     phases that have fewer bodies than the grid has lane groups; schedule 1
+     uses 32. */
+  int32_t lanes_per_body;
   int32_t blocks_per_sm;      /* 0 = automatic                              */
   /* Schedule of the primal/dual iterations on the device:
-     0 = colour phases separated by a grid barrier,
-     1 = dependency wavefront (each body waits only for its neighbours). */
+     0 = colour phases separated by a grid barrier (default),
+     1 = dependency wavefront (each body waits only for its neighbours).
+     Both give the same result for the same nonzero lanes_per_body. */
   int32_t schedule;
   int32_t grid_factor;        /* hash-grid arena multiplier (0 = 1)         */
 } avbd_params;
@@ -240,7 +246,7 @@ typedef struct avbd_profile {
   int32_t np_face;
   int32_t np_edge;
   int32_t np_exact;
-  int32_t reserved;
+  int32_t lanes_per_body;     /* lanes per body the step's solve used       */
 } avbd_profile;
 
 typedef struct avbd_ctx avbd_ctx;

@@ -196,11 +196,12 @@ def test_arena_regrow_preserves_results(abi, scenes, backend_mod):
 
 def test_schedules_agree(abi, scenes, backend_mod):
     """The colour-phase and wavefront schedules run the same per-body
-    updates in the same dependency order: bit-identical trajectories."""
+    updates in the same dependency order: bit-identical trajectories at the
+    same lanes per body (the group width sets the order of the sums)."""
     s = scenes.pyramid(layers=12)
     outs = []
     for schedule in (0, 1):
-        gpu = backend_mod.GpuBackend(params_for(abi, s, schedule=schedule))
+        gpu = backend_mod.GpuBackend(params_for(abi, s, schedule=schedule, lanes_per_body=32))
         gpu.pack(s.world())
         gpu.step(30)
         gpu.idle()
