@@ -1380,20 +1380,24 @@ __device__ __forceinline__ int stage_chunk(const World &w, int cb, int lane, int
 }
 
 // The joints and springs of a body (entries nm..total of its constraint list).
+// Out of line, so the body state and the partial system go by value and come
+// back as the return value: a reference would let their address escape and
+// keep them in local memory through the whole contact loop of every body.
 template <class T>
-__device__ __noinline__ void constraints_primal(const World &w, int nm, int cStart, int total, int lane, int G,
-                                                const BState<T> &self, T alpha, Sys<T> &s) {
+__device__ __noinline__ Sys<T> constraints_primal(const World &w, int nm, int cStart, int total, int lane, int G,
+                                                  const BState<T> self, T alpha, Sys<T> s) {
   for (int e = first_extra(lane, nm, G); e < total; e += G) {
     const uint32_t ref = ld(&w.g.cRef[cStart + e - nm]);
     const uint32_t type = ref >> 30, idx = (ref >> 1) & 0x1fffffffu, side = ref & 1u;
     if (type == kRefJoint) joint_primal<T>(w, (int)idx, (int)side, self, alpha, s);
     else spring_primal<T>(w, (int)idx, (int)side, self, s);
   }
+  return s;
 }
 
 template <class T>
 __device__ __noinline__ void constraints_dual(const World &w, int i, int nm, int cStart, int total, int lane, int G,
-                                              const BState<T> &self, T alpha) {
+                                              const BState<T> self, T alpha) {
   const int myColor = ld(&w.b.color[i]);
   for (int e = first_extra(lane, nm, G); e < total; e += G) {
     const uint32_t ref = ld(&w.g.cRef[cStart + e - nm]);
@@ -1431,7 +1435,7 @@ __device__ void solve_body_staged(const World &w, int4 rec, int lane, int G, uns
     cnt = nk - k0 < kStageSlots ? nk - k0 : kStageSlots;
     stage_chunk(w, cb, lane, G, k0, cnt, ent, stage, false);
   }
-  if (total > nm) constraints_primal<T>(w, nm, cStart, total, lane, G, self, alpha, s);
+  if (total > nm) s = constraints_primal<T>(w, nm, cStart, total, lane, G, self, alpha, s);
   finish_body<T>(w, i, lane, G, mask, velocity, qt, s, self);
   if (!dual) return;
   if (nk <= kStageSlots) {
