@@ -25,6 +25,8 @@ __host__ __device__ inline D4 mkd4(double x, double y, double z, double w) { ret
 
 constexpr int kMaxContacts = 8;
 constexpr int kMaxColors = 64;
+constexpr int kLaneBuckets = 8;     // log2 of the lanes of a body's group: 0..7
+constexpr int kLaneMaxGroup = 128;  // largest group: one solve block
 
 // Overflow / error bits in Control::flags (mirrors AVBD_OVF_* of the ABI).
 constexpr unsigned kOvfCells = 0x1u;
@@ -59,6 +61,7 @@ struct SolverParams {
   int rotatedInertia, springRamp, springGeometric, cachedJacobians;
   double fp64Ratio;
   int schedule;  // 0: colour phases + grid barrier, 1: dependency wavefront
+  int lanes;     // lanes per body of the colour-phase solve; 0: per body, from its constraint count
   long long barrierLimit, waitLimit;  // polls before a grid barrier / a neighbour wait gives up
 };
 
@@ -77,7 +80,8 @@ struct Control {
   int prevCandidates;  // candidates (= manifold slots) of the previous step
   int npCount[3];      // narrow-phase work lists: face, edge, exact
   int colorBad;        // this step's uploaded colouring has a conflict
-  int pad[5];
+  int laneTotal;       // lanes of one iteration's colour phases (sum over bodies)
+  int pad[4];
 };
 
 struct Bodies {
@@ -207,6 +211,13 @@ struct Adjacency {
   int *colorBodies;  // dynamic bodies sorted by (colour, index)
   int4 *colorRec;    // per colour position: body, contact range begin, end, 0
   int *blockHist;    // colouring counting sort scratch
+  // lane layout of the colour-phase solve: per colour, its bodies' lane
+  // groups (G lanes, a power of two, aligned to G) in decreasing G, cut into
+  // chunks of kLaneMaxGroup lanes (one solve block each); entry per lane:
+  // record << 4 | FP64 << 3 | log2 G, or -1 past the colour's last group
+  int *laneTab;      // kLaneMaxGroup * (n + kMaxColors): never overflows
+  int *colorChunk;   // kMaxColors + 1: first chunk of each colour
+  int *laneHist;     // 2 * kMaxColors * kLaneBuckets: group counts, then lane cursors
 };
 
 // Everything a kernel may touch.

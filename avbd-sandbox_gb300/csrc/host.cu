@@ -62,12 +62,8 @@ struct avbd_ctx {
   float4 *hQuat = nullptr, *hVel = nullptr, *hOmega = nullptr, *hPrev = nullptr;
   // candidate count of the latest completed step (pinned, written by the stream)
   int *hCand = nullptr;
-  // per-step counters (numCandidates .. liveContacts), ring of 8 steps, pinned:
-  // the automatic lanes-per-body choice of step t reads step t - kRunAhead's
-  int *hCtlRing = nullptr;
-  bool autoLanes = false;
+  bool autoLanes = false;  // lanes_per_body 0: chosen per body by the colouring
   int nDyn = 0;
-  int64_t packContacts = 0;
   std::vector<void *> growable;  // arenas sized by the candidate capacity
   int64_t regrows = 0;
   int *colorOverride = nullptr;  // device copy of an uploaded colouring (n)
@@ -132,8 +128,6 @@ void free_all(avbd_ctx *ctx) {
   ctx->growable.clear();
   if (ctx->hCand) cudaFreeHost(ctx->hCand);
   ctx->hCand = nullptr;
-  if (ctx->hCtlRing) cudaFreeHost(ctx->hCtlRing);
-  ctx->hCtlRing = nullptr;
   void *pinned[5] = {ctx->hPos, ctx->hQuat, ctx->hVel, ctx->hOmega, ctx->hPrev};
   for (void *p : pinned)
     if (p) cudaFreeHost(p);
@@ -353,25 +347,9 @@ int write_state(avbd_ctx *ctx, const avbd_world *world, bool keepManifolds) {
   return AVBD_OK;
 }
 
-// Lanes per body for the next step's solve, as launch_solve's argument: the
-// parameter when it is set. Otherwise, for the colour-phase schedule, minus
-// a floor for the per-colour choice: the fewest lanes (4..32) whose staging
-// chunk of 4 contacts per lane holds a body's mean contact sides, from the mean contact sides per dynamic body of the step
-// kRunAhead back (complete: the host waited for it), so that the choice does
-// not depend on timing (the first steps use the packed warm-start
-// manifolds); the wavefront schedule keeps 32 lanes.
-int lanes_for_step(avbd_ctx *ctx) {
-  if (!ctx->autoLanes) return ctx->lanes;
-  if (ctx->params.schedule == 1) return ctx->lanes = 32;
-  int64_t contacts = ctx->packContacts;
-  if (ctx->stepSeq >= avbd_ctx::kRunAhead)
-    contacts = ((volatile int *)ctx->hCtlRing)[((ctx->stepSeq - avbd_ctx::kRunAhead) % 8) * 8 + 4];
-  const double sides = 2.0 * (double)contacts / (double)std::max(ctx->nDyn, 1);
-  int G = 4;
-  while (G < 32 && 4.0 * G < sides) G <<= 1;
-  ctx->lanes = G;
-  return -G;
-}
+// Lanes per body of the wavefront schedule (launch_solve's argument); the
+// colour-phase schedule takes each body's lanes from the colouring's layout.
+int wave_lanes(const avbd_ctx *ctx) { return ctx->autoLanes ? 32 : ctx->lanes; }
 
 int one_step(avbd_ctx *ctx) {
   if (ctx->stepSeq >= avbd_ctx::kRunAhead)
@@ -397,7 +375,7 @@ int one_step(avbd_ctx *ctx) {
   CK(launch_coloring(w, st, ctx->smCount));
   ctx->launches += 1 + (w.a.colorOverride ? 2 : 0);
   if ((rc = record(ctx, 4))) return rc;
-  CK(launch_solve(w, lanes_for_step(ctx), ctx->blocksPerSm, st, ctx->smCount));
+  CK(launch_solve(w, wave_lanes(ctx), ctx->blocksPerSm, st, ctx->smCount));
   ctx->launches += 1;
   if ((rc = record(ctx, 5))) return rc;
   launch_commit(w, st, ctx->smCount);
@@ -405,8 +383,6 @@ int one_step(avbd_ctx *ctx) {
   // this step's candidates become next step's previous manifolds
   CK(cudaMemcpyAsync(&w.ctl->prevCandidates, &w.ctl->numCandidates, sizeof(int), cudaMemcpyDeviceToDevice, st));
   CK(cudaMemcpyAsync(ctx->hCand, &w.ctl->numCandidates, sizeof(int), cudaMemcpyDeviceToHost, st));
-  CK(cudaMemcpyAsync(ctx->hCtlRing + (ctx->stepSeq % 8) * 8, &w.ctl->numCandidates, 5 * sizeof(int),
-                     cudaMemcpyDeviceToHost, st));
   if ((rc = record(ctx, 6))) return rc;
   CK(cudaEventRecord(ctx->stepEv[ctx->stepSeq % 8], st));
   ctx->stepSeq++;
@@ -435,7 +411,9 @@ int one_step(avbd_ctx *ctx) {
     ctx->prof.np_face = c.npCount[0];
     ctx->prof.np_edge = c.npCount[1];
     ctx->prof.np_exact = c.npCount[2];
-    ctx->prof.lanes_per_body = ctx->lanes;
+    ctx->prof.lanes_per_body = ctx->params.schedule == 1 || !ctx->autoLanes
+                                   ? wave_lanes(ctx)
+                                   : (c.laneTotal + std::max(ctx->nDyn, 1) / 2) / std::max(ctx->nDyn, 1);
   }
   return AVBD_OK;
 }
@@ -688,7 +666,7 @@ int avbd_pack(avbd_ctx *ctx, const avbd_world *world) {
   w.p = SolverParams{P.dt, P.gravity, P.iterations, P.post_stabilize, P.beta_lin, P.beta_ang, P.alpha, P.gamma,
                      P.penalty_min, P.penalty_max, P.collision_margin, P.stick_threshold, P.rotated_inertia,
                      P.spring_stiffness_ramp, P.spring_geometric_stiffness, P.cached_contact_jacobians,
-                     P.fp64_ratio_threshold, P.schedule == 1 ? 1 : 0,
+                     P.fp64_ratio_threshold, P.schedule == 1 ? 1 : 0, P.lanes_per_body > 0 ? P.lanes_per_body : 0,
                      P.wait_limit > 0 ? (long long)P.wait_limit : 20000000LL,
                      P.wait_limit > 0 ? (long long)P.wait_limit : 4000000LL};
   int rc = 0;
@@ -767,14 +745,15 @@ int avbd_pack(avbd_ctx *ctx, const avbd_world *world) {
       (rc = dalloc(ctx, &w.a.ccount, n + 1)) ||
       (rc = dalloc(ctx, &w.a.colorStart, kMaxColors + 1)) || (rc = dalloc(ctx, &w.a.colorBodies, n)) ||
       (rc = dalloc(ctx, &w.a.colorRec, n)) ||
-      (rc = dalloc(ctx, &w.a.blockHist, (size_t)ctx->colorBlocks * kMaxColors)))
+      (rc = dalloc(ctx, &w.a.blockHist, (size_t)ctx->colorBlocks * kMaxColors)) ||
+      (rc = dalloc(ctx, &w.a.laneTab, (size_t)kLaneMaxGroup * ((size_t)n + kMaxColors))) ||
+      (rc = dalloc(ctx, &w.a.colorChunk, kMaxColors + 1)) ||
+      (rc = dalloc(ctx, &w.a.laneHist, 2 * kMaxColors * kLaneBuckets + kMaxColors)))
     return rc;
   // manifolds (double-buffered), candidate keys, adjacency
   if ((rc = alloc_candidate_arenas(ctx, ctx->candCap))) return rc;
   CK(cudaMallocHost((void **)&ctx->hCand, sizeof(int)));
   *ctx->hCand = 0;
-  CK(cudaMallocHost((void **)&ctx->hCtlRing, sizeof(int) * 64));
-  std::memset(ctx->hCtlRing, 0, sizeof(int) * 64);
   ctx->curIsA = 1;
   set_world_manifolds(ctx);
   if ((rc = dalloc(ctx, &w.ctl, 1)) || (rc = dalloc(ctx, &ctx->statsOut, 3))) return rc;
@@ -789,9 +768,6 @@ int avbd_pack(avbd_ctx *ctx, const avbd_world *world) {
   ctx->lanes = P.lanes_per_body > 0 ? P.lanes_per_body : 32;
   ctx->nDyn = 0;
   for (int i = 0; i < n; i++) ctx->nDyn += B.mass[i] > 0 ? 1 : 0;
-  ctx->packContacts = 0;
-  for (int m = 0; m < world->manifolds.count && world->manifolds.num_contacts; m++)
-    ctx->packContacts += std::max(0, world->manifolds.num_contacts[m]);
   if (ctx->lanes != 1 && ctx->lanes != 2 && ctx->lanes != 4 && ctx->lanes != 8 && ctx->lanes != 16 && ctx->lanes != 32)
     return fail(ctx, AVBD_ERR_ARG, "lanes_per_body must be a power of two <= 32");
   ctx->blocksPerSm = P.blocks_per_sm > 0 ? std::min(P.blocks_per_sm, maxPerSm) : maxPerSm;

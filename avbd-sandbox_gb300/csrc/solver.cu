@@ -33,6 +33,7 @@ namespace avbd {
 namespace {
 
 constexpr int kSolveBlock = 128;   // threads of a solve block (3 blocks per SM)
+static_assert(kSolveBlock == kLaneMaxGroup, "a lane chunk is one solve block");
 constexpr int kStageSlots = 4;     // contacts a lane stages in shared memory at a time
 constexpr int kStageVecs = 9;      // float4 per staged contact
 constexpr size_t kSolveSmem = (size_t)kSolveBlock * kStageSlots * kStageVecs * sizeof(float4);  // 73,728 B
@@ -352,8 +353,89 @@ __device__ inline void constraint_neighbors(const World &w, int i, F &&f) {
   }
 }
 
-// The tail of the colouring: owner bits of the contact entries and the
-// stable counting sort by colour (cooperative: grid barriers inside).
+// log2 of the lanes of a body's group in the colour-phase solve: the fixed
+// lanes parameter, else the fewest lanes (4..128) whose staging of four
+// constraints per lane holds all of the body's constraints; FP64 bodies
+// (register path, warp shuffles) at most 32.
+__device__ __forceinline__ int lane_log2(const World &w, int4 rec) {
+  int G;
+  if (w.p.lanes > 0) {
+    G = w.p.lanes;
+  } else {
+    const int i = rec.x;
+    const int total = (rec.z - rec.y) + (w.g.cStart[i + 1] - w.g.cStart[i]);
+    G = 4;
+    while (G < kLaneMaxGroup && 4 * G < total) G <<= 1;
+  }
+  if ((w.b.flags[rec.x] & kBodyFp64) && G > 32) G = 32;
+  return 31 - __clz(G);
+}
+
+// The lane layout of the colour-phase solve (Adjacency::laneTab), from the
+// sorted colour records: groups counted per (colour, size), each colour's
+// groups placed in decreasing size (so every offset is a multiple of the
+// group's own size and no group crosses a chunk), chunks of all colours
+// numbered in colour order. Placement within a (colour, size) class follows
+// atomics and may vary between runs; a body's arithmetic depends only on its
+// group size, so results do not.
+__device__ void lane_layout(const World &w) {
+  Control *ctl = w.ctl;
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x, stride = gridDim.x * blockDim.x;
+  volatile int *color = w.b.color;
+  int *cnt = w.a.laneHist, *cur = w.a.laneHist + kMaxColors * kLaneBuckets;
+  int *used = w.a.laneHist + 2 * kMaxColors * kLaneBuckets;
+  const int nrec = w.a.colorStart[kMaxColors];
+  for (int r = tid; r < nrec; r += stride) {
+    const int4 rec = w.a.colorRec[r];
+    atomicAdd(&cnt[color[rec.x] * kLaneBuckets + lane_log2(w, rec)], 1);
+  }
+  if (!grid_barrier(ctl, w.p.barrierLimit)) return;
+  if (blockIdx.x == 0) {
+    __shared__ int chunks[kMaxColors];
+    const int c = threadIdx.x;
+    if (c < kMaxColors) {
+      int off = 0;
+      for (int b = kLaneBuckets - 1; b >= 0; b--) {
+        cur[c * kLaneBuckets + b] = off;
+        off += cnt[c * kLaneBuckets + b] << b;
+      }
+      used[c] = off;
+      chunks[c] = (off + kLaneMaxGroup - 1) / kLaneMaxGroup;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      int q = 0, lanes = 0;
+      for (int k = 0; k < kMaxColors; k++) {
+        w.a.colorChunk[k] = q;
+        q += chunks[k];
+        lanes += used[k];
+      }
+      w.a.colorChunk[kMaxColors] = q;
+      ctl->laneTotal = lanes;
+    }
+  }
+  if (!grid_barrier(ctl, w.p.barrierLimit)) return;
+  for (int k = tid; k < kMaxColors * kLaneBuckets; k += stride) cnt[k] = 0;  // for the next step
+  for (int r = tid; r < nrec; r += stride) {
+    const int4 rec = w.a.colorRec[r];
+    const int c = color[rec.x];
+    const int b = lane_log2(w, rec);
+    const int off = atomicAdd(&cur[c * kLaneBuckets + b], 1 << b);
+    int *dst = w.a.laneTab + (size_t)w.a.colorChunk[c] * kLaneMaxGroup + off;
+    const int e = (r << 4) | ((w.b.flags[rec.x] & kBodyFp64) ? 8 : 0) | b;
+    for (int k = 0; k < (1 << b); k++) dst[k] = e;
+  }
+  // the lanes past each colour's last group, up to its last chunk's end
+  for (int k = tid; k < kMaxColors * kLaneMaxGroup; k += stride) {
+    const int c = k / kLaneMaxGroup;
+    const size_t L = (size_t)w.a.colorChunk[c] * kLaneMaxGroup + used[c] + (k % kLaneMaxGroup);
+    if (L < (size_t)w.a.colorChunk[c + 1] * kLaneMaxGroup) w.a.laneTab[L] = -1;
+  }
+}
+
+// The tail of the colouring: owner bits of the contact entries, the stable
+// counting sort by colour and the solve's lane layout (cooperative: grid
+// barriers inside).
 __device__ void coloring_finish(const World &w) {
   Control *ctl = w.ctl;
   const int n = w.b.n;
@@ -439,6 +521,8 @@ __device__ void coloring_finish(const World &w) {
     }
     __syncthreads();
   }
+  if (!grid_barrier(ctl, w.p.barrierLimit)) return;
+  lane_layout(w);
 }
 
 __global__ void __launch_bounds__(256) coloring_kernel(World w) {
@@ -553,7 +637,8 @@ __device__ __forceinline__ void group_reduce(Sys<T> &s, unsigned mask, int G) {
 // For groups of 32 lanes: the same sums by reduce-scatter (xor distances 16,
 // 8, 4, 2, 1, the butterfly's own pairing, so every total is bitwise the
 // butterfly's) and an all-gather: 31 + 27 shuffles instead of 5 x 27.
-__device__ __forceinline__ void group_reduce32(Sys<float> &s) {
+// reduce_scatter32 leaves lane j with the warp's total of value j.
+__device__ __forceinline__ float reduce_scatter32(const Sys<float> &s) {
   const int lane = threadIdx.x & 31;
   float v[32];
 #pragma unroll
@@ -580,19 +665,51 @@ __device__ __forceinline__ void group_reduce32(Sys<float> &s) {
       v[p] = keep + __shfl_xor_sync(0xffffffffu, send, h);
     }
   }
-  // lane j now holds the total of value j
+  return v[0];
+}
+
+// Every lane gets the totals lane j holds (value j).
+__device__ __forceinline__ void all_gather32(Sys<float> &s, float t) {
 #pragma unroll
   for (int k = 0; k < 6; k++) {
-    s.l[k] = __shfl_sync(0xffffffffu, v[0], k);
-    s.a[k] = __shfl_sync(0xffffffffu, v[0], 6 + k);
+    s.l[k] = __shfl_sync(0xffffffffu, t, k);
+    s.a[k] = __shfl_sync(0xffffffffu, t, 6 + k);
   }
 #pragma unroll
-  for (int k = 0; k < 9; k++) s.c[k] = __shfl_sync(0xffffffffu, v[0], 12 + k);
+  for (int k = 0; k < 9; k++) s.c[k] = __shfl_sync(0xffffffffu, t, 12 + k);
 #pragma unroll
   for (int k = 0; k < 3; k++) {
-    s.bl[k] = __shfl_sync(0xffffffffu, v[0], 21 + k);
-    s.ba[k] = __shfl_sync(0xffffffffu, v[0], 24 + k);
+    s.bl[k] = __shfl_sync(0xffffffffu, t, 21 + k);
+    s.ba[k] = __shfl_sync(0xffffffffu, t, 24 + k);
   }
+}
+
+__device__ __forceinline__ void group_reduce32(Sys<float> &s) { all_gather32(s, reduce_scatter32(s)); }
+
+// Barriers 1..3 with immediate ids (barrier 0 is __syncthreads).
+__device__ __forceinline__ void named_barrier(int id, int count) {
+  if (id == 1) asm volatile("bar.sync 1, %0;" ::"r"(count) : "memory");
+  else if (id == 2) asm volatile("bar.sync 2, %0;" ::"r"(count) : "memory");
+  else asm volatile("bar.sync 3, %0;" ::"r"(count) : "memory");
+}
+
+// For groups of G = 64 or 128 lanes (2 or 4 whole warps of one block): each
+// warp's reduce-scatter, the warps' totals added through shared memory in
+// warp order (the same order in every warp, so all warps hold bitwise equal
+// sums), then each warp's all-gather. Named barriers: 1 and 2 for the two
+// 64-lane groups of a block, 3 for a 128-lane group, so that a warp already
+// in a later group of another shape never meets one still in this group.
+__device__ __forceinline__ void group_reduce_warps(Sys<float> &s, int G) {
+  __shared__ float red[kSolveBlock / 32][32];
+  const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
+  const int nw = G >> 5, w0 = warp & ~(nw - 1);
+  const int id = nw == 2 ? 1 + (w0 >> 1) : 3;
+  red[warp][lane] = reduce_scatter32(s);
+  named_barrier(id, G);
+  float t = red[w0][lane];
+  for (int k = 1; k < nw; k++) t += red[w0 + k][lane];
+  named_barrier(id, G);  // every warp has read before the next group writes
+  all_gather32(s, t);
 }
 
 // sym 3x3 lower index
@@ -1247,6 +1364,7 @@ __device__ __forceinline__ void finish_body(const World &w, int i, int lane, int
   const T dt = (T)w.p.dt;
   if constexpr (sizeof(T) == 4) {
     if (G == 32) group_reduce32(s);
+    else if (G > 32) group_reduce_warps(s, G);
     else group_reduce(s, mask, G);
   } else {
     group_reduce(s, mask, G);
@@ -1465,18 +1583,15 @@ __device__ __noinline__ void solve_body_f64(const World &w, int4 rec, int lane, 
   solve_body<double>(w, rec, lane, G, mask, alpha, dual, velocity);
 }
 
-// G > 0: every colour phase uses G lanes per body. G < 0: each phase picks its
-// own: 32 lanes (the lowest latency per body) unless the colour holds more
-// bodies than the grid has groups of that width, then halved while that
-// stays so, down to -G lanes (a floor the host sets from the contact sides per
-// body, so that lanes do not take on many staging chunks).
-__global__ void __launch_bounds__(kSolveBlock, 3) solve_kernel(World w, int G) {
+// Colour phases separated by grid barriers. Each block takes the colour's
+// lane chunks (Adjacency::laneTab) q = blockIdx.x, + gridDim.x, ...: one
+// body per lane group, a group's G lanes working on its constraints.
+__global__ void __launch_bounds__(kSolveBlock, 3) solve_kernel(World w) {
   extern __shared__ float4 stageSm[];
   float4 *stage = stageSm + threadIdx.x;
   const SolverParams &P = w.p;
   Control *ctl = w.ctl;
   const int numColors = *((volatile int *)&ctl->numColors);
-  const int threads = gridDim.x * blockDim.x;
   const int warpLane = threadIdx.x & 31;
   const int total = P.iterations + (P.postStabilize ? 1 : 0);
   for (int it = 0; it < total; it++) {
@@ -1484,21 +1599,16 @@ __global__ void __launch_bounds__(kSolveBlock, 3) solve_kernel(World w, int G) {
     const bool dual = it < P.iterations;
     const bool vel = it == P.iterations - 1;
     for (int c = 0; c < numColors; c++) {
-      const int beg = ld(&w.a.colorStart[c]), end = ld(&w.a.colorStart[c + 1]);
-      int Gc = G;
-      if (G < 0) {
-        Gc = 32;
-        while (Gc > -G && end - beg > threads / Gc) Gc >>= 1;
-      }
-      const int lane = threadIdx.x & (Gc - 1);
-      const unsigned mask = (Gc == 32 ? 0xffffffffu : (((1u << Gc) - 1u) << (warpLane & ~(Gc - 1))));
-      // groups interleaved across blocks, so a thin colour still spreads over all SMs
-      const int group = (threadIdx.x / Gc) * gridDim.x + blockIdx.x;
-      const int groups = threads / Gc;
-      for (int k = beg + group; k < end; k += groups) {
-        const int4 rec = ld(&w.a.colorRec[k]);
-        if (ld(&w.b.flags[rec.x]) & kBodyFp64) solve_body_f64(w, rec, lane, Gc, mask, alpha, dual, vel);
-        else solve_body_staged(w, rec, lane, Gc, mask, (float)alpha, dual, vel, stage);
+      const int q0 = ld(&w.a.colorChunk[c]), q1 = ld(&w.a.colorChunk[c + 1]);
+      for (int q = q0 + (int)blockIdx.x; q < q1; q += gridDim.x) {
+        const int e = ld(&w.a.laneTab[(size_t)q * kLaneMaxGroup + threadIdx.x]);
+        if (e < 0) continue;
+        const int G = 1 << (e & 7);
+        const int lane = threadIdx.x & (G - 1);
+        const unsigned mask = G >= 32 ? 0xffffffffu : (((1u << G) - 1u) << (warpLane & ~(G - 1)));
+        const int4 rec = ld(&w.a.colorRec[e >> 4]);
+        if (e & 8) solve_body_f64(w, rec, lane, G, mask, alpha, dual, vel);
+        else solve_body_staged(w, rec, lane, G, mask, (float)alpha, dual, vel, stage);
       }
       if (!grid_barrier(ctl, w.p.barrierLimit)) return;
     }
@@ -1744,12 +1854,18 @@ int solve_max_blocks_per_sm(int lanesPerBody) {
   return a < b ? a : b;
 }
 
+// lanesPerBody: the wavefront schedule's lanes per body (the colour-phase
+// schedule reads its layout from the colouring).
 cudaError_t launch_solve(const World &w, int lanesPerBody, int blocksPerSm, cudaStream_t st, int smCount) {
   World arg = w;
   int G = lanesPerBody;
-  void *args[] = {&arg, &G};
-  const void *fn = w.p.schedule == 1 ? (const void *)wave_kernel : (const void *)solve_kernel;
-  return cudaLaunchCooperativeKernel(fn, dim3(blocksPerSm * smCount), dim3(kSolveBlock), args, kSolveSmem, st);
+  void *args2[] = {&arg, &G};
+  void *args1[] = {&arg};
+  if (w.p.schedule == 1)
+    return cudaLaunchCooperativeKernel((const void *)wave_kernel, dim3(blocksPerSm * smCount), dim3(kSolveBlock),
+                                       args2, kSolveSmem, st);
+  return cudaLaunchCooperativeKernel((const void *)solve_kernel, dim3(blocksPerSm * smCount), dim3(kSolveBlock), args1,
+                                     kSolveSmem, st);
 }
 
 void launch_commit(const World &w, cudaStream_t st, int smCount) { commit_kernel<<<smCount * 4, 256, 0, st>>>(w); }

@@ -101,11 +101,10 @@ typedef struct avbd_params {
   /* GPU capacity policy (0 = automatic). */
   int32_t max_pairs_per_body; /* candidate partners with a lower index      */
   int32_t max_adjacency;      /* constraints incident to one dynamic body   */
-  /* Lanes of a warp per body update: 1, 2, 4, 8, 16 or 32. 0 = automatic:
-     under schedule 0, the fewest lanes (4..32) whose 4-contact staging per
-     lane holds the mean contact sides of a body, raised towards 32 in colour
-     phases that have fewer bodies than the grid has lane groups; schedule 1
-     uses 32. */
+  /* Lanes per body update: 1, 2, 4, 8, 16 or 32 for every body. 0 =
+     automatic: under schedule 0 each body gets the fewest lanes (4..128, up
+     to four warps; FP64 bodies at most 32) whose staging of four constraints
+     per lane holds all of its constraints; schedule 1 uses 32. */
   int32_t lanes_per_body;
   int32_t blocks_per_sm;      /* 0 = automatic                              */
   /* Schedule of the primal/dual iterations on the device:
