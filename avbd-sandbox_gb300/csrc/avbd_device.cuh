@@ -62,6 +62,7 @@ struct SolverParams {
   double fp64Ratio;
   int schedule;  // 0: colour phases + grid barrier, 1: dependency wavefront
   int lanes;     // lanes per body of the colour-phase solve; 0: per body, from its constraint count
+  int solveBlocksPerSm;  // resident blocks per SM of the solve launch (grid = this x SMs)
   long long barrierLimit, waitLimit;  // polls before a grid barrier / a neighbour wait gives up
 };
 

@@ -666,7 +666,7 @@ int avbd_pack(avbd_ctx *ctx, const avbd_world *world) {
   w.p = SolverParams{P.dt, P.gravity, P.iterations, P.post_stabilize, P.beta_lin, P.beta_ang, P.alpha, P.gamma,
                      P.penalty_min, P.penalty_max, P.collision_margin, P.stick_threshold, P.rotated_inertia,
                      P.spring_stiffness_ramp, P.spring_geometric_stiffness, P.cached_contact_jacobians,
-                     P.fp64_ratio_threshold, P.schedule == 1 ? 1 : 0, P.lanes_per_body > 0 ? P.lanes_per_body : 0,
+                     P.fp64_ratio_threshold, P.schedule == 1 ? 1 : 0, P.lanes_per_body > 0 ? P.lanes_per_body : 0, 1,
                      P.wait_limit > 0 ? (long long)P.wait_limit : 20000000LL,
                      P.wait_limit > 0 ? (long long)P.wait_limit : 4000000LL};
   int rc = 0;
@@ -772,6 +772,7 @@ int avbd_pack(avbd_ctx *ctx, const avbd_world *world) {
     return fail(ctx, AVBD_ERR_ARG, "lanes_per_body must be a power of two <= 32");
   ctx->blocksPerSm = P.blocks_per_sm > 0 ? std::min(P.blocks_per_sm, maxPerSm) : maxPerSm;
   if (ctx->blocksPerSm < 1) return fail(ctx, AVBD_ERR_CUDA, "solve kernel cannot be made resident");
+  w.p.solveBlocksPerSm = ctx->blocksPerSm;
   // colours start at 0 for dynamic bodies
   CK(cudaMemset(w.b.color, 0, sizeof(int) * n));
   CK(cudaMallocHost((void **)&ctx->hPos, sizeof(D4) * n));

@@ -385,9 +385,17 @@ __device__ void lane_layout(const World &w) {
   int *cnt = w.a.laneHist, *cur = w.a.laneHist + kMaxColors * kLaneBuckets;
   int *used = w.a.laneHist + 2 * kMaxColors * kLaneBuckets;
   const int nrec = w.a.colorStart[kMaxColors];
-  for (int r = tid; r < nrec; r += stride) {
-    const int4 rec = w.a.colorRec[r];
-    atomicAdd(&cnt[color[rec.x] * kLaneBuckets + lane_log2(w, rec)], 1);
+  const int lane = threadIdx.x & 31;
+  // warp-uniform loops (stride is a multiple of 32): the records of a warp
+  // with equal (colour, size) share one atomic
+  for (int r = tid; r - lane < nrec; r += stride) {
+    int key = -1;
+    if (r < nrec) {
+      const int4 rec = w.a.colorRec[r];
+      key = color[rec.x] * kLaneBuckets + lane_log2(w, rec);
+    }
+    const unsigned peers = __match_any_sync(0xffffffffu, key);
+    if (key >= 0 && lane == __ffs(peers) - 1) atomicAdd(&cnt[key], __popc(peers));
   }
   if (!grid_barrier(ctl, w.p.barrierLimit)) return;
   if (blockIdx.x == 0) {
@@ -416,14 +424,29 @@ __device__ void lane_layout(const World &w) {
   }
   if (!grid_barrier(ctl, w.p.barrierLimit)) return;
   for (int k = tid; k < kMaxColors * kLaneBuckets; k += stride) cnt[k] = 0;  // for the next step
-  for (int r = tid; r < nrec; r += stride) {
-    const int4 rec = w.a.colorRec[r];
-    const int c = color[rec.x];
-    const int b = lane_log2(w, rec);
-    const int off = atomicAdd(&cur[c * kLaneBuckets + b], 1 << b);
+  for (int r = tid; r - lane < nrec; r += stride) {
+    int key = -1, c = 0, b = 0, e = 0;
+    if (r < nrec) {
+      const int4 rec = w.a.colorRec[r];
+      c = color[rec.x];
+      b = lane_log2(w, rec);
+      key = c * kLaneBuckets + b;
+      e = (r << 4) | ((w.b.flags[rec.x] & kBodyFp64) ? 8 : 0) | b;
+    }
+    const unsigned peers = __match_any_sync(0xffffffffu, key);
+    const int leader = __ffs(peers) - 1;
+    int base = 0;
+    if (key >= 0 && lane == leader) base = atomicAdd(&cur[key], __popc(peers) << b);
+    base = __shfl_sync(0xffffffffu, base, leader);
+    if (key < 0) continue;
+    const int off = base + (__popc(peers & ((1u << lane) - 1u)) << b);
     int *dst = w.a.laneTab + (size_t)w.a.colorChunk[c] * kLaneMaxGroup + off;
-    const int e = (r << 4) | ((w.b.flags[rec.x] & kBodyFp64) ? 8 : 0) | b;
-    for (int k = 0; k < (1 << b); k++) dst[k] = e;
+    if (b >= 2) {  // off and G are multiples of 4: 16-byte stores
+      const int4 e4 = make_int4(e, e, e, e);
+      for (int k = 0; k < (1 << b); k += 4) *reinterpret_cast<int4 *>(dst + k) = e4;
+    } else {
+      for (int k = 0; k < (1 << b); k++) dst[k] = e;
+    }
   }
   // the lanes past each colour's last group, up to its last chunk's end
   for (int k = tid; k < kMaxColors * kLaneMaxGroup; k += stride) {
@@ -1584,8 +1607,12 @@ __device__ __noinline__ void solve_body_f64(const World &w, int4 rec, int lane, 
 }
 
 // Colour phases separated by grid barriers. Each block takes the colour's
-// lane chunks (Adjacency::laneTab) q = blockIdx.x, + gridDim.x, ...: one
-// body per lane group, a group's G lanes working on its constraints.
+// lane chunks (Adjacency::laneTab) j, j + gridDim.x, ...: one body per lane
+// group, a group's G lanes working on its constraints. j transposes the
+// block index (k blocks on each of S SMs: block b takes j = (b mod k) S +
+// b div k), so that a colour of fewer chunks than blocks spreads over
+// distinct SMs whether the launch places consecutive blocks on one SM or
+// deals them round the SMs (k and S coprime).
 __global__ void __launch_bounds__(kSolveBlock, 3) solve_kernel(World w) {
   extern __shared__ float4 stageSm[];
   float4 *stage = stageSm + threadIdx.x;
@@ -1594,13 +1621,15 @@ __global__ void __launch_bounds__(kSolveBlock, 3) solve_kernel(World w) {
   const int numColors = *((volatile int *)&ctl->numColors);
   const int warpLane = threadIdx.x & 31;
   const int total = P.iterations + (P.postStabilize ? 1 : 0);
+  const int kb = P.solveBlocksPerSm > 0 ? P.solveBlocksPerSm : 1, S = gridDim.x / kb;
+  const int jb = S * kb == (int)gridDim.x ? ((int)blockIdx.x % kb) * S + (int)blockIdx.x / kb : (int)blockIdx.x;
   for (int it = 0; it < total; it++) {
     const double alpha = P.postStabilize ? (it < P.iterations ? 1.0 : 0.0) : P.alpha;
     const bool dual = it < P.iterations;
     const bool vel = it == P.iterations - 1;
     for (int c = 0; c < numColors; c++) {
       const int q0 = ld(&w.a.colorChunk[c]), q1 = ld(&w.a.colorChunk[c + 1]);
-      for (int q = q0 + (int)blockIdx.x; q < q1; q += gridDim.x) {
+      for (int q = q0 + jb; q < q1; q += gridDim.x) {
         const int e = ld(&w.a.laneTab[(size_t)q * kLaneMaxGroup + threadIdx.x]);
         if (e < 0) continue;
         const int G = 1 << (e & 7);
