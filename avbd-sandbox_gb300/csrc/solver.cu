@@ -1338,21 +1338,16 @@ __device__ __noinline__ void extra_dual(const World &w, int i, int cb, int nm, i
 
 // Inertial terms of a body's system (solver.js:425-439), added by lane 0.
 template <class T>
-__device__ __forceinline__ void inertial_terms(const World &w, int i, const BState<T> &self, bool selfSphere,
-                                               Sys<T> &s) {
-  const SolverParams &P = w.p;
+__device__ __forceinline__ void inertial_core(const SolverParams &P, T m, T I0, T I1, T I2, float4 y, float4 qy,
+                                              const BState<T> &self, bool selfSphere, Sys<T> &s) {
   const T dt2 = (T)(P.dt * P.dt);
-  const D4 md = ld(&w.b.massD[i]);
-  const T m = (T)md.x;
   const T ml = m / dt2;
   s.l[0] = ml; s.l[2] = ml; s.l[5] = ml;
-  const float4 y = ld(&w.b.yLin[i]), qy = ld(&w.b.yAng[i]);
   const V3<T> dy = self.dp - V3<T>{(T)y.x, (T)y.y, (T)y.z};
   s.bl[0] = ml * dy.x; s.bl[1] = ml * dy.y; s.bl[2] = ml * dy.z;
   // world moment R I R^T (rigid.js:228-247), / dt^2
   T M[9];
   const bool iso = !P.rotatedInertia || selfSphere;
-  const T I0 = (T)md.y, I1 = (T)md.z, I2 = (T)md.w;
   if (iso) {
     M[0] = I0; M[1] = 0; M[2] = 0; M[3] = 0; M[4] = I1; M[5] = 0; M[6] = 0; M[7] = 0; M[8] = I2;
   } else {
@@ -1376,6 +1371,13 @@ __device__ __forceinline__ void inertial_terms(const World &w, int i, const BSta
   s.ba[0] = (M[0] * dq.x + M[1] * dq.y + M[2] * dq.z) / dt2;
   s.ba[1] = (M[3] * dq.x + M[4] * dq.y + M[5] * dq.z) / dt2;
   s.ba[2] = (M[6] * dq.x + M[7] * dq.y + M[8] * dq.z) / dt2;
+}
+
+template <class T>
+__device__ __forceinline__ void inertial_terms(const World &w, int i, const BState<T> &self, bool selfSphere,
+                                               Sys<T> &s) {
+  const D4 md = ld(&w.b.massD[i]);
+  inertial_core<T>(w.p, (T)md.x, (T)md.y, (T)md.z, (T)md.w, ld(&w.b.yLin[i]), ld(&w.b.yAng[i]), self, selfSphere, s);
 }
 
 // Reduce the group's partial systems, solve the 6x6 system (maths.js:660-725),
@@ -1559,14 +1561,23 @@ __device__ void solve_body_staged(const World &w, int4 rec, int lane, int G, uns
   const int nk = lane < nm ? (nm - lane + G - 1) / G : 0;  // this lane's contacts
   int2 ent[kStageSlots];
   int cnt = nk < kStageSlots ? nk : kStageSlots;
-  stage_chunk(w, cb, lane, G, 0, cnt, ent, stage, false);  // in flight while the body's own data loads
+  // the body's own data (state, inertial terms: massF holds massD's f32
+  // conversions) is requested before the contact entries, so that one round
+  // trip serves both; the contact data then follows with cp.async
   const float4 qt = ld(&w.b.quatT[i]);
-  BState<T> self = load_state<T>(w, i);
+  const float4 d0 = ldcg(&w.b.dp[i]), q0 = ldcg(&w.b.quat[i]);
+  const float4 mf = ld(&w.b.massF[i]), y = ld(&w.b.yLin[i]), qy = ld(&w.b.yAng[i]);
   const int cStart = ld(&w.g.cStart[i]), cEnd = ld(&w.g.cStart[i + 1]);
+  const bool sphere = (ld(&w.b.flags0[i]) & kBodySphere) != 0;
+  stage_chunk(w, cb, lane, G, 0, cnt, ent, stage, false);
+  BState<T> self;  // as load_state<float> forms it
+  self.dp = V3<T>{d0.x, d0.y, d0.z};
+  self.q = Q4<T>{q0.x, q0.y, q0.z, q0.w};
+  self.dang = qsub(self.q, Q4<T>{qt.x, qt.y, qt.z, qt.w});
   const int total = nm + (cEnd - cStart);
   Sys<T> s;
   zero(s);
-  if (lane == 0) inertial_terms<T>(w, i, self, (ld(&w.b.flags0[i]) & kBodySphere) != 0, s);
+  if (lane == 0) inertial_core<T>(w.p, mf.x, mf.y, mf.z, mf.w, y, qy, self, sphere, s);
   for (int k0 = 0;;) {
     cp_async_wait_all();
     for (int j = 0; j < cnt; j++)
@@ -1623,12 +1634,15 @@ __global__ void __launch_bounds__(kSolveBlock, 3) solve_kernel(World w) {
   const int total = P.iterations + (P.postStabilize ? 1 : 0);
   const int kb = P.solveBlocksPerSm > 0 ? P.solveBlocksPerSm : 1, S = gridDim.x / kb;
   const int jb = S * kb == (int)gridDim.x ? ((int)blockIdx.x % kb) * S + (int)blockIdx.x / kb : (int)blockIdx.x;
+  __shared__ int chunkSm[kMaxColors + 1];  // colour chunk bounds, constant through the solve
+  for (int k = threadIdx.x; k <= numColors; k += blockDim.x) chunkSm[k] = ld(&w.a.colorChunk[k]);
+  __syncthreads();
   for (int it = 0; it < total; it++) {
     const double alpha = P.postStabilize ? (it < P.iterations ? 1.0 : 0.0) : P.alpha;
     const bool dual = it < P.iterations;
     const bool vel = it == P.iterations - 1;
     for (int c = 0; c < numColors; c++) {
-      const int q0 = ld(&w.a.colorChunk[c]), q1 = ld(&w.a.colorChunk[c + 1]);
+      const int q0 = chunkSm[c], q1 = chunkSm[c + 1];
       for (int q = q0 + jb; q < q1; q += gridDim.x) {
         const int e = ld(&w.a.laneTab[(size_t)q * kLaneMaxGroup + threadIdx.x]);
         if (e < 0) continue;
