@@ -1505,13 +1505,59 @@ __device__ __forceinline__ ContactData<float> staged_contact(const float4 *st, i
   return d;
 }
 
-// Stage chunk [k0, k0 + cnt) of this lane's contacts (contact e = lane + k G).
+__device__ inline int ld_acquire(const int *p) {
+  int v;
+  asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ inline void st_release(int *p, int v) {
+  asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
+// The colour-phase solve's tail: the last colours (few bodies each) run as
+// one dependency-driven segment instead of one phase each. A tail body of
+// colour `color` in iteration t waits, before reading a neighbour, until
+// every neighbour of a lower tail colour (>= from) has published progress
+// t + 1; neighbours of earlier colours finished before the segment began,
+// those of higher colours finished iteration t - 1 before its last barrier.
+// from < 0: no waits.
+struct TailWait {
+  int from, color, need;
+};
+
+// Bounded: past the limit (or once another wait gave up) the timeout flag is
+// set and the caller carries on, so that no group member is left at a named
+// barrier; the kernel then ends at its next grid barrier and the step
+// reports the timeout.
+__device__ __forceinline__ void spin_progress(const World &w, int other, int need) {
+  long long polls = 0;
+  while (ld_acquire(&w.b.progress[other]) < need) {
+    if (++polls > w.p.waitLimit || (*((volatile unsigned *)&w.ctl->flags) & kOvfTimeout)) {
+      atomicOr(&w.ctl->flags, kOvfTimeout);
+      return;
+    }
+    __nanosleep(32);
+  }
+}
+
+__device__ __forceinline__ void tail_wait_body(const World &w, int other, const TailWait &tw) {
+  const int oc = ld(&w.b.color[other]);  // statics: -1
+  if (oc >= tw.from && oc < tw.color) spin_progress(w, other, tw.need);
+}
+
+// Stage chunk [k0, k0 + cnt) of this lane's contacts (contact e = lane + k G),
+// after the tail waits on their other bodies when `tw` is given.
 __device__ __forceinline__ int stage_chunk(const World &w, int cb, int lane, int G, int k0, int cnt, int2 *ent,
-                                           float4 *stage, bool ownedOnly) {
+                                           float4 *stage, bool ownedOnly, const TailWait *tw = nullptr) {
   int staged = 0;
 #pragma unroll
   for (int j = 0; j < kStageSlots; j++)
     if (j < cnt) ent[j] = ld(&w.a.centry[cb + lane + (k0 + j) * G]);
+  if (tw) {
+#pragma unroll
+    for (int j = 0; j < kStageSlots; j++)
+      if (j < cnt) tail_wait_body(w, ent[j].y, *tw);
+  }
 #pragma unroll
   for (int j = 0; j < kStageSlots; j++)
     if (j < cnt && (!ownedOnly || (ent[j].x & 2))) {
@@ -1554,8 +1600,21 @@ __device__ __noinline__ void constraints_dual(const World &w, int i, int nm, int
   }
 }
 
+// The joint and spring partners of a tail body (entries nm..total).
+__device__ __noinline__ void tail_wait_extra(const World &w, int nm, int cStart, int total, int lane, int G,
+                                             const TailWait tw) {
+  for (int e = first_extra(lane, nm, G); e < total; e += G) {
+    const uint32_t ref = ld(&w.g.cRef[cStart + e - nm]);
+    const uint32_t type = ref >> 30, idx = (ref >> 1) & 0x1fffffffu, side = ref & 1u;
+    const int2 ab = type == kRefJoint ? ld(&w.j.bodies[idx]) : ld(&w.s.bodies[idx]);
+    const int other = side ? ab.x : ab.y;
+    if (other >= 0) tail_wait_body(w, other, tw);
+  }
+}
+
+// `tw`: the tail waits of this body (null outside the tail segment).
 __device__ void solve_body_staged(const World &w, int4 rec, int lane, int G, unsigned mask, float alpha, bool dual,
-                                  bool velocity, float4 *stage) {
+                                  bool velocity, float4 *stage, const TailWait *tw = nullptr) {
   using T = float;
   const int i = rec.x, cb = rec.y, nm = rec.z - rec.y;
   const int nk = lane < nm ? (nm - lane + G - 1) / G : 0;  // this lane's contacts
@@ -1569,7 +1628,7 @@ __device__ void solve_body_staged(const World &w, int4 rec, int lane, int G, uns
   const float4 mf = ld(&w.b.massF[i]), y = ld(&w.b.yLin[i]), qy = ld(&w.b.yAng[i]);
   const int cStart = ld(&w.g.cStart[i]), cEnd = ld(&w.g.cStart[i + 1]);
   const bool sphere = (ld(&w.b.flags0[i]) & kBodySphere) != 0;
-  stage_chunk(w, cb, lane, G, 0, cnt, ent, stage, false);
+  stage_chunk(w, cb, lane, G, 0, cnt, ent, stage, false, tw);
   BState<T> self;  // as load_state<float> forms it
   self.dp = V3<T>{d0.x, d0.y, d0.z};
   self.q = Q4<T>{q0.x, q0.y, q0.z, q0.w};
@@ -1585,9 +1644,12 @@ __device__ void solve_body_staged(const World &w, int4 rec, int lane, int G, uns
     k0 += cnt;
     if (k0 >= nk) break;
     cnt = nk - k0 < kStageSlots ? nk - k0 : kStageSlots;
-    stage_chunk(w, cb, lane, G, k0, cnt, ent, stage, false);
+    stage_chunk(w, cb, lane, G, k0, cnt, ent, stage, false, tw);
   }
-  if (total > nm) s = constraints_primal<T>(w, nm, cStart, total, lane, G, self, alpha, s);
+  if (total > nm) {
+    if (tw) tail_wait_extra(w, nm, cStart, total, lane, G, *tw);
+    s = constraints_primal<T>(w, nm, cStart, total, lane, G, self, alpha, s);
+  }
   finish_body<T>(w, i, lane, G, mask, velocity, qt, s, self);
   if (!dual) return;
   if (nk <= kStageSlots) {
@@ -1617,69 +1679,11 @@ __device__ __noinline__ void solve_body_f64(const World &w, int4 rec, int lane, 
   solve_body<double>(w, rec, lane, G, mask, alpha, dual, velocity);
 }
 
-// Colour phases separated by grid barriers. Each block takes the colour's
-// lane chunks (Adjacency::laneTab) j, j + gridDim.x, ...: one body per lane
-// group, a group's G lanes working on its constraints. j transposes the
-// block index (k blocks on each of S SMs: block b takes j = (b mod k) S +
-// b div k), so that a colour of fewer chunks than blocks spreads over
-// distinct SMs whether the launch places consecutive blocks on one SM or
-// deals them round the SMs (k and S coprime).
-__global__ void __launch_bounds__(kSolveBlock, 3) solve_kernel(World w) {
-  extern __shared__ float4 stageSm[];
-  float4 *stage = stageSm + threadIdx.x;
-  const SolverParams &P = w.p;
-  Control *ctl = w.ctl;
-  const int numColors = *((volatile int *)&ctl->numColors);
-  const int warpLane = threadIdx.x & 31;
-  const int total = P.iterations + (P.postStabilize ? 1 : 0);
-  const int kb = P.solveBlocksPerSm > 0 ? P.solveBlocksPerSm : 1, S = gridDim.x / kb;
-  const int jb = S * kb == (int)gridDim.x ? ((int)blockIdx.x % kb) * S + (int)blockIdx.x / kb : (int)blockIdx.x;
-  __shared__ int chunkSm[kMaxColors + 1];  // colour chunk bounds, constant through the solve
-  for (int k = threadIdx.x; k <= numColors; k += blockDim.x) chunkSm[k] = ld(&w.a.colorChunk[k]);
-  __syncthreads();
-  for (int it = 0; it < total; it++) {
-    const double alpha = P.postStabilize ? (it < P.iterations ? 1.0 : 0.0) : P.alpha;
-    const bool dual = it < P.iterations;
-    const bool vel = it == P.iterations - 1;
-    for (int c = 0; c < numColors; c++) {
-      const int q0 = chunkSm[c], q1 = chunkSm[c + 1];
-      for (int q = q0 + jb; q < q1; q += gridDim.x) {
-        const int e = ld(&w.a.laneTab[(size_t)q * kLaneMaxGroup + threadIdx.x]);
-        if (e < 0) continue;
-        const int G = 1 << (e & 7);
-        const int lane = threadIdx.x & (G - 1);
-        const unsigned mask = G >= 32 ? 0xffffffffu : (((1u << G) - 1u) << (warpLane & ~(G - 1)));
-        const int4 rec = ld(&w.a.colorRec[e >> 4]);
-        if (e & 8) solve_body_f64(w, rec, lane, G, mask, alpha, dual, vel);
-        else solve_body_staged(w, rec, lane, G, mask, (float)alpha, dual, vel, stage);
-      }
-      if (!grid_barrier(ctl, w.p.barrierLimit)) return;
-    }
-  }
-}
-
-// ---------------------------------------------------------------------------
-// Dependency-driven wavefront schedule. Body i may run iteration t once every
-// neighbour of lower colour has completed iteration t and every neighbour of
-// higher colour has completed iteration t - 1: exactly the order of the colour
-// phases, without a grid-wide barrier between them. Each group walks its
-// bodies in increasing (iteration, colour) order, so the earliest unfinished
-// body always has its inputs ready and the schedule cannot deadlock while all
-// blocks are resident (cooperative launch). Every wait is bounded.
-// ---------------------------------------------------------------------------
-__device__ inline int ld_acquire(const int *p) {
-  int v;
-  asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-  return v;
-}
-__device__ inline void st_release(int *p, int v) {
-  asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
-}
-
-
 // The neighbours come from the body's manifold list (one entry per touching
 // body, where the per-contact list has up to eight) and its joints/springs.
-__device__ bool wait_neighbors(const World &w, int i, int it, int lane, int G, unsigned mask) {
+// tailFrom < 0: the wavefront's rule. Otherwise the tail segment's: only
+// neighbours of a lower colour >= tailFrom, for iteration it.
+__device__ bool wait_neighbors(const World &w, int i, int it, int lane, int G, unsigned mask, int tailFrom = -1) {
   const int myColor = ld(&w.b.color[i]);
   const int mb = ld(&w.a.start[i]);
   int me = ld(&w.a.start[i + 1]);
@@ -1702,7 +1706,7 @@ __device__ bool wait_neighbors(const World &w, int i, int it, int lane, int G, u
     }
     if (!(ld(&w.b.flags0[other]) & kBodyDynamic)) continue;
     const int oc = ld(&w.b.color[other]);
-    const int need = oc < myColor ? it + 1 : it;
+    const int need = tailFrom < 0 ? (oc < myColor ? it + 1 : it) : (oc >= tailFrom && oc < myColor ? it + 1 : 0);
     while (ld_acquire(&w.b.progress[other]) < need) {
       if (++polls > w.p.waitLimit || (*((volatile unsigned *)&w.ctl->flags) & kOvfTimeout)) {
         atomicOr(&w.ctl->flags, kOvfTimeout);
@@ -1715,6 +1719,103 @@ __device__ bool wait_neighbors(const World &w, int i, int it, int lane, int G, u
   }
   return __all_sync(mask, polls >= 0);
 }
+
+// Every warp of a body's lane group past this point (G > 32: the group's
+// named barrier, as in group_reduce_warps).
+__device__ __forceinline__ void group_sync(int G, unsigned mask) {
+  if (G <= 32) {
+    __syncwarp(mask);
+  } else {
+    const int nw = G >> 5, w0 = (threadIdx.x >> 5) & ~(nw - 1);
+    named_barrier(nw == 2 ? 1 + (w0 >> 1) : 3, G);
+  }
+}
+
+// Colour phases separated by grid barriers. Each block takes the colour's
+// lane chunks (Adjacency::laneTab) j, j + gridDim.x, ...: one body per lane
+// group, a group's G lanes working on its constraints. j transposes the
+// block index (k blocks on each of S SMs: block b takes j = (b mod k) S +
+// b div k), so that a colour of fewer chunks than blocks spreads over
+// distinct SMs whether the launch places consecutive blocks on one SM or
+// deals them round the SMs (k and S coprime).
+// The tail - the last colours, each of at most gridDim / kTailDiv chunks -
+// is one segment per iteration with a single barrier: its chunks, in colour
+// order, taken as above; a body waits only for its lower-colour tail
+// neighbours (TailWait) and publishes its progress when done. Each group
+// walks its chunks in increasing colour, so the earliest unfinished tail
+// body always has its inputs ready (all blocks are resident).
+constexpr int kTailDiv = 8;
+__global__ void __launch_bounds__(kSolveBlock, 3) solve_kernel(World w) {
+  extern __shared__ float4 stageSm[];
+  float4 *stage = stageSm + threadIdx.x;
+  const SolverParams &P = w.p;
+  Control *ctl = w.ctl;
+  const int numColors = *((volatile int *)&ctl->numColors);
+  const int warpLane = threadIdx.x & 31;
+  const int total = P.iterations + (P.postStabilize ? 1 : 0);
+  const int kb = P.solveBlocksPerSm > 0 ? P.solveBlocksPerSm : 1, S = gridDim.x / kb;
+  const int jb = S * kb == (int)gridDim.x ? ((int)blockIdx.x % kb) * S + (int)blockIdx.x / kb : (int)blockIdx.x;
+  __shared__ int chunkSm[kMaxColors + 1];  // colour chunk bounds, constant through the solve
+  for (int k = threadIdx.x; k <= numColors; k += blockDim.x) chunkSm[k] = ld(&w.a.colorChunk[k]);
+  __syncthreads();
+  int tail = numColors;  // first tail colour
+  while (tail > 0 && chunkSm[tail] - chunkSm[tail - 1] <= (int)gridDim.x / kTailDiv) tail--;
+  for (int it = 0; it < total; it++) {
+    const double alpha = P.postStabilize ? (it < P.iterations ? 1.0 : 0.0) : P.alpha;
+    const bool dual = it < P.iterations;
+    const bool vel = it == P.iterations - 1;
+    for (int c = 0; c < tail; c++) {
+      const int q0 = chunkSm[c], q1 = chunkSm[c + 1];
+      for (int q = q0 + jb; q < q1; q += gridDim.x) {
+        const int e = ld(&w.a.laneTab[(size_t)q * kLaneMaxGroup + threadIdx.x]);
+        if (e < 0) continue;
+        const int G = 1 << (e & 7);
+        const int lane = threadIdx.x & (G - 1);
+        const unsigned mask = G >= 32 ? 0xffffffffu : (((1u << G) - 1u) << (warpLane & ~(G - 1)));
+        const int4 rec = ld(&w.a.colorRec[e >> 4]);
+        if (e & 8) solve_body_f64(w, rec, lane, G, mask, alpha, dual, vel);
+        else solve_body_staged(w, rec, lane, G, mask, (float)alpha, dual, vel, stage);
+      }
+      if (!grid_barrier(ctl, w.p.barrierLimit)) return;
+    }
+    if (tail < numColors) {  // the tail segment of iteration it
+      int c = tail;
+      for (int q = chunkSm[tail] + jb; q < chunkSm[numColors]; q += gridDim.x) {
+        while (chunkSm[c + 1] <= q) c++;
+        const int e = ld(&w.a.laneTab[(size_t)q * kLaneMaxGroup + threadIdx.x]);
+        if (e < 0) continue;
+        const int G = 1 << (e & 7);
+        const int lane = threadIdx.x & (G - 1);
+        const unsigned mask = G >= 32 ? 0xffffffffu : (((1u << G) - 1u) << (warpLane & ~(G - 1)));
+        const int4 rec = ld(&w.a.colorRec[e >> 4]);
+        if (e & 8) {
+          wait_neighbors(w, rec.x, it, lane, G, mask, tail);
+          __syncwarp(mask);  // every lane's reads after the others' acquires
+          solve_body_f64(w, rec, lane, G, mask, alpha, dual, vel);
+        } else {
+          const TailWait tw{tail, c, it + 1};
+          solve_body_staged(w, rec, lane, G, mask, (float)alpha, dual, vel, stage, &tw);
+        }
+        // the group's writes before lane 0's release of the body's progress
+        group_sync(G, mask);
+        if (lane == 0) st_release(&w.b.progress[rec.x], it + 1);
+      }
+      if (!grid_barrier(ctl, w.p.barrierLimit)) return;
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Dependency-driven wavefront schedule. Body i may run iteration t once every
+// neighbour of lower colour has completed iteration t and every neighbour of
+// higher colour has completed iteration t - 1: exactly the order of the colour
+// phases, without a grid-wide barrier between them. Each group walks its
+// bodies in increasing (iteration, colour) order, so the earliest unfinished
+// body always has its inputs ready and the schedule cannot deadlock while all
+// blocks are resident (cooperative launch). Every wait is bounded.
+// ---------------------------------------------------------------------------
+
+
 
 __global__ void __launch_bounds__(kSolveBlock, 3) wave_kernel(World w, int G) {
   extern __shared__ float4 stageSm[];
