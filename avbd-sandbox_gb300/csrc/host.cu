@@ -10,10 +10,15 @@
 // Manifold arenas are double-buffered and swapped on the host after each step.
 #include <algorithm>
 #include <cmath>
+#include <condition_variable>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
+#include <functional>
+#include <memory>
+#include <mutex>
 #include <string>
+#include <thread>
 #include <vector>
 
 #include "../../include/avbd_cuda.h"
@@ -32,6 +37,73 @@ struct DevBuf {
 };
 
 }  // namespace
+
+// Host worker threads for the per-body conversions of avbd_write_state and
+// avbd_read_state (memory-bound loops over every body's f64 arrays). Started
+// with the context, joined when it is destroyed; one call at a time (a
+// context is not thread-safe).
+class HostPool {
+ public:
+  explicit HostPool(int workers) {
+    for (int k = 1; k <= workers; k++) threads_.emplace_back([this, k] { loop(k); });
+  }
+  ~HostPool() {
+    {
+      std::lock_guard<std::mutex> g(m_);
+      stop_ = true;
+    }
+    wake_.notify_all();
+    for (auto &t : threads_) t.join();
+  }
+  int parts() const { return (int)threads_.size() + 1; }
+  // fn(part, begin, end) over [0, n) split into parts(); the caller runs part 0
+  void run(int n, const std::function<void(int, int, int)> &fn) {
+    {
+      std::lock_guard<std::mutex> g(m_);
+      fn_ = &fn;
+      n_ = n;
+      pending_ = (int)threads_.size();
+      gen_++;
+    }
+    wake_.notify_all();
+    fn(0, 0, range(0));
+    std::unique_lock<std::mutex> g(m_);
+    done_.wait(g, [this] { return pending_ == 0; });
+    fn_ = nullptr;
+  }
+
+ private:
+  int range(int part) const { return (int)((long long)n_ * (part + 1) / parts()); }
+  void loop(int k) {
+    uint64_t seen = 0;
+    for (;;) {
+      std::unique_lock<std::mutex> g(m_);
+      wake_.wait(g, [&] { return stop_ || gen_ != seen; });
+      if (stop_) return;
+      seen = gen_;
+      const auto *fn = fn_;
+      const int b = (int)((long long)n_ * k / parts()), e = range(k);
+      g.unlock();
+      (*fn)(k, b, e);
+      g.lock();
+      if (--pending_ == 0) done_.notify_one();
+    }
+  }
+  std::vector<std::thread> threads_;
+  std::mutex m_;
+  std::condition_variable wake_, done_;
+  const std::function<void(int, int, int)> *fn_ = nullptr;
+  int n_ = 0, pending_ = 0;
+  uint64_t gen_ = 0;
+  bool stop_ = false;
+};
+
+// fn(part, begin, end) over [0, n): in parts on the pool for large n.
+constexpr int kParallelBodies = 8192;
+void for_bodies(HostPool *pool, int n, const std::function<void(int, int, int)> &fn) {
+  if (pool && n >= kParallelBodies) pool->run(n, fn);
+  else fn(0, 0, n);
+}
 
 struct avbd_ctx {
   avbd_params params{};
@@ -70,6 +142,7 @@ struct avbd_ctx {
   // The host runs at most kRunAhead steps ahead of the device, so the
   // candidate count the regrow check reads is at most that many steps old.
   static constexpr int kRunAhead = 4;
+  std::unique_ptr<HostPool> pool;  // per-body host conversions
   cudaEvent_t stepEv[8]{};
   int64_t stepSeq = 0;
 };
@@ -231,18 +304,27 @@ int record(avbd_ctx *ctx, int k) {
 int write_state(avbd_ctx *ctx, const avbd_world *world, bool keepManifolds) {
   const avbd_body_soa &B = world->bodies;
   const int n = ctx->n;
-  for (int i = 0; i < n; i++) {
-    const double *p = &B.pos[i * 3];
-    if (!finite3(p)) return fail(ctx, AVBD_ERR_NAN, "body %d: non-finite position", i);
-    ctx->hPos[i] = mkd4(p[0], p[1], p[2], 0.0);
-    const double *q = B.quat ? &B.quat[i * 4] : nullptr;
-    ctx->hQuat[i] = q ? make_float4((float)q[0], (float)q[1], (float)q[2], (float)q[3]) : make_float4(0, 0, 0, 1);
-    auto v3 = [&](const double *a) { return a ? make_float4((float)a[i * 3], (float)a[i * 3 + 1], (float)a[i * 3 + 2], 0.f)
-                                              : make_float4(0, 0, 0, 0); };
-    ctx->hVel[i] = v3(B.vel);
-    ctx->hOmega[i] = v3(B.omega);
-    ctx->hPrev[i] = B.prev_vel ? v3(B.prev_vel) : ctx->hVel[i];
-  }
+  std::vector<int> bad(ctx->pool ? ctx->pool->parts() : 1, n);  // first non-finite body per part
+  for_bodies(ctx->pool.get(), n, [&](int part, int b, int e) {
+    for (int i = b; i < e; i++) {
+      const double *p = &B.pos[i * 3];
+      if (!finite3(p)) {
+        bad[part] = i;
+        return;
+      }
+      ctx->hPos[i] = mkd4(p[0], p[1], p[2], 0.0);
+      const double *q = B.quat ? &B.quat[i * 4] : nullptr;
+      ctx->hQuat[i] = q ? make_float4((float)q[0], (float)q[1], (float)q[2], (float)q[3]) : make_float4(0, 0, 0, 1);
+      auto v3 = [&](const double *a) {
+        return a ? make_float4((float)a[i * 3], (float)a[i * 3 + 1], (float)a[i * 3 + 2], 0.f) : make_float4(0, 0, 0, 0);
+      };
+      ctx->hVel[i] = v3(B.vel);
+      ctx->hOmega[i] = v3(B.omega);
+      ctx->hPrev[i] = B.prev_vel ? v3(B.prev_vel) : ctx->hVel[i];
+    }
+  });
+  const int firstBad = *std::min_element(bad.begin(), bad.end());
+  if (firstBad < n) return fail(ctx, AVBD_ERR_NAN, "body %d: non-finite position", firstBad);
   World &w = ctx->w;
   cudaStream_t st = ctx->stream;
   CK(cudaMemcpyAsync(w.b.pos, ctx->hPos, n * sizeof(D4), cudaMemcpyHostToDevice, st));
@@ -765,6 +847,10 @@ int avbd_pack(avbd_ctx *ctx, const avbd_world *world) {
   // launch shape of the persistent solve
   const int maxPerSm = solve_max_blocks_per_sm(ctx->lanes);
   ctx->autoLanes = P.lanes_per_body <= 0;
+  if (n >= kParallelBodies && !ctx->pool) {
+    const int hc = (int)std::thread::hardware_concurrency();
+    ctx->pool.reset(new HostPool(std::max(1, std::min(7, hc - 1))));
+  }
   ctx->lanes = P.lanes_per_body > 0 ? P.lanes_per_body : 32;
   ctx->nDyn = 0;
   for (int i = 0; i < n; i++) ctx->nDyn += B.mass[i] > 0 ? 1 : 0;
@@ -824,13 +910,15 @@ int avbd_read_state(avbd_ctx *ctx, avbd_world *out) {
   CK(cudaStreamSynchronize(st));
   const D4 *pos = ctx->hPos;
   const float4 *q = ctx->hQuat, *v = ctx->hVel, *om = ctx->hOmega, *pv = ctx->hPrev;
-  for (int i = 0; i < n; i++) {
-    if (B.pos) { B.pos[i * 3] = pos[i].x; B.pos[i * 3 + 1] = pos[i].y; B.pos[i * 3 + 2] = pos[i].z; }
-    if (B.quat) { B.quat[i * 4] = q[i].x; B.quat[i * 4 + 1] = q[i].y; B.quat[i * 4 + 2] = q[i].z; B.quat[i * 4 + 3] = q[i].w; }
-    if (B.vel) { B.vel[i * 3] = v[i].x; B.vel[i * 3 + 1] = v[i].y; B.vel[i * 3 + 2] = v[i].z; }
-    if (B.omega) { B.omega[i * 3] = om[i].x; B.omega[i * 3 + 1] = om[i].y; B.omega[i * 3 + 2] = om[i].z; }
-    if (B.prev_vel) { B.prev_vel[i * 3] = pv[i].x; B.prev_vel[i * 3 + 1] = pv[i].y; B.prev_vel[i * 3 + 2] = pv[i].z; }
-  }
+  for_bodies(ctx->pool.get(), n, [&](int, int b, int e) {
+    for (int i = b; i < e; i++) {
+      if (B.pos) { B.pos[i * 3] = pos[i].x; B.pos[i * 3 + 1] = pos[i].y; B.pos[i * 3 + 2] = pos[i].z; }
+      if (B.quat) { B.quat[i * 4] = q[i].x; B.quat[i * 4 + 1] = q[i].y; B.quat[i * 4 + 2] = q[i].z; B.quat[i * 4 + 3] = q[i].w; }
+      if (B.vel) { B.vel[i * 3] = v[i].x; B.vel[i * 3 + 1] = v[i].y; B.vel[i * 3 + 2] = v[i].z; }
+      if (B.omega) { B.omega[i * 3] = om[i].x; B.omega[i * 3 + 1] = om[i].y; B.omega[i * 3 + 2] = om[i].z; }
+      if (B.prev_vel) { B.prev_vel[i * 3] = pv[i].x; B.prev_vel[i * 3 + 1] = pv[i].y; B.prev_vel[i * 3 + 2] = pv[i].z; }
+    }
+  });
   avbd_joint_soa &J = out->joints;
   if (ctx->nj && J.count >= ctx->nj) {
     std::vector<float4> kl(ctx->nj), ka(ctx->nj);
