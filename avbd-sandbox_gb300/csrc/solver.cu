@@ -1380,12 +1380,25 @@ __device__ __forceinline__ void inertial_terms(const World &w, int i, const BSta
   inertial_core<T>(w.p, (T)md.x, (T)md.y, (T)md.z, (T)md.w, ld(&w.b.yLin[i]), ld(&w.b.yAng[i]), self, selfSphere, s);
 }
 
+__device__ inline int ld_acquire(const int *p) {
+  int v;
+  asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
+  return v;
+}
+__device__ inline void st_release(int *p, int v) {
+  asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
+}
+
 // Reduce the group's partial systems, solve the 6x6 system (maths.js:660-725),
 // integrate (maths.js:568-592) and publish the new iterate; on the last main
 // iteration also the BDF1 velocity (solver.js:476-488).
+// publish: lane 0 releases *publish = pubValue once the body's new state is
+// stored (what a later body of the tail segment reads of it), before the
+// velocity and the dual updates.
 template <class T>
 __device__ __forceinline__ void finish_body(const World &w, int i, int lane, int G, unsigned mask, bool velocity,
-                                            float4 qt, Sys<T> &s, BState<T> &self) {
+                                            float4 qt, Sys<T> &s, BState<T> &self, int *publish = nullptr,
+                                            int pubValue = 0) {
   const T dt = (T)w.p.dt;
   if constexpr (sizeof(T) == 4) {
     if (G == 32) group_reduce32(s);
@@ -1413,6 +1426,7 @@ __device__ __forceinline__ void finish_body(const World &w, int i, int lane, int
     stcg(&w.b.dpD[i], mkd4((double)self.dp.x, (double)self.dp.y, (double)self.dp.z, 0.0));
     stcg(&w.b.quatD[i], mkd4((double)self.q.x, (double)self.q.y, (double)self.q.z, (double)self.q.w));
   }
+  if (publish) st_release(publish, pubValue);
   if (velocity) {  // BDF1 (solver.js:476-488)
     w.b.prevVel[i] = ld(&w.b.vel[i]);
     w.b.vel[i] = make_float4((float)(self.dp.x / dt), (float)(self.dp.y / dt), (float)(self.dp.z / dt), 0.f);
@@ -1505,14 +1519,6 @@ __device__ __forceinline__ ContactData<float> staged_contact(const float4 *st, i
   return d;
 }
 
-__device__ inline int ld_acquire(const int *p) {
-  int v;
-  asm volatile("ld.acquire.gpu.global.b32 %0, [%1];" : "=r"(v) : "l"(p) : "memory");
-  return v;
-}
-__device__ inline void st_release(int *p, int v) {
-  asm volatile("st.release.gpu.global.b32 [%0], %1;" ::"l"(p), "r"(v) : "memory");
-}
 
 // The colour-phase solve's tail: the last colours (few bodies each) run as
 // one dependency-driven segment instead of one phase each. A tail body of
@@ -1650,7 +1656,10 @@ __device__ void solve_body_staged(const World &w, int4 rec, int lane, int G, uns
     if (tw) tail_wait_extra(w, nm, cStart, total, lane, G, *tw);
     s = constraints_primal<T>(w, nm, cStart, total, lane, G, self, alpha, s);
   }
-  finish_body<T>(w, i, lane, G, mask, velocity, qt, s, self);
+  // in the tail segment the body's progress is published as soon as its state is stored: the
+  // bodies waiting for it (higher colours) own every constraint they share with it, so they
+  // read nothing its dual updates write
+  finish_body<T>(w, i, lane, G, mask, velocity, qt, s, self, tw ? &w.b.progress[i] : nullptr, tw ? tw->need : 0);
   if (!dual) return;
   if (nk <= kStageSlots) {
     // every contact of this lane is still staged; the owner alone writes a
@@ -1792,13 +1801,12 @@ __global__ void __launch_bounds__(kSolveBlock, 3) solve_kernel(World w) {
           wait_neighbors(w, rec.x, it, lane, G, mask, tail);
           __syncwarp(mask);  // every lane's reads after the others' acquires
           solve_body_f64(w, rec, lane, G, mask, alpha, dual, vel);
+          group_sync(G, mask);  // the group's writes before lane 0's release
+          if (lane == 0) st_release(&w.b.progress[rec.x], it + 1);
         } else {
-          const TailWait tw{tail, c, it + 1};
+          const TailWait tw{tail, c, it + 1};  // publishes the body's progress itself
           solve_body_staged(w, rec, lane, G, mask, (float)alpha, dual, vel, stage, &tw);
         }
-        // the group's writes before lane 0's release of the body's progress
-        group_sync(G, mask);
-        if (lane == 0) st_release(&w.b.progress[rec.x], it + 1);
       }
       if (!grid_barrier(ctl, w.p.barrierLimit)) return;
     }
