@@ -378,6 +378,43 @@ def brick_wall(cols=16, rows=16, fracture=500.0, sphere_mass=50.0, sphere_speed=
     return s
 
 
+def brick_wall_c5(mu=0.6, sphere_velocity=(0.0, 8.0, 0.0), bond_stiffness=INF, cols=16, rows=16,
+                  sphere_mass=50.0, sphere_offset_z=0.1, gravity=-9.81):
+    """The differentiable wall: 16 x 16 bricks of 0.5 x 0.25 x 0.25 m (density
+    1000, friction `mu`) bonded by ball sockets with linear and angular rows of
+    stiffness `bond_stiffness` (hard by default) and no fracture, and a 50 kg
+    sphere of radius 0.3 m launched at `sphere_velocity`, its centre
+    `sphere_offset_z` above the wall's mid-height. Choices that keep the
+    objective differentiable in the f64 engine: the sphere off the seam between
+    rows 7 and 8 (on it, the sign of the vertical velocity decides which row
+    it strikes: a jump), and no fracture (a bond breaking is a jump). Finite
+    bonds ramp their penalty by beta |C| towards the stiffness and, at the
+    reference's ramp, never reach a cap of 1e4..1e6 within 60 steps while the
+    wall sags, so the stiffness has no derivative there; hard bonds have no
+    stiffness parameter (the penalty cap penalty_max stands in for it).
+    Bodies: ground, bricks row by row, then the sphere."""
+    s = Scene("brick_wall_c5")
+    add_ground(s, 0.5)
+    bw, bd, bh = 0.5, 0.25, 0.25
+    grid = [[None] * cols for _ in range(rows)]
+    k = float(bond_stiffness)
+    for r in range(rows):
+        for c in range(cols):
+            b = s.box((bw, bd, bh), 1000.0, float(mu), ((c - cols / 2) * bw, 0.0, bh / 2 + r * bh))
+            grid[r][c] = b
+            if c > 0:
+                s.joint(grid[r][c - 1], b, (bw / 2, 0.0, 0.0), (-bw / 2, 0.0, 0.0), k, k, INF)
+            if r > 0:
+                s.joint(grid[r - 1][c], b, (0.0, 0.0, bh / 2), (0.0, 0.0, -bh / 2), k, k, INF)
+    radius = 0.3
+    density = sphere_mass / ((4 / 3) * math.pi * radius ** 3)
+    s.sphere(2 * radius, density, 0.4, (0.0, -3.0, rows * bh * 0.5 + sphere_offset_z),
+             tuple(float(v) for v in sphere_velocity))
+    s.params = dict(gravity=gravity, iterations=10)
+    s.meta = dict(steps=60, bricks=(1, 1 + rows * cols))
+    return s
+
+
 def parity_scenes():
     """Small scenes with the content of the reference's parity list
     (test/parity/gen_scenes.mjs): ground, spinner, stack, stack_ratio,
