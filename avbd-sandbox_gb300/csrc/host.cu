@@ -3,8 +3,9 @@
 //
 // One context = one CUDA stream on the current device. A step is a fixed
 // launch sequence with all sizes resident on the device (no host round trip):
-//   broadphase (hash grid + candidate keys) -> narrowphase (f64 exact) ->
-//   prepare (forces, bodies, adjacency) -> colouring (cooperative) ->
+//   broadphase (hash grid + candidate keys) -> narrowphase (certified f32,
+//   f64 where a decision is not certain) -> prepare (forces, bodies,
+//   adjacency) -> colouring and the solve's lane layout (cooperative) ->
 //   solve (cooperative persistent: iterations x colours, fused dual,
 //   velocity) -> commit (x_{t+1} = x_t + delta in f64)
 // Manifold arenas are double-buffered and swapped on the host after each step.

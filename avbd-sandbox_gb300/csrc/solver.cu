@@ -12,10 +12,13 @@
 //
 // GB300 design:
 //   * the primal and dual iterations of a step are ONE cooperative persistent
-//     kernel; colour phases are separated by a bounded grid barrier
-//   * a group of `G` lanes assembles one body's 6x6 system (each lane takes a
-//     share of the incident constraints), reduces it with warp shuffles and
-//     every lane solves the LDL^T in registers
+//     kernel; colour phases are separated by a bounded grid barrier, and the
+//     last, thin colours run as one dependency-driven segment per iteration
+//   * a group of G lanes assembles one body's 6x6 system (each lane takes up
+//     to four of the incident constraints per staging round), reduces it with
+//     warp shuffles (2-4 warps: through shared memory) and every lane solves
+//     the LDL^T in registers; G (4..128) is chosen per body by the colouring,
+//     which lays out each colour's groups in 128-lane chunks
 //   * the dual update of a constraint is fused into the primal phase of its
 //     endpoint with the larger colour: both endpoints are final for the
 //     iteration at that moment, so this equals the reference's separate
