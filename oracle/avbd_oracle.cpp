@@ -23,9 +23,22 @@
  * be run in this build environment (there is no JavaScript runtime); the
  * oracle is pinned instead by the reference's closed-form tests
  * (test/analytic.mjs, test/fixtures.mjs, test/spheres.mjs), ported in tests/.
+ *
+ * Compiled with -DORC_TANGENT the same source is the tangent oracle: its
+ * scalar is a forward-mode dual number whose value runs the same double
+ * operations (values identical to the f64 build's) and which carries ND
+ * directional derivatives through the whole step - contact geometry, clamps
+ * and all - the exact derivative of the discrete step that an adjoint's
+ * gradient is checked against (orc_t_seed / orc_t_read_pos below).
  */
 
 #include "../include/avbd_cuda.h"
+
+// The tangent build's own namespace: no C++ symbol is shared with the f64
+// build, so both libraries can live in one process.
+#ifdef ORC_TANGENT
+#define orc orc_tangent
+#endif
 
 #include <algorithm>
 #include <cmath>
@@ -37,96 +50,186 @@
 
 namespace orc {
 
-static const double INF = std::numeric_limits<double>::infinity();
-static const double NaN = std::numeric_limits<double>::quiet_NaN();
+// The scalar of the restatement: double, or (built with -DORC_TANGENT, the
+// tangent oracle) a forward-mode dual number whose value part runs the very
+// same double operations and which carries ND directional derivatives.
+#ifdef ORC_TANGENT
+constexpr int ND = 5;
+struct Real {
+  double v;
+  double d[ND];
+  Real() : v(0), d{} {}
+  Real(double x) : v(x), d{} {}  // NOLINT: constants and inputs enter as values
+};
+inline Real make_real(double v, const double *d) {
+  Real r(v);
+  for (int k = 0; k < ND; k++) r.d[k] = d[k];
+  return r;
+}
+inline Real operator-(const Real &a) {
+  double d[ND];
+  for (int k = 0; k < ND; k++) d[k] = -a.d[k];
+  return make_real(-a.v, d);
+}
+inline Real operator+(const Real &a, const Real &b) {
+  double d[ND];
+  for (int k = 0; k < ND; k++) d[k] = a.d[k] + b.d[k];
+  return make_real(a.v + b.v, d);
+}
+inline Real operator-(const Real &a, const Real &b) {
+  double d[ND];
+  for (int k = 0; k < ND; k++) d[k] = a.d[k] - b.d[k];
+  return make_real(a.v - b.v, d);
+}
+inline Real operator*(const Real &a, const Real &b) {
+  double d[ND];
+  for (int k = 0; k < ND; k++) d[k] = a.d[k] * b.v + a.v * b.d[k];
+  return make_real(a.v * b.v, d);
+}
+inline Real operator/(const Real &a, const Real &b) {
+  const double q = a.v / b.v;
+  double d[ND];
+  for (int k = 0; k < ND; k++) d[k] = (a.d[k] - q * b.d[k]) / b.v;
+  return make_real(q, d);
+}
+inline Real operator+(const Real &a, double b) { return a + Real(b); }
+inline Real operator+(double a, const Real &b) { return Real(a) + b; }
+inline Real operator-(const Real &a, double b) { return a - Real(b); }
+inline Real operator-(double a, const Real &b) { return Real(a) - b; }
+inline Real operator*(const Real &a, double b) { return a * Real(b); }
+inline Real operator*(double a, const Real &b) { return Real(a) * b; }
+inline Real operator/(const Real &a, double b) { return a / Real(b); }
+inline Real operator/(double a, const Real &b) { return Real(a) / b; }
+inline Real &operator+=(Real &a, const Real &b) { return a = a + b; }
+inline Real &operator-=(Real &a, const Real &b) { return a = a - b; }
+inline Real &operator*=(Real &a, const Real &b) { return a = a * b; }
+inline Real &operator/=(Real &a, const Real &b) { return a = a / b; }
+#define ORC_CMP(op)                                                             \
+  inline bool operator op(const Real &a, const Real &b) { return a.v op b.v; } \
+  inline bool operator op(const Real &a, double b) { return a.v op b; }        \
+  inline bool operator op(double a, const Real &b) { return a op b.v; }
+ORC_CMP(<) ORC_CMP(>) ORC_CMP(<=) ORC_CMP(>=) ORC_CMP(==) ORC_CMP(!=)
+#undef ORC_CMP
+// At 0 the derivative of sqrt is taken as 0: the subgradient of the norm of a
+// vector that is and stays zero (a friction force inside the cone's tip).
+inline Real sqrt(const Real &a) {
+  const double r = std::sqrt(a.v);
+  double d[ND];
+  for (int k = 0; k < ND; k++) d[k] = r > 0 ? a.d[k] / (2.0 * r) : 0.0;
+  return make_real(r, d);
+}
+inline Real fabs(const Real &a) {
+  double d[ND];
+  for (int k = 0; k < ND; k++) d[k] = a.v < 0 ? -a.d[k] : a.d[k];
+  return make_real(std::fabs(a.v), d);
+}
+inline Real floor(const Real &a) { return Real(std::floor(a.v)); }
+inline bool isfinite(const Real &a) { return std::isfinite(a.v); }
+inline bool isnan(const Real &a) { return std::isnan(a.v); }
+inline bool signbit(const Real &a) { return std::signbit(a.v); }
+inline double val(const Real &a) { return a.v; }
+#else
+using Real = double;
+using std::fabs;
+using std::floor;
+using std::isfinite;
+using std::isnan;
+using std::signbit;
+using std::sqrt;
+inline double val(double a) { return a; }
+#endif
+inline int64_t floor_i64(const Real &a) { return (int64_t)std::floor(val(a)); }
+
+static const Real INF = std::numeric_limits<double>::infinity();
+static const Real NaN = std::numeric_limits<double>::quiet_NaN();
 
 // ---------------------------------------------------------------------------
 // Scalar helpers with JavaScript semantics (src/math/maths.js:34-44)
 // ---------------------------------------------------------------------------
 
 // Math.min / Math.max: NaN propagates, -0 < +0.
-static inline double js_min(double a, double b) {
+static inline Real js_min(Real a, Real b) {
   if (a != a || b != b) return NaN;
   if (a < b) return a;
   if (b < a) return b;
-  if (a == 0 && b == 0) return (std::signbit(a) || std::signbit(b)) ? -0.0 : 0.0;
+  if (a == 0 && b == 0) return (signbit(a) || signbit(b)) ? -0.0 : 0.0;
   return a;
 }
-static inline double js_max(double a, double b) {
+static inline Real js_max(Real a, Real b) {
   if (a != a || b != b) return NaN;
   if (a > b) return a;
   if (b > a) return b;
-  if (a == 0 && b == 0) return (!std::signbit(a) || !std::signbit(b)) ? 0.0 : -0.0;
+  if (a == 0 && b == 0) return (!signbit(a) || !signbit(b)) ? 0.0 : -0.0;
   return a;
 }
-static inline double sign(double x) { return x < 0 ? -1 : x > 0 ? 1 : 0; }
+static inline Real sign(Real x) { return x < 0 ? -1 : x > 0 ? 1 : 0; }
 // clamp(x, a, b) = Math.max(a, Math.min(b, x))  (maths.js:38-40)
-static inline double clamp(double x, double a, double b) { return js_max(a, js_min(b, x)); }
-static inline bool is_finite(double x) { return std::isfinite(x); }
+static inline Real clamp(Real x, Real a, Real b) { return js_max(a, js_min(b, x)); }
+static inline bool is_finite(Real x) { return isfinite(x); }
 
 // ---------------------------------------------------------------------------
 // vec3 (maths.js:50-193)
 // ---------------------------------------------------------------------------
-static inline void v3_set(double *o, double x, double y, double z) { o[0] = x; o[1] = y; o[2] = z; }
-static inline void v3_copy(double *o, const double *a) { o[0] = a[0]; o[1] = a[1]; o[2] = a[2]; }
-static inline void v3_zero(double *o) { o[0] = 0; o[1] = 0; o[2] = 0; }
-static inline void v3_add(double *o, const double *a, const double *b) {
+static inline void v3_set(Real *o, Real x, Real y, Real z) { o[0] = x; o[1] = y; o[2] = z; }
+static inline void v3_copy(Real *o, const Real *a) { o[0] = a[0]; o[1] = a[1]; o[2] = a[2]; }
+static inline void v3_zero(Real *o) { o[0] = 0; o[1] = 0; o[2] = 0; }
+static inline void v3_add(Real *o, const Real *a, const Real *b) {
   o[0] = a[0] + b[0]; o[1] = a[1] + b[1]; o[2] = a[2] + b[2];
 }
-static inline void v3_sub(double *o, const double *a, const double *b) {
+static inline void v3_sub(Real *o, const Real *a, const Real *b) {
   o[0] = a[0] - b[0]; o[1] = a[1] - b[1]; o[2] = a[2] - b[2];
 }
-static inline void v3_scale(double *o, const double *a, double s) {
+static inline void v3_scale(Real *o, const Real *a, Real s) {
   o[0] = a[0] * s; o[1] = a[1] * s; o[2] = a[2] * s;
 }
-static inline void v3_div(double *o, const double *a, double s) {
+static inline void v3_div(Real *o, const Real *a, Real s) {
   o[0] = a[0] / s; o[1] = a[1] / s; o[2] = a[2] / s;
 }
-static inline void v3_add_scaled(double *o, const double *a, double s) {
+static inline void v3_add_scaled(Real *o, const Real *a, Real s) {
   o[0] += a[0] * s; o[1] += a[1] * s; o[2] += a[2] * s;
 }
-static inline void v3_negate(double *o, const double *a) { o[0] = -a[0]; o[1] = -a[1]; o[2] = -a[2]; }
-static inline double v3_dot(const double *a, const double *b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
-static inline double v3_len_sq(const double *a) { return a[0] * a[0] + a[1] * a[1] + a[2] * a[2]; }
-static inline double v3_len(const double *a) { return std::sqrt(a[0] * a[0] + a[1] * a[1] + a[2] * a[2]); }
-static inline void v3_cross(double *o, const double *a, const double *b) {
-  const double ax = a[0], ay = a[1], az = a[2], bx = b[0], by = b[1], bz = b[2];
+static inline void v3_negate(Real *o, const Real *a) { o[0] = -a[0]; o[1] = -a[1]; o[2] = -a[2]; }
+static inline Real v3_dot(const Real *a, const Real *b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
+static inline Real v3_len_sq(const Real *a) { return a[0] * a[0] + a[1] * a[1] + a[2] * a[2]; }
+static inline Real v3_len(const Real *a) { return sqrt(a[0] * a[0] + a[1] * a[1] + a[2] * a[2]); }
+static inline void v3_cross(Real *o, const Real *a, const Real *b) {
+  const Real ax = a[0], ay = a[1], az = a[2], bx = b[0], by = b[1], bz = b[2];
   o[0] = ay * bz - az * by;
   o[1] = az * bx - ax * bz;
   o[2] = ax * by - ay * bx;
 }
-static inline void v3_abs(double *o, const double *a) {
-  o[0] = std::fabs(a[0]); o[1] = std::fabs(a[1]); o[2] = std::fabs(a[2]);
+static inline void v3_abs(Real *o, const Real *a) {
+  o[0] = fabs(a[0]); o[1] = fabs(a[1]); o[2] = fabs(a[2]);
 }
-static inline void v3_min_scalar(double *o, const double *a, double s) {
+static inline void v3_min_scalar(Real *o, const Real *a, Real s) {
   o[0] = js_min(a[0], s); o[1] = js_min(a[1], s); o[2] = js_min(a[2], s);
 }
-static inline void v3_clamp_scalar(double *o, const double *a, double lo, double hi) {
+static inline void v3_clamp_scalar(Real *o, const Real *a, Real lo, Real hi) {
   o[0] = clamp(a[0], lo, hi); o[1] = clamp(a[1], lo, hi); o[2] = clamp(a[2], lo, hi);
 }
 
 // ---------------------------------------------------------------------------
 // mat3, row-major (maths.js:199-435)
 // ---------------------------------------------------------------------------
-static inline void m3_zero(double *o) { for (int i = 0; i < 9; i++) o[i] = 0; }
-static inline void m3_copy(double *o, const double *a) { for (int i = 0; i < 9; i++) o[i] = a[i]; }
-static inline void m3_diagonal(double *o, double a, double b, double c) {
+static inline void m3_zero(Real *o) { for (int i = 0; i < 9; i++) o[i] = 0; }
+static inline void m3_copy(Real *o, const Real *a) { for (int i = 0; i < 9; i++) o[i] = a[i]; }
+static inline void m3_diagonal(Real *o, Real a, Real b, Real c) {
   o[0] = a; o[1] = 0; o[2] = 0; o[3] = 0; o[4] = b; o[5] = 0; o[6] = 0; o[7] = 0; o[8] = c;
 }
-static inline void m3_add_into(double *o, const double *a) { for (int i = 0; i < 9; i++) o[i] += a[i]; }
-static inline void m3_scale(double *o, const double *a, double s) { for (int i = 0; i < 9; i++) o[i] = a[i] * s; }
-static inline void m3_div(double *o, const double *a, double s) { for (int i = 0; i < 9; i++) o[i] = a[i] / s; }
-static inline void m3_negate(double *o, const double *a) { for (int i = 0; i < 9; i++) o[i] = -a[i]; }
-static inline void m3_get_row(double *o, const double *a, int r) { o[0] = a[r * 3]; o[1] = a[r * 3 + 1]; o[2] = a[r * 3 + 2]; }
-static inline void m3_mul_vec(double *o, const double *a, const double *v) {
-  const double x = v[0], y = v[1], z = v[2];
+static inline void m3_add_into(Real *o, const Real *a) { for (int i = 0; i < 9; i++) o[i] += a[i]; }
+static inline void m3_scale(Real *o, const Real *a, Real s) { for (int i = 0; i < 9; i++) o[i] = a[i] * s; }
+static inline void m3_div(Real *o, const Real *a, Real s) { for (int i = 0; i < 9; i++) o[i] = a[i] / s; }
+static inline void m3_negate(Real *o, const Real *a) { for (int i = 0; i < 9; i++) o[i] = -a[i]; }
+static inline void m3_get_row(Real *o, const Real *a, int r) { o[0] = a[r * 3]; o[1] = a[r * 3 + 1]; o[2] = a[r * 3 + 2]; }
+static inline void m3_mul_vec(Real *o, const Real *a, const Real *v) {
+  const Real x = v[0], y = v[1], z = v[2];
   o[0] = a[0] * x + a[1] * y + a[2] * z;
   o[1] = a[3] * x + a[4] * y + a[5] * z;
   o[2] = a[6] * x + a[7] * y + a[8] * z;
 }
-static inline void m3_mul(double *o, const double *a, const double *b) {
-  const double a0 = a[0], a1 = a[1], a2 = a[2], a3 = a[3], a4 = a[4], a5 = a[5], a6 = a[6], a7 = a[7], a8 = a[8];
-  const double b0 = b[0], b1 = b[1], b2 = b[2], b3 = b[3], b4 = b[4], b5 = b[5], b6 = b[6], b7 = b[7], b8 = b[8];
+static inline void m3_mul(Real *o, const Real *a, const Real *b) {
+  const Real a0 = a[0], a1 = a[1], a2 = a[2], a3 = a[3], a4 = a[4], a5 = a[5], a6 = a[6], a7 = a[7], a8 = a[8];
+  const Real b0 = b[0], b1 = b[1], b2 = b[2], b3 = b[3], b4 = b[4], b5 = b[5], b6 = b[6], b7 = b[7], b8 = b[8];
   o[0] = a0 * b0 + a1 * b3 + a2 * b6;
   o[1] = a0 * b1 + a1 * b4 + a2 * b7;
   o[2] = a0 * b2 + a1 * b5 + a2 * b8;
@@ -137,56 +240,56 @@ static inline void m3_mul(double *o, const double *a, const double *b) {
   o[7] = a6 * b1 + a7 * b4 + a8 * b7;
   o[8] = a6 * b2 + a7 * b5 + a8 * b8;
 }
-static inline void m3_mul_diag_right(double *o, const double *a, double d0, double d1, double d2) {
+static inline void m3_mul_diag_right(Real *o, const Real *a, Real d0, Real d1, Real d2) {
   o[0] = a[0] * d0; o[1] = a[1] * d1; o[2] = a[2] * d2;
   o[3] = a[3] * d0; o[4] = a[4] * d1; o[5] = a[5] * d2;
   o[6] = a[6] * d0; o[7] = a[7] * d1; o[8] = a[8] * d2;
 }
-static inline void m3_transpose(double *o, const double *a) {
-  const double a1 = a[1], a2 = a[2], a5 = a[5];
+static inline void m3_transpose(Real *o, const Real *a) {
+  const Real a1 = a[1], a2 = a[2], a5 = a[5];
   o[0] = a[0]; o[4] = a[4]; o[8] = a[8];
   o[1] = a[3]; o[3] = a1;
   o[2] = a[6]; o[6] = a2;
   o[5] = a[7]; o[7] = a5;
 }
-static inline void m3_outer(double *o, const double *a, const double *b) {
+static inline void m3_outer(Real *o, const Real *a, const Real *b) {
   o[0] = a[0] * b[0]; o[1] = a[0] * b[1]; o[2] = a[0] * b[2];
   o[3] = a[1] * b[0]; o[4] = a[1] * b[1]; o[5] = a[1] * b[2];
   o[6] = a[2] * b[0]; o[7] = a[2] * b[1]; o[8] = a[2] * b[2];
 }
-static inline void m3_skew(double *o, const double *r) {
-  const double rx = r[0], ry = r[1], rz = r[2];
+static inline void m3_skew(Real *o, const Real *r) {
+  const Real rx = r[0], ry = r[1], rz = r[2];
   o[0] = 0; o[1] = -rz; o[2] = ry;
   o[3] = rz; o[4] = 0; o[5] = -rx;
   o[6] = -ry; o[7] = rx; o[8] = 0;
 }
-static inline void m3_diagonalize(double *o, const double *m) {
-  const double c0 = std::sqrt(m[0] * m[0] + m[3] * m[3] + m[6] * m[6]);
-  const double c1 = std::sqrt(m[1] * m[1] + m[4] * m[4] + m[7] * m[7]);
-  const double c2 = std::sqrt(m[2] * m[2] + m[5] * m[5] + m[8] * m[8]);
+static inline void m3_diagonalize(Real *o, const Real *m) {
+  const Real c0 = sqrt(m[0] * m[0] + m[3] * m[3] + m[6] * m[6]);
+  const Real c1 = sqrt(m[1] * m[1] + m[4] * m[4] + m[7] * m[7]);
+  const Real c2 = sqrt(m[2] * m[2] + m[5] * m[5] + m[8] * m[8]);
   o[0] = c0; o[1] = 0; o[2] = 0; o[3] = 0; o[4] = c1; o[5] = 0; o[6] = 0; o[7] = 0; o[8] = c2;
 }
 // maths.js:389-414
-static inline void m3_orthonormal(double *o, const double *normal) {
-  const double nx = normal[0], ny = normal[1], nz = normal[2];
-  double t1x, t1y, t1z;
-  if (std::fabs(nx) > std::fabs(nz)) { t1x = -ny; t1y = nx; t1z = 0; }
+static inline void m3_orthonormal(Real *o, const Real *normal) {
+  const Real nx = normal[0], ny = normal[1], nz = normal[2];
+  Real t1x, t1y, t1z;
+  if (fabs(nx) > fabs(nz)) { t1x = -ny; t1y = nx; t1z = 0; }
   else { t1x = 0; t1y = -nz; t1z = ny; }
-  const double t1len = std::sqrt(t1x * t1x + t1y * t1y + t1z * t1z);
+  const Real t1len = sqrt(t1x * t1x + t1y * t1y + t1z * t1z);
   t1x /= t1len; t1y /= t1len; t1z /= t1len;
-  const double t2x = ny * t1z - nz * t1y;
-  const double t2y = nz * t1x - nx * t1z;
-  const double t2z = nx * t1y - ny * t1x;
+  const Real t2x = ny * t1z - nz * t1y;
+  const Real t2y = nz * t1x - nx * t1z;
+  const Real t2z = nx * t1y - ny * t1x;
   o[0] = nx; o[1] = ny; o[2] = nz;
   o[3] = t1x; o[4] = t1y; o[5] = t1z;
   o[6] = t2x; o[7] = t2y; o[8] = t2z;
 }
 // maths.js:417-434
-static inline void m3_from_quat(double *o, const double *q) {
-  const double x = q[0], y = q[1], z = q[2], w = q[3];
-  const double xx = x * x, yy = y * y, zz = z * z;
-  const double xy = x * y, xz = x * z, yz = y * z;
-  const double wx = w * x, wy = w * y, wz = w * z;
+static inline void m3_from_quat(Real *o, const Real *q) {
+  const Real x = q[0], y = q[1], z = q[2], w = q[3];
+  const Real xx = x * x, yy = y * y, zz = z * z;
+  const Real xy = x * y, xz = x * z, yz = y * z;
+  const Real wx = w * x, wy = w * y, wz = w * z;
   o[0] = 1 - 2 * (yy + zz);
   o[1] = 2 * (xy + wz);
   o[2] = 2 * (xz - wy);
@@ -201,83 +304,83 @@ static inline void m3_from_quat(double *o, const double *q) {
 // ---------------------------------------------------------------------------
 // quat (maths.js:441-627)
 // ---------------------------------------------------------------------------
-static inline void q_copy(double *o, const double *a) { o[0] = a[0]; o[1] = a[1]; o[2] = a[2]; o[3] = a[3]; }
-static inline void q_identity(double *o) { o[0] = 0; o[1] = 0; o[2] = 0; o[3] = 1; }
-static inline void q_conjugate(double *o, const double *q) { o[0] = -q[0]; o[1] = -q[1]; o[2] = -q[2]; o[3] = q[3]; }
+static inline void q_copy(Real *o, const Real *a) { o[0] = a[0]; o[1] = a[1]; o[2] = a[2]; o[3] = a[3]; }
+static inline void q_identity(Real *o) { o[0] = 0; o[1] = 0; o[2] = 0; o[3] = 1; }
+static inline void q_conjugate(Real *o, const Real *q) { o[0] = -q[0]; o[1] = -q[1]; o[2] = -q[2]; o[3] = q[3]; }
 // Eq. 20, maths.js:541-555
-static inline void q_subtract(double *o, const double *a, const double *b) {
-  const double lsq = b[0] * b[0] + b[1] * b[1] + b[2] * b[2] + b[3] * b[3];
-  const double ix = -b[0] / lsq, iy = -b[1] / lsq, iz = -b[2] / lsq, iw = b[3] / lsq;
-  const double ax = a[0], ay = a[1], az = a[2], aw = a[3];
+static inline void q_subtract(Real *o, const Real *a, const Real *b) {
+  const Real lsq = b[0] * b[0] + b[1] * b[1] + b[2] * b[2] + b[3] * b[3];
+  const Real ix = -b[0] / lsq, iy = -b[1] / lsq, iz = -b[2] / lsq, iw = b[3] / lsq;
+  const Real ax = a[0], ay = a[1], az = a[2], aw = a[3];
   o[0] = (aw * ix + ax * iw + ay * iz - az * iy) * 2;
   o[1] = (aw * iy - ax * iz + ay * iw + az * ix) * 2;
   o[2] = (aw * iz + ax * iy - ay * ix + az * iw) * 2;
 }
 // Eq. 21, maths.js:568-592 (the "0 * q" terms are kept: they fix -0 handling)
-static inline void q_integrate(double *o, const double *q, const double *dw) {
-  const double qx = q[0], qy = q[1], qz = q[2], qw = q[3];
-  const double wx = dw[0], wy = dw[1], wz = dw[2];
-  const double px = 0 * qx + wx * qw + wy * qz - wz * qy;
-  const double py = 0 * qy - wx * qz + wy * qw + wz * qx;
-  const double pz = 0 * qz + wx * qy - wy * qx + wz * qw;
-  const double pw = 0 * qw - wx * qx - wy * qy - wz * qz;
-  const double rx = qx + px * 0.5, ry = qy + py * 0.5, rz = qz + pz * 0.5, rw = qw + pw * 0.5;
-  const double len = std::sqrt(rx * rx + ry * ry + rz * rz + rw * rw);
+static inline void q_integrate(Real *o, const Real *q, const Real *dw) {
+  const Real qx = q[0], qy = q[1], qz = q[2], qw = q[3];
+  const Real wx = dw[0], wy = dw[1], wz = dw[2];
+  const Real px = 0 * qx + wx * qw + wy * qz - wz * qy;
+  const Real py = 0 * qy - wx * qz + wy * qw + wz * qx;
+  const Real pz = 0 * qz + wx * qy - wy * qx + wz * qw;
+  const Real pw = 0 * qw - wx * qx - wy * qy - wz * qz;
+  const Real rx = qx + px * 0.5, ry = qy + py * 0.5, rz = qz + pz * 0.5, rw = qw + pw * 0.5;
+  const Real len = sqrt(rx * rx + ry * ry + rz * rz + rw * rw);
   o[0] = rx / len; o[1] = ry / len; o[2] = rz / len; o[3] = rw / len;
 }
 // maths.js:599-613
-static inline void q_rotate(double *o, const double *q, const double *v) {
-  const double ux = q[0], uy = q[1], uz = q[2], w = q[3];
-  const double vx = v[0], vy = v[1], vz = v[2];
-  const double tx = (uy * vz - uz * vy) * 2;
-  const double ty = (uz * vx - ux * vz) * 2;
-  const double tz = (ux * vy - uy * vx) * 2;
+static inline void q_rotate(Real *o, const Real *q, const Real *v) {
+  const Real ux = q[0], uy = q[1], uz = q[2], w = q[3];
+  const Real vx = v[0], vy = v[1], vz = v[2];
+  const Real tx = (uy * vz - uz * vy) * 2;
+  const Real ty = (uz * vx - ux * vz) * 2;
+  const Real tz = (ux * vy - uy * vx) * 2;
   o[0] = vx + tx * w + (uy * tz - uz * ty);
   o[1] = vy + ty * w + (uz * tx - ux * tz);
   o[2] = vz + tz * w + (ux * ty - uy * tx);
 }
 // maths.js:621-627
-static inline void transform_point(double *o, const double *lin, const double *ang, const double *v) {
+static inline void transform_point(Real *o, const Real *lin, const Real *ang, const Real *v) {
   q_rotate(o, ang, v);
   o[0] += lin[0]; o[1] += lin[1]; o[2] += lin[2];
 }
 
 // maths.js:660-725, unrolled LDL^T of the 6x6 block system
-static void solve6(const double *aLin, const double *aAng, const double *aCross, const double *bLin,
-                   const double *bAng, double *xLin, double *xAng) {
-  const double A11 = aLin[0];
-  const double A21 = aLin[3], A22 = aLin[4];
-  const double A31 = aLin[6], A32 = aLin[7], A33 = aLin[8];
-  const double A41 = aCross[0], A42 = aCross[1], A43 = aCross[2], A44 = aAng[0];
-  const double A51 = aCross[3], A52 = aCross[4], A53 = aCross[5], A54 = aAng[3], A55 = aAng[4];
-  const double A61 = aCross[6], A62 = aCross[7], A63 = aCross[8], A64 = aAng[6], A65 = aAng[7], A66 = aAng[8];
+static void solve6(const Real *aLin, const Real *aAng, const Real *aCross, const Real *bLin,
+                   const Real *bAng, Real *xLin, Real *xAng) {
+  const Real A11 = aLin[0];
+  const Real A21 = aLin[3], A22 = aLin[4];
+  const Real A31 = aLin[6], A32 = aLin[7], A33 = aLin[8];
+  const Real A41 = aCross[0], A42 = aCross[1], A43 = aCross[2], A44 = aAng[0];
+  const Real A51 = aCross[3], A52 = aCross[4], A53 = aCross[5], A54 = aAng[3], A55 = aAng[4];
+  const Real A61 = aCross[6], A62 = aCross[7], A63 = aCross[8], A64 = aAng[6], A65 = aAng[7], A66 = aAng[8];
 
-  const double L21 = A21 / A11, L31 = A31 / A11, L41 = A41 / A11, L51 = A51 / A11, L61 = A61 / A11;
-  const double D1 = A11;
-  const double D2 = A22 - L21 * L21 * D1;
-  const double L32 = (A32 - L21 * L31 * D1) / D2;
-  const double L42 = (A42 - L21 * L41 * D1) / D2;
-  const double L52 = (A52 - L21 * L51 * D1) / D2;
-  const double L62 = (A62 - L21 * L61 * D1) / D2;
-  const double D3 = A33 - (L31 * L31 * D1 + L32 * L32 * D2);
-  const double L43 = (A43 - L31 * L41 * D1 - L32 * L42 * D2) / D3;
-  const double L53 = (A53 - L31 * L51 * D1 - L32 * L52 * D2) / D3;
-  const double L63 = (A63 - L31 * L61 * D1 - L32 * L62 * D2) / D3;
-  const double D4 = A44 - (L41 * L41 * D1 + L42 * L42 * D2 + L43 * L43 * D3);
-  const double L54 = (A54 - L41 * L51 * D1 - L42 * L52 * D2 - L43 * L53 * D3) / D4;
-  const double L64 = (A64 - L41 * L61 * D1 - L42 * L62 * D2 - L43 * L63 * D3) / D4;
-  const double D5 = A55 - (L51 * L51 * D1 + L52 * L52 * D2 + L53 * L53 * D3 + L54 * L54 * D4);
-  const double L65 = (A65 - L51 * L61 * D1 - L52 * L62 * D2 - L53 * L63 * D3 - L54 * L64 * D4) / D5;
-  const double D6 = A66 - (L61 * L61 * D1 + L62 * L62 * D2 + L63 * L63 * D3 + L64 * L64 * D4 + L65 * L65 * D5);
+  const Real L21 = A21 / A11, L31 = A31 / A11, L41 = A41 / A11, L51 = A51 / A11, L61 = A61 / A11;
+  const Real D1 = A11;
+  const Real D2 = A22 - L21 * L21 * D1;
+  const Real L32 = (A32 - L21 * L31 * D1) / D2;
+  const Real L42 = (A42 - L21 * L41 * D1) / D2;
+  const Real L52 = (A52 - L21 * L51 * D1) / D2;
+  const Real L62 = (A62 - L21 * L61 * D1) / D2;
+  const Real D3 = A33 - (L31 * L31 * D1 + L32 * L32 * D2);
+  const Real L43 = (A43 - L31 * L41 * D1 - L32 * L42 * D2) / D3;
+  const Real L53 = (A53 - L31 * L51 * D1 - L32 * L52 * D2) / D3;
+  const Real L63 = (A63 - L31 * L61 * D1 - L32 * L62 * D2) / D3;
+  const Real D4 = A44 - (L41 * L41 * D1 + L42 * L42 * D2 + L43 * L43 * D3);
+  const Real L54 = (A54 - L41 * L51 * D1 - L42 * L52 * D2 - L43 * L53 * D3) / D4;
+  const Real L64 = (A64 - L41 * L61 * D1 - L42 * L62 * D2 - L43 * L63 * D3) / D4;
+  const Real D5 = A55 - (L51 * L51 * D1 + L52 * L52 * D2 + L53 * L53 * D3 + L54 * L54 * D4);
+  const Real L65 = (A65 - L51 * L61 * D1 - L52 * L62 * D2 - L53 * L63 * D3 - L54 * L64 * D4) / D5;
+  const Real D6 = A66 - (L61 * L61 * D1 + L62 * L62 * D2 + L63 * L63 * D3 + L64 * L64 * D4 + L65 * L65 * D5);
 
-  const double y1 = bLin[0];
-  const double y2 = bLin[1] - L21 * y1;
-  const double y3 = bLin[2] - L31 * y1 - L32 * y2;
-  const double y4 = bAng[0] - L41 * y1 - L42 * y2 - L43 * y3;
-  const double y5 = bAng[1] - L51 * y1 - L52 * y2 - L53 * y3 - L54 * y4;
-  const double y6 = bAng[2] - L61 * y1 - L62 * y2 - L63 * y3 - L64 * y4 - L65 * y5;
+  const Real y1 = bLin[0];
+  const Real y2 = bLin[1] - L21 * y1;
+  const Real y3 = bLin[2] - L31 * y1 - L32 * y2;
+  const Real y4 = bAng[0] - L41 * y1 - L42 * y2 - L43 * y3;
+  const Real y5 = bAng[1] - L51 * y1 - L52 * y2 - L53 * y3 - L54 * y4;
+  const Real y6 = bAng[2] - L61 * y1 - L62 * y2 - L63 * y3 - L64 * y4 - L65 * y5;
 
-  const double z1 = y1 / D1, z2 = y2 / D2, z3 = y3 / D3, z4 = y4 / D4, z5 = y5 / D5, z6 = y6 / D6;
+  const Real z1 = y1 / D1, z2 = y2 / D2, z3 = y3 / D3, z4 = y4 / D4, z5 = y5 / D5, z6 = y6 / D6;
 
   xAng[2] = z6;
   xAng[1] = z5 - L65 * xAng[2];
@@ -306,29 +409,29 @@ struct Force;
 struct Body {
   int index = 0;
   int shape = AVBD_SHAPE_BOX;
-  double positionLin[3] = {0, 0, 0};
-  double positionAng[4] = {0, 0, 0, 1};
-  double initialLin[3] = {0, 0, 0};
-  double initialAng[4] = {0, 0, 0, 1};
-  double inertialLin[3] = {0, 0, 0};
-  double inertialAng[4] = {0, 0, 0, 1};
-  double velocityLin[3] = {0, 0, 0};
-  double velocityAng[3] = {0, 0, 0};
-  double prevVelocityLin[3] = {0, 0, 0};
-  double size[3] = {1, 1, 1};
-  double friction = 0.5;
-  double mass = 0;
-  double moment[3] = {0, 0, 0};
-  double radius = 0;
+  Real positionLin[3] = {0, 0, 0};
+  Real positionAng[4] = {0, 0, 0, 1};
+  Real initialLin[3] = {0, 0, 0};
+  Real initialAng[4] = {0, 0, 0, 1};
+  Real inertialLin[3] = {0, 0, 0};
+  Real inertialAng[4] = {0, 0, 0, 1};
+  Real velocityLin[3] = {0, 0, 0};
+  Real velocityAng[3] = {0, 0, 0};
+  Real prevVelocityLin[3] = {0, 0, 0};
+  Real size[3] = {1, 1, 1};
+  Real friction = 0.5;
+  Real mass = 0;
+  Real moment[3] = {0, 0, 0};
+  Real radius = 0;
   std::vector<Force *> forces; // creation order; iterate in reverse
 
   // rigid.js:228-247
-  void computeWorldMoment(double *out, bool rotated) const {
+  void computeWorldMoment(Real *out, bool rotated) const {
     if (!rotated || shape == AVBD_SHAPE_SPHERE) {
       m3_diagonal(out, moment[0], moment[1], moment[2]);
       return;
     }
-    double R[9], T[9];
+    Real R[9], T[9];
     m3_from_quat(R, positionAng);
     m3_transpose(R, R);
     m3_diagonal(T, moment[0], moment[1], moment[2]);
@@ -350,12 +453,12 @@ struct Force {
   virtual ~Force() {}
   virtual bool isBroken() const { return false; }
   virtual bool initialize() { return true; }
-  virtual void updatePrimal(Body *body, double alpha, double *lhsLin, double *lhsAng, double *lhsCross,
-                            double *rhsLin, double *rhsAng) = 0;
-  virtual void updateDual(double alpha) = 0;
-  virtual double maxLambda() const { return 0; }
-  virtual double maxPenalty() const { return 0; }
-  virtual double maxConstraintError() const { return 0; }
+  virtual void updatePrimal(Body *body, Real alpha, Real *lhsLin, Real *lhsAng, Real *lhsCross,
+                            Real *rhsLin, Real *rhsAng) = 0;
+  virtual void updateDual(Real alpha) = 0;
+  virtual Real maxLambda() const { return 0; }
+  virtual Real maxPenalty() const { return 0; }
+  virtual Real maxConstraintError() const { return 0; }
 };
 
 // rigid.js:250-259 (a manifold has no `broken` field, which reads falsy)
@@ -369,11 +472,11 @@ bool Body::constrainedTo(const Body *other) const {
 }
 
 struct Params {
-  double dt = 1.0 / 60.0, gravity = -10.0;
+  Real dt = 1.0 / 60.0, gravity = -10.0;
   int iterations = 10;
-  double betaLin = 1e4, betaAng = 100, alpha = 0.95, gamma = 0.999;
+  Real betaLin = 1e4, betaAng = 100, alpha = 0.95, gamma = 0.999;
   bool postStabilize = false;
-  double penaltyMin = 1, penaltyMax = 1e10, collisionMargin = 0.01, stickThreshold = 1e-5;
+  Real penaltyMin = 1, penaltyMax = 1e10, collisionMargin = 0.01, stickThreshold = 1e-5;
   bool rotatedInertia = true, springRamp = false, springGeometric = true, cachedJacobians = true;
   int broadphase = 0, hashThreshold = 150, bodyOrderMode = AVBD_ORDER_REFERENCE;
 };
@@ -383,18 +486,18 @@ struct Params {
 // ---------------------------------------------------------------------------
 static const int MAX_CONTACTS = 8;
 static const int MAX_POLY_VERTS = 16;
-static const double SAT_AXIS_EPSILON = 1.0e-6;
-static const double SPHERE_DISTANCE_EPSILON_SQ = 1.0e-20;
-static const double PLANE_EPSILON = 1.0e-5;
-static const double CONTACT_MERGE_DIST_SQ = 1.0e-6;
+static const Real SAT_AXIS_EPSILON = 1.0e-6;
+static const Real SPHERE_DISTANCE_EPSILON_SQ = 1.0e-20;
+static const Real PLANE_EPSILON = 1.0e-5;
+static const Real CONTACT_MERGE_DIST_SQ = 1.0e-6;
 static const int AXIS_FACE_A = 0, AXIS_FACE_B = 1, AXIS_EDGE = 2;
 
 struct Contact {
   uint32_t feature = 0;
-  double rA[3] = {0, 0, 0}, rB[3] = {0, 0, 0};
-  double C0[3] = {0, 0, 0}, penalty[3] = {0, 0, 0}, lambda[3] = {0, 0, 0};
+  Real rA[3] = {0, 0, 0}, rB[3] = {0, 0, 0};
+  Real C0[3] = {0, 0, 0}, penalty[3] = {0, 0, 0}, lambda[3] = {0, 0, 0};
   bool stick = false;
-  double C[3] = {0, 0, 0};
+  Real C[3] = {0, 0, 0};
   void copyFrom(const Contact &o) { *this = o; }
   void reset() {
     feature = 0;
@@ -404,43 +507,43 @@ struct Contact {
 };
 
 struct OBB {
-  double center[3], half[3], axis[3][3];
+  Real center[3], half[3], axis[3][3];
 };
 
 struct SatAxis {
   int type = 0, indexA = -1, indexB = -1;
-  double separation = 0;
-  double normalAB[3] = {0, 0, 0};
+  Real separation = 0;
+  Real normalAB[3] = {0, 0, 0};
   bool valid = false;
 };
 
 // The module-level scratch of collide.js, gathered in one object.
 struct Collider {
   OBB boxA, boxB;
-  double frameNormal[3], frameCenter[3], frameU[3], frameV[3], frameExtentU, frameExtentV;
-  double faceExtU, faceExtV;
-  double clip0[MAX_POLY_VERTS * 3], clip1[MAX_POLY_VERTS * 3], midpoints[MAX_CONTACTS * 3];
+  Real frameNormal[3], frameCenter[3], frameU[3], frameV[3], frameExtentU, frameExtentV;
+  Real faceExtU, faceExtV;
+  Real clip0[MAX_POLY_VERTS * 3], clip1[MAX_POLY_VERTS * 3], midpoints[MAX_CONTACTS * 3];
   int stateCount = 0;
 
   static void makeOBB(OBB &box, const Body &b) {
-    static const double ux[3] = {1, 0, 0}, uy[3] = {0, 1, 0}, uz[3] = {0, 0, 1};
+    static const Real ux[3] = {1, 0, 0}, uy[3] = {0, 1, 0}, uz[3] = {0, 0, 1};
     v3_copy(box.center, b.positionLin);
     v3_scale(box.half, b.size, 0.5);
     q_rotate(box.axis[0], b.positionAng, ux);
     q_rotate(box.axis[1], b.positionAng, uy);
     q_rotate(box.axis[2], b.positionAng, uz);
   }
-  static double absDot(const double *a, const double *b) { return std::fabs(v3_dot(a, b)); }
-  static void supportPoint(double *out, const OBB &box, const double *dir) {
-    const double sx = v3_dot(dir, box.axis[0]) >= 0 ? 1 : -1;
-    const double sy = v3_dot(dir, box.axis[1]) >= 0 ? 1 : -1;
-    const double sz = v3_dot(dir, box.axis[2]) >= 0 ? 1 : -1;
+  static Real absDot(const Real *a, const Real *b) { return fabs(v3_dot(a, b)); }
+  static void supportPoint(Real *out, const OBB &box, const Real *dir) {
+    const Real sx = v3_dot(dir, box.axis[0]) >= 0 ? 1 : -1;
+    const Real sy = v3_dot(dir, box.axis[1]) >= 0 ? 1 : -1;
+    const Real sz = v3_dot(dir, box.axis[2]) >= 0 ? 1 : -1;
     v3_copy(out, box.center);
     v3_add_scaled(out, box.axis[0], box.half[0] * sx);
     v3_add_scaled(out, box.axis[1], box.half[1] * sy);
     v3_add_scaled(out, box.axis[2], box.half[2] * sz);
   }
-  void getFaceAxes(const OBB &box, int axisIndex, double *u, double *v) {
+  void getFaceAxes(const OBB &box, int axisIndex, Real *u, Real *v) {
     if (axisIndex == 0) {
       v3_copy(u, box.axis[1]); v3_copy(v, box.axis[2]); faceExtU = box.half[1]; faceExtV = box.half[2];
     } else if (axisIndex == 1) {
@@ -449,8 +552,8 @@ struct Collider {
       v3_copy(u, box.axis[0]); v3_copy(v, box.axis[1]); faceExtU = box.half[0]; faceExtV = box.half[1];
     }
   }
-  void buildFaceFrame(const OBB &box, int axisIndex, const double *outwardNormal) {
-    const double s = v3_dot(outwardNormal, box.axis[axisIndex]) >= 0 ? 1 : -1;
+  void buildFaceFrame(const OBB &box, int axisIndex, const Real *outwardNormal) {
+    const Real s = v3_dot(outwardNormal, box.axis[axisIndex]) >= 0 ? 1 : -1;
     v3_scale(frameNormal, box.axis[axisIndex], s);
     v3_copy(frameCenter, box.center);
     v3_add_scaled(frameCenter, frameNormal, box.half[axisIndex]);
@@ -458,45 +561,45 @@ struct Collider {
     frameExtentU = faceExtU;
     frameExtentV = faceExtV;
   }
-  static int chooseIncidentFaceAxis(const OBB &box, const double *referenceNormal) {
+  static int chooseIncidentFaceAxis(const OBB &box, const Real *referenceNormal) {
     int axis = 0;
-    double best = -INF;
+    Real best = -INF;
     for (int i = 0; i < 3; i++) {
-      const double d = absDot(box.axis[i], referenceNormal);
+      const Real d = absDot(box.axis[i], referenceNormal);
       if (d > best) { best = d; axis = i; }
     }
     return axis;
   }
-  void buildIncidentFace(double *outVerts, const OBB &box, int axisIndex, const double *referenceNormal) {
-    double t0[3], t1[3], t2[3], t3[3];
-    const double s = v3_dot(box.axis[axisIndex], referenceNormal) > 0 ? -1 : 1;
+  void buildIncidentFace(Real *outVerts, const OBB &box, int axisIndex, const Real *referenceNormal) {
+    Real t0[3], t1[3], t2[3], t3[3];
+    const Real s = v3_dot(box.axis[axisIndex], referenceNormal) > 0 ? -1 : 1;
     v3_scale(t0, box.axis[axisIndex], s);
     v3_copy(t1, box.center);
     v3_add_scaled(t1, t0, box.half[axisIndex]);
     getFaceAxes(box, axisIndex, t2, t3);
-    const double eU = faceExtU, eV = faceExtV;
+    const Real eU = faceExtU, eV = faceExtV;
     for (int i = 0; i < 4; i++) {
-      const double su = (i == 0 || i == 3) ? 1 : -1;
-      const double sv = (i == 0 || i == 1) ? 1 : -1;
+      const Real su = (i == 0 || i == 3) ? 1 : -1;
+      const Real sv = (i == 0 || i == 1) ? 1 : -1;
       outVerts[i * 3 + 0] = t1[0] + t2[0] * (eU * su) + t3[0] * (eV * sv);
       outVerts[i * 3 + 1] = t1[1] + t2[1] * (eU * su) + t3[1] * (eV * sv);
       outVerts[i * 3 + 2] = t1[2] + t2[2] * (eU * su) + t3[2] * (eV * sv);
     }
   }
-  static int clipPolygonAgainstPlane(const double *inV, int inCount, const double *pn, double po, double *outV) {
+  static int clipPolygonAgainstPlane(const Real *inV, int inCount, const Real *pn, Real po, Real *outV) {
     if (inCount <= 0) return 0;
     int outCount = 0;
-    double ax = inV[(inCount - 1) * 3 + 0], ay = inV[(inCount - 1) * 3 + 1], az = inV[(inCount - 1) * 3 + 2];
-    double da = pn[0] * ax + pn[1] * ay + pn[2] * az - po;
+    Real ax = inV[(inCount - 1) * 3 + 0], ay = inV[(inCount - 1) * 3 + 1], az = inV[(inCount - 1) * 3 + 2];
+    Real da = pn[0] * ax + pn[1] * ay + pn[2] * az - po;
     for (int i = 0; i < inCount; i++) {
-      const double bx = inV[i * 3 + 0], by = inV[i * 3 + 1], bz = inV[i * 3 + 2];
-      const double db = pn[0] * bx + pn[1] * by + pn[2] * bz - po;
+      const Real bx = inV[i * 3 + 0], by = inV[i * 3 + 1], bz = inV[i * 3 + 2];
+      const Real db = pn[0] * bx + pn[1] * by + pn[2] * bz - po;
       const bool aInside = da <= PLANE_EPSILON;
       const bool bInside = db <= PLANE_EPSILON;
       if (aInside != bInside) {
-        double t = 0;
-        const double denom = da - db;
-        if (std::fabs(denom) > SAT_AXIS_EPSILON) t = clamp(da / denom, 0, 1);
+        Real t = 0;
+        const Real denom = da - db;
+        if (fabs(denom) > SAT_AXIS_EPSILON) t = clamp(da / denom, 0, 1);
         if (outCount < MAX_POLY_VERTS) {
           outV[outCount * 3 + 0] = ax + (bx - ax) * t;
           outV[outCount * 3 + 1] = ay + (by - ay) * t;
@@ -513,16 +616,16 @@ struct Collider {
     return outCount;
   }
   // collide.js:254-285
-  bool addContact(const Body &A, const Body &B, Contact *contacts, const double *xA, const double *xB, uint32_t key) {
-    const double mx = (xA[0] + xB[0]) * 0.5, my = (xA[1] + xB[1]) * 0.5, mz = (xA[2] + xB[2]) * 0.5;
+  bool addContact(const Body &A, const Body &B, Contact *contacts, const Real *xA, const Real *xB, uint32_t key) {
+    const Real mx = (xA[0] + xB[0]) * 0.5, my = (xA[1] + xB[1]) * 0.5, mz = (xA[2] + xB[2]) * 0.5;
     for (int i = 0; i < stateCount; i++) {
-      const double dx = mx - midpoints[i * 3 + 0], dy = my - midpoints[i * 3 + 1], dz = mz - midpoints[i * 3 + 2];
+      const Real dx = mx - midpoints[i * 3 + 0], dy = my - midpoints[i * 3 + 1], dz = mz - midpoints[i * 3 + 2];
       if (dx * dx + dy * dy + dz * dz < CONTACT_MERGE_DIST_SQ) return false;
     }
     if (stateCount >= MAX_CONTACTS) return false;
     Contact &c = contacts[stateCount];
     c.feature = key;
-    double inv[4], t[3];
+    Real inv[4], t[3];
     q_conjugate(inv, A.positionAng);
     v3_sub(t, xA, A.positionLin);
     q_rotate(c.rA, inv, t);
@@ -534,19 +637,19 @@ struct Collider {
     return true;
   }
   // collide.js:291-324
-  bool testAxis(const double *delta, const double *axis, int type, int indexA, int indexB, SatAxis &target) {
-    const double lenSq = v3_len_sq(axis);
+  bool testAxis(const Real *delta, const Real *axis, int type, int indexA, int indexB, SatAxis &target) {
+    const Real lenSq = v3_len_sq(axis);
     if (lenSq < SAT_AXIS_EPSILON) return true;
-    const double invLen = 1.0 / std::sqrt(lenSq);
-    double n[3];
+    const Real invLen = 1.0 / sqrt(lenSq);
+    Real n[3];
     v3_scale(n, axis, invLen);
     if (v3_dot(n, delta) < 0) v3_negate(n, n);
-    const double distance = std::fabs(v3_dot(delta, n));
-    const double rA = boxA.half[0] * absDot(n, boxA.axis[0]) + boxA.half[1] * absDot(n, boxA.axis[1]) +
+    const Real distance = fabs(v3_dot(delta, n));
+    const Real rA = boxA.half[0] * absDot(n, boxA.axis[0]) + boxA.half[1] * absDot(n, boxA.axis[1]) +
                       boxA.half[2] * absDot(n, boxA.axis[2]);
-    const double rB = boxB.half[0] * absDot(n, boxB.axis[0]) + boxB.half[1] * absDot(n, boxB.axis[1]) +
+    const Real rB = boxB.half[0] * absDot(n, boxB.axis[0]) + boxB.half[1] * absDot(n, boxB.axis[1]) +
                       boxB.half[2] * absDot(n, boxB.axis[2]);
-    const double separation = distance - (rA + rB);
+    const Real separation = distance - (rA + rB);
     if (separation > 0) return false;
     if (!target.valid || separation > target.separation) {
       target.valid = true;
@@ -556,11 +659,11 @@ struct Collider {
     }
     return true;
   }
-  static void supportEdge(const OBB &box, int axisIndex, const double *dir, double *edgeA, double *edgeB) {
+  static void supportEdge(const OBB &box, int axisIndex, const Real *dir, Real *edgeA, Real *edgeB) {
     const int axis1 = (axisIndex + 1) % 3, axis2 = (axisIndex + 2) % 3;
-    const double sign1 = v3_dot(dir, box.axis[axis1]) >= 0 ? 1 : -1;
-    const double sign2 = v3_dot(dir, box.axis[axis2]) >= 0 ? 1 : -1;
-    double t[3];
+    const Real sign1 = v3_dot(dir, box.axis[axis1]) >= 0 ? 1 : -1;
+    const Real sign2 = v3_dot(dir, box.axis[axis2]) >= 0 ? 1 : -1;
+    Real t[3];
     v3_copy(t, box.center);
     v3_add_scaled(t, box.axis[axis1], box.half[axis1] * sign1);
     v3_add_scaled(t, box.axis[axis2], box.half[axis2] * sign2);
@@ -570,15 +673,15 @@ struct Collider {
     v3_add_scaled(edgeB, box.axis[axisIndex], box.half[axisIndex]);
   }
   // collide.js:345-393
-  static void closestPointsOnSegments(const double *p0, const double *p1, const double *q0, const double *q1,
-                                      double *c0, double *c1) {
-    const double d1x = p1[0] - p0[0], d1y = p1[1] - p0[1], d1z = p1[2] - p0[2];
-    const double d2x = q1[0] - q0[0], d2y = q1[1] - q0[1], d2z = q1[2] - q0[2];
-    const double rx = p0[0] - q0[0], ry = p0[1] - q0[1], rz = p0[2] - q0[2];
-    const double a = d1x * d1x + d1y * d1y + d1z * d1z;
-    const double e = d2x * d2x + d2y * d2y + d2z * d2z;
-    const double f = d2x * rx + d2y * ry + d2z * rz;
-    double s = 0, t = 0;
+  static void closestPointsOnSegments(const Real *p0, const Real *p1, const Real *q0, const Real *q1,
+                                      Real *c0, Real *c1) {
+    const Real d1x = p1[0] - p0[0], d1y = p1[1] - p0[1], d1z = p1[2] - p0[2];
+    const Real d2x = q1[0] - q0[0], d2y = q1[1] - q0[1], d2z = q1[2] - q0[2];
+    const Real rx = p0[0] - q0[0], ry = p0[1] - q0[1], rz = p0[2] - q0[2];
+    const Real a = d1x * d1x + d1y * d1y + d1z * d1z;
+    const Real e = d2x * d2x + d2y * d2y + d2z * d2z;
+    const Real f = d2x * rx + d2y * ry + d2z * rz;
+    Real s = 0, t = 0;
     if (a <= SAT_AXIS_EPSILON && e <= SAT_AXIS_EPSILON) {
       v3_copy(c0, p0); v3_copy(c1, q0);
       return;
@@ -586,13 +689,13 @@ struct Collider {
     if (a <= SAT_AXIS_EPSILON) {
       t = clamp(f / e, 0, 1);
     } else {
-      const double c = d1x * rx + d1y * ry + d1z * rz;
+      const Real c = d1x * rx + d1y * ry + d1z * rz;
       if (e <= SAT_AXIS_EPSILON) {
         s = clamp(-c / a, 0, 1);
       } else {
-        const double b = d1x * d2x + d1y * d2y + d1z * d2z;
-        const double denom = a * e - b * b;
-        if (std::fabs(denom) > SAT_AXIS_EPSILON) s = clamp((b * f - c * e) / denom, 0, 1);
+        const Real b = d1x * d2x + d1y * d2y + d1z * d2z;
+        const Real denom = a * e - b * b;
+        if (fabs(denom) > SAT_AXIS_EPSILON) s = clamp((b * f - c * e) / denom, 0, 1);
         t = (b * s + f) / e;
         if (t < 0) { t = 0; s = clamp(-c / a, 0, 1); }
         else if (t > 1) { t = 1; s = clamp((b - c) / a, 0, 1); }
@@ -602,18 +705,18 @@ struct Collider {
     c1[0] = q0[0] + d2x * t; c1[1] = q0[1] + d2y * t; c1[2] = q0[2] + d2z * t;
   }
   // collide.js:403-472
-  int buildFaceManifold(const Body &A, const Body &B, bool referenceIsA, int referenceAxis, const double *normalAB,
+  int buildFaceManifold(const Body &A, const Body &B, bool referenceIsA, int referenceAxis, const Real *normalAB,
                         Contact *contacts) {
     const OBB &referenceBox = referenceIsA ? boxA : boxB;
     const OBB &incidentBox = referenceIsA ? boxB : boxA;
-    double t0[3];
+    Real t0[3];
     if (referenceIsA) v3_copy(t0, normalAB);
     else v3_negate(t0, normalAB);
     buildFaceFrame(referenceBox, referenceAxis, t0);
     const int incidentAxis = chooseIncidentFaceAxis(incidentBox, frameNormal);
     buildIncidentFace(clip0, incidentBox, incidentAxis, frameNormal);
     int count = 4;
-    double pn[3];
+    Real pn[3];
     v3_copy(pn, frameU);
     count = clipPolygonAgainstPlane(clip0, count, pn, v3_dot(pn, frameCenter) + frameExtentU, clip1);
     if (!count) return 0;
@@ -631,11 +734,11 @@ struct Collider {
     uint32_t featurePrefix = (uint32_t)(referenceIsA ? AXIS_FACE_A : AXIS_FACE_B) << 24;
     featurePrefix |= (uint32_t)(referenceAxis & 0xff) << 16;
     featurePrefix |= (uint32_t)(incidentAxis & 0xff) << 8;
-    double p[3], q[3], xA[3], xB[3];
+    Real p[3], q[3], xA[3], xB[3];
     for (int i = 0; i < count && stateCount < MAX_CONTACTS; i++) {
       p[0] = clip0[i * 3 + 0]; p[1] = clip0[i * 3 + 1]; p[2] = clip0[i * 3 + 2];
       v3_sub(q, p, frameCenter);
-      const double distance = v3_dot(q, frameNormal);
+      const Real distance = v3_dot(q, frameNormal);
       if (distance > PLANE_EPSILON) continue;
       v3_copy(q, p);
       v3_add_scaled(q, frameNormal, -distance);
@@ -644,7 +747,7 @@ struct Collider {
       addContact(A, B, contacts, xA, xB, featurePrefix | (uint32_t)(i & 0xff));
     }
     if (!stateCount) {
-      double neg[3];
+      Real neg[3];
       supportPoint(xA, boxA, normalAB);
       v3_negate(neg, normalAB);
       supportPoint(xB, boxB, neg);
@@ -653,8 +756,8 @@ struct Collider {
     return stateCount;
   }
   // collide.js:475-493
-  int buildEdgeContact(const Body &A, const Body &B, int axisA, int axisB, const double *normalAB, Contact *contacts) {
-    double neg[3], eA0[3], eA1[3], eB0[3], eB1[3], xA[3], xB[3];
+  int buildEdgeContact(const Body &A, const Body &B, int axisA, int axisB, const Real *normalAB, Contact *contacts) {
+    Real neg[3], eA0[3], eA1[3], eB0[3], eB1[3], xA[3], xB[3];
     v3_negate(neg, normalAB);
     supportEdge(boxA, axisA, normalAB, eA0, eA1);
     supportEdge(boxB, axisB, neg, eB0, eB1);
@@ -670,13 +773,13 @@ struct Collider {
     return stateCount;
   }
   // collide.js:496-520
-  int sphereSphere(const Body &A, const Body &B, Contact *contacts, double *basisOut) {
-    double delta[3], n[3], t[3], xA[3], xB[3];
+  int sphereSphere(const Body &A, const Body &B, Contact *contacts, Real *basisOut) {
+    Real delta[3], n[3], t[3], xA[3], xB[3];
     v3_sub(delta, B.positionLin, A.positionLin);
-    const double distanceSq = v3_len_sq(delta);
-    const double radiusSum = A.radius + B.radius;
+    const Real distanceSq = v3_len_sq(delta);
+    const Real radiusSum = A.radius + B.radius;
     if (distanceSq > radiusSum * radiusSum) return 0;
-    if (distanceSq > SPHERE_DISTANCE_EPSILON_SQ) v3_scale(n, delta, 1 / std::sqrt(distanceSq));
+    if (distanceSq > SPHERE_DISTANCE_EPSILON_SQ) v3_scale(n, delta, 1 / sqrt(distanceSq));
     else v3_set(n, 1, 0, 0);
     v3_negate(t, n);
     m3_orthonormal(basisOut, t);
@@ -689,38 +792,38 @@ struct Collider {
     return stateCount;
   }
   // collide.js:526-600
-  int sphereBox(const Body &A, const Body &B, Contact *contacts, double *basisOut, bool sphereIsA) {
+  int sphereBox(const Body &A, const Body &B, Contact *contacts, Real *basisOut, bool sphereIsA) {
     const Body &sphere = sphereIsA ? A : B;
     const Body &boxBody = sphereIsA ? B : A;
     makeOBB(boxA, boxBody);
-    double delta[3], closest[3], t3[3], n[3], t0[3], xA[3], xB[3];
+    Real delta[3], closest[3], t3[3], n[3], t0[3], xA[3], xB[3];
     v3_sub(delta, sphere.positionLin, boxA.center);
-    const double lx = v3_dot(delta, boxA.axis[0]);
-    const double ly = v3_dot(delta, boxA.axis[1]);
-    const double lz = v3_dot(delta, boxA.axis[2]);
-    const double cx = clamp(lx, -boxA.half[0], boxA.half[0]);
-    const double cy = clamp(ly, -boxA.half[1], boxA.half[1]);
-    const double cz = clamp(lz, -boxA.half[2], boxA.half[2]);
+    const Real lx = v3_dot(delta, boxA.axis[0]);
+    const Real ly = v3_dot(delta, boxA.axis[1]);
+    const Real lz = v3_dot(delta, boxA.axis[2]);
+    const Real cx = clamp(lx, -boxA.half[0], boxA.half[0]);
+    const Real cy = clamp(ly, -boxA.half[1], boxA.half[1]);
+    const Real cz = clamp(lz, -boxA.half[2], boxA.half[2]);
     v3_copy(closest, boxA.center);
     v3_add_scaled(closest, boxA.axis[0], cx);
     v3_add_scaled(closest, boxA.axis[1], cy);
     v3_add_scaled(closest, boxA.axis[2], cz);
     v3_sub(t3, sphere.positionLin, closest);
-    const double distanceSq = v3_len_sq(t3);
+    const Real distanceSq = v3_len_sq(t3);
     int featureAxis = 0;
     if (distanceSq > SPHERE_DISTANCE_EPSILON_SQ) {
-      const double distance = std::sqrt(distanceSq);
+      const Real distance = sqrt(distanceSq);
       if (distance > sphere.radius) return 0;
       v3_scale(n, t3, 1 / distance);
     } else {
-      const double gx = boxA.half[0] - std::fabs(lx);
-      const double gy = boxA.half[1] - std::fabs(ly);
-      const double gz = boxA.half[2] - std::fabs(lz);
+      const Real gx = boxA.half[0] - fabs(lx);
+      const Real gy = boxA.half[1] - fabs(ly);
+      const Real gz = boxA.half[2] - fabs(lz);
       featureAxis = gx < gy ? (gx < gz ? 0 : 2) : (gy < gz ? 1 : 2);
-      const double local = featureAxis == 0 ? lx : featureAxis == 1 ? ly : lz;
-      const double sgn = local >= 0 ? 1 : -1;
+      const Real local = featureAxis == 0 ? lx : featureAxis == 1 ? ly : lz;
+      const Real sgn = local >= 0 ? 1 : -1;
       v3_scale(n, boxA.axis[featureAxis], sgn);
-      const double gap = featureAxis == 0 ? gx : featureAxis == 1 ? gy : gz;
+      const Real gap = featureAxis == 0 ? gx : featureAxis == 1 ? gy : gz;
       v3_copy(closest, sphere.positionLin);
       v3_add_scaled(closest, n, gap);
     }
@@ -739,7 +842,7 @@ struct Collider {
     int sideY = ly < -boxA.half[1] ? 1 : ly > boxA.half[1] ? 2 : 0;
     int sideZ = lz < -boxA.half[2] ? 1 : lz > boxA.half[2] ? 2 : 0;
     if ((sideX | sideY | sideZ) == 0) {
-      const double local = featureAxis == 0 ? lx : featureAxis == 1 ? ly : lz;
+      const Real local = featureAxis == 0 ? lx : featureAxis == 1 ? ly : lz;
       const int side = local >= 0 ? 2 : 1;
       if (featureAxis == 0) sideX = side;
       else if (featureAxis == 1) sideY = side;
@@ -751,13 +854,13 @@ struct Collider {
     return stateCount;
   }
   // collide.js:612-685
-  int collide(const Body &A, const Body &B, Contact *contacts, double *basisOut) {
+  int collide(const Body &A, const Body &B, Contact *contacts, Real *basisOut) {
     const bool sA = A.shape == AVBD_SHAPE_SPHERE, sB = B.shape == AVBD_SHAPE_SPHERE;
     if (sA && sB) return sphereSphere(A, B, contacts, basisOut);
     if (sA || sB) return sphereBox(A, B, contacts, basisOut, sA);
     makeOBB(boxA, A);
     makeOBB(boxB, B);
-    double delta[3], axis[3], t0[3];
+    Real delta[3], axis[3], t0[3];
     v3_sub(delta, boxB.center, boxA.center);
     SatAxis bestFace, bestEdge, best;
     bestFace.separation = -INF; bestFace.valid = false;
@@ -774,7 +877,7 @@ struct Collider {
     if (!bestFace.valid) return 0;
     best = bestFace;
     if (bestEdge.valid) {
-      const double edgeRelTol = 0.95, edgeAbsTol = 0.01;
+      const Real edgeRelTol = 0.95, edgeAbsTol = 0.01;
       if (edgeRelTol * bestEdge.separation > bestFace.separation + edgeAbsTol) best = bestEdge;
     }
     v3_negate(t0, best.normalAB);
@@ -805,9 +908,9 @@ struct Solver {
 // ---------------------------------------------------------------------------
 // Manifold (src/physics/manifold.js)
 // ---------------------------------------------------------------------------
-static void transportComponents(double *out, const double *value, const double *oldB, const double *newB) {
-  const double x = value[0], y = value[1], z = value[2];
-  double r3[3];
+static void transportComponents(Real *out, const Real *value, const Real *oldB, const Real *newB) {
+  const Real x = value[0], y = value[1], z = value[2];
+  Real r3[3];
   for (int r = 0; r < 3; r++) {
     const int n = r * 3;
     r3[r] = x * (newB[n] * oldB[0] + newB[n + 1] * oldB[1] + newB[n + 2] * oldB[2]) +
@@ -816,13 +919,13 @@ static void transportComponents(double *out, const double *value, const double *
     out[r] = r3[r];
   }
 }
-static void transportPenalty(double *out, const double *value, const double *oldB, const double *newB) {
-  const double x = value[0], y = value[1], z = value[2];
+static void transportPenalty(Real *out, const Real *value, const Real *oldB, const Real *newB) {
+  const Real x = value[0], y = value[1], z = value[2];
   for (int r = 0; r < 3; r++) {
     const int n = r * 3;
-    const double dx = newB[n] * oldB[0] + newB[n + 1] * oldB[1] + newB[n + 2] * oldB[2];
-    const double dy = newB[n] * oldB[3] + newB[n + 1] * oldB[4] + newB[n + 2] * oldB[5];
-    const double dz = newB[n] * oldB[6] + newB[n + 1] * oldB[7] + newB[n + 2] * oldB[8];
+    const Real dx = newB[n] * oldB[0] + newB[n + 1] * oldB[1] + newB[n + 2] * oldB[2];
+    const Real dy = newB[n] * oldB[3] + newB[n + 1] * oldB[4] + newB[n + 2] * oldB[5];
+    const Real dz = newB[n] * oldB[6] + newB[n + 1] * oldB[7] + newB[n + 2] * oldB[8];
     out[r] = x * dx * dx + y * dy * dy + z * dz * dz;
   }
 }
@@ -830,14 +933,14 @@ static void transportPenalty(double *out, const double *value, const double *old
 struct Manifold : Force {
   Contact contacts[MAX_CONTACTS];
   Contact newContacts[MAX_CONTACTS];
-  double basis[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  Real basis[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
   int numContacts = 0;
-  double friction = 0;
-  double jacobians[MAX_CONTACTS * 18];
+  Real friction = 0;
+  Real jacobians[MAX_CONTACTS * 18];
   bool jacobiansValid = false;
   // _beginPass scratch
-  double dqALin[3], dqAAng[3], dqBLin[3], dqBAng[3], jALin[9], jBLin[9], jAAng[9], jBAng[9];
-  double K[9], Cv[3], F[3];
+  Real dqALin[3], dqAAng[3], dqBLin[3], dqBAng[3], jALin[9], jBLin[9], jAAng[9], jBAng[9];
+  Real K[9], Cv[3], F[3];
 
   Manifold() { kind = KIND_MANIFOLD; }
 
@@ -847,9 +950,9 @@ struct Manifold : Force {
     jacobiansValid = false;
     const bool hasSphere = A.shape == AVBD_SHAPE_SPHERE || B.shape == AVBD_SHAPE_SPHERE;
     const bool hadContacts = numContacts > 0;
-    double oldBasis[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+    Real oldBasis[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
     if (hasSphere && hadContacts) m3_copy(oldBasis, basis);
-    friction = std::sqrt(A.friction * B.friction);
+    friction = sqrt(A.friction * B.friction);
     for (int i = 0; i < MAX_CONTACTS; i++) newContacts[i].reset();
     const int newNum = solver->collider.collide(A, B, newContacts, basis);
     const bool basisCompatible =
@@ -857,7 +960,7 @@ struct Manifold : Force {
     for (int i = 0; i < newNum; i++) {
       for (int j = 0; j < numContacts; j++) {
         if (basisCompatible && newContacts[i].feature == contacts[j].feature) {
-          double nrA[3], nrB[3];
+          Real nrA[3], nrB[3];
           v3_copy(nrA, newContacts[i].rA);
           v3_copy(nrB, newContacts[i].rB);
           newContacts[i].copyFrom(contacts[j]);
@@ -878,7 +981,7 @@ struct Manifold : Force {
     const Params &P = solver->p;
     for (int i = 0; i < numContacts; i++) {
       Contact &c = contacts[i];
-      double xA[3], xB[3], d[3];
+      Real xA[3], xB[3], d[3];
       transform_point(xA, A.positionLin, A.positionAng, c.rA);
       transform_point(xB, B.positionLin, B.positionAng, c.rB);
       v3_sub(d, xA, xB);
@@ -895,9 +998,9 @@ struct Manifold : Force {
   }
 
   // manifold.js:325-350
-  static void angularBlocks(const double *rAW, const double *rBW, const double *jALin, const double *jBLin,
-                            double *jAAng, double *jBAng) {
-    double row[3], acc[3];
+  static void angularBlocks(const Real *rAW, const Real *rBW, const Real *jALin, const Real *jBLin,
+                            Real *jAAng, Real *jBAng) {
+    Real row[3], acc[3];
     for (int r = 0; r < 3; r++) {
       m3_get_row(row, jALin, r);
       v3_cross(acc, rAW, row);
@@ -917,29 +1020,29 @@ struct Manifold : Force {
     m3_negate(jBLin, basis);
     if (solver->p.cachedJacobians && !jacobiansValid) {
       for (int i = 0; i < numContacts; i++) {
-        double rAW[3], rBW[3];
+        Real rAW[3], rBW[3];
         q_rotate(rAW, A.initialAng, contacts[i].rA);
         q_rotate(rBW, B.initialAng, contacts[i].rB);
         angularBlocks(rAW, rBW, jALin, jBLin, jAAng, jBAng);
-        std::memcpy(&jacobians[i * 18], jAAng, sizeof(double) * 9);
-        std::memcpy(&jacobians[i * 18 + 9], jBAng, sizeof(double) * 9);
+        std::memcpy(&jacobians[i * 18], jAAng, sizeof(Real) * 9);
+        std::memcpy(&jacobians[i * 18 + 9], jBAng, sizeof(Real) * 9);
       }
       jacobiansValid = true;
     }
   }
   // manifold.js:358-409
-  bool evaluate(int i, double alpha) {
+  bool evaluate(int i, Real alpha) {
     Contact &c = contacts[i];
     if (solver->p.cachedJacobians) {
       for (int k = 0; k < 9; k++) { jAAng[k] = jacobians[i * 18 + k]; jBAng[k] = jacobians[i * 18 + 9 + k]; }
     } else {
-      double rAW[3], rBW[3];
+      Real rAW[3], rBW[3];
       q_rotate(rAW, bodyA->positionAng, c.rA);
       q_rotate(rBW, bodyB->positionAng, c.rB);
       angularBlocks(rAW, rBW, jALin, jBLin, jAAng, jBAng);
     }
     m3_diagonal(K, c.penalty[0], c.penalty[1], c.penalty[2]);
-    double acc[3];
+    Real acc[3];
     v3_scale(Cv, c.C0, 1 - alpha);
     m3_mul_vec(acc, jALin, dqALin); v3_add(Cv, Cv, acc);
     m3_mul_vec(acc, jBLin, dqBLin); v3_add(Cv, Cv, acc);
@@ -948,8 +1051,8 @@ struct Manifold : Force {
     m3_mul_vec(F, K, Cv);
     v3_add(F, F, c.lambda);
     F[0] = js_min(F[0], 0);
-    const double bounds = std::fabs(F[0]) * friction;
-    const double frictionScale = std::sqrt(F[1] * F[1] + F[2] * F[2]);
+    const Real bounds = fabs(F[0]) * friction;
+    const Real frictionScale = sqrt(F[1] * F[1] + F[2] * F[2]);
     if (frictionScale > bounds && frictionScale > 0) {
       F[1] *= bounds / frictionScale;
       F[2] *= bounds / frictionScale;
@@ -957,16 +1060,16 @@ struct Manifold : Force {
     return frictionScale <= bounds;
   }
   // manifold.js:411-445
-  void updatePrimal(Body *body, double alpha, double *lhsLin, double *lhsAng, double *lhsCross, double *rhsLin,
-                    double *rhsAng) override {
+  void updatePrimal(Body *body, Real alpha, Real *lhsLin, Real *lhsAng, Real *lhsCross, Real *rhsLin,
+                    Real *rhsAng) override {
     const bool isA = body == bodyA;
     beginPass();
-    double jLinT[9], jAngT[9], jAngTk[9], m0[9], acc[3];
+    Real jLinT[9], jAngT[9], jAngTk[9], m0[9], acc[3];
     for (int i = 0; i < numContacts; i++) {
       Contact &c = contacts[i];
       evaluate(i, alpha);
-      const double *jLin = isA ? jALin : jBLin;
-      const double *jAng = isA ? jAAng : jBAng;
+      const Real *jLin = isA ? jALin : jBLin;
+      const Real *jAng = isA ? jAAng : jBAng;
       m3_transpose(jLinT, jLin);
       m3_transpose(jAngT, jAng);
       m3_mul_diag_right(jAngTk, jAngT, c.penalty[0], c.penalty[1], c.penalty[2]);
@@ -984,7 +1087,7 @@ struct Manifold : Force {
     }
   }
   // manifold.js:447-491
-  void updateDual(double alpha) override {
+  void updateDual(Real alpha) override {
     const Params &P = solver->p;
     beginPass();
     for (int i = 0; i < numContacts; i++) {
@@ -992,34 +1095,34 @@ struct Manifold : Force {
       const bool within = evaluate(i, alpha);
       v3_copy(c.lambda, F);
       v3_copy(c.C, Cv);
-      if (F[0] < 0) c.penalty[0] = js_min(c.penalty[0] + P.betaLin * std::fabs(Cv[0]), P.penaltyMax);
+      if (F[0] < 0) c.penalty[0] = js_min(c.penalty[0] + P.betaLin * fabs(Cv[0]), P.penaltyMax);
       if (within) {
-        c.penalty[1] = js_min(c.penalty[1] + P.betaLin * std::fabs(Cv[1]), P.penaltyMax);
-        c.penalty[2] = js_min(c.penalty[2] + P.betaLin * std::fabs(Cv[2]), P.penaltyMax);
-        c.stick = std::sqrt(Cv[1] * Cv[1] + Cv[2] * Cv[2]) < P.stickThreshold;
+        c.penalty[1] = js_min(c.penalty[1] + P.betaLin * fabs(Cv[1]), P.penaltyMax);
+        c.penalty[2] = js_min(c.penalty[2] + P.betaLin * fabs(Cv[2]), P.penaltyMax);
+        c.stick = sqrt(Cv[1] * Cv[1] + Cv[2] * Cv[2]) < P.stickThreshold;
       } else if (bodyA->shape == AVBD_SHAPE_SPHERE || bodyB->shape == AVBD_SHAPE_SPHERE) {
         c.stick = false;
       }
     }
   }
-  double maxLambda() const override {
-    double m = 0;
+  Real maxLambda() const override {
+    Real m = 0;
     for (int i = 0; i < numContacts; i++) {
-      const double *l = contacts[i].lambda;
-      m = js_max(m, js_max(std::fabs(l[0]), js_max(std::fabs(l[1]), std::fabs(l[2]))));
+      const Real *l = contacts[i].lambda;
+      m = js_max(m, js_max(fabs(l[0]), js_max(fabs(l[1]), fabs(l[2]))));
     }
     return m;
   }
-  double maxPenalty() const override {
-    double m = 0;
+  Real maxPenalty() const override {
+    Real m = 0;
     for (int i = 0; i < numContacts; i++) {
-      const double *p = contacts[i].penalty;
+      const Real *p = contacts[i].penalty;
       m = js_max(m, js_max(p[0], js_max(p[1], p[2])));
     }
     return m;
   }
-  double maxConstraintError() const override {
-    double m = 0;
+  Real maxConstraintError() const override {
+    Real m = 0;
     for (int i = 0; i < numContacts; i++) m = js_max(m, js_max(0, -contacts[i].C[0]));
     return m;
   }
@@ -1028,7 +1131,7 @@ struct Manifold : Force {
 // ---------------------------------------------------------------------------
 // Joint (src/physics/joint.js)
 // ---------------------------------------------------------------------------
-static void geometricStiffnessBallSocket(double *out, int k, const double *v) {
+static void geometricStiffnessBallSocket(Real *out, int k, const Real *v) {
   m3_diagonal(out, -v[k], -v[k], -v[k]);
   out[0 * 3 + k] += v[0];
   out[1 * 3 + k] += v[1];
@@ -1036,33 +1139,33 @@ static void geometricStiffnessBallSocket(double *out, int k, const double *v) {
 }
 
 struct Joint : Force {
-  double rA[3], rB[3];
-  double stiffnessLin = INF, stiffnessAng = 0, fracture = INF;
+  Real rA[3], rB[3];
+  Real stiffnessLin = INF, stiffnessAng = 0, fracture = INF;
   bool broken = false;
-  double C0Lin[3] = {0, 0, 0}, C0Ang[3] = {0, 0, 0};
-  double penaltyLin[3] = {0, 0, 0}, penaltyAng[3] = {0, 0, 0};
-  double lambdaLin[3] = {0, 0, 0}, lambdaAng[3] = {0, 0, 0};
-  double CLin[3] = {0, 0, 0}, CAng[3] = {0, 0, 0};
-  double torqueArm = 0;
+  Real C0Lin[3] = {0, 0, 0}, C0Ang[3] = {0, 0, 0};
+  Real penaltyLin[3] = {0, 0, 0}, penaltyAng[3] = {0, 0, 0};
+  Real lambdaLin[3] = {0, 0, 0}, lambdaAng[3] = {0, 0, 0};
+  Real CLin[3] = {0, 0, 0}, CAng[3] = {0, 0, 0};
+  Real torqueArm = 0;
 
   Joint() { kind = KIND_JOINT; }
   bool isBroken() const override { return broken; }
   void setup() { // joint.js:108-112
-    const double *sA = bodyA ? bodyA->size : nullptr;
-    const double sx = (sA ? sA[0] : 0) + bodyB->size[0];
-    const double sy = (sA ? sA[1] : 0) + bodyB->size[1];
-    const double sz = (sA ? sA[2] : 0) + bodyB->size[2];
+    const Real *sA = bodyA ? bodyA->size : nullptr;
+    const Real sx = (sA ? sA[0] : 0) + bodyB->size[0];
+    const Real sy = (sA ? sA[1] : 0) + bodyB->size[1];
+    const Real sz = (sA ? sA[2] : 0) + bodyB->size[2];
     torqueArm = sx * sx + sy * sy + sz * sz;
   }
-  void evalLinear(double *out) const {
-    double pA[3], pB[3];
+  void evalLinear(Real *out) const {
+    Real pA[3], pB[3];
     if (bodyA) transform_point(pA, bodyA->positionLin, bodyA->positionAng, rA);
     else v3_copy(pA, rA);
     transform_point(pB, bodyB->positionLin, bodyB->positionAng, rB);
     v3_sub(out, pA, pB);
   }
-  void evalAngular(double *out) const {
-    static const double identity[4] = {0, 0, 0, 1};
+  void evalAngular(Real *out) const {
+    static const Real identity[4] = {0, 0, 0, 1};
     q_subtract(out, bodyA ? bodyA->positionAng : identity, bodyB->positionAng);
     v3_scale(out, out, torqueArm);
   }
@@ -1084,10 +1187,10 @@ struct Joint : Force {
     return !broken;
   }
   // joint.js:162-253
-  void updatePrimal(Body *body, double alpha, double *lhsLin, double *lhsAng, double *lhsCross, double *rhsLin,
-                    double *rhsAng) override {
+  void updatePrimal(Body *body, Real alpha, Real *lhsLin, Real *lhsAng, Real *lhsCross, Real *rhsLin,
+                    Real *rhsAng) override {
     const bool isA = body == bodyA;
-    double K[9], C[3], F[3], rW[3], r[3], jLin[9], jAng[9], jLinT[9], jAngT[9], jAngTk[9], m0[9], H[9], G[9], acc[3];
+    Real K[9], C[3], F[3], rW[3], r[3], jLin[9], jAng[9], jLinT[9], jAngT[9], jAngTk[9], m0[9], H[9], G[9], acc[3];
     if (v3_len_sq(penaltyLin) > 0) {
       m3_diagonal(K, penaltyLin[0], penaltyLin[1], penaltyLin[2]);
       evalLinear(C);
@@ -1106,7 +1209,7 @@ struct Joint : Force {
         m3_skew(jAng, rW);
         v3_negate(r, rW);
       }
-      const double k0 = penaltyLin[0], k1 = penaltyLin[1], k2 = penaltyLin[2];
+      const Real k0 = penaltyLin[0], k1 = penaltyLin[1], k2 = penaltyLin[2];
       m3_transpose(jLinT, jLin);
       m3_transpose(jAngT, jAng);
       m3_mul_diag_right(jAngTk, jAngT, k0, k1, k2);
@@ -1136,7 +1239,7 @@ struct Joint : Force {
       if (stiffnessAng == INF) v3_add_scaled(C, C0Ang, -alpha);
       m3_mul_vec(F, K, C);
       v3_add(F, F, lambdaAng);
-      const double s = isA ? torqueArm : -torqueArm;
+      const Real s = isA ? torqueArm : -torqueArm;
       m3_diagonal(jAng, s, s, s);
       m3_transpose(jAngT, jAng);
       m3_mul(m0, jAngT, K);
@@ -1147,9 +1250,9 @@ struct Joint : Force {
     }
   }
   // joint.js:255-317
-  void updateDual(double alpha) override {
+  void updateDual(Real alpha) override {
     const Params &P = solver->p;
-    double K[9], C[3], F[3], acc[3];
+    Real K[9], C[3], F[3], acc[3];
     if (v3_len_sq(penaltyLin) > 0) {
       m3_diagonal(K, penaltyLin[0], penaltyLin[1], penaltyLin[2]);
       evalLinear(C);
@@ -1183,46 +1286,46 @@ struct Joint : Force {
       broken = true;
     }
   }
-  double maxLambda() const override { return std::sqrt(js_max(v3_len_sq(lambdaLin), v3_len_sq(lambdaAng))); }
-  double maxPenalty() const override {
-    double m = penaltyLin[0];
+  Real maxLambda() const override { return sqrt(js_max(v3_len_sq(lambdaLin), v3_len_sq(lambdaAng))); }
+  Real maxPenalty() const override {
+    Real m = penaltyLin[0];
     m = js_max(m, penaltyLin[1]); m = js_max(m, penaltyLin[2]);
     m = js_max(m, penaltyAng[0]); m = js_max(m, penaltyAng[1]); m = js_max(m, penaltyAng[2]);
     return m;
   }
-  double maxConstraintError() const override { return std::sqrt(v3_len_sq(CLin)); }
+  Real maxConstraintError() const override { return sqrt(v3_len_sq(CLin)); }
 };
 
 // ---------------------------------------------------------------------------
 // Spring (src/physics/spring.js)
 // ---------------------------------------------------------------------------
 struct Spring : Force {
-  double rA[3], rB[3];
-  double stiffness = 0, rest = 0, penalty = 0, C = 0;
-  double tearStrain = INF;
+  Real rA[3], rB[3];
+  Real stiffness = 0, rest = 0, penalty = 0, C = 0;
+  Real tearStrain = INF;
   bool broken = false;
-  double peakStrain = 0;
+  Real peakStrain = 0;
   // _evaluate scratch (module-level in spring.js)
-  double d[3], n[3], rW[3];
+  Real d[3], n[3], rW[3];
 
   Spring() { kind = KIND_SPRING; }
   bool isBroken() const override { return broken; }
   bool rampEnabled() const { return solver->p.springRamp; }
   bool geometricEnabled() const { return solver->p.springGeometric; }
 
-  double evaluate() { // spring.js:447-458
-    double pA[3], pB[3];
+  Real evaluate() { // spring.js:447-458
+    Real pA[3], pB[3];
     transform_point(pA, bodyA->positionLin, bodyA->positionAng, rA);
     transform_point(pB, bodyB->positionLin, bodyB->positionAng, rB);
     v3_sub(d, pA, pB);
-    const double dLen = v3_len(d);
+    const Real dLen = v3_len(d);
     if (dLen <= 1.0e-6) return NaN;
     v3_div(n, d, dLen);
     return dLen - rest;
   }
-  bool updateTearing(double Cv) { // spring.js:461-470
+  bool updateTearing(Real Cv) { // spring.js:461-470
     if (rest <= 1.0e-6) return false;
-    const double strain = js_max(0, Cv / rest);
+    const Real strain = js_max(0, Cv / rest);
     peakStrain = js_max(peakStrain, strain);
     if (strain <= tearStrain) return false;
     broken = true;
@@ -1233,7 +1336,7 @@ struct Spring : Force {
   bool initialize() override { // spring.js:472-507
     if (broken) { penalty = 0; C = 0; return true; }
     if (is_finite(tearStrain)) {
-      const double Cv = evaluate();
+      const Real Cv = evaluate();
       if (!(Cv != Cv)) {
         C = Cv;
         if (updateTearing(Cv)) return true;
@@ -1248,17 +1351,17 @@ struct Spring : Force {
     penalty = js_min(penalty, stiffness);
     return stiffness > 0;
   }
-  void updatePrimal(Body *body, double alpha, double *lhsLin, double *lhsAng, double *lhsCross, double *rhsLin,
-                    double *rhsAng) override { // spring.js:509-553
+  void updatePrimal(Body *body, Real alpha, Real *lhsLin, Real *lhsAng, Real *lhsCross, Real *rhsLin,
+                    Real *rhsAng) override { // spring.js:509-553
     (void)alpha;
     (void)lhsCross;
     if (broken) return;
-    const double Cv = evaluate();
+    const Real Cv = evaluate();
     if (Cv != Cv) return;
     const bool isA = body == bodyA;
-    const double k = penalty;
-    const double f = k * Cv;
-    double jLin[3], jAng[3], m0[9];
+    const Real k = penalty;
+    const Real f = k * Cv;
+    Real jLin[3], jAng[3], m0[9];
     if (isA) {
       q_rotate(rW, bodyA->positionAng, rA);
       v3_copy(jLin, n);
@@ -1277,10 +1380,10 @@ struct Spring : Force {
     if (geometricEnabled()) stampGeometricStiffness(isA, f, lhsLin, lhsAng);
     C = Cv;
   }
-  void stampGeometricStiffness(bool isA, double f, double *lhsLin, double *lhsAng) { // spring.js:564-616
-    const double dLen = v3_len(d);
-    const double s = isA ? 1 : -1;
-    double P[9], S[9], Gll[9], Gla[9], Gal[9], Gaa[9], m0[9];
+  void stampGeometricStiffness(bool isA, Real f, Real *lhsLin, Real *lhsAng) { // spring.js:564-616
+    const Real dLen = v3_len(d);
+    const Real s = isA ? 1 : -1;
+    Real P[9], S[9], Gll[9], Gla[9], Gal[9], Gaa[9], m0[9];
     m3_outer(P, n, n);
     m3_negate(P, P);
     P[0] += 1; P[4] += 1; P[8] += 1;
@@ -1293,39 +1396,39 @@ struct Spring : Force {
     m3_mul(Gaa, S, P);
     m3_mul(Gaa, Gaa, S);
     m3_negate(Gaa, Gaa);
-    const double ndotr = v3_dot(n, rW);
+    const Real ndotr = v3_dot(n, rW);
     m3_outer(m0, rW, n);
     m0[0] -= ndotr; m0[4] -= ndotr; m0[8] -= ndotr;
     m3_scale(m0, m0, s);
     m3_add_into(Gaa, m0);
-    const double af = std::fabs(f);
+    const Real af = fabs(f);
     for (int c = 0; c < 3; c++) {
-      const double a0 = Gll[c], a1 = Gll[3 + c], a2 = Gll[6 + c];
-      const double a3 = Gal[c], a4 = Gal[3 + c], a5 = Gal[6 + c];
-      const double g = std::sqrt(a0 * a0 + a1 * a1 + a2 * a2 + a3 * a3 + a4 * a4 + a5 * a5) * af;
+      const Real a0 = Gll[c], a1 = Gll[3 + c], a2 = Gll[6 + c];
+      const Real a3 = Gal[c], a4 = Gal[3 + c], a5 = Gal[6 + c];
+      const Real g = sqrt(a0 * a0 + a1 * a1 + a2 * a2 + a3 * a3 + a4 * a4 + a5 * a5) * af;
       lhsLin[c * 3 + c] += g;
     }
     for (int c = 0; c < 3; c++) {
-      const double a0 = Gla[c], a1 = Gla[3 + c], a2 = Gla[6 + c];
-      const double a3 = Gaa[c], a4 = Gaa[3 + c], a5 = Gaa[6 + c];
-      const double g = std::sqrt(a0 * a0 + a1 * a1 + a2 * a2 + a3 * a3 + a4 * a4 + a5 * a5) * af;
+      const Real a0 = Gla[c], a1 = Gla[3 + c], a2 = Gla[6 + c];
+      const Real a3 = Gaa[c], a4 = Gaa[3 + c], a5 = Gaa[6 + c];
+      const Real g = sqrt(a0 * a0 + a1 * a1 + a2 * a2 + a3 * a3 + a4 * a4 + a5 * a5) * af;
       lhsAng[c * 3 + c] += g;
     }
   }
-  void updateDual(double alpha) override { // spring.js:618-634
+  void updateDual(Real alpha) override { // spring.js:618-634
     (void)alpha;
     if (broken) return;
-    const double Cv = evaluate();
+    const Real Cv = evaluate();
     if (Cv != Cv) return;
     C = Cv;
     if (is_finite(tearStrain) && updateTearing(Cv)) return;
     if (!rampEnabled()) return;
     const Params &P = solver->p;
-    penalty = js_min(penalty + P.betaLin * std::fabs(Cv), js_min(stiffness, P.penaltyMax));
+    penalty = js_min(penalty + P.betaLin * fabs(Cv), js_min(stiffness, P.penaltyMax));
   }
-  double maxLambda() const override { return broken ? 0 : std::fabs(penalty * C); }
-  double maxPenalty() const override { return broken ? 0 : penalty; }
-  double maxConstraintError() const override { return broken ? 0 : std::fabs(C); }
+  Real maxLambda() const override { return broken ? 0 : fabs(penalty * C); }
+  Real maxPenalty() const override { return broken ? 0 : penalty; }
+  Real maxConstraintError() const override { return broken ? 0 : fabs(C); }
 };
 
 Solver::~Solver() {
@@ -1347,21 +1450,21 @@ template <class Visit>
 static void for_each_pair_hash(const std::vector<Body *> &bodies, Visit &&visit) { // broadphase.js:47-215
   const int n = (int)bodies.size();
   if (n < 2) return;
-  double radiusSum = 0;
+  Real radiusSum = 0;
   for (int i = 0; i < n; i++) radiusSum += bodies[i]->radius;
-  const double meanRadius = radiusSum / n;
-  const double largeThreshold = js_max(meanRadius * 8, 1e-6);
-  const double inv = 1 / js_max(meanRadius * 2, 1e-4);
+  const Real meanRadius = radiusSum / n;
+  const Real largeThreshold = js_max(meanRadius * 8, 1e-6);
+  const Real inv = 1 / js_max(meanRadius * 2, 1e-4);
   std::vector<int32_t> large;
   int64_t insertions = 0;
   for (int i = 0; i < n; i++) {
     const Body &b = *bodies[i];
     if (b.radius > largeThreshold) { large.push_back(i); continue; }
-    const double r = b.radius;
-    const double *p = b.positionLin;
-    const int64_t nx = (int64_t)std::floor((p[0] + r) * inv) - (int64_t)std::floor((p[0] - r) * inv) + 1;
-    const int64_t ny = (int64_t)std::floor((p[1] + r) * inv) - (int64_t)std::floor((p[1] - r) * inv) + 1;
-    const int64_t nz = (int64_t)std::floor((p[2] + r) * inv) - (int64_t)std::floor((p[2] - r) * inv) + 1;
+    const Real r = b.radius;
+    const Real *p = b.positionLin;
+    const int64_t nx = floor_i64((p[0] + r) * inv) - floor_i64((p[0] - r) * inv) + 1;
+    const int64_t ny = floor_i64((p[1] + r) * inv) - floor_i64((p[1] - r) * inv) + 1;
+    const int64_t nz = floor_i64((p[2] + r) * inv) - floor_i64((p[2] - r) * inv) + 1;
     insertions += nx * ny * nz;
   }
   int64_t tableSize = 64;
@@ -1371,11 +1474,11 @@ static void for_each_pair_hash(const std::vector<Body *> &bodies, Visit &&visit)
   std::vector<int32_t> entries(std::max<int64_t>(insertions, 1));
   std::vector<int32_t> lastSeen(n, -1);
   auto cell_range = [&](const Body &b, int64_t *lo, int64_t *hi) {
-    const double r = b.radius;
-    const double *p = b.positionLin;
+    const Real r = b.radius;
+    const Real *p = b.positionLin;
     for (int a = 0; a < 3; a++) {
-      lo[a] = (int64_t)std::floor((p[a] - r) * inv);
-      hi[a] = (int64_t)std::floor((p[a] + r) * inv);
+      lo[a] = floor_i64((p[a] - r) * inv);
+      hi[a] = floor_i64((p[a] + r) * inv);
     }
   };
   for (int i = 0; i < n; i++) {
@@ -1519,17 +1622,17 @@ static int index_coloring(const Solver &s, std::vector<int32_t> &colorOf) {
 // Algorithm 1 (src/physics/solver.js:307-493)
 // ---------------------------------------------------------------------------
 static void step(Solver &s) {
-  const double dt = s.p.dt;
+  const Real dt = s.p.dt;
   std::vector<Body *> &bodies = s.bodies;
   const Params &P = s.p;
 
   // 1. broad phase
   std::vector<Force *> created;
   auto visit = [&](Body *A, Body *B) {
-    const double dx = A->positionLin[0] - B->positionLin[0];
-    const double dy = A->positionLin[1] - B->positionLin[1];
-    const double dz = A->positionLin[2] - B->positionLin[2];
-    const double r = A->radius + B->radius;
+    const Real dx = A->positionLin[0] - B->positionLin[0];
+    const Real dy = A->positionLin[1] - B->positionLin[1];
+    const Real dz = A->positionLin[2] - B->positionLin[2];
+    const Real r = A->radius + B->radius;
     if (dx * dx + dy * dy + dz * dz <= r * r && !A->constrainedTo(B)) {
       if (A->mass > 0 || B->mass > 0) {
         // Manifold.reinit (manifold.js:201-212) on a pooled manifold, or a new one
@@ -1584,17 +1687,17 @@ static void step(Solver &s) {
   }
 
   // 3. body initialisation (Eq. 2 + adaptive guess)
-  double gravityVec[3] = {0, 0, P.gravity};
+  Real gravityVec[3] = {0, 0, P.gravity};
   for (Body *b : bodies) {
-    double tmp[3];
+    Real tmp[3];
     v3_copy(b->inertialLin, b->positionLin);
     v3_add_scaled(b->inertialLin, b->velocityLin, dt);
     if (b->mass > 0) v3_add_scaled(b->inertialLin, gravityVec, dt * dt);
     v3_scale(tmp, b->velocityAng, dt);
     q_integrate(b->inertialAng, b->positionAng, tmp);
-    const double accelZ = (b->velocityLin[2] - b->prevVelocityLin[2]) / dt;
-    const double accelExt = accelZ * sign(P.gravity);
-    double accelWeight = clamp(accelExt / std::fabs(P.gravity), 0.0, 1.0);
+    const Real accelZ = (b->velocityLin[2] - b->prevVelocityLin[2]) / dt;
+    const Real accelExt = accelZ * sign(P.gravity);
+    Real accelWeight = clamp(accelExt / fabs(P.gravity), 0.0, 1.0);
     if (!is_finite(accelWeight)) accelWeight = 0.0;
     v3_copy(b->initialLin, b->positionLin);
     q_copy(b->initialAng, b->positionAng);
@@ -1620,16 +1723,16 @@ static void step(Solver &s) {
   }
 
   // 4. main loop
-  const double dt2 = dt * dt;
+  const Real dt2 = dt * dt;
   const int totalIterations = P.iterations + (P.postStabilize ? 1 : 0);
   std::vector<Force *> &forces = s.forces;
   for (int it = 0; it < totalIterations; it++) {
-    const double alpha = P.postStabilize ? (it < P.iterations ? 1.0 : 0.0) : P.alpha;
+    const Real alpha = P.postStabilize ? (it < P.iterations ? 1.0 : 0.0) : P.alpha;
     const int sweep = orderPtr ? (int)orderPtr->size() : (int)bodies.size();
     for (int si = 0; si < sweep; si++) {
       Body *b = orderPtr ? bodies[(*orderPtr)[si]] : bodies[bodies.size() - 1 - si];
       if (b->mass <= 0) continue;
-      double MLin[9], MAng[9], lhsLin[9], lhsAng[9], lhsCross[9], rhsLin[3], rhsAng[3], tmp[3], dq[3], dxLin[3],
+      Real MLin[9], MAng[9], lhsLin[9], lhsAng[9], lhsCross[9], rhsLin[3], rhsAng[3], tmp[3], dq[3], dxLin[3],
           dxAng[3];
       m3_diagonal(MLin, b->mass, b->mass, b->mass);
       b->computeWorldMoment(MAng, P.rotatedInertia);
@@ -1843,12 +1946,12 @@ int orc_read_state(orc_solver *o, avbd_world *w) {
   for (int i = 0; i < n; i++) {
     const Body *b = s.bodies[i];
     for (int k = 0; k < 3; k++) {
-      if (B.pos) B.pos[i * 3 + k] = b->positionLin[k];
-      if (B.vel) B.vel[i * 3 + k] = b->velocityLin[k];
-      if (B.omega) B.omega[i * 3 + k] = b->velocityAng[k];
-      if (B.prev_vel) B.prev_vel[i * 3 + k] = b->prevVelocityLin[k];
+      if (B.pos) B.pos[i * 3 + k] = val(b->positionLin[k]);
+      if (B.vel) B.vel[i * 3 + k] = val(b->velocityLin[k]);
+      if (B.omega) B.omega[i * 3 + k] = val(b->velocityAng[k]);
+      if (B.prev_vel) B.prev_vel[i * 3 + k] = val(b->prevVelocityLin[k]);
     }
-    if (B.quat) for (int k = 0; k < 4; k++) B.quat[i * 4 + k] = b->positionAng[k];
+    if (B.quat) for (int k = 0; k < 4; k++) B.quat[i * 4 + k] = val(b->positionAng[k]);
   }
   avbd_manifold_soa &M = w->manifolds;
   int m = 0, pos = 0;
@@ -1858,10 +1961,10 @@ int orc_read_state(orc_solver *o, avbd_world *w) {
       avbd_joint_soa &J = w->joints;
       if (j->id < J.count) {
         for (int k = 0; k < 3; k++) {
-          if (J.penalty_lin) J.penalty_lin[j->id * 3 + k] = j->penaltyLin[k];
-          if (J.penalty_ang) J.penalty_ang[j->id * 3 + k] = j->penaltyAng[k];
-          if (J.lambda_lin) J.lambda_lin[j->id * 3 + k] = j->lambdaLin[k];
-          if (J.lambda_ang) J.lambda_ang[j->id * 3 + k] = j->lambdaAng[k];
+          if (J.penalty_lin) J.penalty_lin[j->id * 3 + k] = val(j->penaltyLin[k]);
+          if (J.penalty_ang) J.penalty_ang[j->id * 3 + k] = val(j->penaltyAng[k]);
+          if (J.lambda_lin) J.lambda_lin[j->id * 3 + k] = val(j->lambdaLin[k]);
+          if (J.lambda_ang) J.lambda_ang[j->id * 3 + k] = val(j->lambdaAng[k]);
         }
         if (J.broken) J.broken[j->id] = j->broken ? 1 : 0;
         if (J.order) J.order[j->id] = pos;
@@ -1870,30 +1973,30 @@ int orc_read_state(orc_solver *o, avbd_world *w) {
       const Spring *sp = static_cast<const Spring *>(f);
       avbd_spring_soa &S = w->springs;
       if (sp->id < S.count) {
-        if (S.penalty) S.penalty[sp->id] = sp->penalty;
-        if (S.peak_strain) S.peak_strain[sp->id] = sp->peakStrain;
+        if (S.penalty) S.penalty[sp->id] = val(sp->penalty);
+        if (S.peak_strain) S.peak_strain[sp->id] = val(sp->peakStrain);
         if (S.broken) S.broken[sp->id] = sp->broken ? 1 : 0;
         if (S.order) S.order[sp->id] = pos;
       }
     } else {
       const Manifold *mf = static_cast<const Manifold *>(f);
       if (m < M.capacity) {
-        if (M.body_a) M.body_a[m] = mf->bodyA->index;
-        if (M.body_b) M.body_b[m] = mf->bodyB->index;
-        if (M.num_contacts) M.num_contacts[m] = mf->numContacts;
-        if (M.basis) for (int k = 0; k < 9; k++) M.basis[m * 9 + k] = mf->basis[k];
-        if (M.friction) M.friction[m] = mf->friction;
+        if (M.body_a) M.body_a[m] = val(mf->bodyA->index);
+        if (M.body_b) M.body_b[m] = val(mf->bodyB->index);
+        if (M.num_contacts) M.num_contacts[m] = val(mf->numContacts);
+        if (M.basis) for (int k = 0; k < 9; k++) M.basis[m * 9 + k] = val(mf->basis[k]);
+        if (M.friction) M.friction[m] = val(mf->friction);
         for (int i = 0; i < MAX_CONTACTS; i++) {
           const Contact &c = mf->contacts[i];
           const int slot = m * MAX_CONTACTS + i;
           if (M.feature) M.feature[slot] = i < mf->numContacts ? c.feature : 0;
           for (int k = 0; k < 3; k++) {
             const bool live = i < mf->numContacts;
-            if (M.r_a) M.r_a[slot * 3 + k] = live ? c.rA[k] : 0;
-            if (M.r_b) M.r_b[slot * 3 + k] = live ? c.rB[k] : 0;
-            if (M.c0) M.c0[slot * 3 + k] = live ? c.C0[k] : 0;
-            if (M.penalty) M.penalty[slot * 3 + k] = live ? c.penalty[k] : 0;
-            if (M.lambda) M.lambda[slot * 3 + k] = live ? c.lambda[k] : 0;
+            if (M.r_a) M.r_a[slot * 3 + k] = live ? val(c.rA[k]) : 0;
+            if (M.r_b) M.r_b[slot * 3 + k] = live ? val(c.rB[k]) : 0;
+            if (M.c0) M.c0[slot * 3 + k] = live ? val(c.C0[k]) : 0;
+            if (M.penalty) M.penalty[slot * 3 + k] = live ? val(c.penalty[k]) : 0;
+            if (M.lambda) M.lambda[slot * 3 + k] = live ? val(c.lambda[k]) : 0;
           }
           if (M.stick) M.stick[slot] = (i < mf->numContacts && c.stick) ? 1 : 0;
         }
@@ -1912,10 +2015,10 @@ int orc_read_state(orc_solver *o, avbd_world *w) {
     avbd_joint_soa &J = w->joints;
     if (j->id >= J.count) continue;
     for (int k = 0; k < 3; k++) {
-      if (J.penalty_lin) J.penalty_lin[j->id * 3 + k] = j->penaltyLin[k];
-      if (J.penalty_ang) J.penalty_ang[j->id * 3 + k] = j->penaltyAng[k];
-      if (J.lambda_lin) J.lambda_lin[j->id * 3 + k] = j->lambdaLin[k];
-      if (J.lambda_ang) J.lambda_ang[j->id * 3 + k] = j->lambdaAng[k];
+      if (J.penalty_lin) J.penalty_lin[j->id * 3 + k] = val(j->penaltyLin[k]);
+      if (J.penalty_ang) J.penalty_ang[j->id * 3 + k] = val(j->penaltyAng[k]);
+      if (J.lambda_lin) J.lambda_lin[j->id * 3 + k] = val(j->lambdaLin[k]);
+      if (J.lambda_ang) J.lambda_ang[j->id * 3 + k] = val(j->lambdaAng[k]);
     }
     if (J.broken) J.broken[j->id] = j->broken ? 1 : 0;
     if (J.order) J.order[j->id] = -1;
@@ -1973,7 +2076,7 @@ int orc_stats(orc_solver *o, avbd_stats *st) {
   const Solver &s = o->s;
   std::memset(st, 0, sizeof(*st));
   st->bodies = (int64_t)s.bodies.size();
-  double maxErr = 0, maxL = 0, maxP = 0;
+  Real maxErr = 0, maxL = 0, maxP = 0;
   for (const Force *f : s.forces) {
     if (f->kind == KIND_MANIFOLD) {
       st->manifolds++;
@@ -1988,9 +2091,9 @@ int orc_stats(orc_solver *o, avbd_stats *st) {
     if (f->kind == KIND_JOINT && static_cast<const Joint *>(f)->broken) st->joints_broken++;
   st->candidate_pairs = (int64_t)s.lastPairs.size();
   st->colors = s.lastNumColors;
-  st->max_constraint_error = maxErr;
-  st->max_lambda = maxL;
-  st->max_penalty = maxP;
+  st->max_constraint_error = val(maxErr);
+  st->max_lambda = val(maxL);
+  st->max_penalty = val(maxP);
   return AVBD_OK;
 }
 
@@ -2000,7 +2103,7 @@ int orc_read_joint(orc_solver *o, int32_t id, double *penalty_lin, double *lambd
     for (const Force *f : list)
       if (f->kind == KIND_JOINT && f->id == id) {
         const Joint *j = static_cast<const Joint *>(f);
-        for (int k = 0; k < 3; k++) { penalty_lin[k] = j->penaltyLin[k]; lambda_ang[k] = j->lambdaAng[k]; }
+        for (int k = 0; k < 3; k++) { penalty_lin[k] = val(j->penaltyLin[k]); lambda_ang[k] = val(j->lambdaAng[k]); }
         *broken = j->broken ? 1 : 0;
         return true;
       }
@@ -2010,6 +2113,7 @@ int orc_read_joint(orc_solver *o, int32_t id, double *penalty_lin, double *lambd
   return AVBD_ERR_ARG;
 }
 
+#ifndef ORC_TANGENT  // the f64 build's golden-vector helpers
 // World-space inertia of body i (rigid.js:228-247).
 int orc_world_moment(orc_solver *o, int32_t i, int32_t rotated, double *out9) {
   o->s.bodies[i]->computeWorldMoment(out9, rotated != 0);
@@ -2041,6 +2145,46 @@ void orc_quat_subtract(double *out3, const double *a, const double *b) { q_subtr
 void orc_quat_integrate(double *out4, const double *q, const double *dw) { q_integrate(out4, q, dw); }
 void orc_quat_rotate(double *out3, const double *q, const double *v) { q_rotate(out3, q, v); }
 void orc_orthonormal(double *out9, const double *n) { m3_orthonormal(out9, n); }
+#endif
 uint32_t orc_color_priority(uint32_t i) { return color_priority(i); }
+
+#ifdef ORC_TANGENT
+// The tangent oracle's inputs and outputs. A seed sets direction `dir`
+// (0..ND-1) of one input to 1, after orc_load:
+//   what 0: linear velocity component `comp` of body `index` (its previous
+//           velocity too: a scene starts with the two equal, rigid.js:51)
+//   what 1: the friction of body `index`
+//   what 2: the penalty cap penalty_max
+int orc_t_dims() { return ND; }
+int orc_t_seed(orc_solver *o, int32_t what, int32_t index, int32_t comp, int32_t dir) {
+  if (dir < 0 || dir >= ND) return AVBD_ERR_ARG;
+  Solver &s = o->s;
+  const bool body = what == 0 || what == 1;
+  if (body && (index < 0 || index >= (int32_t)s.bodies.size())) return AVBD_ERR_ARG;
+  if (what == 0) {
+    if (comp < 0 || comp > 2) return AVBD_ERR_ARG;
+    s.bodies[index]->velocityLin[comp].d[dir] = 1.0;
+    s.bodies[index]->prevVelocityLin[comp].d[dir] = 1.0;
+  } else if (what == 1) {
+    s.bodies[index]->friction.d[dir] = 1.0;
+  } else if (what == 2) {
+    s.p.penaltyMax.d[dir] = 1.0;
+  } else {
+    return AVBD_ERR_ARG;
+  }
+  return AVBD_OK;
+}
+// Body positions (n x 3) and their tangents (n x 3 x ND).
+int orc_t_read_pos(orc_solver *o, double *pos, double *tangents) {
+  const Solver &s = o->s;
+  for (size_t i = 0; i < s.bodies.size(); i++)
+    for (int k = 0; k < 3; k++) {
+      const Real &x = s.bodies[i]->positionLin[k];
+      pos[i * 3 + k] = x.v;
+      for (int d = 0; d < ND; d++) tangents[(i * 3 + k) * ND + d] = x.d[d];
+    }
+  return AVBD_OK;
+}
+#endif
 
 } // extern "C"

@@ -14,54 +14,79 @@ import numpy as np
 
 HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "liborc.so")
+LIB_TANGENT = os.path.join(HERE, "liborc_t.so")
 SRC = os.path.join(HERE, "avbd_oracle.cpp")
+FLAGS = ["g++", "-std=c++17", "-O2", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fast-math"]
 
 
 def build(force: bool = False) -> str:
     """Compile the oracle with the flags that keep it a faithful f64
     restatement: no FMA contraction, no fast-math."""
     if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < os.path.getmtime(SRC):
-        cmd = ["g++", "-std=c++17", "-O2", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fast-math",
-               "-o", LIB, SRC]
-        subprocess.check_call(cmd)
+        subprocess.check_call(FLAGS + ["-o", LIB, SRC])
     return LIB
 
 
+def build_tangent(force: bool = False) -> str:
+    """The tangent oracle: the same source with a forward-mode dual-number
+    scalar (-DORC_TANGENT), whose values follow the f64 build's operations."""
+    if force or not os.path.exists(LIB_TANGENT) or os.path.getmtime(LIB_TANGENT) < os.path.getmtime(SRC):
+        subprocess.check_call(FLAGS + ["-DORC_TANGENT", "-o", LIB_TANGENT, SRC])
+    return LIB_TANGENT
+
+
 _lib = None
+_lib_tangent = None
+
+
+def _bind(L, tangent=False):
+    vp = C.c_void_p
+    L.orc_create.restype = vp
+    L.orc_create.argtypes = [vp]
+    L.orc_destroy.argtypes = [vp]
+    for name in ("orc_load", "orc_read_state", "orc_set_params"):
+        getattr(L, name).argtypes = [vp, vp]
+    L.orc_step.argtypes = [vp, C.c_int32]
+    L.orc_set_body_order.argtypes = [vp, vp, C.c_int32]
+    L.orc_read_coloring.argtypes = [vp, vp, vp]
+    L.orc_priority_coloring.argtypes = [vp, vp, vp]
+    L.orc_index_coloring.argtypes = [vp, vp, vp]
+    L.orc_read_pairs.argtypes = [vp, vp, vp, C.c_int64, vp]
+    L.orc_stats.argtypes = [vp, vp]
+    L.orc_num_forces.argtypes = [vp, vp, vp, vp]
+    L.orc_read_joint.argtypes = [vp, C.c_int32, vp, vp, vp]
+    if tangent:
+        L.orc_t_dims.restype = C.c_int
+        L.orc_t_seed.argtypes = [vp, C.c_int32, C.c_int32, C.c_int32, C.c_int32]
+        L.orc_t_read_pos.argtypes = [vp, vp, vp]
+        return L
+    L.orc_world_moment.argtypes = [vp, C.c_int32, C.c_int32, vp]
+    L.orc_collide.argtypes = [vp, C.c_int32, C.c_int32, vp, vp, vp, vp]
+    L.orc_collide.restype = C.c_int
+    for name in ("orc_solve6",):
+        getattr(L, name).argtypes = [vp] * 7
+    for name in ("orc_quat_subtract", "orc_quat_integrate", "orc_quat_rotate"):
+        getattr(L, name).argtypes = [vp, vp, vp]
+    L.orc_orthonormal.argtypes = [vp, vp]
+    L.orc_color_priority.argtypes = [C.c_uint32]
+    L.orc_color_priority.restype = C.c_uint32
+    return L
 
 
 def lib():
     global _lib
     if _lib is None:
         build()
-        L = C.CDLL(LIB)
-        vp = C.c_void_p
-        L.orc_create.restype = vp
-        L.orc_create.argtypes = [vp]
-        L.orc_destroy.argtypes = [vp]
-        for name in ("orc_load", "orc_read_state", "orc_set_params"):
-            getattr(L, name).argtypes = [vp, vp]
-        L.orc_step.argtypes = [vp, C.c_int32]
-        L.orc_set_body_order.argtypes = [vp, vp, C.c_int32]
-        L.orc_read_coloring.argtypes = [vp, vp, vp]
-        L.orc_priority_coloring.argtypes = [vp, vp, vp]
-        L.orc_index_coloring.argtypes = [vp, vp, vp]
-        L.orc_read_pairs.argtypes = [vp, vp, vp, C.c_int64, vp]
-        L.orc_stats.argtypes = [vp, vp]
-        L.orc_num_forces.argtypes = [vp, vp, vp, vp]
-        L.orc_read_joint.argtypes = [vp, C.c_int32, vp, vp, vp]
-        L.orc_world_moment.argtypes = [vp, C.c_int32, C.c_int32, vp]
-        L.orc_collide.argtypes = [vp, C.c_int32, C.c_int32, vp, vp, vp, vp]
-        L.orc_collide.restype = C.c_int
-        for name in ("orc_solve6",):
-            getattr(L, name).argtypes = [vp] * 7
-        for name in ("orc_quat_subtract", "orc_quat_integrate", "orc_quat_rotate"):
-            getattr(L, name).argtypes = [vp, vp, vp]
-        L.orc_orthonormal.argtypes = [vp, vp]
-        L.orc_color_priority.argtypes = [C.c_uint32]
-        L.orc_color_priority.restype = C.c_uint32
-        _lib = L
+        _lib = _bind(C.CDLL(LIB))
     return _lib
+
+
+def lib_tangent():
+    global _lib_tangent
+    if _lib_tangent is None:
+        build_tangent()
+        _lib_tangent = _bind(C.CDLL(LIB_TANGENT), tangent=True)
+    return _lib_tangent
 
 
 def _p(a):
@@ -71,9 +96,11 @@ def _p(a):
 class Oracle:
     """One f64 CPU solver instance holding one scene."""
 
+    _library = staticmethod(lib)
+
     def __init__(self, params, world=None):
         self.params = params
-        self.L = lib()
+        self.L = self._library()
         self.h = self.L.orc_create(C.byref(params))
         self.world = None
         if world is not None:
@@ -210,3 +237,40 @@ def orthonormal(n):
 
 def color_priority(i):
     return lib().orc_color_priority(i)
+
+
+class TangentOracle(Oracle):
+    """The tangent oracle: the f64 restatement carrying `dims` forward-mode
+    directional derivatives through every operation of the step (values
+    identical to Oracle's). Inputs get a direction with the seed_* calls after
+    loading; positions() returns the positions and their derivatives along
+    each direction: the exact derivative of the discrete step, which central
+    differences only approximate."""
+
+    _library = staticmethod(lib_tangent)
+
+    @property
+    def dims(self) -> int:
+        return self.L.orc_t_dims()
+
+    def _seed(self, what, index, comp, direction):
+        if self.L.orc_t_seed(self.h, what, index, comp, direction) != 0:
+            raise ValueError(f"bad seed ({what}, {index}, {comp}, {direction})")
+
+    def seed_velocity(self, body, comp, direction):
+        """Linear velocity component `comp` of `body` (and its previous velocity)."""
+        self._seed(0, body, comp, direction)
+
+    def seed_friction(self, body, direction):
+        self._seed(1, body, 0, direction)
+
+    def seed_penalty_max(self, direction):
+        self._seed(2, 0, 0, direction)
+
+    def positions(self):
+        n = self.world.n_bodies
+        pos = np.zeros((n, 3))
+        tan = np.zeros((n, 3, self.dims))
+        self.L.orc_t_read_pos(self.h, _p(pos), _p(tan))
+        return pos, tan
+

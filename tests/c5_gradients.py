@@ -15,7 +15,7 @@ import importlib
 
 import numpy as np
 
-from oracle import Oracle
+from oracle import Oracle, TangentOracle
 
 NAMES = ("v0_x", "v0_y", "v0_z", "mu", "penalty_max")
 STEPS = 30  # the horizon whose differences converge (over 60 steps contact events flip within +-h)
@@ -34,6 +34,30 @@ def objective(abi, scenes, theta, steps: int) -> float:
     o.step(steps)
     b0, b1 = s.meta["bricks"]
     return float(np.linalg.norm(o.state().pos[b0:b1] - w.pos[b0:b1], axis=1).mean())
+
+
+def tangent_gradient(abi, scenes, theta, steps: int):
+    """The objective and its exact derivative along theta, from the tangent
+    oracle: the sphere's velocity components, every brick's friction and the
+    penalty cap each carry one direction."""
+    s = scenes.brick_wall_c5(mu=float(theta[3]), sphere_velocity=tuple(float(v) for v in theta[:3]))
+    params = abi.default_params(**s.params, penalty_max=float(theta[4]))
+    w = s.world()
+    o = TangentOracle(params, w)
+    sphere = w.n_bodies - 1
+    b0, b1 = s.meta["bricks"]
+    for k in range(3):
+        o.seed_velocity(sphere, k, k)
+    for b in range(b0, b1):
+        o.seed_friction(b, 3)
+    o.seed_penalty_max(4)
+    o.step(steps)
+    pos, tan = o.positions()
+    d = pos[b0:b1] - w.pos[b0:b1]
+    dist = np.linalg.norm(d, axis=1)
+    grad = np.einsum("ij,ijk->k", d / dist[:, None], tan[b0:b1]) / (b1 - b0)
+    grad[4] *= theta[4]  # per relative change of the cap, as the differences step it
+    return float(dist.mean()), grad
 
 
 def central_differences(abi, scenes, theta, steps: int, h: float) -> np.ndarray:

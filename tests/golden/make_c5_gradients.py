@@ -1,7 +1,8 @@
 """Writes tests/golden/c5_gradients.json (run from the repo root:
 `python tests/golden/make_c5_gradients.py`): the differentiable wall's
-objective and its central differences on the f64 oracle at the two steps of
-tests/c5_gradients.py, the reference of an adjoint's gradient."""
+objective, its central differences on the f64 oracle at the two steps of
+tests/c5_gradients.py, and its exact derivative from the tangent oracle: the
+reference of an adjoint's gradient."""
 import json
 import os
 import sys
@@ -20,7 +21,8 @@ def main():
     th = c5.theta0(abi)
     out = {"steps": c5.STEPS, "names": list(c5.NAMES), "theta": th.tolist(),
            "objective": c5.objective(abi, scenes, th, c5.STEPS),
-           "differences": {repr(h): c5.central_differences(abi, scenes, th, c5.STEPS, h).tolist() for h in c5.H}}
+           "differences": {repr(h): c5.central_differences(abi, scenes, th, c5.STEPS, h).tolist() for h in c5.H},
+           "tangent": c5.tangent_gradient(abi, scenes, th, c5.STEPS)[1].tolist()}
     with open(os.path.join(HERE, "c5_gradients.json"), "w") as f:
         json.dump(out, f, indent=1)
         f.write("\n")
