@@ -19,7 +19,6 @@ describe the CPU engine's behaviour too:
 import math
 
 import numpy as np
-import pytest
 
 from oracle import Oracle
 
