@@ -124,6 +124,10 @@ inline Real fabs(const Real &a) {
   return make_real(std::fabs(a.v), d);
 }
 inline Real floor(const Real &a) { return Real(std::floor(a.v)); }
+// Tangents the narrow phase's geometry is denied (orc_t_freeze): bit 0 the
+// contact bases, bit 1 the body-local anchors - what an adjoint that holds
+// the contact frames constant within a step would compute.
+static int g_freeze_geometry = 0;
 inline bool isfinite(const Real &a) { return std::isfinite(a.v); }
 inline bool isnan(const Real &a) { return std::isnan(a.v); }
 inline bool signbit(const Real &a) { return std::signbit(a.v); }
@@ -978,6 +982,16 @@ struct Manifold : Force {
     }
     numContacts = newNum;
     for (int i = 0; i < newNum; i++) contacts[i].copyFrom(newContacts[i]);
+#ifdef ORC_TANGENT
+    if (g_freeze_geometry & 1)
+      for (int k = 0; k < 9; k++) basis[k] = Real(val(basis[k]));
+    if (g_freeze_geometry & 2)
+      for (int i = 0; i < numContacts; i++)
+        for (int k = 0; k < 3; k++) {
+          contacts[i].rA[k] = Real(val(contacts[i].rA[k]));
+          contacts[i].rB[k] = Real(val(contacts[i].rB[k]));
+        }
+#endif
     const Params &P = solver->p;
     for (int i = 0; i < numContacts; i++) {
       Contact &c = contacts[i];
@@ -2156,6 +2170,7 @@ uint32_t orc_color_priority(uint32_t i) { return color_priority(i); }
 //   what 1: the friction of body `index`
 //   what 2: the penalty cap penalty_max
 int orc_t_dims() { return ND; }
+void orc_t_freeze(int32_t mode) { g_freeze_geometry = mode; }
 int orc_t_seed(orc_solver *o, int32_t what, int32_t index, int32_t comp, int32_t dir) {
   if (dir < 0 || dir >= ND) return AVBD_ERR_ARG;
   Solver &s = o->s;

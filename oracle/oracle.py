@@ -59,6 +59,7 @@ def _bind(L, tangent=False):
         L.orc_t_dims.restype = C.c_int
         L.orc_t_seed.argtypes = [vp, C.c_int32, C.c_int32, C.c_int32, C.c_int32]
         L.orc_t_read_pos.argtypes = [vp, vp, vp]
+        L.orc_t_freeze.argtypes = [C.c_int32]
         return L
     L.orc_world_moment.argtypes = [vp, C.c_int32, C.c_int32, vp]
     L.orc_collide.argtypes = [vp, C.c_int32, C.c_int32, vp, vp, vp, vp]
@@ -266,6 +267,13 @@ class TangentOracle(Oracle):
 
     def seed_penalty_max(self, direction):
         self._seed(2, 0, 0, direction)
+
+    @staticmethod
+    def freeze_geometry(mode: int):
+        """Deny the narrow phase's geometry its tangents in every tangent
+        oracle of the process (bit 0: contact bases, bit 1: body-local anchors;
+        0 restores the exact derivative)."""
+        lib_tangent().orc_t_freeze(mode)
 
     def positions(self):
         n = self.world.n_bodies

@@ -75,3 +75,20 @@ def test_tangent_values_follow_f64(name):
     sa, sb = a.state(), b.state()
     assert np.array_equal(sa.pos, sb.pos) and np.array_equal(sa.quat, sb.quat) and np.array_equal(sa.vel, sb.vel)
 
+
+
+def test_contact_geometry_tangents_matter():
+    """Why an adjoint must differentiate the narrow phase: holding the contact
+    bases and anchors constant within each step (C0 still following the poses)
+    moves the v0_y derivative by far more than the 5 % tolerance."""
+    from oracle import TangentOracle
+
+    abi, scenes = c5.modules()
+    th = c5.theta0(abi)
+    exact = c5.tangent_gradient(abi, scenes, th, c5.STEPS)[1]
+    try:
+        TangentOracle.freeze_geometry(3)
+        frozen = c5.tangent_gradient(abi, scenes, th, c5.STEPS)[1]
+    finally:
+        TangentOracle.freeze_geometry(0)
+    assert abs(frozen[1] - exact[1]) > 0.2 * abs(exact[1])
