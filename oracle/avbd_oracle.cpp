@@ -2162,6 +2162,21 @@ void orc_orthonormal(double *out9, const double *n) { m3_orthonormal(out9, n); }
 #endif
 uint32_t orc_color_priority(uint32_t i) { return color_priority(i); }
 
+// The normal row of every live contact's last evaluated constraint C (the
+// `contact.C` of manifold.js:479, what test/convergence.mjs:57-71 reads as
+// penetration), in force order; `count` returns the total.
+int orc_contact_normal_c(orc_solver *o, double *out, int64_t capacity, int64_t *count) {
+  int64_t k = 0;
+  for (const Force *f : o->s.forces) {
+    if (f->kind != KIND_MANIFOLD) continue;
+    const Manifold *m = static_cast<const Manifold *>(f);
+    for (int i = 0; i < m->numContacts; i++, k++)
+      if (out && k < capacity) out[k] = val(m->contacts[i].C[0]);
+  }
+  *count = k;
+  return AVBD_OK;
+}
+
 #ifdef ORC_TANGENT
 // The tangent oracle's inputs and outputs. A seed sets direction `dir`
 // (0..ND-1) of one input to 1, after orc_load:

@@ -55,6 +55,7 @@ def _bind(L, tangent=False):
     L.orc_stats.argtypes = [vp, vp]
     L.orc_num_forces.argtypes = [vp, vp, vp, vp]
     L.orc_read_joint.argtypes = [vp, C.c_int32, vp, vp, vp]
+    L.orc_contact_normal_c.argtypes = [vp, vp, C.c_int64, vp]
     if tangent:
         L.orc_t_dims.restype = C.c_int
         L.orc_t_seed.argtypes = [vp, C.c_int32, C.c_int32, C.c_int32, C.c_int32]
@@ -178,6 +179,14 @@ class Oracle:
         st = abi.Stats()
         self.L.orc_stats(self.h, C.byref(st))
         return st.as_dict()
+
+    def contact_normal_c(self):
+        """The normal row of every live contact's last evaluated constraint C."""
+        cnt = C.c_int64()
+        self.L.orc_contact_normal_c(self.h, None, 0, C.byref(cnt))
+        out = np.zeros(max(cnt.value, 1))
+        self.L.orc_contact_normal_c(self.h, _p(out), cnt.value, C.byref(cnt))
+        return out[:cnt.value]
 
     def joint(self, jid):
         pl = np.zeros(3)
