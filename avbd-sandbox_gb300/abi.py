@@ -28,7 +28,7 @@ ORDER_EXPLICIT = 1
 ORDER_PRIORITY = 2
 
 MAX_CONTACTS = 8
-MAX_COLORS = 64
+MAX_COLORS = 1024
 
 _d = C.POINTER(C.c_double)
 _i = C.POINTER(C.c_int32)
@@ -51,6 +51,7 @@ class Params(C.Structure):
         ("max_pairs_per_body", C.c_int32), ("max_adjacency", C.c_int32),
         ("lanes_per_body", C.c_int32), ("blocks_per_sm", C.c_int32),
         ("schedule", C.c_int32), ("grid_factor", C.c_int32),
+        ("neighbor_wait_limit", C.c_int32),
     ]
 
 

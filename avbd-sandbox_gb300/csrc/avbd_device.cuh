@@ -24,7 +24,10 @@ struct __align__(32) D4 {
 __host__ __device__ inline D4 mkd4(double x, double y, double z, double w) { return D4{x, y, z, w}; }
 
 constexpr int kMaxContacts = 8;
-constexpr int kMaxColors = 64;
+// Colours the device colouring can hold. The greedy colouring needs at most
+// (largest number of dynamic neighbours of a body) + 1; per-colour loops run
+// over the colours in use only.
+constexpr int kMaxColors = 1024;
 constexpr int kLaneBuckets = 8;     // log2 of the lanes of a body's group: 0..7
 constexpr int kLaneMaxGroup = 128;  // largest group: one solve block
 
@@ -83,6 +86,14 @@ struct Control {
   int colorBad;        // this step's uploaded colouring has a conflict
   int laneTotal;       // lanes of one iteration's colour phases (sum over bodies)
   int pad[4];
+  // Candidate overflow: a step whose candidate pairs exceed the arena is
+  // skipped as a whole (every kernel after the broad phase returns at once, so
+  // body, joint, spring and warm-start state stay as they were before the
+  // step), and so is every step queued after it until the host has regrown
+  // the arenas and queued the skipped steps again.
+  int skip;            // sticky: set by the broad phase, cleared by the host
+  int stepsSkipped;    // steps skipped since the host last cleared `skip`
+  int wantCandidates;  // candidate pairs the last broad phase found (may exceed the arena)
 };
 
 struct Bodies {
@@ -208,7 +219,7 @@ struct Adjacency {
   int *hpEntry;      // per body, within its manifold range: dynamic neighbours of higher colouring priority
   int *hpCount;      // n
   const int *colorOverride;  // uploaded colours (avbd_set_coloring), or null
-  int *colorStart;   // kMaxColors + 1
+  int *colorStart;   // kMaxColors + 1 (entries past the colours in use hold the total)
   int *colorBodies;  // dynamic bodies sorted by (colour, index)
   int4 *colorRec;    // per colour position: body, contact range begin, end, 0
   int *blockHist;    // colouring counting sort scratch

@@ -426,13 +426,17 @@ __global__ void large_extra_kernel(World w) {
   sort_segment(seg, n);
 }
 
+// The step's candidate count; a step whose candidates exceed the arena (or
+// that follows a skipped step) is skipped: no candidate reaches the narrow
+// phase and every later kernel of the step returns at once (Control::skip).
 __global__ void finish_kernel(World w) {
-  int total = w.g.pairStart[w.b.n];
+  const int total = w.g.pairStart[w.b.n];
+  w.ctl->wantCandidates = total;
   if (total > w.g.candCap) {
     atomicOr(&w.ctl->flags, kOvfPairs);
-    total = w.g.candCap;
+    w.ctl->skip = 1;
   }
-  w.ctl->numCandidates = total;
+  w.ctl->numCandidates = w.ctl->skip ? 0 : total;
 }
 
 __global__ void prev_index_kernel(World w) {

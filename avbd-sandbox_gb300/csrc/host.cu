@@ -133,7 +133,8 @@ struct avbd_ctx {
   // pinned staging of the per-step body state (upload / readback)
   D4 *hPos = nullptr;
   float4 *hQuat = nullptr, *hVel = nullptr, *hOmega = nullptr, *hPrev = nullptr;
-  // candidate count of the latest completed step (pinned, written by the stream)
+  // of the latest completed step (pinned, written by the stream): [0] steps
+  // skipped for a candidate overflow since the last regrow, [1] candidates
   int *hCand = nullptr;
   bool autoLanes = false;  // lanes_per_body 0: chosen per body by the colouring
   int nDyn = 0;
@@ -248,21 +249,13 @@ int alloc_candidate_arenas(avbd_ctx *ctx, int cap) {
   return AVBD_OK;
 }
 
-// Overflow-driven regrow (src/physics/gpu/backend.js:1683-1739), done ahead
-// of the overflow: when the last completed step used more than 70% of the
-// candidate capacity, the arenas double and the previous step's manifolds
-// (the warm-start state) move into the new ones.
-int maybe_regrow(avbd_ctx *ctx) {
-  const int last = *((volatile int *)ctx->hCand);
-  if (last * 10LL <= ctx->candCap * 7LL) return AVBD_OK;
-  CK(cudaStreamSynchronize(ctx->stream));
-  Control c{};
-  CK(cudaMemcpy(&c, ctx->w.ctl, sizeof(Control), cudaMemcpyDeviceToHost));
-  const int keep = c.prevCandidates;
-  const Manifolds old = ctx->curIsA ? ctx->mB : ctx->mA;  // last step's arena
+// Arena regrow (src/physics/gpu/backend.js:1683-1739): the candidate arenas
+// are reallocated with `cap` slots and the manifolds of the step that has
+// been stepped last (`old`, `keep` of them: the warm-start state of the next
+// step) move into the new "previous" arena.
+int grow_arenas(avbd_ctx *ctx, int cap, const Manifolds old, int keep) {
   std::vector<void *> oldBufs;
   oldBufs.swap(ctx->growable);
-  const int cap = (int)std::min<long long>(std::max<long long>(2LL * ctx->candCap, 2LL * last), 0x3fffffff);
   int rc = alloc_candidate_arenas(ctx, cap);
   if (rc) {
     for (void *p : oldBufs) cudaFree(p);
@@ -288,6 +281,61 @@ int maybe_regrow(avbd_ctx *ctx) {
   set_world_manifolds(ctx);
   ctx->regrows++;
   return AVBD_OK;
+}
+
+int one_step(avbd_ctx *ctx);
+
+// Steps skipped for a candidate overflow (Control::skip): the arenas grow to
+// twice what the broad phase asked for, the manifolds of the last step that
+// did run become the warm-start state again, and the skipped steps are queued
+// once more. The state of a skipped step is the state before it, so the
+// result equals a run whose arenas were large enough from the start.
+int resolve_skips(avbd_ctx *ctx) {
+  for (int round = 0; round < 4; round++) {
+    CK(cudaStreamSynchronize(ctx->stream));
+    Control c{};
+    CK(cudaMemcpy(&c, ctx->w.ctl, sizeof(Control), cudaMemcpyDeviceToHost));
+    ctx->hCand[0] = 0;
+    if (c.stepsSkipped <= 0) return AVBD_OK;
+    const int S = c.stepsSkipped;
+    // the host flipped the arenas once per queued step; the first skipped step
+    // found the valid warm-start manifolds in its "previous" arena
+    const bool firstCurIsA = (ctx->curIsA ^ (S & 1)) != 0;
+    const Manifolds valid = firstCurIsA ? ctx->mB : ctx->mA;
+    const long long want = std::max<long long>(c.wantCandidates, ctx->candCap);
+    const int cap = (int)std::min<long long>(std::max<long long>(2LL * want, 2LL * ctx->candCap), 0x3fffffff);
+    if (cap <= ctx->candCap)
+      return fail(ctx, AVBD_ERR_CAPACITY, "%lld candidate pairs exceed the largest arena (%d)", want, ctx->candCap);
+    int rc = grow_arenas(ctx, cap, valid, c.prevCandidates);
+    if (rc) return rc;
+    c.skip = 0;
+    c.stepsSkipped = 0;
+    c.flags &= ~kOvfPairs;
+    CK(cudaMemcpy(ctx->w.ctl, &c, sizeof(Control), cudaMemcpyHostToDevice));
+    ctx->steps -= S;
+    for (int k = 0; k < S; k++) {
+      rc = one_step(ctx);
+      if (rc) return rc;
+    }
+  }
+  return fail(ctx, AVBD_ERR_CAPACITY, "candidate arena overflow persists after regrowing");
+}
+
+// Regrow ahead of overflow: when the last completed step used more than 70%
+// of the candidate capacity, the arenas double and the previous step's
+// manifolds (the warm-start state) move into the new ones. A step that did
+// overflow has been skipped: resolve_skips regrows and steps it again.
+int maybe_regrow(avbd_ctx *ctx) {
+  if (*((volatile int *)&ctx->hCand[0]) > 0) return resolve_skips(ctx);
+  const int last = *((volatile int *)&ctx->hCand[1]);
+  if (last * 10LL <= ctx->candCap * 7LL) return AVBD_OK;
+  CK(cudaStreamSynchronize(ctx->stream));
+  Control c{};
+  CK(cudaMemcpy(&c, ctx->w.ctl, sizeof(Control), cudaMemcpyDeviceToHost));
+  if (c.stepsSkipped > 0) return resolve_skips(ctx);
+  const Manifolds old = ctx->curIsA ? ctx->mB : ctx->mA;  // last step's arena
+  const int cap = (int)std::min<long long>(std::max<long long>(2LL * ctx->candCap, 2LL * last), 0x3fffffff);
+  return grow_arenas(ctx, cap, old, c.prevCandidates);
 }
 
 inline uint32_t priority_of(uint32_t local) { return color_priority(local); }
@@ -349,7 +397,9 @@ int write_state(avbd_ctx *ctx, const avbd_world *world, bool keepManifolds) {
       ka[j] = f(J.penalty_ang);
       ll[j] = d(J.lambda_lin);
       la[j] = d(J.lambda_ang);
-      st[j] = (J.broken && J.broken[j]) ? (kBroken | kRemoved) : 0;
+      // a broken joint is warm-started once more by the next step, then leaves
+      // the force list (Joint.initialize, src/physics/joint.js:131-160)
+      st[j] = (J.broken && J.broken[j]) ? kBroken : 0;
     }
     CK(cudaMemcpy(w.j.penLin, kl.data(), ctx->nj * sizeof(float4), cudaMemcpyHostToDevice));
     CK(cudaMemcpy(w.j.penAng, ka.data(), ctx->nj * sizeof(float4), cudaMemcpyHostToDevice));
@@ -463,9 +513,9 @@ int one_step(avbd_ctx *ctx) {
   if ((rc = record(ctx, 5))) return rc;
   launch_commit(w, st, ctx->smCount);
   ctx->launches += 1;
-  // this step's candidates become next step's previous manifolds
-  CK(cudaMemcpyAsync(&w.ctl->prevCandidates, &w.ctl->numCandidates, sizeof(int), cudaMemcpyDeviceToDevice, st));
-  CK(cudaMemcpyAsync(ctx->hCand, &w.ctl->numCandidates, sizeof(int), cudaMemcpyDeviceToHost, st));
+  // (commit_kernel made this step's candidates the next step's previous
+  // manifolds, unless the step was skipped)
+  CK(cudaMemcpyAsync(ctx->hCand, &w.ctl->stepsSkipped, 2 * sizeof(int), cudaMemcpyDeviceToHost, st));
   if ((rc = record(ctx, 6))) return rc;
   CK(cudaEventRecord(ctx->stepEv[ctx->stepSeq % 8], st));
   ctx->stepSeq++;
@@ -486,6 +536,7 @@ int one_step(avbd_ctx *ctx) {
     ctx->prof.step_ms = tot;
     Control c{};
     CK(cudaMemcpy(&c, w.ctl, sizeof(Control), cudaMemcpyDeviceToHost));
+    if (c.stepsSkipped > 0) return resolve_skips(ctx);  // the step runs again (and is profiled then)
     ctx->prof.candidate_pairs = c.numCandidates;
     ctx->prof.manifolds = c.liveManifolds;
     ctx->prof.contacts = c.liveContacts;
@@ -751,7 +802,8 @@ int avbd_pack(avbd_ctx *ctx, const avbd_world *world) {
                      P.spring_stiffness_ramp, P.spring_geometric_stiffness, P.cached_contact_jacobians,
                      P.fp64_ratio_threshold, P.schedule == 1 ? 1 : 0, P.lanes_per_body > 0 ? P.lanes_per_body : 0, 1,
                      P.wait_limit > 0 ? (long long)P.wait_limit : 20000000LL,
-                     P.wait_limit > 0 ? (long long)P.wait_limit : 4000000LL};
+                     P.neighbor_wait_limit > 0 ? (long long)P.neighbor_wait_limit
+                                               : (P.wait_limit > 0 ? (long long)P.wait_limit : 4000000LL)};
   int rc = 0;
   D4 *sizeP, *massDP;
   float4 *massFP;
@@ -835,8 +887,8 @@ int avbd_pack(avbd_ctx *ctx, const avbd_world *world) {
     return rc;
   // manifolds (double-buffered), candidate keys, adjacency
   if ((rc = alloc_candidate_arenas(ctx, ctx->candCap))) return rc;
-  CK(cudaMallocHost((void **)&ctx->hCand, sizeof(int)));
-  *ctx->hCand = 0;
+  CK(cudaMallocHost((void **)&ctx->hCand, 2 * sizeof(int)));
+  ctx->hCand[0] = ctx->hCand[1] = 0;
   ctx->curIsA = 1;
   set_world_manifolds(ctx);
   if ((rc = dalloc(ctx, &w.ctl, 1)) || (rc = dalloc(ctx, &ctx->statsOut, 3))) return rc;
@@ -891,13 +943,16 @@ int avbd_synchronize(avbd_ctx *ctx) {
   if (!ctx) return AVBD_ERR_ARG;
   CK(cudaStreamSynchronize(ctx->stream));
   if (!ctx->packed) return AVBD_OK;
+  int rc = resolve_skips(ctx);
+  if (rc) return rc;
   return check_flags(ctx);
 }
 
 int avbd_read_state(avbd_ctx *ctx, avbd_world *out) {
   if (!ctx || !out) return AVBD_ERR_ARG;
   if (!ctx->packed) return fail(ctx, AVBD_ERR_STATE, "avbd_read_state before avbd_pack");
-  CK(cudaStreamSynchronize(ctx->stream));
+  int rs = resolve_skips(ctx);  // steps skipped for an overflow run again first
+  if (rs) return rs;
   const World &w = ctx->w;
   const int n = ctx->n;
   avbd_body_soa &B = out->bodies;
@@ -1022,13 +1077,15 @@ int avbd_write_state(avbd_ctx *ctx, const avbd_world *world) {
   if (!ctx->packed) return fail(ctx, AVBD_ERR_STATE, "avbd_write_state before avbd_pack");
   if (world->bodies.count != ctx->n || world->joints.count != ctx->nj || world->springs.count != ctx->ns)
     return fail(ctx, AVBD_ERR_ARG, "avbd_write_state: topology differs from the packed world");
-  CK(cudaStreamSynchronize(ctx->stream));
+  int rs = resolve_skips(ctx);
+  if (rs) return rs;
   return write_state(ctx, world, true);
 }
 
 int avbd_read_coloring(avbd_ctx *ctx, int32_t *color_of, int32_t *num_colors) {
   if (!ctx || !ctx->packed) return fail(ctx, AVBD_ERR_STATE, "avbd_read_coloring before avbd_pack");
-  CK(cudaStreamSynchronize(ctx->stream));
+  int rs = resolve_skips(ctx);
+  if (rs) return rs;
   if (color_of) CK(cudaMemcpy(color_of, ctx->w.b.color, ctx->n * sizeof(int), cudaMemcpyDeviceToHost));
   Control c{};
   CK(cudaMemcpy(&c, ctx->w.ctl, sizeof(Control), cudaMemcpyDeviceToHost));
@@ -1038,7 +1095,8 @@ int avbd_read_coloring(avbd_ctx *ctx, int32_t *color_of, int32_t *num_colors) {
 
 int avbd_read_pairs(avbd_ctx *ctx, int32_t *body_a, int32_t *body_b, int64_t capacity, int64_t *count) {
   if (!ctx || !ctx->packed) return fail(ctx, AVBD_ERR_STATE, "avbd_read_pairs before avbd_pack");
-  CK(cudaStreamSynchronize(ctx->stream));
+  int rs = resolve_skips(ctx);
+  if (rs) return rs;
   Control c{};
   CK(cudaMemcpy(&c, ctx->w.ctl, sizeof(Control), cudaMemcpyDeviceToHost));
   const int total = c.prevCandidates;
@@ -1060,12 +1118,13 @@ int avbd_read_stats(avbd_ctx *ctx, avbd_stats *out) {
   if (!ctx || !out) return AVBD_ERR_ARG;
   std::memset(out, 0, sizeof(*out));
   if (!ctx->packed) return AVBD_OK;
+  int rs = resolve_skips(ctx);
+  if (rs) return rs;
   const World &w = ctx->w;
   World sw = w;
   const Manifolds &pm = ctx->curIsA ? ctx->mB : ctx->mA;
   sw.cur = pm;
   Control c{};
-  CK(cudaStreamSynchronize(ctx->stream));
   CK(cudaMemcpy(&c, w.ctl, sizeof(Control), cudaMemcpyDeviceToHost));
   // the stats kernel reads numCandidates: point it at the last step's count
   Control tmp = c;
@@ -1121,7 +1180,8 @@ int avbd_kernel_launches(avbd_ctx *ctx, int64_t *out) {
 int avbd_set_coloring(avbd_ctx *ctx, const int32_t *color_of) {
   if (!ctx) return AVBD_ERR_ARG;
   if (!ctx->packed) return fail(ctx, AVBD_ERR_STATE, "avbd_set_coloring before avbd_pack");
-  CK(cudaStreamSynchronize(ctx->stream));
+  int rs = resolve_skips(ctx);
+  if (rs) return rs;
   if (!color_of) {
     ctx->w.a.colorOverride = nullptr;
     return AVBD_OK;
@@ -1141,6 +1201,8 @@ int avbd_update_joint_anchor(avbd_ctx *ctx, int32_t joint, const double r_a[3]) 
   if (joint < 0 || joint >= ctx->nj) return fail(ctx, AVBD_ERR_ARG, "joint %d out of range (%d joints)", joint, ctx->nj);
   if (!std::isfinite(r_a[0]) || !std::isfinite(r_a[1]) || !std::isfinite(r_a[2]))
     return fail(ctx, AVBD_ERR_NAN, "joint %d: non-finite anchor", joint);
+  int rs = resolve_skips(ctx);  // the new anchor applies after the steps already queued
+  if (rs) return rs;
   CK(launch_joint_anchor(ctx->w, joint, r_a[0], r_a[1], r_a[2], ctx->stream));
   ctx->launches += 1;
   return AVBD_OK;

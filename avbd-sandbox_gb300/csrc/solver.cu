@@ -80,6 +80,10 @@ __device__ bool grid_barrier(Control *ctl, long long limit) {
 // ---------------------------------------------------------------------------
 // Preparation
 // ---------------------------------------------------------------------------
+// A step skipped for a candidate overflow (Control::skip): its kernels after
+// the broad phase return at once and leave every state array untouched.
+__device__ __forceinline__ bool step_skipped(const World &w) { return *((volatile int *)&w.ctl->skip) != 0; }
+
 __device__ inline double jsmin(double a, double b) { return a < b ? a : (b < a ? b : a); }
 __device__ inline double jsmax(double a, double b) { return a > b ? a : (b > a ? b : a); }
 __device__ inline double clampd(double x, double a, double b) { return x != x ? x : jsmax(a, jsmin(b, x)); }
@@ -91,13 +95,34 @@ __device__ inline Q4<double> body_q_t(const World &w, int i) {
 
 // joint.js:131-160 / spring.js:472-507, plus the f64 offsets p_A(t) - p_B(t).
 __global__ void prepare_forces_kernel(World w) {
+  if (step_skipped(w)) return;
   const SolverParams &P = w.p;
   const int tid = blockIdx.x * blockDim.x + threadIdx.x, stride = gridDim.x * blockDim.x;
   for (int j = tid; j < w.j.n; j += stride) {
-    int st = w.j.state[j];
-    if (st & kBroken) st |= kRemoved;  // Joint.initialize returns !broken
-    w.j.state[j] = st;
-    if (st) continue;
+    const int st = w.j.state[j];
+    if (st & kRemoved) continue;  // left the force list in an earlier step
+    if (st & kBroken) {
+      // Joint.initialize still warm-starts a joint broken in the last step
+      // (lambda = alpha gamma 0, k = min(clamp(gamma 0, kmin, kmax), stiffness)),
+      // then returns !broken and the joint leaves the force list
+      // (solver.js:346-360)
+      const D4 sf = w.j.stiff[j];
+      auto warm0 = [&](float k, double cap) {
+        return (float)jsmin(clampd((double)k * P.gamma, P.penaltyMin, P.penaltyMax), cap);
+      };
+      const float4 kl = w.j.penLin[j], ka = w.j.penAng[j];
+      w.j.penLin[j] = make_float4(warm0(kl.x, sf.x), warm0(kl.y, sf.x), warm0(kl.z, sf.x), 0.f);
+      w.j.penAng[j] = make_float4(warm0(ka.x, sf.y), warm0(ka.y, sf.y), warm0(ka.z, sf.y), 0.f);
+      if (!P.postStabilize) {
+        D4 ll = w.j.lamLin[j], la = w.j.lamAng[j];
+        ll.x = ll.x * P.alpha * P.gamma; ll.y = ll.y * P.alpha * P.gamma; ll.z = ll.z * P.alpha * P.gamma;
+        la.x = la.x * P.alpha * P.gamma; la.y = la.y * P.alpha * P.gamma; la.z = la.z * P.alpha * P.gamma;
+        w.j.lamLin[j] = ll;
+        w.j.lamAng[j] = la;
+      }
+      w.j.state[j] = st | kRemoved;
+      continue;
+    }
     const int2 ab = w.j.bodies[j];
     const D4 rA = w.j.rAD[j], rB = w.j.rBD[j], sf = w.j.stiff[j];
     const Q4<double> qB = body_q_t(w, ab.y);
@@ -180,6 +205,7 @@ __global__ void prepare_forces_kernel(World w) {
 
 // solver.js:369-401, in delta form.
 __global__ void prepare_bodies_kernel(World w) {
+  if (step_skipped(w)) return;
   const SolverParams &P = w.p;
   const double dt = P.dt, g = P.gravity;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < w.b.n; i += gridDim.x * blockDim.x) {
@@ -269,6 +295,7 @@ __global__ void adj_fill_kernel(World w) {
 
 // Sort each body's manifold list (determinism) and decide its precision.
 __global__ void adj_sort_kernel(World w) {
+  if (step_skipped(w)) return;
   const double dt2 = w.p.dt * w.p.dt;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < w.b.n; i += gridDim.x * blockDim.x) {
     int fl = w.b.flags[i];
@@ -388,6 +415,7 @@ __device__ void lane_layout(const World &w) {
   int *cnt = w.a.laneHist, *cur = w.a.laneHist + kMaxColors * kLaneBuckets;
   int *used = w.a.laneHist + 2 * kMaxColors * kLaneBuckets;
   const int nrec = w.a.colorStart[kMaxColors];
+  const int numColors = *((volatile int *)&ctl->numColors);
   const int lane = threadIdx.x & 31;
   // warp-uniform loops (stride is a multiple of 32): the records of a warp
   // with equal (colour, size) share one atomic
@@ -402,31 +430,45 @@ __device__ void lane_layout(const World &w) {
   }
   if (!grid_barrier(ctl, w.p.barrierLimit)) return;
   if (blockIdx.x == 0) {
-    __shared__ int chunks[kMaxColors];
-    const int c = threadIdx.x;
-    if (c < kMaxColors) {
-      int off = 0;
-      for (int b = kLaneBuckets - 1; b >= 0; b--) {
-        cur[c * kLaneBuckets + b] = off;
-        off += cnt[c * kLaneBuckets + b] << b;
-      }
-      used[c] = off;
-      chunks[c] = (off + kLaneMaxGroup - 1) / kLaneMaxGroup;
-    }
+    // per colour: the offsets of its size classes (largest first) and its
+    // lane count; then the colours' first chunks by a block-wide scan
+    __shared__ int chunkScan[256];
+    __shared__ int carry;
+    if (threadIdx.x == 0) carry = 0;
     __syncthreads();
-    if (threadIdx.x == 0) {
-      int q = 0, lanes = 0;
-      for (int k = 0; k < kMaxColors; k++) {
-        w.a.colorChunk[k] = q;
-        q += chunks[k];
-        lanes += used[k];
+    int lanesTotal = 0;
+    for (int c0 = 0; c0 < numColors; c0 += blockDim.x) {
+      const int c = c0 + threadIdx.x;
+      int chunks = 0;
+      if (c < numColors) {
+        int off = 0;
+        for (int b = kLaneBuckets - 1; b >= 0; b--) {
+          cur[c * kLaneBuckets + b] = off;
+          off += cnt[c * kLaneBuckets + b] << b;
+        }
+        used[c] = off;
+        lanesTotal += off;
+        chunks = (off + kLaneMaxGroup - 1) / kLaneMaxGroup;
       }
-      w.a.colorChunk[kMaxColors] = q;
-      ctl->laneTotal = lanes;
+      chunkScan[threadIdx.x] = chunks;
+      __syncthreads();
+      for (int d = 1; d < (int)blockDim.x; d <<= 1) {  // inclusive scan
+        const int v = threadIdx.x >= d ? chunkScan[threadIdx.x - d] : 0;
+        __syncthreads();
+        chunkScan[threadIdx.x] += v;
+        __syncthreads();
+      }
+      if (c < numColors) w.a.colorChunk[c] = carry + chunkScan[threadIdx.x] - chunks;
+      __syncthreads();
+      if (threadIdx.x == blockDim.x - 1) carry += chunkScan[threadIdx.x];
+      __syncthreads();
     }
+    if (threadIdx.x == 0) w.a.colorChunk[numColors] = carry;
+    lanesTotal = __reduce_add_sync(0xffffffffu, lanesTotal);
+    if (lane == 0 && lanesTotal) atomicAdd(&ctl->laneTotal, lanesTotal);
   }
   if (!grid_barrier(ctl, w.p.barrierLimit)) return;
-  for (int k = tid; k < kMaxColors * kLaneBuckets; k += stride) cnt[k] = 0;  // for the next step
+  for (int k = tid; k < numColors * kLaneBuckets; k += stride) cnt[k] = 0;  // for the next step
   for (int r = tid; r - lane < nrec; r += stride) {
     int key = -1, c = 0, b = 0, e = 0;
     if (r < nrec) {
@@ -452,7 +494,7 @@ __device__ void lane_layout(const World &w) {
     }
   }
   // the lanes past each colour's last group, up to its last chunk's end
-  for (int k = tid; k < kMaxColors * kLaneMaxGroup; k += stride) {
+  for (int k = tid; k < numColors * kLaneMaxGroup; k += stride) {
     const int c = k / kLaneMaxGroup;
     const size_t L = (size_t)w.a.colorChunk[c] * kLaneMaxGroup + used[c] + (k % kLaneMaxGroup);
     if (L < (size_t)w.a.colorChunk[c + 1] * kLaneMaxGroup) w.a.laneTab[L] = -1;
@@ -461,17 +503,22 @@ __device__ void lane_layout(const World &w) {
 
 // The tail of the colouring: owner bits of the contact entries, the stable
 // counting sort by colour and the solve's lane layout (cooperative: grid
-// barriers inside).
+// barriers inside). Per-colour loops run over the colours in use only
+// (Control::numColors, from the largest colour found), so a step of few
+// colours pays nothing for the colour capacity.
 __device__ void coloring_finish(const World &w) {
   Control *ctl = w.ctl;
   const int n = w.b.n;
   const int tid = blockIdx.x * blockDim.x + threadIdx.x, stride = gridDim.x * blockDim.x;
   volatile int *color = w.b.color;
   // owner bit (bit 1) of every contact entry: the endpoint with the larger
-  // colour owns the contact's dual update (a static endpoint has colour -1)
+  // colour owns the contact's dual update (a static endpoint has colour -1);
+  // and the number of colours in use
+  int maxColor = -1;
   for (int i = tid; i < n; i += stride) {
     if (!(w.b.flags0[i] & kBodyDynamic)) continue;
     const int ci = color[i];
+    maxColor = max(maxColor, ci);
     const int e1 = min(w.a.cstart[i + 1], w.a.ccap);
     for (int e = w.a.cstart[i]; e < e1; e++) {
       int2 v = w.a.centry[e];
@@ -480,78 +527,109 @@ __device__ void coloring_finish(const World &w) {
       w.a.centry[e] = v;
     }
   }
+  maxColor = __reduce_max_sync(0xffffffffu, maxColor);
+  if ((threadIdx.x & 31) == 0 && maxColor >= 0) atomicMax(&ctl->numColors, maxColor + 1);
+  if (tid == 0) ctl->laneTotal = 0;  // summed by lane_layout after the next barriers
+  if (!grid_barrier(ctl, w.p.barrierLimit)) return;
+  const int numColors = *((volatile int *)&ctl->numColors);
   // --- stable counting sort by colour (per-block chunk of body indices) ---
   __shared__ int hist[kMaxColors];
   __shared__ int base[kMaxColors];
-  __shared__ int warpCnt[8][kMaxColors];
   const int chunk = (n + gridDim.x - 1) / gridDim.x;
   const int b0 = blockIdx.x * chunk, b1 = min(n, b0 + chunk);
-  for (int c = threadIdx.x; c < kMaxColors; c += blockDim.x) hist[c] = 0;
+  for (int c = threadIdx.x; c < numColors; c += blockDim.x) hist[c] = 0;
   __syncthreads();
   for (int i = b0 + threadIdx.x; i < b1; i += blockDim.x) {
     const int c = color[i];
     if (c >= 0) atomicAdd(&hist[c], 1);
   }
   __syncthreads();
-  for (int c = threadIdx.x; c < kMaxColors; c += blockDim.x) w.a.blockHist[blockIdx.x * kMaxColors + c] = hist[c];
+  for (int c = threadIdx.x; c < numColors; c += blockDim.x) w.a.blockHist[blockIdx.x * kMaxColors + c] = hist[c];
   if (!grid_barrier(ctl, w.p.barrierLimit)) return;
   if (blockIdx.x == 0) {
-    __shared__ int totals[kMaxColors];
-    if (threadIdx.x < kMaxColors) {
-      const int c = threadIdx.x;
-      int run = 0;
-      for (int b = 0; b < (int)gridDim.x; b++) {
-        const int h = w.a.blockHist[b * kMaxColors + c];
-        w.a.blockHist[b * kMaxColors + c] = run;
-        run += h;
-      }
-      totals[c] = run;
-    }
+    // per colour: the blocks' offsets (a scan over blocks), then the colours'
+    // starts (a block-wide scan over colours, in rounds of blockDim colours)
+    __shared__ int scan[256];
+    __shared__ int carry;
+    if (threadIdx.x == 0) carry = 0;
     __syncthreads();
-    if (threadIdx.x == 0) {
-      int run = 0, used = 0;
-      for (int c = 0; c < kMaxColors; c++) {
-        w.a.colorStart[c] = run;
-        run += totals[c];
-        if (totals[c] > 0) used = c + 1;
+    for (int c0 = 0; c0 < numColors; c0 += blockDim.x) {
+      const int c = c0 + threadIdx.x;
+      int run = 0;
+      if (c < numColors)
+        for (int b = 0; b < (int)gridDim.x; b++) {
+          const int h = w.a.blockHist[b * kMaxColors + c];
+          w.a.blockHist[b * kMaxColors + c] = run;
+          run += h;
+        }
+      scan[threadIdx.x] = run;
+      __syncthreads();
+      for (int d = 1; d < (int)blockDim.x; d <<= 1) {  // inclusive scan
+        const int v = threadIdx.x >= d ? scan[threadIdx.x - d] : 0;
+        __syncthreads();
+        scan[threadIdx.x] += v;
+        __syncthreads();
       }
-      w.a.colorStart[kMaxColors] = run;
-      ctl->numColors = used;
+      if (c < numColors) w.a.colorStart[c] = carry + scan[threadIdx.x] - run;
+      __syncthreads();
+      if (threadIdx.x == blockDim.x - 1) carry += scan[threadIdx.x];
+      __syncthreads();
     }
+    for (int c = numColors + (int)threadIdx.x; c <= kMaxColors; c += blockDim.x) w.a.colorStart[c] = carry;
   }
   if (!grid_barrier(ctl, w.p.barrierLimit)) return;
-  for (int c = threadIdx.x; c < kMaxColors; c += blockDim.x)
+  for (int c = threadIdx.x; c < numColors; c += blockDim.x)
     base[c] = w.a.colorStart[c] + w.a.blockHist[blockIdx.x * kMaxColors + c];
   __syncthreads();
+  // within a tile of blockDim bodies: rank among the tile's bodies of the same
+  // colour = rank within the warp + the counts of that colour in earlier warps
+  // (each warp lists its distinct colours with their counts)
+  __shared__ int2 warpList[8][32];
+  __shared__ int warpLen[8];
   const int lane = threadIdx.x & 31, warp = threadIdx.x >> 5;
   for (int t0 = b0; t0 < b1; t0 += blockDim.x) {
-    for (int c = threadIdx.x; c < 8 * kMaxColors; c += blockDim.x) (&warpCnt[0][0])[c] = 0;
-    __syncthreads();
     const int i = t0 + threadIdx.x;
     const int c = (i < b1) ? color[i] : -1;
     const unsigned m = __match_any_sync(0xffffffffu, c);
     const int rankInWarp = __popc(m & ((1u << lane) - 1u));
-    if (c >= 0 && rankInWarp == 0) warpCnt[warp][c] = __popc(m);
+    const bool leader = rankInWarp == 0 && c >= 0;
+    const unsigned leaders = __ballot_sync(0xffffffffu, leader);
+    if (leader) warpList[warp][__popc(leaders & ((1u << lane) - 1u))] = make_int2(c, __popc(m));
+    if (lane == 0) warpLen[warp] = __popc(leaders);
     __syncthreads();
     if (c >= 0) {
       int r = base[c] + rankInWarp;
-      for (int q = 0; q < warp; q++) r += warpCnt[q][c];
+      for (int q = 0; q < warp; q++)
+        for (int k = 0; k < warpLen[q]; k++)
+          if (warpList[q][k].x == c) r += warpList[q][k].y;
       w.a.colorBodies[r] = i;
       w.a.colorRec[r] = make_int4(i, w.a.cstart[i], min(w.a.cstart[i + 1], w.a.ccap), 0);
     }
     __syncthreads();
-    for (int cc = threadIdx.x; cc < kMaxColors; cc += blockDim.x) {
-      int s = 0;
-      for (int q = 0; q < 8; q++) s += warpCnt[q][cc];
-      base[cc] += s;
-    }
+    for (int q = 0; q < (int)(blockDim.x >> 5); q++)  // advance the bases past this tile
+      for (int k = threadIdx.x; k < warpLen[q]; k += blockDim.x) atomicAdd(&base[warpList[q][k].x], warpList[q][k].y);
     __syncthreads();
   }
   if (!grid_barrier(ctl, w.p.barrierLimit)) return;
   lane_layout(w);
 }
 
+// Smallest colour no neighbour of higher priority holds, searched in windows
+// of 64 colours: one pass unless all of 0..63 are taken.
+template <class F>
+__device__ __forceinline__ int smallest_free_color(F &&neighbors) {
+  for (int base = 0; base < kMaxColors; base += 64) {
+    unsigned long long used = 0ull;
+    neighbors([&](int c) {
+      if (c >= base && c < base + 64) used |= 1ull << (c - base);
+    });
+    if (~used) return base + __ffsll((long long)~used) - 1;
+  }
+  return -1;
+}
+
 __global__ void __launch_bounds__(256) coloring_kernel(World w) {
+  if (step_skipped(w)) return;  // every block reads the same value: none waits at a barrier
   Control *ctl = w.ctl;
   const int n = w.b.n;
   const int tid = blockIdx.x * blockDim.x + threadIdx.x, stride = gridDim.x * blockDim.x;
@@ -581,20 +659,14 @@ __global__ void __launch_bounds__(256) coloring_kernel(World w) {
     int changed = 0;
     for (int i = tid; i < n; i += stride) {
       if (!(w.b.flags0[i] & kBodyDynamic)) continue;
-      unsigned long long used = 0ull;
       const int hb = w.a.start[i], hc = w.a.hpCount[i];
-      for (int k = 0; k < hc; k++) {
-        const int c = color[w.a.hpEntry[hb + k]];
-        if (c >= 0 && c < kMaxColors) used |= 1ull << c;
-      }
-      if (w.g.hasConstraints)
-        constraint_neighbors(w, i, [&](int j) {
-          if (precedes(w, j, i)) {
-            const int c = color[j];
-            if (c >= 0 && c < kMaxColors) used |= 1ull << c;
-          }
-        });
-      int c = __ffsll((long long)~used) - 1;
+      int c = smallest_free_color([&](auto &&mark) {
+        for (int k = 0; k < hc; k++) mark(color[w.a.hpEntry[hb + k]]);
+        if (w.g.hasConstraints)
+          constraint_neighbors(w, i, [&](int j) {
+            if (precedes(w, j, i)) mark(color[j]);
+          });
+      });
       if (c < 0) {
         c = kMaxColors - 1;
         atomicOr(&ctl->flags, kOvfColors);
@@ -1757,7 +1829,9 @@ __device__ __forceinline__ void group_sync(int G, unsigned mask) {
 // walks its chunks in increasing colour, so the earliest unfinished tail
 // body always has its inputs ready (all blocks are resident).
 constexpr int kTailDiv = 8;
+constexpr int kChunkCache = 64;  // colours whose chunk bounds the solve keeps in shared memory
 __global__ void __launch_bounds__(kSolveBlock, 3) solve_kernel(World w) {
+  if (step_skipped(w)) return;
   extern __shared__ float4 stageSm[];
   float4 *stage = stageSm + threadIdx.x;
   const SolverParams &P = w.p;
@@ -1767,17 +1841,20 @@ __global__ void __launch_bounds__(kSolveBlock, 3) solve_kernel(World w) {
   const int total = P.iterations + (P.postStabilize ? 1 : 0);
   const int kb = P.solveBlocksPerSm > 0 ? P.solveBlocksPerSm : 1, S = gridDim.x / kb;
   const int jb = S * kb == (int)gridDim.x ? ((int)blockIdx.x % kb) * S + (int)blockIdx.x / kb : (int)blockIdx.x;
-  __shared__ int chunkSm[kMaxColors + 1];  // colour chunk bounds, constant through the solve
-  for (int k = threadIdx.x; k <= numColors; k += blockDim.x) chunkSm[k] = ld(&w.a.colorChunk[k]);
+  // colour chunk bounds, constant through the solve: the first kChunkCache + 1
+  // in shared memory, the rest (steps of many colours) through L1
+  __shared__ int chunkSm[kChunkCache + 1];
+  for (int k = threadIdx.x; k <= numColors && k <= kChunkCache; k += blockDim.x) chunkSm[k] = ld(&w.a.colorChunk[k]);
   __syncthreads();
+  auto chunkAt = [&](int c) { return c <= kChunkCache ? chunkSm[c] : ld(&w.a.colorChunk[c]); };
   int tail = numColors;  // first tail colour
-  while (tail > 0 && chunkSm[tail] - chunkSm[tail - 1] <= (int)gridDim.x / kTailDiv) tail--;
+  while (tail > 0 && chunkAt(tail) - chunkAt(tail - 1) <= (int)gridDim.x / kTailDiv) tail--;
   for (int it = 0; it < total; it++) {
     const double alpha = P.postStabilize ? (it < P.iterations ? 1.0 : 0.0) : P.alpha;
     const bool dual = it < P.iterations;
     const bool vel = it == P.iterations - 1;
     for (int c = 0; c < tail; c++) {
-      const int q0 = chunkSm[c], q1 = chunkSm[c + 1];
+      const int q0 = chunkAt(c), q1 = chunkAt(c + 1);
       for (int q = q0 + jb; q < q1; q += gridDim.x) {
         const int e = ld(&w.a.laneTab[(size_t)q * kLaneMaxGroup + threadIdx.x]);
         if (e < 0) continue;
@@ -1792,8 +1869,9 @@ __global__ void __launch_bounds__(kSolveBlock, 3) solve_kernel(World w) {
     }
     if (tail < numColors) {  // the tail segment of iteration it
       int c = tail;
-      for (int q = chunkSm[tail] + jb; q < chunkSm[numColors]; q += gridDim.x) {
-        while (chunkSm[c + 1] <= q) c++;
+      const int qEnd = chunkAt(numColors);
+      for (int q = chunkAt(tail) + jb; q < qEnd; q += gridDim.x) {
+        while (chunkAt(c + 1) <= q) c++;
         const int e = ld(&w.a.laneTab[(size_t)q * kLaneMaxGroup + threadIdx.x]);
         if (e < 0) continue;
         const int G = 1 << (e & 7);
@@ -1801,9 +1879,12 @@ __global__ void __launch_bounds__(kSolveBlock, 3) solve_kernel(World w) {
         const unsigned mask = G >= 32 ? 0xffffffffu : (((1u << G) - 1u) << (warpLane & ~(G - 1)));
         const int4 rec = ld(&w.a.colorRec[e >> 4]);
         if (e & 8) {
-          wait_neighbors(w, rec.x, it, lane, G, mask, tail);
-          __syncwarp(mask);  // every lane's reads after the others' acquires
-          solve_body_f64(w, rec, lane, G, mask, alpha, dual, vel);
+          // a wait that gave up has set the timeout flag: the body is not
+          // solved on stale data, and the kernel ends at the next grid barrier
+          if (wait_neighbors(w, rec.x, it, lane, G, mask, tail)) {
+            __syncwarp(mask);  // every lane's reads after the others' acquires
+            solve_body_f64(w, rec, lane, G, mask, alpha, dual, vel);
+          }
           group_sync(G, mask);  // the group's writes before lane 0's release
           if (lane == 0) st_release(&w.b.progress[rec.x], it + 1);
         } else {
@@ -1829,6 +1910,7 @@ __global__ void __launch_bounds__(kSolveBlock, 3) solve_kernel(World w) {
 
 
 __global__ void __launch_bounds__(kSolveBlock, 3) wave_kernel(World w, int G) {
+  if (step_skipped(w)) return;
   extern __shared__ float4 stageSm[];
   float4 *stage = stageSm + threadIdx.x;
   const SolverParams &P = w.p;
@@ -1865,7 +1947,14 @@ __global__ void __launch_bounds__(kSolveBlock, 3) wave_kernel(World w, int G) {
 }
 
 // x_{t+1} = x_t + delta (f64); statics: prevVel <- vel (solver.js:479).
+// Also the step's bookkeeping: its candidates become the next step's previous
+// manifolds, or, for a skipped step, the skip is counted and nothing moves.
 __global__ void commit_kernel(World w) {
+  if (step_skipped(w)) {
+    if (blockIdx.x == 0 && threadIdx.x == 0) w.ctl->stepsSkipped++;
+    return;
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) w.ctl->prevCandidates = w.ctl->numCandidates;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < w.b.n; i += gridDim.x * blockDim.x) {
     const int fl = w.b.flags[i];
     if (!(fl & kBodyDynamic)) {
@@ -1955,12 +2044,14 @@ int coloring_grid(int smCount) { return coloring_blocks(smCount); }
 
 // An uploaded colouring: copied, then checked against this step's graph.
 __global__ void color_copy_kernel(World w) {
+  if (step_skipped(w)) return;
   if (blockIdx.x == 0 && threadIdx.x == 0) w.ctl->colorBad = 0;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < w.b.n; i += gridDim.x * blockDim.x)
     w.b.color[i] = (w.b.flags0[i] & kBodyDynamic) ? w.a.colorOverride[i] : -1;
 }
 
 __global__ void color_check_kernel(World w) {
+  if (step_skipped(w)) return;
   int bad = 0;
   for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < w.b.n && !bad; i += gridDim.x * blockDim.x) {
     if (!(w.b.flags0[i] & kBodyDynamic)) continue;

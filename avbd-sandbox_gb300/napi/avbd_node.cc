@@ -236,6 +236,7 @@ void bind_params(napi_env env, napi_value obj, avbd_params *p) {
   if (get_number(env, obj, "springGeometricStiffness", &v)) p->spring_geometric_stiffness = v != 0;
   if (get_number(env, obj, "cachedContactJacobians", &v)) p->cached_contact_jacobians = v != 0;
   if (get_number(env, obj, "waitLimit", &v)) p->wait_limit = (int32_t)v;
+  if (get_number(env, obj, "neighborWaitLimit", &v)) p->neighbor_wait_limit = (int32_t)v;
   if (get_number(env, obj, "fp64RatioThreshold", &v)) p->fp64_ratio_threshold = v;
   if (get_number(env, obj, "lanesPerBody", &v)) p->lanes_per_body = (int32_t)v;
   if (get_number(env, obj, "schedule", &v)) p->schedule = (int32_t)v;

@@ -415,6 +415,55 @@ def brick_wall_c5(mu=0.6, sphere_velocity=(0.0, 8.0, 0.0), bond_stiffness=INF, c
     return s
 
 
+def breakage(cols=6, rows=4, fracture=100.0, tear_strains=(0.02, 0.05), gravity=-9.81):
+    """Constraints that break within the first steps: a `cols` x `rows` brick
+    wall bonded by hard ball sockets with hard angular rows and a fracture
+    threshold on |lambda_ang| (src/physics/joint.js:307-316), struck by a 50 kg
+    sphere launched 0.8 m in front of it (bonds start breaking at step 4 in
+    the f64 engine at fracture 100), and beside it one hanging chain of six
+    1 kg boxes on springs (stiffness 1e3 / 1e4 alternating, rest 1 m) per
+    entry of `tear_strains`, released at rest length so that the top spring
+    overshoots its static strain and tears (src/physics/spring.js:461-470):
+    at step 5 for 0.02, step 9 for 0.05."""
+    s = brick_wall(cols=cols, rows=rows, fracture=fracture, gravity=gravity)
+    s.name = "breakage"
+    s.b["pos"][-1] = (0.0, -0.8, rows * 0.25 * 0.5)
+    for c, tear in enumerate(tear_strains):
+        x = 10.0 + 3.0 * c
+        anchor = s.box((0.4, 0.4, 0.4), 0.0, 0.5, (x, 0.0, 20.0))
+        prev, z = anchor, 20.0
+        for i in range(6):
+            z -= 1.0
+            b = s.box((0.1, 0.1, 0.1), 1000.0, 0.5, (x, 0.0, z))
+            s.spring(prev, b, (0.0, 0.0, 0.0), (0.0, 0.0, 0.0), 1e3 if i % 2 == 0 else 1e4, 1.0, tear)
+            prev = b
+    s.meta = dict(steps=15)
+    return s
+
+
+def joint_clique(n=72, stiffness=100.0, radius=6.0, gravity=-9.81):
+    """A constraint graph that needs more colours than a body has contacts:
+    `n` 1 kg boxes (0.3 m) on a horizontal circle, every pair joined by a
+    finite ball socket (stiffness `stiffness`, no angular rows) anchored at
+    the midpoint of the two centres, so every joint starts at C = 0. The
+    graph is complete: any proper colouring needs n colours."""
+    s = Scene("joint_clique")
+    add_ground(s)
+    ids, pos = [], []
+    for k in range(n):
+        a = 2.0 * math.pi * k / n
+        p = (radius * math.cos(a), radius * math.sin(a), 10.0)
+        ids.append(s.box((0.3, 0.3, 0.3), 1.0 / 0.027, 0.5, p))
+        pos.append(p)
+    for i in range(n):
+        for j in range(i + 1, n):
+            h = tuple((pos[j][k] - pos[i][k]) * 0.5 for k in range(3))
+            s.joint(ids[i], ids[j], h, tuple(-x for x in h), stiffness, 0.0, INF)
+    s.params = dict(gravity=gravity, iterations=10)
+    s.meta = dict(steps=30)
+    return s
+
+
 def parity_scenes():
     """Small scenes with the content of the reference's parity list
     (test/parity/gen_scenes.mjs): ground, spinner, stack, stack_ratio,

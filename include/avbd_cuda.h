@@ -62,7 +62,9 @@ extern "C" {
 #define AVBD_ERR_COLORING 0x200u /* an uploaded colouring was not proper     */
 
 #define AVBD_MAX_CONTACTS 8 /* contacts per manifold (src/physics/collide.js:22) */
-#define AVBD_MAX_COLORS 64  /* colours the device colouring can encode       */
+#define AVBD_MAX_COLORS 1024 /* colours the device colouring can hold: the greedy
+                                colouring needs at most the largest number of
+                                dynamic neighbours of one body, plus one      */
 
 /*
  * Solver parameters. Field meanings and defaults follow
@@ -113,6 +115,10 @@ typedef struct avbd_params {
      Both give the same result for the same nonzero lanes_per_body. */
   int32_t schedule;
   int32_t grid_factor;        /* hash-grid arena multiplier (0 = 1)         */
+  /* Polls before a neighbour-progress wait (the wavefront schedule, the
+     colour-phase schedule's tail segment) gives up; 0 = wait_limit (or its
+     default when that is 0 as well). Grid barriers keep wait_limit.        */
+  int32_t neighbor_wait_limit;
 } avbd_params;
 
 /*

@@ -179,11 +179,13 @@ def test_determinism(abi, scenes, backend_mod, schedule):
 def test_arena_regrow_preserves_results(abi, scenes, backend_mod):
     """Overflow-driven regrow (src/physics/gpu/backend.js:1683-1739): with a
     candidate arena sized just above the first step's need, the library grows
-    it ahead of overflow, carries the warm-start manifolds over, and the
-    trajectory is bit-identical to a run with ample capacity."""
+    it ahead of overflow; with one far below it (1 candidate per body), the
+    first step overflows, is skipped on the device, and runs again after the
+    regrow. Either way the warm-start manifolds carry over and the trajectory
+    is bit-identical to a run with ample capacity."""
     s = scenes.pyramid(layers=10)
     outs = []
-    for cap in (0, 9):
+    for cap in (0, 9, 1):
         params = abi.default_params(**s.params, body_order=abi.ORDER_PRIORITY, max_pairs_per_body=cap)
         gpu = backend_mod.GpuBackend(params)
         gpu.pack(s.world())
@@ -192,6 +194,30 @@ def test_arena_regrow_preserves_results(abi, scenes, backend_mod):
         assert gpu.last_stats["overflow"] == 0
         outs.append(gpu.read_state().pos.copy())
     assert np.array_equal(outs[0], outs[1])
+    assert np.array_equal(outs[0], outs[2])
+
+
+def test_overflow_retry_from_a_packed_pile(abi, scenes, backend_mod):
+    """A state packed with more warm-start manifolds than the default arena's
+    candidate headroom (a settled 12-layer pyramid, capacity 2 candidates per
+    body): the first step overflows mid-step, is skipped and redone after the
+    regrow, and equals the oracle's step from the same state."""
+    s = scenes.pyramid(layers=12)
+    params = params_for(abi, s)
+    o = Oracle(params, s.world())
+    o.step(60)
+    state = o.state().round_to_device()
+    ref = Oracle(params, state)
+    ref.step(1)
+    gpu = backend_mod.GpuBackend(params_for(abi, s, max_pairs_per_body=2))
+    gpu.pack(state)
+    gpu.step(1)
+    gpu.idle()
+    assert gpu.last_stats["overflow"] == 0 and gpu.last_stats["steps"] == 1
+    want, got = ref.state(), gpu.read_state(manifolds=True)
+    assert got.manifold_dict() == want.manifold_dict()
+    dyn = want.mass > 0
+    assert np.max(np.abs(got.pos[dyn] - want.pos[dyn])) <= POS_TOL
 
 
 def test_schedules_agree(abi, scenes, backend_mod):
@@ -266,3 +292,27 @@ def test_narrowphase_stress_topology(abi, scenes, backend_mod, seed):
     got = gpu.read_state(manifolds=True).manifold_dict()
     assert len(want) > 1000
     assert got == want
+
+
+@pytest.mark.parametrize("schedule", [0, 1])
+def test_more_colors_than_a_word(abi, scenes, backend_mod, schedule):
+    """A complete constraint graph of 72 bodies needs 72 colours, past the
+    64 of one bit word: the device colouring equals the oracle's greedy
+    priority colouring, one step matches the oracle, and 30 more steps run
+    without error within the reference harness's tolerance at step 4
+    (src/app/gputest.js:91-96) and the 30-step drift bound."""
+    s = scenes.joint_clique()
+    ref, gpu = compare_step(abi, backend_mod, s, 0, schedule=schedule)
+    oc, on = ref.coloring()
+    gc, gn = gpu.read_coloring()
+    assert on == 72 and gn == on and np.array_equal(gc, oc)
+    want, got = ref.state(), gpu.read_state()
+    dyn = want.mass > 0
+    assert np.max(np.abs(got.pos[dyn] - want.pos[dyn])) <= POS_TOL
+    assert np.max(np.abs(got.quat[dyn] - want.quat[dyn])) <= QUAT_TOL
+    ref.step(29)
+    gpu.step(29)
+    gpu.idle()
+    want, got = ref.state(), gpu.read_state()
+    assert gpu.last_stats["colors"] == 72 and gpu.last_stats["overflow"] == 0
+    assert np.max(np.abs(got.pos[dyn] - want.pos[dyn])) < 5e-3
