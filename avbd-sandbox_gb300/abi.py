@@ -51,7 +51,7 @@ class Params(C.Structure):
         ("max_pairs_per_body", C.c_int32), ("max_adjacency", C.c_int32),
         ("lanes_per_body", C.c_int32), ("blocks_per_sm", C.c_int32),
         ("schedule", C.c_int32), ("grid_factor", C.c_int32),
-        ("neighbor_wait_limit", C.c_int32),
+        ("neighbor_wait_limit", C.c_int32), ("tail_div", C.c_int32), ("graph", C.c_int32),
     ]
 
 
@@ -123,10 +123,31 @@ class Stats(C.Structure):
                 ("springs_broken", C.c_int64), ("colors", C.c_int32), ("fp64_bodies", C.c_int32),
                 ("overflow", C.c_uint32), ("steps", C.c_int32),
                 ("max_constraint_error", C.c_double), ("max_lambda", C.c_double),
-                ("max_penalty", C.c_double)]
+                ("max_penalty", C.c_double), ("graph_steps", C.c_int64)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+class Tuning(C.Structure):
+    _fields_ = [("schedule", C.c_int32), ("lanes_per_body", C.c_int32), ("tail_div", C.c_int32),
+                ("blocks_per_sm", C.c_int32), ("candidates", C.c_int32), ("trial_steps", C.c_int32),
+                ("default_ms", C.c_double), ("best_ms", C.c_double), ("bodies", C.c_int64),
+                ("manifolds", C.c_int64)]
+
+    def as_dict(self):
+        return {k: getattr(self, k) for k, _ in self._fields_}
+
+
+TANGENT_DIMS = 5
+SEED_VELOCITY = 0
+SEED_FRICTION = 1
+SEED_PENALTY_MAX = 2
+SEED_JOINT_STIFFNESS = 3
+
+
+class TangentSeed(C.Structure):
+    _fields_ = [("kind", C.c_int32), ("index", C.c_int32), ("comp", C.c_int32), ("dir", C.c_int32)]
 
 
 class DeviceViews(C.Structure):
@@ -142,7 +163,7 @@ class Profile(C.Structure):
                 ("candidate_pairs", C.c_int64), ("manifolds", C.c_int64), ("contacts", C.c_int64),
                 ("colors", C.c_int32), ("fp64_bodies", C.c_int32),
                 ("np_face", C.c_int32), ("np_edge", C.c_int32), ("np_exact", C.c_int32),
-                ("lanes_per_body", C.c_int32)]
+                ("lanes_per_body", C.c_int32), ("via_graph", C.c_int32)]
 
     def as_dict(self):
         return {k: getattr(self, k) for k, _ in self._fields_}
@@ -328,6 +349,41 @@ class World:
         w.m_capacity = len(w.m_body_a)
         w._c = None
         return w
+
+    def scene(self, s: int) -> "World":
+        """Scene `s` of a batched world as a world of its own: its bodies
+        renumbered from 0, its joints, springs and manifolds (constraints
+        never cross scenes)."""
+        b0, b1 = int(self.scene_start[s]), int(self.scene_start[s + 1])
+        js = np.nonzero((self.j_body_b >= b0) & (self.j_body_b < b1))[0]
+        ss = np.nonzero((self.s_body_b >= b0) & (self.s_body_b < b1))[0]
+        ms = np.nonzero((self.m_body_a[:self.m_count] >= b0) & (self.m_body_a[:self.m_count] < b1))[0]
+        out = World(b1 - b0, len(js), len(ss), max(len(ms), 1))
+        for f in ("shape", "size", "mass", "moment", "radius", "friction", "pos", "quat", "vel", "omega",
+                  "prev_vel"):
+            setattr(out, f, np.ascontiguousarray(getattr(self, f)[b0:b1]))
+        for f in ("j_r_a", "j_r_b", "j_stiffness_lin", "j_stiffness_ang", "j_fracture", "j_penalty_lin",
+                  "j_penalty_ang", "j_lambda_lin", "j_lambda_ang", "j_broken"):
+            setattr(out, f, np.ascontiguousarray(getattr(self, f)[js]))
+        out.j_body_a = np.where(self.j_body_a[js] < 0, -1, self.j_body_a[js] - b0).astype(np.int32)
+        out.j_body_b = (self.j_body_b[js] - b0).astype(np.int32)
+        for f in ("s_r_a", "s_r_b", "s_stiffness", "s_rest", "s_tear_strain", "s_penalty", "s_peak_strain",
+                  "s_broken"):
+            setattr(out, f, np.ascontiguousarray(getattr(self, f)[ss]))
+        out.s_body_a = (self.s_body_a[ss] - b0).astype(np.int32)
+        out.s_body_b = (self.s_body_b[ss] - b0).astype(np.int32)
+        order = np.argsort(np.concatenate([self.j_order[js], self.s_order[ss]]), kind="stable")
+        rank = np.empty(len(order), np.int32)
+        rank[order] = np.arange(len(order), dtype=np.int32)
+        out.j_order, out.s_order = rank[:len(js)].copy(), rank[len(js):].copy()
+        out.m_count = len(ms)
+        for f in ("m_num_contacts", "m_basis", "m_friction", "m_feature", "m_r_a", "m_r_b", "m_c0", "m_penalty",
+                  "m_lambda", "m_stick"):
+            getattr(out, f)[:len(ms)] = getattr(self, f)[ms]
+        out.m_body_a[:len(ms)] = self.m_body_a[ms] - b0
+        out.m_body_b[:len(ms)] = self.m_body_b[ms] - b0
+        out.m_order[:len(ms)] = np.arange(len(ms))
+        return out
 
     def manifold_dict(self):
         """Live manifolds keyed by (A, B) -> (num_contacts, features tuple)."""

@@ -61,6 +61,15 @@ def load_library(path: str = LIB_PATH):
     L.avbd_update_joint_anchor.restype = C.c_int
     L.avbd_device_views_get.argtypes = [vp, vp]
     L.avbd_device_views_get.restype = C.c_int
+    L.avbd_autotune.argtypes = [vp, C.c_int32, vp]
+    L.avbd_autotune.restype = C.c_int
+    L.avbd_set_grab.argtypes = [vp, C.c_int32, vp, vp, C.c_double]
+    L.avbd_set_grab.restype = C.c_int
+    L.avbd_adjoint_forward.argtypes = [vp, vp, C.c_int32, vp, C.c_int32]
+    L.avbd_adjoint_read.argtypes = [vp, vp, vp, vp]
+    L.avbd_adjoint_backward.argtypes = [vp, vp, vp]
+    for name in ("avbd_adjoint_forward", "avbd_adjoint_read", "avbd_adjoint_backward"):
+        getattr(L, name).restype = C.c_int
     for name in ("avbd_create", "avbd_destroy", "avbd_pack", "avbd_step", "avbd_synchronize", "avbd_read_state",
                  "avbd_write_state", "avbd_read_coloring", "avbd_read_pairs", "avbd_read_stats",
                  "avbd_set_profiling", "avbd_read_profile", "avbd_kernel_launches"):
@@ -168,12 +177,59 @@ class GpuBackend:
         a = np.ascontiguousarray(r_a, dtype=np.float64)
         self._check(self.L.avbd_update_joint_anchor(self.h, int(joint), a.ctypes.data_as(C.c_void_p)))
 
+    def set_grab(self, body: int, local=(0.0, 0.0, 0.0), target=(0.0, 0.0, 0.0), stiffness: float = 0.0):
+        """The reference's `grab` ({body, local, target, stiffness},
+        backend.js:302-307): a topology-free pull of `body`'s local point
+        toward the world `target`; body = -1 releases."""
+        if body < 0:
+            self._check(self.L.avbd_set_grab(self.h, -1, None, None, 0.0))
+            return
+        a = np.ascontiguousarray(local, dtype=np.float64)
+        b = np.ascontiguousarray(target, dtype=np.float64)
+        self._check(self.L.avbd_set_grab(self.h, int(body), a.ctypes.data_as(C.c_void_p),
+                                         b.ctypes.data_as(C.c_void_p), float(stiffness)))
+
     def device_views(self) -> dict:
         """getConstraintGpuState (backend.js:1950-1967): device pointers of the
         live body poses and joint/spring state."""
         v = abi.DeviceViews()
         self._check(self.L.avbd_device_views_get(self.h, C.byref(v)))
         return {k: getattr(v, k) for k, _ in v._fields_}
+
+    def autotune(self, trial_steps: int = 3) -> dict:
+        """Time the solve's launch configurations from the current state, keep
+        the fastest (the state is put back unchanged) and return the choice."""
+        t = abi.Tuning()
+        self._check(self.L.avbd_autotune(self.h, int(trial_steps), C.byref(t)))
+        return t.as_dict()
+
+    # --- the differentiable step ---------------------------------------------
+    def adjoint_forward(self, world: abi.World, steps: int, seeds):
+        """avbd_adjoint_forward: `steps` differentiable steps of `world`,
+        seeds = [(kind, index, comp, direction), ...] (abi.SEED_*)."""
+        arr = (abi.TangentSeed * max(len(seeds), 1))()
+        for k, (kind, index, comp, d) in enumerate(seeds):
+            arr[k] = abi.TangentSeed(kind, index, comp, d)
+        self._tangent_world = world.copy()
+        wc = self._tangent_world.c(with_manifolds=False)
+        self._check(self.L.avbd_adjoint_forward(self.h, C.byref(wc), int(steps), arr, len(seeds)))
+
+    def adjoint_read(self):
+        """Positions (n, 3), their derivatives (n, 3, TANGENT_DIMS), orientations (n, 4)."""
+        n = self._tangent_world.n_bodies
+        pos = np.zeros((n, 3))
+        dpos = np.zeros((n, 3, abi.TANGENT_DIMS))
+        quat = np.zeros((n, 4))
+        self._check(self.L.avbd_adjoint_read(self.h, pos.ctypes.data_as(C.c_void_p), dpos.ctypes.data_as(C.c_void_p),
+                                             quat.ctypes.data_as(C.c_void_p)))
+        return pos, dpos, quat
+
+    def adjoint_backward(self, grad_pos) -> np.ndarray:
+        """Vector-Jacobian product: d<grad_pos, pos_T> / d theta for each direction."""
+        g = np.ascontiguousarray(grad_pos, dtype=np.float64)
+        out = np.zeros(abi.TANGENT_DIMS)
+        self._check(self.L.avbd_adjoint_backward(self.h, g.ctypes.data_as(C.c_void_p), out.ctypes.data_as(C.c_void_p)))
+        return out
 
     @property
     def last_stats(self) -> dict:

@@ -23,6 +23,7 @@ UNITS = {
     "broadphase.cu": ["--fmad=false"],
     "solver.cu": [],
     "host.cu": [],
+    "tangent.cu": ["--fmad=false"],
 }
 
 
@@ -42,7 +43,8 @@ def _stale(out, deps):
 
 def build(force: bool = False, verbose: bool = False, ptxas_verbose: bool = False) -> str:
     os.makedirs(BUILD, exist_ok=True)
-    headers = [os.path.join(CSRC, "avbd_device.cuh"), os.path.join(HERE, "..", "include", "avbd_cuda.h")]
+    headers = [os.path.join(CSRC, h) for h in ("avbd_device.cuh", "collider.cuh", "dual.cuh")]
+    headers.append(os.path.join(HERE, "..", "include", "avbd_cuda.h"))
     objs = []
     jobs = []
     for unit, extra in UNITS.items():

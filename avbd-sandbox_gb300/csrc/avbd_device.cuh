@@ -67,6 +67,7 @@ struct SolverParams {
   int lanes;     // lanes per body of the colour-phase solve; 0: per body, from its constraint count
   int solveBlocksPerSm;  // resident blocks per SM of the solve launch (grid = this x SMs)
   long long barrierLimit, waitLimit;  // polls before a grid barrier / a neighbour wait gives up
+  int tailDiv;   // colours of at most (grid / tailDiv) chunks form the tail segment
 };
 
 // Device scalars shared by all kernels of a step.
@@ -232,6 +233,17 @@ struct Adjacency {
   int *laneHist;     // 2 * kMaxColors * kLaneBuckets: group counts, then lane cursors
 };
 
+// The uniform mouse grab (src/physics/gpu/shaders.js:2119-2161): a finite
+// ball socket from a world target to a body-local point of one body, penalty
+// fixed at the stiffness, no multiplier, applied in that body's primal only.
+struct __align__(32) Grab {
+  D4 target;     // world point, f64
+  D4 localD;     // body-local anchor, f64 (FP64 bodies)
+  float4 local;  // the same, f32
+  double k;      // stiffness
+  int body;      // -1: nothing grabbed
+};
+
 // Everything a kernel may touch.
 struct World {
   SolverParams p;
@@ -242,6 +254,7 @@ struct World {
   Grid g;
   Adjacency a;
   Control *ctl;
+  Grab *grab;
 };
 
 // ---------------------------------------------------------------------------
@@ -382,14 +395,23 @@ void launch_broadphase_impl(const World &w, int numLarge, void *temp, size_t tem
 void launch_narrowphase(const World &w, cudaStream_t st, int smCount);
 size_t solver_temp_bytes(int n);
 void launch_prepare(const World &w, void *temp, size_t tempBytes, cudaStream_t st, int smCount);
-cudaError_t launch_coloring(const World &w, cudaStream_t st, int smCount);
-int coloring_grid(int smCount);
+cudaError_t launch_coloring(const World &w, cudaStream_t st, int blocks);
+int coloring_grid(int smCount);  // blocks of the cooperative colouring launch
 cudaError_t launch_solve(const World &w, int lanesPerBody, int blocksPerSm, cudaStream_t st, int smCount);
 int solve_max_blocks_per_sm(int lanesPerBody);
 void launch_commit(const World &w, cudaStream_t st, int smCount);
 void launch_stats(const World &w, double *out3, cudaStream_t st, int smCount);
 cudaError_t launch_joint_anchor(const World &w, int joint, double x, double y, double z, cudaStream_t st);
+cudaError_t launch_set_grab(const World &w, int body, const double *local, const double *target, double k,
+                            cudaStream_t st);
 // Error text of a context-free ABI call (read back by avbd_last_error(NULL)).
 int set_context_free_error(int code, const char *msg);
+// The differentiable step (tangent.cu).
+struct TangentCtx;
+void tangent_destroy(TangentCtx *t);
+size_t tangent_temp_bytes(const TangentCtx *t);
+int tangent_step(TangentCtx *t, int steps, void *temp, size_t tempBytes, char *msg, size_t msgLen, cudaStream_t st);
+int tangent_read(TangentCtx *t, double *pos, double *dpos, double *quat, cudaStream_t st);
+int tangent_backward(TangentCtx *t, const double *gradPos, double *gradParams, cudaStream_t st);
 
 }  // namespace avbd

@@ -27,6 +27,11 @@
 
 using namespace avbd;
 
+namespace avbd {
+int tangent_pack(TangentCtx **out, const avbd_world *world, const avbd_params &P, const avbd_tangent_seed *seeds,
+                 int nSeeds, char *msg, size_t msgLen, cudaStream_t st);
+}
+
 namespace {
 
 const char *g_create_error = "";
@@ -147,6 +152,20 @@ struct avbd_ctx {
   std::unique_ptr<HostPool> pool;  // per-body host conversions
   cudaEvent_t stepEv[8]{};
   int64_t stepSeq = 0;
+  // CUDA graphs of one step, one per manifold-arena parity (the arenas swap
+  // every step, and their pointers are part of the launches' arguments);
+  // rebuilt after anything that changes a launch (pack, regrow, an uploaded
+  // colouring, a new schedule)
+  cudaGraphExec_t graphExec[2]{};
+  bool graphFailed = false;  // a capture failed: this context launches directly
+  int stepKernels = 0;       // own kernels of one step (the launch count)
+  int64_t graphSteps = 0;    // steps run as a graph
+  int maxBlocksPerSm = 1;    // resident solve blocks per SM at most
+  bool capturing = false;    // a graph capture is recording the step
+  bool lastViaGraph = false; // the last step ran as a graph
+  TangentCtx *tangent = nullptr;  // the differentiable step (avbd_adjoint_forward)
+  void *tanTemp = nullptr;
+  size_t tanTempBytes = 0;
 };
 
 namespace {
@@ -196,7 +215,10 @@ int upload(avbd_ctx *ctx, T **p, const std::vector<T> &h) {
   return AVBD_OK;
 }
 
+void invalidate_graphs(avbd_ctx *ctx);
+
 void free_all(avbd_ctx *ctx) {
+  invalidate_graphs(ctx);
   for (void *p : ctx->allocs) cudaFree(p);
   ctx->allocs.clear();
   for (void *p : ctx->growable) cudaFree(p);
@@ -254,6 +276,7 @@ int alloc_candidate_arenas(avbd_ctx *ctx, int cap) {
 // been stepped last (`old`, `keep` of them: the warm-start state of the next
 // step) move into the new "previous" arena.
 int grow_arenas(avbd_ctx *ctx, int cap, const Manifolds old, int keep) {
+  invalidate_graphs(ctx);
   std::vector<void *> oldBufs;
   oldBufs.swap(ctx->growable);
   int rc = alloc_candidate_arenas(ctx, cap);
@@ -344,7 +367,7 @@ bool finite3(const double *p) { return std::isfinite(p[0]) && std::isfinite(p[1]
 
 
 int record(avbd_ctx *ctx, int k) {
-  if (ctx->profiling) CK(cudaEventRecord(ctx->ev[k], ctx->stream));
+  if (ctx->profiling && !ctx->capturing) CK(cudaEventRecord(ctx->ev[k], ctx->stream));
   return AVBD_OK;
 }
 
@@ -484,6 +507,82 @@ int write_state(avbd_ctx *ctx, const avbd_world *world, bool keepManifolds) {
 // colour-phase schedule takes each body's lanes from the colouring's layout.
 int wave_lanes(const avbd_ctx *ctx) { return ctx->autoLanes ? 32 : ctx->lanes; }
 
+void invalidate_graphs(avbd_ctx *ctx) {
+  for (auto &g : ctx->graphExec)
+    if (g) {
+      cudaGraphExecDestroy(g);
+      g = nullptr;
+    }
+}
+
+// The launch sequence of one step on the context's stream (what a graph
+// captures); the profiling events between the phases only when profiling.
+int enqueue_step(avbd_ctx *ctx) {
+  World &w = ctx->w;
+  cudaStream_t st = ctx->stream;
+  // per-step counters: numCandidates .. adjTotal
+  CK(cudaMemsetAsync(&w.ctl->numCandidates, 0, sizeof(int) * 7, st));
+  int rc;
+  if ((rc = record(ctx, 0))) return rc;
+  launch_broadphase_impl(w, ctx->numLarge, ctx->bpTemp, ctx->bpTempBytes, st, ctx->smCount);
+  if ((rc = record(ctx, 1))) return rc;
+  launch_narrowphase(w, st, ctx->smCount);
+  if ((rc = record(ctx, 2))) return rc;
+  launch_prepare(w, ctx->svTemp, ctx->svTempBytes, st, ctx->smCount);
+  if ((rc = record(ctx, 3))) return rc;
+  CK(launch_coloring(w, st, ctx->colorBlocks));
+  if ((rc = record(ctx, 4))) return rc;
+  CK(launch_solve(w, wave_lanes(ctx), ctx->blocksPerSm, st, ctx->smCount));
+  if ((rc = record(ctx, 5))) return rc;
+  launch_commit(w, st, ctx->smCount);
+  // (commit_kernel made this step's candidates the next step's previous
+  // manifolds, unless the step was skipped)
+  CK(cudaMemcpyAsync(ctx->hCand, &w.ctl->stepsSkipped, 2 * sizeof(int), cudaMemcpyDeviceToHost, st));
+  return record(ctx, 6);
+}
+
+// Own kernels of one step: broad phase 6 (+4 with large bodies; its two scans
+// are library code), narrow phase 4, prepare 5, colouring 1 (+2 with an
+// uploaded colouring), solve 1, commit 1.
+int step_kernels(const avbd_ctx *ctx) {
+  return 6 + (ctx->numLarge > 0 ? 4 : 0) + 4 + 5 + 1 + (ctx->w.a.colorOverride ? 2 : 0) + 1 + 1;
+}
+
+// One step as a CUDA graph (captured on first use for this arena parity).
+// Returns false when graphs are off, profiling is on, or capture failed (the
+// context then launches directly from now on).
+bool launch_step_graph(avbd_ctx *ctx, int *rc) {
+  *rc = AVBD_OK;
+  if (!ctx->params.graph || ctx->graphFailed) return false;
+  const int slot = ctx->curIsA ? 1 : 0;
+  cudaStream_t st = ctx->stream;
+  if (!ctx->graphExec[slot]) {
+    cudaGraph_t g = nullptr;
+    if (cudaStreamBeginCapture(st, cudaStreamCaptureModeThreadLocal) != cudaSuccess) {
+      cudaGetLastError();
+      ctx->graphFailed = true;
+      return false;
+    }
+    ctx->capturing = true;
+    const int erc = enqueue_step(ctx);
+    ctx->capturing = false;
+    const cudaError_t e = cudaStreamEndCapture(st, &g);
+    cudaGraphExec_t exec = nullptr;
+    if (erc == AVBD_OK && e == cudaSuccess && g && cudaGraphInstantiate(&exec, g, 0) == cudaSuccess) {
+      ctx->graphExec[slot] = exec;
+    } else {
+      cudaGetLastError();  // a launch this stream cannot capture: launch directly
+      ctx->graphFailed = true;
+    }
+    if (g) cudaGraphDestroy(g);
+    if (ctx->graphFailed) return false;
+  }
+  const cudaError_t e = cudaGraphLaunch(ctx->graphExec[slot], st);
+  if (e != cudaSuccess) *rc = fail(ctx, AVBD_ERR_CUDA, "cudaGraphLaunch: %s", cudaGetErrorString(e));
+  ctx->graphSteps++;
+  return true;
+}
+
 int one_step(avbd_ctx *ctx) {
   if (ctx->stepSeq >= avbd_ctx::kRunAhead)
     CK(cudaEventSynchronize(ctx->stepEv[(ctx->stepSeq - avbd_ctx::kRunAhead) % 8]));
@@ -492,31 +591,15 @@ int one_step(avbd_ctx *ctx) {
   World &w = ctx->w;
   set_world_manifolds(ctx);
   cudaStream_t st = ctx->stream;
-  // per-step counters: numCandidates .. adjTotal
-  CK(cudaMemsetAsync(&w.ctl->numCandidates, 0, sizeof(int) * 7, st));
-  int rc;
-  if ((rc = record(ctx, 0))) return rc;
-  launch_broadphase_impl(w, ctx->numLarge, ctx->bpTemp, ctx->bpTempBytes, st, ctx->smCount);
-  ctx->launches += 6 + (ctx->numLarge > 0 ? 4 : 0);  // own kernels (the two scans are library code)
-  if ((rc = record(ctx, 1))) return rc;
-  launch_narrowphase(w, st, ctx->smCount);
-  ctx->launches += 4;
-  if ((rc = record(ctx, 2))) return rc;
-  launch_prepare(w, ctx->svTemp, ctx->svTempBytes, st, ctx->smCount);
-  ctx->launches += 5;
-  if ((rc = record(ctx, 3))) return rc;
-  CK(launch_coloring(w, st, ctx->smCount));
-  ctx->launches += 1 + (w.a.colorOverride ? 2 : 0);
-  if ((rc = record(ctx, 4))) return rc;
-  CK(launch_solve(w, wave_lanes(ctx), ctx->blocksPerSm, st, ctx->smCount));
-  ctx->launches += 1;
-  if ((rc = record(ctx, 5))) return rc;
-  launch_commit(w, st, ctx->smCount);
-  ctx->launches += 1;
-  // (commit_kernel made this step's candidates the next step's previous
-  // manifolds, unless the step was skipped)
-  CK(cudaMemcpyAsync(ctx->hCand, &w.ctl->stepsSkipped, 2 * sizeof(int), cudaMemcpyDeviceToHost, st));
-  if ((rc = record(ctx, 6))) return rc;
+  // a profiled graph step has the whole step's events only (no phase split)
+  int rc = AVBD_OK;
+  if (ctx->params.graph && !ctx->graphFailed && (rc = record(ctx, 0))) return rc;
+  ctx->lastViaGraph = launch_step_graph(ctx, &rc);
+  if (rc) return rc;
+  if (ctx->lastViaGraph) rc = record(ctx, 6);
+  else rc = enqueue_step(ctx);
+  if (rc) return rc;
+  ctx->launches += step_kernels(ctx);
   CK(cudaEventRecord(ctx->stepEv[ctx->stepSeq % 8], st));
   ctx->stepSeq++;
   CK(cudaGetLastError());
@@ -524,8 +607,10 @@ int one_step(avbd_ctx *ctx) {
   ctx->steps++;
   if (ctx->profiling) {
     CK(cudaEventSynchronize(ctx->ev[6]));
-    float t[5];
-    for (int k = 0; k < 5; k++) cudaEventElapsedTime(&t[k], ctx->ev[k], ctx->ev[k + 1]);
+    float t[5] = {0, 0, 0, 0, 0};
+    if (!ctx->lastViaGraph)
+      for (int k = 0; k < 5; k++) cudaEventElapsedTime(&t[k], ctx->ev[k], ctx->ev[k + 1]);
+    ctx->prof.via_graph = ctx->lastViaGraph ? 1 : 0;
     ctx->prof.broadphase_ms = t[0];
     ctx->prof.narrowphase_ms = t[1];
     ctx->prof.prepare_ms = t[2];
@@ -575,6 +660,113 @@ int check_flags(avbd_ctx *ctx) {
                 kMaxColors);
   }
   return AVBD_OK;
+}
+
+// --- autotuner --------------------------------------------------------------
+// The device arrays a step changes, as (address, bytes): body state and
+// colours (the colouring's seed), joint and spring state, the warm-start
+// manifolds (`keep` of them, in the arena the next step reads) and the
+// control block. Saved and put back around the tuner's trial steps.
+std::vector<std::pair<void *, size_t>> mutable_regions(avbd_ctx *ctx, int keep) {
+  World &w = ctx->w;
+  const size_t n = ctx->n, nj = ctx->nj, ns = ctx->ns, K = kMaxContacts, m = keep;
+  const Manifolds &pm = ctx->curIsA ? ctx->mB : ctx->mA;
+  std::vector<std::pair<void *, size_t>> r = {
+      {w.b.pos, n * sizeof(D4)}, {w.b.quat, n * sizeof(float4)}, {w.b.vel, n * sizeof(float4)},
+      {w.b.omega, n * sizeof(float4)}, {w.b.prevVel, n * sizeof(float4)}, {w.b.color, n * sizeof(int)},
+      {w.j.penLin, nj * sizeof(float4)}, {w.j.penAng, nj * sizeof(float4)}, {w.j.lamLin, nj * sizeof(D4)},
+      {w.j.lamAng, nj * sizeof(D4)}, {w.j.state, nj * sizeof(int)}, {w.s.penalty, ns * sizeof(float)},
+      {w.s.peak, ns * sizeof(double)}, {w.s.state, ns * sizeof(int)}, {pm.key, m * sizeof(uint64_t)},
+      {pm.count, m * sizeof(int)}, {pm.basis0, m * sizeof(float4)}, {pm.basis1, m * sizeof(float4)},
+      {pm.basis2, m * sizeof(float4)}, {pm.basisD, m * 9 * sizeof(double)}, {pm.feat, m * K * sizeof(uint32_t)},
+      {pm.rA, m * K * sizeof(float4)}, {pm.rB, m * K * sizeof(float4)}, {pm.cA, m * K * sizeof(float4)},
+      {pm.cB, m * K * sizeof(float4)}, {pm.cK, m * K * sizeof(float4)}, {pm.cL, m * K * sizeof(float4)},
+      {w.ctl, sizeof(Control)}};
+  return r;
+}
+
+struct Snapshot {
+  void *blob = nullptr;
+  int keep = 0, steps = 0;
+  ~Snapshot() {
+    if (blob) cudaFree(blob);
+  }
+};
+
+int take_snapshot(avbd_ctx *ctx, Snapshot &s) {
+  int rc = resolve_skips(ctx);
+  if (rc) return rc;
+  Control c{};
+  CK(cudaMemcpy(&c, ctx->w.ctl, sizeof(Control), cudaMemcpyDeviceToHost));
+  s.keep = c.prevCandidates;
+  s.steps = ctx->steps;
+  size_t total = 0;
+  for (auto &r : mutable_regions(ctx, s.keep)) total += (r.second + 255) & ~size_t(255);
+  CK(cudaMalloc(&s.blob, std::max<size_t>(total, 256)));
+  size_t at = 0;
+  for (auto &r : mutable_regions(ctx, s.keep)) {
+    if (r.second) CK(cudaMemcpyAsync((char *)s.blob + at, r.first, r.second, cudaMemcpyDeviceToDevice, ctx->stream));
+    at += (r.second + 255) & ~size_t(255);
+  }
+  CK(cudaStreamSynchronize(ctx->stream));
+  return AVBD_OK;
+}
+
+int restore_snapshot(avbd_ctx *ctx, const Snapshot &s) {
+  int rc = resolve_skips(ctx);
+  if (rc) return rc;
+  size_t at = 0;
+  for (auto &r : mutable_regions(ctx, s.keep)) {
+    if (r.second) CK(cudaMemcpyAsync(r.first, (char *)s.blob + at, r.second, cudaMemcpyDeviceToDevice, ctx->stream));
+    at += (r.second + 255) & ~size_t(255);
+  }
+  CK(cudaStreamSynchronize(ctx->stream));
+  ctx->hCand[0] = 0;
+  ctx->hCand[1] = 0;
+  ctx->steps = s.steps;
+  return AVBD_OK;
+}
+
+struct TuneConfig {
+  int schedule, lanes, tailDiv, blocksPerSm;
+};
+
+void apply_config(avbd_ctx *ctx, const TuneConfig &c) {
+  avbd_params &P = ctx->params;
+  P.schedule = c.schedule;
+  P.lanes_per_body = c.lanes;
+  P.tail_div = c.tailDiv;
+  P.blocks_per_sm = c.blocksPerSm;
+  ctx->w.p.schedule = c.schedule == 1 ? 1 : 0;
+  ctx->w.p.lanes = c.lanes > 0 ? c.lanes : 0;
+  ctx->w.p.tailDiv = c.tailDiv > 0 ? c.tailDiv : 8;
+  ctx->autoLanes = c.lanes <= 0;
+  ctx->lanes = c.lanes > 0 ? c.lanes : 32;
+  ctx->blocksPerSm = c.blocksPerSm;
+  ctx->w.p.solveBlocksPerSm = c.blocksPerSm;
+  invalidate_graphs(ctx);
+}
+
+// Mean device time of `steps` steps from the snapshot's state (one untimed
+// step first, which also captures the graphs), then the snapshot restored.
+int time_config(avbd_ctx *ctx, const Snapshot &snap, int steps, double *ms) {
+  int rc;
+  if ((rc = restore_snapshot(ctx, snap)) || (rc = one_step(ctx)) || (rc = restore_snapshot(ctx, snap))) return rc;
+  cudaEvent_t a, b;
+  CK(cudaEventCreate(&a));
+  CK(cudaEventCreate(&b));
+  CK(cudaEventRecord(a, ctx->stream));
+  for (int k = 0; k < steps && !rc; k++) rc = one_step(ctx);
+  cudaEventRecord(b, ctx->stream);
+  cudaEventSynchronize(b);
+  float t = 0;
+  cudaEventElapsedTime(&t, a, b);
+  cudaEventDestroy(a);
+  cudaEventDestroy(b);
+  if (rc) return rc;
+  if ((rc = check_flags(ctx))) return rc;
+  *ms = t / std::max(steps, 1);
+  return restore_snapshot(ctx, snap);
 }
 
 }  // namespace
@@ -636,6 +828,8 @@ int avbd_destroy(avbd_ctx *ctx) {
   if (!ctx) return AVBD_OK;
   cudaStreamSynchronize(ctx->stream);
   free_all(ctx);
+  if (ctx->tangent) tangent_destroy(ctx->tangent);
+  if (ctx->tanTemp) cudaFree(ctx->tanTemp);
   for (auto &e : ctx->ev)
     if (e) cudaEventDestroy(e);
   for (auto &e : ctx->stepEv)
@@ -803,7 +997,8 @@ int avbd_pack(avbd_ctx *ctx, const avbd_world *world) {
                      P.fp64_ratio_threshold, P.schedule == 1 ? 1 : 0, P.lanes_per_body > 0 ? P.lanes_per_body : 0, 1,
                      P.wait_limit > 0 ? (long long)P.wait_limit : 20000000LL,
                      P.neighbor_wait_limit > 0 ? (long long)P.neighbor_wait_limit
-                                               : (P.wait_limit > 0 ? (long long)P.wait_limit : 4000000LL)};
+                                               : (P.wait_limit > 0 ? (long long)P.wait_limit : 4000000LL),
+                     P.tail_div > 0 ? P.tail_div : 8};
   int rc = 0;
   D4 *sizeP, *massDP;
   float4 *massFP;
@@ -891,7 +1086,9 @@ int avbd_pack(avbd_ctx *ctx, const avbd_world *world) {
   ctx->hCand[0] = ctx->hCand[1] = 0;
   ctx->curIsA = 1;
   set_world_manifolds(ctx);
-  if ((rc = dalloc(ctx, &w.ctl, 1)) || (rc = dalloc(ctx, &ctx->statsOut, 3))) return rc;
+  if ((rc = dalloc(ctx, &w.ctl, 1)) || (rc = dalloc(ctx, &ctx->statsOut, 3)) || (rc = dalloc(ctx, &w.grab, 1)))
+    return rc;
+  CK(launch_set_grab(w, -1, nullptr, nullptr, 0.0, ctx->stream));  // nothing grabbed
   // scratch of the scans
   ctx->bpTempBytes = broadphase_temp_bytes(n, ctx->tableSize);
   ctx->svTempBytes = solver_temp_bytes(n);
@@ -910,6 +1107,7 @@ int avbd_pack(avbd_ctx *ctx, const avbd_world *world) {
   if (ctx->lanes != 1 && ctx->lanes != 2 && ctx->lanes != 4 && ctx->lanes != 8 && ctx->lanes != 16 && ctx->lanes != 32)
     return fail(ctx, AVBD_ERR_ARG, "lanes_per_body must be a power of two <= 32");
   ctx->blocksPerSm = P.blocks_per_sm > 0 ? std::min(P.blocks_per_sm, maxPerSm) : maxPerSm;
+  ctx->maxBlocksPerSm = maxPerSm;
   if (ctx->blocksPerSm < 1) return fail(ctx, AVBD_ERR_CUDA, "solve kernel cannot be made resident");
   w.p.solveBlocksPerSm = ctx->blocksPerSm;
   // colours start at 0 for dynamic bodies
@@ -923,6 +1121,8 @@ int avbd_pack(avbd_ctx *ctx, const avbd_world *world) {
   ctx->stepSeq = 0;
   ctx->steps = 0;
   ctx->launches = 0;
+  ctx->graphSteps = 0;
+  ctx->graphFailed = false;
   rc = write_state(ctx, world, false);
   if (rc) return rc;
   CK(cudaDeviceSynchronize());
@@ -1146,6 +1346,7 @@ int avbd_read_stats(avbd_ctx *ctx, avbd_stats *out) {
   out->max_constraint_error = st3[0];
   out->max_lambda = st3[1];
   out->max_penalty = st3[2];
+  out->graph_steps = ctx->graphSteps;
   if (ctx->nj) {
     std::vector<int> st(ctx->nj);
     CK(cudaMemcpy(st.data(), w.j.state, ctx->nj * sizeof(int), cudaMemcpyDeviceToHost));
@@ -1182,6 +1383,7 @@ int avbd_set_coloring(avbd_ctx *ctx, const int32_t *color_of) {
   if (!ctx->packed) return fail(ctx, AVBD_ERR_STATE, "avbd_set_coloring before avbd_pack");
   int rs = resolve_skips(ctx);
   if (rs) return rs;
+  invalidate_graphs(ctx);  // the step's launch sequence changes
   if (!color_of) {
     ctx->w.a.colorOverride = nullptr;
     return AVBD_OK;
@@ -1208,6 +1410,22 @@ int avbd_update_joint_anchor(avbd_ctx *ctx, int32_t joint, const double r_a[3]) 
   return AVBD_OK;
 }
 
+int avbd_set_grab(avbd_ctx *ctx, int32_t body, const double local[3], const double target[3], double stiffness) {
+  if (!ctx) return AVBD_ERR_ARG;
+  if (!ctx->packed) return fail(ctx, AVBD_ERR_STATE, "avbd_set_grab before avbd_pack");
+  if (body >= ctx->n) return fail(ctx, AVBD_ERR_ARG, "grab body %d out of range (%d bodies)", body, ctx->n);
+  if (body >= 0) {
+    if (!local || !target) return fail(ctx, AVBD_ERR_ARG, "avbd_set_grab: NULL anchor");
+    if (!finite3(local) || !finite3(target) || !(stiffness > 0) || !std::isfinite(stiffness))
+      return fail(ctx, AVBD_ERR_ARG, "avbd_set_grab: anchors must be finite and the stiffness finite and > 0");
+  }
+  int rs = resolve_skips(ctx);  // the grab applies after the steps already queued
+  if (rs) return rs;
+  CK(launch_set_grab(ctx->w, body < 0 ? -1 : body, local, target, stiffness, ctx->stream));
+  ctx->launches += 1;
+  return AVBD_OK;
+}
+
 int avbd_device_views_get(avbd_ctx *ctx, avbd_device_views *out) {
   if (!ctx || !out) return AVBD_ERR_ARG;
   if (!ctx->packed) return fail(ctx, AVBD_ERR_STATE, "avbd_device_views_get before avbd_pack");
@@ -1222,6 +1440,103 @@ int avbd_device_views_get(avbd_ctx *ctx, avbd_device_views *out) {
 }
 
 const char *avbd_last_error(const avbd_ctx *ctx) { return ctx ? ctx->err.c_str() : g_create_error; }
+
+int avbd_adjoint_forward(avbd_ctx *ctx, const avbd_world *world, int32_t steps, const avbd_tangent_seed *seeds,
+                         int32_t n_seeds) {
+  if (!ctx || !world || steps < 0 || n_seeds < 0 || (n_seeds > 0 && !seeds))
+    return fail(ctx, AVBD_ERR_ARG, "avbd_adjoint_forward: NULL argument or negative count");
+  char msg[256] = "";
+  CK(cudaStreamSynchronize(ctx->stream));
+  if (ctx->tangent) {
+    tangent_destroy(ctx->tangent);
+    ctx->tangent = nullptr;
+  }
+  TangentCtx *t = nullptr;
+  int rc = tangent_pack(&t, world, ctx->params, seeds, n_seeds, msg, sizeof(msg), ctx->stream);
+  if (rc) return fail(ctx, rc, "%s", msg);
+  ctx->tangent = t;
+  const size_t need = tangent_temp_bytes(t);
+  if (need > ctx->tanTempBytes) {
+    if (ctx->tanTemp) cudaFree(ctx->tanTemp);
+    ctx->tanTemp = nullptr;
+    ctx->tanTempBytes = 0;
+    CK(cudaMalloc(&ctx->tanTemp, need));
+    ctx->tanTempBytes = need;
+  }
+  rc = tangent_step(t, steps, ctx->tanTemp, ctx->tanTempBytes, msg, sizeof(msg), ctx->stream);
+  if (rc) return fail(ctx, rc, "%s", msg);
+  ctx->launches += (int64_t)steps * 9;
+  return AVBD_OK;
+}
+
+int avbd_adjoint_read(avbd_ctx *ctx, double *pos, double *dpos, double *quat) {
+  if (!ctx) return AVBD_ERR_ARG;
+  if (!ctx->tangent) return fail(ctx, AVBD_ERR_STATE, "avbd_adjoint_read before avbd_adjoint_forward");
+  if (!pos) return fail(ctx, AVBD_ERR_ARG, "avbd_adjoint_read: NULL positions");
+  const int rc = tangent_read(ctx->tangent, pos, dpos, quat, ctx->stream);
+  return rc ? fail(ctx, rc, "avbd_adjoint_read: CUDA error") : AVBD_OK;
+}
+
+int avbd_adjoint_backward(avbd_ctx *ctx, const double *grad_pos, double *grad_params) {
+  if (!ctx || !grad_pos || !grad_params) return fail(ctx, AVBD_ERR_ARG, "avbd_adjoint_backward: NULL argument");
+  if (!ctx->tangent) return fail(ctx, AVBD_ERR_STATE, "avbd_adjoint_backward before avbd_adjoint_forward");
+  const int rc = tangent_backward(ctx->tangent, grad_pos, grad_params, ctx->stream);
+  return rc ? fail(ctx, rc, "avbd_adjoint_backward: CUDA error") : AVBD_OK;
+}
+
+int avbd_autotune(avbd_ctx *ctx, int32_t trial_steps, avbd_tuning *out) {
+  if (!ctx || !out || trial_steps < 1) return fail(ctx, AVBD_ERR_ARG, "avbd_autotune: NULL argument or trial_steps < 1");
+  if (!ctx->packed) return fail(ctx, AVBD_ERR_STATE, "avbd_autotune before avbd_pack");
+  const bool profiling = ctx->profiling;
+  ctx->profiling = false;
+  Snapshot snap;
+  int rc = take_snapshot(ctx, snap);
+  if (rc) return rc;
+  const TuneConfig start{ctx->params.schedule == 1 ? 1 : 0, ctx->autoLanes ? 0 : ctx->lanes,
+                         ctx->params.tail_div > 0 ? ctx->params.tail_div : 8, ctx->blocksPerSm};
+  std::vector<TuneConfig> cands = {start};
+  const int maxB = ctx->maxBlocksPerSm;
+  for (int b = maxB; b >= std::max(1, maxB - 1); b--) {
+    for (int lanes : {0, 32})
+      for (int td : {4, 8, 16}) cands.push_back({0, lanes, td, b});
+    for (int lanes : {16, 32}) cands.push_back({1, lanes, 8, b});
+  }
+  std::memset(out, 0, sizeof(*out));
+  double best = 0, first = 0;
+  TuneConfig pick = start;
+  int tried = 0;
+  for (size_t k = 0; k < cands.size(); k++) {
+    if (k > 0 && std::memcmp(&cands[k], &start, sizeof(TuneConfig)) == 0) continue;
+    apply_config(ctx, cands[k]);
+    double ms = 0;
+    rc = time_config(ctx, snap, trial_steps, &ms);
+    if (rc) break;
+    tried++;
+    if (k == 0) first = ms;
+    if (k == 0 || ms < best) {
+      best = ms;
+      pick = cands[k];
+    }
+  }
+  apply_config(ctx, rc ? start : pick);
+  const int rr = restore_snapshot(ctx, snap);
+  ctx->profiling = profiling;
+  if (rc) return rc;
+  if (rr) return rr;
+  Control c{};
+  CK(cudaMemcpy(&c, ctx->w.ctl, sizeof(Control), cudaMemcpyDeviceToHost));
+  out->schedule = pick.schedule;
+  out->lanes_per_body = pick.lanes;
+  out->tail_div = pick.tailDiv;
+  out->blocks_per_sm = pick.blocksPerSm;
+  out->candidates = tried;
+  out->trial_steps = trial_steps;
+  out->default_ms = first;
+  out->best_ms = best;
+  out->bodies = ctx->n;
+  out->manifolds = c.prevCandidates;
+  return AVBD_OK;
+}
 
 }  // extern "C"
 

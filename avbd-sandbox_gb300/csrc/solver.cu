@@ -1094,6 +1094,71 @@ __device__ __forceinline__ JointGeo<T> joint_geo(const World &w, int j, int2 ab,
   return g;
 }
 
+// The linear rows of a ball socket on one of its bodies (joint.js:162-221):
+// penalties K, forces F = K C + lambda, the body's Jacobians jLin = sl I and
+// jAng = S = skew(v), and the geometric stiffness of the lever arm r
+// (-(F.r) I + r F^T, column-norm lumped onto the angular diagonal).
+template <class T>
+__device__ __forceinline__ void stamp_ball_socket(Sys<T> &s, const T K[3], const T F[3], V3<T> v, V3<T> r, T sl) {
+  // skew(v) rows: [0,-vz,vy],[vz,0,-vx],[-vy,vx,0]
+  const T S[9] = {T(0), -v.z, v.y, v.z, T(0), -v.x, -v.y, v.x, T(0)};
+#pragma unroll
+  for (int rr = 0; rr < 3; rr++) s.l[L(rr, rr)] += K[rr];
+  // jAng^T K jAng  and  jAng^T K jLin = sl * (S^T K)
+#pragma unroll
+  for (int a = 0; a < 3; a++) {
+#pragma unroll
+    for (int b = 0; b <= a; b++) {
+      T acc = T(0);
+#pragma unroll
+      for (int q = 0; q < 3; q++) acc += S[q * 3 + a] * K[q] * S[q * 3 + b];
+      s.a[L(a, b)] += acc;
+    }
+#pragma unroll
+    for (int b = 0; b < 3; b++) s.c[a * 3 + b] += sl * S[b * 3 + a] * K[b];
+  }
+  const T fr = F[0] * r.x + F[1] * r.y + F[2] * r.z;
+  const T rv[3] = {r.x, r.y, r.z};
+#pragma unroll
+  for (int col = 0; col < 3; col++) {
+    T n2 = T(0);
+#pragma unroll
+    for (int row = 0; row < 3; row++) {
+      const T h = (row == col ? -fr : T(0)) + rv[row] * F[col];
+      n2 += h * h;
+    }
+    s.a[L(col, col)] += sqrt(n2);
+  }
+#pragma unroll
+  for (int a = 0; a < 3; a++) {
+    s.bl[a] += sl * F[a];
+    s.ba[a] += S[0 * 3 + a] * F[0] + S[1 * 3 + a] * F[1] + S[2 * 3 + a] * F[2];
+  }
+}
+
+// The grab on body i (the joint's B side, its A side the world target):
+// C = target - (p + R r), F = k C (shaders.js:2119-2161).
+template <class T>
+__device__ __noinline__ Sys<T> grab_primal(const World &w, int i, const BState<T> self, Sys<T> s) {
+  const Grab *g = w.grab;
+  const D4 tg = ld(&g->target), pB = ld(&w.b.pos[i]);
+  const V3<T> dpt{(T)(tg.x - pB.x), (T)(tg.y - pB.y), (T)(tg.z - pB.z)};
+  V3<T> rl;
+  if (sizeof(T) == 8) {
+    const D4 l = ld(&g->localD);
+    rl = V3<T>{(T)l.x, (T)l.y, (T)l.z};
+  } else {
+    const float4 l = ld(&g->local);
+    rl = V3<T>{(T)l.x, (T)l.y, (T)l.z};
+  }
+  const V3<T> rW = qrotate(self.q, rl);
+  const V3<T> C = (dpt - self.dp) - rW;
+  const T k = (T)ld(&g->k);
+  const T K[3] = {k, k, k}, F[3] = {k * C.x, k * C.y, k * C.z};
+  stamp_ball_socket<T>(s, K, F, rW, -rW, T(-1));
+  return s;
+}
+
 template <class T>
 __device__ __forceinline__ void joint_primal(const World &w, int j, int side, const BState<T> &self, T alpha, Sys<T> &s) {
   if (__ldcg(&w.j.state[j])) return;
@@ -1115,44 +1180,7 @@ __device__ __forceinline__ void joint_primal(const World &w, int j, int side, co
     const T K[3] = {(T)kl.x, (T)kl.y, (T)kl.z};
     const T F[3] = {K[0] * C.x + (T)lam.x, K[1] * C.y + (T)lam.y, K[2] * C.z + (T)lam.z};
     // A: jLin = I, jAng = skew(-rAw), r = rAw ; B: jLin = -I, jAng = skew(rBw), r = -rBw
-    const V3<T> v = side ? g.rBw : -g.rAw;
-    const V3<T> r = side ? -g.rBw : g.rAw;
-    const T sl = side ? T(-1) : T(1);
-    // skew(v) rows: [0,-vz,vy],[vz,0,-vx],[-vy,vx,0]
-    const T S[9] = {T(0), -v.z, v.y, v.z, T(0), -v.x, -v.y, v.x, T(0)};
-#pragma unroll
-    for (int rr = 0; rr < 3; rr++) s.l[L(rr, rr)] += K[rr];
-    // jAng^T K jAng  and  jAng^T K jLin = sl * (S^T K)
-#pragma unroll
-    for (int a = 0; a < 3; a++) {
-#pragma unroll
-      for (int b = 0; b <= a; b++) {
-        T acc = T(0);
-#pragma unroll
-        for (int q = 0; q < 3; q++) acc += S[q * 3 + a] * K[q] * S[q * 3 + b];
-        s.a[L(a, b)] += acc;
-      }
-#pragma unroll
-      for (int b = 0; b < 3; b++) s.c[a * 3 + b] += sl * S[b * 3 + a] * K[b];
-    }
-    // geometric stiffness (joint.js:214-221): H = -(F.r) I + r F^T, column-norm lumped
-    const T fr = F[0] * r.x + F[1] * r.y + F[2] * r.z;
-    const T rv[3] = {r.x, r.y, r.z};
-#pragma unroll
-    for (int col = 0; col < 3; col++) {
-      T n2 = T(0);
-#pragma unroll
-      for (int row = 0; row < 3; row++) {
-        const T h = (row == col ? -fr : T(0)) + rv[row] * F[col];
-        n2 += h * h;
-      }
-      s.a[L(col, col)] += sqrt(n2);
-    }
-#pragma unroll
-    for (int a = 0; a < 3; a++) {
-      s.bl[a] += sl * F[a];
-      s.ba[a] += S[0 * 3 + a] * F[0] + S[1 * 3 + a] * F[1] + S[2 * 3 + a] * F[2];
-    }
+    stamp_ball_socket<T>(s, K, F, side ? g.rBw : -g.rAw, side ? -g.rBw : g.rAw, side ? T(-1) : T(1));
   }
   const float4 ka = __ldcg(&w.j.penAng[j]);
   if (ka.x * ka.x + ka.y * ka.y + ka.z * ka.z > 0.f) {
@@ -1530,6 +1558,7 @@ __device__ void solve_body(const World &w, int4 rec, int lane, int G, unsigned m
   if (lane == 0) inertial_terms<T>(w, i, self, selfSphere, s);
   if (has0) contact_primal<T>(d0, self, alpha, s);
   if (extra) extra_primal<T>(w, i, cb, nm, cStart, total, lane, G, self, alpha, s);
+  if (lane == 0 && ld(&w.grab->body) == i) s = grab_primal<T>(w, i, self, s);
   finish_body<T>(w, i, lane, G, mask, velocity, ld(&w.b.quatT[i]), s, self);
   if (!dual) return;
   // dual updates of the constraints this body owns (it has the larger colour)
@@ -1709,6 +1738,7 @@ __device__ void solve_body_staged(const World &w, int4 rec, int lane, int G, uns
   const float4 mf = ld(&w.b.massF[i]), y = ld(&w.b.yLin[i]), qy = ld(&w.b.yAng[i]);
   const int cStart = ld(&w.g.cStart[i]), cEnd = ld(&w.g.cStart[i + 1]);
   const bool sphere = (ld(&w.b.flags0[i]) & kBodySphere) != 0;
+  const bool grabbed = lane == 0 && ld(&w.grab->body) == i;
   stage_chunk(w, cb, lane, G, 0, cnt, ent, stage, false, tw);
   BState<T> self;  // as load_state<float> forms it
   self.dp = V3<T>{d0.x, d0.y, d0.z};
@@ -1731,6 +1761,7 @@ __device__ void solve_body_staged(const World &w, int4 rec, int lane, int G, uns
     if (tw) tail_wait_extra(w, nm, cStart, total, lane, G, *tw);
     s = constraints_primal<T>(w, nm, cStart, total, lane, G, self, alpha, s);
   }
+  if (grabbed) s = grab_primal<T>(w, i, self, s);
   // in the tail segment the body's progress is published as soon as its state is stored: the
   // bodies waiting for it (higher colours) own every constraint they share with it, so they
   // read nothing its dual updates write
@@ -1828,7 +1859,7 @@ __device__ __forceinline__ void group_sync(int G, unsigned mask) {
 // neighbours (TailWait) and publishes its progress when done. Each group
 // walks its chunks in increasing colour, so the earliest unfinished tail
 // body always has its inputs ready (all blocks are resident).
-constexpr int kTailDiv = 8;
+constexpr int kTailDiv = 8;  // default of SolverParams::tailDiv
 constexpr int kChunkCache = 64;  // colours whose chunk bounds the solve keeps in shared memory
 __global__ void __launch_bounds__(kSolveBlock, 3) solve_kernel(World w) {
   if (step_skipped(w)) return;
@@ -1848,7 +1879,8 @@ __global__ void __launch_bounds__(kSolveBlock, 3) solve_kernel(World w) {
   __syncthreads();
   auto chunkAt = [&](int c) { return c <= kChunkCache ? chunkSm[c] : ld(&w.a.colorChunk[c]); };
   int tail = numColors;  // first tail colour
-  while (tail > 0 && chunkAt(tail) - chunkAt(tail - 1) <= (int)gridDim.x / kTailDiv) tail--;
+  const int tailDiv = P.tailDiv > 0 ? P.tailDiv : kTailDiv;
+  while (tail > 0 && chunkAt(tail) - chunkAt(tail - 1) <= (int)gridDim.x / tailDiv) tail--;
   for (int it = 0; it < total; it++) {
     const double alpha = P.postStabilize ? (it < P.iterations ? 1.0 : 0.0) : P.alpha;
     const bool dual = it < P.iterations;
@@ -2068,15 +2100,32 @@ __global__ void color_check_kernel(World w) {
   if (bad) atomicOr(&w.ctl->colorBad, 1);
 }
 
-cudaError_t launch_coloring(const World &w, cudaStream_t st, int smCount) {
+cudaError_t launch_coloring(const World &w, cudaStream_t st, int blocks) {
   if (w.a.colorOverride) {
-    color_copy_kernel<<<smCount * 4, 256, 0, st>>>(w);
-    color_check_kernel<<<smCount * 4, 256, 0, st>>>(w);
+    color_copy_kernel<<<blocks * 2, 256, 0, st>>>(w);
+    color_check_kernel<<<blocks * 2, 256, 0, st>>>(w);
   }
   World arg = w;
   void *args[] = {&arg};
-  return cudaLaunchCooperativeKernel((void *)coloring_kernel, dim3(coloring_blocks(smCount)), dim3(256), args, 0,
+  return cudaLaunchCooperativeKernel((void *)coloring_kernel, dim3(blocks), dim3(256), args, 0,
                                      st);
+}
+
+// The grab, set between steps (avbd_set_grab); body < 0 releases it.
+static __global__ void grab_kernel(Grab *g, int body, D4 local, D4 target, double k) {
+  g->body = body;
+  g->target = target;
+  g->localD = local;
+  g->local = make_float4((float)local.x, (float)local.y, (float)local.z, 0.f);
+  g->k = k;
+}
+
+cudaError_t launch_set_grab(const World &w, int body, const double *local, const double *target, double k,
+                            cudaStream_t st) {
+  const D4 l = local ? mkd4(local[0], local[1], local[2], 0.0) : mkd4(0, 0, 0, 0);
+  const D4 t = target ? mkd4(target[0], target[1], target[2], 0.0) : mkd4(0, 0, 0, 0);
+  grab_kernel<<<1, 1, 0, st>>>(w.grab, body, l, t, k);
+  return cudaGetLastError();
 }
 
 // A joint's anchor on body A, set between steps (avbd_update_joint_anchor).

@@ -1,0 +1,1326 @@
+// tangent.cu - the differentiable AVBD step: forward-mode tangents through
+// the whole world step, on the device.
+//
+// Every scalar of the step is a Dual (dual.cuh): a double value and
+// kTangentDims directional derivatives along inputs the caller seeds (a
+// body's initial velocity, a body's friction, the penalty cap, a joint's
+// stiffness). The value part runs in f64 with the reference engine's
+// operations (this unit is built with --fmad=false), so the discrete
+// decisions of a step - the candidate pairs, the SAT axis and clip topology,
+// the feature-ID warm start, the colouring, the cone and normal clamps, the
+// stick test, the penalty caps - are the f64 engine's, and the derivatives
+// follow the continuous path those decisions select: contact geometry as a
+// function of the poses at the step's start (collider.cuh on Dual),
+// warm start, every primal 6x6 solve and every dual update of every
+// iteration, and the BDF1 velocity. Forward mode carries all seeded
+// directions in one pass, so no checkpoints are needed; the backward of the
+// C ABI contracts these columns with an upstream gradient.
+//
+// Reference path (src/physics/solver.js:307-493):
+//   broad phase      solver.js:316-336, rigid.js:250-259 (constrainedTo)
+//   narrow phase     collide.js:612-685 (collider.cuh), manifold.js:214-318
+//   force init       joint.js:131-160, spring.js:472-507
+//   body init        solver.js:366-401
+//   primal           solver.js:418-458, manifold.js:325-445, joint.js:162-253,
+//                    spring.js:509-616, maths.js:660-725 (solve6), :568-592
+//   dual             manifold.js:447-491, joint.js:255-317, spring.js:618-634
+//   velocity         solver.js:476-488
+// Bodies are visited in the colour order of the integer-priority greedy
+// colouring (src/physics/gpu/layout.js:50-66), as the CUDA backend's step.
+//
+// Layout: small scenes (the differentiable workloads: hundreds of bodies),
+// structure of records, one thread per pair / force / body; the iterations
+// run in one block (colour phases separated by __syncthreads).
+#include <cub/cub.cuh>
+
+#include <cstdio>
+#include <vector>
+
+#include "../../include/avbd_cuda.h"
+#include "avbd_device.cuh"
+#include "collider.cuh"
+#include "dual.cuh"
+
+namespace avbd {
+namespace tg {
+
+using R = Dual;
+constexpr int K8 = kMaxContacts;
+constexpr int kBlock = 256;  // threads of the single-block kernels
+
+struct TBody {
+  R p[3], q[4];    // the iterate x (positionLin / positionAng)
+  R v[3], w[3];    // velocity, angular velocity
+  R pv[3];         // previous velocity
+  R p0[3], q0[4];  // x_t (initialLin / initialAng)
+  R yl[3], yq[4];  // inertial target y
+};
+struct TBodyStatic {
+  double mass, moment[3], half[3], radius;
+  R friction;
+  int shape;
+  int cStart, cEnd;  // joint/spring references (make_ref layout)
+};
+struct TJoint {
+  int a, b;  // a = -1: rA is a world point
+  R rA[3], rB[3];
+  R stiffLin, stiffAng;
+  double fracture, torqueArm;
+  R penLin[3], penAng[3], lamLin[3], lamAng[3], C0Lin[3], C0Ang[3];
+  int broken, removed;
+};
+struct TSpring {
+  int a, b;
+  R rA[3], rB[3];
+  R stiffness;
+  double rest, tear;
+  R penalty, peak;
+  int broken;
+};
+struct TContact {
+  R rA[3], rB[3], C0[3], pen[3], lam[3];
+  uint32_t feature;
+  int stick;
+};
+struct TManifold {
+  int a, b, count;
+  R basis[9];
+  R friction;
+  TContact c[K8];
+};
+
+struct TParams {
+  double dt, gravity, alpha, gamma, betaLin, betaAng, penaltyMin, margin, stickThreshold;
+  R penaltyMax;
+  int iterations, postStabilize, rotatedInertia, springRamp, springGeometric, cachedJacobians;
+};
+
+// Everything the tangent kernels touch (device pointers).
+struct TWorld {
+  TParams P;
+  int n, nj, ns;
+  TBody *b;
+  TBodyStatic *bs;
+  const uint32_t *cRef;
+  TJoint *j;
+  TSpring *s;
+  // candidate pairs of the step and the manifolds (double-buffered by pair key)
+  int mcap;
+  int *pairCount, *pairStart;  // n + 1
+  uint64_t *key;               // current candidates (mcap)
+  TManifold *cur, *prev;
+  uint64_t *prevKey;
+  int *ctl;  // [0] candidates, [1] previous candidates, [2] overflow, [3] colours
+  // adjacency of the solve (per dynamic body: its forces) and the colouring
+  int *fStart, *fCount;  // n + 1
+  uint32_t *fRef;        // (type << 30) | (index << 1) | side; type 0 = manifold
+  int fcap;
+  int *color, *order, *colorStart;  // colour per body; bodies by (colour, index); kMaxColors + 1
+  uint32_t *prio;
+};
+
+// ---------------------------------------------------------------------------
+// vec3 / mat3 / quaternion on R (maths.js: the operation order of the reference)
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ R js_min(R a, R b) {
+  if (a != a || b != b) return R(NAN);
+  if (a < b) return a;
+  if (b < a) return b;
+  return a;
+}
+__device__ __forceinline__ R js_max(R a, R b) {
+  if (a != a || b != b) return R(NAN);
+  if (a > b) return a;
+  if (b > a) return b;
+  return a;
+}
+__device__ __forceinline__ R clampR(R x, R a, R b) { return js_max(a, js_min(b, x)); }
+__device__ __forceinline__ void v3_sub(R *o, const R *a, const R *b) {
+  o[0] = a[0] - b[0]; o[1] = a[1] - b[1]; o[2] = a[2] - b[2];
+}
+__device__ __forceinline__ void v3_add(R *o, const R *a, const R *b) {
+  o[0] = a[0] + b[0]; o[1] = a[1] + b[1]; o[2] = a[2] + b[2];
+}
+__device__ __forceinline__ void v3_add_scaled(R *o, const R *a, R s) {
+  o[0] += a[0] * s; o[1] += a[1] * s; o[2] += a[2] * s;
+}
+__device__ __forceinline__ R v3_dot(const R *a, const R *b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
+__device__ __forceinline__ R v3_len_sq(const R *a) { return a[0] * a[0] + a[1] * a[1] + a[2] * a[2]; }
+__device__ __forceinline__ void v3_cross(R *o, const R *a, const R *b) {
+  const R ax = a[0], ay = a[1], az = a[2], bx = b[0], by = b[1], bz = b[2];
+  o[0] = ay * bz - az * by;
+  o[1] = az * bx - ax * bz;
+  o[2] = ax * by - ay * bx;
+}
+__device__ __forceinline__ void m3_zero(R *o) {
+  for (int i = 0; i < 9; i++) o[i] = 0.0;
+}
+__device__ __forceinline__ void m3_diag(R *o, R a, R b, R c) {
+  m3_zero(o);
+  o[0] = a; o[4] = b; o[8] = c;
+}
+__device__ __forceinline__ void m3_mul_vec(R *o, const R *a, const R *v) {
+  const R x = v[0], y = v[1], z = v[2];
+  o[0] = a[0] * x + a[1] * y + a[2] * z;
+  o[1] = a[3] * x + a[4] * y + a[5] * z;
+  o[2] = a[6] * x + a[7] * y + a[8] * z;
+}
+__device__ void m3_mul(R *o, const R *a, const R *b) {
+  R t[9];
+  for (int r = 0; r < 3; r++)
+    for (int c = 0; c < 3; c++) t[r * 3 + c] = a[r * 3] * b[c] + a[r * 3 + 1] * b[3 + c] + a[r * 3 + 2] * b[6 + c];
+  for (int i = 0; i < 9; i++) o[i] = t[i];
+}
+__device__ __forceinline__ void m3_transpose(R *o, const R *a) {
+  R t[9];
+  for (int r = 0; r < 3; r++)
+    for (int c = 0; c < 3; c++) t[c * 3 + r] = a[r * 3 + c];
+  for (int i = 0; i < 9; i++) o[i] = t[i];
+}
+__device__ __forceinline__ void m3_skew(R *o, const R *r) {
+  o[0] = 0.0; o[1] = -r[2]; o[2] = r[1];
+  o[3] = r[2]; o[4] = 0.0; o[5] = -r[0];
+  o[6] = -r[1]; o[7] = r[0]; o[8] = 0.0;
+}
+__device__ __forceinline__ void m3_add_into(R *o, const R *a) {
+  for (int i = 0; i < 9; i++) o[i] += a[i];
+}
+// Eq. 20 (maths.js:541-555)
+__device__ void q_subtract(R *o, const R *a, const R *b) {
+  const R lsq = b[0] * b[0] + b[1] * b[1] + b[2] * b[2] + b[3] * b[3];
+  const R ix = -b[0] / lsq, iy = -b[1] / lsq, iz = -b[2] / lsq, iw = b[3] / lsq;
+  const R ax = a[0], ay = a[1], az = a[2], aw = a[3];
+  o[0] = (aw * ix + ax * iw + ay * iz - az * iy) * 2.0;
+  o[1] = (aw * iy - ax * iz + ay * iw + az * ix) * 2.0;
+  o[2] = (aw * iz + ax * iy - ay * ix + az * iw) * 2.0;
+}
+// Eq. 21 (maths.js:568-592), its "0 * q" terms kept
+__device__ void q_integrate(R *o, const R *q, const R *dw) {
+  const R qx = q[0], qy = q[1], qz = q[2], qw = q[3];
+  const R wx = dw[0], wy = dw[1], wz = dw[2];
+  const R px = 0.0 * qx + wx * qw + wy * qz - wz * qy;
+  const R py = 0.0 * qy - wx * qz + wy * qw + wz * qx;
+  const R pz = 0.0 * qz + wx * qy - wy * qx + wz * qw;
+  const R pw = 0.0 * qw - wx * qx - wy * qy - wz * qz;
+  const R rx = qx + px * 0.5, ry = qy + py * 0.5, rz = qz + pz * 0.5, rw = qw + pw * 0.5;
+  const R len = sqrt(rx * rx + ry * ry + rz * rz + rw * rw);
+  o[0] = rx / len; o[1] = ry / len; o[2] = rz / len; o[3] = rw / len;
+}
+// maths.js:599-613
+__device__ void q_rotate(R *o, const R *q, const R *v) {
+  const R ux = q[0], uy = q[1], uz = q[2], w = q[3];
+  const R vx = v[0], vy = v[1], vz = v[2];
+  const R tx = (uy * vz - uz * vy) * 2.0;
+  const R ty = (uz * vx - ux * vz) * 2.0;
+  const R tz = (ux * vy - uy * vx) * 2.0;
+  o[0] = vx + tx * w + (uy * tz - uz * ty);
+  o[1] = vy + ty * w + (uz * tx - ux * tz);
+  o[2] = vz + tz * w + (ux * ty - uy * tx);
+}
+// maths.js:621-627
+__device__ __forceinline__ void transform_point(R *o, const R *lin, const R *ang, const R *v) {
+  q_rotate(o, ang, v);
+  o[0] += lin[0]; o[1] += lin[1]; o[2] += lin[2];
+}
+// R I R^T of a body (rigid.js:228-247), maths.js:417-434 for R
+__device__ void world_moment(R *out, const TBodyStatic &st, const R *q, bool rotated) {
+  if (!rotated || st.shape == AVBD_SHAPE_SPHERE) {
+    m3_diag(out, R(st.moment[0]), R(st.moment[1]), R(st.moment[2]));
+    return;
+  }
+  const R x = q[0], y = q[1], z = q[2], w = q[3];
+  const R xx = x * x, yy = y * y, zz = z * z, xy = x * y, xz = x * z, yz = y * z, wx = w * x, wy = w * y, wz = w * z;
+  R Rm[9];
+  Rm[0] = 1.0 - 2.0 * (yy + zz); Rm[1] = 2.0 * (xy + wz); Rm[2] = 2.0 * (xz - wy);
+  Rm[3] = 2.0 * (xy - wz); Rm[4] = 1.0 - 2.0 * (xx + zz); Rm[5] = 2.0 * (yz + wx);
+  Rm[6] = 2.0 * (xz + wy); Rm[7] = 2.0 * (yz - wx); Rm[8] = 1.0 - 2.0 * (xx + yy);
+  R T[9], Rt[9];
+  m3_transpose(Rt, Rm);
+  m3_diag(T, R(st.moment[0]), R(st.moment[1]), R(st.moment[2]));
+  m3_mul(out, Rt, T);
+  m3_mul(out, out, Rm);
+}
+// maths.js:660-725, unrolled LDL^T of the 6x6 block system
+__device__ void solve6(const R *aLin, const R *aAng, const R *aCross, const R *bLin, const R *bAng, R *xLin, R *xAng) {
+  const R A11 = aLin[0];
+  const R A21 = aLin[3], A22 = aLin[4];
+  const R A31 = aLin[6], A32 = aLin[7], A33 = aLin[8];
+  const R A41 = aCross[0], A42 = aCross[1], A43 = aCross[2], A44 = aAng[0];
+  const R A51 = aCross[3], A52 = aCross[4], A53 = aCross[5], A54 = aAng[3], A55 = aAng[4];
+  const R A61 = aCross[6], A62 = aCross[7], A63 = aCross[8], A64 = aAng[6], A65 = aAng[7], A66 = aAng[8];
+  const R L21 = A21 / A11, L31 = A31 / A11, L41 = A41 / A11, L51 = A51 / A11, L61 = A61 / A11;
+  const R D1 = A11;
+  const R D2 = A22 - L21 * L21 * D1;
+  const R L32 = (A32 - L21 * L31 * D1) / D2;
+  const R L42 = (A42 - L21 * L41 * D1) / D2;
+  const R L52 = (A52 - L21 * L51 * D1) / D2;
+  const R L62 = (A62 - L21 * L61 * D1) / D2;
+  const R D3 = A33 - (L31 * L31 * D1 + L32 * L32 * D2);
+  const R L43 = (A43 - L31 * L41 * D1 - L32 * L42 * D2) / D3;
+  const R L53 = (A53 - L31 * L51 * D1 - L32 * L52 * D2) / D3;
+  const R L63 = (A63 - L31 * L61 * D1 - L32 * L62 * D2) / D3;
+  const R D4 = A44 - (L41 * L41 * D1 + L42 * L42 * D2 + L43 * L43 * D3);
+  const R L54 = (A54 - L41 * L51 * D1 - L42 * L52 * D2 - L43 * L53 * D3) / D4;
+  const R L64 = (A64 - L41 * L61 * D1 - L42 * L62 * D2 - L43 * L63 * D3) / D4;
+  const R D5 = A55 - (L51 * L51 * D1 + L52 * L52 * D2 + L53 * L53 * D3 + L54 * L54 * D4);
+  const R L65 = (A65 - L51 * L61 * D1 - L52 * L62 * D2 - L53 * L63 * D3 - L54 * L64 * D4) / D5;
+  const R D6 = A66 - (L61 * L61 * D1 + L62 * L62 * D2 + L63 * L63 * D3 + L64 * L64 * D4 + L65 * L65 * D5);
+  const R y1 = bLin[0];
+  const R y2 = bLin[1] - L21 * y1;
+  const R y3 = bLin[2] - L31 * y1 - L32 * y2;
+  const R y4 = bAng[0] - L41 * y1 - L42 * y2 - L43 * y3;
+  const R y5 = bAng[1] - L51 * y1 - L52 * y2 - L53 * y3 - L54 * y4;
+  const R y6 = bAng[2] - L61 * y1 - L62 * y2 - L63 * y3 - L64 * y4 - L65 * y5;
+  const R z1 = y1 / D1, z2 = y2 / D2, z3 = y3 / D3, z4 = y4 / D4, z5 = y5 / D5, z6 = y6 / D6;
+  xAng[2] = z6;
+  xAng[1] = z5 - L65 * xAng[2];
+  xAng[0] = z4 - L54 * xAng[1] - L64 * xAng[2];
+  xLin[2] = z3 - L43 * xAng[0] - L53 * xAng[1] - L63 * xAng[2];
+  xLin[1] = z2 - L32 * xLin[2] - L42 * xAng[0] - L52 * xAng[1] - L62 * xAng[2];
+  xLin[0] = z1 - L21 * xLin[1] - L31 * xLin[2] - L41 * xAng[0] - L51 * xAng[1] - L61 * xAng[2];
+}
+
+// A body's 6x6 system, accumulated by its forces.
+struct Sys6 {
+  R lin[9], ang[9], cross[9], bl[3], ba[3];
+};
+
+__device__ __forceinline__ bool is_dynamic(const TWorld &w, int i) { return i >= 0 && w.bs[i].mass > 0; }
+__device__ __forceinline__ uint64_t pair_key(int a, int b) { return ((uint64_t)(uint32_t)a << 32) | (uint32_t)b; }
+
+// Index of `key` in the sorted array, or -1.
+__device__ int find_key(const uint64_t *keys, int n, uint64_t key) {
+  int l = 0, h = n;
+  while (l < h) {
+    const int m = (l + h) >> 1;
+    if (keys[m] < key) l = m + 1;
+    else h = m;
+  }
+  return l < n && keys[l] == key ? l : -1;
+}
+
+// A live joint or spring joins a and b (rigid.js:250-259).
+__device__ bool constrained(const TWorld &w, int a, int b) {
+  const TBodyStatic &s = w.bs[a];
+  for (int k = s.cStart; k < s.cEnd; k++) {
+    const uint32_t ref = w.cRef[k];
+    const uint32_t type = ref >> 30, idx = (ref >> 1) & 0x1fffffffu;
+    int x, y;
+    if (type == kRefJoint) {
+      const TJoint &j = w.j[idx];
+      if (j.broken) continue;
+      x = j.a; y = j.b;
+    } else {
+      const TSpring &sp = w.s[idx];
+      if (sp.broken) continue;
+      x = sp.a; y = sp.b;
+    }
+    if ((x == a && y == b) || (x == b && y == a)) return true;
+  }
+  return false;
+}
+
+// solver.js:316-336: pairs (a, b), b < a, whose bounding spheres overlap (f64
+// values), not both static and not joined, and every pair that held contacts
+// in the previous step (its manifold stays in the force list).
+__device__ bool is_candidate(const TWorld &w, int a, int b, int prevCount) {
+  if (!(w.bs[a].mass > 0 || w.bs[b].mass > 0)) return false;
+  if (find_key(w.prevKey, prevCount, pair_key(a, b)) >= 0) return true;
+  const R dx = w.b[a].p[0] - w.b[b].p[0], dy = w.b[a].p[1] - w.b[b].p[1], dz = w.b[a].p[2] - w.b[b].p[2];
+  const double r = w.bs[a].radius + w.bs[b].radius;
+  if (!(dx * dx + dy * dy + dz * dz <= r * r)) return false;
+  return !constrained(w, a, b);
+}
+
+__global__ void pairs_count_kernel(TWorld w) {
+  const int prevCount = w.ctl[1];
+  for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < w.n; a += gridDim.x * blockDim.x) {
+    int c = 0;
+    for (int b = 0; b < a; b++) c += is_candidate(w, a, b, prevCount) ? 1 : 0;
+    w.pairCount[a] = c;
+  }
+}
+
+__global__ void pairs_write_kernel(TWorld w) {
+  const int prevCount = w.ctl[1];
+  for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < w.n; a += gridDim.x * blockDim.x) {
+    int at = w.pairStart[a];
+    for (int b = 0; b < a; b++)
+      if (is_candidate(w, a, b, prevCount)) {
+        if (at < w.mcap) w.key[at] = pair_key(a, b);
+        at++;
+      }
+  }
+  if (blockIdx.x == 0 && threadIdx.x == 0) {
+    const int total = w.pairStart[w.n];
+    w.ctl[0] = total < w.mcap ? total : w.mcap;
+    if (total > w.mcap) w.ctl[2] = 1;
+  }
+}
+
+// manifold.js:222-270, the sphere pairs' transport of lambda and k into the new basis
+__device__ void transport(R *lam, R *pen, const R *oldB, const R *newB) {
+  const R x = lam[0], y = lam[1], z = lam[2];
+  R o[3];
+  for (int r = 0; r < 3; r++) {
+    const int n = r * 3;
+    o[r] = x * (newB[n] * oldB[0] + newB[n + 1] * oldB[1] + newB[n + 2] * oldB[2]) +
+           y * (newB[n] * oldB[3] + newB[n + 1] * oldB[4] + newB[n + 2] * oldB[5]) +
+           z * (newB[n] * oldB[6] + newB[n + 1] * oldB[7] + newB[n + 2] * oldB[8]);
+  }
+  lam[0] = o[0]; lam[1] = o[1]; lam[2] = o[2];
+  const R px = pen[0], py = pen[1], pz = pen[2];
+  for (int r = 0; r < 3; r++) {
+    const int n = r * 3;
+    const R dx = newB[n] * oldB[0] + newB[n + 1] * oldB[1] + newB[n + 2] * oldB[2];
+    const R dy = newB[n] * oldB[3] + newB[n + 1] * oldB[4] + newB[n + 2] * oldB[5];
+    const R dz = newB[n] * oldB[6] + newB[n + 1] * oldB[7] + newB[n + 2] * oldB[8];
+    o[r] = px * dx * dx + py * dy * dy + pz * dz * dz;
+  }
+  pen[0] = o[0]; pen[1] = o[1]; pen[2] = o[2];
+}
+
+__device__ geo::BodyT<R> body_geo(const TWorld &w, int i) {
+  geo::BodyT<R> g;
+  const TBody &b = w.b[i];
+  const TBodyStatic &s = w.bs[i];
+  g.p = geo::D3T<R>{b.p[0], b.p[1], b.p[2]};
+  g.q = geo::QDT<R>{b.q[0], b.q[1], b.q[2], b.q[3]};
+  g.half = geo::D3T<R>{R(s.half[0]), R(s.half[1]), R(s.half[2])};
+  g.radius = s.radius;
+  g.sphere = s.shape == AVBD_SHAPE_SPHERE;
+  return g;
+}
+
+// Manifold.initialize (manifold.js:214-318) of candidate c, at x_t.
+__global__ void narrow_kernel(TWorld w) {
+  const int total = w.ctl[0], prevCount = w.ctl[1];
+  const TParams &P = w.P;
+  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < total; c += gridDim.x * blockDim.x) {
+    const uint64_t key = w.key[c];
+    const int ia = (int)(key >> 32), ib = (int)(key & 0xffffffffu);
+    TManifold &m = w.cur[c];
+    m.a = ia;
+    m.b = ib;
+    const int pi = find_key(w.prevKey, prevCount, key);
+    const TManifold *old = pi >= 0 ? &w.prev[pi] : nullptr;
+    const int oldNum = old ? old->count : 0;
+    const bool hasSphere = w.bs[ia].shape == AVBD_SHAPE_SPHERE || w.bs[ib].shape == AVBD_SHAPE_SPHERE;
+    m.friction = sqrt(w.bs[ia].friction * w.bs[ib].friction);
+    const geo::BodyT<R> A = body_geo(w, ia), B = body_geo(w, ib);
+    geo::NewContactT<R> nc[K8];
+    R basis[9];
+    for (int k = 0; k < 9; k++) basis[k] = 0.0;
+    geo::ColliderT<R> col(A, B, nc);
+    const int num = col.collide(basis);
+    bool compatible = true;
+    if (hasSphere && oldNum > 0)
+      compatible = (old->basis[0] * basis[0] + old->basis[1] * basis[1] + old->basis[2] * basis[2]) > 0.85;
+    for (int i = 0; i < num; i++) {
+      TContact &t = m.c[i];
+      for (int k = 0; k < 3; k++) {
+        t.rA[k] = k == 0 ? nc[i].rA.x : (k == 1 ? nc[i].rA.y : nc[i].rA.z);
+        t.rB[k] = k == 0 ? nc[i].rB.x : (k == 1 ? nc[i].rB.y : nc[i].rB.z);
+        t.pen[k] = 0.0;
+        t.lam[k] = 0.0;
+      }
+      t.feature = nc[i].feature;
+      t.stick = 0;
+      for (int j = 0; j < oldNum; j++) {
+        const TContact &o = old->c[j];
+        if (compatible && nc[i].feature == o.feature) {
+          for (int k = 0; k < 3; k++) {
+            t.pen[k] = o.pen[k];
+            t.lam[k] = o.lam[k];
+          }
+          t.stick = o.stick;
+          if (hasSphere) transport(t.lam, t.pen, old->basis, basis);
+          if (o.stick && !hasSphere)  // a stuck box contact keeps its anchors (manifold.js:279-282)
+            for (int k = 0; k < 3; k++) {
+              t.rA[k] = o.rA[k];
+              t.rB[k] = o.rB[k];
+            }
+          break;
+        }
+      }
+    }
+    m.count = num;
+    for (int k = 0; k < 9; k++) m.basis[k] = basis[k];
+    const TBody &bA = w.b[ia], &bB = w.b[ib];
+    for (int i = 0; i < num; i++) {  // C*(x_t) + margin, warm start (manifold.js:292-315)
+      TContact &t = m.c[i];
+      R xA[3], xB[3], d[3];
+      transform_point(xA, bA.p, bA.q, t.rA);
+      transform_point(xB, bB.p, bB.q, t.rB);
+      v3_sub(d, xA, xB);
+      m3_mul_vec(t.C0, m.basis, d);
+      t.C0[0] = t.C0[0] + P.margin;
+      for (int k = 0; k < 3; k++) {
+        if (!P.postStabilize) t.lam[k] = (t.lam[k] * P.alpha) * P.gamma;
+        t.pen[k] = clampR(t.pen[k] * P.gamma, R(P.penaltyMin), P.penaltyMax);
+      }
+    }
+  }
+}
+
+// Joint.initialize (joint.js:131-160) and Spring.initialize (spring.js:472-507).
+__device__ void joint_eval_lin(const TWorld &w, const TJoint &j, R *out) {
+  R pA[3], pB[3];
+  if (j.a >= 0) transform_point(pA, w.b[j.a].p, w.b[j.a].q, j.rA);
+  else { pA[0] = j.rA[0]; pA[1] = j.rA[1]; pA[2] = j.rA[2]; }
+  transform_point(pB, w.b[j.b].p, w.b[j.b].q, j.rB);
+  v3_sub(out, pA, pB);
+}
+__device__ void joint_eval_ang(const TWorld &w, const TJoint &j, R *out) {
+  const R id[4] = {R(0.0), R(0.0), R(0.0), R(1.0)};
+  q_subtract(out, j.a >= 0 ? w.b[j.a].q : id, w.b[j.b].q);
+  for (int k = 0; k < 3; k++) out[k] = out[k] * j.torqueArm;
+}
+// spring.js:447-458: C = |d| - rest, n = d / |d| (NaN C when |d| <= 1e-6)
+__device__ R spring_eval(const TWorld &w, const TSpring &s, R *d, R *n) {
+  R pA[3], pB[3];
+  transform_point(pA, w.b[s.a].p, w.b[s.a].q, s.rA);
+  transform_point(pB, w.b[s.b].p, w.b[s.b].q, s.rB);
+  v3_sub(d, pA, pB);
+  const R len = sqrt(v3_len_sq(d));
+  if (len <= 1.0e-6) return R(NAN);
+  for (int k = 0; k < 3; k++) n[k] = d[k] / len;
+  return len - s.rest;
+}
+// spring.js:461-470
+__device__ bool spring_tear(TSpring &s, R Cv) {
+  if (s.rest <= 1.0e-6) return false;
+  const R strain = js_max(R(0.0), Cv / s.rest);
+  s.peak = js_max(s.peak, strain);
+  if (strain <= s.tear) return false;
+  s.broken = 1;
+  s.penalty = 0.0;
+  return true;
+}
+
+__global__ void forces_init_kernel(TWorld w) {
+  const TParams &P = w.P;
+  const int tid = blockIdx.x * blockDim.x + threadIdx.x, stride = gridDim.x * blockDim.x;
+  for (int k = tid; k < w.nj; k += stride) {
+    TJoint &j = w.j[k];
+    if (j.removed) continue;
+    joint_eval_lin(w, j, j.C0Lin);
+    joint_eval_ang(w, j, j.C0Ang);
+    for (int c = 0; c < 3; c++) {
+      if (!P.postStabilize) {
+        j.lamLin[c] = (j.lamLin[c] * P.alpha) * P.gamma;
+        j.lamAng[c] = (j.lamAng[c] * P.alpha) * P.gamma;
+      }
+      j.penLin[c] = js_min(clampR(j.penLin[c] * P.gamma, R(P.penaltyMin), P.penaltyMax), j.stiffLin);
+      j.penAng[c] = js_min(clampR(j.penAng[c] * P.gamma, R(P.penaltyMin), P.penaltyMax), j.stiffAng);
+    }
+    if (j.broken) j.removed = 1;  // returns !broken: leaves the force list
+  }
+  for (int k = tid; k < w.ns; k += stride) {
+    TSpring &s = w.s[k];
+    if (s.broken) {
+      s.penalty = 0.0;
+      continue;
+    }
+    if (isfinite(s.tear)) {
+      R d[3], n[3];
+      const R Cv = spring_eval(w, s, d, n);
+      if (!(Cv != Cv) && spring_tear(s, Cv)) continue;
+    }
+    if (!P.springRamp) s.penalty = s.stiffness;
+    else s.penalty = js_min(clampR(s.penalty * P.gamma, R(P.penaltyMin), P.penaltyMax), s.stiffness);
+  }
+}
+
+// solver.js:366-401: y = x + v dt + g dt^2 (z), the adaptive initial guess.
+__global__ void bodies_init_kernel(TWorld w) {
+  const TParams &P = w.P;
+  const double dt = P.dt;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < w.n; i += gridDim.x * blockDim.x) {
+    TBody &b = w.b[i];
+    const bool dyn = w.bs[i].mass > 0;
+    const R g[3] = {R(0.0), R(0.0), R(P.gravity)};
+    R tmp[3];
+    for (int k = 0; k < 3; k++) b.yl[k] = b.p[k];
+    v3_add_scaled(b.yl, b.v, R(dt));
+    if (dyn) v3_add_scaled(b.yl, g, R(dt * dt));
+    for (int k = 0; k < 3; k++) tmp[k] = b.w[k] * dt;
+    q_integrate(b.yq, b.q, tmp);
+    const R accelZ = (b.v[2] - b.pv[2]) / dt;
+    const double sgn = P.gravity < 0 ? -1.0 : (P.gravity > 0 ? 1.0 : 0.0);
+    const R accelExt = accelZ * sgn;
+    R weight = clampR(accelExt / ::fabs(P.gravity), R(0.0), R(1.0));
+    if (!isfinite(weight)) weight = 0.0;
+    for (int k = 0; k < 3; k++) b.p0[k] = b.p[k];
+    for (int k = 0; k < 4; k++) b.q0[k] = b.q[k];
+    if (dyn) {
+      v3_add_scaled(b.p, b.v, R(dt));
+      v3_add_scaled(b.p, g, weight * dt * dt);
+      R q1[4];
+      q_integrate(q1, b.q, tmp);
+      for (int k = 0; k < 4; k++) b.q[k] = q1[k];
+    }
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Adjacency, colouring (single block)
+// ---------------------------------------------------------------------------
+// The forces of the step after initialisation (solver.js:346-360): live
+// manifolds, joints that did not leave, every spring (a broken one stays and
+// does nothing). Per dynamic body its list of (type, index, side).
+template <class F>
+__device__ void for_each_force(const TWorld &w, int total, F &&f) {
+  for (int c = 0; c < total; c++)
+    if (w.cur[c].count > 0) f(0u, c, w.cur[c].a, w.cur[c].b, false);
+  for (int k = 0; k < w.nj; k++)
+    if (!w.j[k].removed) f((uint32_t)kRefJoint, k, w.j[k].a, w.j[k].b, false);
+  for (int k = 0; k < w.ns; k++) f((uint32_t)kRefSpring, k, w.s[k].a, w.s[k].b, w.s[k].broken != 0);
+}
+
+// The integer-priority greedy colouring (statics -1), computed as the fixed
+// point of Jacobi rounds (the CUDA step's colouring; the oracle's
+// priority_coloring); colour edges: forces between two dynamic bodies,
+// broken ones excluded (oracle constraint_edges).
+__global__ void __launch_bounds__(kBlock) adjacency_coloring_kernel(TWorld w) {
+  const int n = w.n, total = w.ctl[0];
+  const int t = threadIdx.x;
+  for (int i = t; i <= n; i += blockDim.x) w.fCount[i] = 0;
+  __syncthreads();
+  if (t == 0) {
+    // per-body force lists in force-list order (single thread: small scenes)
+    for_each_force(w, total, [&](uint32_t type, int idx, int a, int b, bool) {
+      if (a >= 0 && w.bs[a].mass > 0) w.fCount[a]++;
+      if (w.bs[b].mass > 0) w.fCount[b]++;
+    });
+    int run = 0;
+    for (int i = 0; i < n; i++) {
+      w.fStart[i] = run;
+      run += w.fCount[i];
+      w.fCount[i] = 0;
+    }
+    w.fStart[n] = run;
+    if (run > w.fcap) w.ctl[2] = 1;
+    for_each_force(w, total, [&](uint32_t type, int idx, int a, int b, bool) {
+      const uint32_t base = (type << 30) | ((uint32_t)idx << 1);
+      if (a >= 0 && w.bs[a].mass > 0) {
+        const int at = w.fStart[a] + w.fCount[a]++;
+        if (at < w.fcap) w.fRef[at] = base | 0u;
+      }
+      if (w.bs[b].mass > 0) {
+        const int at = w.fStart[b] + w.fCount[b]++;
+        if (at < w.fcap) w.fRef[at] = base | 1u;
+      }
+    });
+  }
+  __syncthreads();
+  if (w.ctl[2]) return;
+  for (int i = t; i < n; i += blockDim.x) w.color[i] = is_dynamic(w, i) ? 0 : -1;
+  __shared__ int changed;
+  for (int round = 0; round < 4096; round++) {
+    __syncthreads();
+    if (t == 0) changed = 0;
+    __syncthreads();
+    for (int i = t; i < n; i += blockDim.x) {
+      if (!is_dynamic(w, i)) continue;
+      const uint32_t pi = w.prio[i];
+      int c = -1;
+      for (int base = 0; c < 0 && base < kMaxColors; base += 64) {
+        unsigned long long used = 0ull;
+        for (int e = w.fStart[i]; e < w.fStart[i + 1]; e++) {
+          const uint32_t ref = w.fRef[e];
+          const uint32_t type = ref >> 30, idx = (ref >> 1) & 0x1fffffffu, side = ref & 1u;
+          int a, b;
+          bool broken = false;
+          if (type == 0) { a = w.cur[idx].a; b = w.cur[idx].b; }
+          else if (type == kRefJoint) { a = w.j[idx].a; b = w.j[idx].b; }
+          else { a = w.s[idx].a; b = w.s[idx].b; broken = w.s[idx].broken != 0; }
+          const int o = side ? a : b;
+          if (broken || !is_dynamic(w, o)) continue;
+          const uint32_t po = w.prio[o];
+          if (!(po < pi || (po == pi && o < i))) continue;
+          const int co = w.color[o];
+          if (co >= base && co < base + 64) used |= 1ull << (co - base);
+        }
+        if (~used) c = base + __ffsll((long long)~used) - 1;
+      }
+      if (c < 0) c = kMaxColors - 1;
+      if (c != w.color[i]) {
+        w.color[i] = c;
+        changed = 1;
+      }
+    }
+    __syncthreads();
+    if (!changed) break;
+  }
+  __syncthreads();
+  if (t == 0) {  // bodies in (colour, index) order
+    int numColors = 0;
+    for (int i = 0; i < n; i++) numColors = max(numColors, w.color[i] + 1);
+    int at = 0;
+    for (int c = 0; c < numColors; c++) {
+      w.colorStart[c] = at;
+      for (int i = 0; i < n; i++)
+        if (w.color[i] == c) w.order[at++] = i;
+    }
+    w.colorStart[numColors] = at;
+    w.ctl[3] = numColors;
+  }
+}
+
+// ---------------------------------------------------------------------------
+// Primal (solver.js:418-458) and dual (solver.js:466-470) of one iteration
+// ---------------------------------------------------------------------------
+// Manifold._evaluate (manifold.js:358-409) of contact i with cached
+// Jacobians from the x_t orientations: C = (1 - alpha) C0 + J (x - x_t).
+struct ContactEvalT {
+  R C[3], F[3];
+  bool within;
+};
+__device__ ContactEvalT contact_eval(const TWorld &w, const TManifold &m, int i, R alpha, R *jAAng, R *jBAng) {
+  const TBody &A = w.b[m.a], &B = w.b[m.b];
+  const TContact &c = m.c[i];
+  R dqALin[3], dqAAng[3], dqBLin[3], dqBAng[3], jBLin[9];
+  v3_sub(dqALin, A.p, A.p0);
+  q_subtract(dqAAng, A.q, A.q0);
+  v3_sub(dqBLin, B.p, B.p0);
+  q_subtract(dqBAng, B.q, B.q0);
+  for (int k = 0; k < 9; k++) jBLin[k] = -m.basis[k];
+  R rAW[3], rBW[3], row[3], acc[3];
+  // cached Jacobians: the contact arms at the x_t orientations (manifold.js:325-350)
+  q_rotate(rAW, w.P.cachedJacobians ? A.q0 : A.q, c.rA);
+  q_rotate(rBW, w.P.cachedJacobians ? B.q0 : B.q, c.rB);
+  for (int r = 0; r < 3; r++) {  // manifold.js:325-350
+    row[0] = m.basis[r * 3]; row[1] = m.basis[r * 3 + 1]; row[2] = m.basis[r * 3 + 2];
+    v3_cross(acc, rAW, row);
+    jAAng[r * 3] = acc[0]; jAAng[r * 3 + 1] = acc[1]; jAAng[r * 3 + 2] = acc[2];
+    row[0] = jBLin[r * 3]; row[1] = jBLin[r * 3 + 1]; row[2] = jBLin[r * 3 + 2];
+    v3_cross(acc, rBW, row);
+    jBAng[r * 3] = acc[0]; jBAng[r * 3 + 1] = acc[1]; jBAng[r * 3 + 2] = acc[2];
+  }
+  ContactEvalT e;
+  for (int k = 0; k < 3; k++) e.C[k] = c.C0[k] * (1.0 - alpha);
+  m3_mul_vec(acc, m.basis, dqALin); v3_add(e.C, e.C, acc);
+  m3_mul_vec(acc, jBLin, dqBLin); v3_add(e.C, e.C, acc);
+  m3_mul_vec(acc, jAAng, dqAAng); v3_add(e.C, e.C, acc);
+  m3_mul_vec(acc, jBAng, dqBAng); v3_add(e.C, e.C, acc);
+  for (int k = 0; k < 3; k++) e.F[k] = c.pen[k] * e.C[k] + c.lam[k];
+  e.F[0] = js_min(e.F[0], R(0.0));
+  const R bounds = fabs(e.F[0]) * m.friction;
+  const R fs = sqrt(e.F[1] * e.F[1] + e.F[2] * e.F[2]);
+  if (fs > bounds && fs > 0.0) {
+    e.F[1] *= bounds / fs;
+    e.F[2] *= bounds / fs;
+  }
+  e.within = fs <= bounds;
+  return e;
+}
+
+// H += J_lin^T K J_lin etc. of one 3-row block with diagonal K.
+__device__ void stamp_rows(Sys6 &s, const R *jLin, const R *jAng, const R *Kd, const R *F) {
+  R jLinT[9], jAngT[9], jAngTk[9], m0[9], acc[3];
+  m3_transpose(jLinT, jLin);
+  m3_transpose(jAngT, jAng);
+  for (int r = 0; r < 3; r++)
+    for (int c = 0; c < 3; c++) {
+      jAngTk[r * 3 + c] = jAngT[r * 3 + c] * Kd[c];
+      m0[r * 3 + c] = jLinT[r * 3 + c] * Kd[c];
+    }
+  m3_mul(m0, m0, jLin);
+  m3_add_into(s.lin, m0);
+  m3_mul(m0, jAngTk, jAng);
+  m3_add_into(s.ang, m0);
+  m3_mul(m0, jAngTk, jLin);
+  m3_add_into(s.cross, m0);
+  m3_mul_vec(acc, jLinT, F);
+  v3_add(s.bl, s.bl, acc);
+  m3_mul_vec(acc, jAngT, F);
+  v3_add(s.ba, s.ba, acc);
+}
+
+// manifold.js:411-445
+__device__ void manifold_primal(const TWorld &w, const TManifold &m, int side, R alpha, Sys6 &s) {
+  R jBLin[9];
+  for (int k = 0; k < 9; k++) jBLin[k] = -m.basis[k];
+  for (int i = 0; i < m.count; i++) {
+    R jAAng[9], jBAng[9];
+    const ContactEvalT e = contact_eval(w, m, i, alpha, jAAng, jBAng);
+    stamp_rows(s, side ? jBLin : m.basis, side ? jBAng : jAAng, m.c[i].pen, e.F);
+  }
+}
+
+// joint.js:214-221: the geometric stiffness of a ball socket, lumped
+__device__ void ball_socket_geometric(R *G, const R *r, const R *F) {
+  R H[9];
+  m3_zero(H);
+  for (int k = 0; k < 3; k++) {  // geometricStiffnessBallSocket(v = r, k) * F[k]
+    R g[9];
+    m3_diag(g, -r[k], -r[k], -r[k]);
+    g[0 * 3 + k] += r[0];
+    g[1 * 3 + k] += r[1];
+    g[2 * 3 + k] += r[2];
+    for (int q = 0; q < 9; q++) H[q] += g[q] * F[k];
+  }
+  const R c0 = sqrt(H[0] * H[0] + H[3] * H[3] + H[6] * H[6]);
+  const R c1 = sqrt(H[1] * H[1] + H[4] * H[4] + H[7] * H[7]);
+  const R c2 = sqrt(H[2] * H[2] + H[5] * H[5] + H[8] * H[8]);
+  m3_diag(G, c0, c1, c2);
+}
+
+// joint.js:162-253
+__device__ void joint_primal(const TWorld &w, const TJoint &j, int side, R alpha, Sys6 &s) {
+  R C[3], F[3];
+  if (v3_len_sq(j.penLin) > 0.0) {
+    joint_eval_lin(w, j, C);
+    if (j.stiffLin.v == INFINITY)
+      for (int k = 0; k < 3; k++) C[k] = C[k] + j.C0Lin[k] * (-alpha);
+    for (int k = 0; k < 3; k++) F[k] = j.penLin[k] * C[k] + j.lamLin[k];
+    R jLin[9], jAng[9], rW[3], r[3];
+    if (!side) {
+      m3_diag(jLin, R(1.0), R(1.0), R(1.0));
+      q_rotate(rW, w.b[j.a].q, j.rA);
+      for (int k = 0; k < 3; k++) r[k] = -rW[k];
+      m3_skew(jAng, r);
+      for (int k = 0; k < 3; k++) r[k] = rW[k];
+    } else {
+      m3_diag(jLin, R(-1.0), R(-1.0), R(-1.0));
+      q_rotate(rW, w.b[j.b].q, j.rB);
+      m3_skew(jAng, rW);
+      for (int k = 0; k < 3; k++) r[k] = -rW[k];
+    }
+    stamp_rows(s, jLin, jAng, j.penLin, F);
+    R G[9];
+    ball_socket_geometric(G, r, F);
+    m3_add_into(s.ang, G);
+  }
+  if (v3_len_sq(j.penAng) > 0.0) {
+    joint_eval_ang(w, j, C);
+    if (j.stiffAng.v == INFINITY)
+      for (int k = 0; k < 3; k++) C[k] = C[k] + j.C0Ang[k] * (-alpha);
+    for (int k = 0; k < 3; k++) F[k] = j.penAng[k] * C[k] + j.lamAng[k];
+    const double sg = side ? -j.torqueArm : j.torqueArm;
+    // jAng = sg I: H_ang += sg K sg, f_ang += sg F
+    for (int k = 0; k < 3; k++) {
+      s.ang[k * 3 + k] += (sg * j.penAng[k]) * sg;
+      s.ba[k] += F[k] * sg;
+    }
+  }
+}
+
+// spring.js:509-616
+__device__ void spring_primal(const TWorld &w, const TSpring &sp, int side, Sys6 &s, const TParams &P) {
+  if (sp.broken) return;
+  R d[3], n[3];
+  const R Cv = spring_eval(w, sp, d, n);
+  if (Cv != Cv) return;
+  const R k = sp.penalty;
+  const R f = k * Cv;
+  R rW[3], jLin[3], jAng[3];
+  if (!side) {
+    q_rotate(rW, w.b[sp.a].q, sp.rA);
+    for (int c = 0; c < 3; c++) jLin[c] = n[c];
+    v3_cross(jAng, rW, n);
+  } else {
+    q_rotate(rW, w.b[sp.b].q, sp.rB);
+    for (int c = 0; c < 3; c++) jLin[c] = -n[c];
+    v3_cross(jAng, rW, n);
+    for (int c = 0; c < 3; c++) jAng[c] = -jAng[c];
+  }
+  for (int r = 0; r < 3; r++)
+    for (int c = 0; c < 3; c++) {
+      s.lin[r * 3 + c] += (jLin[r] * jLin[c]) * k;
+      s.ang[r * 3 + c] += (jAng[r] * jAng[c]) * k;
+      s.cross[r * 3 + c] += (jAng[r] * jLin[c]) * k;
+    }
+  v3_add_scaled(s.bl, jLin, f);
+  v3_add_scaled(s.ba, jAng, f);
+  if (!P.springGeometric) return;
+  const R dLen = sqrt(v3_len_sq(d));
+  const double sg = side ? -1.0 : 1.0;
+  R Pm[9], S[9], Gla[9], Gal[9], Gaa[9], m0[9];
+  for (int r = 0; r < 3; r++)
+    for (int c = 0; c < 3; c++) Pm[r * 3 + c] = -(n[r] * n[c]);
+  Pm[0] = Pm[0] + 1.0; Pm[4] = Pm[4] + 1.0; Pm[8] = Pm[8] + 1.0;
+  for (int q = 0; q < 9; q++) Pm[q] = Pm[q] / dLen;
+  m3_skew(S, rW);
+  m3_mul(Gla, Pm, S);
+  for (int q = 0; q < 9; q++) Gla[q] = -Gla[q];
+  m3_mul(Gal, S, Pm);
+  m3_mul(Gaa, S, Pm);
+  m3_mul(Gaa, Gaa, S);
+  for (int q = 0; q < 9; q++) Gaa[q] = -Gaa[q];
+  const R ndotr = v3_dot(n, rW);
+  for (int r = 0; r < 3; r++)
+    for (int c = 0; c < 3; c++) m0[r * 3 + c] = rW[r] * n[c];
+  m0[0] = m0[0] - ndotr; m0[4] = m0[4] - ndotr; m0[8] = m0[8] - ndotr;
+  for (int q = 0; q < 9; q++) Gaa[q] += m0[q] * sg;
+  const R af = fabs(f);
+  for (int c = 0; c < 3; c++) {
+    const R a0 = Pm[c], a1 = Pm[3 + c], a2 = Pm[6 + c], a3 = Gal[c], a4 = Gal[3 + c], a5 = Gal[6 + c];
+    s.lin[c * 3 + c] += sqrt(a0 * a0 + a1 * a1 + a2 * a2 + a3 * a3 + a4 * a4 + a5 * a5) * af;
+  }
+  for (int c = 0; c < 3; c++) {
+    const R a0 = Gla[c], a1 = Gla[3 + c], a2 = Gla[6 + c], a3 = Gaa[c], a4 = Gaa[3 + c], a5 = Gaa[6 + c];
+    s.ang[c * 3 + c] += sqrt(a0 * a0 + a1 * a1 + a2 * a2 + a3 * a3 + a4 * a4 + a5 * a5) * af;
+  }
+}
+
+// One body's update (solver.js:425-457).
+__device__ void body_primal(const TWorld &w, int i, R alpha) {
+  const TParams &P = w.P;
+  TBody &b = w.b[i];
+  const TBodyStatic &st = w.bs[i];
+  const double dt2 = P.dt * P.dt;
+  Sys6 s;
+  R MAng[9], tmp[3], dq[3];
+  m3_diag(s.lin, R(st.mass / dt2), R(st.mass / dt2), R(st.mass / dt2));
+  world_moment(MAng, st, b.q, P.rotatedInertia != 0);
+  for (int k = 0; k < 9; k++) s.ang[k] = MAng[k] / dt2;
+  m3_zero(s.cross);
+  v3_sub(tmp, b.p, b.yl);
+  m3_mul_vec(s.bl, s.lin, tmp);
+  q_subtract(dq, b.q, b.yq);
+  m3_mul_vec(s.ba, s.ang, dq);
+  for (int e = w.fStart[i + 1] - 1; e >= w.fStart[i]; e--) {  // the body's forces, newest first
+    const uint32_t ref = w.fRef[e];
+    const uint32_t type = ref >> 30, idx = (ref >> 1) & 0x1fffffffu, side = ref & 1u;
+    if (type == 0) manifold_primal(w, w.cur[idx], (int)side, alpha, s);
+    else if (type == kRefJoint) joint_primal(w, w.j[idx], (int)side, alpha, s);
+    else spring_primal(w, w.s[idx], (int)side, s, P);
+  }
+  R xl[3], xa[3], nl[3], na[3];
+  for (int k = 0; k < 3; k++) {
+    nl[k] = -s.bl[k];
+    na[k] = -s.ba[k];
+  }
+  solve6(s.lin, s.ang, s.cross, nl, na, xl, xa);
+  v3_add(b.p, b.p, xl);
+  R q1[4];
+  q_integrate(q1, b.q, xa);
+  for (int k = 0; k < 4; k++) b.q[k] = q1[k];
+}
+
+// manifold.js:447-491
+__device__ void manifold_dual(const TWorld &w, TManifold &m, R alpha) {
+  const TParams &P = w.P;
+  const bool sphere = w.bs[m.a].shape == AVBD_SHAPE_SPHERE || w.bs[m.b].shape == AVBD_SHAPE_SPHERE;
+  for (int i = 0; i < m.count; i++) {
+    R jAAng[9], jBAng[9];
+    const ContactEvalT e = contact_eval(w, m, i, alpha, jAAng, jBAng);
+    TContact &c = m.c[i];
+    for (int k = 0; k < 3; k++) c.lam[k] = e.F[k];
+    if (e.F[0] < 0.0) c.pen[0] = js_min(c.pen[0] + P.betaLin * fabs(e.C[0]), P.penaltyMax);
+    if (e.within) {
+      c.pen[1] = js_min(c.pen[1] + P.betaLin * fabs(e.C[1]), P.penaltyMax);
+      c.pen[2] = js_min(c.pen[2] + P.betaLin * fabs(e.C[2]), P.penaltyMax);
+      c.stick = sqrt(e.C[1] * e.C[1] + e.C[2] * e.C[2]) < P.stickThreshold ? 1 : 0;
+    } else if (sphere) {
+      c.stick = 0;
+    }
+  }
+}
+
+// joint.js:255-317
+__device__ void joint_dual(const TWorld &w, TJoint &j, R alpha) {
+  const TParams &P = w.P;
+  R C[3];
+  if (v3_len_sq(j.penLin) > 0.0) {
+    joint_eval_lin(w, j, C);
+    if (j.stiffLin.v == INFINITY) {
+      for (int k = 0; k < 3; k++) C[k] = C[k] + j.C0Lin[k] * (-alpha);
+      for (int k = 0; k < 3; k++) j.lamLin[k] = j.penLin[k] * C[k] + j.lamLin[k];
+    }
+    const R cap = js_min(j.stiffLin, P.penaltyMax);
+    for (int k = 0; k < 3; k++) j.penLin[k] = js_min(j.penLin[k] + fabs(C[k]) * P.betaLin, cap);
+  }
+  if (v3_len_sq(j.penAng) > 0.0) {
+    joint_eval_ang(w, j, C);
+    if (j.stiffAng.v == INFINITY) {
+      for (int k = 0; k < 3; k++) C[k] = C[k] + j.C0Ang[k] * (-alpha);
+      for (int k = 0; k < 3; k++) j.lamAng[k] = j.penAng[k] * C[k] + j.lamAng[k];
+    }
+    const R cap = js_min(j.stiffAng, P.penaltyMax);
+    for (int k = 0; k < 3; k++) j.penAng[k] = js_min(j.penAng[k] + fabs(C[k]) * P.betaAng, cap);
+  }
+  if (v3_len_sq(j.lamAng) > j.fracture * j.fracture) {
+    for (int k = 0; k < 3; k++) j.penLin[k] = j.penAng[k] = j.lamLin[k] = j.lamAng[k] = 0.0;
+    j.broken = 1;
+  }
+}
+
+// spring.js:618-634
+__device__ void spring_dual(const TWorld &w, TSpring &s) {
+  if (s.broken) return;
+  R d[3], n[3];
+  const R Cv = spring_eval(w, s, d, n);
+  if (Cv != Cv) return;
+  if (isfinite(s.tear) && spring_tear(s, Cv)) return;
+  if (!w.P.springRamp) return;
+  s.penalty = js_min(s.penalty + fabs(Cv) * w.P.betaLin, js_min(s.stiffness, w.P.penaltyMax));
+}
+
+// The iterations of one step in one block: per iteration the colour phases
+// (bodies of one colour are independent), then every force's dual update,
+// and on the last iteration the BDF1 velocity (solver.js:476-488).
+__global__ void __launch_bounds__(kBlock) iterate_kernel(TWorld w) {
+  if (w.ctl[2]) return;
+  const TParams &P = w.P;
+  const int numColors = w.ctl[3], total = w.ctl[0];
+  const int total_it = P.iterations + (P.postStabilize ? 1 : 0);
+  const int t = threadIdx.x;
+  for (int it = 0; it < total_it; it++) {
+    const R alpha = P.postStabilize ? (it < P.iterations ? 1.0 : 0.0) : P.alpha;
+    for (int c = 0; c < numColors; c++) {
+      for (int k = w.colorStart[c] + t; k < w.colorStart[c + 1]; k += blockDim.x) body_primal(w, w.order[k], alpha);
+      __syncthreads();
+    }
+    if (it < P.iterations) {
+      for (int k = t; k < total; k += blockDim.x)
+        if (w.cur[k].count > 0) manifold_dual(w, w.cur[k], alpha);
+      for (int k = t; k < w.nj; k += blockDim.x)
+        if (!w.j[k].removed) joint_dual(w, w.j[k], alpha);
+      for (int k = t; k < w.ns; k += blockDim.x) spring_dual(w, w.s[k]);
+      __syncthreads();
+    }
+    if (it == P.iterations - 1) {
+      for (int i = t; i < w.n; i += blockDim.x) {
+        TBody &b = w.b[i];
+        for (int k = 0; k < 3; k++) b.pv[k] = b.v[k];
+        if (w.bs[i].mass > 0) {
+          for (int k = 0; k < 3; k++) b.v[k] = (b.p[k] - b.p0[k]) / P.dt;
+          R dq[3];
+          q_subtract(dq, b.q, b.q0);
+          for (int k = 0; k < 3; k++) b.w[k] = dq[k] / P.dt;
+        }
+      }
+      __syncthreads();
+    }
+  }
+}
+
+// This step's manifolds become the next step's previous ones: keys of the
+// live ones, in key order (candidates are in key order already).
+__global__ void __launch_bounds__(kBlock) commit_kernel(TWorld w) {
+  if (w.ctl[2]) return;
+  const int total = w.ctl[0];
+  __shared__ int base;
+  if (threadIdx.x == 0) base = 0;
+  __syncthreads();
+  typedef cub::BlockScan<int, kBlock> Scan;
+  __shared__ typename Scan::TempStorage tmp;
+  for (int c0 = 0; c0 < total; c0 += kBlock) {
+    const int c = c0 + threadIdx.x;
+    const int live = c < total && w.cur[c].count > 0 ? 1 : 0;
+    int at, tot;
+    Scan(tmp).ExclusiveSum(live, at, tot);
+    if (live) {
+      w.prev[base + at] = w.cur[c];
+      w.prevKey[base + at] = w.key[c];
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) base += tot;
+    __syncthreads();
+  }
+  if (threadIdx.x == 0) w.ctl[1] = base;
+}
+
+// grad[d] = sum over bodies and components of g[i][k] * dx_i,k / d theta_d
+__global__ void backward_kernel(TWorld w, const double *g, double *grad) {
+  __shared__ double acc[kTangentDims];
+  if (threadIdx.x < kTangentDims) acc[threadIdx.x] = 0.0;
+  __syncthreads();
+  double part[kTangentDims] = {};
+  for (int i = threadIdx.x; i < w.n; i += blockDim.x)
+    for (int k = 0; k < 3; k++)
+      for (int d = 0; d < kTangentDims; d++) part[d] += g[i * 3 + k] * w.b[i].p[k].d[d];
+  for (int d = 0; d < kTangentDims; d++) atomicAdd(&acc[d], part[d]);
+  __syncthreads();
+  if (threadIdx.x < kTangentDims) grad[threadIdx.x] = acc[threadIdx.x];
+}
+
+__global__ void read_kernel(TWorld w, double *pos, double *dpos, double *quat) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < w.n; i += gridDim.x * blockDim.x) {
+    for (int k = 0; k < 3; k++) {
+      pos[i * 3 + k] = w.b[i].p[k].v;
+      if (dpos)
+        for (int d = 0; d < kTangentDims; d++) dpos[(i * 3 + k) * kTangentDims + d] = w.b[i].p[k].d[d];
+    }
+    if (quat)
+      for (int k = 0; k < 4; k++) quat[i * 4 + k] = w.b[i].q[k].v;
+  }
+}
+
+}  // namespace tg
+
+// ---------------------------------------------------------------------------
+// Host side: the differentiable step's own device state, packed from a host
+// world (f64) with the caller's seeds.
+// ---------------------------------------------------------------------------
+struct TangentCtx {
+  tg::TWorld w{};
+  std::vector<void *> allocs;
+  int smCount = 0;
+  ~TangentCtx() {
+    for (void *p : allocs) cudaFree(p);
+  }
+  template <class T>
+  cudaError_t alloc(T **p, size_t count) {
+    void *q = nullptr;
+    const cudaError_t e = cudaMalloc(&q, std::max<size_t>(count, 1) * sizeof(T));
+    if (e != cudaSuccess) return e;
+    cudaMemset(q, 0, std::max<size_t>(count, 1) * sizeof(T));
+    allocs.push_back(q);
+    *p = (T *)q;
+    return cudaSuccess;
+  }
+};
+
+void tangent_destroy(TangentCtx *t) { delete t; }
+
+static tg::R dual_of(double v) { return tg::R(v); }
+
+// Pack `world` and seed its inputs. Returns 0 or an AVBD_ERR_* with `msg`.
+int tangent_pack(TangentCtx **out, const avbd_world *world, const avbd_params &P, const avbd_tangent_seed *seeds,
+                 int nSeeds, char *msg, size_t msgLen, cudaStream_t st) {
+  using namespace tg;
+  const avbd_body_soa &B = world->bodies;
+  const avbd_joint_soa &J = world->joints;
+  const avbd_spring_soa &S = world->springs;
+  const int n = B.count, nj = J.count, ns = S.count;
+  if (n <= 0 || !B.pos || !B.size || !B.mass || !B.moment || !B.radius || !B.friction) {
+    snprintf(msg, msgLen, "avbd_adjoint_forward: bodies need count > 0 and size/mass/moment/radius/friction/pos");
+    return AVBD_ERR_ARG;
+  }
+  if (world->num_scenes > 1) {
+    snprintf(msg, msgLen, "avbd_adjoint_forward: one scene per call");
+    return AVBD_ERR_ARG;
+  }
+  std::vector<TBody> hb(n);
+  std::vector<TBodyStatic> hs(n);
+  std::vector<std::vector<uint32_t>> refs(n);
+  std::vector<TJoint> hj(nj);
+  std::vector<TSpring> hsp(ns);
+  for (int i = 0; i < n; i++) {
+    TBody &b = hb[i];
+    TBodyStatic &s = hs[i];
+    for (int k = 0; k < 3; k++) {
+      b.p[k] = dual_of(B.pos[i * 3 + k]);
+      b.v[k] = dual_of(B.vel ? B.vel[i * 3 + k] : 0.0);
+      b.w[k] = dual_of(B.omega ? B.omega[i * 3 + k] : 0.0);
+      b.pv[k] = dual_of(B.prev_vel ? B.prev_vel[i * 3 + k] : (B.vel ? B.vel[i * 3 + k] : 0.0));
+      s.moment[k] = B.moment[i * 3 + k];
+      s.half[k] = B.size[i * 3 + k] * 0.5;
+    }
+    for (int k = 0; k < 4; k++) b.q[k] = dual_of(B.quat ? B.quat[i * 4 + k] : (k == 3 ? 1.0 : 0.0));
+    s.mass = B.mass[i];
+    s.radius = B.radius[i];
+    s.friction = dual_of(B.friction[i]);
+    s.shape = B.shape ? B.shape[i] : AVBD_SHAPE_BOX;
+  }
+  for (int k = 0; k < nj; k++) {
+    TJoint &j = hj[k];
+    j.a = J.body_a[k];
+    j.b = J.body_b[k];
+    if (j.b < 0 || j.b >= n || j.a >= n || j.a == j.b) {
+      snprintf(msg, msgLen, "avbd_adjoint_forward: joint %d: bad body indices", k);
+      return AVBD_ERR_ARG;
+    }
+    for (int c = 0; c < 3; c++) {
+      j.rA[c] = dual_of(J.r_a[k * 3 + c]);
+      j.rB[c] = dual_of(J.r_b[k * 3 + c]);
+      j.penLin[c] = dual_of(J.penalty_lin ? J.penalty_lin[k * 3 + c] : 0.0);
+      j.penAng[c] = dual_of(J.penalty_ang ? J.penalty_ang[k * 3 + c] : 0.0);
+      j.lamLin[c] = dual_of(J.lambda_lin ? J.lambda_lin[k * 3 + c] : 0.0);
+      j.lamAng[c] = dual_of(J.lambda_ang ? J.lambda_ang[k * 3 + c] : 0.0);
+    }
+    j.stiffLin = dual_of(J.stiffness_lin[k]);
+    j.stiffAng = dual_of(J.stiffness_ang[k]);
+    j.fracture = J.fracture[k];
+    const double sx = (j.a >= 0 ? B.size[j.a * 3] : 0) + B.size[j.b * 3];
+    const double sy = (j.a >= 0 ? B.size[j.a * 3 + 1] : 0) + B.size[j.b * 3 + 1];
+    const double sz = (j.a >= 0 ? B.size[j.a * 3 + 2] : 0) + B.size[j.b * 3 + 2];
+    j.torqueArm = sx * sx + sy * sy + sz * sz;  // joint.js:108-112
+    j.broken = J.broken && J.broken[k] ? 1 : 0;
+    if (j.a >= 0) refs[j.a].push_back(make_ref(kRefJoint, k, 0));
+    refs[j.b].push_back(make_ref(kRefJoint, k, 1));
+  }
+  for (int k = 0; k < ns; k++) {
+    TSpring &s = hsp[k];
+    s.a = S.body_a[k];
+    s.b = S.body_b[k];
+    if (s.a < 0 || s.b < 0 || s.a >= n || s.b >= n || s.a == s.b || !(S.rest[k] >= 0)) {
+      snprintf(msg, msgLen, "avbd_adjoint_forward: spring %d: bad body indices or unresolved rest length", k);
+      return AVBD_ERR_ARG;
+    }
+    for (int c = 0; c < 3; c++) {
+      s.rA[c] = dual_of(S.r_a[k * 3 + c]);
+      s.rB[c] = dual_of(S.r_b[k * 3 + c]);
+    }
+    s.stiffness = dual_of(S.stiffness[k]);
+    s.rest = S.rest[k];
+    s.tear = S.tear_strain ? S.tear_strain[k] : INFINITY;
+    s.penalty = dual_of(S.penalty ? S.penalty[k] : 0.0);
+    s.peak = dual_of(S.peak_strain ? S.peak_strain[k] : 0.0);
+    s.broken = S.broken && S.broken[k] ? 1 : 0;
+    refs[s.a].push_back(make_ref(kRefSpring, k, 0));
+    refs[s.b].push_back(make_ref(kRefSpring, k, 1));
+  }
+  std::vector<uint32_t> cRef;
+  for (int i = 0; i < n; i++) {
+    hs[i].cStart = (int)cRef.size();
+    cRef.insert(cRef.end(), refs[i].begin(), refs[i].end());
+    hs[i].cEnd = (int)cRef.size();
+  }
+  TParams tp{};
+  tp.dt = P.dt; tp.gravity = P.gravity; tp.alpha = P.alpha; tp.gamma = P.gamma; tp.betaLin = P.beta_lin;
+  tp.betaAng = P.beta_ang; tp.penaltyMin = P.penalty_min; tp.margin = P.collision_margin;
+  tp.stickThreshold = P.stick_threshold; tp.penaltyMax = dual_of(P.penalty_max); tp.iterations = P.iterations;
+  tp.postStabilize = P.post_stabilize; tp.rotatedInertia = P.rotated_inertia; tp.springRamp = P.spring_stiffness_ramp;
+  tp.springGeometric = P.spring_geometric_stiffness;
+  tp.cachedJacobians = P.cached_contact_jacobians;
+  // seeds
+  for (int k = 0; k < nSeeds; k++) {
+    const avbd_tangent_seed &sd = seeds[k];
+    const int d = sd.dir;
+    if (d < 0 || d >= kTangentDims) {
+      snprintf(msg, msgLen, "avbd_adjoint_forward: seed %d: direction %d outside 0..%d", k, d, kTangentDims - 1);
+      return AVBD_ERR_ARG;
+    }
+    if (sd.kind == AVBD_SEED_VELOCITY) {
+      if (sd.index < 0 || sd.index >= n || sd.comp < 0 || sd.comp > 2) {
+        snprintf(msg, msgLen, "avbd_adjoint_forward: seed %d: bad body or component", k);
+        return AVBD_ERR_ARG;
+      }
+      hb[sd.index].v[sd.comp].d[d] = 1.0;
+      hb[sd.index].pv[sd.comp].d[d] = 1.0;  // a scene starts with the two equal (rigid.js:51)
+    } else if (sd.kind == AVBD_SEED_FRICTION) {
+      if (sd.index < 0 || sd.index >= n) {
+        snprintf(msg, msgLen, "avbd_adjoint_forward: seed %d: bad body", k);
+        return AVBD_ERR_ARG;
+      }
+      hs[sd.index].friction.d[d] = 1.0;
+    } else if (sd.kind == AVBD_SEED_PENALTY_MAX) {
+      tp.penaltyMax.d[d] = 1.0;
+    } else if (sd.kind == AVBD_SEED_JOINT_STIFFNESS) {
+      if (sd.index < 0 || sd.index >= nj) {
+        snprintf(msg, msgLen, "avbd_adjoint_forward: seed %d: bad joint", k);
+        return AVBD_ERR_ARG;
+      }
+      if (std::isfinite(hj[sd.index].stiffLin.v)) hj[sd.index].stiffLin.d[d] = 1.0;
+      if (std::isfinite(hj[sd.index].stiffAng.v)) hj[sd.index].stiffAng.d[d] = 1.0;
+    } else {
+      snprintf(msg, msgLen, "avbd_adjoint_forward: seed %d: unknown kind %d", k, sd.kind);
+      return AVBD_ERR_ARG;
+    }
+  }
+  TangentCtx *t = new TangentCtx();
+  TWorld &w = t->w;
+  w.P = tp;
+  w.n = n; w.nj = nj; w.ns = ns;
+  w.mcap = std::max(16 * n, 256);
+  w.fcap = 2 * w.mcap + 2 * (nj + ns) + 64;
+  cudaError_t e = cudaSuccess;
+  uint32_t *cRefD = nullptr;
+  std::vector<uint32_t> prio(n);
+  for (int i = 0; i < n; i++) prio[i] = color_priority((uint32_t)i);
+  uint32_t *prioD = nullptr;
+  if ((e = t->alloc(&w.b, n)) || (e = t->alloc(&w.bs, n)) || (e = t->alloc(&cRefD, cRef.size())) ||
+      (e = t->alloc(&w.j, nj)) || (e = t->alloc(&w.s, ns)) || (e = t->alloc(&w.pairCount, n + 1)) ||
+      (e = t->alloc(&w.pairStart, n + 1)) || (e = t->alloc(&w.key, w.mcap)) || (e = t->alloc(&w.cur, w.mcap)) ||
+      (e = t->alloc(&w.prev, w.mcap)) || (e = t->alloc(&w.prevKey, w.mcap)) || (e = t->alloc(&w.ctl, 4)) ||
+      (e = t->alloc(&w.fStart, n + 1)) || (e = t->alloc(&w.fCount, n + 1)) || (e = t->alloc(&w.fRef, w.fcap)) ||
+      (e = t->alloc(&w.color, n)) || (e = t->alloc(&w.order, n)) || (e = t->alloc(&w.colorStart, kMaxColors + 1)) ||
+      (e = t->alloc(&prioD, n))) {
+    delete t;
+    snprintf(msg, msgLen, "avbd_adjoint_forward: cudaMalloc: %s", cudaGetErrorString(e));
+    return AVBD_ERR_CUDA;
+  }
+  w.cRef = cRefD;
+  w.prio = prioD;
+  cudaMemcpyAsync(w.b, hb.data(), sizeof(TBody) * n, cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(w.bs, hs.data(), sizeof(TBodyStatic) * n, cudaMemcpyHostToDevice, st);
+  if (!cRef.empty()) cudaMemcpyAsync(cRefD, cRef.data(), sizeof(uint32_t) * cRef.size(), cudaMemcpyHostToDevice, st);
+  if (nj) cudaMemcpyAsync(w.j, hj.data(), sizeof(TJoint) * nj, cudaMemcpyHostToDevice, st);
+  if (ns) cudaMemcpyAsync(w.s, hsp.data(), sizeof(TSpring) * ns, cudaMemcpyHostToDevice, st);
+  cudaMemcpyAsync(prioD, prio.data(), sizeof(uint32_t) * n, cudaMemcpyHostToDevice, st);
+  cudaDeviceGetAttribute(&t->smCount, cudaDevAttrMultiProcessorCount, 0);
+  e = cudaStreamSynchronize(st);
+  if (e != cudaSuccess) {
+    delete t;
+    snprintf(msg, msgLen, "avbd_adjoint_forward: %s", cudaGetErrorString(e));
+    return AVBD_ERR_CUDA;
+  }
+  *out = t;
+  return AVBD_OK;
+}
+
+// `steps` differentiable steps; the scan of the pair counts on the stream.
+int tangent_step(TangentCtx *t, int steps, void *temp, size_t tempBytes, char *msg, size_t msgLen, cudaStream_t st) {
+  using namespace tg;
+  TWorld &w = t->w;
+  const int blocks = std::max(1, std::min((w.n + 127) / 128, t->smCount * 4));
+  for (int s = 0; s < steps; s++) {
+    cudaMemsetAsync(w.pairCount + w.n, 0, sizeof(int), st);
+    pairs_count_kernel<<<blocks, 128, 0, st>>>(w);
+    size_t tb = tempBytes;
+    cub::DeviceScan::ExclusiveSum(temp, tb, w.pairCount, w.pairStart, w.n + 1, st);
+    pairs_write_kernel<<<blocks, 128, 0, st>>>(w);
+    narrow_kernel<<<std::max(1, std::min((w.mcap + 63) / 64, t->smCount * 4)), 64, 0, st>>>(w);
+    forces_init_kernel<<<blocks, 128, 0, st>>>(w);
+    bodies_init_kernel<<<blocks, 128, 0, st>>>(w);
+    adjacency_coloring_kernel<<<1, kBlock, 0, st>>>(w);
+    iterate_kernel<<<1, kBlock, 0, st>>>(w);
+    commit_kernel<<<1, kBlock, 0, st>>>(w);
+  }
+  cudaError_t e = cudaStreamSynchronize(st);
+  if (e == cudaSuccess) e = cudaGetLastError();
+  if (e != cudaSuccess) {
+    snprintf(msg, msgLen, "avbd_adjoint_forward: %s", cudaGetErrorString(e));
+    return AVBD_ERR_CUDA;
+  }
+  int ctl[4];
+  cudaMemcpy(ctl, w.ctl, sizeof(ctl), cudaMemcpyDeviceToHost);
+  if (ctl[2]) {
+    snprintf(msg, msgLen, "avbd_adjoint_forward: candidate pairs or force lists exceed the differentiable step's "
+                          "arenas (%d pair slots)", w.mcap);
+    return AVBD_ERR_CAPACITY;
+  }
+  return AVBD_OK;
+}
+
+size_t tangent_temp_bytes(const TangentCtx *t) {
+  size_t a = 0;
+  cub::DeviceScan::ExclusiveSum(nullptr, a, (int *)nullptr, (int *)nullptr, t->w.n + 1);
+  return a;
+}
+
+int tangent_read(TangentCtx *t, double *pos, double *dpos, double *quat, cudaStream_t st) {
+  const int n = t->w.n;
+  double *d = nullptr;
+  const size_t bytes = sizeof(double) * ((size_t)n * 3 + (size_t)n * 3 * kTangentDims + (size_t)n * 4);
+  if (cudaMalloc(&d, bytes) != cudaSuccess) return AVBD_ERR_CUDA;
+  double *dp = d, *dd = d + (size_t)n * 3, *dq = dd + (size_t)n * 3 * kTangentDims;
+  tg::read_kernel<<<std::max(1, (n + 255) / 256), 256, 0, st>>>(t->w, dp, dd, dq);
+  cudaMemcpyAsync(pos ? pos : nullptr, dp, pos ? sizeof(double) * n * 3 : 0, cudaMemcpyDeviceToHost, st);
+  if (dpos) cudaMemcpyAsync(dpos, dd, sizeof(double) * n * 3 * kTangentDims, cudaMemcpyDeviceToHost, st);
+  if (quat) cudaMemcpyAsync(quat, dq, sizeof(double) * n * 4, cudaMemcpyDeviceToHost, st);
+  const cudaError_t e = cudaStreamSynchronize(st);
+  cudaFree(d);
+  return e == cudaSuccess ? AVBD_OK : AVBD_ERR_CUDA;
+}
+
+int tangent_backward(TangentCtx *t, const double *gradPos, double *gradParams, cudaStream_t st) {
+  const int n = t->w.n;
+  double *d = nullptr;
+  if (cudaMalloc(&d, sizeof(double) * ((size_t)n * 3 + kTangentDims)) != cudaSuccess) return AVBD_ERR_CUDA;
+  cudaMemcpyAsync(d, gradPos, sizeof(double) * n * 3, cudaMemcpyHostToDevice, st);
+  tg::backward_kernel<<<1, 256, 0, st>>>(t->w, d, d + (size_t)n * 3);
+  cudaMemcpyAsync(gradParams, d + (size_t)n * 3, sizeof(double) * kTangentDims, cudaMemcpyDeviceToHost, st);
+  const cudaError_t e = cudaStreamSynchronize(st);
+  cudaFree(d);
+  return e == cudaSuccess ? AVBD_OK : AVBD_ERR_CUDA;
+}
+
+int tangent_dims() { return kTangentDims; }
+
+}  // namespace avbd

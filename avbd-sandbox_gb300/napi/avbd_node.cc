@@ -237,6 +237,8 @@ void bind_params(napi_env env, napi_value obj, avbd_params *p) {
   if (get_number(env, obj, "cachedContactJacobians", &v)) p->cached_contact_jacobians = v != 0;
   if (get_number(env, obj, "waitLimit", &v)) p->wait_limit = (int32_t)v;
   if (get_number(env, obj, "neighborWaitLimit", &v)) p->neighbor_wait_limit = (int32_t)v;
+  if (get_number(env, obj, "tailDiv", &v)) p->tail_div = (int32_t)v;
+  if (get_number(env, obj, "graph", &v)) p->graph = (int32_t)v;
   if (get_number(env, obj, "fp64RatioThreshold", &v)) p->fp64_ratio_threshold = v;
   if (get_number(env, obj, "lanesPerBody", &v)) p->lanes_per_body = (int32_t)v;
   if (get_number(env, obj, "schedule", &v)) p->schedule = (int32_t)v;
@@ -405,6 +407,60 @@ napi_value UpdateJointAnchor(napi_env env, napi_callback_info info) {
   return rc ? throw_status(env, a.h->ctx, rc) : undefined(env);
 }
 
+// setGrab(handle, body, Float64Array(3) local, Float64Array(3) target, stiffness); body -1 releases
+napi_value SetGrab(napi_env env, napi_callback_info info) {
+  Args a;
+  if (!args(env, info, &a)) return nullptr;
+  int32_t body = -1;
+  if (a.argc < 2 || napi_get_value_int32(env, a.argv[1], &body) != napi_ok) {
+    napi_throw_type_error(env, nullptr, "setGrab(handle, body, local, target, stiffness)");
+    return nullptr;
+  }
+  if (body < 0) {
+    const int rc = avbd_set_grab(a.h->ctx, -1, nullptr, nullptr, 0.0);
+    return rc ? throw_status(env, a.h->ctx, rc) : undefined(env);
+  }
+  double k = 0;
+  if (a.argc < 5 || napi_get_value_double(env, a.argv[4], &k) != napi_ok) {
+    napi_throw_type_error(env, nullptr, "setGrab(handle, body, local, target, stiffness)");
+    return nullptr;
+  }
+  napi_value holder;
+  napi_create_object(env, &holder);
+  napi_set_named_property(env, holder, "local", a.argv[2]);
+  napi_set_named_property(env, holder, "target", a.argv[3]);
+  double *local = nullptr, *target = nullptr;
+  if (!get_array(env, holder, "local", napi_float64_array, 3, &local) || !local) return nullptr;
+  if (!get_array(env, holder, "target", napi_float64_array, 3, &target) || !target) return nullptr;
+  const int rc = avbd_set_grab(a.h->ctx, body, local, target, k);
+  return rc ? throw_status(env, a.h->ctx, rc) : undefined(env);
+}
+
+// autotune(handle, trialSteps) -> {schedule, lanesPerBody, tailDiv, blocksPerSm, candidates, defaultMs, bestMs}
+napi_value Autotune(napi_env env, napi_callback_info info) {
+  Args a;
+  if (!args(env, info, &a)) return nullptr;
+  int32_t steps = 3;
+  if (a.argc >= 2) napi_get_value_int32(env, a.argv[1], &steps);
+  avbd_tuning t;
+  const int rc = avbd_autotune(a.h->ctx, steps, &t);
+  if (rc) return throw_status(env, a.h->ctx, rc);
+  napi_value o, v;
+  napi_create_object(env, &o);
+  const struct {
+    const char *name;
+    double value;
+  } fields[] = {{"schedule", (double)t.schedule},      {"lanesPerBody", (double)t.lanes_per_body},
+                {"tailDiv", (double)t.tail_div},       {"blocksPerSm", (double)t.blocks_per_sm},
+                {"candidates", (double)t.candidates},  {"defaultMs", t.default_ms},
+                {"bestMs", t.best_ms}};
+  for (const auto &f : fields) {
+    napi_create_double(env, f.value, &v);
+    napi_set_named_property(env, o, f.name, v);
+  }
+  return o;
+}
+
 // setProfiling(handle, on)
 napi_value SetProfiling(napi_env env, napi_callback_info info) {
   Args a;
@@ -504,6 +560,8 @@ napi_value Init(napi_env env, napi_value exports) {
                      {"readColoring", ReadColoring},
                      {"setColoring", SetColoring},
                      {"updateJointAnchor", UpdateJointAnchor},
+                     {"setGrab", SetGrab},
+                     {"autotune", Autotune},
                      {"setProfiling", SetProfiling},
                      {"lastProfile", LastProfile},
                      {"stats", Stats},

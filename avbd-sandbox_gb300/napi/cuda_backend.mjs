@@ -64,6 +64,9 @@ function toSoA(solver) {
   const jointOrder = [];
   const springOrder = [];
   solver.forces.forEach((f, k) => {
+    // the app's drag joint stays CPU-side: the grab is uniform state here
+    // (boot.js:606-611; the WebGPU pack skips it too, backend.js:945)
+    if (f.isDragJoint) return;
     if (isJoint(f)) { joints.push(f); jointOrder.push(k); }
     else if (isSpring(f)) { springs.push(f); springOrder.push(k); }
   });
@@ -149,8 +152,7 @@ export class CudaBackend {
     this.ready = false;
     this.topologyDirty = true;
     this.overrideColoring = null; // {colorOf: Int32Array, numColors}
-    this._grab = null;
-    this.dragJoint = null;
+    this.grab = null; // {body, local, target, stiffness} (backend.js:302-307), pushed every step
     this._profiling = false;
   }
 
@@ -170,7 +172,6 @@ export class CudaBackend {
       if (this._profiling) addon.setProfiling(this.handle, true);
     }
     this.packed = toSoA(solver);
-    this.dragJoint = [...this.packed.jointIndex.keys()].find((j) => j.isDragJoint) || null;
     addon.pack(this.handle, this.packed.world);
     if (this.overrideColoring) addon.setColoring(this.handle, this.overrideColoring.colorOf);
     this.topologyDirty = false;
@@ -182,21 +183,19 @@ export class CudaBackend {
   // step(solver) -> ms spent encoding (backend.js:1393); asynchronous on the device.
   step(solver) {
     if (this.topologyDirty || !this.handle) this.pack(solver);
-    if (this.dragJoint) this.updateJointAnchor(this.dragJoint);
+    // the grab as the WebGPU backend passes it: uniform state of every step
+    // (backend.js:1330-1334); the tool moves grab.target in place
+    const g = this.grab;
+    if (g) addon.setGrab(this.handle, g.body, Float64Array.from(g.local), Float64Array.from(g.target), g.stiffness);
+    else if (this._grabbed) addon.setGrab(this.handle, -1);
+    this._grabbed = !!g;
     const t0 = performance.now();
     addon.step(this.handle, 1);
     return performance.now() - t0;
   }
 
-  // Mouse grab (backend.js:302-307). The CPU engine's drag joint (boot.js:610,
-  // flagged isDragJoint) is packed as a real joint with no body A, and its
-  // world anchor - the grab target the tool writes into joint.rA as the mouse
-  // moves (boot.js:632) - is pushed before every step.
-  get grab() { return this._grab; }
-  set grab(g) {
-    this._grab = g;
-    this.topologyDirty = true; // the drag joint joins or leaves the pack
-  }
+  // The launch configuration tuned on the current state (avbd_autotune).
+  autotune(trialSteps = 3) { return addon.autotune(this.handle, trialSteps); }
 
   async idle() { if (this.handle) addon.synchronize(this.handle); }
 

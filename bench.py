@@ -455,44 +455,86 @@ def run_batched(abi, backend, args, flush):
     """The batched workload: 512 independent random box piles (body counts
     log-uniform in [64, 8192], edges U[0.3, 2] m, densities log-uniform
     [100, 1e4] kg/m^3, mu U[0.2, 0.9], contact-free column drop), all in one
-    context: every phase of a step is one launch over all scenes. Timed like
-    the main workload (per-step device events, L2 flushed between steps)."""
+    context: every phase of a step is one launch over all scenes. Steps 1..K,
+    timed like the main workload (per-step device events on the library's
+    stream, L2 flushed between steps), in three configurations: the default
+    launches; each step replayed as a CUDA graph; and the graph with the
+    launch configuration avbd_autotune picked on the run's state after
+    K/2 steps. Accuracy: after the tuned run, one more step of the batch
+    against the oracle's step of each of a sample of scenes from the same
+    state."""
     import torch
+    from oracle import Oracle
 
     sc = pkg().scene
     parts = sc.pile_batch()
-    worlds = [p.world() for p in parts]
-    batch = sc.batch_worlds(worlds)
-    params = abi.default_params(gravity=-9.81, iterations=10, body_order=abi.ORDER_PRIORITY)
-    gpu = backend.GpuBackend(params)
-    gpu.pack(batch)
-    gpu.step(args.warmup)
-    gpu.idle()
-    gpu.pack(batch)
-    gpu.set_profiling(True)
-    total_ms, K = 0.0, args.batched_steps
-    phases = {k: 0.0 for k in ("broadphase_ms", "narrowphase_ms", "prepare_ms", "coloring_ms", "solve_ms")}
-    contacts = lanes = 0
-    for _ in range(K):
-        flush.fill_(1.0)
-        torch.cuda.synchronize()
-        gpu.step(1)
-        p = gpu.last_profile
-        total_ms += p["step_ms"]
-        contacts += p["contacts"]
-        lanes += p["lanes_per_body"]
-        for k in phases:
-            phases[k] += p[k]
-    gpu.set_profiling(False)
-    gpu.destroy()
+    batch = sc.batch_worlds([p.world() for p in parts])
+    base = dict(gravity=-9.81, iterations=10, body_order=abi.ORDER_PRIORITY)
+    K = args.batched_steps
     n_scenes = len(parts)
-    return {
-        "value": n_scenes * K / (total_ms / 1e3), "unit": "scene-steps/s", "scenes": n_scenes,
-        "bodies": batch.n_bodies, "steps": K, "ms_per_step": total_ms / K,
-        "steps_per_s": K / (total_ms / 1e3), "mean_contacts": contacts / K, "mean_lanes_per_body": lanes / K,
-        "phases_ms": {k: v / K for k, v in phases.items()},
-        "workload": f"{n_scenes} random box piles ({batch.n_bodies:,} bodies) in one context, steps 1..{K}",
-    }
+
+    def timed(params):
+        gpu = backend.GpuBackend(params)
+        gpu.pack(batch)
+        gpu.step(args.warmup)
+        gpu.idle()
+        gpu.pack(batch)
+        gpu.set_profiling(True)
+        ms, contacts, lanes, graphs = 0.0, 0, 0, 0
+        for _ in range(K):
+            flush.fill_(1.0)
+            torch.cuda.synchronize()
+            gpu.step(1)
+            p = gpu.last_profile
+            ms += p["step_ms"]
+            contacts += p["contacts"]
+            lanes += p["lanes_per_body"]
+            graphs += p["via_graph"]
+        gpu.set_profiling(False)
+        rec = {"value": n_scenes * K / (ms / 1e3), "unit": "scene-steps/s", "ms_per_step": ms / K,
+               "graph_steps": graphs, "mean_contacts": contacts / K, "mean_lanes_per_body": lanes / K}
+        return gpu, rec
+
+    out = {"scenes": n_scenes, "bodies": batch.n_bodies, "steps": K,
+           "workload": f"{n_scenes} random box piles ({batch.n_bodies:,} bodies) in one context, steps 1..{K}"}
+    gpu, out["default"] = timed(abi.default_params(**base))
+    gpu.destroy()
+    gpu, out["graph"] = timed(abi.default_params(**base, graph=1))
+    gpu.destroy()
+    # tune on the run's own state half way through
+    gpu = backend.GpuBackend(abi.default_params(**base, graph=1))
+    gpu.pack(batch)
+    gpu.step(K // 2)
+    gpu.idle()
+    tune = gpu.autotune(3)
+    gpu.destroy()
+    tuned = abi.default_params(**base, graph=1, schedule=tune["schedule"], lanes_per_body=tune["lanes_per_body"],
+                               tail_div=tune["tail_div"], blocks_per_sm=tune["blocks_per_sm"])
+    gpu, out["tuned_graph"] = timed(tuned)
+    out["autotune"] = dict(tune, tuned_at_step=K // 2)
+    best = max(("default", "graph", "tuned_graph"), key=lambda k: out[k]["value"])
+    out["value"], out["unit"], out["ms_per_step"], out["best"] = (out[best]["value"], "scene-steps/s",
+                                                                   out[best]["ms_per_step"], best)
+    # accuracy: every 32nd scene against its own oracle, one step from the state after step K
+    state = gpu.read_state(manifolds=True).round_to_device()
+    gpu.destroy()
+    gpu = backend.GpuBackend(tuned)
+    gpu.pack(state)
+    gpu.step(1)
+    gpu.idle()
+    got = gpu.read_state(manifolds=True)
+    gpu.destroy()
+    worst, same_topo, sample = 0.0, True, list(range(0, n_scenes, 32))
+    for k in sample:
+        ref = Oracle(tuned, state.scene(k))
+        ref.step(1)
+        want, g = ref.state(), got.scene(k)
+        dyn = want.mass > 0
+        worst = max(worst, float(np.abs(g.pos[dyn] - want.pos[dyn]).max()))
+        same_topo = same_topo and g.manifold_dict() == want.manifold_dict()
+    out["accuracy_vs_oracle"] = {"scenes": sample, "from_step": K, "max_pos_error_m": worst,
+                                 "manifolds_identical": same_topo, "tolerance_m": 1e-5}
+    return out
 
 
 def run_accuracy(abi, backend):

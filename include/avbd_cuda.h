@@ -119,6 +119,15 @@ typedef struct avbd_params {
      colour-phase schedule's tail segment) gives up; 0 = wait_limit (or its
      default when that is 0 as well). Grid barriers keep wait_limit.        */
   int32_t neighbor_wait_limit;
+  /* Colour-phase schedule: colours of at most (solve blocks / tail_div) lane
+     chunks run as one dependency-driven tail segment per iteration instead
+     of one grid barrier each; 0 = 8. Does not change results. */
+  int32_t tail_div;
+  /* 1: each step is replayed as a CUDA graph (captured on first use, once
+     per manifold-arena parity; rebuilt after a pack, an arena regrow, an
+     uploaded colouring or avbd_autotune). Profiled steps launch directly.
+     Does not change results. */
+  int32_t graph;
 } avbd_params;
 
 /*
@@ -230,6 +239,7 @@ typedef struct avbd_stats {
   double max_constraint_error;
   double max_lambda;
   double max_penalty;
+  int64_t graph_steps;     /* steps replayed as a CUDA graph since the pack  */
 } avbd_stats;
 
 /* Per-phase device times of the last step, ms (src/physics/gpu/backend.js:58),
@@ -252,6 +262,8 @@ typedef struct avbd_profile {
   int32_t np_edge;
   int32_t np_exact;
   int32_t lanes_per_body;     /* lanes per body the step's solve used       */
+  int32_t via_graph;          /* 1: the step ran as a CUDA graph; only
+                                 step_ms is timed then (phases read 0)     */
 } avbd_profile;
 
 typedef struct avbd_ctx avbd_ctx;
@@ -306,6 +318,16 @@ int avbd_set_coloring(avbd_ctx *ctx, const int32_t *color_of);
    Ordered on the context's stream after the steps already queued. */
 int avbd_update_joint_anchor(avbd_ctx *ctx, int32_t joint, const double r_a[3]);
 
+/* Replaces the mouse grab of `GpuBackend` (src/physics/gpu/backend.js:302-307,
+   1330-1334; applied in src/physics/gpu/shaders.js:2119-2161): from the next
+   queued step on, body `body` is pulled by a finite ball socket from the
+   world point `target` to its body-local point `local`, C = target - (p +
+   R local), with penalty fixed at `stiffness` (the app uses max(400,
+   900 m), src/app/boot.js:592), no multiplier, in that body's primal only.
+   No topology change: no repack, no colouring edge. body = -1 releases it
+   (local and target may then be NULL). Ordered on the context's stream. */
+int avbd_set_grab(avbd_ctx *ctx, int32_t body, const double local[3], const double target[3], double stiffness);
+
 /* Replaces `getConstraintGpuState()` (src/physics/gpu/backend.js:1950-1967):
    where a renderer or another CUDA consumer on the same device finds the
    live state, without a copy. Valid until the next avbd_pack or
@@ -330,12 +352,77 @@ int avbd_read_pairs(avbd_ctx *ctx, int32_t *body_a, int32_t *body_b,
 int avbd_read_stats(avbd_ctx *ctx, avbd_stats *out);
 
 /* Replaces `setProfiling(on)` / `lastProfile` (src/physics/gpu/backend.js:1836-1897).
-   When on, each step records per-phase CUDA events (adds a sync per step). */
+   When on, each step records CUDA events on the context's stream (per phase,
+   or around the whole step when it runs as a graph) and waits for them. */
 int avbd_set_profiling(avbd_ctx *ctx, int32_t on);
 int avbd_read_profile(avbd_ctx *ctx, avbd_profile *out);
 
 /* Number of device kernels launched since the last pack. */
 int avbd_kernel_launches(avbd_ctx *ctx, int64_t *out);
+
+/*
+ * Autotuner of the solve's launch configuration: the schedule (colour phases
+ * or dependency wavefront), lanes per body, the tail segment's threshold and
+ * resident solve blocks per SM. Each candidate runs `trial_steps` steps from
+ * the current state (device time by CUDA events); the state is then put back
+ * exactly as it was and the fastest configuration is kept for the following
+ * steps (and reported in `out`). The per-step counts the choice was made on
+ * (bodies, warm-start manifolds) are reported beside it. Configurations of
+ * equal lanes per body give identical results; other lane counts change the
+ * order of the f32 sums within a body's update. The reference's counterpart
+ * is its per-frame choice of encoded colours (src/physics/gpu/backend.js:
+ * 1673-1681).
+ */
+typedef struct avbd_tuning {
+  int32_t schedule;
+  int32_t lanes_per_body;  /* 0: chosen per body                            */
+  int32_t tail_div;
+  int32_t blocks_per_sm;
+  int32_t candidates;      /* configurations timed                          */
+  int32_t trial_steps;
+  double default_ms;       /* ms per step of the configuration before       */
+  double best_ms;          /* ms per step of the chosen configuration       */
+  int64_t bodies;
+  int64_t manifolds;       /* warm-start manifold slots of the tuned state  */
+} avbd_tuning;
+int avbd_autotune(avbd_ctx *ctx, int32_t trial_steps, avbd_tuning *out);
+
+/*
+ * The differentiable step (forward-mode tangents through the whole AVBD
+ * step; the C5 configuration's gradients). `avbd_adjoint_forward` packs
+ * `world` into the context's differentiable step - its own device state, f64
+ * values (the f64 engine's discrete decisions: pairs, SAT/clip topology,
+ * feature-ID warm start, colouring, clamps, stick) and AVBD_TANGENT_DIMS
+ * directional derivatives - seeds the inputs `seeds` name, and runs `steps`
+ * steps: every contact point and basis as a function of the poses, the warm
+ * start, every primal 6x6 solve and dual update of every iteration, and the
+ * BDF1 velocity carry the derivatives. `avbd_adjoint_read` returns the body
+ * positions (n x 3), their derivatives (n x 3 x AVBD_TANGENT_DIMS, direction
+ * fastest) and the orientations (n x 4). `avbd_adjoint_backward` is the
+ * vector-Jacobian product of the run: grad_params[d] = sum over bodies and
+ * components of grad_pos[i][k] d pos[i][k] / d theta_d, theta_d the input of
+ * direction d - the backward of a torch.autograd.Function whose forward is
+ * avbd_adjoint_forward (forward mode carries every seeded direction at once,
+ * so nothing is checkpointed and the backward is one contraction).
+ * Independent of the context's own (FP32) state and of avbd_pack; one scene.
+ * No counterpart in the reference (which has no derivatives); its rows are
+ * the reference's step (src/physics/solver.js:307-493).
+ */
+#define AVBD_TANGENT_DIMS 5
+#define AVBD_SEED_VELOCITY 0        /* initial velocity component `comp` of body `index` */
+#define AVBD_SEED_FRICTION 1        /* the friction of body `index`                      */
+#define AVBD_SEED_PENALTY_MAX 2     /* the penalty cap penalty_max                       */
+#define AVBD_SEED_JOINT_STIFFNESS 3 /* the finite stiffnesses of joint `index`           */
+typedef struct avbd_tangent_seed {
+  int32_t kind;   /* AVBD_SEED_*                                           */
+  int32_t index;  /* body or joint                                         */
+  int32_t comp;   /* velocity component 0..2                               */
+  int32_t dir;    /* direction 0..AVBD_TANGENT_DIMS-1 (seeds may share one) */
+} avbd_tangent_seed;
+int avbd_adjoint_forward(avbd_ctx *ctx, const avbd_world *world, int32_t steps, const avbd_tangent_seed *seeds,
+                         int32_t n_seeds);
+int avbd_adjoint_read(avbd_ctx *ctx, double *pos, double *dpos, double *quat);
+int avbd_adjoint_backward(avbd_ctx *ctx, const double *grad_pos, double *grad_params);
 
 /* Text of the last error on this context (or, when ctx is NULL, of the last
    failed avbd_create or context-free call). Never NULL. */

@@ -906,6 +906,12 @@ struct Solver {
   Collider collider;
   std::vector<Force *> graveyard;   // removed joints/springs, freed with the solver
   std::vector<Force *> manifoldPool;  // recycled manifolds (solver.js:68-73)
+  // The WebGPU backend's mouse grab (src/physics/gpu/shaders.js:2119-2161,
+  // src/physics/gpu/backend.js:302-307): a finite ball socket from a world
+  // target to a point on one body, with its penalty fixed at the stiffness,
+  // no multiplier and no dual update, applied in that body's primal only (no
+  // force list, no colouring edge). Null when nothing is grabbed.
+  Force *grab = nullptr;
   ~Solver();
 };
 
@@ -1446,6 +1452,7 @@ struct Spring : Force {
 };
 
 Solver::~Solver() {
+  delete grab;
   for (Body *b : bodies) delete b;
   for (Force *f : forces) delete f;
   for (Force *f : graveyard) delete f;
@@ -1759,6 +1766,7 @@ static void step(Solver &s) {
       m3_mul_vec(rhsAng, lhsAng, dq);
       for (int k = (int)b->forces.size() - 1; k >= 0; k--)
         b->forces[k]->updatePrimal(b, alpha, lhsLin, lhsAng, lhsCross, rhsLin, rhsAng);
+      if (s.grab && s.grab->bodyB == b) s.grab->updatePrimal(b, alpha, lhsLin, lhsAng, lhsCross, rhsLin, rhsAng);
       v3_negate(rhsLin, rhsLin);
       v3_negate(rhsAng, rhsAng);
       solve6(lhsLin, lhsAng, lhsCross, rhsLin, rhsAng, dxLin, dxAng);
@@ -1862,6 +1870,8 @@ static void load_manifolds(orc_solver *o, const avbd_manifold_soa &M, std::vecto
 // else joints, then springs, then manifolds, each in array order.
 int orc_load(orc_solver *o, const avbd_world *w) {
   Solver &s = o->s;
+  delete s.grab;
+  s.grab = nullptr;
   for (Body *b : s.bodies) delete b;
   for (Force *f : s.forces) delete f;
   s.bodies.clear();
@@ -2042,6 +2052,30 @@ int orc_read_state(orc_solver *o, avbd_world *w) {
 
 // Joints/springs that were removed from the force list (broken joints) keep
 // the state they had when removed; report them via this accessor.
+// The uniform mouse grab (src/physics/gpu/shaders.js:2119-2161): body < 0
+// releases it. Applies from the next step on.
+int orc_set_grab(orc_solver *o, int32_t body, const double *local, const double *target, double stiffness) {
+  Solver &s = o->s;
+  delete s.grab;
+  s.grab = nullptr;
+  if (body < 0) return AVBD_OK;
+  if (body >= (int32_t)s.bodies.size() || !(stiffness > 0)) return AVBD_ERR_ARG;
+  Joint *j = new Joint();
+  j->solver = &s;
+  j->bodyA = nullptr;
+  j->bodyB = s.bodies[body];
+  for (int k = 0; k < 3; k++) {
+    j->rA[k] = target[k];
+    j->rB[k] = local[k];
+    j->penaltyLin[k] = stiffness;
+  }
+  j->stiffnessLin = stiffness;
+  j->stiffnessAng = 0;
+  j->setup();
+  s.grab = j;
+  return AVBD_OK;
+}
+
 int orc_num_forces(orc_solver *o, int32_t *joints, int32_t *springs, int32_t *manifolds) {
   int j = 0, sp = 0, m = 0;
   for (const Force *f : o->s.forces) {

@@ -56,6 +56,7 @@ def _bind(L, tangent=False):
     L.orc_num_forces.argtypes = [vp, vp, vp, vp]
     L.orc_read_joint.argtypes = [vp, C.c_int32, vp, vp, vp]
     L.orc_contact_normal_c.argtypes = [vp, vp, C.c_int64, vp]
+    L.orc_set_grab.argtypes = [vp, C.c_int32, vp, vp, C.c_double]
     if tangent:
         L.orc_t_dims.restype = C.c_int
         L.orc_t_seed.argtypes = [vp, C.c_int32, C.c_int32, C.c_int32, C.c_int32]
@@ -128,6 +129,14 @@ class Oracle:
 
     def step(self, n=1):
         self.L.orc_step(self.h, n)
+
+    def set_grab(self, body, local=(0.0, 0.0, 0.0), target=(0.0, 0.0, 0.0), stiffness=0.0):
+        """The WebGPU backend's uniform mouse grab (shaders.js:2119-2161);
+        body < 0 releases it."""
+        a = np.ascontiguousarray(local, np.float64)
+        b = np.ascontiguousarray(target, np.float64)
+        if self.L.orc_set_grab(self.h, int(body), _p(a), _p(b), float(stiffness)) != 0:
+            raise ValueError("bad grab")
 
     def num_forces(self):
         j, s, m = C.c_int32(), C.c_int32(), C.c_int32()

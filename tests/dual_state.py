@@ -119,24 +119,5 @@ def all_errors(got, want):
 
 
 def scene_slice(w, s):
-    """Scene `s` of a batched world as a world of its own (bodies renumbered
-    from 0, its manifolds only; the batches compared here have no joints or
-    springs)."""
-    import importlib
-
-    abi = importlib.import_module("avbd-sandbox_gb300.abi")
-    b0, b1 = int(w.scene_start[s]), int(w.scene_start[s + 1])
-    assert w.n_joints == 0 and w.n_springs == 0
-    out = abi.World(b1 - b0)
-    for f in ("shape", "size", "mass", "moment", "radius", "friction", "pos", "quat", "vel", "omega", "prev_vel"):
-        setattr(out, f, np.ascontiguousarray(getattr(w, f)[b0:b1]))
-    sel = np.nonzero((w.m_body_a[:w.m_count] >= b0) & (w.m_body_a[:w.m_count] < b1))[0]
-    out.ensure_manifold_capacity(max(len(sel), 1))
-    out.m_count = len(sel)
-    for f in ("m_num_contacts", "m_basis", "m_friction", "m_feature", "m_r_a", "m_r_b", "m_c0", "m_penalty",
-              "m_lambda", "m_stick"):
-        getattr(out, f)[:len(sel)] = getattr(w, f)[sel]
-    out.m_body_a[:len(sel)] = w.m_body_a[sel] - b0
-    out.m_body_b[:len(sel)] = w.m_body_b[sel] - b0
-    out.m_order[:len(sel)] = np.arange(len(sel))
-    return out
+    """Scene `s` of a batched world as a world of its own (abi.World.scene)."""
+    return w.scene(s)

@@ -133,3 +133,95 @@ def test_device_views(abi, scenes, backend_mod):
     st = np.zeros(w.n_joints, np.int32)
     assert rt.cudaMemcpy(st.ctypes.data, v["joint_state"], st.nbytes, 2) == 0
     assert np.array_equal(st & 1, gpu.read_state().j_broken)
+
+
+def test_graph_replay_is_bit_identical(abi, scenes, backend_mod):
+    """Steps replayed as CUDA graphs (one per manifold-arena parity) give the
+    same trajectory bit for bit as directly launched steps, through an arena
+    regrow (which rebuilds the graphs) and an overflowing step that is
+    skipped and run again."""
+    s = scenes.pyramid(layers=10)
+    outs = []
+    for graph, cap in ((0, 0), (1, 0), (1, 1)):
+        gpu = backend_mod.GpuBackend(abi.default_params(**s.params, body_order=abi.ORDER_PRIORITY, graph=graph,
+                                                        max_pairs_per_body=cap))
+        gpu.pack(s.world())
+        gpu.step(40)
+        gpu.idle()
+        st = gpu.last_stats
+        assert st["overflow"] == 0 and st["steps"] == 40
+        assert (st["graph_steps"] > 0) == (graph == 1)
+        outs.append(gpu.read_state())
+    for o in outs[1:]:
+        assert np.array_equal(outs[0].pos, o.pos) and np.array_equal(outs[0].quat, o.quat)
+
+
+def test_autotune_restores_state_and_keeps_parity(abi, scenes, backend_mod):
+    """avbd_autotune times its candidate configurations from the current
+    state and puts that state back exactly; the next step under the chosen
+    configuration matches the oracle's step from the same state."""
+    s = scenes.pyramid(layers=8)
+    params, s0 = warm_state(abi, s, 30)
+    gpu = backend_mod.GpuBackend(params)
+    gpu.pack(s0)
+    gpu.step(2)
+    gpu.idle()
+    before = gpu.read_state(manifolds=True)
+    t = gpu.autotune(2)
+    assert t["candidates"] >= 10 and t["best_ms"] <= t["default_ms"] and t["bodies"] == s0.n_bodies
+    after = gpu.read_state(manifolds=True)
+    assert np.array_equal(before.pos, after.pos) and np.array_equal(before.quat, after.quat)
+    assert after.manifold_dict() == before.manifold_dict()
+    assert np.array_equal(before.m_lambda[:before.m_count], after.m_lambda[:after.m_count])
+    ref = Oracle(params, before.round_to_device())
+    ref.step(1)
+    gpu.step(1)
+    gpu.idle()
+    dyn = s0.mass > 0
+    assert np.max(np.abs(gpu.read_state().pos[dyn] - ref.state().pos[dyn])) <= 1e-5
+
+
+@pytest.mark.parametrize("schedule", [0, 1])
+def test_uniform_grab_matches_oracle(abi, scenes, backend_mod, schedule):
+    """The topology-free grab (backend.js:302-307, shaders.js:2119-2161)
+    through avbd_set_grab, against the oracle's grab: one step from the same
+    state within 1e-5 m, then 20 steps with the target moved before each step
+    (as the app's pointer drag does, boot.js:633-636) within 5e-3 m, then a
+    release; the grab changes no topology (same colouring as without it)."""
+    s = scenes.cube_stack(n=6, beta=None)
+    params = abi.default_params(**s.params, body_order=abi.ORDER_PRIORITY, schedule=schedule)
+    o = Oracle(params, s.world())
+    o.step(20)
+    s0 = o.state().round_to_device()
+    body, local = 4, np.array([0.3, -0.2, 0.5])
+    k = max(400.0, 900.0 * s0.mass[body])
+    target = s0.pos[body] + local + np.array([0.2, 0.1, 0.6])
+    ref = Oracle(params, s0)
+    gpu = backend_mod.GpuBackend(params)
+    gpu.pack(s0)
+    ref.set_grab(body, local, target, k)
+    gpu.set_grab(body, local, target, k)
+    ref.step(1)
+    gpu.step(1)
+    gpu.idle()
+    dyn = s0.mass > 0
+    want, got = ref.state(), gpu.read_state()
+    assert np.max(np.abs(got.pos[dyn] - want.pos[dyn])) <= 1e-5
+    assert np.max(np.abs(got.quat[dyn] - want.quat[dyn])) <= 1e-5
+    assert np.array_equal(gpu.read_coloring()[0], ref.coloring()[0])
+    for step in range(20):
+        target = target + np.array([0.02, 0.0, 0.03])
+        ref.set_grab(body, local, target, k)
+        gpu.set_grab(body, local, target, k)
+        ref.step(1)
+        gpu.step(1)
+    gpu.idle()
+    want, got = ref.state(), gpu.read_state()
+    assert want.pos[body, 2] > s0.pos[body, 2] + 0.5
+    assert np.max(np.abs(got.pos[dyn] - want.pos[dyn])) < 5e-3
+    ref.set_grab(-1)
+    gpu.set_grab(-1)
+    ref.step(3)
+    gpu.step(3)
+    gpu.idle()
+    assert np.max(np.abs(gpu.read_state().pos[dyn] - ref.state().pos[dyn])) < 5e-3

@@ -10,9 +10,9 @@ tolerances, per quantity, relative with the floors of dual_state.FLOORS:
 
   quantity                       max        99.9th percentile
   contact lambda, normal         3e-2       1e-3
-  contact lambda, friction rows  (*)        1e-3
+  contact lambda, friction rows  (*)        5e-3
   contact penalty, normal        3e-2       1e-3
-  contact penalty, friction      (*)        1e-3
+  contact penalty, friction      (*)        5e-3
   contact anchors rA, rB         5e-2       1e-3   (floor 1 mm)
   contact C0                     2e-5 m     -      (absolute)
   joint lambda (lin, ang)        1e-3       -
@@ -42,7 +42,7 @@ from oracle import Oracle
 pytestmark = pytest.mark.gpu
 
 CONTACT_MAX = {"lambda_normal": 3e-2, "penalty_normal": 3e-2, "r_a": 5e-2, "r_b": 5e-2, "c0": 2e-5}
-CONTACT_P999 = {"lambda_normal": 1e-3, "lambda_tangent": 1e-3, "penalty_normal": 1e-3, "penalty_tangent": 1e-3,
+CONTACT_P999 = {"lambda_normal": 1e-3, "lambda_tangent": 5e-3, "penalty_normal": 1e-3, "penalty_tangent": 5e-3,
                 "r_a": 1e-3, "r_b": 1e-3}
 FRICTION_OUTLIER = (1e-2, 1e-4)  # (relative error, largest fraction of contacts above it)
 JOINT_MAX = {"lambda_lin": 1e-3, "lambda_ang": 1e-3, "penalty_lin": 3e-2, "penalty_ang": 3e-2}
