@@ -399,6 +399,8 @@ def run_gpu(args):
         out["dense"] = run_dense(abi, backend, args, s, world, params, flush, n_dyn, ws, rank)
     if args.batched_steps > 0:
         out["batched"] = run_batched(abi, backend, args, flush)
+    if rank == 0 and args.adjoint_steps > 0:
+        out["adjoint"] = run_adjoint(abi, backend, args)
     if rank == 0 and not args.no_accuracy:
         out["accuracy_vs_oracle"] = run_accuracy(abi, backend)
     if rank == 0:
@@ -537,6 +539,102 @@ def run_batched(abi, backend, args, flush):
     return out
 
 
+def run_adjoint(abi, backend, args):
+    """The differentiable wall: 16 x 16 bricks of 0.5 x 0.25 x 0.25 m (hard
+    bonds) struck by a 50 kg sphere; the gradient of the mean brick
+    displacement after S steps with respect to the sphere's initial velocity
+    (3), the bricks' friction and the penalty cap (5 directions).
+
+    adjoint: avbd_adjoint_forward over S steps (every step carries the five
+    derivatives) + avbd_adjoint_read + avbd_adjoint_backward, timed on the
+    host around the C ABI calls (pack, steps, readback of positions,
+    derivatives and gradient included), median of R runs after one warm-up.
+    plain: the same scene's FP32 step over the same S steps (device time,
+    CUDA events). CPU: the oracle and the tangent oracle over the same steps,
+    1 thread. Accuracy: at 30 steps (the horizon where the oracle's central
+    differences converge) the device gradient against the tangent oracle's
+    exact gradient, and along the sphere's y velocity against the
+    differences."""
+    import torch
+    from oracle import Oracle, TangentOracle
+
+    sys.path.insert(0, os.path.join(ROOT, "tests"))
+    import c5_gradients as c5
+
+    sc = pkg().scene
+    S, R = args.adjoint_steps, 3
+    th = c5.theta0(abi)
+    s = sc.brick_wall_c5()
+    w = s.world()
+    params = c5.params_of(abi, s, th, abi.ORDER_PRIORITY)
+    seeds = c5.seeds(abi, s, w)
+    gpu = backend.GpuBackend(params)
+    times = []
+    for r in range(R + 1):
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        gpu.adjoint_forward(w, S, seeds)
+        pos, tan, _ = gpu.adjoint_read()
+        grad = gpu.adjoint_backward(c5.upstream(s, w, pos))
+        t = time.perf_counter() - t0
+        if r:
+            times.append(t)
+    adj_s = statistics.median(times)
+    # the plain FP32 step of the same scene, same steps
+    plain = backend.GpuBackend(params)
+    plain.pack(w)
+    plain.step(3)
+    plain.idle()
+    plain.pack(w)
+    plain.set_profiling(True)
+    ms = 0.0
+    for _ in range(S):
+        plain.step(1)
+        ms += plain.last_profile["step_ms"]
+    plain.set_profiling(False)
+    plain.destroy()
+    # CPU: the oracle and the tangent oracle, same steps
+    t0 = time.perf_counter()
+    Oracle(params, w).step(S)
+    cpu_plain = time.perf_counter() - t0
+    o = TangentOracle(params, w)
+    for sd in seeds:
+        o.seed(*sd)
+    t0 = time.perf_counter()
+    o.step(S)
+    cpu_tan = time.perf_counter() - t0
+    # accuracy at the differences' horizon
+    T = c5.STEPS
+    gpu.adjoint_forward(w, T, seeds)
+    pos, tan, _ = gpu.adjoint_read()
+    L_dev, g_dev = c5.gradient_from_tangents(s, w, pos, tan, th)
+    L_ref, g_ref = c5.tangent_gradient(abi, sc, th, T, abi.ORDER_PRIORITY)
+    fd = c5.central_differences(abi, sc, th, T, c5.H[1], abi.ORDER_PRIORITY)
+    gpu.destroy()
+    scale = float(np.max(np.abs(g_ref)))
+    return {
+        "workload": "differentiable wall: 256 bricks (16 x 16, 0.5 x 0.25 x 0.25 m, 1000 kg/m^3, hard bonds) + "
+                    "50 kg sphere at 8 m/s; gradient of the mean brick displacement w.r.t. the sphere's initial "
+                    "velocity (3), brick mu and the penalty cap",
+        "bodies": w.n_bodies, "joints": w.n_joints, "steps": S, "directions": abi.TANGENT_DIMS,
+        "value": S / adj_s, "unit": "adjoint steps/s",
+        "how": f"avbd_adjoint_forward({S} steps, 5 forward-mode tangents, f64 values) + read + "
+               f"avbd_adjoint_backward, host-timed around the C ABI calls, median of {R}",
+        "ms_per_step": adj_s * 1e3 / S,
+        "plain_fp32_step": {"value": S / (ms / 1e3), "unit": "steps/s", "ms_per_step": ms / S,
+                            "how": "the same scene's FP32 step, device time (CUDA events)"},
+        "cpu_baseline": {"plain_f64": S / cpu_plain, "tangent_f64": S / cpu_tan, "unit": "steps/s", "cores": 1,
+                         "kind": "port", "sample": f"the oracle and the tangent oracle over the same {S} steps"},
+        "accuracy": {"steps": T, "objective_device": L_dev, "objective_oracle": L_ref,
+                     "gradient_device": g_dev.tolist(), "gradient_tangent_oracle": g_ref.tolist(),
+                     "max_rel_error_vs_tangent_oracle": float(np.max(np.abs(g_dev - g_ref))) / scale,
+                     "central_differences_h5e-5": fd.tolist(),
+                     "v0_y_rel_error_vs_differences": abs(g_dev[1] - fd[1]) / abs(fd[1]),
+                     "tolerance": "1e-6 relative to the tangent oracle (f64, same operations); 5 % along v0_y "
+                                  "against the differences"},
+    }
+
+
 def run_accuracy(abi, backend):
     """The small configurations against the f64 oracle over their whole runs,
     both stepping the same start state (device colouring order replayed by
@@ -658,6 +756,7 @@ def main():
     ap.add_argument("--batched-steps", type=int, default=240, help="steps of the 512-scene batch (0: skip)")
     ap.add_argument("--dense-start", type=int, default=300, help="step the crushed-pile window starts after")
     ap.add_argument("--dense-steps", type=int, default=20, help="timed steps of the crushed-pile window (0: skip)")
+    ap.add_argument("--adjoint-steps", type=int, default=60, help="steps of the differentiable wall (0: skip)")
     ap.add_argument("--trace", default="", help="write each timed step's profile and counters (JSON lines)")
     args = ap.parse_args()
     if args.warmup < 3:

@@ -2233,6 +2233,15 @@ int orc_t_seed(orc_solver *o, int32_t what, int32_t index, int32_t comp, int32_t
     s.bodies[index]->friction.d[dir] = 1.0;
   } else if (what == 2) {
     s.p.penaltyMax.d[dir] = 1.0;
+  } else if (what == 3) {
+    // joint `index`'s finite stiffnesses (joint.js:95-96; the caps of the
+    // penalty ramp, joint.js:283-301)
+    Joint *hit = nullptr;
+    for (Force *f : s.forces)
+      if (f->kind == KIND_JOINT && static_cast<Joint *>(f)->id == index) hit = static_cast<Joint *>(f);
+    if (!hit) return AVBD_ERR_ARG;
+    if (std::isfinite(hit->stiffnessLin.v)) hit->stiffnessLin.d[dir] = 1.0;
+    if (std::isfinite(hit->stiffnessAng.v)) hit->stiffnessAng.d[dir] = 1.0;
   } else {
     return AVBD_ERR_ARG;
   }

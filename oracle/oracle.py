@@ -286,6 +286,15 @@ class TangentOracle(Oracle):
     def seed_penalty_max(self, direction):
         self._seed(2, 0, 0, direction)
 
+    def seed_joint_stiffness(self, joint, direction):
+        """The finite linear and angular stiffness of joint `joint`."""
+        self._seed(3, joint, 0, direction)
+
+    def seed(self, kind, index, comp, direction):
+        """One seed in the C ABI's form (AVBD_SEED_* kind, index, comp,
+        direction), as avbd_adjoint_forward takes them."""
+        self._seed(kind, index, comp, direction)
+
     @staticmethod
     def freeze_geometry(mode: int):
         """Deny the narrow phase's geometry its tangents in every tangent

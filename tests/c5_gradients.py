@@ -26,9 +26,18 @@ def theta0(abi) -> np.ndarray:
     return np.array([0.0, 8.0, 0.0, 0.6, abi.default_params().penalty_max])
 
 
-def objective(abi, scenes, theta, steps: int) -> float:
+def params_of(abi, s, theta, order):
+    """The wall's parameters at theta; `order` is the primal sweep's body
+    order: None for the reference engine's (newest body first), or
+    abi.ORDER_PRIORITY for the colour order of the integer-priority
+    colouring (the CUDA backend's schedule)."""
+    kw = {} if order is None else {"body_order": order}
+    return abi.default_params(**s.params, penalty_max=float(theta[4]), **kw)
+
+
+def objective(abi, scenes, theta, steps: int, order=None) -> float:
     s = scenes.brick_wall_c5(mu=float(theta[3]), sphere_velocity=tuple(float(v) for v in theta[:3]))
-    params = abi.default_params(**s.params, penalty_max=float(theta[4]))
+    params = params_of(abi, s, theta, order)
     w = s.world()
     o = Oracle(params, w)
     o.step(steps)
@@ -36,23 +45,22 @@ def objective(abi, scenes, theta, steps: int) -> float:
     return float(np.linalg.norm(o.state().pos[b0:b1] - w.pos[b0:b1], axis=1).mean())
 
 
-def tangent_gradient(abi, scenes, theta, steps: int):
-    """The objective and its exact derivative along theta, from the tangent
-    oracle: the sphere's velocity components, every brick's friction and the
-    penalty cap each carry one direction."""
-    s = scenes.brick_wall_c5(mu=float(theta[3]), sphere_velocity=tuple(float(v) for v in theta[:3]))
-    params = abi.default_params(**s.params, penalty_max=float(theta[4]))
-    w = s.world()
-    o = TangentOracle(params, w)
+def seeds(abi, s, w):
+    """The seeds of the gradient's five directions, as (kind, index, comp,
+    direction): the sphere's velocity components (0-2), every brick's
+    friction (3), the penalty cap (4)."""
     sphere = w.n_bodies - 1
     b0, b1 = s.meta["bricks"]
-    for k in range(3):
-        o.seed_velocity(sphere, k, k)
-    for b in range(b0, b1):
-        o.seed_friction(b, 3)
-    o.seed_penalty_max(4)
-    o.step(steps)
-    pos, tan = o.positions()
+    out = [(abi.SEED_VELOCITY, sphere, k, k) for k in range(3)]
+    out += [(abi.SEED_FRICTION, b, 0, 3) for b in range(b0, b1)]
+    out.append((abi.SEED_PENALTY_MAX, 0, 0, 4))
+    return out
+
+
+def gradient_from_tangents(s, w, pos, tan, theta):
+    """The objective and its gradient from the positions after the run and
+    their derivatives along the five directions."""
+    b0, b1 = s.meta["bricks"]
     d = pos[b0:b1] - w.pos[b0:b1]
     dist = np.linalg.norm(d, axis=1)
     grad = np.einsum("ij,ijk->k", d / dist[:, None], tan[b0:b1]) / (b1 - b0)
@@ -60,13 +68,43 @@ def tangent_gradient(abi, scenes, theta, steps: int):
     return float(dist.mean()), grad
 
 
-def central_differences(abi, scenes, theta, steps: int, h: float) -> np.ndarray:
+def upstream(s, w, pos):
+    """dL/dpos of the objective at positions `pos` (n x 3): the upstream
+    gradient a backward pass contracts with the position derivatives."""
+    b0, b1 = s.meta["bricks"]
+    g = np.zeros_like(pos)
+    d = pos[b0:b1] - w.pos[b0:b1]
+    g[b0:b1] = d / np.linalg.norm(d, axis=1)[:, None] / (b1 - b0)
+    return g
+
+
+def tangent_gradient(abi, scenes, theta, steps: int, order=None):
+    """The objective and its exact derivative along theta, from the tangent
+    oracle: the sphere's velocity components, every brick's friction and the
+    penalty cap each carry one direction."""
+    s = scenes.brick_wall_c5(mu=float(theta[3]), sphere_velocity=tuple(float(v) for v in theta[:3]))
+    params = params_of(abi, s, theta, order)
+    w = s.world()
+    o = TangentOracle(params, w)
+    for kind, index, comp, direction in seeds(abi, s, w):
+        if kind == abi.SEED_VELOCITY:
+            o.seed_velocity(index, comp, direction)
+        elif kind == abi.SEED_FRICTION:
+            o.seed_friction(index, direction)
+        else:
+            o.seed_penalty_max(direction)
+    o.step(steps)
+    pos, tan = o.positions()
+    return gradient_from_tangents(s, w, pos, tan, theta)
+
+
+def central_differences(abi, scenes, theta, steps: int, h: float, order=None) -> np.ndarray:
     scale = np.array([1.0, 1.0, 1.0, 1.0, theta[4]])
     g = np.zeros(len(theta))
     for i in range(len(theta)):
         e = np.zeros(len(theta))
         e[i] = h * scale[i]
-        g[i] = (objective(abi, scenes, theta + e, steps) - objective(abi, scenes, theta - e, steps)) / (2 * h)
+        g[i] = (objective(abi, scenes, theta + e, steps, order) - objective(abi, scenes, theta - e, steps, order)) / (2 * h)
     return g
 
 

@@ -1,8 +1,11 @@
-"""Writes tests/golden/c5_gradients.json (run from the repo root:
-`python tests/golden/make_c5_gradients.py`): the differentiable wall's
-objective, its central differences on the f64 oracle at the two steps of
-tests/c5_gradients.py, and its exact derivative from the tangent oracle: the
-reference of an adjoint's gradient."""
+"""Writes the differentiable wall's reference gradients (run from the repo
+root: `python tests/golden/make_c5_gradients.py`): its objective, its central
+differences on the f64 oracle at the two steps of tests/c5_gradients.py, and
+its exact derivative from the tangent oracle - the reference an adjoint's
+gradient is checked against. Two files, one per primal body order:
+c5_gradients.json (the reference engine's order, newest body first) and
+c5_gradients_priority.json (the colour order of the integer-priority
+colouring, the schedule of the CUDA backend and of its differentiable step)."""
 import json
 import os
 import sys
@@ -15,18 +18,27 @@ for p in (ROOT, os.path.join(ROOT, "oracle"), os.path.dirname(HERE)):
 
 import c5_gradients as c5  # noqa: E402
 
+FILES = {None: "c5_gradients.json", "priority": "c5_gradients_priority.json"}
+
+
+def compute(abi, scenes, order):
+    th = c5.theta0(abi)
+    return {"steps": c5.STEPS, "names": list(c5.NAMES), "theta": th.tolist(),
+            "body_order": "reference" if order is None else "priority",
+            "objective": c5.objective(abi, scenes, th, c5.STEPS, order),
+            "differences": {repr(h): c5.central_differences(abi, scenes, th, c5.STEPS, h, order).tolist()
+                            for h in c5.H},
+            "tangent": c5.tangent_gradient(abi, scenes, th, c5.STEPS, order)[1].tolist()}
+
 
 def main():
     abi, scenes = c5.modules()
-    th = c5.theta0(abi)
-    out = {"steps": c5.STEPS, "names": list(c5.NAMES), "theta": th.tolist(),
-           "objective": c5.objective(abi, scenes, th, c5.STEPS),
-           "differences": {repr(h): c5.central_differences(abi, scenes, th, c5.STEPS, h).tolist() for h in c5.H},
-           "tangent": c5.tangent_gradient(abi, scenes, th, c5.STEPS)[1].tolist()}
-    with open(os.path.join(HERE, "c5_gradients.json"), "w") as f:
-        json.dump(out, f, indent=1)
-        f.write("\n")
-    print(json.dumps(out, indent=1))
+    for key, name in FILES.items():
+        out = compute(abi, scenes, None if key is None else abi.ORDER_PRIORITY)
+        with open(os.path.join(HERE, name), "w") as f:
+            json.dump(out, f, indent=1)
+            f.write("\n")
+        print(name, json.dumps(out))
 
 
 if __name__ == "__main__":
