@@ -385,6 +385,107 @@ class World:
         out.m_order[:len(ms)] = np.arange(len(ms))
         return out
 
+    def edited(self, keep, extra: "World | None" = None):
+        """The scene graph after an edit: the bodies with keep[i] true, in
+        their order, then the bodies of `extra` appended (with its joints and
+        springs, renumbered); joints and springs touching an erased body are
+        dropped, the rest keep their relative force-list order. Returns the
+        new world (this world's current state for the survivors, no
+        manifolds) and the maps new -> old index of bodies, joints and springs
+        (-1 for appended elements), as avbd_repack takes them."""
+        keep = np.asarray(keep, bool)
+        n0 = int(keep.sum())
+        ex = extra if extra is not None else World(0)
+        new_of = np.full(self.n_bodies, -1, np.int64)
+        new_of[keep] = np.arange(n0)
+        jk = (new_of[self.j_body_b] >= 0) & ((self.j_body_a < 0) | (new_of[np.maximum(self.j_body_a, 0)] >= 0))
+        sk = (new_of[self.s_body_a] >= 0) & (new_of[self.s_body_b] >= 0)
+        nj, ns = int(jk.sum()) + ex.n_joints, int(sk.sum()) + ex.n_springs
+        w = World(n0 + ex.n_bodies, nj, ns)
+        for f in ("shape", "size", "mass", "moment", "radius", "friction", "pos", "quat", "vel", "omega",
+                  "prev_vel"):
+            getattr(w, f)[:n0] = getattr(self, f)[keep]
+            getattr(w, f)[n0:] = getattr(ex, f)
+        jf = ("j_r_a", "j_r_b", "j_stiffness_lin", "j_stiffness_ang", "j_fracture", "j_penalty_lin", "j_penalty_ang",
+              "j_lambda_lin", "j_lambda_ang", "j_broken")
+        sf = ("s_r_a", "s_r_b", "s_stiffness", "s_rest", "s_tear_strain", "s_penalty", "s_peak_strain", "s_broken")
+        j0, s0 = int(jk.sum()), int(sk.sum())
+        for f in jf:
+            getattr(w, f)[:j0] = getattr(self, f)[jk]
+            getattr(w, f)[j0:] = getattr(ex, f)
+        for f in sf:
+            getattr(w, f)[:s0] = getattr(self, f)[sk]
+            getattr(w, f)[s0:] = getattr(ex, f)
+        ja = self.j_body_a[jk]
+        w.j_body_a[:j0] = np.where(ja < 0, -1, new_of[np.maximum(ja, 0)])
+        w.j_body_b[:j0] = new_of[self.j_body_b[jk]]
+        w.j_body_a[j0:] = np.where(ex.j_body_a < 0, -1, ex.j_body_a + n0)
+        w.j_body_b[j0:] = ex.j_body_b + n0
+        w.s_body_a[:s0] = new_of[self.s_body_a[sk]]
+        w.s_body_b[:s0] = new_of[self.s_body_b[sk]]
+        w.s_body_a[s0:] = ex.s_body_a + n0
+        w.s_body_b[s0:] = ex.s_body_b + n0
+        # force-list order: survivors in their old order, then the appended
+        # forces in theirs
+        old_rank = np.concatenate([self.j_order[jk], self.s_order[sk]]).astype(np.int64)
+        new_rank = np.concatenate([ex.j_order, ex.s_order]).astype(np.int64) + (old_rank.max() + 1 if len(old_rank)
+                                                                              else 0)
+        rank = np.concatenate([old_rank, new_rank])
+        order = np.empty(len(rank), np.int32)
+        order[np.argsort(rank, kind="stable")] = np.arange(len(rank), dtype=np.int32)
+        w.j_order[:j0], w.s_order[:s0] = order[:j0], order[j0:j0 + s0]
+        w.j_order[j0:], w.s_order[s0:] = order[j0 + s0:j0 + s0 + ex.n_joints], order[j0 + s0 + ex.n_joints:]
+        old_body = np.concatenate([np.nonzero(keep)[0], np.full(ex.n_bodies, -1)]).astype(np.int32)
+        old_joint = np.concatenate([np.nonzero(jk)[0], np.full(ex.n_joints, -1)]).astype(np.int32)
+        old_spring = np.concatenate([np.nonzero(sk)[0], np.full(ex.n_springs, -1)]).astype(np.int32)
+        return w, old_body, old_joint, old_spring
+
+    def carry_from(self, old: "World", old_body=None, old_joint=None, old_spring=None) -> "World":
+        """A copy of this (edited) world with the live state of the elements
+        it carries from `old` (the state before the edit): what avbd_repack
+        does on the device, on the host. old_body[i] is the old index of body
+        i or -1 (likewise joints and springs; None carries nothing of that
+        kind). Bodies keep position, orientation and velocities; joints their
+        penalties, multipliers and broken flag; springs penalty, peak strain
+        and torn flag. When the carried bodies keep their old relative order,
+        old's live manifolds between two carried bodies are carried,
+        renumbered (keeping the pair order); otherwise there are none."""
+        w = self.copy()
+        ob = None if old_body is None else np.asarray(old_body, np.int64)
+        if ob is not None:
+            k = ob >= 0
+            for f in ("pos", "quat", "vel", "omega", "prev_vel"):
+                getattr(w, f)[k] = getattr(old, f)[ob[k]]
+        for m, prefix, fields in ((old_joint, "j_", ("penalty_lin", "penalty_ang", "lambda_lin", "lambda_ang",
+                                                     "broken")),
+                                  (old_spring, "s_", ("penalty", "peak_strain", "broken"))):
+            if m is None:
+                continue
+            m = np.asarray(m, np.int64)
+            k = m >= 0
+            for f in fields:
+                getattr(w, prefix + f)[k] = getattr(old, prefix + f)[m[k]]
+        w.m_count = 0
+        if ob is None:
+            return w
+        carried = ob[ob >= 0]
+        if len(carried) == 0 or np.any(np.diff(carried) <= 0):
+            return w
+        new_of = np.full(old.n_bodies, -1, np.int64)
+        new_of[carried] = np.nonzero(ob >= 0)[0]
+        live = np.arange(old.m_count)
+        live = live[(old.m_num_contacts[live] > 0) & (new_of[old.m_body_a[live]] >= 0)
+                    & (new_of[old.m_body_b[live]] >= 0)]
+        w._alloc_manifolds(max(len(live), 1))
+        w.m_count = len(live)
+        for f in ("m_num_contacts", "m_basis", "m_friction", "m_feature", "m_r_a", "m_r_b", "m_c0", "m_penalty",
+                  "m_lambda", "m_stick"):
+            getattr(w, f)[:len(live)] = getattr(old, f)[live]
+        w.m_body_a[:len(live)] = new_of[old.m_body_a[live]]
+        w.m_body_b[:len(live)] = new_of[old.m_body_b[live]]
+        w.m_order[:len(live)] = np.arange(len(live))
+        return w
+
     def manifold_dict(self):
         """Live manifolds keyed by (A, B) -> (num_contacts, features tuple)."""
         out = {}

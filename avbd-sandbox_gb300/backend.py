@@ -65,6 +65,8 @@ def load_library(path: str = LIB_PATH):
     L.avbd_autotune.restype = C.c_int
     L.avbd_set_grab.argtypes = [vp, C.c_int32, vp, vp, C.c_double]
     L.avbd_set_grab.restype = C.c_int
+    L.avbd_repack.argtypes = [vp, vp, vp, vp, vp, vp]
+    L.avbd_repack.restype = C.c_int
     L.avbd_adjoint_forward.argtypes = [vp, vp, C.c_int32, vp, C.c_int32]
     L.avbd_adjoint_read.argtypes = [vp, vp, vp, vp]
     L.avbd_adjoint_backward.argtypes = [vp, vp, vp]
@@ -120,6 +122,27 @@ class GpuBackend:
         self.world = world.copy()
         wc = self.world.c()
         self._check(self.L.avbd_pack(self.h, C.byref(wc)))
+
+    def repack(self, world: abi.World, old_body=None, old_joint=None, old_spring=None) -> int:
+        """avbd_repack: `world` is the edited scene graph; old_body[i] is the
+        index new body i had before (-1: new), likewise for joints and springs
+        (None: none carried). Carried elements keep their live device state;
+        returns the number of warm-start manifolds carried."""
+        maps = []
+        for m, count in ((old_body, world.n_bodies), (old_joint, world.n_joints), (old_spring, world.n_springs)):
+            if m is None:
+                maps.append(None)
+                continue
+            a = np.ascontiguousarray(m, dtype=np.int32)
+            if a.shape != (count,):
+                raise ValueError(f"map of {a.shape} entries for {count} elements")
+            maps.append(a)
+        self.world = world.copy()
+        wc = self.world.c(with_manifolds=False)
+        carried = C.c_int64(0)
+        ptr = [None if m is None else m.ctypes.data_as(C.c_void_p) for m in maps]
+        self._check(self.L.avbd_repack(self.h, C.byref(wc), ptr[0], ptr[1], ptr[2], C.byref(carried)))
+        return int(carried.value)
 
     def step(self, n: int = 1):
         self._check(self.L.avbd_step(self.h, n))

@@ -24,6 +24,7 @@ UNITS = {
     "solver.cu": [],
     "host.cu": [],
     "tangent.cu": ["--fmad=false"],
+    "repack.cu": [],
 }
 
 

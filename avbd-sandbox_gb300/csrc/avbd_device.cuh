@@ -404,6 +404,16 @@ void launch_stats(const World &w, double *out3, cudaStream_t st, int smCount);
 cudaError_t launch_joint_anchor(const World &w, int joint, double x, double y, double z, cudaStream_t st);
 cudaError_t launch_set_grab(const World &w, int body, const double *local, const double *target, double k,
                             cudaStream_t st);
+// Identity-preserving repack (repack.cu): the dynamic state of carried
+// bodies, joints and springs gathered from the old arrays (maps new -> old
+// index, -1 = keep what the pack uploaded), and the old warm-start arena's
+// live manifolds between surviving bodies renumbered into the new one.
+// `flag`/`at` hold oldSlots + 1 ints each; the carried count ends up in
+// ctl->prevCandidates.
+cudaError_t launch_repack_state(const World &oldW, const World &newW, const int *oldBody, const int *oldJoint,
+                                const int *oldSpring, cudaStream_t st);
+cudaError_t launch_repack_manifolds(const Manifolds &oldM, const Manifolds &newM, int oldSlots, const int *newOf,
+                                    int *flag, int *at, Control *ctl, cudaStream_t st);
 // Error text of a context-free ABI call (read back by avbd_last_error(NULL)).
 int set_context_free_error(int code, const char *msg);
 // The differentiable step (tangent.cu).

@@ -1272,6 +1272,111 @@ int avbd_read_state(avbd_ctx *ctx, avbd_world *out) {
   return AVBD_OK;
 }
 
+int avbd_repack(avbd_ctx *ctx, const avbd_world *world, const int32_t *old_body, const int32_t *old_joint,
+                const int32_t *old_spring, int64_t *carried) {
+  if (!ctx || !world) return fail(ctx, AVBD_ERR_ARG, "avbd_repack: NULL argument");
+  if (!ctx->packed) return fail(ctx, AVBD_ERR_STATE, "avbd_repack before avbd_pack");
+  if (world->num_scenes > 1 || ctx->numScenes > 1)
+    return fail(ctx, AVBD_ERR_ARG, "avbd_repack: one scene (batches are packed whole)");
+  int rc = resolve_skips(ctx);
+  if (rc) return rc;
+  CK(cudaStreamSynchronize(ctx->stream));
+  const int on = ctx->n, onj = ctx->nj, ons = ctx->ns;
+  const int n = world->bodies.count, nj = world->joints.count, ns = world->springs.count;
+  // the maps: every old element carried at most once; survivors in their old
+  // relative order keep the warm-start manifolds (their A/B roles and the
+  // arena's key order stay valid), otherwise the contacts start afresh
+  std::vector<int> newOf(std::max(on, 1), -1);
+  bool monotone = true;
+  int last = -1, survivors = 0;
+  for (int i = 0; i < n && old_body; i++) {
+    const int o = old_body[i];
+    if (o < -1 || o >= on) return fail(ctx, AVBD_ERR_ARG, "avbd_repack: old_body[%d] = %d outside -1..%d", i, o, on - 1);
+    if (o < 0) continue;
+    if (newOf[o] >= 0) return fail(ctx, AVBD_ERR_ARG, "avbd_repack: old body %d carried twice", o);
+    newOf[o] = i;
+    monotone = monotone && o > last;
+    last = o;
+    survivors++;
+  }
+  auto check_map = [&](const int32_t *m, int count, int oldCount, const char *what) -> int {
+    if (!m) return AVBD_OK;
+    std::vector<char> seen(std::max(oldCount, 1), 0);
+    for (int k = 0; k < count; k++) {
+      const int o = m[k];
+      if (o < -1 || o >= oldCount)
+        return fail(ctx, AVBD_ERR_ARG, "avbd_repack: old_%s[%d] = %d outside -1..%d", what, k, o, oldCount - 1);
+      if (o >= 0 && seen[o]++) return fail(ctx, AVBD_ERR_ARG, "avbd_repack: old %s %d carried twice", what, o);
+    }
+    return AVBD_OK;
+  };
+  if ((rc = check_map(old_joint, nj, onj, "joint")) || (rc = check_map(old_spring, ns, ons, "spring"))) return rc;
+  Control oc{};
+  CK(cudaMemcpy(&oc, ctx->w.ctl, sizeof(Control), cudaMemcpyDeviceToHost));
+  const int oldSlots = (monotone && survivors > 0) ? oc.prevCandidates : 0;
+
+  // keep the old device arrays alive through the pack: the carried state is
+  // gathered from them on the device, then they are freed
+  const World ow = ctx->w;
+  const Manifolds opm = ctx->curIsA ? ctx->mB : ctx->mA;
+  std::vector<void *> oldAllocs, oldGrowable;
+  oldAllocs.swap(ctx->allocs);
+  oldGrowable.swap(ctx->growable);
+  auto free_old = [&]() {
+    cudaStreamSynchronize(ctx->stream);
+    for (void *p : oldAllocs) cudaFree(p);
+    for (void *p : oldGrowable) cudaFree(p);
+    oldAllocs.clear();
+    oldGrowable.clear();
+  };
+  avbd_world nw = *world;
+  nw.manifolds.count = 0;
+  rc = avbd_pack(ctx, &nw);
+  if (!rc && oldSlots > ctx->candCap)
+    rc = grow_arenas(ctx, (int)std::min<long long>(2LL * oldSlots, 0x3fffffff), ctx->mB, 0);
+  if (rc) {
+    free_old();
+    return rc;
+  }
+  // the maps on the device, then one gather per kind and the arena remap
+  World &w = ctx->w;
+  cudaStream_t st = ctx->stream;
+  int *dMaps = nullptr;
+  const size_t mapInts = (size_t)n + nj + ns + on + 2 * (size_t)oldSlots + 2;
+  if (cudaMalloc(&dMaps, mapInts * sizeof(int)) != cudaSuccess) {
+    free_old();
+    return fail(ctx, AVBD_ERR_CUDA, "avbd_repack: cudaMalloc of the maps failed");
+  }
+  int *dBody = dMaps, *dJoint = dBody + n, *dSpring = dJoint + nj, *dNewOf = dSpring + ns;
+  int *dFlag = dNewOf + on, *dAt = dFlag + oldSlots + 1;
+  std::vector<int> hb(n, -1), hj(nj, -1), hs(ns, -1);
+  if (old_body) std::copy(old_body, old_body + n, hb.begin());
+  if (old_joint) std::copy(old_joint, old_joint + nj, hj.begin());
+  if (old_spring) std::copy(old_spring, old_spring + ns, hs.begin());
+  cudaError_t e = cudaSuccess;
+  if (n) e = cudaMemcpyAsync(dBody, hb.data(), n * sizeof(int), cudaMemcpyHostToDevice, st);
+  if (!e && nj) e = cudaMemcpyAsync(dJoint, hj.data(), nj * sizeof(int), cudaMemcpyHostToDevice, st);
+  if (!e && ns) e = cudaMemcpyAsync(dSpring, hs.data(), ns * sizeof(int), cudaMemcpyHostToDevice, st);
+  if (!e && on) e = cudaMemcpyAsync(dNewOf, newOf.data(), on * sizeof(int), cudaMemcpyHostToDevice, st);
+  if (!e) e = launch_repack_state(ow, w, dBody, dJoint, dSpring, st);
+  int carriedSlots = 0;
+  if (!e && oldSlots > 0) {
+    Manifolds npm = ctx->curIsA ? ctx->mB : ctx->mA;  // the new context's warm-start arena
+    e = launch_repack_manifolds(opm, npm, oldSlots, dNewOf, dFlag, dAt, w.ctl, st);
+    int tot[2] = {0, 0};
+    if (!e) e = cudaMemcpyAsync(tot, dAt + oldSlots - 1, sizeof(int), cudaMemcpyDeviceToHost, st);
+    if (!e) e = cudaMemcpyAsync(tot + 1, dFlag + oldSlots - 1, sizeof(int), cudaMemcpyDeviceToHost, st);
+    if (!e) e = cudaStreamSynchronize(st);
+    carriedSlots = tot[0] + tot[1];
+  }
+  if (!e) e = cudaStreamSynchronize(st);
+  cudaFree(dMaps);
+  free_old();
+  if (e != cudaSuccess) return fail(ctx, AVBD_ERR_CUDA, "avbd_repack: %s", cudaGetErrorString(e));
+  if (carried) *carried = carriedSlots;
+  return AVBD_OK;
+}
+
 int avbd_write_state(avbd_ctx *ctx, const avbd_world *world) {
   if (!ctx || !world) return AVBD_ERR_ARG;
   if (!ctx->packed) return fail(ctx, AVBD_ERR_STATE, "avbd_write_state before avbd_pack");

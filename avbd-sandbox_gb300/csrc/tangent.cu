@@ -141,8 +141,14 @@ __device__ __forceinline__ void v3_sub(R *o, const R *a, const R *b) {
 __device__ __forceinline__ void v3_add(R *o, const R *a, const R *b) {
   o[0] = a[0] + b[0]; o[1] = a[1] + b[1]; o[2] = a[2] + b[2];
 }
-__device__ __forceinline__ void v3_add_scaled(R *o, const R *a, R s) {
+// o += a * s; `o` an R array or a recording row (RecRow) of a body's system
+template <class O>
+__device__ __forceinline__ void v3_add_scaled(O &&o, const R *a, R s) {
   o[0] += a[0] * s; o[1] += a[1] * s; o[2] += a[2] * s;
+}
+template <class O>
+__device__ __forceinline__ void v3_add_into(O &&o, const R *a) {
+  o[0] += a[0]; o[1] += a[1]; o[2] += a[2];
 }
 __device__ __forceinline__ R v3_dot(const R *a, const R *b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
 __device__ __forceinline__ R v3_len_sq(const R *a) { return a[0] * a[0] + a[1] * a[1] + a[2] * a[2]; }
@@ -182,7 +188,8 @@ __device__ __forceinline__ void m3_skew(R *o, const R *r) {
   o[3] = r[2]; o[4] = 0.0; o[5] = -r[0];
   o[6] = -r[1]; o[7] = r[0]; o[8] = 0.0;
 }
-__device__ __forceinline__ void m3_add_into(R *o, const R *a) {
+template <class O>
+__device__ __forceinline__ void m3_add_into(O &&o, const R *a) {
   for (int i = 0; i < 9; i++) o[i] += a[i];
 }
 // Eq. 20 (maths.js:541-555)
@@ -280,9 +287,38 @@ __device__ void solve6(const R *aLin, const R *aAng, const R *aCross, const R *b
   xLin[0] = z1 - L21 * xLin[1] - L31 * xLin[2] - L41 * xAng[0] - L51 * xAng[1] - L61 * xAng[2];
 }
 
-// A body's 6x6 system, accumulated by its forces.
+// A body's 6x6 system, accumulated by its forces: 33 entries in this order.
 struct Sys6 {
   R lin[9], ang[9], cross[9], bl[3], ba[3];
+};
+constexpr int kSysEntries = 33;
+static_assert(sizeof(Sys6) == kSysEntries * sizeof(R), "Sys6 is 33 contiguous entries");
+
+// The recording form of a body's system: one constraint's contribution as
+// the sequence of addends it adds to each entry (at most kMaxAdd: a joint's
+// angular diagonal gets its rows, its geometric stiffness and its angular
+// rows), so that the addends of many constraints, computed by different
+// lanes, are summed afterwards in the f64 engine's order.
+constexpr int kMaxAdd = 3;
+struct RecElem {
+  R *slot;
+  unsigned char *cnt;
+  __device__ void operator+=(const R &x) const {
+    const int k = *cnt;
+    if (k < kMaxAdd) slot[k] = x;
+    *cnt = (unsigned char)(k + 1);  // > kMaxAdd is reported by the replay
+  }
+};
+struct RecRow {
+  R *slot;
+  unsigned char *cnt;
+  __device__ RecElem operator[](int e) const { return RecElem{slot + e * kMaxAdd, cnt + e}; }
+};
+struct RecSys6 {
+  RecRow lin, ang, cross, bl, ba;
+  __device__ RecSys6(R *slots, unsigned char *cnt)
+      : lin{slots, cnt}, ang{slots + 9 * kMaxAdd, cnt + 9}, cross{slots + 18 * kMaxAdd, cnt + 18},
+        bl{slots + 27 * kMaxAdd, cnt + 27}, ba{slots + 30 * kMaxAdd, cnt + 30} {}
 };
 
 __device__ __forceinline__ bool is_dynamic(const TWorld &w, int i) { return i >= 0 && w.bs[i].mass > 0; }
@@ -717,7 +753,8 @@ __device__ ContactEvalT contact_eval(const TWorld &w, const TManifold &m, int i,
 }
 
 // H += J_lin^T K J_lin etc. of one 3-row block with diagonal K.
-__device__ void stamp_rows(Sys6 &s, const R *jLin, const R *jAng, const R *Kd, const R *F) {
+template <class S>
+__device__ void stamp_rows(S &s, const R *jLin, const R *jAng, const R *Kd, const R *F) {
   R jLinT[9], jAngT[9], jAngTk[9], m0[9], acc[3];
   m3_transpose(jLinT, jLin);
   m3_transpose(jAngT, jAng);
@@ -733,20 +770,19 @@ __device__ void stamp_rows(Sys6 &s, const R *jLin, const R *jAng, const R *Kd, c
   m3_mul(m0, jAngTk, jLin);
   m3_add_into(s.cross, m0);
   m3_mul_vec(acc, jLinT, F);
-  v3_add(s.bl, s.bl, acc);
+  v3_add_into(s.bl, acc);
   m3_mul_vec(acc, jAngT, F);
-  v3_add(s.ba, s.ba, acc);
+  v3_add_into(s.ba, acc);
 }
 
-// manifold.js:411-445
-__device__ void manifold_primal(const TWorld &w, const TManifold &m, int side, R alpha, Sys6 &s) {
+// manifold.js:411-445, contact i of the manifold
+template <class S>
+__device__ void contact_primal(const TWorld &w, const TManifold &m, int i, int side, R alpha, S &s) {
   R jBLin[9];
   for (int k = 0; k < 9; k++) jBLin[k] = -m.basis[k];
-  for (int i = 0; i < m.count; i++) {
-    R jAAng[9], jBAng[9];
-    const ContactEvalT e = contact_eval(w, m, i, alpha, jAAng, jBAng);
-    stamp_rows(s, side ? jBLin : m.basis, side ? jBAng : jAAng, m.c[i].pen, e.F);
-  }
+  R jAAng[9], jBAng[9];
+  const ContactEvalT e = contact_eval(w, m, i, alpha, jAAng, jBAng);
+  stamp_rows(s, side ? jBLin : m.basis, side ? jBAng : jAAng, m.c[i].pen, e.F);
 }
 
 // joint.js:214-221: the geometric stiffness of a ball socket, lumped
@@ -768,7 +804,8 @@ __device__ void ball_socket_geometric(R *G, const R *r, const R *F) {
 }
 
 // joint.js:162-253
-__device__ void joint_primal(const TWorld &w, const TJoint &j, int side, R alpha, Sys6 &s) {
+template <class S>
+__device__ void joint_primal(const TWorld &w, const TJoint &j, int side, R alpha, S &s) {
   R C[3], F[3];
   if (v3_len_sq(j.penLin) > 0.0) {
     joint_eval_lin(w, j, C);
@@ -808,7 +845,8 @@ __device__ void joint_primal(const TWorld &w, const TJoint &j, int side, R alpha
 }
 
 // spring.js:509-616
-__device__ void spring_primal(const TWorld &w, const TSpring &sp, int side, Sys6 &s, const TParams &P) {
+template <class Sink>
+__device__ void spring_primal(const TWorld &w, const TSpring &sp, int side, Sink &s, const TParams &P) {
   if (sp.broken) return;
   R d[3], n[3];
   const R Cv = spring_eval(w, sp, d, n);
@@ -865,46 +903,118 @@ __device__ void spring_primal(const TWorld &w, const TSpring &sp, int side, Sys6
   }
 }
 
-// One body's update (solver.js:425-457).
-__device__ void body_primal(const TWorld &w, int i, R alpha) {
+// One body's update (solver.js:425-457) by one warp. The body's constraint
+// rows - each contact of each manifold, each joint, each spring, newest force
+// first - go to the lanes 32 at a time; every lane records the addends its
+// row makes to each of the 33 system entries (RecSys6), and lane e then adds
+// the recorded addends of entry e row after row: every entry is summed in the
+// f64 engine's order, so the values stay the serial update's.
+constexpr int kWarp = 32;
+struct BodySmem {
+  R rec[kWarp][kSysEntries * kMaxAdd];  // lane's row: its addends per entry
+  unsigned char cnt[kWarp][kSysEntries + 3];
+  R acc[kSysEntries];                   // the entries, summed so far
+  uint32_t items[kWarp];                // (force entry << 3) | contact
+  int nItems, cursorE, cursorC;
+};
+
+__device__ void body_update_warp(const TWorld &w, int i, R alpha, BodySmem &sm) {
   const TParams &P = w.P;
-  TBody &b = w.b[i];
-  const TBodyStatic &st = w.bs[i];
-  const double dt2 = P.dt * P.dt;
-  Sys6 s;
-  R MAng[9], tmp[3], dq[3];
-  m3_diag(s.lin, R(st.mass / dt2), R(st.mass / dt2), R(st.mass / dt2));
-  world_moment(MAng, st, b.q, P.rotatedInertia != 0);
-  for (int k = 0; k < 9; k++) s.ang[k] = MAng[k] / dt2;
-  m3_zero(s.cross);
-  v3_sub(tmp, b.p, b.yl);
-  m3_mul_vec(s.bl, s.lin, tmp);
-  q_subtract(dq, b.q, b.yq);
-  m3_mul_vec(s.ba, s.ang, dq);
-  for (int e = w.fStart[i + 1] - 1; e >= w.fStart[i]; e--) {  // the body's forces, newest first
-    const uint32_t ref = w.fRef[e];
-    const uint32_t type = ref >> 30, idx = (ref >> 1) & 0x1fffffffu, side = ref & 1u;
-    if (type == 0) manifold_primal(w, w.cur[idx], (int)side, alpha, s);
-    else if (type == kRefJoint) joint_primal(w, w.j[idx], (int)side, alpha, s);
-    else spring_primal(w, w.s[idx], (int)side, s, P);
+  const int lane = threadIdx.x;
+  if (lane == 0) {
+    TBody &b = w.b[i];
+    const TBodyStatic &st = w.bs[i];
+    const double dt2 = P.dt * P.dt;
+    Sys6 s;
+    R MAng[9], tmp[3], dq[3];
+    m3_diag(s.lin, R(st.mass / dt2), R(st.mass / dt2), R(st.mass / dt2));
+    world_moment(MAng, st, b.q, P.rotatedInertia != 0);
+    for (int k = 0; k < 9; k++) s.ang[k] = MAng[k] / dt2;
+    m3_zero(s.cross);
+    v3_sub(tmp, b.p, b.yl);
+    m3_mul_vec(s.bl, s.lin, tmp);
+    q_subtract(dq, b.q, b.yq);
+    m3_mul_vec(s.ba, s.ang, dq);
+    const R *e = &s.lin[0];
+    for (int k = 0; k < kSysEntries; k++) sm.acc[k] = e[k];
+    sm.cursorE = w.fStart[i + 1] - 1;  // the body's forces, newest first
+    sm.cursorC = 0;
   }
-  R xl[3], xa[3], nl[3], na[3];
-  for (int k = 0; k < 3; k++) {
-    nl[k] = -s.bl[k];
-    na[k] = -s.ba[k];
+  __syncwarp();
+  for (;;) {
+    if (lane == 0) {  // the next (up to) 32 rows
+      int n = 0, e = sm.cursorE, c = sm.cursorC;
+      const int e0 = w.fStart[i];
+      while (n < kWarp && e >= e0) {
+        const uint32_t ref = w.fRef[e];
+        if ((ref >> 30) == 0) {
+          if (c < w.cur[(ref >> 1) & 0x1fffffffu].count) {
+            sm.items[n++] = ((uint32_t)e << 3) | (uint32_t)c;
+            c++;
+            continue;
+          }
+          e--;
+          c = 0;
+          continue;
+        }
+        sm.items[n++] = (uint32_t)e << 3;
+        e--;
+        c = 0;
+      }
+      sm.nItems = n;
+      sm.cursorE = e;
+      sm.cursorC = c;
+    }
+    __syncwarp();
+    const int n = sm.nItems;
+    if (n == 0) break;
+    if (lane < n) {
+      for (int k = 0; k < kSysEntries; k++) sm.cnt[lane][k] = 0;
+      RecSys6 rs(sm.rec[lane], sm.cnt[lane]);
+      const uint32_t item = sm.items[lane];
+      const uint32_t ref = w.fRef[item >> 3];
+      const uint32_t type = ref >> 30, idx = (ref >> 1) & 0x1fffffffu, side = ref & 1u;
+      if (type == 0) contact_primal(w, w.cur[idx], (int)(item & 7u), (int)side, alpha, rs);
+      else if (type == kRefJoint) joint_primal(w, w.j[idx], (int)side, alpha, rs);
+      else spring_primal(w, w.s[idx], (int)side, rs, P);
+    }
+    __syncwarp();
+    for (int entry = lane; entry < kSysEntries; entry += kWarp) {
+      R a = sm.acc[entry];
+      for (int it = 0; it < n; it++) {
+        const int k = sm.cnt[it][entry];
+        if (k > kMaxAdd) w.ctl[7] = 1;  // more addends than recorded: the result is not the serial sum
+        for (int q = 0; q < k && q < kMaxAdd; q++) a += sm.rec[it][entry * kMaxAdd + q];
+      }
+      sm.acc[entry] = a;
+    }
+    __syncwarp();
   }
-  solve6(s.lin, s.ang, s.cross, nl, na, xl, xa);
-  v3_add(b.p, b.p, xl);
-  R q1[4];
-  q_integrate(q1, b.q, xa);
-  for (int k = 0; k < 4; k++) b.q[k] = q1[k];
+  if (lane == 0) {
+    TBody &b = w.b[i];
+    Sys6 s;
+    R *e = &s.lin[0];
+    for (int k = 0; k < kSysEntries; k++) e[k] = sm.acc[k];
+    R xl[3], xa[3], nl[3], na[3];
+    for (int k = 0; k < 3; k++) {
+      nl[k] = -s.bl[k];
+      na[k] = -s.ba[k];
+    }
+    solve6(s.lin, s.ang, s.cross, nl, na, xl, xa);
+    v3_add(b.p, b.p, xl);
+    R q1[4];
+    q_integrate(q1, b.q, xa);
+    for (int k = 0; k < 4; k++) b.q[k] = q1[k];
+  }
+  __syncwarp();
 }
 
-// manifold.js:447-491
-__device__ void manifold_dual(const TWorld &w, TManifold &m, R alpha) {
+// manifold.js:447-491, contact i of the manifold (the contacts' dual updates
+// are independent of one another)
+__device__ void contact_dual(const TWorld &w, TManifold &m, int i, R alpha) {
   const TParams &P = w.P;
   const bool sphere = w.bs[m.a].shape == AVBD_SHAPE_SPHERE || w.bs[m.b].shape == AVBD_SHAPE_SPHERE;
-  for (int i = 0; i < m.count; i++) {
+  {
     R jAAng[9], jBAng[9];
     const ContactEvalT e = contact_eval(w, m, i, alpha, jAAng, jBAng);
     TContact &c = m.c[i];
@@ -959,31 +1069,75 @@ __device__ void spring_dual(const TWorld &w, TSpring &s) {
   s.penalty = js_min(s.penalty + fabs(Cv) * w.P.betaLin, js_min(s.stiffness, w.P.penaltyMax));
 }
 
-// The iterations of one step in one block: per iteration the colour phases
-// (bodies of one colour are independent), then every force's dual update,
-// and on the last iteration the BDF1 velocity (solver.js:476-488).
-__global__ void __launch_bounds__(kBlock) iterate_kernel(TWorld w) {
+// Bounded grid barrier of the cooperative iterate kernel (ctl[4] arrivals,
+// ctl[5] generation, ctl[6] set when a wait gave up: the kernel returns and
+// the host reports AVBD_ERR_TIMEOUT).
+constexpr long long kGridWaitLimit = 1ll << 25;
+__device__ bool tg_grid_sync(const TWorld &w) {
+  __shared__ int ok;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    ok = 1;
+    volatile int *gen = (volatile int *)&w.ctl[5];
+    const int g = *gen;
+    __threadfence();
+    const unsigned arrived = atomicAdd((unsigned *)&w.ctl[4], 1u) + 1u;
+    if (arrived == gridDim.x) {
+      w.ctl[4] = 0;
+      __threadfence();
+      atomicAdd(&w.ctl[5], 1);
+    } else {
+      long long spins = 0;
+      while (*gen == g) {
+        if (++spins > kGridWaitLimit || *((volatile int *)&w.ctl[6])) {
+          atomicOr(&w.ctl[6], 1);
+          break;
+        }
+        __nanosleep(64);
+      }
+    }
+    __threadfence();
+    if (*((volatile int *)&w.ctl[6])) ok = 0;
+  }
+  __syncthreads();
+  return ok != 0;
+}
+
+// The iterations of one step (cooperative: one warp per block, blocks spread
+// over the SMs, FP64 being the bound): per iteration the colour phases (a
+// warp per body; bodies of one colour are independent), then every force's
+// dual update (a thread per contact, joint, spring), and on the last
+// iteration the BDF1 velocity (solver.js:476-488); a grid barrier between
+// phases.
+__global__ void __launch_bounds__(kWarp) iterate_kernel(TWorld w) {
   if (w.ctl[2]) return;
+  extern __shared__ __align__(16) unsigned char smemRaw[];
+  BodySmem &sm = *reinterpret_cast<BodySmem *>(smemRaw);
   const TParams &P = w.P;
   const int numColors = w.ctl[3], total = w.ctl[0];
   const int total_it = P.iterations + (P.postStabilize ? 1 : 0);
-  const int t = threadIdx.x;
+  // thread index spread so that consecutive items land on different SMs
+  const int g = blockIdx.x + gridDim.x * threadIdx.x, gs = gridDim.x * blockDim.x;
   for (int it = 0; it < total_it; it++) {
     const R alpha = P.postStabilize ? (it < P.iterations ? 1.0 : 0.0) : P.alpha;
     for (int c = 0; c < numColors; c++) {
-      for (int k = w.colorStart[c] + t; k < w.colorStart[c + 1]; k += blockDim.x) body_primal(w, w.order[k], alpha);
-      __syncthreads();
+      const int c0 = w.colorStart[c], cn = w.colorStart[c + 1] - c0;
+      for (int k = blockIdx.x; k < cn; k += gridDim.x) body_update_warp(w, w.order[c0 + k], alpha, sm);
+      if (!tg_grid_sync(w)) return;
     }
     if (it < P.iterations) {
-      for (int k = t; k < total; k += blockDim.x)
-        if (w.cur[k].count > 0) manifold_dual(w, w.cur[k], alpha);
-      for (int k = t; k < w.nj; k += blockDim.x)
+      for (int k = g; k < total * kMaxContacts; k += gs) {
+        TManifold &m = w.cur[k / kMaxContacts];
+        const int i = k % kMaxContacts;
+        if (i < m.count) contact_dual(w, m, i, alpha);
+      }
+      for (int k = g; k < w.nj; k += gs)
         if (!w.j[k].removed) joint_dual(w, w.j[k], alpha);
-      for (int k = t; k < w.ns; k += blockDim.x) spring_dual(w, w.s[k]);
-      __syncthreads();
+      for (int k = g; k < w.ns; k += gs) spring_dual(w, w.s[k]);
+      if (!tg_grid_sync(w)) return;
     }
     if (it == P.iterations - 1) {
-      for (int i = t; i < w.n; i += blockDim.x) {
+      for (int i = g; i < w.n; i += gs) {
         TBody &b = w.b[i];
         for (int k = 0; k < 3; k++) b.pv[k] = b.v[k];
         if (w.bs[i].mass > 0) {
@@ -993,7 +1147,7 @@ __global__ void __launch_bounds__(kBlock) iterate_kernel(TWorld w) {
           for (int k = 0; k < 3; k++) b.w[k] = dq[k] / P.dt;
         }
       }
-      __syncthreads();
+      if (!tg_grid_sync(w)) return;
     }
   }
 }
@@ -1060,6 +1214,7 @@ struct TangentCtx {
   tg::TWorld w{};
   std::vector<void *> allocs;
   int smCount = 0;
+  int iterGrid = 0;  // blocks of the cooperative iterate kernel (one warp each)
   ~TangentCtx() {
     for (void *p : allocs) cudaFree(p);
   }
@@ -1227,7 +1382,7 @@ int tangent_pack(TangentCtx **out, const avbd_world *world, const avbd_params &P
   if ((e = t->alloc(&w.b, n)) || (e = t->alloc(&w.bs, n)) || (e = t->alloc(&cRefD, cRef.size())) ||
       (e = t->alloc(&w.j, nj)) || (e = t->alloc(&w.s, ns)) || (e = t->alloc(&w.pairCount, n + 1)) ||
       (e = t->alloc(&w.pairStart, n + 1)) || (e = t->alloc(&w.key, w.mcap)) || (e = t->alloc(&w.cur, w.mcap)) ||
-      (e = t->alloc(&w.prev, w.mcap)) || (e = t->alloc(&w.prevKey, w.mcap)) || (e = t->alloc(&w.ctl, 4)) ||
+      (e = t->alloc(&w.prev, w.mcap)) || (e = t->alloc(&w.prevKey, w.mcap)) || (e = t->alloc(&w.ctl, 8)) ||
       (e = t->alloc(&w.fStart, n + 1)) || (e = t->alloc(&w.fCount, n + 1)) || (e = t->alloc(&w.fRef, w.fcap)) ||
       (e = t->alloc(&w.color, n)) || (e = t->alloc(&w.order, n)) || (e = t->alloc(&w.colorStart, kMaxColors + 1)) ||
       (e = t->alloc(&prioD, n))) {
@@ -1243,7 +1398,21 @@ int tangent_pack(TangentCtx **out, const avbd_world *world, const avbd_params &P
   if (nj) cudaMemcpyAsync(w.j, hj.data(), sizeof(TJoint) * nj, cudaMemcpyHostToDevice, st);
   if (ns) cudaMemcpyAsync(w.s, hsp.data(), sizeof(TSpring) * ns, cudaMemcpyHostToDevice, st);
   cudaMemcpyAsync(prioD, prio.data(), sizeof(uint32_t) * n, cudaMemcpyHostToDevice, st);
-  cudaDeviceGetAttribute(&t->smCount, cudaDevAttrMultiProcessorCount, 0);
+  int dev = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&t->smCount, cudaDevAttrMultiProcessorCount, dev);
+  // the iterate kernel: one warp and one BodySmem per block, all blocks resident
+  int perSm = 0;
+  e = cudaFuncSetAttribute(iterate_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(BodySmem));
+  if (e == cudaSuccess)
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, iterate_kernel, kWarp, sizeof(BodySmem));
+  if (e != cudaSuccess || perSm < 1) {
+    delete t;
+    snprintf(msg, msgLen, "avbd_adjoint_forward: the iterate kernel cannot be made resident (%s)",
+             e != cudaSuccess ? cudaGetErrorString(e) : "no block fits an SM");
+    return AVBD_ERR_CUDA;
+  }
+  t->iterGrid = std::max(1, std::min(t->smCount, std::max(n, 1)));
   e = cudaStreamSynchronize(st);
   if (e != cudaSuccess) {
     delete t;
@@ -1269,7 +1438,15 @@ int tangent_step(TangentCtx *t, int steps, void *temp, size_t tempBytes, char *m
     forces_init_kernel<<<blocks, 128, 0, st>>>(w);
     bodies_init_kernel<<<blocks, 128, 0, st>>>(w);
     adjacency_coloring_kernel<<<1, kBlock, 0, st>>>(w);
-    iterate_kernel<<<1, kBlock, 0, st>>>(w);
+    {
+      void *args[] = {(void *)&w};
+      const cudaError_t le = cudaLaunchCooperativeKernel((const void *)iterate_kernel, dim3(t->iterGrid), dim3(kWarp),
+                                                         args, sizeof(BodySmem), st);
+      if (le != cudaSuccess) {
+        snprintf(msg, msgLen, "avbd_adjoint_forward: cooperative launch: %s", cudaGetErrorString(le));
+        return AVBD_ERR_CUDA;
+      }
+    }
     commit_kernel<<<1, kBlock, 0, st>>>(w);
   }
   cudaError_t e = cudaStreamSynchronize(st);
@@ -1278,8 +1455,17 @@ int tangent_step(TangentCtx *t, int steps, void *temp, size_t tempBytes, char *m
     snprintf(msg, msgLen, "avbd_adjoint_forward: %s", cudaGetErrorString(e));
     return AVBD_ERR_CUDA;
   }
-  int ctl[4];
+  int ctl[8];
   cudaMemcpy(ctl, w.ctl, sizeof(ctl), cudaMemcpyDeviceToHost);
+  if (ctl[6]) {
+    snprintf(msg, msgLen, "avbd_adjoint_forward: a grid barrier of the iterations gave up");
+    return AVBD_ERR_TIMEOUT;
+  }
+  if (ctl[7]) {
+    snprintf(msg, msgLen, "avbd_adjoint_forward: a constraint row made more than %d addends to one system entry",
+             kMaxAdd);
+    return AVBD_ERR_STATE;
+  }
   if (ctl[2]) {
     snprintf(msg, msgLen, "avbd_adjoint_forward: candidate pairs or force lists exceed the differentiable step's "
                           "arenas (%d pair slots)", w.mcap);

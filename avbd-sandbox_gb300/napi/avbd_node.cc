@@ -301,6 +301,34 @@ napi_value Pack(napi_env env, napi_callback_info info) {
   return rc ? throw_status(env, a.h->ctx, rc) : undefined(env);
 }
 
+// repack(handle, world, oldBody, oldJoint, oldSpring) -> carried manifolds:
+// the identity-preserving repack; each map an Int32Array (new -> old index,
+// -1 new) or undefined
+napi_value Repack(napi_env env, napi_callback_info info) {
+  Args a;
+  if (!args(env, info, &a)) return nullptr;
+  avbd_world w;
+  if (a.argc < 2 || !bind_world(env, a.argv[1], &w)) return nullptr;
+  napi_value holder;
+  napi_create_object(env, &holder);
+  const char *names[3] = {"oldBody", "oldJoint", "oldSpring"};
+  const size_t counts[3] = {(size_t)w.bodies.count, (size_t)w.joints.count, (size_t)w.springs.count};
+  int32_t *maps[3] = {nullptr, nullptr, nullptr};
+  for (int k = 0; k < 3; k++) {
+    napi_valuetype t = napi_undefined;
+    if ((size_t)a.argc > (size_t)(2 + k)) napi_typeof(env, a.argv[2 + k], &t);
+    if (t == napi_undefined || t == napi_null) continue;
+    napi_set_named_property(env, holder, names[k], a.argv[2 + k]);
+    if (!get_array(env, holder, names[k], napi_int32_array, counts[k], &maps[k])) return nullptr;
+  }
+  int64_t carried = 0;
+  const int rc = avbd_repack(a.h->ctx, &w, maps[0], maps[1], maps[2], &carried);
+  if (rc) return throw_status(env, a.h->ctx, rc);
+  napi_value out;
+  napi_create_double(env, (double)carried, &out);
+  return out;
+}
+
 // writeState(handle, world)
 napi_value WriteState(napi_env env, napi_callback_info info) {
   Args a;
@@ -553,6 +581,7 @@ napi_value Init(napi_env env, napi_value exports) {
   } const table[] = {{"create", Create},
                      {"destroy", Destroy},
                      {"pack", Pack},
+                     {"repack", Repack},
                      {"writeState", WriteState},
                      {"readState", ReadState},
                      {"step", Step},

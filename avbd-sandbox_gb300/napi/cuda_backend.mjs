@@ -171,8 +171,23 @@ export class CudaBackend {
       this.paramsKey = key;
       if (this._profiling) addon.setProfiling(this.handle, true);
     }
+    const prev = this.packed && key === this.paramsKeyPacked ? this.packed : null;
     this.packed = toSoA(solver);
-    addon.pack(this.handle, this.packed.world);
+    if (prev) {
+      // a topology edit: the live device state follows each Rigid, Joint and
+      // Spring object to its new index (backend.js:662-1301, identity runs
+      // :107-145), the warm-start contacts too when survivors keep their order
+      const map = (items, index) => Int32Array.from(items, (x) => (index.has(x) ? index.get(x) : -1));
+      const P = this.packed;
+      const bodies = [...P.bodyIndex.keys()];
+      const joints = [...P.jointIndex.keys()];
+      const springs = [...P.springIndex.keys()];
+      this.lastCarriedManifolds = addon.repack(this.handle, P.world, map(bodies, prev.bodyIndex),
+        map(joints, prev.jointIndex), map(springs, prev.springIndex));
+    } else {
+      addon.pack(this.handle, this.packed.world);
+    }
+    this.paramsKeyPacked = key;
     if (this.overrideColoring) addon.setColoring(this.handle, this.overrideColoring.colorOf);
     this.topologyDirty = false;
   }

@@ -298,6 +298,26 @@ int avbd_read_state(avbd_ctx *ctx, avbd_world *out);
    an already-packed world with the same topology. */
 int avbd_write_state(avbd_ctx *ctx, const avbd_world *world);
 
+/*
+ * Replaces the identity-preserving repack of `pack(solver)` after a topology
+ * edit (src/physics/gpu/backend.js:662-1301; identity runs :107-145): spawn,
+ * erase, joints and springs added or removed. `world` is the new scene graph
+ * (one scene); old_body[i] is the index body i had in the packed world, or -1
+ * for a new body (likewise old_joint, old_spring; a NULL map means nothing of
+ * that kind is carried). Carried elements keep their live device state -
+ * bodies: position, orientation, velocities; joints: penalties, multipliers,
+ * broken; springs: penalty, peak strain, torn - gathered on the device, with
+ * no readback; everything else comes from `world` as in avbd_pack. When the
+ * carried bodies keep their old relative order (append, erase, order-
+ * preserving compaction), the warm-start contacts between two carried bodies
+ * survive, renumbered; otherwise the contacts start afresh (the reference
+ * starts a fresh generation then). `carried` (optional) returns the number of
+ * warm-start manifolds carried. The grab and an uploaded colouring are
+ * released, as by avbd_pack. Synchronous.
+ */
+int avbd_repack(avbd_ctx *ctx, const avbd_world *world, const int32_t *old_body, const int32_t *old_joint,
+                const int32_t *old_spring, int64_t *carried);
+
 /* Replaces `readColoring()` (src/physics/gpu/backend.js:2053): colour of every
    body in the last step (-1 for static bodies) and the number of colours. */
 int avbd_read_coloring(avbd_ctx *ctx, int32_t *color_of, int32_t *num_colors);
