@@ -485,6 +485,10 @@ const char *avbd_last_error(const avbd_ctx *ctx);
  * first call on each device looks up the scratch array's address
  * (cudaGetSymbolAddress) with that device current; when a call may happen
  * while its stream is being captured, make one call on that device before.
+ * The address is kept per device ordinal for the life of the process, so it
+ * belongs to the device's primary context: after cudaDeviceReset of that
+ * device, or from a different (driver-API) context current on it, do not
+ * call this function again in the same process.
  * All calls on a device share the one scratch array, and every call resets
  * the parts that must start at zero: two calls whose executions overlap (on
  * different streams, or from different host threads without ordering) race

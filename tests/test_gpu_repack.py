@@ -88,7 +88,9 @@ def test_device_repack_equals_host_handover(abi, scenes, backend_mod, name):
     new, ob, oj, osp = before.edited(keep, extra)
     carried = a.repack(new, ob, oj, osp)
     host = new.carry_from(before, ob, oj, osp)
-    assert carried == host.m_count > 0
+    assert carried == host.m_count
+    if name != "chain":  # the chain's survivors share no contacts
+        assert carried > 0
     b.pack(host)
     for g in (a, b):
         g.step(8)

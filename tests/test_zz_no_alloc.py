@@ -78,6 +78,36 @@ def test_static_pairs_reports_short_capacity(abi, scenes, backend_mod):
     assert int(count.item()) == len(expect) > 8
 
 
+def test_static_pairs_at_the_documented_maximum(abi, scenes, backend_mod):
+    """Exactly AVBD_STATIC_PAIRS_MAX_BODIES bodies fit the static scratch
+    array: a sparse random cloud of that many boxes gives the pairs of a
+    context's first step on the same positions."""
+    torch = pytest.importorskip("torch")
+    n = backend_mod.STATIC_PAIRS_MAX_BODIES
+    rng = np.random.default_rng(7)
+    s = scenes.Scene("cloud")
+    side = int(np.ceil(n ** (1 / 3)))
+    for k in range(n):
+        x, y, z = k % side, (k // side) % side, k // (side * side)
+        s.box((0.5, 0.5, 0.5), 100.0, 0.5, (1.2 * x + rng.uniform(-0.4, 0.4), 1.2 * y + rng.uniform(-0.4, 0.4),
+                                            1.2 * z + rng.uniform(-0.4, 0.4)))
+    s.params = dict(gravity=0.0)
+    w = s.world()
+    expect = step_pairs(abi, backend_mod, s)
+    dev = torch.device("cuda", torch.cuda.current_device())
+    pos = torch.tensor(np.ascontiguousarray(w.pos), dtype=torch.float64, device=dev)
+    rad = torch.tensor(np.ascontiguousarray(w.radius), dtype=torch.float64, device=dev)
+    cap = len(expect) + 64
+    keys = torch.full((cap,), -1, dtype=torch.int64, device=dev)
+    count = torch.zeros(1, dtype=torch.int32, device=dev)
+    cell = 2.0 * float(np.max(w.radius)) * (1 + 1e-6) + 1e-9
+    backend_mod.overlap_pairs_static(n, pos.data_ptr(), rad.data_ptr(), 0, cell, keys.data_ptr(), cap,
+                                     count.data_ptr(), torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    got = keys[:int(count.item())].cpu().numpy().view(np.uint64)
+    assert len(expect) > 0 and np.array_equal(got, expect)
+
+
 def test_static_pairs_rejects_too_many_bodies(backend_mod):
     with pytest.raises(backend_mod.AvbdError) as e:
         backend_mod.overlap_pairs_static(backend_mod.STATIC_PAIRS_MAX_BODIES + 1, 1, 1, 0, 1.0, 1, 1, 1, 0)
