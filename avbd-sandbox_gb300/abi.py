@@ -26,6 +26,8 @@ SHAPE_SPHERE = 1
 ORDER_REFERENCE = 0
 ORDER_EXPLICIT = 1
 ORDER_PRIORITY = 2
+CONTACT_CPU = 0
+CONTACT_MATERIALS = 1
 
 MAX_CONTACTS = 8
 MAX_COLORS = 1024
@@ -52,6 +54,8 @@ class Params(C.Structure):
         ("lanes_per_body", C.c_int32), ("blocks_per_sm", C.c_int32),
         ("schedule", C.c_int32), ("grid_factor", C.c_int32),
         ("neighbor_wait_limit", C.c_int32), ("tail_div", C.c_int32), ("graph", C.c_int32),
+        ("contact_model", C.c_int32), ("contact_offset", C.c_double), ("rest_offset", C.c_double),
+        ("restitution_threshold", C.c_double), ("contact_persistence", C.c_double),
     ]
 
 
@@ -79,6 +83,11 @@ def default_params(**overrides) -> Params:
     p.body_order = ORDER_REFERENCE
     p.fp64_ratio_threshold = 1e5
     p.schedule = 0
+    p.contact_model = CONTACT_CPU
+    p.contact_offset = 0.005
+    p.rest_offset = -0.005
+    p.restitution_threshold = 1.0
+    p.contact_persistence = 0.002
     for k, v in overrides.items():
         if not hasattr(p, k):
             raise AttributeError(k)
@@ -89,7 +98,8 @@ def default_params(**overrides) -> Params:
 class BodySoA(C.Structure):
     _fields_ = [("count", C.c_int32), ("shape", _i), ("size", _d), ("mass", _d), ("moment", _d),
                 ("radius", _d), ("friction", _d), ("pos", _d), ("quat", _d), ("vel", _d),
-                ("omega", _d), ("prev_vel", _d)]
+                ("omega", _d), ("prev_vel", _d), ("static_friction", _d), ("dynamic_friction", _d),
+                ("restitution", _d), ("contact_offset", _d), ("rest_offset", _d)]
 
 
 class JointSoA(C.Structure):
@@ -109,7 +119,7 @@ class ManifoldSoA(C.Structure):
     _fields_ = [("count", C.c_int32), ("capacity", C.c_int32), ("body_a", _i), ("body_b", _i),
                 ("num_contacts", _i), ("basis", _d), ("friction", _d), ("feature", _u),
                 ("r_a", _d), ("r_b", _d), ("c0", _d), ("penalty", _d), ("lambda_", _d),
-                ("stick", _i), ("order", _i)]
+                ("stick", _i), ("order", _i), ("restitution_bias", _d)]
 
 
 class WorldC(C.Structure):
@@ -180,6 +190,36 @@ class World:
     """numpy SoA of a world (one scene or a batch of scenes)."""
 
     BODY_F = ("size", "mass", "moment", "radius", "friction", "pos", "quat", "vel", "omega", "prev_vel")
+    MATERIAL_F = ("static_friction", "dynamic_friction", "restitution", "contact_offset", "rest_offset")
+
+    def set_materials(self, static_friction=None, dynamic_friction=None, restitution=None, contact_offset=None,
+                      rest_offset=None):
+        """Per-body contact materials of AVBD_CONTACT_MATERIALS
+        (Rigid.setMaterial, src/physics/rigid.js:144-214): arrays of n
+        values or scalars; None leaves that field at its default (static and
+        dynamic friction: `friction`; restitution 0; offsets: the params').
+        Checks as setMaterial does: values finite, friction, restitution and
+        the contact offset non-negative, restitution <= 1, dynamic <= static
+        friction."""
+        n = self.n_bodies
+        vals = {"static_friction": static_friction, "dynamic_friction": dynamic_friction,
+                "restitution": restitution, "contact_offset": contact_offset, "rest_offset": rest_offset}
+        for k, v in vals.items():
+            if v is None:
+                continue
+            a = np.broadcast_to(np.asarray(v, np.float64), (n,)).copy()
+            if not np.all(np.isfinite(a)):
+                raise ValueError(f"{k} must be finite")
+            if k != "rest_offset" and np.any(a < 0):
+                raise ValueError(f"{k} must be non-negative")
+            if k == "restitution" and np.any(a > 1):
+                raise ValueError("restitution must be in [0, 1]")
+            setattr(self, k, a)
+        sf = self.static_friction if self.static_friction is not None else self.friction
+        df = self.dynamic_friction if self.dynamic_friction is not None else self.friction
+        if np.any(df > sf):
+            raise ValueError("dynamicFriction must not exceed staticFriction")
+        self._c = None
 
     def __init__(self, n_bodies: int, n_joints: int = 0, n_springs: int = 0, manifold_capacity: int = 0,
                  scene_start=None):
@@ -196,6 +236,12 @@ class World:
         self.vel = np.zeros((n, 3))
         self.omega = np.zeros((n, 3))
         self.prev_vel = np.zeros((n, 3))
+        # contact materials (AVBD_CONTACT_MATERIALS); None = the defaults
+        self.static_friction = None
+        self.dynamic_friction = None
+        self.restitution = None
+        self.contact_offset = None
+        self.rest_offset = None
         # joints
         self.j_body_a = np.zeros(j, np.int32)
         self.j_body_b = np.zeros(j, np.int32)
@@ -246,6 +292,7 @@ class World:
         self.m_lambda = np.zeros((m, K, 3))
         self.m_stick = np.zeros((m, K), np.int32)
         self.m_order = np.zeros(m, np.int32)
+        self.m_restitution_bias = np.zeros((m, K))
         self._c = None
 
     def ensure_manifold_capacity(self, m: int):
@@ -274,7 +321,7 @@ class World:
         b = w.bodies
         b.count = self.n_bodies
         b.shape = _ptr(self.shape, _i)
-        for f in self.BODY_F:
+        for f in self.BODY_F + self.MATERIAL_F:
             setattr(b, f, _ptr(getattr(self, f), _d))
         j = w.joints
         j.count = self.n_joints
@@ -300,6 +347,7 @@ class World:
             m.r_a, m.r_b, m.c0 = _ptr(self.m_r_a, _d), _ptr(self.m_r_b, _d), _ptr(self.m_c0, _d)
             m.penalty, m.lambda_ = _ptr(self.m_penalty, _d), _ptr(self.m_lambda, _d)
             m.stick, m.order = _ptr(self.m_stick, _i), _ptr(self.m_order, _i)
+            m.restitution_bias = _ptr(self.m_restitution_bias, _d)
         w.num_scenes = self.num_scenes
         w.scene_start = _ptr(self.scene_start, _i)
         self._c = w
@@ -328,7 +376,7 @@ class World:
         w.omega = f32(w.omega)
         w.prev_vel = f32(w.prev_vel)
         for k in ("j_penalty_lin", "j_penalty_ang", "s_penalty", "m_r_a", "m_r_b", "m_penalty",
-                  "m_lambda"):
+                  "m_lambda", "m_restitution_bias"):
             setattr(w, k, f32(getattr(w, k)))
         return w
 
@@ -347,6 +395,9 @@ class World:
                 setattr(w, k, np.array(d[prefix + k]))
         w.m_count = int(d[prefix + "m_count"])
         w.m_capacity = len(w.m_body_a)
+        # manifold fields added after the arrays were written: zeros of the right shape
+        if w.m_restitution_bias.shape[0] != w.m_capacity:
+            w.m_restitution_bias = np.zeros((w.m_capacity, MAX_CONTACTS))
         w._c = None
         return w
 
@@ -362,6 +413,9 @@ class World:
         for f in ("shape", "size", "mass", "moment", "radius", "friction", "pos", "quat", "vel", "omega",
                   "prev_vel"):
             setattr(out, f, np.ascontiguousarray(getattr(self, f)[b0:b1]))
+        for f in self.MATERIAL_F:
+            if getattr(self, f) is not None:
+                setattr(out, f, np.ascontiguousarray(getattr(self, f)[b0:b1]))
         for f in ("j_r_a", "j_r_b", "j_stiffness_lin", "j_stiffness_ang", "j_fracture", "j_penalty_lin",
                   "j_penalty_ang", "j_lambda_lin", "j_lambda_ang", "j_broken"):
             setattr(out, f, np.ascontiguousarray(getattr(self, f)[js]))
@@ -378,7 +432,7 @@ class World:
         out.j_order, out.s_order = rank[:len(js)].copy(), rank[len(js):].copy()
         out.m_count = len(ms)
         for f in ("m_num_contacts", "m_basis", "m_friction", "m_feature", "m_r_a", "m_r_b", "m_c0", "m_penalty",
-                  "m_lambda", "m_stick"):
+                  "m_lambda", "m_stick", "m_restitution_bias"):
             getattr(out, f)[:len(ms)] = getattr(self, f)[ms]
         out.m_body_a[:len(ms)] = self.m_body_a[ms] - b0
         out.m_body_b[:len(ms)] = self.m_body_b[ms] - b0
@@ -406,6 +460,17 @@ class World:
                   "prev_vel"):
             getattr(w, f)[:n0] = getattr(self, f)[keep]
             getattr(w, f)[n0:] = getattr(ex, f)
+        for f in self.MATERIAL_F:
+            mine, theirs = getattr(self, f), getattr(ex, f)
+            if mine is None and theirs is None:
+                continue
+            default = {"static_friction": "friction", "dynamic_friction": "friction"}.get(f)
+            fill = lambda src, a, wd: (a if a is not None else (getattr(src, default) if default else
+                                                               np.full(src.n_bodies, np.nan)))
+            a = np.concatenate([fill(self, mine, self)[keep], fill(ex, theirs, ex)])
+            if np.isnan(a).any():
+                raise ValueError(f"{f}: set on one side of the edit only; give both worlds the field")
+            setattr(w, f, a)
         jf = ("j_r_a", "j_r_b", "j_stiffness_lin", "j_stiffness_ang", "j_fracture", "j_penalty_lin", "j_penalty_ang",
               "j_lambda_lin", "j_lambda_ang", "j_broken")
         sf = ("s_r_a", "s_r_b", "s_stiffness", "s_rest", "s_tear_strain", "s_penalty", "s_peak_strain", "s_broken")
@@ -479,7 +544,7 @@ class World:
         w._alloc_manifolds(max(len(live), 1))
         w.m_count = len(live)
         for f in ("m_num_contacts", "m_basis", "m_friction", "m_feature", "m_r_a", "m_r_b", "m_c0", "m_penalty",
-                  "m_lambda", "m_stick"):
+                  "m_lambda", "m_stick", "m_restitution_bias"):
             getattr(w, f)[:len(live)] = getattr(old, f)[live]
         w.m_body_a[:len(live)] = new_of[old.m_body_a[live]]
         w.m_body_b[:len(live)] = new_of[old.m_body_b[live]]

@@ -68,6 +68,9 @@ struct SolverParams {
   int solveBlocksPerSm;  // resident blocks per SM of the solve launch (grid = this x SMs)
   long long barrierLimit, waitLimit;  // polls before a grid barrier / a neighbour wait gives up
   int tailDiv;   // colours of at most (grid / tailDiv) chunks form the tail segment
+  // AVBD_CONTACT_MATERIALS (the WebGPU engine's contact extensions) when 1
+  int contactModel;
+  double restitutionThreshold, contactPersistence;
 };
 
 // Device scalars shared by all kernels of a step.
@@ -121,6 +124,10 @@ struct Bodies {
   int *flags;     // per-step flags (static bits | kBodyFp64)
   int *color;     // colour, -1 for static bodies
   int *progress;  // iterations completed in the current step (wavefront schedule)
+  // contact materials (AVBD_CONTACT_MATERIALS only, else null): static and
+  // dynamic friction, restitution, rest offset; contact offset
+  const D4 *mat;
+  const double *contactOffset;
 };
 
 struct Manifolds {
@@ -135,6 +142,8 @@ struct Manifolds {
   float4 *cB;  // rB world at x_t, C0.y
   float4 *cK;  // penalty xyz, C0.z
   float4 *cL;  // lambda xyz, stick
+  float *cX;   // restitution bias (AVBD_CONTACT_MATERIALS); basis1.w bit 1 then marks
+               // a positive contact skin and basis2.w holds the dynamic friction
 };
 
 struct Joints {

@@ -246,7 +246,8 @@ int alloc_manifolds(avbd_ctx *ctx, Manifolds &m, int cap) {
       (rc = galloc(ctx, &m.basis1, cap)) || (rc = galloc(ctx, &m.basis2, cap)) ||
       (rc = galloc(ctx, &m.basisD, (size_t)cap * 9)) || (rc = galloc(ctx, &m.feat, S)) ||
       (rc = galloc(ctx, &m.rA, S)) || (rc = galloc(ctx, &m.rB, S)) || (rc = galloc(ctx, &m.cA, S)) ||
-      (rc = galloc(ctx, &m.cB, S)) || (rc = galloc(ctx, &m.cK, S)) || (rc = galloc(ctx, &m.cL, S)))
+      (rc = galloc(ctx, &m.cB, S)) || (rc = galloc(ctx, &m.cK, S)) || (rc = galloc(ctx, &m.cL, S)) ||
+      (rc = galloc(ctx, &m.cX, S)))
     return rc;
   return AVBD_OK;
 }
@@ -298,6 +299,7 @@ int grow_arenas(avbd_ctx *ctx, int cap, const Manifolds old, int keep) {
     float4 *dst[6] = {pm.rA, pm.rB, pm.cA, pm.cB, pm.cK, pm.cL};
     float4 *src[6] = {old.rA, old.rB, old.cA, old.cB, old.cK, old.cL};
     for (int k = 0; k < 6; k++) CK(cudaMemcpy(dst[k], src[k], keep * K * sizeof(float4), cudaMemcpyDeviceToDevice));
+    CK(cudaMemcpy(pm.cX, old.cX, keep * K * sizeof(float), cudaMemcpyDeviceToDevice));
   }
   CK(cudaDeviceSynchronize());
   for (void *p : oldBufs) cudaFree(p);
@@ -467,6 +469,8 @@ int write_state(avbd_ctx *ctx, const avbd_world *world, bool keepManifolds) {
     std::vector<double> basisD((size_t)live * 9);
     std::vector<uint32_t> feat(live * K, 0);
     std::vector<float4> rA(live * K), rB(live * K), cK(live * K), cL(live * K);
+    std::vector<float> cX(live * K, 0.f);
+    std::vector<float4> cA(live * K, make_float4(0.f, 0.f, 0.f, 0.f));  // .w: C0 on the normal
     for (int t = 0; t < live; t++) {
       const int m = idx[t];
       key[t] = (uint64_t)M.body_a[m] << 32 | (uint32_t)M.body_b[m];
@@ -482,6 +486,8 @@ int write_state(avbd_ctx *ctx, const avbd_world *world, bool keepManifolds) {
         rB[dst] = f3(M.r_b, 0.f);
         cK[dst] = f3(M.penalty, 0.f);
         cL[dst] = f3(M.lambda, (M.stick && M.stick[src]) ? 1.f : 0.f);
+        cX[dst] = M.restitution_bias ? (float)M.restitution_bias[src] : 0.f;
+        cA[dst].w = M.c0 ? (float)M.c0[src * 3] : 0.f;  // re-arms restitution (AVBD_CONTACT_MATERIALS)
       }
     }
     CK(cudaMemcpy(pm.key, key.data(), live * sizeof(uint64_t), cudaMemcpyHostToDevice));
@@ -492,6 +498,8 @@ int write_state(avbd_ctx *ctx, const avbd_world *world, bool keepManifolds) {
     CK(cudaMemcpy(pm.rB, rB.data(), rB.size() * sizeof(float4), cudaMemcpyHostToDevice));
     CK(cudaMemcpy(pm.cK, cK.data(), cK.size() * sizeof(float4), cudaMemcpyHostToDevice));
     CK(cudaMemcpy(pm.cL, cL.data(), cL.size() * sizeof(float4), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(pm.cX, cX.data(), cX.size() * sizeof(float), cudaMemcpyHostToDevice));
+    CK(cudaMemcpy(pm.cA, cA.data(), cA.size() * sizeof(float4), cudaMemcpyHostToDevice));
   }
   if (M.count > 0 || !keepManifolds) {
     Control c{};
@@ -998,7 +1006,8 @@ int avbd_pack(avbd_ctx *ctx, const avbd_world *world) {
                      P.wait_limit > 0 ? (long long)P.wait_limit : 20000000LL,
                      P.neighbor_wait_limit > 0 ? (long long)P.neighbor_wait_limit
                                                : (P.wait_limit > 0 ? (long long)P.wait_limit : 4000000LL),
-                     P.tail_div > 0 ? P.tail_div : 8};
+                     P.tail_div > 0 ? P.tail_div : 8, P.contact_model == AVBD_CONTACT_MATERIALS ? 1 : 0,
+                     P.restitution_threshold, P.contact_persistence};
   int rc = 0;
   D4 *sizeP, *massDP;
   float4 *massFP;
@@ -1015,6 +1024,31 @@ int avbd_pack(avbd_ctx *ctx, const avbd_world *world) {
       (rc = upload(ctx, &largeListP, largeList)) || (rc = upload(ctx, &cStartP, cStart)) || (rc = upload(ctx, &cRefP, cRef)))
     return rc;
   w.b.n = n;
+  w.b.mat = nullptr;
+  w.b.contactOffset = nullptr;
+  if (P.contact_model == AVBD_CONTACT_MATERIALS) {
+    // contact materials (Rigid.setMaterial, src/physics/rigid.js:144-214)
+    std::vector<D4> mat(n);
+    std::vector<double> cofs(n);
+    for (int i = 0; i < n; i++) {
+      const double sf = B.static_friction ? B.static_friction[i] : B.friction[i];
+      const double df = B.dynamic_friction ? B.dynamic_friction[i] : B.friction[i];
+      const double e = B.restitution ? B.restitution[i] : 0.0;
+      const double ro = B.rest_offset ? B.rest_offset[i] : P.rest_offset;
+      const double co = B.contact_offset ? B.contact_offset[i] : P.contact_offset;
+      if (!(sf >= 0) || !(df >= 0) || df > sf || !(e >= 0 && e <= 1) || !(co >= 0) || !std::isfinite(ro) ||
+          !std::isfinite(sf) || !std::isfinite(co))
+        return fail(ctx, AVBD_ERR_ARG, "body %d: contact material out of range (friction >= 0, dynamic <= static, "
+                                       "restitution in [0, 1], contact offset >= 0, finite rest offset)", i);
+      mat[i] = mkd4(sf, df, e, ro);
+      cofs[i] = co;
+    }
+    D4 *matP;
+    double *cofsP;
+    if ((rc = upload(ctx, &matP, mat)) || (rc = upload(ctx, &cofsP, cofs))) return rc;
+    w.b.mat = matP;
+    w.b.contactOffset = cofsP;
+  }
   w.b.size = sizeP; w.b.massD = massDP; w.b.massF = massFP; w.b.friction = fricP; w.b.flags0 = flags0P;
   w.b.scene = sceneP; w.b.priority = prioP;
   if ((rc = dalloc(ctx, &w.b.pos, n)) || (rc = dalloc(ctx, &w.b.quat, n)) || (rc = dalloc(ctx, &w.b.vel, n)) ||
@@ -1234,6 +1268,7 @@ int avbd_read_state(avbd_ctx *ctx, avbd_world *out) {
     std::vector<float4> b0(total);
     std::vector<uint32_t> feat((size_t)total * K);
     std::vector<float4> rA(total * K), rB(total * K), cA(total * K), cB(total * K), cK(total * K), cL(total * K);
+    std::vector<float> cX(total * K);
     if (total) {
       CK(cudaMemcpy(basisD.data(), pm.basisD, basisD.size() * sizeof(double), cudaMemcpyDeviceToHost));
       CK(cudaMemcpy(b0.data(), pm.basis0, total * sizeof(float4), cudaMemcpyDeviceToHost));
@@ -1244,6 +1279,7 @@ int avbd_read_state(avbd_ctx *ctx, avbd_world *out) {
       CK(cudaMemcpy(cB.data(), pm.cB, cB.size() * sizeof(float4), cudaMemcpyDeviceToHost));
       CK(cudaMemcpy(cK.data(), pm.cK, cK.size() * sizeof(float4), cudaMemcpyDeviceToHost));
       CK(cudaMemcpy(cL.data(), pm.cL, cL.size() * sizeof(float4), cudaMemcpyDeviceToHost));
+      CK(cudaMemcpy(cX.data(), pm.cX, cX.size() * sizeof(float), cudaMemcpyDeviceToHost));
     }
     for (int t = 0; t < wrote; t++) {
       const int m = live[t];
@@ -1265,6 +1301,7 @@ int avbd_read_state(avbd_ctx *ctx, avbd_world *out) {
             dst[f][d * 3 + 2] = on ? v[f].z : 0;
           }
         if (M.stick) M.stick[d] = (on && cL[src].w != 0.f) ? 1 : 0;
+        if (M.restitution_bias) M.restitution_bias[d] = on ? cX[src] : 0.0;
       }
       if (M.order) M.order[t] = t;
     }
@@ -1550,6 +1587,9 @@ int avbd_adjoint_forward(avbd_ctx *ctx, const avbd_world *world, int32_t steps, 
                          int32_t n_seeds) {
   if (!ctx || !world || steps < 0 || n_seeds < 0 || (n_seeds > 0 && !seeds))
     return fail(ctx, AVBD_ERR_ARG, "avbd_adjoint_forward: NULL argument or negative count");
+  if (ctx->params.contact_model != AVBD_CONTACT_CPU)
+    return fail(ctx, AVBD_ERR_ARG, "avbd_adjoint_forward: the differentiable step follows the CPU contact model "
+                                   "(contact_model = AVBD_CONTACT_CPU)");
   char msg[256] = "";
   CK(cudaStreamSynchronize(ctx->stream));
   if (ctx->tangent) {

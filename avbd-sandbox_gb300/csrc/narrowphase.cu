@@ -422,9 +422,24 @@ __device__ void transport(double *lam, double *pen, const double *ob, const doub
 
 // Box pairs, in f32 in A's frame (xA - xB = R_A rA - R_B rB - (pB - pA)); the
 // outputs are stored in f32.
+__device__ void write_manifold_materials(const World &w, int c, int ia, int ib, const BodyD &A, const BodyD &B,
+                                         const D3 *ncA, const D3 *ncB, const uint32_t *feat, int num,
+                                         const double *basis);
+
 __device__ void write_box_manifold(const World &w, int c, int ia, int ib, const BodyD &A, const BodyD &B,
                                    const NewContactF *nc, int num, const double *basis) {
   const SolverParams &P = w.p;
+  if (P.contactModel) {
+    D3 ra[kMaxContacts], rb[kMaxContacts];
+    uint32_t ft[kMaxContacts];
+    for (int i = 0; i < num; i++) {
+      ra[i] = mk(nc[i].ra[0], nc[i].ra[1], nc[i].ra[2]);
+      rb[i] = mk(nc[i].rb[0], nc[i].rb[1], nc[i].rb[2]);
+      ft[i] = nc[i].feature;
+    }
+    write_manifold_materials(w, c, ia, ib, A, B, ra, rb, ft, num, basis);
+    return;
+  }
   w.cur.count[c] = num;
   if (num == 0) return;
   const int pi = w.g.candPrev[c];
@@ -488,6 +503,17 @@ __device__ void write_box_manifold(const World &w, int c, int ia, int ib, const 
 __device__ void write_sphere_manifold(const World &w, int c, int ia, int ib, const BodyD &A, const BodyD &B,
                                       const NewContact *nc, int num, const double *basis) {
   const SolverParams &P = w.p;
+  if (P.contactModel) {
+    D3 ra[kMaxContacts], rb[kMaxContacts];
+    uint32_t ft[kMaxContacts];
+    for (int i = 0; i < num; i++) {
+      ra[i] = nc[i].rA;
+      rb[i] = nc[i].rB;
+      ft[i] = nc[i].feature;
+    }
+    write_manifold_materials(w, c, ia, ib, A, B, ra, rb, ft, num, basis);
+    return;
+  }
   w.cur.count[c] = num;
   if (num == 0) return;
   const int pi = w.g.candPrev[c];
@@ -544,6 +570,143 @@ __device__ void write_sphere_manifold(const World &w, int c, int ia, int ib, con
   w.cur.basis0[c] = make_float4((float)basis[0], (float)basis[1], (float)basis[2], (float)friction);
   w.cur.basis1[c] = make_float4((float)basis[3], (float)basis[4], (float)basis[5], 1.f);  // .w: sphere pair
   w.cur.basis2[c] = make_float4((float)basis[6], (float)basis[7], (float)basis[8], 0.f);
+}
+
+// AVBD_CONTACT_MATERIALS: the WebGPU engine's manifold warm start with its
+// contact extensions (src/physics/gpu/shaders.js:1105-1366), in f64 for box
+// and sphere pairs alike (an opt-in model; the default path above keeps the
+// f32 box merge). Pair materials: friction as the geometric mean of the
+// static and of the dynamic coefficients, restitution as the max, contact
+// and rest offsets summed. A new contact matches the old one with its
+// feature ID, else the nearest old contact within the persistence distance
+// (separation, tangential offset and midpoint distance within it), each old
+// contact claimed once and only when the normals agree (dot > 0.85);
+// multiplier and penalty are transported into the new basis; a matched
+// static box contact keeps its anchors; a new contact starts static. C0 on
+// the normal is measured to the rest distance; a new or re-armed impact
+// (the old contact still outside rest and without a bias) faster than the
+// restitution threshold gets a one-frame bias.
+__device__ void write_manifold_materials(const World &w, int c, int ia, int ib, const BodyD &A, const BodyD &B,
+                                         const D3 *ncA, const D3 *ncB, const uint32_t *feat, int num,
+                                         const double *basis) {
+  const SolverParams &P = w.p;
+  w.cur.count[c] = num;
+  if (num == 0) return;
+  const int pi = w.g.candPrev[c];
+  const int oldNum = pi >= 0 ? w.prev.count[pi] : 0;
+  double ob[9];
+  for (int k = 0; k < 9; k++) ob[k] = oldNum > 0 ? w.prev.basisD[pi * 9 + k] : basis[k];
+  const D4 ma = w.b.mat[ia], mb = w.b.mat[ib];
+  const double mus = sqrt(ma.x * mb.x), mud = sqrt(ma.y * mb.y);
+  const double restitution = ma.z > mb.z ? ma.z : (mb.z > ma.z ? mb.z : ma.z);
+  const double contactDistance = w.b.contactOffset[ia] + w.b.contactOffset[ib];
+  const double restDistance = ma.w + mb.w;
+  const D3 nN = mk(basis[0], basis[1], basis[2]);
+  const bool compatible = oldNum > 0 && (ob[0] * basis[0] + ob[1] * basis[1] + ob[2] * basis[2]) > 0.85;
+  const double minA = fmin(A.half.x, fmin(A.half.y, A.half.z)), minB = fmin(B.half.x, fmin(B.half.y, B.half.z));
+  const double minExtent = 2.0 * fmin(minA, minB);
+  const double persistence = fmax(P.contactPersistence, fmax(contactDistance, minExtent * 0.02));
+  const double psq = persistence * persistence;
+  const bool curved = A.sphere || B.sphere;
+  const float4 vA4 = w.b.vel[ia], wA4 = w.b.omega[ia], vB4 = w.b.vel[ib], wB4 = w.b.omega[ib];
+  const D3 vA = mk(vA4.x, vA4.y, vA4.z), wA = mk(wA4.x, wA4.y, wA4.z);
+  const D3 vB = mk(vB4.x, vB4.y, vB4.z), wB = mk(wB4.x, wB4.y, wB4.z);
+  unsigned used = 0u;
+  for (int i = 0; i < num; i++) {
+    D3 rA = ncA[i], rB = ncB[i];
+    double lam[3] = {0, 0, 0}, pen[3] = {0, 0, 0};
+    bool stick = true, priorOut = false, priorBias = false, found = false, exact = false;
+    int match = -1;
+    double best = psq;
+    const D3 nxA = add(rot(A.q, rA), A.p), nxB = add(rot(B.q, rB), B.p);
+    const D3 mid = mk((nxA.x + nxB.x) * 0.5, (nxA.y + nxB.y) * 0.5, (nxA.z + nxB.z) * 0.5);
+    if (compatible) {
+      for (int j = 0; j < oldNum; j++) {
+        if (used & (1u << j)) continue;
+        const int os = pi * kMaxContacts + j;
+        const bool same = w.prev.feat[os] == feat[i];
+        if (curved && same) {
+          match = j;
+          exact = true;
+          break;
+        }
+        const float4 oa = w.prev.rA[os], obb = w.prev.rB[os];
+        const D3 oxA = add(rot(A.q, mk(oa.x, oa.y, oa.z)), A.p);
+        const D3 oxB = add(rot(B.q, mk(obb.x, obb.y, obb.z)), B.p);
+        const D3 od = sub(oxA, oxB);
+        const double sep = nN.x * od.x + nN.y * od.y + nN.z * od.z;
+        const D3 td = mk(od.x - nN.x * sep, od.y - nN.y * sep, od.z - nN.z * sep);
+        if (sep > contactDistance + persistence) continue;
+        if (td.x * td.x + td.y * td.y + td.z * td.z > psq) continue;
+        const D3 md = mk(mid.x - (oxA.x + oxB.x) * 0.5, mid.y - (oxA.y + oxB.y) * 0.5, mid.z - (oxA.z + oxB.z) * 0.5);
+        const double mdSq = md.x * md.x + md.y * md.y + md.z * md.z;
+        if (mdSq > psq) continue;
+        if (same) {
+          match = j;
+          exact = true;
+          break;
+        }
+        if (!found || mdSq < best) {
+          found = true;
+          match = j;
+          best = mdSq;
+        }
+      }
+    }
+    found = found || exact;
+    if (found) {
+      const int os = pi * kMaxContacts + match;
+      used |= 1u << match;
+      const float4 ok = w.prev.cK[os], ol = w.prev.cL[os];
+      for (int r = 0; r < 3; r++) {  // transport into the new basis (shaders.js:1050-1085)
+        const double *nr = &basis[r * 3];
+        const double a = nr[0] * ob[0] + nr[1] * ob[1] + nr[2] * ob[2];
+        const double b = nr[0] * ob[3] + nr[1] * ob[4] + nr[2] * ob[5];
+        const double cc = nr[0] * ob[6] + nr[1] * ob[7] + nr[2] * ob[8];
+        pen[r] = (double)ok.x * (a * a) + (double)ok.y * (b * b) + (double)ok.z * (cc * cc);
+        lam[r] = (double)ol.x * a + (double)ol.y * b + (double)ol.z * cc;
+      }
+      stick = ol.w != 0.0f;
+      priorOut = w.prev.cA[os].w > 0.0f;
+      priorBias = w.prev.cX[os] > 0.0f;
+      if (stick && !A.sphere && !B.sphere) {
+        const float4 oa = w.prev.rA[os], obb = w.prev.rB[os];
+        rA = mk(oa.x, oa.y, oa.z);
+        rB = mk(obb.x, obb.y, obb.z);
+      }
+    }
+    const D3 rAw = rot(A.q, rA), rBw = rot(B.q, rB);
+    const D3 d = sub(add(rAw, A.p), add(rBw, B.p));
+    double C0[3];
+    C0[0] = basis[0] * d.x + basis[1] * d.y + basis[2] * d.z - restDistance;
+    C0[1] = basis[3] * d.x + basis[4] * d.y + basis[5] * d.z;
+    C0[2] = basis[6] * d.x + basis[7] * d.y + basis[8] * d.z;
+    double bias = 0.0;
+    if ((!found || (priorOut && !priorBias)) && restitution > 0.0) {
+      const D3 ua = add(vA, crs(wA, rAw)), ub = add(vB, crs(wB, rBw));
+      const D3 rel = sub(ua, ub);
+      const double vn = nN.x * rel.x + nN.y * rel.y + nN.z * rel.z;
+      const double closing = fmax(0.0, -vn * P.dt), toRest = fmax(0.0, C0[0]);
+      if (vn < -P.restitutionThreshold && closing > toRest) bias = restitution * (closing - toRest);
+    }
+    if (!P.postStabilize)
+      for (int k = 0; k < 3; k++) lam[k] = lam[k] * P.alpha * P.gamma;
+    for (int k = 0; k < 3; k++) pen[k] = clampd(pen[k] * P.gamma, P.penaltyMin, P.penaltyMax);
+    const int s = c * kMaxContacts + i;
+    w.cur.feat[s] = feat[i];
+    w.cur.rA[s] = make_float4((float)rA.x, (float)rA.y, (float)rA.z, 0.f);
+    w.cur.rB[s] = make_float4((float)rB.x, (float)rB.y, (float)rB.z, 0.f);
+    w.cur.cA[s] = make_float4((float)rAw.x, (float)rAw.y, (float)rAw.z, (float)C0[0]);
+    w.cur.cB[s] = make_float4((float)rBw.x, (float)rBw.y, (float)rBw.z, (float)C0[1]);
+    w.cur.cK[s] = make_float4((float)pen[0], (float)pen[1], (float)pen[2], (float)C0[2]);
+    w.cur.cL[s] = make_float4((float)lam[0], (float)lam[1], (float)lam[2], stick ? 1.f : 0.f);
+    w.cur.cX[s] = (float)bias;
+  }
+  for (int k = 0; k < 9; k++) w.cur.basisD[c * 9 + k] = basis[k];
+  const float flags = (curved ? 1.f : 0.f) + (contactDistance > 0.0 ? 2.f : 0.f);
+  w.cur.basis0[c] = make_float4((float)basis[0], (float)basis[1], (float)basis[2], (float)mus);
+  w.cur.basis1[c] = make_float4((float)basis[3], (float)basis[4], (float)basis[5], flags);
+  w.cur.basis2[c] = make_float4((float)basis[6], (float)basis[7], (float)basis[8], (float)mud);
 }
 
 // Append to one of the work lists, one atomic per coalesced group of lanes.

@@ -64,7 +64,7 @@ __global__ void repack_flag_kernel(const Manifolds om, int slots, const int *new
 // move to their compacted position with renumbered bodies. The fields are the
 // ones a warm start reads (the CPU handover of avbd_write_state writes the
 // same): key, count, f64 basis, and per contact the feature ID, body-local
-// anchors, penalty and multiplier with the stick bit.
+// anchors, penalty and multiplier with the stick bit, restitution bias.
 __global__ void repack_move_kernel(const Manifolds om, Manifolds nm, int slots, const int *newOf, const int *flag,
                                    const int *at) {
   const long long total = (long long)slots * kMaxContacts;
@@ -89,6 +89,8 @@ __global__ void repack_move_kernel(const Manifolds om, Manifolds nm, int slots, 
     nm.cK[dst] = on ? make_float4(k.x, k.y, k.z, 0.f) : make_float4(0.f, 0.f, 0.f, 0.f);
     const float4 l = om.cL[src];
     nm.cL[dst] = on ? make_float4(l.x, l.y, l.z, l.w != 0.f ? 1.f : 0.f) : make_float4(0.f, 0.f, 0.f, 0.f);
+    nm.cX[dst] = on ? om.cX[src] : 0.f;
+    nm.cA[dst] = on ? om.cA[src] : make_float4(0.f, 0.f, 0.f, 0.f);  // .w: C0 on the normal
   }
 }
 

@@ -938,24 +938,56 @@ struct ContactEval {
   bool within;
 };
 
+// The contact extensions of AVBD_CONTACT_MATERIALS (the WebGPU engine's,
+// src/physics/gpu/shaders.js:1806-1845): the pair's dynamic friction, a
+// positive contact skin, the contact's restitution bias, and whether this
+// pass is the post-stabilisation projection (no bias there).
+template <class T>
+struct ContactExt {
+  bool on;
+  bool skin, projection;
+  T mud;
+  float bias;
+};
+
 // manifold.js:358-409 in delta form: C = (1 - alpha) C0 + n_r . (dx_A - dx_B),
-// dx = delta + dtheta x r_world(x_t).
+// dx = delta + dtheta x r_world(x_t). With the extensions: a positive gap is
+// kept unscaled while the skin is on, the restitution bias comes off the
+// normal row, a static contact (cL.w) is bounded by the static cone and a
+// force outside it is clamped to the dynamic one.
 template <class T>
 __device__ __forceinline__ ContactEval<T> eval_contact(const V3<T> n[3], T mu, float4 cA, float4 cB, float4 cK, float4 cL,
-                                              const BState<T> &A, const BState<T> &B, T alpha) {
+                                              const BState<T> &A, const BState<T> &B, T alpha,
+                                              const ContactExt<T> &x = ContactExt<T>{false, false, false, T(0), 0.f}) {
   const V3<T> rA{(T)cA.x, (T)cA.y, (T)cA.z}, rB{(T)cB.x, (T)cB.y, (T)cB.z};
   const V3<T> u = (A.dp + cross(A.dang, rA)) - (B.dp + cross(B.dang, rB));
   ContactEval<T> e;
   const T om = T(1) - alpha;
-  e.C.x = om * (T)cA.w + dot(n[0], u);
+  if (x.on) {
+    T c0 = (x.skin && (T)cA.w > T(0)) ? (T)cA.w : om * (T)cA.w;
+    if (!x.projection) c0 = c0 - (T)x.bias;
+    e.C.x = c0 + dot(n[0], u);
+  } else {
+    e.C.x = om * (T)cA.w + dot(n[0], u);
+  }
   e.C.y = om * (T)cB.w + dot(n[1], u);
   e.C.z = om * (T)cK.w + dot(n[2], u);
   e.F.x = (T)cK.x * e.C.x + (T)cL.x;
   e.F.y = (T)cK.y * e.C.y + (T)cL.y;
   e.F.z = (T)cK.z * e.C.z + (T)cL.z;
   e.F.x = e.F.x < T(0) ? e.F.x : T(0);
-  const T bounds = fabs(e.F.x) * mu;
   const T fs = sqrt(e.F.y * e.F.y + e.F.z * e.F.z);
+  if (x.on) {
+    const T active = fabs(e.F.x) * (cL.w != 0.f ? mu : x.mud);
+    e.within = fs <= active;
+    if (!e.within && fs > T(0)) {
+      const T dyn = fabs(e.F.x) * x.mud;
+      e.F.y = e.F.y * dyn / fs;
+      e.F.z = e.F.z * dyn / fs;
+    }
+    return e;
+  }
+  const T bounds = fabs(e.F.x) * mu;
   if (fs > bounds && fs > T(0)) {
     e.F.y *= bounds / fs;
     e.F.z *= bounds / fs;
@@ -971,7 +1003,7 @@ __device__ __forceinline__ void manifold_rows(const World &w, int m, V3<T> n[3],
   n[1] = V3<T>{(T)b1.x, (T)b1.y, (T)b1.z};
   n[2] = V3<T>{(T)b2.x, (T)b2.y, (T)b2.z};
   mu = (T)b0.w;
-  sphere = b1.w != 0.0f;  // the narrow phase marks sphere pairs here
+  sphere = ((int)b1.w & 1) != 0;  // the narrow phase marks sphere pairs here (bit 1: a contact skin)
 }
 
 // A neighbour's state as the contact rows read it: displacement and
@@ -1001,10 +1033,21 @@ struct ContactData {
   int slot, side;
   bool owned;  // this body owns the contact's dual update
   bool sphere;
+  ContactExt<T> x;  // AVBD_CONTACT_MATERIALS
 };
 
+// The extension fields of a contact (AVBD_CONTACT_MATERIALS; off otherwise).
 template <class T>
-__device__ __forceinline__ ContactData<T> load_contact(const World &w, int2 ent) {
+__device__ __forceinline__ void load_ext(const World &w, ContactData<T> &d, float b1w, float b2w, T alpha) {
+  d.x.on = true;
+  d.x.skin = ((int)b1w & 2) != 0;
+  d.x.mud = (T)b2w;
+  d.x.bias = ld(&w.cur.cX[d.slot]);
+  d.x.projection = w.p.postStabilize && alpha < T(0.5);
+}
+
+template <class T, bool E>
+__device__ __forceinline__ ContactData<T> load_contact(const World &w, int2 ent, T alpha) {
   ContactData<T> d;
   d.slot = ent.x >> 2;
   d.owned = (ent.x & 2) != 0;
@@ -1015,6 +1058,8 @@ __device__ __forceinline__ ContactData<T> load_contact(const World &w, int2 ent)
   d.cK = __ldcg(&w.cur.cK[d.slot]);
   d.cL = __ldcg(&w.cur.cL[d.slot]);
   d.o = load_other<T>(w, ent.y);
+  d.x.on = false;
+  if (E) load_ext<T>(w, d, ld(&w.cur.basis1[d.slot >> 3]).w, ld(&w.cur.basis2[d.slot >> 3]).w, alpha);
   return d;
 }
 
@@ -1023,7 +1068,7 @@ __device__ __forceinline__ void contact_primal(const ContactData<T> &d, const BS
   const BState<T> &A = d.side ? d.o : self;
   const BState<T> &B = d.side ? self : d.o;
   const T sgn = d.side ? T(-1) : T(1);
-  const ContactEval<T> e = eval_contact(d.n, d.mu, d.cA, d.cB, d.cK, d.cL, A, B, alpha);
+  const ContactEval<T> e = eval_contact(d.n, d.mu, d.cA, d.cB, d.cK, d.cL, A, B, alpha, d.x);
   const V3<T> r = d.side ? V3<T>{(T)d.cB.x, (T)d.cB.y, (T)d.cB.z} : V3<T>{(T)d.cA.x, (T)d.cA.y, (T)d.cA.z};
   const T kk[3] = {(T)d.cK.x, (T)d.cK.y, (T)d.cK.z};
   const T ff[3] = {e.F.x, e.F.y, e.F.z};
@@ -1043,7 +1088,7 @@ __device__ __forceinline__ void contact_dual(const World &w, const ContactData<T
   const BState<T> &A = d.side ? d.o : self;
   const BState<T> &B = d.side ? self : d.o;
   const T beta = (T)w.p.betaLin, kmax = (T)w.p.penaltyMax, thr = (T)w.p.stickThreshold;
-  const ContactEval<T> e = eval_contact(d.n, d.mu, d.cA, d.cB, d.cK, d.cL, A, B, alpha);
+  const ContactEval<T> e = eval_contact(d.n, d.mu, d.cA, d.cB, d.cK, d.cL, A, B, alpha, d.x);
   float4 cK = d.cK;
   float stick = d.cL.w;
   if (e.F.x < T(0)) cK.x = (float)fmin((T)cK.x + beta * fabs(e.C.x), kmax);
@@ -1054,6 +1099,7 @@ __device__ __forceinline__ void contact_dual(const World &w, const ContactData<T
   } else if (d.sphere) {
     stick = 0.f;
   }
+  if (d.x.on) stick = e.within ? 1.f : 0.f;  // static = inside the cone (shaders.js:2253-2260)
   __stcg(&w.cur.cK[d.slot], cK);
   __stcg(&w.cur.cL[d.slot], make_float4((float)e.F.x, (float)e.F.y, (float)e.F.z, stick));
 }
@@ -1385,19 +1431,19 @@ __device__ __forceinline__ int first_extra(int lane, int nm, int G) {
   return lane < nm ? lane + ((nm - lane + G - 1) / G) * G : lane;
 }
 
-template <class T>
+template <class T, bool E>
 __device__ __noinline__ void extra_primal(const World &w, int i, int cb, int nm, int cStart, int total, int lane,
                                           int G, const BState<T> &self, T alpha, Sys<T> &s) {
   // contacts beyond the lane's first, two at a time so that their loads overlap
   int e = lane + G;
   for (; e + G < nm; e += 2 * G) {
     const int2 ea = ld(&w.a.centry[cb + e]), eb = ld(&w.a.centry[cb + e + G]);
-    const ContactData<T> da = load_contact<T>(w, ea);
-    const ContactData<T> db = load_contact<T>(w, eb);
+    const ContactData<T> da = load_contact<T, E>(w, ea, alpha);
+    const ContactData<T> db = load_contact<T, E>(w, eb, alpha);
     contact_primal<T>(da, self, alpha, s);
     contact_primal<T>(db, self, alpha, s);
   }
-  if (e < nm) contact_primal<T>(load_contact<T>(w, ld(&w.a.centry[cb + e])), self, alpha, s);
+  if (e < nm) contact_primal<T>(load_contact<T, E>(w, ld(&w.a.centry[cb + e]), alpha), self, alpha, s);
   for (e = first_extra(lane, nm, G); e < total; e += G) {
     const uint32_t ref = ld(&w.g.cRef[cStart + e - nm]);
     const uint32_t type = ref >> 30, idx = (ref >> 1) & 0x1fffffffu, side = ref & 1u;
@@ -1408,7 +1454,7 @@ __device__ __noinline__ void extra_primal(const World &w, int i, int cb, int nm,
 
 // The dual updates of the extra entries this body owns; a contact's data is
 // loaded only when its owner bit says so.
-template <class T>
+template <class T, bool E>
 __device__ __noinline__ void extra_dual(const World &w, int i, int cb, int nm, int cStart, int total, int lane, int G,
                                         const BState<T> &self, T alpha) {
   int pending = -1;  // an owned contact waiting for a partner, so loads go two at a time
@@ -1419,13 +1465,13 @@ __device__ __noinline__ void extra_dual(const World &w, int i, int cb, int nm, i
       pending = e;
       continue;
     }
-    const ContactData<T> da = load_contact<T>(w, ld(&w.a.centry[cb + pending]));
-    const ContactData<T> db = load_contact<T>(w, ent);
+    const ContactData<T> da = load_contact<T, E>(w, ld(&w.a.centry[cb + pending]), alpha);
+    const ContactData<T> db = load_contact<T, E>(w, ent, alpha);
     contact_dual<T>(w, da, self, alpha);
     contact_dual<T>(w, db, self, alpha);
     pending = -1;
   }
-  if (pending >= 0) contact_dual<T>(w, load_contact<T>(w, ld(&w.a.centry[cb + pending])), self, alpha);
+  if (pending >= 0) contact_dual<T>(w, load_contact<T, E>(w, ld(&w.a.centry[cb + pending]), alpha), self, alpha);
   const int myColor = total > nm ? ld(&w.b.color[i]) : 0;
   for (int e = first_extra(lane, nm, G); e < total; e += G) {
     const uint32_t ref = ld(&w.g.cRef[cStart + e - nm]);
@@ -1541,7 +1587,7 @@ __device__ __forceinline__ void finish_body(const World &w, int i, int lane, int
 // the dual updates (manifold.js:447, joint.js:255, spring.js:618) of the
 // constraints it owns, and on the last main iteration its BDF1 velocity.
 // Register form: the FP64 path.
-template <class T>
+template <class T, bool E>
 __device__ void solve_body(const World &w, int4 rec, int lane, int G, unsigned mask, T alpha, bool dual, bool velocity) {
   const int i = rec.x, cb = rec.y, nm = rec.z - rec.y;
   // one round of loads: own state, constraint ranges and this lane's first contact
@@ -1551,19 +1597,19 @@ __device__ void solve_body(const World &w, int4 rec, int lane, int G, unsigned m
   const bool selfSphere = (ld(&w.b.flags0[i]) & kBodySphere) != 0;
   const bool has0 = lane < nm;
   ContactData<T> d0;
-  if (has0) d0 = load_contact<T>(w, ld(&w.a.centry[cb + lane]));
+  if (has0) d0 = load_contact<T, E>(w, ld(&w.a.centry[cb + lane]), alpha);
   const bool extra = total > nm || nm > G;  // joints, springs or more contacts than lanes
   Sys<T> s;
   zero(s);
   if (lane == 0) inertial_terms<T>(w, i, self, selfSphere, s);
   if (has0) contact_primal<T>(d0, self, alpha, s);
-  if (extra) extra_primal<T>(w, i, cb, nm, cStart, total, lane, G, self, alpha, s);
+  if (extra) extra_primal<T, E>(w, i, cb, nm, cStart, total, lane, G, self, alpha, s);
   if (lane == 0 && ld(&w.grab->body) == i) s = grab_primal<T>(w, i, self, s);
   finish_body<T>(w, i, lane, G, mask, velocity, ld(&w.b.quatT[i]), s, self);
   if (!dual) return;
   // dual updates of the constraints this body owns (it has the larger colour)
   if (has0 && d0.owned) contact_dual<T>(w, d0, self, alpha);
-  if (extra) extra_dual<T>(w, i, cb, nm, cStart, total, lane, G, self, alpha);
+  if (extra) extra_dual<T, E>(w, i, cb, nm, cStart, total, lane, G, self, alpha);
 }
 
 // ---------------------------------------------------------------------------
@@ -1601,7 +1647,8 @@ __device__ __forceinline__ void stage_contact(const World &w, int2 ent, float4 *
   cp_async_cg(st + 8 * kSolveBlock, &w.b.dang[ent.y]);
 }
 
-__device__ __forceinline__ ContactData<float> staged_contact(const float4 *st, int2 ent) {
+template <bool E>
+__device__ __forceinline__ ContactData<float> staged_contact(const World &w, const float4 *st, int2 ent, float alpha) {
   ContactData<float> d;
   d.slot = ent.x >> 2;
   d.owned = (ent.x & 2) != 0;
@@ -1611,7 +1658,10 @@ __device__ __forceinline__ ContactData<float> staged_contact(const float4 *st, i
   d.n[1] = V3<float>{b1.x, b1.y, b1.z};
   d.n[2] = V3<float>{b2.x, b2.y, b2.z};
   d.mu = b0.w;
-  d.sphere = b1.w != 0.0f;
+  d.sphere = ((int)b1.w & 1) != 0;
+  d.x.on = false;
+  d.x.skin = ((int)b1.w & 2) != 0;
+  d.x.mud = b2.w;
   d.cA = st[3 * kSolveBlock];
   d.cB = st[4 * kSolveBlock];
   d.cK = st[5 * kSolveBlock];
@@ -1620,6 +1670,11 @@ __device__ __forceinline__ ContactData<float> staged_contact(const float4 *st, i
   d.o.dp = V3<float>{dp.x, dp.y, dp.z};
   d.o.dang = V3<float>{da.x, da.y, da.z};
   d.o.q = Q4<float>{0.f, 0.f, 0.f, 1.f};  // not read by the contact rows
+  if (E) {
+    d.x.on = true;
+    d.x.bias = ld(&w.cur.cX[d.slot]);
+    d.x.projection = w.p.postStabilize && alpha < 0.5f;
+  }
   return d;
 }
 
@@ -1682,7 +1737,7 @@ __device__ __forceinline__ int stage_chunk(const World &w, int cb, int lane, int
 // Out of line, so the body state and the partial system go by value and come
 // back as the return value: a reference would let their address escape and
 // keep them in local memory through the whole contact loop of every body.
-template <class T>
+template <class T, bool E>
 __device__ __noinline__ Sys<T> constraints_primal(const World &w, int nm, int cStart, int total, int lane, int G,
                                                   const BState<T> self, T alpha, Sys<T> s) {
   for (int e = first_extra(lane, nm, G); e < total; e += G) {
@@ -1694,7 +1749,7 @@ __device__ __noinline__ Sys<T> constraints_primal(const World &w, int nm, int cS
   return s;
 }
 
-template <class T>
+template <class T, bool E>
 __device__ __noinline__ void constraints_dual(const World &w, int i, int nm, int cStart, int total, int lane, int G,
                                               const BState<T> self, T alpha) {
   const int myColor = ld(&w.b.color[i]);
@@ -1723,6 +1778,7 @@ __device__ __noinline__ void tail_wait_extra(const World &w, int nm, int cStart,
 }
 
 // `tw`: the tail waits of this body (null outside the tail segment).
+template <bool E>
 __device__ void solve_body_staged(const World &w, int4 rec, int lane, int G, unsigned mask, float alpha, bool dual,
                                   bool velocity, float4 *stage, const TailWait *tw = nullptr) {
   using T = float;
@@ -1751,7 +1807,7 @@ __device__ void solve_body_staged(const World &w, int4 rec, int lane, int G, uns
   for (int k0 = 0;;) {
     cp_async_wait_all();
     for (int j = 0; j < cnt; j++)
-      contact_primal<T>(staged_contact(stage + j * kStageVecs * kSolveBlock, ent[j]), self, alpha, s);
+      contact_primal<T>(staged_contact<E>(w, stage + j * kStageVecs * kSolveBlock, ent[j], alpha), self, alpha, s);
     k0 += cnt;
     if (k0 >= nk) break;
     cnt = nk - k0 < kStageSlots ? nk - k0 : kStageSlots;
@@ -1759,7 +1815,7 @@ __device__ void solve_body_staged(const World &w, int4 rec, int lane, int G, uns
   }
   if (total > nm) {
     if (tw) tail_wait_extra(w, nm, cStart, total, lane, G, *tw);
-    s = constraints_primal<T>(w, nm, cStart, total, lane, G, self, alpha, s);
+    s = constraints_primal<T, E>(w, nm, cStart, total, lane, G, self, alpha, s);
   }
   if (grabbed) s = grab_primal<T>(w, i, self, s);
   // in the tail segment the body's progress is published as soon as its state is stored: the
@@ -1772,7 +1828,7 @@ __device__ void solve_body_staged(const World &w, int4 rec, int lane, int G, uns
     // contact's multiplier and penalty, and the other body is done with
     // this iteration, so the staged values are current
     for (int j = 0; j < cnt; j++)
-      if (ent[j].x & 2) contact_dual<T>(w, staged_contact(stage + j * kStageVecs * kSolveBlock, ent[j]), self, alpha);
+      if (ent[j].x & 2) contact_dual<T>(w, staged_contact<E>(w, stage + j * kStageVecs * kSolveBlock, ent[j], alpha), self, alpha);
   } else {
     for (int k0 = 0; k0 < nk; k0 += kStageSlots) {
       const int c2 = nk - k0 < kStageSlots ? nk - k0 : kStageSlots;
@@ -1780,18 +1836,19 @@ __device__ void solve_body_staged(const World &w, int4 rec, int lane, int G, uns
       cp_async_wait_all();
       for (int j = 0; j < c2; j++)
         if (ent[j].x & 2)
-          contact_dual<T>(w, staged_contact(stage + j * kStageVecs * kSolveBlock, ent[j]), self, alpha);
+          contact_dual<T>(w, staged_contact<E>(w, stage + j * kStageVecs * kSolveBlock, ent[j], alpha), self, alpha);
     }
   }
-  if (total > nm) constraints_dual<T>(w, i, nm, cStart, total, lane, G, self, alpha);
+  if (total > nm) constraints_dual<T, E>(w, i, nm, cStart, total, lane, G, self, alpha);
 }
 
 // The FP64 path is kept out of line so that its register demand (and any
 // spills under the 2-blocks-per-SM bound) stays in the rare FP64 bodies
 // instead of lowering the occupancy of the FP32 path.
+template <bool E>
 __device__ __noinline__ void solve_body_f64(const World &w, int4 rec, int lane, int G, unsigned mask, double alpha,
                                             bool dual, bool velocity) {
-  solve_body<double>(w, rec, lane, G, mask, alpha, dual, velocity);
+  solve_body<double, E>(w, rec, lane, G, mask, alpha, dual, velocity);
 }
 
 // The neighbours come from the body's manifold list (one entry per touching
@@ -1861,6 +1918,7 @@ __device__ __forceinline__ void group_sync(int G, unsigned mask) {
 // body always has its inputs ready (all blocks are resident).
 constexpr int kTailDiv = 8;  // default of SolverParams::tailDiv
 constexpr int kChunkCache = 64;  // colours whose chunk bounds the solve keeps in shared memory
+template <bool E>
 __global__ void __launch_bounds__(kSolveBlock, 3) solve_kernel(World w) {
   if (step_skipped(w)) return;
   extern __shared__ float4 stageSm[];
@@ -1894,8 +1952,8 @@ __global__ void __launch_bounds__(kSolveBlock, 3) solve_kernel(World w) {
         const int lane = threadIdx.x & (G - 1);
         const unsigned mask = G >= 32 ? 0xffffffffu : (((1u << G) - 1u) << (warpLane & ~(G - 1)));
         const int4 rec = ld(&w.a.colorRec[e >> 4]);
-        if (e & 8) solve_body_f64(w, rec, lane, G, mask, alpha, dual, vel);
-        else solve_body_staged(w, rec, lane, G, mask, (float)alpha, dual, vel, stage);
+        if (e & 8) solve_body_f64<E>(w, rec, lane, G, mask, alpha, dual, vel);
+        else solve_body_staged<E>(w, rec, lane, G, mask, (float)alpha, dual, vel, stage);
       }
       if (!grid_barrier(ctl, w.p.barrierLimit)) return;
     }
@@ -1915,13 +1973,13 @@ __global__ void __launch_bounds__(kSolveBlock, 3) solve_kernel(World w) {
           // solved on stale data, and the kernel ends at the next grid barrier
           if (wait_neighbors(w, rec.x, it, lane, G, mask, tail)) {
             __syncwarp(mask);  // every lane's reads after the others' acquires
-            solve_body_f64(w, rec, lane, G, mask, alpha, dual, vel);
+            solve_body_f64<E>(w, rec, lane, G, mask, alpha, dual, vel);
           }
           group_sync(G, mask);  // the group's writes before lane 0's release
           if (lane == 0) st_release(&w.b.progress[rec.x], it + 1);
         } else {
           const TailWait tw{tail, c, it + 1};  // publishes the body's progress itself
-          solve_body_staged(w, rec, lane, G, mask, (float)alpha, dual, vel, stage, &tw);
+          solve_body_staged<E>(w, rec, lane, G, mask, (float)alpha, dual, vel, stage, &tw);
         }
       }
       if (!grid_barrier(ctl, w.p.barrierLimit)) return;
@@ -1941,6 +1999,7 @@ __global__ void __launch_bounds__(kSolveBlock, 3) solve_kernel(World w) {
 
 
 
+template <bool E>
 __global__ void __launch_bounds__(kSolveBlock, 3) wave_kernel(World w, int G) {
   if (step_skipped(w)) return;
   extern __shared__ float4 stageSm[];
@@ -1967,8 +2026,8 @@ __global__ void __launch_bounds__(kSolveBlock, 3) wave_kernel(World w, int G) {
         const int i = rec.x;
         if (!wait_neighbors(w, i, it, lane, G, mask)) return;
         __syncwarp(mask);  // orders every lane's reads after the acquires of the others
-        if (ld(&w.b.flags[i]) & kBodyFp64) solve_body_f64(w, rec, lane, G, mask, alpha, dual, vel);
-        else solve_body_staged(w, rec, lane, G, mask, (float)alpha, dual, vel, stage);
+        if (ld(&w.b.flags[i]) & kBodyFp64) solve_body_f64<E>(w, rec, lane, G, mask, alpha, dual, vel);
+        else solve_body_staged<E>(w, rec, lane, G, mask, (float)alpha, dual, vel, stage);
         // the warp barrier orders every lane's writes before lane 0's release,
         // which makes them visible at gpu scope to whoever acquires the flag
         __syncwarp(mask);
@@ -2141,12 +2200,16 @@ cudaError_t launch_joint_anchor(const World &w, int joint, double x, double y, d
 
 int solve_max_blocks_per_sm(int lanesPerBody) {
   (void)lanesPerBody;
-  cudaFuncSetAttribute(solve_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSolveSmem);
-  cudaFuncSetAttribute(wave_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSolveSmem);
-  int a = 0, b = 0;
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, solve_kernel, kSolveBlock, kSolveSmem);
-  cudaOccupancyMaxActiveBlocksPerMultiprocessor(&b, wave_kernel, kSolveBlock, kSolveSmem);
-  return a < b ? a : b;
+  const void *kernels[4] = {(const void *)solve_kernel<false>, (const void *)wave_kernel<false>,
+                            (const void *)solve_kernel<true>, (const void *)wave_kernel<true>};
+  int best = 1 << 30;
+  for (const void *k : kernels) {
+    cudaFuncSetAttribute(k, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)kSolveSmem);
+    int a = 0;
+    cudaOccupancyMaxActiveBlocksPerMultiprocessor(&a, k, kSolveBlock, kSolveSmem);
+    best = a < best ? a : best;
+  }
+  return best;
 }
 
 // lanesPerBody: the wavefront schedule's lanes per body (the colour-phase
@@ -2156,11 +2219,14 @@ cudaError_t launch_solve(const World &w, int lanesPerBody, int blocksPerSm, cuda
   int G = lanesPerBody;
   void *args2[] = {&arg, &G};
   void *args1[] = {&arg};
+  // the contact extensions (AVBD_CONTACT_MATERIALS) are a separate
+  // instantiation, so the default kernels carry none of their registers
+  const bool ext = w.p.contactModel != 0;
   if (w.p.schedule == 1)
-    return cudaLaunchCooperativeKernel((const void *)wave_kernel, dim3(blocksPerSm * smCount), dim3(kSolveBlock),
-                                       args2, kSolveSmem, st);
-  return cudaLaunchCooperativeKernel((const void *)solve_kernel, dim3(blocksPerSm * smCount), dim3(kSolveBlock), args1,
-                                     kSolveSmem, st);
+    return cudaLaunchCooperativeKernel(ext ? (const void *)wave_kernel<true> : (const void *)wave_kernel<false>,
+                                       dim3(blocksPerSm * smCount), dim3(kSolveBlock), args2, kSolveSmem, st);
+  return cudaLaunchCooperativeKernel(ext ? (const void *)solve_kernel<true> : (const void *)solve_kernel<false>,
+                                     dim3(blocksPerSm * smCount), dim3(kSolveBlock), args1, kSolveSmem, st);
 }
 
 void launch_commit(const World &w, cudaStream_t st, int smCount) { commit_kernel<<<smCount * 4, 256, 0, st>>>(w); }

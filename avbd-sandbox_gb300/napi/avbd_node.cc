@@ -146,7 +146,13 @@ bool bind_world(napi_env env, napi_value obj, avbd_world *w) {
         !get_array(env, b, "quat", napi_float64_array, 4 * n, &B.quat) ||
         !get_array(env, b, "vel", napi_float64_array, 3 * n, &B.vel) ||
         !get_array(env, b, "omega", napi_float64_array, 3 * n, &B.omega) ||
-        !get_array(env, b, "prevVel", napi_float64_array, 3 * n, &B.prev_vel))
+        !get_array(env, b, "prevVel", napi_float64_array, 3 * n, &B.prev_vel) ||
+        // contact materials (Rigid.setMaterial, rigid.js:144-214), each optional
+        !get_array(env, b, "staticFriction", napi_float64_array, n, &B.static_friction) ||
+        !get_array(env, b, "dynamicFriction", napi_float64_array, n, &B.dynamic_friction) ||
+        !get_array(env, b, "restitution", napi_float64_array, n, &B.restitution) ||
+        !get_array(env, b, "contactOffset", napi_float64_array, n, &B.contact_offset) ||
+        !get_array(env, b, "restOffset", napi_float64_array, n, &B.rest_offset))
       return false;
   }
   if (get_object(env, obj, "joints", &j)) {
@@ -203,7 +209,8 @@ bool bind_world(napi_env env, napi_value obj, avbd_world *w) {
         !get_array(env, m, "penalty", napi_float64_array, 3 * K * n, &M.penalty) ||
         !get_array(env, m, "lambda", napi_float64_array, 3 * K * n, &M.lambda) ||
         !get_array(env, m, "stick", napi_int32_array, K * n, &M.stick) ||
-        !get_array(env, m, "order", napi_int32_array, n, &M.order))
+        !get_array(env, m, "order", napi_int32_array, n, &M.order) ||
+        !get_array(env, m, "restitutionBias", napi_float64_array, K * n, &M.restitution_bias))
       return false;
   }
   double ns = 0;
@@ -242,6 +249,12 @@ void bind_params(napi_env env, napi_value obj, avbd_params *p) {
   if (get_number(env, obj, "fp64RatioThreshold", &v)) p->fp64_ratio_threshold = v;
   if (get_number(env, obj, "lanesPerBody", &v)) p->lanes_per_body = (int32_t)v;
   if (get_number(env, obj, "schedule", &v)) p->schedule = (int32_t)v;
+  // the WebGPU engine's contact extensions (solver.js:151-162)
+  if (get_number(env, obj, "contactModel", &v)) p->contact_model = (int32_t)v;
+  if (get_number(env, obj, "contactOffset", &v)) p->contact_offset = v;
+  if (get_number(env, obj, "restOffset", &v)) p->rest_offset = v;
+  if (get_number(env, obj, "restitutionThreshold", &v)) p->restitution_threshold = v;
+  if (get_number(env, obj, "contactPersistence", &v)) p->contact_persistence = v;
 }
 
 napi_value make_double_obj(napi_env env, const char *const *names, const double *vals, int n) {

@@ -21,6 +21,7 @@ const PARAM_NAMES = [
   'dt', 'gravity', 'iterations', 'postStabilize', 'betaLin', 'betaAng', 'alpha', 'gamma',
   'penaltyMin', 'penaltyMax', 'collisionMargin', 'stickThreshold', 'rotatedInertia',
   'springStiffnessRamp', 'springGeometricStiffness', 'cachedContactJacobians',
+  'contactOffset', 'restOffset', 'restitutionThreshold', 'contactPersistence',
 ];
 
 function paramsOf(solver, extra) {
@@ -43,6 +44,9 @@ function toSoA(solver) {
     moment: new Float64Array(3 * n), radius: new Float64Array(n), friction: new Float64Array(n),
     pos: new Float64Array(3 * n), quat: new Float64Array(4 * n), vel: new Float64Array(3 * n),
     omega: new Float64Array(3 * n), prevVel: new Float64Array(3 * n),
+    // contact materials (rigid.js:54-68; read under contactModel 1)
+    staticFriction: new Float64Array(n), dynamicFriction: new Float64Array(n), restitution: new Float64Array(n),
+    contactOffset: new Float64Array(n), restOffset: new Float64Array(n),
   };
   bodies.forEach((b, i) => {
     bodyIndex.set(b, i);
@@ -57,6 +61,12 @@ function toSoA(solver) {
     fill3(B.vel, i, b.velocityLin);
     fill3(B.omega, i, b.velocityAng);
     fill3(B.prevVel, i, b.prevVelocityLin);
+    B.staticFriction[i] = b.staticFriction ?? b.friction;
+    B.dynamicFriction[i] = b.dynamicFriction ?? b.friction;
+    B.restitution[i] = b.restitution ?? 0;
+    // null offsets inherit the solver's (rigid.js:61-67)
+    B.contactOffset[i] = b.contactOffset ?? solver.contactOffset ?? 0.005;
+    B.restOffset[i] = b.restOffset ?? solver.restOffset ?? -0.005;
   });
 
   const joints = [];
@@ -145,7 +155,9 @@ function fromSoA(solver, packed) {
 
 export class CudaBackend {
   constructor(options = {}) {
-    this.options = options; // CUDA-only knobs: lanesPerBody, schedule, fp64RatioThreshold, waitLimit
+    // CUDA-only knobs: lanesPerBody, schedule, fp64RatioThreshold, waitLimit; contactModel: 1 selects the
+    // WebGPU engine's contact extensions (materials, restitution, rest offsets)
+    this.options = options;
     this.handle = null;
     this.paramsKey = '';
     this.packed = null;

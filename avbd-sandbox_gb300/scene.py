@@ -579,3 +579,45 @@ def spheres_scene():
     s.box((1.2, 0.6, 0.8), 1.0, 0.5, (2.5, -1.5, 0.4))
     s.sphere(1.0, 1.0, 0.5, (1.25, -1.48, 0.5), velocity=(3.5, 0.6, 0), omega=(0, 0, 1.3))
     return s
+
+
+def material_scene(kind="pile", seed=7):
+    """Scenes for the WebGPU engine's contact extensions
+    (AVBD_CONTACT_MATERIALS), with seeded per-body materials: static friction
+    U[0.3, 0.9], dynamic friction a U[0.3, 1] fraction of it, restitution
+    U[0, 0.8], rest offsets U[-0.02, -0.005] (the ground keeps the defaults).
+    "pile": a 60-box random pile falling onto the ground; "drop": boxes and
+    spheres thrown down onto the ground and each other fast enough to arm
+    restitution; "spheres": spheres_scene. Returns (scene, materials dict for
+    World.set_materials)."""
+    if kind == "pile":
+        s = random_pile(60, seed)
+    elif kind == "drop":
+        s = Scene("drop")
+        add_ground(s, 0.6)
+        rnd = LCG(seed)
+        for i in range(12):
+            x, y = (i % 4 - 1.5) * 1.6, (i // 4 - 1) * 1.6
+            if i % 3 == 2:
+                s.sphere(rnd.uniform(0.5, 1.0), 800.0, 0.6, (x, y, rnd.uniform(0.6, 1.2)),
+                         velocity=(rnd.uniform(-0.5, 0.5), 0.0, -rnd.uniform(2.0, 4.0)))
+            else:
+                s.box((rnd.uniform(0.5, 1.0), rnd.uniform(0.5, 1.0), rnd.uniform(0.5, 1.0)), 600.0, 0.6,
+                      (x, y, rnd.uniform(0.7, 1.3)), velocity=(rnd.uniform(-0.5, 0.5), 0.0, -rnd.uniform(2.0, 4.0)))
+        s.params = dict(gravity=-9.81, iterations=10)
+    elif kind == "spheres":
+        s = spheres_scene()
+        s.params = dict(gravity=-9.81, iterations=10)
+    else:
+        raise KeyError(kind)
+    rnd = LCG(seed * 7 + 3)
+    n = s.n
+    sf, df, e, ro = [], [], [], []
+    for i in range(n):
+        static = s.b["mass"][i] == 0
+        a = rnd.uniform(0.3, 0.9)
+        sf.append(s.b["friction"][i] if static else a)
+        df.append(s.b["friction"][i] if static else a * rnd.uniform(0.3, 1.0))
+        e.append(0.0 if static else rnd.uniform(0.0, 0.8))
+        ro.append(-0.005 if static else rnd.uniform(-0.02, -0.005))
+    return s, dict(static_friction=sf, dynamic_friction=df, restitution=e, rest_offset=ro)

@@ -128,7 +128,31 @@ typedef struct avbd_params {
      uploaded colouring or avbd_autotune). Profiled steps launch directly.
      Does not change results. */
   int32_t graph;
+  /* Contact model. AVBD_CONTACT_CPU (0, default): the CPU engine's - one
+     friction coefficient, collision_margin on C0, stick = |C_t| below
+     stick_threshold, warm start by feature ID (src/physics/manifold.js).
+     AVBD_CONTACT_MATERIALS (1): the WebGPU engine's contact extensions
+     (src/physics/gpu/shaders.js:1152-1366, 1772-1849, 2235-2260;
+     src/physics/rigid.js:144-214): static and dynamic friction (a contact
+     that was static uses the static cone; once outside it is clamped to
+     the dynamic one), stick = inside the cone, new contacts start static;
+     thresholded restitution (a one-frame bias for new or re-armed impacts);
+     C0 on the normal measured to the rest distance (the pair's rest offsets)
+     with a speculative gap kept unscaled while the pair's contact offsets
+     are positive; warm start by feature ID, then by the nearest old contact
+     within the persistence distance, each old contact claimed once, with
+     multipliers and penalties transported into the new basis. Contact
+     generation stays the CPU collider's (no speculative contacts at a
+     positive separation). */
+  int32_t contact_model;
+  double contact_offset;        /* per-body default, 0.005 (solver.js:151)   */
+  double rest_offset;           /* per-body default, -0.005 (solver.js:152)  */
+  double restitution_threshold; /* 1.0 m/s (solver.js:155)                   */
+  double contact_persistence;   /* 0.002 m (solver.js:162)                   */
 } avbd_params;
+
+#define AVBD_CONTACT_CPU 0
+#define AVBD_CONTACT_MATERIALS 1
 
 /*
  * Bodies, `Rigid` (src/physics/rigid.js:29-133). Static shape/material fields
@@ -148,6 +172,16 @@ typedef struct avbd_body_soa {
   double *vel;        /* 3 per body                                          */
   double *omega;      /* 3 per body                                          */
   double *prev_vel;   /* 3 per body                                          */
+  /* Contact materials of AVBD_CONTACT_MATERIALS (Rigid.setMaterial,
+     src/physics/rigid.js:144-214), each optional (NULL = default): static
+     and dynamic friction (default: friction; pairs combine as sqrt(a b)),
+     restitution in [0, 1] (default 0; pairs take the max), contact and rest
+     offsets (defaults: the params'; pairs add them). */
+  double *static_friction;
+  double *dynamic_friction;
+  double *restitution;
+  double *contact_offset;
+  double *rest_offset;
 } avbd_body_soa;
 
 /* Ball-socket joints, `Joint` (src/physics/joint.js:74-113). */
@@ -208,6 +242,7 @@ typedef struct avbd_manifold_soa {
   double *lambda;         /* 8*3 per manifold                                */
   int32_t *stick;         /* 8 per manifold                                  */
   int32_t *order;         /* optional: position in the global force list     */
+  double *restitution_bias; /* 8 per manifold, AVBD_CONTACT_MATERIALS only  */
 } avbd_manifold_soa;
 
 /*

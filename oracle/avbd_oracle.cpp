@@ -424,6 +424,8 @@ struct Body {
   Real prevVelocityLin[3] = {0, 0, 0};
   Real size[3] = {1, 1, 1};
   Real friction = 0.5;
+  // contact materials (rigid.js:54-68, 144-214)
+  Real staticFriction = 0.5, dynamicFriction = 0.5, restitution = 0, contactOffset = 0.005, restOffset = -0.005;
   Real mass = 0;
   Real moment[3] = {0, 0, 0};
   Real radius = 0;
@@ -483,6 +485,10 @@ struct Params {
   Real penaltyMin = 1, penaltyMax = 1e10, collisionMargin = 0.01, stickThreshold = 1e-5;
   bool rotatedInertia = true, springRamp = false, springGeometric = true, cachedJacobians = true;
   int broadphase = 0, hashThreshold = 150, bodyOrderMode = AVBD_ORDER_REFERENCE;
+  // the WebGPU engine's contact extensions (AVBD_CONTACT_MATERIALS) and their
+  // defaults (solver.js:151-162)
+  int contactModel = AVBD_CONTACT_CPU;
+  Real contactOffset = 0.005, restOffset = -0.005, restitutionThreshold = 1.0, contactPersistence = 0.002;
 };
 
 // ---------------------------------------------------------------------------
@@ -502,11 +508,13 @@ struct Contact {
   Real C0[3] = {0, 0, 0}, penalty[3] = {0, 0, 0}, lambda[3] = {0, 0, 0};
   bool stick = false;
   Real C[3] = {0, 0, 0};
+  Real restitutionBias = 0;  // AVBD_CONTACT_MATERIALS: this step's one-frame normal target
   void copyFrom(const Contact &o) { *this = o; }
   void reset() {
     feature = 0;
     v3_zero(penalty); v3_zero(lambda); v3_zero(C0); v3_zero(C);
     stick = false;
+    restitutionBias = 0;
   }
 };
 
@@ -946,6 +954,10 @@ struct Manifold : Force {
   Real basis[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
   int numContacts = 0;
   Real friction = 0;
+  // AVBD_CONTACT_MATERIALS: the pair's dynamic friction and whether its
+  // contact skin (the sum of the contact offsets) is positive
+  Real dynamicFriction = 0;
+  bool skin = false;
   Real jacobians[MAX_CONTACTS * 18];
   bool jacobiansValid = false;
   // _beginPass scratch
@@ -961,10 +973,11 @@ struct Manifold : Force {
     const bool hasSphere = A.shape == AVBD_SHAPE_SPHERE || B.shape == AVBD_SHAPE_SPHERE;
     const bool hadContacts = numContacts > 0;
     Real oldBasis[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-    if (hasSphere && hadContacts) m3_copy(oldBasis, basis);
+    if ((hasSphere || solver->p.contactModel == AVBD_CONTACT_MATERIALS) && hadContacts) m3_copy(oldBasis, basis);
     friction = sqrt(A.friction * B.friction);
     for (int i = 0; i < MAX_CONTACTS; i++) newContacts[i].reset();
     const int newNum = solver->collider.collide(A, B, newContacts, basis);
+    if (solver->p.contactModel == AVBD_CONTACT_MATERIALS) return initializeMaterials(oldBasis, hadContacts, newNum);
     const bool basisCompatible =
         !hasSphere || !hadContacts || (oldBasis[0] * basis[0] + oldBasis[1] * basis[1] + oldBasis[2] * basis[2]) > 0.85;
     for (int i = 0; i < newNum; i++) {
@@ -1017,6 +1030,143 @@ struct Manifold : Force {
     return numContacts > 0;
   }
 
+  // The WebGPU engine's manifold warm start with its contact extensions
+  // (src/physics/gpu/shaders.js:1105-1366): pair materials (friction as the
+  // geometric mean of static and of dynamic coefficients, restitution as the
+  // max, contact and rest offsets summed); each new contact matches the old
+  // one with its feature ID, else the nearest old contact within the
+  // persistence distance (separation, tangential offset and midpoint
+  // distance all within it), each old contact claimed once and only when the
+  // normals agree (dot > 0.85); multipliers and penalties are transported
+  // into the new basis; a matched static box contact keeps its anchors; a
+  // new contact starts static. C0 on the normal is measured to the rest
+  // distance, and a new or re-armed impact gets a one-frame restitution bias.
+  bool initializeMaterials(const Real *oldBasis, bool hadContacts, int newNum) {
+    Body &A = *bodyA, &B = *bodyB;
+    const Params &P = solver->p;
+    friction = sqrt(A.staticFriction * B.staticFriction);
+    dynamicFriction = sqrt(A.dynamicFriction * B.dynamicFriction);
+    const Real restitution = js_max(A.restitution, B.restitution);
+    const Real contactDistance = A.contactOffset + B.contactOffset;
+    const Real restDistance = A.restOffset + B.restOffset;
+    skin = contactDistance > 0;
+    const Real *newN = &basis[0];
+    const Real *oldN = hadContacts ? &oldBasis[0] : newN;
+    const bool compatible = hadContacts && v3_dot(oldN, newN) > 0.85;
+    const Real minExtent =
+        2.0 * js_min(js_min(A.size[0] * 0.5, js_min(A.size[1] * 0.5, A.size[2] * 0.5)),
+                     js_min(B.size[0] * 0.5, js_min(B.size[1] * 0.5, B.size[2] * 0.5)));
+    const Real persistence = js_max(P.contactPersistence, js_max(contactDistance, minExtent * 0.02));
+    const Real persistenceSq = persistence * persistence;
+    const bool curved = A.shape == AVBD_SHAPE_SPHERE || B.shape == AVBD_SHAPE_SPHERE;
+    unsigned oldUsed = 0;
+    for (int c = 0; c < newNum; c++) {
+      Contact &nc = newContacts[c];
+      Real rA[3], rB[3], pen[3] = {0, 0, 0}, lam[3] = {0, 0, 0};
+      v3_copy(rA, nc.rA);
+      v3_copy(rB, nc.rB);
+      bool priorOutsideRest = false, priorHadBias = false, stick = true;
+      bool found = false, exact = false;
+      int match = -1;
+      Real best = persistenceSq;
+      Real nxA[3], nxB[3], mid[3];
+      transform_point(nxA, A.positionLin, A.positionAng, rA);
+      transform_point(nxB, B.positionLin, B.positionAng, rB);
+      for (int k = 0; k < 3; k++) mid[k] = (nxA[k] + nxB[k]) * 0.5;
+      if (compatible) {
+        for (int o = 0; o < numContacts; o++) {
+          if (oldUsed & (1u << o)) continue;
+          const Contact &oc = contacts[o];
+          const bool same = oc.feature == nc.feature;
+          if (curved && same) {
+            match = o;
+            exact = true;
+            break;
+          }
+          Real oxA[3], oxB[3], od[3], td[3], md[3];
+          transform_point(oxA, A.positionLin, A.positionAng, oc.rA);
+          transform_point(oxB, B.positionLin, B.positionAng, oc.rB);
+          v3_sub(od, oxA, oxB);
+          const Real sep = v3_dot(newN, od);
+          for (int k = 0; k < 3; k++) td[k] = od[k] - newN[k] * sep;
+          if (sep > contactDistance + persistence) continue;
+          if (v3_dot(td, td) > persistenceSq) continue;
+          for (int k = 0; k < 3; k++) md[k] = mid[k] - (oxA[k] + oxB[k]) * 0.5;
+          const Real mdSq = v3_dot(md, md);
+          if (mdSq > persistenceSq) continue;
+          if (same) {
+            match = o;
+            exact = true;
+            break;
+          }
+          if (!found || mdSq < best) {
+            found = true;
+            match = o;
+            best = mdSq;
+          }
+        }
+      }
+      found = found || exact;
+      if (found) {
+        const Contact &oc = contacts[match];
+        oldUsed |= 1u << match;
+        transportMaterials(pen, lam, oc.penalty, oc.lambda, oldBasis, basis);
+        stick = oc.stick;
+        priorOutsideRest = oc.C0[0] > 0;
+        priorHadBias = oc.restitutionBias > 0;
+        if (stick && A.shape != AVBD_SHAPE_SPHERE && B.shape != AVBD_SHAPE_SPHERE) {
+          v3_copy(rA, oc.rA);
+          v3_copy(rB, oc.rB);
+        }
+      }
+      Contact &out = nc;  // newContacts[c] becomes the contact
+      v3_copy(out.rA, rA);
+      v3_copy(out.rB, rB);
+      Real xA[3], xB[3], d[3];
+      transform_point(xA, A.positionLin, A.positionAng, rA);
+      transform_point(xB, B.positionLin, B.positionAng, rB);
+      v3_sub(d, xA, xB);
+      out.C0[0] = v3_dot(&basis[0], d) - restDistance;
+      out.C0[1] = v3_dot(&basis[3], d);
+      out.C0[2] = v3_dot(&basis[6], d);
+      Real bias = 0;
+      const bool armed = !found || (priorOutsideRest && !priorHadBias);
+      if (armed && restitution > 0) {
+        Real wA[3], wB[3], vA[3], vB[3], rel[3];
+        q_rotate(wA, A.positionAng, rA);
+        q_rotate(wB, B.positionAng, rB);
+        v3_cross(vA, A.velocityAng, wA);
+        v3_cross(vB, B.velocityAng, wB);
+        for (int k = 0; k < 3; k++) rel[k] = (A.velocityLin[k] + vA[k]) - (B.velocityLin[k] + vB[k]);
+        const Real vn = v3_dot(newN, rel);
+        const Real closing = js_max(0.0, -vn * P.dt);
+        const Real toRest = js_max(0.0, out.C0[0]);
+        if (vn < -P.restitutionThreshold && closing > toRest) bias = restitution * (closing - toRest);
+      }
+      out.restitutionBias = bias;
+      if (!P.postStabilize)
+        for (int k = 0; k < 3; k++) lam[k] = lam[k] * P.alpha * P.gamma;
+      for (int k = 0; k < 3; k++) out.penalty[k] = js_max(P.penaltyMin, js_min(P.penaltyMax, pen[k] * P.gamma));
+      v3_copy(out.lambda, lam);
+      out.stick = stick;
+    }
+    numContacts = newNum;
+    for (int i = 0; i < newNum; i++) contacts[i].copyFrom(newContacts[i]);
+    return numContacts > 0;
+  }
+  // transportPenalty / transportComponents of the WebGPU engine
+  // (src/physics/gpu/shaders.js:1050-1085): rows of the new basis against the
+  // old basis's rows
+  static void transportMaterials(Real *pen, Real *lam, const Real *oldPen, const Real *oldLam, const Real *oldB,
+                                 const Real *newB) {
+    for (int r = 0; r < 3; r++) {
+      const Real *n = &newB[r * 3];
+      const Real a = v3_dot(n, &oldB[0]), b = v3_dot(n, &oldB[3]), c = v3_dot(n, &oldB[6]);
+      pen[r] = oldPen[0] * (a * a) + oldPen[1] * (b * b) + oldPen[2] * (c * c);
+      lam[r] = oldLam[0] * a + oldLam[1] * b + oldLam[2] * c;
+    }
+  }
+
   // manifold.js:325-350
   static void angularBlocks(const Real *rAW, const Real *rBW, const Real *jALin, const Real *jBLin,
                             Real *jAAng, Real *jBAng) {
@@ -1064,6 +1214,14 @@ struct Manifold : Force {
     m3_diagonal(K, c.penalty[0], c.penalty[1], c.penalty[2]);
     Real acc[3];
     v3_scale(Cv, c.C0, 1 - alpha);
+    const bool materials = solver->p.contactModel == AVBD_CONTACT_MATERIALS;
+    if (materials) {
+      // a positive speculative gap is kept unscaled while the skin is on, and
+      // the restitution target applies outside the projection pass
+      // (shaders.js:1806-1818)
+      if (skin && c.C0[0] > 0) Cv[0] = c.C0[0];
+      if (!(solver->p.postStabilize && alpha < 0.5)) Cv[0] = Cv[0] - c.restitutionBias;
+    }
     m3_mul_vec(acc, jALin, dqALin); v3_add(Cv, Cv, acc);
     m3_mul_vec(acc, jBLin, dqBLin); v3_add(Cv, Cv, acc);
     m3_mul_vec(acc, jAAng, dqAAng); v3_add(Cv, Cv, acc);
@@ -1071,6 +1229,19 @@ struct Manifold : Force {
     m3_mul_vec(F, K, Cv);
     v3_add(F, F, c.lambda);
     F[0] = js_min(F[0], 0);
+    if (materials) {
+      // the static cone while the contact was static, else the dynamic one;
+      // outside it the force is clamped to the dynamic cone (shaders.js:1826-1845)
+      const Real fs = sqrt(F[1] * F[1] + F[2] * F[2]);
+      const Real active = fabs(F[0]) * (c.stick ? friction : dynamicFriction);
+      const bool within = fs <= active;
+      if (!within && fs > 0) {
+        const Real dyn = fabs(F[0]) * dynamicFriction;
+        F[1] = F[1] * dyn / fs;
+        F[2] = F[2] * dyn / fs;
+      }
+      return within;
+    }
     const Real bounds = fabs(F[0]) * friction;
     const Real frictionScale = sqrt(F[1] * F[1] + F[2] * F[2]);
     if (frictionScale > bounds && frictionScale > 0) {
@@ -1123,6 +1294,7 @@ struct Manifold : Force {
       } else if (bodyA->shape == AVBD_SHAPE_SPHERE || bodyB->shape == AVBD_SHAPE_SPHERE) {
         c.stick = false;
       }
+      if (P.contactModel == AVBD_CONTACT_MATERIALS) c.stick = within;  // static = inside the cone (shaders.js:2253-2260)
     }
   }
   Real maxLambda() const override {
@@ -1809,6 +1981,8 @@ static void params_from(Params &p, const avbd_params *a) {
   p.springRamp = a->spring_stiffness_ramp != 0; p.springGeometric = a->spring_geometric_stiffness != 0;
   p.cachedJacobians = a->cached_contact_jacobians != 0; p.broadphase = a->broadphase;
   p.hashThreshold = a->hash_threshold; p.bodyOrderMode = a->body_order;
+  p.contactModel = a->contact_model; p.contactOffset = a->contact_offset; p.restOffset = a->rest_offset;
+  p.restitutionThreshold = a->restitution_threshold; p.contactPersistence = a->contact_persistence;
 }
 
 extern "C" {
@@ -1821,6 +1995,8 @@ void orc_default_params(avbd_params *o) {
   o->rotated_inertia = 1; o->spring_stiffness_ramp = 0; o->spring_geometric_stiffness = 1;
   o->cached_contact_jacobians = 1; o->broadphase = 0; o->hash_threshold = 150;
   o->body_order = AVBD_ORDER_REFERENCE; o->fp64_ratio_threshold = 0; o->schedule = 1;
+  o->contact_model = AVBD_CONTACT_CPU; o->contact_offset = 0.005; o->rest_offset = -0.005;
+  o->restitution_threshold = 1.0; o->contact_persistence = 0.002;
 }
 
 orc_solver *orc_create(const avbd_params *params) {
@@ -1861,6 +2037,13 @@ static void load_manifolds(orc_solver *o, const avbd_manifold_soa &M, std::vecto
         c.C0[k] = M.c0 ? M.c0[slot * 3 + k] : 0;
       }
       c.stick = M.stick ? M.stick[slot] != 0 : false;
+      c.restitutionBias = M.restitution_bias ? M.restitution_bias[slot] : 0;
+    }
+    if (s.p.contactModel == AVBD_CONTACT_MATERIALS) {  // the pair's materials, as initializeMaterials sets them
+      const Body &A = *f->bodyA, &B = *f->bodyB;
+      f->friction = sqrt(A.staticFriction * B.staticFriction);
+      f->dynamicFriction = sqrt(A.dynamicFriction * B.dynamicFriction);
+      f->skin = A.contactOffset + B.contactOffset > 0;
     }
     ordered.push_back({M.order ? M.order[m] : base + m, f});
   }
@@ -1895,6 +2078,11 @@ int orc_load(orc_solver *o, const avbd_world *w) {
     b->mass = B.mass[i];
     b->radius = B.radius[i];
     b->friction = B.friction[i];
+    b->staticFriction = B.static_friction ? B.static_friction[i] : b->friction;
+    b->dynamicFriction = B.dynamic_friction ? B.dynamic_friction[i] : b->friction;
+    b->restitution = B.restitution ? B.restitution[i] : 0;
+    b->contactOffset = B.contact_offset ? B.contact_offset[i] : s.p.contactOffset;
+    b->restOffset = B.rest_offset ? B.rest_offset[i] : s.p.restOffset;
     s.bodies.push_back(b);
   }
   std::vector<std::pair<int, Force *>> ordered;
@@ -2023,6 +2211,7 @@ int orc_read_state(orc_solver *o, avbd_world *w) {
             if (M.lambda) M.lambda[slot * 3 + k] = live ? val(c.lambda[k]) : 0;
           }
           if (M.stick) M.stick[slot] = (i < mf->numContacts && c.stick) ? 1 : 0;
+          if (M.restitution_bias) M.restitution_bias[slot] = i < mf->numContacts ? val(c.restitutionBias) : 0;
         }
         if (M.order) M.order[m] = pos;
       }

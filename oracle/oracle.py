@@ -16,13 +16,18 @@ HERE = os.path.dirname(os.path.abspath(__file__))
 LIB = os.path.join(HERE, "liborc.so")
 LIB_TANGENT = os.path.join(HERE, "liborc_t.so")
 SRC = os.path.join(HERE, "avbd_oracle.cpp")
+HEADER = os.path.join(os.path.dirname(HERE), "include", "avbd_cuda.h")  # the structs it reads
 FLAGS = ["g++", "-std=c++17", "-O2", "-fPIC", "-shared", "-ffp-contract=off", "-fno-fast-math"]
+
+
+def _stale(lib: str) -> bool:
+    return not os.path.exists(lib) or any(os.path.getmtime(lib) < os.path.getmtime(f) for f in (SRC, HEADER))
 
 
 def build(force: bool = False) -> str:
     """Compile the oracle with the flags that keep it a faithful f64
     restatement: no FMA contraction, no fast-math."""
-    if force or not os.path.exists(LIB) or os.path.getmtime(LIB) < os.path.getmtime(SRC):
+    if force or _stale(LIB):
         subprocess.check_call(FLAGS + ["-o", LIB, SRC])
     return LIB
 
@@ -30,7 +35,7 @@ def build(force: bool = False) -> str:
 def build_tangent(force: bool = False) -> str:
     """The tangent oracle: the same source with a forward-mode dual-number
     scalar (-DORC_TANGENT), whose values follow the f64 build's operations."""
-    if force or not os.path.exists(LIB_TANGENT) or os.path.getmtime(LIB_TANGENT) < os.path.getmtime(SRC):
+    if force or _stale(LIB_TANGENT):
         subprocess.check_call(FLAGS + ["-DORC_TANGENT", "-o", LIB_TANGENT, SRC])
     return LIB_TANGENT
 
