@@ -50,6 +50,7 @@ constexpr int kBlock = 256;  // threads of the single-block kernels
 
 struct TBody {
   R p[3], q[4];    // the iterate x (positionLin / positionAng)
+  R dqL[3], dqA[3];  // p - p0 and qsub(q, q0) of the current iterate (what contact rows read), kept with p, q
   R v[3], w[3];    // velocity, angular velocity
   R pv[3];         // previous velocity
   R p0[3], q0[4];  // x_t (initialLin / initialAng)
@@ -100,6 +101,10 @@ struct TWorld {
   TParams P;
   int n, nj, ns;
   TBody *b;
+  // per contact slot of the current manifolds (manifold * 8 + contact): the
+  // angular Jacobian rows of A and B at the x_t orientations (the cached
+  // Jacobians of manifold.js:325-350), computed once per step
+  R *jac;
   TBodyStatic *bs;
   const uint32_t *cRef;
   TJoint *j;
@@ -429,6 +434,22 @@ __device__ geo::BodyT<R> body_geo(const TWorld &w, int i) {
 }
 
 // Manifold.initialize (manifold.js:214-318) of candidate c, at x_t.
+// manifold.js:325-350: the angular Jacobian rows of a contact, rows of
+// rA_world x n_r (A) and rB_world x (-n_r) (B), into out[0..8] and out[9..17]
+__device__ void contact_jacobians(R *out, const R *basis, const R *qA, const R *qB, const R *rA, const R *rB) {
+  R rAW[3], rBW[3], row[3], acc[3];
+  q_rotate(rAW, qA, rA);
+  q_rotate(rBW, qB, rB);
+  for (int r = 0; r < 3; r++) {
+    row[0] = basis[r * 3]; row[1] = basis[r * 3 + 1]; row[2] = basis[r * 3 + 2];
+    v3_cross(acc, rAW, row);
+    out[r * 3] = acc[0]; out[r * 3 + 1] = acc[1]; out[r * 3 + 2] = acc[2];
+    row[0] = -basis[r * 3]; row[1] = -basis[r * 3 + 1]; row[2] = -basis[r * 3 + 2];
+    v3_cross(acc, rBW, row);
+    out[9 + r * 3] = acc[0]; out[9 + r * 3 + 1] = acc[1]; out[9 + r * 3 + 2] = acc[2];
+  }
+}
+
 __global__ void narrow_kernel(TWorld w) {
   const int total = w.ctl[0], prevCount = w.ctl[1];
   const TParams &P = w.P;
@@ -495,6 +516,8 @@ __global__ void narrow_kernel(TWorld w) {
         if (!P.postStabilize) t.lam[k] = (t.lam[k] * P.alpha) * P.gamma;
         t.pen[k] = clampR(t.pen[k] * P.gamma, R(P.penaltyMin), P.penaltyMax);
       }
+      if (P.cachedJacobians)  // the orientations here are the step's x_t ones
+        contact_jacobians(&w.jac[((size_t)c * K8 + i) * 18], m.basis, bA.q, bB.q, t.rA, t.rB);
     }
   }
 }
@@ -596,6 +619,8 @@ __global__ void bodies_init_kernel(TWorld w) {
       q_integrate(q1, b.q, tmp);
       for (int k = 0; k < 4; k++) b.q[k] = q1[k];
     }
+    v3_sub(b.dqL, b.p, b.p0);
+    q_subtract(b.dqA, b.q, b.q0);
   }
 }
 
@@ -716,23 +741,23 @@ struct ContactEvalT {
 __device__ ContactEvalT contact_eval(const TWorld &w, const TManifold &m, int i, R alpha, R *jAAng, R *jBAng) {
   const TBody &A = w.b[m.a], &B = w.b[m.b];
   const TContact &c = m.c[i];
-  R dqALin[3], dqAAng[3], dqBLin[3], dqBAng[3], jBLin[9];
-  v3_sub(dqALin, A.p, A.p0);
-  q_subtract(dqAAng, A.q, A.q0);
-  v3_sub(dqBLin, B.p, B.p0);
-  q_subtract(dqBAng, B.q, B.q0);
+  // the bodies' displacements from x_t, kept with their iterates
+  const R *dqALin = A.dqL, *dqAAng = A.dqA, *dqBLin = B.dqL, *dqBAng = B.dqA;
+  R jBLin[9], acc[3];
   for (int k = 0; k < 9; k++) jBLin[k] = -m.basis[k];
-  R rAW[3], rBW[3], row[3], acc[3];
-  // cached Jacobians: the contact arms at the x_t orientations (manifold.js:325-350)
-  q_rotate(rAW, w.P.cachedJacobians ? A.q0 : A.q, c.rA);
-  q_rotate(rBW, w.P.cachedJacobians ? B.q0 : B.q, c.rB);
-  for (int r = 0; r < 3; r++) {  // manifold.js:325-350
-    row[0] = m.basis[r * 3]; row[1] = m.basis[r * 3 + 1]; row[2] = m.basis[r * 3 + 2];
-    v3_cross(acc, rAW, row);
-    jAAng[r * 3] = acc[0]; jAAng[r * 3 + 1] = acc[1]; jAAng[r * 3 + 2] = acc[2];
-    row[0] = jBLin[r * 3]; row[1] = jBLin[r * 3 + 1]; row[2] = jBLin[r * 3 + 2];
-    v3_cross(acc, rBW, row);
-    jBAng[r * 3] = acc[0]; jBAng[r * 3 + 1] = acc[1]; jBAng[r * 3 + 2] = acc[2];
+  if (w.P.cachedJacobians) {  // computed once per step at the x_t orientations (narrow_kernel)
+    const R *jc = &w.jac[((size_t)(&m - w.cur) * K8 + i) * 18];
+    for (int k = 0; k < 9; k++) {
+      jAAng[k] = jc[k];
+      jBAng[k] = jc[9 + k];
+    }
+  } else {
+    R jc[18];
+    contact_jacobians(jc, m.basis, A.q, B.q, c.rA, c.rB);
+    for (int k = 0; k < 9; k++) {
+      jAAng[k] = jc[k];
+      jBAng[k] = jc[9 + k];
+    }
   }
   ContactEvalT e;
   for (int k = 0; k < 3; k++) e.C[k] = c.C0[k] * (1.0 - alpha);
@@ -1005,6 +1030,8 @@ __device__ void body_update_warp(const TWorld &w, int i, R alpha, BodySmem &sm) 
     R q1[4];
     q_integrate(q1, b.q, xa);
     for (int k = 0; k < 4; k++) b.q[k] = q1[k];
+    v3_sub(b.dqL, b.p, b.p0);
+    q_subtract(b.dqA, b.q, b.q0);
   }
   __syncwarp();
 }
@@ -1385,7 +1412,7 @@ int tangent_pack(TangentCtx **out, const avbd_world *world, const avbd_params &P
       (e = t->alloc(&w.prev, w.mcap)) || (e = t->alloc(&w.prevKey, w.mcap)) || (e = t->alloc(&w.ctl, 8)) ||
       (e = t->alloc(&w.fStart, n + 1)) || (e = t->alloc(&w.fCount, n + 1)) || (e = t->alloc(&w.fRef, w.fcap)) ||
       (e = t->alloc(&w.color, n)) || (e = t->alloc(&w.order, n)) || (e = t->alloc(&w.colorStart, kMaxColors + 1)) ||
-      (e = t->alloc(&prioD, n))) {
+      (e = t->alloc(&prioD, n)) || (e = t->alloc(&w.jac, (size_t)w.mcap * K8 * 18))) {
     delete t;
     snprintf(msg, msgLen, "avbd_adjoint_forward: cudaMalloc: %s", cudaGetErrorString(e));
     return AVBD_ERR_CUDA;

@@ -757,12 +757,21 @@ def main():
     ap.add_argument("--dense-start", type=int, default=300, help="step the crushed-pile window starts after")
     ap.add_argument("--dense-steps", type=int, default=20, help="timed steps of the crushed-pile window (0: skip)")
     ap.add_argument("--adjoint-steps", type=int, default=60, help="steps of the differentiable wall (0: skip)")
+    ap.add_argument("--only", default="", choices=["", "adjoint"],
+                    help="run one record alone and print it (for profiling): adjoint = the differentiable wall")
     ap.add_argument("--trace", default="", help="write each timed step's profile and counters (JSON lines)")
     args = ap.parse_args()
     if args.warmup < 3:
         args.warmup = 3
     if args.impl == "reference":
         run_reference(args)
+    elif args.only == "adjoint":
+        import torch
+
+        torch.cuda.set_device(0)
+        abi = pkg().abi
+        backend = importlib.import_module("avbd-sandbox_gb300.backend")
+        print(json.dumps({"adjoint": run_adjoint(abi, backend, args)}), flush=True)
     else:
         run_gpu(args)
 
