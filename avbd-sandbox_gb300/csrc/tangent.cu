@@ -300,30 +300,54 @@ constexpr int kSysEntries = 33;
 static_assert(sizeof(Sys6) == kSysEntries * sizeof(R), "Sys6 is 33 contiguous entries");
 
 // The recording form of a body's system: one constraint's contribution as
-// the sequence of addends it adds to each entry (at most kMaxAdd: a joint's
-// angular diagonal gets its rows, its geometric stiffness and its angular
-// rows), so that the addends of many constraints, computed by different
-// lanes, are summed afterwards in the f64 engine's order.
+// the sequence of addends it adds to each entry, so that the addends of many
+// constraints, computed by different threads, are summed afterwards in the
+// f64 engine's order. An entry has room for the most addends one row makes
+// to it: a joint's angular diagonal gets its rows, its geometric stiffness
+// and its angular rows (3), the angular off-diagonal and the angular
+// right-hand side two, a spring's linear diagonal two (its geometric
+// stiffness), every other entry one - 51 slots per row.
 constexpr int kMaxAdd = 3;
+// room per entry: lin (diagonal 2), ang (diagonal 3, off-diagonal 2), cross, bl, ba
+__device__ __forceinline__ int rec_cap(int e) {
+  return e < 9 ? ((e == 0 || e == 4 || e == 8) ? 2 : 1)
+       : e < 18 ? ((e == 9 || e == 13 || e == 17) ? 3 : 2)
+       : e < 30 ? 1
+       : 2;
+}
+// first slot of entry e: the caps above summed
+__device__ __forceinline__ int rec_off(int e) {
+  if (e < 9) return e + (e > 0) + (e > 4);             // lin: 12 slots
+  if (e < 18) {                                         // ang: 21 slots from 12
+    const int k = e - 9;
+    return 12 + 2 * k + (k > 0) + (k > 4);
+  }
+  if (e < 30) return 33 + (e - 18);                     // cross, bl: 12 slots from 33
+  return 45 + 2 * (e - 30);                             // ba: 6 slots from 45
+}
+constexpr int kRecSlots = 51;
 struct RecElem {
   R *slot;
   unsigned char *cnt;
+  int cap;
   __device__ void operator+=(const R &x) const {
     const int k = *cnt;
-    if (k < kMaxAdd) slot[k] = x;
-    *cnt = (unsigned char)(k + 1);  // > kMaxAdd is reported by the replay
+    if (k < cap) slot[k] = x;
+    *cnt = (unsigned char)(k + 1);  // above the entry's room: reported by the replay
   }
 };
 struct RecRow {
   R *slot;
   unsigned char *cnt;
-  __device__ RecElem operator[](int e) const { return RecElem{slot + e * kMaxAdd, cnt + e}; }
+  int base;  // first entry of the row
+  __device__ RecElem operator[](int e) const {
+    return RecElem{slot + rec_off(base + e), cnt + base + e, rec_cap(base + e)};
+  }
 };
 struct RecSys6 {
   RecRow lin, ang, cross, bl, ba;
   __device__ RecSys6(R *slots, unsigned char *cnt)
-      : lin{slots, cnt}, ang{slots + 9 * kMaxAdd, cnt + 9}, cross{slots + 18 * kMaxAdd, cnt + 18},
-        bl{slots + 27 * kMaxAdd, cnt + 27}, ba{slots + 30 * kMaxAdd, cnt + 30} {}
+      : lin{slots, cnt, 0}, ang{slots, cnt, 9}, cross{slots, cnt, 18}, bl{slots, cnt, 27}, ba{slots, cnt, 30} {}
 };
 
 __device__ __forceinline__ bool is_dynamic(const TWorld &w, int i) { return i >= 0 && w.bs[i].mass > 0; }
@@ -928,25 +952,53 @@ __device__ void spring_primal(const TWorld &w, const TSpring &sp, int side, Sink
   }
 }
 
-// One body's update (solver.js:425-457) by one warp. The body's constraint
-// rows - each contact of each manifold, each joint, each spring, newest force
-// first - go to the lanes 32 at a time; every lane records the addends its
-// row makes to each of the 33 system entries (RecSys6), and lane e then adds
-// the recorded addends of entry e row after row: every entry is summed in the
-// f64 engine's order, so the values stay the serial update's.
-constexpr int kWarp = 32;
+// One body's update (solver.js:425-457) by one block of kBodyThreads. The
+// body's constraint rows - each contact of each manifold, each joint, each
+// spring, newest force first - go to the threads kBodyThreads at a time;
+// every thread records the addends its row makes to each of the 33 system
+// entries (RecSys6), and thread e then adds the recorded addends of entry e
+// row after row: every entry is summed in the f64 engine's order, so the
+// values stay the serial update's. The inertial terms (the entries' first
+// values) are formed by the last thread while the first threads walk the
+// body's force list.
+constexpr int kBodyThreads = 64;
 struct BodySmem {
-  R rec[kWarp][kSysEntries * kMaxAdd];  // lane's row: its addends per entry
-  unsigned char cnt[kWarp][kSysEntries + 3];
-  R acc[kSysEntries];                   // the entries, summed so far
-  uint32_t items[kWarp];                // (force entry << 3) | contact
+  R rec[kBodyThreads][kRecSlots];  // a thread's row: its addends per entry
+  unsigned char cnt[kBodyThreads][kSysEntries + 3];
+  R acc[kSysEntries];              // the entries, summed so far
+  uint32_t items[kBodyThreads];    // (force entry << 3) | contact
   int nItems, cursorE, cursorC;
 };
 
-__device__ void body_update_warp(const TWorld &w, int i, R alpha, BodySmem &sm) {
+// The next (up to) kBodyThreads rows of body i's force list, from the cursor.
+__device__ void next_rows(const TWorld &w, int i, BodySmem &sm) {
+  int n = 0, e = sm.cursorE, c = sm.cursorC;
+  const int e0 = w.fStart[i];
+  while (n < kBodyThreads && e >= e0) {
+    const uint32_t ref = w.fRef[e];
+    if ((ref >> 30) == 0) {
+      if (c < w.cur[(ref >> 1) & 0x1fffffffu].count) {
+        sm.items[n++] = ((uint32_t)e << 3) | (uint32_t)c;
+        c++;
+        continue;
+      }
+      e--;
+      c = 0;
+      continue;
+    }
+    sm.items[n++] = (uint32_t)e << 3;
+    e--;
+    c = 0;
+  }
+  sm.nItems = n;
+  sm.cursorE = e;
+  sm.cursorC = c;
+}
+
+__device__ void body_update_block(const TWorld &w, int i, R alpha, BodySmem &sm) {
   const TParams &P = w.P;
-  const int lane = threadIdx.x;
-  if (lane == 0) {
+  const int t = threadIdx.x, nt = blockDim.x;
+  if (t == nt - 1) {  // the inertial terms
     TBody &b = w.b[i];
     const TBodyStatic &st = w.bs[i];
     const double dt2 = P.dt * P.dt;
@@ -962,60 +1014,41 @@ __device__ void body_update_warp(const TWorld &w, int i, R alpha, BodySmem &sm) 
     m3_mul_vec(s.ba, s.ang, dq);
     const R *e = &s.lin[0];
     for (int k = 0; k < kSysEntries; k++) sm.acc[k] = e[k];
+  }
+  if (t == 0) {
     sm.cursorE = w.fStart[i + 1] - 1;  // the body's forces, newest first
     sm.cursorC = 0;
+    next_rows(w, i, sm);
   }
-  __syncwarp();
+  __syncthreads();
   for (;;) {
-    if (lane == 0) {  // the next (up to) 32 rows
-      int n = 0, e = sm.cursorE, c = sm.cursorC;
-      const int e0 = w.fStart[i];
-      while (n < kWarp && e >= e0) {
-        const uint32_t ref = w.fRef[e];
-        if ((ref >> 30) == 0) {
-          if (c < w.cur[(ref >> 1) & 0x1fffffffu].count) {
-            sm.items[n++] = ((uint32_t)e << 3) | (uint32_t)c;
-            c++;
-            continue;
-          }
-          e--;
-          c = 0;
-          continue;
-        }
-        sm.items[n++] = (uint32_t)e << 3;
-        e--;
-        c = 0;
-      }
-      sm.nItems = n;
-      sm.cursorE = e;
-      sm.cursorC = c;
-    }
-    __syncwarp();
     const int n = sm.nItems;
     if (n == 0) break;
-    if (lane < n) {
-      for (int k = 0; k < kSysEntries; k++) sm.cnt[lane][k] = 0;
-      RecSys6 rs(sm.rec[lane], sm.cnt[lane]);
-      const uint32_t item = sm.items[lane];
+    if (t < n) {
+      for (int k = 0; k < kSysEntries; k++) sm.cnt[t][k] = 0;
+      RecSys6 rs(sm.rec[t], sm.cnt[t]);
+      const uint32_t item = sm.items[t];
       const uint32_t ref = w.fRef[item >> 3];
       const uint32_t type = ref >> 30, idx = (ref >> 1) & 0x1fffffffu, side = ref & 1u;
       if (type == 0) contact_primal(w, w.cur[idx], (int)(item & 7u), (int)side, alpha, rs);
       else if (type == kRefJoint) joint_primal(w, w.j[idx], (int)side, alpha, rs);
       else spring_primal(w, w.s[idx], (int)side, rs, P);
     }
-    __syncwarp();
-    for (int entry = lane; entry < kSysEntries; entry += kWarp) {
+    __syncthreads();
+    for (int entry = t; entry < kSysEntries; entry += nt) {
       R a = sm.acc[entry];
+      const int cap = rec_cap(entry), off = rec_off(entry);
       for (int it = 0; it < n; it++) {
         const int k = sm.cnt[it][entry];
-        if (k > kMaxAdd) w.ctl[7] = 1;  // more addends than recorded: the result is not the serial sum
-        for (int q = 0; q < k && q < kMaxAdd; q++) a += sm.rec[it][entry * kMaxAdd + q];
+        if (k > cap) w.ctl[7] = 1;  // more addends than recorded: the result is not the serial sum
+        for (int q = 0; q < k && q < cap; q++) a += sm.rec[it][off + q];
       }
       sm.acc[entry] = a;
     }
-    __syncwarp();
+    if (t == nt - 1) next_rows(w, i, sm);  // the rows are recorded; the replay reads only rec and cnt
+    __syncthreads();
   }
-  if (lane == 0) {
+  if (t == 0) {
     TBody &b = w.b[i];
     Sys6 s;
     R *e = &s.lin[0];
@@ -1033,7 +1066,7 @@ __device__ void body_update_warp(const TWorld &w, int i, R alpha, BodySmem &sm) 
     v3_sub(b.dqL, b.p, b.p0);
     q_subtract(b.dqA, b.q, b.q0);
   }
-  __syncwarp();
+  __syncthreads();
 }
 
 // manifold.js:447-491, contact i of the manifold (the contacts' dual updates
@@ -1130,13 +1163,13 @@ __device__ bool tg_grid_sync(const TWorld &w) {
   return ok != 0;
 }
 
-// The iterations of one step (cooperative: one warp per block, blocks spread
-// over the SMs, FP64 being the bound): per iteration the colour phases (a
-// warp per body; bodies of one colour are independent), then every force's
+// The iterations of one step (cooperative: one block of kBodyThreads per SM,
+// latency being the bound): per iteration the colour phases (a block per
+// body; bodies of one colour are independent), then every force's
 // dual update (a thread per contact, joint, spring), and on the last
 // iteration the BDF1 velocity (solver.js:476-488); a grid barrier between
 // phases.
-__global__ void __launch_bounds__(kWarp) iterate_kernel(TWorld w) {
+__global__ void __launch_bounds__(kBodyThreads) iterate_kernel(TWorld w) {
   if (w.ctl[2]) return;
   extern __shared__ __align__(16) unsigned char smemRaw[];
   BodySmem &sm = *reinterpret_cast<BodySmem *>(smemRaw);
@@ -1149,7 +1182,7 @@ __global__ void __launch_bounds__(kWarp) iterate_kernel(TWorld w) {
     const R alpha = P.postStabilize ? (it < P.iterations ? 1.0 : 0.0) : P.alpha;
     for (int c = 0; c < numColors; c++) {
       const int c0 = w.colorStart[c], cn = w.colorStart[c + 1] - c0;
-      for (int k = blockIdx.x; k < cn; k += gridDim.x) body_update_warp(w, w.order[c0 + k], alpha, sm);
+      for (int k = blockIdx.x; k < cn; k += gridDim.x) body_update_block(w, w.order[c0 + k], alpha, sm);
       if (!tg_grid_sync(w)) return;
     }
     if (it < P.iterations) {
@@ -1241,7 +1274,7 @@ struct TangentCtx {
   tg::TWorld w{};
   std::vector<void *> allocs;
   int smCount = 0;
-  int iterGrid = 0;  // blocks of the cooperative iterate kernel (one warp each)
+  int iterGrid = 0;  // blocks of the cooperative iterate kernel (kBodyThreads each)
   ~TangentCtx() {
     for (void *p : allocs) cudaFree(p);
   }
@@ -1432,7 +1465,7 @@ int tangent_pack(TangentCtx **out, const avbd_world *world, const avbd_params &P
   int perSm = 0;
   e = cudaFuncSetAttribute(iterate_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)sizeof(BodySmem));
   if (e == cudaSuccess)
-    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, iterate_kernel, kWarp, sizeof(BodySmem));
+    e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&perSm, iterate_kernel, kBodyThreads, sizeof(BodySmem));
   if (e != cudaSuccess || perSm < 1) {
     delete t;
     snprintf(msg, msgLen, "avbd_adjoint_forward: the iterate kernel cannot be made resident (%s)",
@@ -1467,7 +1500,7 @@ int tangent_step(TangentCtx *t, int steps, void *temp, size_t tempBytes, char *m
     adjacency_coloring_kernel<<<1, kBlock, 0, st>>>(w);
     {
       void *args[] = {(void *)&w};
-      const cudaError_t le = cudaLaunchCooperativeKernel((const void *)iterate_kernel, dim3(t->iterGrid), dim3(kWarp),
+      const cudaError_t le = cudaLaunchCooperativeKernel((const void *)iterate_kernel, dim3(t->iterGrid), dim3(kBodyThreads),
                                                          args, sizeof(BodySmem), st);
       if (le != cudaSuccess) {
         snprintf(msg, msgLen, "avbd_adjoint_forward: cooperative launch: %s", cudaGetErrorString(le));
