@@ -157,6 +157,10 @@ struct ColliderT {
   D3 mid[kMaxContactsG];
   int count = 0;
   NewContact *out;
+  // the pair's contact skin: contacts are generated up to this separation
+  // (AVBD_CONTACT_MATERIALS, the WGSL collider's contactDistance,
+  // src/physics/gpu/shaders.js:716-886, 1039); 0 for the CPU engine's collider
+  double cd = 0.0;
 
   __device__ ColliderT(const BodyD &a, const BodyD &b, NewContact *o) : A(a), B(b), out(o) {}
 
@@ -251,7 +255,7 @@ struct ColliderT {
     const R rB = boxB.h.x * fabs(dt3(n, boxB.ax[0])) + boxB.h.y * fabs(dt3(n, boxB.ax[1])) +
                  boxB.h.z * fabs(dt3(n, boxB.ax[2]));
     const R separation = distance - (rA + rB);
-    if (separation > 0) return false;
+    if (separation > cd) return false;
     if (!t.valid || separation > t.sep) {
       t.valid = true; t.type = type; t.ia = ia; t.ib = ib; t.sep = separation; t.n = n;
     }
@@ -357,7 +361,7 @@ struct ColliderT {
     for (int i = 0; i < n && count < kMaxContactsG; i++) {
       const D3 p = clip0[i];
       const R distance = dt3(sub(p, fC), fN);
-      if (distance > kPlaneEps) continue;
+      if (distance > cd + kPlaneEps) continue;
       const D3 proj = adds(p, fN, -distance);
       if (refIsA) addContact(proj, p, prefix | (uint32_t)(i & 0xff));
       else addContact(p, proj, prefix | (uint32_t)(i & 0xff));
@@ -382,7 +386,7 @@ struct ColliderT {
   __device__ int sphereSphere(R *basis) {
     const D3 delta = sub(B.p, A.p);
     const R d2 = delta.x * delta.x + delta.y * delta.y + delta.z * delta.z;
-    const R rs = A.radius + B.radius;
+    const R rs = A.radius + B.radius + cd;
     if (d2 > rs * rs) return 0;
     D3 n = d2 > kSphereEpsSq ? scl(delta, 1 / sqrt(d2)) : unit(0);
     orthonormal(basis, neg(n));
@@ -412,7 +416,7 @@ struct ColliderT {
     D3 n;
     if (d2 > kSphereEpsSq) {
       const R d = sqrt(d2);
-      if (d > sp.radius) return 0;
+      if (d - sp.radius > cd) return 0;
       n = scl(t3, 1 / d);
     } else {
       const R gx = boxA.h.x - fabs(lx), gy = boxA.h.y - fabs(ly), gz = boxA.h.z - fabs(lz);

@@ -877,6 +877,23 @@ int avbd_pack(avbd_ctx *ctx, const avbd_world *world) {
   for (int s = 0; s < S; s++)
     for (int i = sceneStart[s]; i < sceneStart[s + 1]; i++) scene[i] = s;
 
+  // The broad phase's reach per body: the bounding radius, plus the contact
+  // offset under AVBD_CONTACT_MATERIALS (pairs within the skin are candidates,
+  // src/physics/gpu/shaders.js:440-442).
+  const bool materials = ctx->params.contact_model == AVBD_CONTACT_MATERIALS;
+  std::vector<double> reach(n);
+  for (int i = 0; i < n; i++) {
+    reach[i] = B.radius[i];
+    if (materials) {
+      const double co = B.contact_offset ? B.contact_offset[i] : ctx->params.contact_offset;
+      if (!(co >= 0) || !std::isfinite(co)) return fail(ctx, AVBD_ERR_ARG, "body %d: contact offset must be >= 0", i);
+      reach[i] = B.radius[i] + co;
+      const int shape = B.shape ? B.shape[i] : AVBD_SHAPE_BOX;
+      if (shape == AVBD_SHAPE_SPHERE && B.radius[i] != B.size[i * 3] * 0.5)
+        return fail(ctx, AVBD_ERR_ARG, "body %d: a sphere's radius must be half its size (Rigid.sphere)", i);
+    }
+  }
+
   // static body tables
   std::vector<D4> size(n), massD(n);
   std::vector<float4> massF(n);
@@ -890,7 +907,7 @@ int avbd_pack(avbd_ctx *ctx, const avbd_world *world) {
     // remaining radius, padded so rounding cannot separate overlapping bodies
     // by more than one cell.
     const int cnt = sceneStart[s + 1] - sceneStart[s];
-    std::vector<double> radii(B.radius + sceneStart[s], B.radius + sceneStart[s + 1]);
+    std::vector<double> radii(reach.begin() + sceneStart[s], reach.begin() + sceneStart[s + 1]);
     double r95 = 1.0;
     if (cnt > 0) {
       const size_t k = std::min<size_t>((size_t)(0.95 * (cnt - 1)), (size_t)cnt - 1);
@@ -900,7 +917,7 @@ int avbd_pack(avbd_ctx *ctx, const avbd_world *world) {
     const double thr = 2.0 * r95;
     double rmax = 0;
     for (int i = sceneStart[s]; i < sceneStart[s + 1]; i++)
-      if (B.radius[i] <= thr) rmax = std::max(rmax, B.radius[i]);
+      if (reach[i] <= thr) rmax = std::max(rmax, reach[i]);
     const double cell = std::max(2.0 * rmax * (1.0 + 1e-6) + 1e-9, 1e-4);
     invCell[s] = 1.0 / cell;
     for (int i = sceneStart[s]; i < sceneStart[s + 1]; i++) {
@@ -909,7 +926,7 @@ int avbd_pack(avbd_ctx *ctx, const avbd_world *world) {
         return fail(ctx, AVBD_ERR_ARG, "body %d: mass must be finite and >= 0", i);
       if (!(B.radius[i] >= 0) || !std::isfinite(B.radius[i]))
         return fail(ctx, AVBD_ERR_ARG, "body %d: radius must be finite and >= 0", i);
-      size[i] = mkd4(B.size[i * 3], B.size[i * 3 + 1], B.size[i * 3 + 2], B.radius[i]);
+      size[i] = mkd4(B.size[i * 3], B.size[i * 3 + 1], B.size[i * 3 + 2], reach[i]);
       massD[i] = mkd4(B.mass[i], B.moment[i * 3], B.moment[i * 3 + 1], B.moment[i * 3 + 2]);
       massF[i] = make_float4((float)B.mass[i], (float)B.moment[i * 3], (float)B.moment[i * 3 + 1],
                              (float)B.moment[i * 3 + 2]);
@@ -917,7 +934,7 @@ int avbd_pack(avbd_ctx *ctx, const avbd_world *world) {
       int f = 0;
       if (B.mass[i] > 0) f |= kBodyDynamic;
       if (shape == AVBD_SHAPE_SPHERE) f |= kBodySphere;
-      if (B.radius[i] > thr) {
+      if (reach[i] > thr) {
         f |= kBodyLarge;
         large[s].push_back(i);
       }

@@ -391,9 +391,18 @@ __device__ BodyD load_body(const World &w, int i) {
   b.p = mk(p.x, p.y, p.z);
   b.q = QD{(double)q.x, (double)q.y, (double)q.z, (double)q.w};
   b.half = mk(s.x * 0.5, s.y * 0.5, s.z * 0.5);
-  b.radius = s.w;
   b.sphere = (w.b.flags0[i] & kBodySphere) != 0;
+  // size.w is the broad phase's reach (the bounding radius plus the contact
+  // offset under AVBD_CONTACT_MATERIALS); a sphere's own radius is half its
+  // diameter (Rigid.sphere, src/physics/rigid.js:105-133)
+  b.radius = (w.b.contactOffset && b.sphere) ? s.x * 0.5 : s.w;
   return b;
+}
+
+// The pair's contact skin (AVBD_CONTACT_MATERIALS: the sum of the contact
+// offsets; 0 for the CPU engine's collider).
+__device__ __forceinline__ double pair_skin(const World &w, int ia, int ib) {
+  return w.b.contactOffset ? w.b.contactOffset[ia] + w.b.contactOffset[ib] : 0.0;
 }
 
 // transportComponents / transportPenalty (manifold.js:100-162)
@@ -765,7 +774,9 @@ __global__ void __launch_bounds__(256) classify_kernel(World w) {
     const uint64_t key = w.g.candKey[c];
     const int ia = (int)(key >> 32), ib = (int)(key & 0xffffffffu);
     const BodyD A = load_body(w, ia), B = load_body(w, ib);
-    if (A.sphere || B.sphere) {
+    // spheres, and pairs with a contact skin (speculative contacts: the f32
+    // certification covers the skin-free tests), go to the exact collider
+    if (A.sphere || B.sphere || pair_skin(w, ia, ib) != 0.0) {
       push_exact(w, c);
       continue;
     }
@@ -862,6 +873,7 @@ __global__ void __launch_bounds__(128) exact_kernel(World w) {
     double basis[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
     NewContact nc[kMaxContacts];
     Collider col(A, B, nc);
+    col.cd = pair_skin(w, ia, ib);
     const int num = col.collide(basis);
     if (A.sphere || B.sphere) {
       write_sphere_manifold(w, c, ia, ib, A, B, nc, num, basis);

@@ -608,6 +608,19 @@ def material_scene(kind="pile", seed=7):
     elif kind == "spheres":
         s = spheres_scene()
         s.params = dict(gravity=-9.81, iterations=10)
+    elif kind == "hover":
+        # bodies starting a few millimetres apart, inside each other's contact
+        # skin: speculative contacts from the first step
+        s = Scene("hover")
+        add_ground(s, 0.6)
+        rnd = LCG(seed)
+        for i in range(6):
+            x = (i - 2.5) * 1.3
+            s.box((1.0, 1.0, 0.5), 700.0, 0.6, (x, 0.0, 0.25 + rnd.uniform(0.001, 0.009)))
+            s.box((0.6, 0.6, 0.6), 400.0, 0.6, (x, 0.0, 0.8 + rnd.uniform(0.0015, 0.009)),
+                  velocity=(0.0, 0.0, -rnd.uniform(0.5, 1.5)))
+        s.sphere(0.5, 900.0, 0.6, (4.5, 0.0, 0.25 + 0.004))
+        s.params = dict(gravity=-9.81, iterations=10)
     else:
         raise KeyError(kind)
     rnd = LCG(seed * 7 + 3)

@@ -426,6 +426,9 @@ struct Body {
   Real friction = 0.5;
   // contact materials (rigid.js:54-68, 144-214)
   Real staticFriction = 0.5, dynamicFriction = 0.5, restitution = 0, contactOffset = 0.005, restOffset = -0.005;
+  // the broad phase's reach: the bounding radius, plus the contact offset
+  // under AVBD_CONTACT_MATERIALS (shaders.js:440-442)
+  Real reach = 0;
   Real mass = 0;
   Real moment[3] = {0, 0, 0};
   Real radius = 0;
@@ -531,6 +534,10 @@ struct SatAxis {
 
 // The module-level scratch of collide.js, gathered in one object.
 struct Collider {
+  // the pair's contact skin: contacts are generated up to this separation
+  // (AVBD_CONTACT_MATERIALS: the WGSL collider's contactDistance,
+  // src/physics/gpu/shaders.js:716-886, 1039); 0 for the CPU engine's
+  Real skin = 0;
   OBB boxA, boxB;
   Real frameNormal[3], frameCenter[3], frameU[3], frameV[3], frameExtentU, frameExtentV;
   Real faceExtU, faceExtV;
@@ -662,7 +669,7 @@ struct Collider {
     const Real rB = boxB.half[0] * absDot(n, boxB.axis[0]) + boxB.half[1] * absDot(n, boxB.axis[1]) +
                       boxB.half[2] * absDot(n, boxB.axis[2]);
     const Real separation = distance - (rA + rB);
-    if (separation > 0) return false;
+    if (separation > skin) return false;
     if (!target.valid || separation > target.separation) {
       target.valid = true;
       target.type = type; target.indexA = indexA; target.indexB = indexB;
@@ -751,7 +758,7 @@ struct Collider {
       p[0] = clip0[i * 3 + 0]; p[1] = clip0[i * 3 + 1]; p[2] = clip0[i * 3 + 2];
       v3_sub(q, p, frameCenter);
       const Real distance = v3_dot(q, frameNormal);
-      if (distance > PLANE_EPSILON) continue;
+      if (distance > skin + PLANE_EPSILON) continue;
       v3_copy(q, p);
       v3_add_scaled(q, frameNormal, -distance);
       if (referenceIsA) { v3_copy(xA, q); v3_copy(xB, p); }
@@ -789,7 +796,7 @@ struct Collider {
     Real delta[3], n[3], t[3], xA[3], xB[3];
     v3_sub(delta, B.positionLin, A.positionLin);
     const Real distanceSq = v3_len_sq(delta);
-    const Real radiusSum = A.radius + B.radius;
+    const Real radiusSum = A.radius + B.radius + skin;
     if (distanceSq > radiusSum * radiusSum) return 0;
     if (distanceSq > SPHERE_DISTANCE_EPSILON_SQ) v3_scale(n, delta, 1 / sqrt(distanceSq));
     else v3_set(n, 1, 0, 0);
@@ -825,7 +832,7 @@ struct Collider {
     int featureAxis = 0;
     if (distanceSq > SPHERE_DISTANCE_EPSILON_SQ) {
       const Real distance = sqrt(distanceSq);
-      if (distance > sphere.radius) return 0;
+      if (distance - sphere.radius > skin) return 0;
       v3_scale(n, t3, 1 / distance);
     } else {
       const Real gx = boxA.half[0] - fabs(lx);
@@ -976,8 +983,10 @@ struct Manifold : Force {
     if ((hasSphere || solver->p.contactModel == AVBD_CONTACT_MATERIALS) && hadContacts) m3_copy(oldBasis, basis);
     friction = sqrt(A.friction * B.friction);
     for (int i = 0; i < MAX_CONTACTS; i++) newContacts[i].reset();
+    const bool materials = solver->p.contactModel == AVBD_CONTACT_MATERIALS;
+    solver->collider.skin = materials ? A.contactOffset + B.contactOffset : 0;
     const int newNum = solver->collider.collide(A, B, newContacts, basis);
-    if (solver->p.contactModel == AVBD_CONTACT_MATERIALS) return initializeMaterials(oldBasis, hadContacts, newNum);
+    if (materials) return initializeMaterials(oldBasis, hadContacts, newNum);
     const bool basisCompatible =
         !hasSphere || !hadContacts || (oldBasis[0] * basis[0] + oldBasis[1] * basis[1] + oldBasis[2] * basis[2]) > 0.85;
     for (int i = 0; i < newNum; i++) {
@@ -1644,7 +1653,7 @@ static void for_each_pair_hash(const std::vector<Body *> &bodies, Visit &&visit)
   const int n = (int)bodies.size();
   if (n < 2) return;
   Real radiusSum = 0;
-  for (int i = 0; i < n; i++) radiusSum += bodies[i]->radius;
+  for (int i = 0; i < n; i++) radiusSum += bodies[i]->reach;
   const Real meanRadius = radiusSum / n;
   const Real largeThreshold = js_max(meanRadius * 8, 1e-6);
   const Real inv = 1 / js_max(meanRadius * 2, 1e-4);
@@ -1652,8 +1661,8 @@ static void for_each_pair_hash(const std::vector<Body *> &bodies, Visit &&visit)
   int64_t insertions = 0;
   for (int i = 0; i < n; i++) {
     const Body &b = *bodies[i];
-    if (b.radius > largeThreshold) { large.push_back(i); continue; }
-    const Real r = b.radius;
+    if (b.reach > largeThreshold) { large.push_back(i); continue; }
+    const Real r = b.reach;
     const Real *p = b.positionLin;
     const int64_t nx = floor_i64((p[0] + r) * inv) - floor_i64((p[0] - r) * inv) + 1;
     const int64_t ny = floor_i64((p[1] + r) * inv) - floor_i64((p[1] - r) * inv) + 1;
@@ -1667,7 +1676,7 @@ static void for_each_pair_hash(const std::vector<Body *> &bodies, Visit &&visit)
   std::vector<int32_t> entries(std::max<int64_t>(insertions, 1));
   std::vector<int32_t> lastSeen(n, -1);
   auto cell_range = [&](const Body &b, int64_t *lo, int64_t *hi) {
-    const Real r = b.radius;
+    const Real r = b.reach;
     const Real *p = b.positionLin;
     for (int a = 0; a < 3; a++) {
       lo[a] = floor_i64((p[a] - r) * inv);
@@ -1676,7 +1685,7 @@ static void for_each_pair_hash(const std::vector<Body *> &bodies, Visit &&visit)
   };
   for (int i = 0; i < n; i++) {
     const Body &b = *bodies[i];
-    if (b.radius > largeThreshold) continue;
+    if (b.reach > largeThreshold) continue;
     int64_t lo[3], hi[3];
     cell_range(b, lo, hi);
     for (int64_t x = lo[0]; x <= hi[0]; x++)
@@ -1691,7 +1700,7 @@ static void for_each_pair_hash(const std::vector<Body *> &bodies, Visit &&visit)
   }
   for (int i = 0; i < n; i++) {
     const Body &b = *bodies[i];
-    if (b.radius > largeThreshold) continue;
+    if (b.reach > largeThreshold) continue;
     int64_t lo[3], hi[3];
     cell_range(b, lo, hi);
     for (int64_t x = lo[0]; x <= hi[0]; x++)
@@ -1702,7 +1711,7 @@ static void for_each_pair_hash(const std::vector<Body *> &bodies, Visit &&visit)
   candidates.reserve(256);
   for (int i = n - 1; i >= 1; i--) {
     Body *bodyA = bodies[i];
-    if (bodyA->radius > largeThreshold) {
+    if (bodyA->reach > largeThreshold) {
       for (int j = i - 1; j >= 0; j--) visit(bodyA, bodies[j]);
       continue;
     }
@@ -1825,7 +1834,7 @@ static void step(Solver &s) {
     const Real dx = A->positionLin[0] - B->positionLin[0];
     const Real dy = A->positionLin[1] - B->positionLin[1];
     const Real dz = A->positionLin[2] - B->positionLin[2];
-    const Real r = A->radius + B->radius;
+    const Real r = A->reach + B->reach;
     if (dx * dx + dy * dy + dz * dz <= r * r && !A->constrainedTo(B)) {
       if (A->mass > 0 || B->mass > 0) {
         // Manifold.reinit (manifold.js:201-212) on a pooled manifold, or a new one
@@ -2083,6 +2092,7 @@ int orc_load(orc_solver *o, const avbd_world *w) {
     b->restitution = B.restitution ? B.restitution[i] : 0;
     b->contactOffset = B.contact_offset ? B.contact_offset[i] : s.p.contactOffset;
     b->restOffset = B.rest_offset ? B.rest_offset[i] : s.p.restOffset;
+    b->reach = s.p.contactModel == AVBD_CONTACT_MATERIALS ? b->radius + b->contactOffset : b->radius;
     s.bodies.push_back(b);
   }
   std::vector<std::pair<int, Force *>> ordered;
@@ -2364,7 +2374,9 @@ int orc_collide(orc_solver *o, int32_t a, int32_t b, double *basis9, uint32_t *f
   Contact c[MAX_CONTACTS];
   for (auto &x : c) x.reset();
   double basis[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
-  const int n = o->s.collider.collide(*o->s.bodies[a], *o->s.bodies[b], c, basis);
+  const Body &A = *o->s.bodies[a], &B = *o->s.bodies[b];
+  o->s.collider.skin = o->s.p.contactModel == AVBD_CONTACT_MATERIALS ? val(A.contactOffset + B.contactOffset) : 0.0;
+  const int n = o->s.collider.collide(A, B, c, basis);
   for (int k = 0; k < 9; k++) basis9[k] = basis[k];
   for (int i = 0; i < MAX_CONTACTS; i++) {
     features8[i] = c[i].feature;

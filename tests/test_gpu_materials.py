@@ -9,7 +9,9 @@ candidate pairs, manifold topology and colouring identical; body state and
 every contact's multiplier, penalty, stick flag, anchors and C0 within the
 dual-state bounds of tests/test_gpu_dual_state.py; every contact's
 restitution bias within 1e-6 m + 1e-4 of its value (f32 velocities on the
-device). The warm steps include impact steps, where biases are armed.
+device). The warm steps include impact steps, where biases are armed, and
+the "hover" scene starts with bodies inside each other's contact skin
+(speculative contacts at a positive separation).
 """
 import importlib
 
@@ -37,7 +39,7 @@ def setup(abi, scenes, kind):
 
 
 CASES = [("drop", 4), ("drop", 5), ("drop", 9), ("drop", 12), ("drop", 20), ("pile", 0), ("pile", 27), ("pile", 40),
-         ("spheres", 0), ("spheres", 3), ("spheres", 11), ("spheres", 25)]
+         ("spheres", 0), ("spheres", 3), ("spheres", 11), ("spheres", 25), ("hover", 0), ("hover", 1), ("hover", 6)]
 
 
 @pytest.mark.parametrize("kind, warm", CASES)

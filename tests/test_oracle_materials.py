@@ -111,3 +111,27 @@ def test_materials_are_validated(scenes, kw):
     w = resting_box(scenes).world()
     with pytest.raises(ValueError):
         w.set_materials(**kw)
+
+
+@pytest.mark.parametrize("gap, expect", [(0.004, 4), (0.009, 4), (0.012, 0)])
+def test_speculative_contacts_within_the_skin(abi, scenes, gap, expect):
+    """The pair's contact skin (the two contact offsets, 0.005 each by
+    default) generates contacts at a positive separation below it, with C0
+    on the normal = the gap minus the rest distance; the CPU engine's
+    collider generates none at any positive separation."""
+    s = scenes.Scene("hover")
+    scenes.add_ground(s, 0.5)
+    s.box((1, 1, 1), 1000, 0.5, (0, 0, 0.5 + gap))
+    s.sphere(0.6, 1000, 0.5, (3.0, 0, 0.3 + gap))
+    for model in (abi.CONTACT_CPU, abi.CONTACT_MATERIALS):
+        o = Oracle(abi.default_params(gravity=0.0, contact_model=model), s.world())
+        o.step(1)
+        st = o.state()
+        got = {(int(a), int(b)): int(n) for a, b, n in zip(st.m_body_a[:st.m_count], st.m_body_b[:st.m_count],
+                                                           st.m_num_contacts[:st.m_count])}
+        if model == abi.CONTACT_CPU or not expect:
+            assert sum(got.values()) == 0
+            continue
+        assert got == {(1, 0): 4, (2, 0): 1}
+        m = list(zip(st.m_body_a, st.m_body_b)).index((1, 0))
+        np.testing.assert_allclose(st.m_c0[m, :4, 0], gap + 0.01, atol=1e-12)
