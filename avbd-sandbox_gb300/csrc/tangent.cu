@@ -127,163 +127,183 @@ struct TWorld {
 // ---------------------------------------------------------------------------
 // vec3 / mat3 / quaternion on R (maths.js: the operation order of the reference)
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ R js_min(R a, R b) {
-  if (a != a || b != b) return R(NAN);
+template <class S>
+__device__ __forceinline__ S js_min(S a, S b) {
+  if (a != a || b != b) return S(NAN);
   if (a < b) return a;
   if (b < a) return b;
   return a;
 }
-__device__ __forceinline__ R js_max(R a, R b) {
-  if (a != a || b != b) return R(NAN);
+template <class S>
+__device__ __forceinline__ S js_max(S a, S b) {
+  if (a != a || b != b) return S(NAN);
   if (a > b) return a;
   if (b > a) return b;
   return a;
 }
-__device__ __forceinline__ R clampR(R x, R a, R b) { return js_max(a, js_min(b, x)); }
-__device__ __forceinline__ void v3_sub(R *o, const R *a, const R *b) {
+template <class S>
+__device__ __forceinline__ S clampR(S x, S a, S b) { return js_max(a, js_min(b, x)); }
+template <class S>
+__device__ __forceinline__ void v3_sub(S *o, const S *a, const S *b) {
   o[0] = a[0] - b[0]; o[1] = a[1] - b[1]; o[2] = a[2] - b[2];
 }
-__device__ __forceinline__ void v3_add(R *o, const R *a, const R *b) {
+template <class S>
+__device__ __forceinline__ void v3_add(S *o, const S *a, const S *b) {
   o[0] = a[0] + b[0]; o[1] = a[1] + b[1]; o[2] = a[2] + b[2];
 }
 // o += a * s; `o` an R array or a recording row (RecRow) of a body's system
-template <class O>
-__device__ __forceinline__ void v3_add_scaled(O &&o, const R *a, R s) {
+template <class O, class S>
+__device__ __forceinline__ void v3_add_scaled(O &&o, const S *a, S s) {
   o[0] += a[0] * s; o[1] += a[1] * s; o[2] += a[2] * s;
 }
-template <class O>
-__device__ __forceinline__ void v3_add_into(O &&o, const R *a) {
+template <class O, class S>
+__device__ __forceinline__ void v3_add_into(O &&o, const S *a) {
   o[0] += a[0]; o[1] += a[1]; o[2] += a[2];
 }
-__device__ __forceinline__ R v3_dot(const R *a, const R *b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
-__device__ __forceinline__ R v3_len_sq(const R *a) { return a[0] * a[0] + a[1] * a[1] + a[2] * a[2]; }
-__device__ __forceinline__ void v3_cross(R *o, const R *a, const R *b) {
-  const R ax = a[0], ay = a[1], az = a[2], bx = b[0], by = b[1], bz = b[2];
+template <class S>
+__device__ __forceinline__ S v3_dot(const S *a, const S *b) { return a[0] * b[0] + a[1] * b[1] + a[2] * b[2]; }
+template <class S>
+__device__ __forceinline__ S v3_len_sq(const S *a) { return a[0] * a[0] + a[1] * a[1] + a[2] * a[2]; }
+template <class S>
+__device__ __forceinline__ void v3_cross(S *o, const S *a, const S *b) {
+  const S ax = a[0], ay = a[1], az = a[2], bx = b[0], by = b[1], bz = b[2];
   o[0] = ay * bz - az * by;
   o[1] = az * bx - ax * bz;
   o[2] = ax * by - ay * bx;
 }
-__device__ __forceinline__ void m3_zero(R *o) {
+template <class S>
+__device__ __forceinline__ void m3_zero(S *o) {
   for (int i = 0; i < 9; i++) o[i] = 0.0;
 }
-__device__ __forceinline__ void m3_diag(R *o, R a, R b, R c) {
+template <class S>
+__device__ __forceinline__ void m3_diag(S *o, S a, S b, S c) {
   m3_zero(o);
   o[0] = a; o[4] = b; o[8] = c;
 }
-__device__ __forceinline__ void m3_mul_vec(R *o, const R *a, const R *v) {
-  const R x = v[0], y = v[1], z = v[2];
+template <class S>
+__device__ __forceinline__ void m3_mul_vec(S *o, const S *a, const S *v) {
+  const S x = v[0], y = v[1], z = v[2];
   o[0] = a[0] * x + a[1] * y + a[2] * z;
   o[1] = a[3] * x + a[4] * y + a[5] * z;
   o[2] = a[6] * x + a[7] * y + a[8] * z;
 }
-__device__ void m3_mul(R *o, const R *a, const R *b) {
-  R t[9];
+template <class S>
+__device__ void m3_mul(S *o, const S *a, const S *b) {
+  S t[9];
   for (int r = 0; r < 3; r++)
     for (int c = 0; c < 3; c++) t[r * 3 + c] = a[r * 3] * b[c] + a[r * 3 + 1] * b[3 + c] + a[r * 3 + 2] * b[6 + c];
   for (int i = 0; i < 9; i++) o[i] = t[i];
 }
-__device__ __forceinline__ void m3_transpose(R *o, const R *a) {
-  R t[9];
+template <class S>
+__device__ __forceinline__ void m3_transpose(S *o, const S *a) {
+  S t[9];
   for (int r = 0; r < 3; r++)
     for (int c = 0; c < 3; c++) t[c * 3 + r] = a[r * 3 + c];
   for (int i = 0; i < 9; i++) o[i] = t[i];
 }
-__device__ __forceinline__ void m3_skew(R *o, const R *r) {
+template <class S>
+__device__ __forceinline__ void m3_skew(S *o, const S *r) {
   o[0] = 0.0; o[1] = -r[2]; o[2] = r[1];
   o[3] = r[2]; o[4] = 0.0; o[5] = -r[0];
   o[6] = -r[1]; o[7] = r[0]; o[8] = 0.0;
 }
-template <class O>
-__device__ __forceinline__ void m3_add_into(O &&o, const R *a) {
+template <class O, class S>
+__device__ __forceinline__ void m3_add_into(O &&o, const S *a) {
   for (int i = 0; i < 9; i++) o[i] += a[i];
 }
 // Eq. 20 (maths.js:541-555)
-__device__ void q_subtract(R *o, const R *a, const R *b) {
-  const R lsq = b[0] * b[0] + b[1] * b[1] + b[2] * b[2] + b[3] * b[3];
-  const R ix = -b[0] / lsq, iy = -b[1] / lsq, iz = -b[2] / lsq, iw = b[3] / lsq;
-  const R ax = a[0], ay = a[1], az = a[2], aw = a[3];
+template <class S>
+__device__ void q_subtract(S *o, const S *a, const S *b) {
+  const S lsq = b[0] * b[0] + b[1] * b[1] + b[2] * b[2] + b[3] * b[3];
+  const S ix = -b[0] / lsq, iy = -b[1] / lsq, iz = -b[2] / lsq, iw = b[3] / lsq;
+  const S ax = a[0], ay = a[1], az = a[2], aw = a[3];
   o[0] = (aw * ix + ax * iw + ay * iz - az * iy) * 2.0;
   o[1] = (aw * iy - ax * iz + ay * iw + az * ix) * 2.0;
   o[2] = (aw * iz + ax * iy - ay * ix + az * iw) * 2.0;
 }
 // Eq. 21 (maths.js:568-592), its "0 * q" terms kept
-__device__ void q_integrate(R *o, const R *q, const R *dw) {
-  const R qx = q[0], qy = q[1], qz = q[2], qw = q[3];
-  const R wx = dw[0], wy = dw[1], wz = dw[2];
-  const R px = 0.0 * qx + wx * qw + wy * qz - wz * qy;
-  const R py = 0.0 * qy - wx * qz + wy * qw + wz * qx;
-  const R pz = 0.0 * qz + wx * qy - wy * qx + wz * qw;
-  const R pw = 0.0 * qw - wx * qx - wy * qy - wz * qz;
-  const R rx = qx + px * 0.5, ry = qy + py * 0.5, rz = qz + pz * 0.5, rw = qw + pw * 0.5;
-  const R len = sqrt(rx * rx + ry * ry + rz * rz + rw * rw);
+template <class S>
+__device__ void q_integrate(S *o, const S *q, const S *dw) {
+  const S qx = q[0], qy = q[1], qz = q[2], qw = q[3];
+  const S wx = dw[0], wy = dw[1], wz = dw[2];
+  const S px = 0.0 * qx + wx * qw + wy * qz - wz * qy;
+  const S py = 0.0 * qy - wx * qz + wy * qw + wz * qx;
+  const S pz = 0.0 * qz + wx * qy - wy * qx + wz * qw;
+  const S pw = 0.0 * qw - wx * qx - wy * qy - wz * qz;
+  const S rx = qx + px * 0.5, ry = qy + py * 0.5, rz = qz + pz * 0.5, rw = qw + pw * 0.5;
+  const S len = sqrt(rx * rx + ry * ry + rz * rz + rw * rw);
   o[0] = rx / len; o[1] = ry / len; o[2] = rz / len; o[3] = rw / len;
 }
 // maths.js:599-613
-__device__ void q_rotate(R *o, const R *q, const R *v) {
-  const R ux = q[0], uy = q[1], uz = q[2], w = q[3];
-  const R vx = v[0], vy = v[1], vz = v[2];
-  const R tx = (uy * vz - uz * vy) * 2.0;
-  const R ty = (uz * vx - ux * vz) * 2.0;
-  const R tz = (ux * vy - uy * vx) * 2.0;
+template <class S>
+__device__ void q_rotate(S *o, const S *q, const S *v) {
+  const S ux = q[0], uy = q[1], uz = q[2], w = q[3];
+  const S vx = v[0], vy = v[1], vz = v[2];
+  const S tx = (uy * vz - uz * vy) * 2.0;
+  const S ty = (uz * vx - ux * vz) * 2.0;
+  const S tz = (ux * vy - uy * vx) * 2.0;
   o[0] = vx + tx * w + (uy * tz - uz * ty);
   o[1] = vy + ty * w + (uz * tx - ux * tz);
   o[2] = vz + tz * w + (ux * ty - uy * tx);
 }
 // maths.js:621-627
-__device__ __forceinline__ void transform_point(R *o, const R *lin, const R *ang, const R *v) {
+template <class S>
+__device__ __forceinline__ void transform_point(S *o, const S *lin, const S *ang, const S *v) {
   q_rotate(o, ang, v);
   o[0] += lin[0]; o[1] += lin[1]; o[2] += lin[2];
 }
 // R I R^T of a body (rigid.js:228-247), maths.js:417-434 for R
-__device__ void world_moment(R *out, const TBodyStatic &st, const R *q, bool rotated) {
+template <class S>
+__device__ void world_moment(S *out, const TBodyStatic &st, const S *q, bool rotated) {
   if (!rotated || st.shape == AVBD_SHAPE_SPHERE) {
-    m3_diag(out, R(st.moment[0]), R(st.moment[1]), R(st.moment[2]));
+    m3_diag(out, S(st.moment[0]), S(st.moment[1]), S(st.moment[2]));
     return;
   }
-  const R x = q[0], y = q[1], z = q[2], w = q[3];
-  const R xx = x * x, yy = y * y, zz = z * z, xy = x * y, xz = x * z, yz = y * z, wx = w * x, wy = w * y, wz = w * z;
-  R Rm[9];
+  const S x = q[0], y = q[1], z = q[2], w = q[3];
+  const S xx = x * x, yy = y * y, zz = z * z, xy = x * y, xz = x * z, yz = y * z, wx = w * x, wy = w * y, wz = w * z;
+  S Rm[9];
   Rm[0] = 1.0 - 2.0 * (yy + zz); Rm[1] = 2.0 * (xy + wz); Rm[2] = 2.0 * (xz - wy);
   Rm[3] = 2.0 * (xy - wz); Rm[4] = 1.0 - 2.0 * (xx + zz); Rm[5] = 2.0 * (yz + wx);
   Rm[6] = 2.0 * (xz + wy); Rm[7] = 2.0 * (yz - wx); Rm[8] = 1.0 - 2.0 * (xx + yy);
-  R T[9], Rt[9];
+  S T[9], Rt[9];
   m3_transpose(Rt, Rm);
-  m3_diag(T, R(st.moment[0]), R(st.moment[1]), R(st.moment[2]));
+  m3_diag(T, S(st.moment[0]), S(st.moment[1]), S(st.moment[2]));
   m3_mul(out, Rt, T);
   m3_mul(out, out, Rm);
 }
 // maths.js:660-725, unrolled LDL^T of the 6x6 block system
-__device__ void solve6(const R *aLin, const R *aAng, const R *aCross, const R *bLin, const R *bAng, R *xLin, R *xAng) {
-  const R A11 = aLin[0];
-  const R A21 = aLin[3], A22 = aLin[4];
-  const R A31 = aLin[6], A32 = aLin[7], A33 = aLin[8];
-  const R A41 = aCross[0], A42 = aCross[1], A43 = aCross[2], A44 = aAng[0];
-  const R A51 = aCross[3], A52 = aCross[4], A53 = aCross[5], A54 = aAng[3], A55 = aAng[4];
-  const R A61 = aCross[6], A62 = aCross[7], A63 = aCross[8], A64 = aAng[6], A65 = aAng[7], A66 = aAng[8];
-  const R L21 = A21 / A11, L31 = A31 / A11, L41 = A41 / A11, L51 = A51 / A11, L61 = A61 / A11;
-  const R D1 = A11;
-  const R D2 = A22 - L21 * L21 * D1;
-  const R L32 = (A32 - L21 * L31 * D1) / D2;
-  const R L42 = (A42 - L21 * L41 * D1) / D2;
-  const R L52 = (A52 - L21 * L51 * D1) / D2;
-  const R L62 = (A62 - L21 * L61 * D1) / D2;
-  const R D3 = A33 - (L31 * L31 * D1 + L32 * L32 * D2);
-  const R L43 = (A43 - L31 * L41 * D1 - L32 * L42 * D2) / D3;
-  const R L53 = (A53 - L31 * L51 * D1 - L32 * L52 * D2) / D3;
-  const R L63 = (A63 - L31 * L61 * D1 - L32 * L62 * D2) / D3;
-  const R D4 = A44 - (L41 * L41 * D1 + L42 * L42 * D2 + L43 * L43 * D3);
-  const R L54 = (A54 - L41 * L51 * D1 - L42 * L52 * D2 - L43 * L53 * D3) / D4;
-  const R L64 = (A64 - L41 * L61 * D1 - L42 * L62 * D2 - L43 * L63 * D3) / D4;
-  const R D5 = A55 - (L51 * L51 * D1 + L52 * L52 * D2 + L53 * L53 * D3 + L54 * L54 * D4);
-  const R L65 = (A65 - L51 * L61 * D1 - L52 * L62 * D2 - L53 * L63 * D3 - L54 * L64 * D4) / D5;
-  const R D6 = A66 - (L61 * L61 * D1 + L62 * L62 * D2 + L63 * L63 * D3 + L64 * L64 * D4 + L65 * L65 * D5);
-  const R y1 = bLin[0];
-  const R y2 = bLin[1] - L21 * y1;
-  const R y3 = bLin[2] - L31 * y1 - L32 * y2;
-  const R y4 = bAng[0] - L41 * y1 - L42 * y2 - L43 * y3;
-  const R y5 = bAng[1] - L51 * y1 - L52 * y2 - L53 * y3 - L54 * y4;
-  const R y6 = bAng[2] - L61 * y1 - L62 * y2 - L63 * y3 - L64 * y4 - L65 * y5;
-  const R z1 = y1 / D1, z2 = y2 / D2, z3 = y3 / D3, z4 = y4 / D4, z5 = y5 / D5, z6 = y6 / D6;
+template <class S>
+__device__ void solve6(const S *aLin, const S *aAng, const S *aCross, const S *bLin, const S *bAng, S *xLin, S *xAng) {
+  const S A11 = aLin[0];
+  const S A21 = aLin[3], A22 = aLin[4];
+  const S A31 = aLin[6], A32 = aLin[7], A33 = aLin[8];
+  const S A41 = aCross[0], A42 = aCross[1], A43 = aCross[2], A44 = aAng[0];
+  const S A51 = aCross[3], A52 = aCross[4], A53 = aCross[5], A54 = aAng[3], A55 = aAng[4];
+  const S A61 = aCross[6], A62 = aCross[7], A63 = aCross[8], A64 = aAng[6], A65 = aAng[7], A66 = aAng[8];
+  const S L21 = A21 / A11, L31 = A31 / A11, L41 = A41 / A11, L51 = A51 / A11, L61 = A61 / A11;
+  const S D1 = A11;
+  const S D2 = A22 - L21 * L21 * D1;
+  const S L32 = (A32 - L21 * L31 * D1) / D2;
+  const S L42 = (A42 - L21 * L41 * D1) / D2;
+  const S L52 = (A52 - L21 * L51 * D1) / D2;
+  const S L62 = (A62 - L21 * L61 * D1) / D2;
+  const S D3 = A33 - (L31 * L31 * D1 + L32 * L32 * D2);
+  const S L43 = (A43 - L31 * L41 * D1 - L32 * L42 * D2) / D3;
+  const S L53 = (A53 - L31 * L51 * D1 - L32 * L52 * D2) / D3;
+  const S L63 = (A63 - L31 * L61 * D1 - L32 * L62 * D2) / D3;
+  const S D4 = A44 - (L41 * L41 * D1 + L42 * L42 * D2 + L43 * L43 * D3);
+  const S L54 = (A54 - L41 * L51 * D1 - L42 * L52 * D2 - L43 * L53 * D3) / D4;
+  const S L64 = (A64 - L41 * L61 * D1 - L42 * L62 * D2 - L43 * L63 * D3) / D4;
+  const S D5 = A55 - (L51 * L51 * D1 + L52 * L52 * D2 + L53 * L53 * D3 + L54 * L54 * D4);
+  const S L65 = (A65 - L51 * L61 * D1 - L52 * L62 * D2 - L53 * L63 * D3 - L54 * L64 * D4) / D5;
+  const S D6 = A66 - (L61 * L61 * D1 + L62 * L62 * D2 + L63 * L63 * D3 + L64 * L64 * D4 + L65 * L65 * D5);
+  const S y1 = bLin[0];
+  const S y2 = bLin[1] - L21 * y1;
+  const S y3 = bLin[2] - L31 * y1 - L32 * y2;
+  const S y4 = bAng[0] - L41 * y1 - L42 * y2 - L43 * y3;
+  const S y5 = bAng[1] - L51 * y1 - L52 * y2 - L53 * y3 - L54 * y4;
+  const S y6 = bAng[2] - L61 * y1 - L62 * y2 - L63 * y3 - L64 * y4 - L65 * y5;
+  const S z1 = y1 / D1, z2 = y2 / D2, z3 = y3 / D3, z4 = y4 / D4, z5 = y5 / D5, z6 = y6 / D6;
   xAng[2] = z6;
   xAng[1] = z5 - L65 * xAng[2];
   xAng[0] = z4 - L54 * xAng[1] - L64 * xAng[2];
@@ -293,11 +313,14 @@ __device__ void solve6(const R *aLin, const R *aAng, const R *aCross, const R *b
 }
 
 // A body's 6x6 system, accumulated by its forces: 33 entries in this order.
-struct Sys6 {
-  R lin[9], ang[9], cross[9], bl[3], ba[3];
+template <class S>
+struct Sys6T {
+  S lin[9], ang[9], cross[9], bl[3], ba[3];
 };
+using Sys6 = Sys6T<R>;
 constexpr int kSysEntries = 33;
 static_assert(sizeof(Sys6) == kSysEntries * sizeof(R), "Sys6 is 33 contiguous entries");
+static_assert(sizeof(Sys6T<Dual1>) == kSysEntries * sizeof(Dual1), "33 contiguous entries");
 
 // The recording form of a body's system: one constraint's contribution as
 // the sequence of addends it adds to each entry, so that the addends of many
@@ -998,22 +1021,33 @@ __device__ void next_rows(const TWorld &w, int i, BodySmem &sm) {
 __device__ void body_update_block(const TWorld &w, int i, R alpha, BodySmem &sm) {
   const TParams &P = w.P;
   const int t = threadIdx.x, nt = blockDim.x;
-  if (t == nt - 1) {  // the inertial terms
-    TBody &b = w.b[i];
+  if (t >= nt - kTangentDims) {  // the inertial terms, one tangent direction per thread
+    using S = Dual1;
+    const int k = t - (nt - kTangentDims);
+    const TBody &b = w.b[i];
     const TBodyStatic &st = w.bs[i];
     const double dt2 = P.dt * P.dt;
-    Sys6 s;
-    R MAng[9], tmp[3], dq[3];
-    m3_diag(s.lin, R(st.mass / dt2), R(st.mass / dt2), R(st.mass / dt2));
-    world_moment(MAng, st, b.q, P.rotatedInertia != 0);
-    for (int k = 0; k < 9; k++) s.ang[k] = MAng[k] / dt2;
+    S p[3], yl[3], q[4], yq[4];
+    for (int c = 0; c < 3; c++) {
+      p[c] = dir_of(b.p[c], k);
+      yl[c] = dir_of(b.yl[c], k);
+    }
+    for (int c = 0; c < 4; c++) {
+      q[c] = dir_of(b.q[c], k);
+      yq[c] = dir_of(b.yq[c], k);
+    }
+    Sys6T<S> s;
+    S MAng[9], tmp[3], dq[3];
+    m3_diag(s.lin, S(st.mass / dt2), S(st.mass / dt2), S(st.mass / dt2));
+    world_moment(MAng, st, q, P.rotatedInertia != 0);
+    for (int c = 0; c < 9; c++) s.ang[c] = MAng[c] / dt2;
     m3_zero(s.cross);
-    v3_sub(tmp, b.p, b.yl);
+    v3_sub(tmp, p, yl);
     m3_mul_vec(s.bl, s.lin, tmp);
-    q_subtract(dq, b.q, b.yq);
+    q_subtract(dq, q, yq);
     m3_mul_vec(s.ba, s.ang, dq);
-    const R *e = &s.lin[0];
-    for (int k = 0; k < kSysEntries; k++) sm.acc[k] = e[k];
+    const S *e = &s.lin[0];
+    for (int c = 0; c < kSysEntries; c++) set_dir(sm.acc[c], e[c], k);
   }
   if (t == 0) {
     sm.cursorE = w.fStart[i + 1] - 1;  // the body's forces, newest first
@@ -1048,23 +1082,40 @@ __device__ void body_update_block(const TWorld &w, int i, R alpha, BodySmem &sm)
     if (t == nt - 1) next_rows(w, i, sm);  // the rows are recorded; the replay reads only rec and cnt
     __syncthreads();
   }
-  if (t == 0) {
+  if (t < kTangentDims) {  // the 6x6 solve and the update, one tangent direction per thread
+    using S = Dual1;
+    const int k = t;
     TBody &b = w.b[i];
-    Sys6 s;
-    R *e = &s.lin[0];
-    for (int k = 0; k < kSysEntries; k++) e[k] = sm.acc[k];
-    R xl[3], xa[3], nl[3], na[3];
-    for (int k = 0; k < 3; k++) {
-      nl[k] = -s.bl[k];
-      na[k] = -s.ba[k];
+    Sys6T<S> s;
+    S *e = &s.lin[0];
+    for (int c = 0; c < kSysEntries; c++) e[c] = dir_of(sm.acc[c], k);
+    S p[3], p0[3], q[4], q0[4];
+    for (int c = 0; c < 3; c++) {
+      p[c] = dir_of(b.p[c], k);
+      p0[c] = dir_of(b.p0[c], k);
+    }
+    for (int c = 0; c < 4; c++) {
+      q[c] = dir_of(b.q[c], k);
+      q0[c] = dir_of(b.q0[c], k);
+    }
+    __syncwarp(0x1fu);  // every direction has read the body before any writes it
+    S xl[3], xa[3], nl[3], na[3];
+    for (int c = 0; c < 3; c++) {
+      nl[c] = -s.bl[c];
+      na[c] = -s.ba[c];
     }
     solve6(s.lin, s.ang, s.cross, nl, na, xl, xa);
-    v3_add(b.p, b.p, xl);
-    R q1[4];
-    q_integrate(q1, b.q, xa);
-    for (int k = 0; k < 4; k++) b.q[k] = q1[k];
-    v3_sub(b.dqL, b.p, b.p0);
-    q_subtract(b.dqA, b.q, b.q0);
+    v3_add(p, p, xl);
+    S q1[4], dqL[3], dqA[3];
+    q_integrate(q1, q, xa);
+    v3_sub(dqL, p, p0);
+    q_subtract(dqA, q1, q0);
+    for (int c = 0; c < 3; c++) {
+      set_dir(b.p[c], p[c], k);
+      set_dir(b.dqL[c], dqL[c], k);
+      set_dir(b.dqA[c], dqA[c], k);
+    }
+    for (int c = 0; c < 4; c++) set_dir(b.q[c], q1[c], k);
   }
   __syncthreads();
 }
