@@ -322,6 +322,19 @@ constexpr int kSysEntries = 33;
 static_assert(sizeof(Sys6) == kSysEntries * sizeof(R), "Sys6 is 33 contiguous entries");
 static_assert(sizeof(Sys6T<Dual1>) == kSysEntries * sizeof(Dual1), "33 contiguous entries");
 
+// A stored value as a thread computing in S sees it: the whole dual number,
+// or its value and the derivative of tangent direction k.
+template <class S>
+__device__ __forceinline__ S ld(const R &x, int k);
+template <>
+__device__ __forceinline__ R ld<R>(const R &x, int) { return x; }
+template <>
+__device__ __forceinline__ Dual1 ld<Dual1>(const R &x, int k) { return dir_of(x, k); }
+template <class S>
+__device__ __forceinline__ void ldn(S *o, const R *x, int n, int k) {
+  for (int c = 0; c < n; c++) o[c] = ld<S>(x[c], k);
+}
+
 // The recording form of a body's system: one constraint's contribution as
 // the sequence of addends it adds to each entry, so that the addends of many
 // constraints, computed by different threads, are summed afterwards in the
@@ -349,28 +362,35 @@ __device__ __forceinline__ int rec_off(int e) {
   return 45 + 2 * (e - 30);                             // ba: 6 slots from 45
 }
 constexpr int kRecSlots = 51;
+// One addend of tangent direction dir, recorded into its slot of the full
+// dual number: direction 0 also writes the value (the same in every
+// direction), so each thread owns the doubles it writes.
 struct RecElem {
   R *slot;
   unsigned char *cnt;
-  int cap;
-  __device__ void operator+=(const R &x) const {
+  int cap, dir;
+  __device__ void operator+=(const Dual1 &x) const {
     const int k = *cnt;
-    if (k < cap) slot[k] = x;
+    if (k < cap) {
+      if (dir == 0) slot[k].v = x.v;
+      slot[k].d[dir] = x.d[0];
+    }
     *cnt = (unsigned char)(k + 1);  // above the entry's room: reported by the replay
   }
 };
 struct RecRow {
   R *slot;
   unsigned char *cnt;
-  int base;  // first entry of the row
+  int base, dir;  // first entry of the row
   __device__ RecElem operator[](int e) const {
-    return RecElem{slot + rec_off(base + e), cnt + base + e, rec_cap(base + e)};
+    return RecElem{slot + rec_off(base + e), cnt + base + e, rec_cap(base + e), dir};
   }
 };
 struct RecSys6 {
   RecRow lin, ang, cross, bl, ba;
-  __device__ RecSys6(R *slots, unsigned char *cnt)
-      : lin{slots, cnt, 0}, ang{slots, cnt, 9}, cross{slots, cnt, 18}, bl{slots, cnt, 27}, ba{slots, cnt, 30} {}
+  __device__ RecSys6(R *slots, unsigned char *cnt, int dir)
+      : lin{slots, cnt, 0, dir}, ang{slots, cnt, 9, dir}, cross{slots, cnt, 18, dir}, bl{slots, cnt, 27, dir},
+        ba{slots, cnt, 30, dir} {}
 };
 
 __device__ __forceinline__ bool is_dynamic(const TWorld &w, int i) { return i >= 0 && w.bs[i].mass > 0; }
@@ -483,8 +503,9 @@ __device__ geo::BodyT<R> body_geo(const TWorld &w, int i) {
 // Manifold.initialize (manifold.js:214-318) of candidate c, at x_t.
 // manifold.js:325-350: the angular Jacobian rows of a contact, rows of
 // rA_world x n_r (A) and rB_world x (-n_r) (B), into out[0..8] and out[9..17]
-__device__ void contact_jacobians(R *out, const R *basis, const R *qA, const R *qB, const R *rA, const R *rB) {
-  R rAW[3], rBW[3], row[3], acc[3];
+template <class S>
+__device__ void contact_jacobians(S *out, const S *basis, const S *qA, const S *qB, const S *rA, const S *rB) {
+  S rAW[3], rBW[3], row[3], acc[3];
   q_rotate(rAW, qA, rA);
   q_rotate(rBW, qB, rB);
   for (int r = 0; r < 3; r++) {
@@ -570,26 +591,48 @@ __global__ void narrow_kernel(TWorld w) {
 }
 
 // Joint.initialize (joint.js:131-160) and Spring.initialize (spring.js:472-507).
-__device__ void joint_eval_lin(const TWorld &w, const TJoint &j, R *out) {
-  R pA[3], pB[3];
-  if (j.a >= 0) transform_point(pA, w.b[j.a].p, w.b[j.a].q, j.rA);
-  else { pA[0] = j.rA[0]; pA[1] = j.rA[1]; pA[2] = j.rA[2]; }
-  transform_point(pB, w.b[j.b].p, w.b[j.b].q, j.rB);
+// A body's iterate (p, q) as seen in S by direction k.
+template <class S>
+__device__ __forceinline__ void body_pose(const TWorld &w, int i, S *p, S *q, int k) {
+  ldn(p, w.b[i].p, 3, k);
+  ldn(q, w.b[i].q, 4, k);
+}
+template <class S>
+__device__ void joint_eval_lin(const TWorld &w, const TJoint &j, S *out, int dir = 0) {
+  S pA[3], pB[3], p[3], q[4], r[3];
+  ldn(r, j.rA, 3, dir);
+  if (j.a >= 0) {
+    body_pose(w, j.a, p, q, dir);
+    transform_point(pA, p, q, r);
+  } else {
+    pA[0] = r[0]; pA[1] = r[1]; pA[2] = r[2];
+  }
+  ldn(r, j.rB, 3, dir);
+  body_pose(w, j.b, p, q, dir);
+  transform_point(pB, p, q, r);
   v3_sub(out, pA, pB);
 }
-__device__ void joint_eval_ang(const TWorld &w, const TJoint &j, R *out) {
-  const R id[4] = {R(0.0), R(0.0), R(0.0), R(1.0)};
-  q_subtract(out, j.a >= 0 ? w.b[j.a].q : id, w.b[j.b].q);
+template <class S>
+__device__ void joint_eval_ang(const TWorld &w, const TJoint &j, S *out, int dir = 0) {
+  S qA[4] = {S(0.0), S(0.0), S(0.0), S(1.0)}, qB[4];
+  if (j.a >= 0) ldn(qA, w.b[j.a].q, 4, dir);
+  ldn(qB, w.b[j.b].q, 4, dir);
+  q_subtract(out, qA, qB);
   for (int k = 0; k < 3; k++) out[k] = out[k] * j.torqueArm;
 }
 // spring.js:447-458: C = |d| - rest, n = d / |d| (NaN C when |d| <= 1e-6)
-__device__ R spring_eval(const TWorld &w, const TSpring &s, R *d, R *n) {
-  R pA[3], pB[3];
-  transform_point(pA, w.b[s.a].p, w.b[s.a].q, s.rA);
-  transform_point(pB, w.b[s.b].p, w.b[s.b].q, s.rB);
+template <class S>
+__device__ S spring_eval(const TWorld &w, const TSpring &s, S *d, S *n, int dir = 0) {
+  S pA[3], pB[3], p[3], q[4], r[3];
+  ldn(r, s.rA, 3, dir);
+  body_pose(w, s.a, p, q, dir);
+  transform_point(pA, p, q, r);
+  ldn(r, s.rB, 3, dir);
+  body_pose(w, s.b, p, q, dir);
+  transform_point(pB, p, q, r);
   v3_sub(d, pA, pB);
-  const R len = sqrt(v3_len_sq(d));
-  if (len <= 1.0e-6) return R(NAN);
+  const S len = sqrt(v3_len_sq(d));
+  if (len <= 1.0e-6) return S(NAN);
   for (int k = 0; k < 3; k++) n[k] = d[k] / len;
   return len - s.rest;
 }
@@ -781,41 +824,53 @@ __global__ void __launch_bounds__(kBlock) adjacency_coloring_kernel(TWorld w) {
 // ---------------------------------------------------------------------------
 // Manifold._evaluate (manifold.js:358-409) of contact i with cached
 // Jacobians from the x_t orientations: C = (1 - alpha) C0 + J (x - x_t).
+// Computed in S by tangent direction dir (S = R: every direction).
+template <class S>
 struct ContactEvalT {
-  R C[3], F[3];
+  S C[3], F[3];
   bool within;
 };
-__device__ ContactEvalT contact_eval(const TWorld &w, const TManifold &m, int i, R alpha, R *jAAng, R *jBAng) {
+template <class S>
+__device__ ContactEvalT<S> contact_eval(const TWorld &w, const TManifold &m, int i, R alpha, S *basis, S *jAAng,
+                                        S *jBAng, int dir = 0) {
   const TBody &A = w.b[m.a], &B = w.b[m.b];
   const TContact &c = m.c[i];
   // the bodies' displacements from x_t, kept with their iterates
-  const R *dqALin = A.dqL, *dqAAng = A.dqA, *dqBLin = B.dqL, *dqBAng = B.dqA;
-  R jBLin[9], acc[3];
-  for (int k = 0; k < 9; k++) jBLin[k] = -m.basis[k];
+  S dqALin[3], dqAAng[3], dqBLin[3], dqBAng[3];
+  ldn(dqALin, A.dqL, 3, dir);
+  ldn(dqAAng, A.dqA, 3, dir);
+  ldn(dqBLin, B.dqL, 3, dir);
+  ldn(dqBAng, B.dqA, 3, dir);
+  ldn(basis, m.basis, 9, dir);
+  S jBLin[9], acc[3];
+  for (int k = 0; k < 9; k++) jBLin[k] = -basis[k];
   if (w.P.cachedJacobians) {  // computed once per step at the x_t orientations (narrow_kernel)
     const R *jc = &w.jac[((size_t)(&m - w.cur) * K8 + i) * 18];
-    for (int k = 0; k < 9; k++) {
-      jAAng[k] = jc[k];
-      jBAng[k] = jc[9 + k];
-    }
+    ldn(jAAng, jc, 9, dir);
+    ldn(jBAng, jc + 9, 9, dir);
   } else {
-    R jc[18];
-    contact_jacobians(jc, m.basis, A.q, B.q, c.rA, c.rB);
+    S jc[18], qA[4], qB[4], rA[3], rB[3];
+    ldn(qA, A.q, 4, dir);
+    ldn(qB, B.q, 4, dir);
+    ldn(rA, c.rA, 3, dir);
+    ldn(rB, c.rB, 3, dir);
+    contact_jacobians(jc, basis, qA, qB, rA, rB);
     for (int k = 0; k < 9; k++) {
       jAAng[k] = jc[k];
       jBAng[k] = jc[9 + k];
     }
   }
-  ContactEvalT e;
-  for (int k = 0; k < 3; k++) e.C[k] = c.C0[k] * (1.0 - alpha);
-  m3_mul_vec(acc, m.basis, dqALin); v3_add(e.C, e.C, acc);
+  ContactEvalT<S> e;
+  const S keep = 1.0 - ld<S>(alpha, dir);
+  for (int k = 0; k < 3; k++) e.C[k] = ld<S>(c.C0[k], dir) * keep;
+  m3_mul_vec(acc, basis, dqALin); v3_add(e.C, e.C, acc);
   m3_mul_vec(acc, jBLin, dqBLin); v3_add(e.C, e.C, acc);
   m3_mul_vec(acc, jAAng, dqAAng); v3_add(e.C, e.C, acc);
   m3_mul_vec(acc, jBAng, dqBAng); v3_add(e.C, e.C, acc);
-  for (int k = 0; k < 3; k++) e.F[k] = c.pen[k] * e.C[k] + c.lam[k];
-  e.F[0] = js_min(e.F[0], R(0.0));
-  const R bounds = fabs(e.F[0]) * m.friction;
-  const R fs = sqrt(e.F[1] * e.F[1] + e.F[2] * e.F[2]);
+  for (int k = 0; k < 3; k++) e.F[k] = ld<S>(c.pen[k], dir) * e.C[k] + ld<S>(c.lam[k], dir);
+  e.F[0] = js_min(e.F[0], S(0.0));
+  const S bounds = fabs(e.F[0]) * ld<S>(m.friction, dir);
+  const S fs = sqrt(e.F[1] * e.F[1] + e.F[2] * e.F[2]);
   if (fs > bounds && fs > 0.0) {
     e.F[1] *= bounds / fs;
     e.F[2] *= bounds / fs;
@@ -824,114 +879,134 @@ __device__ ContactEvalT contact_eval(const TWorld &w, const TManifold &m, int i,
   return e;
 }
 
-// H += J_lin^T K J_lin etc. of one 3-row block with diagonal K.
-template <class S>
-__device__ void stamp_rows(S &s, const R *jLin, const R *jAng, const R *Kd, const R *F) {
-  R jLinT[9], jAngT[9], jAngTk[9], m0[9], acc[3];
-  m3_transpose(jLinT, jLin);
-  m3_transpose(jAngT, jAng);
-  for (int r = 0; r < 3; r++)
+// H += J_lin^T K J_lin etc. of one 3-row block with diagonal K: entry (r, c)
+// is sum_k (J[k][r] K[k]) J[k][c] over k = 0, 1, 2 in order, the terms of
+// transpose, column scale and 3x3 product, and f += J^T F likewise.
+template <class S, class Sink>
+__device__ void stamp_rows(Sink &s, const S *jLin, const S *jAng, const S *Kd, const S *F) {
+  for (int r = 0; r < 3; r++) {
+    const S l0 = jLin[r] * Kd[0], l1 = jLin[3 + r] * Kd[1], l2 = jLin[6 + r] * Kd[2];
+    const S a0 = jAng[r] * Kd[0], a1 = jAng[3 + r] * Kd[1], a2 = jAng[6 + r] * Kd[2];
     for (int c = 0; c < 3; c++) {
-      jAngTk[r * 3 + c] = jAngT[r * 3 + c] * Kd[c];
-      m0[r * 3 + c] = jLinT[r * 3 + c] * Kd[c];
+      s.lin[r * 3 + c] += l0 * jLin[c] + l1 * jLin[3 + c] + l2 * jLin[6 + c];
+      s.ang[r * 3 + c] += a0 * jAng[c] + a1 * jAng[3 + c] + a2 * jAng[6 + c];
+      s.cross[r * 3 + c] += a0 * jLin[c] + a1 * jLin[3 + c] + a2 * jLin[6 + c];
     }
-  m3_mul(m0, m0, jLin);
-  m3_add_into(s.lin, m0);
-  m3_mul(m0, jAngTk, jAng);
-  m3_add_into(s.ang, m0);
-  m3_mul(m0, jAngTk, jLin);
-  m3_add_into(s.cross, m0);
-  m3_mul_vec(acc, jLinT, F);
-  v3_add_into(s.bl, acc);
-  m3_mul_vec(acc, jAngT, F);
-  v3_add_into(s.ba, acc);
+  }
+  for (int r = 0; r < 3; r++) {
+    s.bl[r] += jLin[r] * F[0] + jLin[3 + r] * F[1] + jLin[6 + r] * F[2];
+    s.ba[r] += jAng[r] * F[0] + jAng[3 + r] * F[1] + jAng[6 + r] * F[2];
+  }
 }
 
 // manifold.js:411-445, contact i of the manifold
-template <class S>
-__device__ void contact_primal(const TWorld &w, const TManifold &m, int i, int side, R alpha, S &s) {
-  R jBLin[9];
-  for (int k = 0; k < 9; k++) jBLin[k] = -m.basis[k];
-  R jAAng[9], jBAng[9];
-  const ContactEvalT e = contact_eval(w, m, i, alpha, jAAng, jBAng);
-  stamp_rows(s, side ? jBLin : m.basis, side ? jBAng : jAAng, m.c[i].pen, e.F);
+template <class S, class Sink>
+__device__ void contact_primal(const TWorld &w, const TManifold &m, int i, int side, R alpha, Sink &s, int dir) {
+  S basis[9], jAAng[9], jBAng[9], pen[3];
+  const ContactEvalT<S> e = contact_eval(w, m, i, alpha, basis, jAAng, jBAng, dir);
+  for (int k = 0; k < 9; k++) {  // body B's rows: -basis and its angular Jacobian
+    if (side) basis[k] = -basis[k];
+    jAAng[k] = side ? jBAng[k] : jAAng[k];
+  }
+  ldn(pen, m.c[i].pen, 3, dir);
+  stamp_rows(s, basis, jAAng, pen, e.F);
 }
 
 // joint.js:214-221: the geometric stiffness of a ball socket, lumped
-__device__ void ball_socket_geometric(R *G, const R *r, const R *F) {
-  R H[9];
+template <class S>
+__device__ void ball_socket_geometric(S *G, const S *r, const S *F) {
+  S H[9];
   m3_zero(H);
   for (int k = 0; k < 3; k++) {  // geometricStiffnessBallSocket(v = r, k) * F[k]
-    R g[9];
+    S g[9];
     m3_diag(g, -r[k], -r[k], -r[k]);
     g[0 * 3 + k] += r[0];
     g[1 * 3 + k] += r[1];
     g[2 * 3 + k] += r[2];
     for (int q = 0; q < 9; q++) H[q] += g[q] * F[k];
   }
-  const R c0 = sqrt(H[0] * H[0] + H[3] * H[3] + H[6] * H[6]);
-  const R c1 = sqrt(H[1] * H[1] + H[4] * H[4] + H[7] * H[7]);
-  const R c2 = sqrt(H[2] * H[2] + H[5] * H[5] + H[8] * H[8]);
+  const S c0 = sqrt(H[0] * H[0] + H[3] * H[3] + H[6] * H[6]);
+  const S c1 = sqrt(H[1] * H[1] + H[4] * H[4] + H[7] * H[7]);
+  const S c2 = sqrt(H[2] * H[2] + H[5] * H[5] + H[8] * H[8]);
   m3_diag(G, c0, c1, c2);
 }
 
+// the value of |x|^2 > 0 (the branch tests of the joint's rows)
+__device__ __forceinline__ bool nonzero3(const R *x) {
+  return x[0].v * x[0].v + x[1].v * x[1].v + x[2].v * x[2].v > 0.0;
+}
+
 // joint.js:162-253
-template <class S>
-__device__ void joint_primal(const TWorld &w, const TJoint &j, int side, R alpha, S &s) {
-  R C[3], F[3];
-  if (v3_len_sq(j.penLin) > 0.0) {
-    joint_eval_lin(w, j, C);
-    if (j.stiffLin.v == INFINITY)
-      for (int k = 0; k < 3; k++) C[k] = C[k] + j.C0Lin[k] * (-alpha);
-    for (int k = 0; k < 3; k++) F[k] = j.penLin[k] * C[k] + j.lamLin[k];
-    R jLin[9], jAng[9], rW[3], r[3];
+template <class S, class Sink>
+__device__ void joint_primal(const TWorld &w, const TJoint &j, int side, R alpha, Sink &s, int dir) {
+  S C[3], F[3], pen[3];
+  if (nonzero3(j.penLin)) {
+    joint_eval_lin(w, j, C, dir);
+    if (j.stiffLin.v == INFINITY) {
+      const S na = -ld<S>(alpha, dir);
+      for (int k = 0; k < 3; k++) C[k] = C[k] + ld<S>(j.C0Lin[k], dir) * na;
+    }
+    ldn(pen, j.penLin, 3, dir);
+    for (int k = 0; k < 3; k++) F[k] = pen[k] * C[k] + ld<S>(j.lamLin[k], dir);
+    S jLin[9], jAng[9], rW[3], r[3], q[4], rl[3];
     if (!side) {
-      m3_diag(jLin, R(1.0), R(1.0), R(1.0));
-      q_rotate(rW, w.b[j.a].q, j.rA);
+      m3_diag(jLin, S(1.0), S(1.0), S(1.0));
+      ldn(q, w.b[j.a].q, 4, dir);
+      ldn(rl, j.rA, 3, dir);
+      q_rotate(rW, q, rl);
       for (int k = 0; k < 3; k++) r[k] = -rW[k];
       m3_skew(jAng, r);
       for (int k = 0; k < 3; k++) r[k] = rW[k];
     } else {
-      m3_diag(jLin, R(-1.0), R(-1.0), R(-1.0));
-      q_rotate(rW, w.b[j.b].q, j.rB);
+      m3_diag(jLin, S(-1.0), S(-1.0), S(-1.0));
+      ldn(q, w.b[j.b].q, 4, dir);
+      ldn(rl, j.rB, 3, dir);
+      q_rotate(rW, q, rl);
       m3_skew(jAng, rW);
       for (int k = 0; k < 3; k++) r[k] = -rW[k];
     }
-    stamp_rows(s, jLin, jAng, j.penLin, F);
-    R G[9];
+    stamp_rows(s, jLin, jAng, pen, F);
+    S G[9];
     ball_socket_geometric(G, r, F);
     m3_add_into(s.ang, G);
   }
-  if (v3_len_sq(j.penAng) > 0.0) {
-    joint_eval_ang(w, j, C);
-    if (j.stiffAng.v == INFINITY)
-      for (int k = 0; k < 3; k++) C[k] = C[k] + j.C0Ang[k] * (-alpha);
-    for (int k = 0; k < 3; k++) F[k] = j.penAng[k] * C[k] + j.lamAng[k];
+  if (nonzero3(j.penAng)) {
+    joint_eval_ang(w, j, C, dir);
+    if (j.stiffAng.v == INFINITY) {
+      const S na = -ld<S>(alpha, dir);
+      for (int k = 0; k < 3; k++) C[k] = C[k] + ld<S>(j.C0Ang[k], dir) * na;
+    }
+    ldn(pen, j.penAng, 3, dir);
+    for (int k = 0; k < 3; k++) F[k] = pen[k] * C[k] + ld<S>(j.lamAng[k], dir);
     const double sg = side ? -j.torqueArm : j.torqueArm;
     // jAng = sg I: H_ang += sg K sg, f_ang += sg F
     for (int k = 0; k < 3; k++) {
-      s.ang[k * 3 + k] += (sg * j.penAng[k]) * sg;
+      s.ang[k * 3 + k] += (sg * pen[k]) * sg;
       s.ba[k] += F[k] * sg;
     }
   }
 }
 
 // spring.js:509-616
-template <class Sink>
-__device__ void spring_primal(const TWorld &w, const TSpring &sp, int side, Sink &s, const TParams &P) {
+template <class S, class Sink>
+__device__ void spring_primal(const TWorld &w, const TSpring &sp, int side, Sink &s, const TParams &P, int dir) {
   if (sp.broken) return;
-  R d[3], n[3];
-  const R Cv = spring_eval(w, sp, d, n);
+  S d[3], n[3];
+  const S Cv = spring_eval(w, sp, d, n, dir);
   if (Cv != Cv) return;
-  const R k = sp.penalty;
-  const R f = k * Cv;
-  R rW[3], jLin[3], jAng[3];
+  const S k = ld<S>(sp.penalty, dir);
+  const S f = k * Cv;
+  S rW[3], jLin[3], jAng[3], q[4], rl[3];
   if (!side) {
-    q_rotate(rW, w.b[sp.a].q, sp.rA);
+    ldn(q, w.b[sp.a].q, 4, dir);
+    ldn(rl, sp.rA, 3, dir);
+    q_rotate(rW, q, rl);
     for (int c = 0; c < 3; c++) jLin[c] = n[c];
     v3_cross(jAng, rW, n);
   } else {
-    q_rotate(rW, w.b[sp.b].q, sp.rB);
+    ldn(q, w.b[sp.b].q, 4, dir);
+    ldn(rl, sp.rB, 3, dir);
+    q_rotate(rW, q, rl);
     for (int c = 0; c < 3; c++) jLin[c] = -n[c];
     v3_cross(jAng, rW, n);
     for (int c = 0; c < 3; c++) jAng[c] = -jAng[c];
@@ -945,59 +1020,64 @@ __device__ void spring_primal(const TWorld &w, const TSpring &sp, int side, Sink
   v3_add_scaled(s.bl, jLin, f);
   v3_add_scaled(s.ba, jAng, f);
   if (!P.springGeometric) return;
-  const R dLen = sqrt(v3_len_sq(d));
+  const S dLen = sqrt(v3_len_sq(d));
   const double sg = side ? -1.0 : 1.0;
-  R Pm[9], S[9], Gla[9], Gal[9], Gaa[9], m0[9];
+  S Pm[9], Sk[9], Gla[9], Gal[9], Gaa[9], m0[9];
   for (int r = 0; r < 3; r++)
     for (int c = 0; c < 3; c++) Pm[r * 3 + c] = -(n[r] * n[c]);
   Pm[0] = Pm[0] + 1.0; Pm[4] = Pm[4] + 1.0; Pm[8] = Pm[8] + 1.0;
   for (int q = 0; q < 9; q++) Pm[q] = Pm[q] / dLen;
-  m3_skew(S, rW);
-  m3_mul(Gla, Pm, S);
+  m3_skew(Sk, rW);
+  m3_mul(Gla, Pm, Sk);
   for (int q = 0; q < 9; q++) Gla[q] = -Gla[q];
-  m3_mul(Gal, S, Pm);
-  m3_mul(Gaa, S, Pm);
-  m3_mul(Gaa, Gaa, S);
+  m3_mul(Gal, Sk, Pm);
+  m3_mul(Gaa, Sk, Pm);
+  m3_mul(Gaa, Gaa, Sk);
   for (int q = 0; q < 9; q++) Gaa[q] = -Gaa[q];
-  const R ndotr = v3_dot(n, rW);
+  const S ndotr = v3_dot(n, rW);
   for (int r = 0; r < 3; r++)
     for (int c = 0; c < 3; c++) m0[r * 3 + c] = rW[r] * n[c];
   m0[0] = m0[0] - ndotr; m0[4] = m0[4] - ndotr; m0[8] = m0[8] - ndotr;
   for (int q = 0; q < 9; q++) Gaa[q] += m0[q] * sg;
-  const R af = fabs(f);
+  const S af = fabs(f);
   for (int c = 0; c < 3; c++) {
-    const R a0 = Pm[c], a1 = Pm[3 + c], a2 = Pm[6 + c], a3 = Gal[c], a4 = Gal[3 + c], a5 = Gal[6 + c];
+    const S a0 = Pm[c], a1 = Pm[3 + c], a2 = Pm[6 + c], a3 = Gal[c], a4 = Gal[3 + c], a5 = Gal[6 + c];
     s.lin[c * 3 + c] += sqrt(a0 * a0 + a1 * a1 + a2 * a2 + a3 * a3 + a4 * a4 + a5 * a5) * af;
   }
   for (int c = 0; c < 3; c++) {
-    const R a0 = Gla[c], a1 = Gla[3 + c], a2 = Gla[6 + c], a3 = Gaa[c], a4 = Gaa[3 + c], a5 = Gaa[6 + c];
+    const S a0 = Gla[c], a1 = Gla[3 + c], a2 = Gla[6 + c], a3 = Gaa[c], a4 = Gaa[3 + c], a5 = Gaa[6 + c];
     s.ang[c * 3 + c] += sqrt(a0 * a0 + a1 * a1 + a2 * a2 + a3 * a3 + a4 * a4 + a5 * a5) * af;
   }
 }
 
-// One body's update (solver.js:425-457) by one block of kBodyThreads. The
-// body's constraint rows - each contact of each manifold, each joint, each
-// spring, newest force first - go to the threads kBodyThreads at a time;
-// every thread records the addends its row makes to each of the 33 system
-// entries (RecSys6), and thread e then adds the recorded addends of entry e
-// row after row: every entry is summed in the f64 engine's order, so the
-// values stay the serial update's. The inertial terms (the entries' first
-// values) are formed by the last thread while the first threads walk the
-// body's force list.
-constexpr int kBodyThreads = 64;
+// One body's update (solver.js:425-457) by one block of kBodyThreads: five
+// threads (one per tangent direction, each also computing the value) per
+// constraint row. The body's rows - each contact of each manifold, each
+// joint, each spring, newest force first - go to the threads kRowsPerPass at
+// a time; every thread records its direction of the addends its row makes to
+// each of the 33 system entries (RecSys6), and then each double of each
+// entry (its value or one derivative) is summed by one thread row after row:
+// every entry is summed in the f64 engine's order, so the values stay the
+// serial update's. The inertial terms (the entries' first values) are formed
+// by the last five threads while the first walks the body's force list.
+constexpr int kRowsPerPass = 51;
+constexpr int kBodyThreads = 256;  // two warps per SM sub-partition: 255 registers a thread
+static_assert(kRowsPerPass * kTangentDims <= kBodyThreads, "five threads per row");
+constexpr int kDualDoubles = kTangentDims + 1;
+static_assert(sizeof(R) == kDualDoubles * sizeof(double), "a dual number is its value and its derivatives");
 struct BodySmem {
-  R rec[kBodyThreads][kRecSlots];  // a thread's row: its addends per entry
-  unsigned char cnt[kBodyThreads][kSysEntries + 3];
-  R acc[kSysEntries];              // the entries, summed so far
-  uint32_t items[kBodyThreads];    // (force entry << 3) | contact
+  R rec[kRowsPerPass][kRecSlots];                  // a row's addends per entry
+  unsigned char cnt[kBodyThreads][kSysEntries + 3];  // a thread's addends per entry
+  R acc[kSysEntries];                              // the entries, summed so far
+  uint32_t items[kRowsPerPass];                    // (force entry << 3) | contact
   int nItems, cursorE, cursorC;
 };
 
-// The next (up to) kBodyThreads rows of body i's force list, from the cursor.
+// The next (up to) kRowsPerPass rows of body i's force list, from the cursor.
 __device__ void next_rows(const TWorld &w, int i, BodySmem &sm) {
   int n = 0, e = sm.cursorE, c = sm.cursorC;
   const int e0 = w.fStart[i];
-  while (n < kBodyThreads && e >= e0) {
+  while (n < kRowsPerPass && e >= e0) {
     const uint32_t ref = w.fRef[e];
     if ((ref >> 30) == 0) {
       if (c < w.cur[(ref >> 1) & 0x1fffffffu].count) {
@@ -1058,26 +1138,30 @@ __device__ void body_update_block(const TWorld &w, int i, R alpha, BodySmem &sm)
   for (;;) {
     const int n = sm.nItems;
     if (n == 0) break;
-    if (t < n) {
+    const int row = t / kTangentDims, dir = t % kTangentDims;
+    if (row < n) {
       for (int k = 0; k < kSysEntries; k++) sm.cnt[t][k] = 0;
-      RecSys6 rs(sm.rec[t], sm.cnt[t]);
-      const uint32_t item = sm.items[t];
+      RecSys6 rs(sm.rec[row], sm.cnt[t], dir);
+      const uint32_t item = sm.items[row];
       const uint32_t ref = w.fRef[item >> 3];
       const uint32_t type = ref >> 30, idx = (ref >> 1) & 0x1fffffffu, side = ref & 1u;
-      if (type == 0) contact_primal(w, w.cur[idx], (int)(item & 7u), (int)side, alpha, rs);
-      else if (type == kRefJoint) joint_primal(w, w.j[idx], (int)side, alpha, rs);
-      else spring_primal(w, w.s[idx], (int)side, rs, P);
+      if (type == 0) contact_primal<Dual1>(w, w.cur[idx], (int)(item & 7u), (int)side, alpha, rs, dir);
+      else if (type == kRefJoint) joint_primal<Dual1>(w, w.j[idx], (int)side, alpha, rs, dir);
+      else spring_primal<Dual1>(w, w.s[idx], (int)side, rs, P, dir);
     }
     __syncthreads();
-    for (int entry = t; entry < kSysEntries; entry += nt) {
-      R a = sm.acc[entry];
+    for (int q = t; q < kSysEntries * kDualDoubles; q += nt) {  // one double of one entry per thread
+      const int entry = q / kDualDoubles, part = q % kDualDoubles;
+      double *accp = reinterpret_cast<double *>(&sm.acc[entry]) + part;
+      double a = *accp;
       const int cap = rec_cap(entry), off = rec_off(entry);
       for (int it = 0; it < n; it++) {
-        const int k = sm.cnt[it][entry];
+        const int k = sm.cnt[it * kTangentDims][entry];  // the same count in every direction
         if (k > cap) w.ctl[7] = 1;  // more addends than recorded: the result is not the serial sum
-        for (int q = 0; q < k && q < cap; q++) a += sm.rec[it][off + q];
+        const double *r = reinterpret_cast<const double *>(&sm.rec[it][off]) + part;
+        for (int m = 0; m < k && m < cap; m++) a += r[m * kDualDoubles];
       }
-      sm.acc[entry] = a;
+      *accp = a;
     }
     if (t == nt - 1) next_rows(w, i, sm);  // the rows are recorded; the replay reads only rec and cnt
     __syncthreads();
@@ -1126,8 +1210,8 @@ __device__ void contact_dual(const TWorld &w, TManifold &m, int i, R alpha) {
   const TParams &P = w.P;
   const bool sphere = w.bs[m.a].shape == AVBD_SHAPE_SPHERE || w.bs[m.b].shape == AVBD_SHAPE_SPHERE;
   {
-    R jAAng[9], jBAng[9];
-    const ContactEvalT e = contact_eval(w, m, i, alpha, jAAng, jBAng);
+    R basis[9], jAAng[9], jBAng[9];
+    const ContactEvalT<R> e = contact_eval(w, m, i, alpha, basis, jAAng, jBAng);
     TContact &c = m.c[i];
     for (int k = 0; k < 3; k++) c.lam[k] = e.F[k];
     if (e.F[0] < 0.0) c.pen[0] = js_min(c.pen[0] + P.betaLin * fabs(e.C[0]), P.penaltyMax);
@@ -1220,7 +1304,7 @@ __device__ bool tg_grid_sync(const TWorld &w) {
 // dual update (a thread per contact, joint, spring), and on the last
 // iteration the BDF1 velocity (solver.js:476-488); a grid barrier between
 // phases.
-__global__ void __launch_bounds__(kBodyThreads) iterate_kernel(TWorld w) {
+__global__ void __launch_bounds__(kBodyThreads, 1) iterate_kernel(TWorld w) {
   if (w.ctl[2]) return;
   extern __shared__ __align__(16) unsigned char smemRaw[];
   BodySmem &sm = *reinterpret_cast<BodySmem *>(smemRaw);
