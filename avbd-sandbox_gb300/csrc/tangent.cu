@@ -105,6 +105,10 @@ struct TWorld {
   // angular Jacobian rows of A and B at the x_t orientations (the cached
   // Jacobians of manifold.js:325-350), computed once per step
   R *jac;
+  // per body: the 33 inertial entries of its next update's system (they
+  // depend only on the body's own iterate, so they are formed in the phase
+  // before its colour's)
+  R *inert;
   TBodyStatic *bs;
   const uint32_t *cRef;
   TJoint *j;
@@ -1058,8 +1062,8 @@ __device__ void spring_primal(const TWorld &w, const TSpring &sp, int side, Sink
 // each of the 33 system entries (RecSys6), and then each double of each
 // entry (its value or one derivative) is summed by one thread row after row:
 // every entry is summed in the f64 engine's order, so the values stay the
-// serial update's. The inertial terms (the entries' first values) are formed
-// by the last five threads while the first walks the body's force list.
+// serial update's. The inertial terms (the entries' first values) were
+// formed in the phase before (inertial_terms).
 constexpr int kRowsPerPass = 51;
 constexpr int kBodyThreads = 256;  // two warps per SM sub-partition: 255 registers a thread
 static_assert(kRowsPerPass * kTangentDims <= kBodyThreads, "five threads per row");
@@ -1098,37 +1102,47 @@ __device__ void next_rows(const TWorld &w, int i, BodySmem &sm) {
   sm.cursorC = c;
 }
 
+// solver.js:425-433: the inertial terms M/dt^2 and M (x - y)/dt^2 of body
+// i's system, tangent direction k, into its entries of w.inert (the value
+// by direction 0).
+__device__ void inertial_terms(const TWorld &w, int i, int k) {
+  using S = Dual1;
+  const TParams &P = w.P;
+  const TBody &b = w.b[i];
+  const TBodyStatic &st = w.bs[i];
+  const double dt2 = P.dt * P.dt;
+  S p[3], yl[3], q[4], yq[4];
+  for (int c = 0; c < 3; c++) {
+    p[c] = dir_of(b.p[c], k);
+    yl[c] = dir_of(b.yl[c], k);
+  }
+  for (int c = 0; c < 4; c++) {
+    q[c] = dir_of(b.q[c], k);
+    yq[c] = dir_of(b.yq[c], k);
+  }
+  Sys6T<S> s;
+  S MAng[9], tmp[3], dq[3];
+  m3_diag(s.lin, S(st.mass / dt2), S(st.mass / dt2), S(st.mass / dt2));
+  world_moment(MAng, st, q, P.rotatedInertia != 0);
+  for (int c = 0; c < 9; c++) s.ang[c] = MAng[c] / dt2;
+  m3_zero(s.cross);
+  v3_sub(tmp, p, yl);
+  m3_mul_vec(s.bl, s.lin, tmp);
+  q_subtract(dq, q, yq);
+  m3_mul_vec(s.ba, s.ang, dq);
+  const S *e = &s.lin[0];
+  R *o = &w.inert[(size_t)i * kSysEntries];
+  for (int c = 0; c < kSysEntries; c++) {
+    if (k == 0) o[c].v = e[c].v;
+    o[c].d[k] = e[c].d[0];
+  }
+}
+
 __device__ void body_update_block(const TWorld &w, int i, R alpha, BodySmem &sm) {
   const TParams &P = w.P;
   const int t = threadIdx.x, nt = blockDim.x;
-  if (t >= nt - kTangentDims) {  // the inertial terms, one tangent direction per thread
-    using S = Dual1;
-    const int k = t - (nt - kTangentDims);
-    const TBody &b = w.b[i];
-    const TBodyStatic &st = w.bs[i];
-    const double dt2 = P.dt * P.dt;
-    S p[3], yl[3], q[4], yq[4];
-    for (int c = 0; c < 3; c++) {
-      p[c] = dir_of(b.p[c], k);
-      yl[c] = dir_of(b.yl[c], k);
-    }
-    for (int c = 0; c < 4; c++) {
-      q[c] = dir_of(b.q[c], k);
-      yq[c] = dir_of(b.yq[c], k);
-    }
-    Sys6T<S> s;
-    S MAng[9], tmp[3], dq[3];
-    m3_diag(s.lin, S(st.mass / dt2), S(st.mass / dt2), S(st.mass / dt2));
-    world_moment(MAng, st, q, P.rotatedInertia != 0);
-    for (int c = 0; c < 9; c++) s.ang[c] = MAng[c] / dt2;
-    m3_zero(s.cross);
-    v3_sub(tmp, p, yl);
-    m3_mul_vec(s.bl, s.lin, tmp);
-    q_subtract(dq, q, yq);
-    m3_mul_vec(s.ba, s.ang, dq);
-    const S *e = &s.lin[0];
-    for (int c = 0; c < kSysEntries; c++) set_dir(sm.acc[c], e[c], k);
-  }
+  for (int q = t; q < kSysEntries * kDualDoubles; q += nt)  // the inertial terms, formed ahead
+    reinterpret_cast<double *>(sm.acc)[q] = reinterpret_cast<const double *>(&w.inert[(size_t)i * kSysEntries])[q];
   if (t == 0) {
     sm.cursorE = w.fStart[i + 1] - 1;  // the body's forces, newest first
     sm.cursorC = 0;
@@ -1313,6 +1327,12 @@ __global__ void __launch_bounds__(kBodyThreads, 1) iterate_kernel(TWorld w) {
   const int total_it = P.iterations + (P.postStabilize ? 1 : 0);
   // thread index spread so that consecutive items land on different SMs
   const int g = blockIdx.x + gridDim.x * threadIdx.x, gs = gridDim.x * blockDim.x;
+  // the inertial terms from the top of the thread range (the dual updates
+  // take it from the bottom)
+  const int gi = gs - 1 - g;
+  for (int q = gi; q < w.n * kTangentDims; q += gs)
+    if (w.bs[q / kTangentDims].mass > 0) inertial_terms(w, q / kTangentDims, q % kTangentDims);
+  if (!tg_grid_sync(w)) return;
   for (int it = 0; it < total_it; it++) {
     const R alpha = P.postStabilize ? (it < P.iterations ? 1.0 : 0.0) : P.alpha;
     for (int c = 0; c < numColors; c++) {
@@ -1329,6 +1349,9 @@ __global__ void __launch_bounds__(kBodyThreads, 1) iterate_kernel(TWorld w) {
       for (int k = g; k < w.nj; k += gs)
         if (!w.j[k].removed) joint_dual(w, w.j[k], alpha);
       for (int k = g; k < w.ns; k += gs) spring_dual(w, w.s[k]);
+      if (it + 1 < total_it)  // the next iteration's inertial terms (the iterates are final for this one)
+        for (int q = gi; q < w.n * kTangentDims; q += gs)
+          if (w.bs[q / kTangentDims].mass > 0) inertial_terms(w, q / kTangentDims, q % kTangentDims);
       if (!tg_grid_sync(w)) return;
     }
     if (it == P.iterations - 1) {
@@ -1580,7 +1603,8 @@ int tangent_pack(TangentCtx **out, const avbd_world *world, const avbd_params &P
       (e = t->alloc(&w.prev, w.mcap)) || (e = t->alloc(&w.prevKey, w.mcap)) || (e = t->alloc(&w.ctl, 8)) ||
       (e = t->alloc(&w.fStart, n + 1)) || (e = t->alloc(&w.fCount, n + 1)) || (e = t->alloc(&w.fRef, w.fcap)) ||
       (e = t->alloc(&w.color, n)) || (e = t->alloc(&w.order, n)) || (e = t->alloc(&w.colorStart, kMaxColors + 1)) ||
-      (e = t->alloc(&prioD, n)) || (e = t->alloc(&w.jac, (size_t)w.mcap * K8 * 18))) {
+      (e = t->alloc(&prioD, n)) || (e = t->alloc(&w.jac, (size_t)w.mcap * K8 * 18)) ||
+      (e = t->alloc(&w.inert, (size_t)n * kSysEntries))) {
     delete t;
     snprintf(msg, msgLen, "avbd_adjoint_forward: cudaMalloc: %s", cudaGetErrorString(e));
     return AVBD_ERR_CUDA;
