@@ -1054,48 +1054,73 @@ __device__ void spring_primal(const TWorld &w, const TSpring &sp, int side, Sink
   }
 }
 
-// One body's update (solver.js:425-457) by one block of kBodyThreads: five
-// threads (one per tangent direction, each also computing the value) per
-// constraint row. The body's rows - each contact of each manifold, each
-// joint, each spring, newest force first - go to the threads kRowsPerPass at
-// a time; every thread records its direction of the addends its row makes to
-// each of the 33 system entries (RecSys6), and then each double of each
-// entry (its value or one derivative) is summed by one thread row after row:
-// every entry is summed in the f64 engine's order, so the values stay the
-// serial update's. The inertial terms (the entries' first values) were
-// formed in the phase before (inertial_terms).
-constexpr int kRowsPerPass = 51;
+// One body's update (solver.js:425-457) by one block of kBodyThreads. The
+// body's constraint rows - each contact of each manifold, each joint, each
+// spring, newest force first - go to the threads up to kRowsPerPass at a
+// time, five threads per row (one per tangent direction, each also
+// computing the value). A warp holds six such groups, and the rows of one
+// kind (contact, joint, spring) start on a warp of their own: a warp's
+// threads then follow one instruction stream, and the kinds run side by
+// side on the SM's sub-partitions (an FP64 instruction costs the same
+// however few of its lanes are active). Every thread records its
+// direction of the addends its row makes to each of the 33 system entries
+// (RecSys6), and then each double of each entry (its value or one
+// derivative) is summed by one thread row after row in force order: every
+// entry is summed in the f64 engine's order, so the values stay the serial
+// update's. The inertial terms (the entries' first values) were formed in
+// the phase before (inertial_terms).
 constexpr int kBodyThreads = 256;  // two warps per SM sub-partition: 255 registers a thread
-static_assert(kRowsPerPass * kTangentDims <= kBodyThreads, "five threads per row");
+constexpr int kGroupsPerWarp = 6;  // 30 of a warp's 32 lanes
+constexpr int kRowsPerPass = kBodyThreads / 32 * kGroupsPerWarp;
 constexpr int kDualDoubles = kTangentDims + 1;
+static_assert(kGroupsPerWarp * kTangentDims <= 32, "a row's five threads in one warp");
 static_assert(sizeof(R) == kDualDoubles * sizeof(double), "a dual number is its value and its derivatives");
 struct BodySmem {
-  R rec[kRowsPerPass][kRecSlots];                  // a row's addends per entry
-  unsigned char cnt[kBodyThreads][kSysEntries + 3];  // a thread's addends per entry
-  R acc[kSysEntries];                              // the entries, summed so far
-  uint32_t items[kRowsPerPass];                    // (force entry << 3) | contact
+  R rec[kRowsPerPass][kRecSlots];                                 // a row's addends per entry
+  unsigned char cnt[kRowsPerPass * kTangentDims][kSysEntries + 3];  // a (row, direction)'s addends per entry
+  R acc[kSysEntries];                                             // the entries, summed so far
+  uint32_t items[kRowsPerPass];                                   // (force entry << 3) | contact, force order
+  signed char groupRow[kRowsPerPass];                             // the row of a thread group, or -1
   int nItems, cursorE, cursorC;
 };
 
-// The next (up to) kRowsPerPass rows of body i's force list, from the cursor.
+__device__ __forceinline__ int round_up_groups(int g) { return (g + kGroupsPerWarp - 1) / kGroupsPerWarp * kGroupsPerWarp; }
+
+// The next rows of body i's force list, from the cursor: as many as fit the
+// groups with each kind starting on a warp boundary.
 __device__ void next_rows(const TWorld &w, int i, BodySmem &sm) {
-  int n = 0, e = sm.cursorE, c = sm.cursorC;
+  int n = 0, e = sm.cursorE, c = sm.cursorC, per[3] = {0, 0, 0};
   const int e0 = w.fStart[i];
-  while (n < kRowsPerPass && e >= e0) {
+  while (e >= e0) {
     const uint32_t ref = w.fRef[e];
-    if ((ref >> 30) == 0) {
-      if (c < w.cur[(ref >> 1) & 0x1fffffffu].count) {
-        sm.items[n++] = ((uint32_t)e << 3) | (uint32_t)c;
-        c++;
-        continue;
-      }
+    const int kind = (ref >> 30) == 0 ? 0 : ((ref >> 30) == kRefJoint ? 1 : 2);
+    if (kind == 0 && c >= w.cur[(ref >> 1) & 0x1fffffffu].count) {  // the manifold's contacts are done
       e--;
       c = 0;
       continue;
     }
-    sm.items[n++] = (uint32_t)e << 3;
-    e--;
-    c = 0;
+    per[kind]++;
+    if (round_up_groups(per[0]) + round_up_groups(per[1]) + per[2] > kRowsPerPass) {
+      per[kind]--;
+      break;
+    }
+    if (kind == 0) {
+      sm.items[n++] = ((uint32_t)e << 3) | (uint32_t)c;
+      c++;
+    } else {
+      sm.items[n++] = (uint32_t)e << 3;
+      e--;
+      c = 0;
+    }
+  }
+  // contacts from group 0, joints and springs each from the next warp
+  int at[3] = {0, round_up_groups(per[0]), round_up_groups(per[0]) + round_up_groups(per[1])};
+  for (int g = 0; g < kRowsPerPass; g++) sm.groupRow[g] = -1;
+  for (int r = 0; r < n; r++) {
+    const uint32_t ref = w.fRef[sm.items[r] >> 3];
+    const int kind = (ref >> 30) == 0 ? 0 : ((ref >> 30) == kRefJoint ? 1 : 2);
+    const int g = at[kind]++;
+    sm.groupRow[g] = (signed char)r;
   }
   sm.nItems = n;
   sm.cursorE = e;
@@ -1152,10 +1177,12 @@ __device__ void body_update_block(const TWorld &w, int i, R alpha, BodySmem &sm)
   for (;;) {
     const int n = sm.nItems;
     if (n == 0) break;
-    const int row = t / kTangentDims, dir = t % kTangentDims;
-    if (row < n) {
-      for (int k = 0; k < kSysEntries; k++) sm.cnt[t][k] = 0;
-      RecSys6 rs(sm.rec[row], sm.cnt[t], dir);
+    const int lane = t & 31, group = (t >> 5) * kGroupsPerWarp + lane / kTangentDims, dir = lane % kTangentDims;
+    const int row = lane < kGroupsPerWarp * kTangentDims ? sm.groupRow[group] : -1;
+    if (row >= 0) {
+      unsigned char *cnt = sm.cnt[row * kTangentDims + dir];
+      for (int k = 0; k < kSysEntries; k++) cnt[k] = 0;
+      RecSys6 rs(sm.rec[row], cnt, dir);
       const uint32_t item = sm.items[row];
       const uint32_t ref = w.fRef[item >> 3];
       const uint32_t type = ref >> 30, idx = (ref >> 1) & 0x1fffffffu, side = ref & 1u;
