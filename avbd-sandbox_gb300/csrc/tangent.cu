@@ -1245,64 +1245,104 @@ __device__ void body_update_block(const TWorld &w, int i, R alpha, BodySmem &sm)
   __syncthreads();
 }
 
+// The dual updates, one tangent direction per thread of a five-lane group
+// (mask: the group's lanes). Every thread reads the force, the group
+// synchronises, and then each thread writes its direction (direction 0 the
+// value and the flags), so that no read sees a half-written dual number.
 // manifold.js:447-491, contact i of the manifold (the contacts' dual updates
 // are independent of one another)
-__device__ void contact_dual(const TWorld &w, TManifold &m, int i, R alpha) {
+__device__ void contact_dual_dir(const TWorld &w, TManifold &m, int i, R alpha, int dir, unsigned mask) {
+  using S = Dual1;
   const TParams &P = w.P;
   const bool sphere = w.bs[m.a].shape == AVBD_SHAPE_SPHERE || w.bs[m.b].shape == AVBD_SHAPE_SPHERE;
-  {
-    R basis[9], jAAng[9], jBAng[9];
-    const ContactEvalT<R> e = contact_eval(w, m, i, alpha, basis, jAAng, jBAng);
-    TContact &c = m.c[i];
-    for (int k = 0; k < 3; k++) c.lam[k] = e.F[k];
-    if (e.F[0] < 0.0) c.pen[0] = js_min(c.pen[0] + P.betaLin * fabs(e.C[0]), P.penaltyMax);
-    if (e.within) {
-      c.pen[1] = js_min(c.pen[1] + P.betaLin * fabs(e.C[1]), P.penaltyMax);
-      c.pen[2] = js_min(c.pen[2] + P.betaLin * fabs(e.C[2]), P.penaltyMax);
-      c.stick = sqrt(e.C[1] * e.C[1] + e.C[2] * e.C[2]) < P.stickThreshold ? 1 : 0;
-    } else if (sphere) {
-      c.stick = 0;
-    }
+  S basis[9], jAAng[9], jBAng[9], pen[3];
+  const ContactEvalT<S> e = contact_eval(w, m, i, alpha, basis, jAAng, jBAng, dir);
+  TContact &c = m.c[i];
+  ldn(pen, c.pen, 3, dir);
+  const S pMax = ld<S>(P.penaltyMax, dir);
+  int stick = c.stick;
+  if (e.F[0] < 0.0) pen[0] = js_min(pen[0] + P.betaLin * fabs(e.C[0]), pMax);
+  if (e.within) {
+    pen[1] = js_min(pen[1] + P.betaLin * fabs(e.C[1]), pMax);
+    pen[2] = js_min(pen[2] + P.betaLin * fabs(e.C[2]), pMax);
+    stick = sqrt(e.C[1] * e.C[1] + e.C[2] * e.C[2]) < P.stickThreshold ? 1 : 0;
+  } else if (sphere) {
+    stick = 0;
   }
+  __syncwarp(mask);
+  for (int k = 0; k < 3; k++) {
+    set_dir(c.lam[k], e.F[k], dir);
+    set_dir(c.pen[k], pen[k], dir);
+  }
+  if (dir == 0) c.stick = stick;
 }
 
 // joint.js:255-317
-__device__ void joint_dual(const TWorld &w, TJoint &j, R alpha) {
+__device__ void joint_dual_dir(const TWorld &w, TJoint &j, R alpha, int dir, unsigned mask) {
+  using S = Dual1;
   const TParams &P = w.P;
-  R C[3];
-  if (v3_len_sq(j.penLin) > 0.0) {
-    joint_eval_lin(w, j, C);
+  S C[3], penL[3], penA[3], lamL[3], lamA[3];
+  ldn(penL, j.penLin, 3, dir);
+  ldn(penA, j.penAng, 3, dir);
+  ldn(lamL, j.lamLin, 3, dir);
+  ldn(lamA, j.lamAng, 3, dir);
+  const S pMax = ld<S>(P.penaltyMax, dir);
+  if (nonzero3(j.penLin)) {
+    joint_eval_lin(w, j, C, dir);
     if (j.stiffLin.v == INFINITY) {
-      for (int k = 0; k < 3; k++) C[k] = C[k] + j.C0Lin[k] * (-alpha);
-      for (int k = 0; k < 3; k++) j.lamLin[k] = j.penLin[k] * C[k] + j.lamLin[k];
+      const S na = -ld<S>(alpha, dir);
+      for (int k = 0; k < 3; k++) C[k] = C[k] + ld<S>(j.C0Lin[k], dir) * na;
+      for (int k = 0; k < 3; k++) lamL[k] = penL[k] * C[k] + lamL[k];
     }
-    const R cap = js_min(j.stiffLin, P.penaltyMax);
-    for (int k = 0; k < 3; k++) j.penLin[k] = js_min(j.penLin[k] + fabs(C[k]) * P.betaLin, cap);
+    const S cap = js_min(ld<S>(j.stiffLin, dir), pMax);
+    for (int k = 0; k < 3; k++) penL[k] = js_min(penL[k] + fabs(C[k]) * P.betaLin, cap);
   }
-  if (v3_len_sq(j.penAng) > 0.0) {
-    joint_eval_ang(w, j, C);
+  if (nonzero3(j.penAng)) {
+    joint_eval_ang(w, j, C, dir);
     if (j.stiffAng.v == INFINITY) {
-      for (int k = 0; k < 3; k++) C[k] = C[k] + j.C0Ang[k] * (-alpha);
-      for (int k = 0; k < 3; k++) j.lamAng[k] = j.penAng[k] * C[k] + j.lamAng[k];
+      const S na = -ld<S>(alpha, dir);
+      for (int k = 0; k < 3; k++) C[k] = C[k] + ld<S>(j.C0Ang[k], dir) * na;
+      for (int k = 0; k < 3; k++) lamA[k] = penA[k] * C[k] + lamA[k];
     }
-    const R cap = js_min(j.stiffAng, P.penaltyMax);
-    for (int k = 0; k < 3; k++) j.penAng[k] = js_min(j.penAng[k] + fabs(C[k]) * P.betaAng, cap);
+    const S cap = js_min(ld<S>(j.stiffAng, dir), pMax);
+    for (int k = 0; k < 3; k++) penA[k] = js_min(penA[k] + fabs(C[k]) * P.betaAng, cap);
   }
-  if (v3_len_sq(j.lamAng) > j.fracture * j.fracture) {
-    for (int k = 0; k < 3; k++) j.penLin[k] = j.penAng[k] = j.lamLin[k] = j.lamAng[k] = 0.0;
-    j.broken = 1;
+  const bool broken = v3_len_sq(lamA) > j.fracture * j.fracture;
+  if (broken)
+    for (int k = 0; k < 3; k++) penL[k] = penA[k] = lamL[k] = lamA[k] = S(0.0);
+  __syncwarp(mask);
+  for (int k = 0; k < 3; k++) {
+    set_dir(j.penLin[k], penL[k], dir);
+    set_dir(j.penAng[k], penA[k], dir);
+    set_dir(j.lamLin[k], lamL[k], dir);
+    set_dir(j.lamAng[k], lamA[k], dir);
   }
+  if (broken && dir == 0) j.broken = 1;
 }
 
-// spring.js:618-634
-__device__ void spring_dual(const TWorld &w, TSpring &s) {
+// spring.js:618-634 (the tear test of spring.js:461-470 inline)
+__device__ void spring_dual_dir(const TWorld &w, TSpring &s, int dir, unsigned mask) {
+  using S = Dual1;
   if (s.broken) return;
-  R d[3], n[3];
-  const R Cv = spring_eval(w, s, d, n);
+  S d[3], n[3];
+  const S Cv = spring_eval(w, s, d, n, dir);
   if (Cv != Cv) return;
-  if (isfinite(s.tear) && spring_tear(s, Cv)) return;
-  if (!w.P.springRamp) return;
-  s.penalty = js_min(s.penalty + fabs(Cv) * w.P.betaLin, js_min(s.stiffness, w.P.penaltyMax));
+  S peak = ld<S>(s.peak, dir), penalty = ld<S>(s.penalty, dir);
+  bool torn = false;
+  if (isfinite(s.tear) && s.rest > 1.0e-6) {  // spring_tear
+    const S strain = js_max(S(0.0), Cv / s.rest);
+    peak = js_max(peak, strain);
+    if (!(strain <= s.tear)) {
+      torn = true;
+      penalty = S(0.0);
+    }
+  }
+  if (!torn && w.P.springRamp)
+    penalty = js_min(penalty + fabs(Cv) * w.P.betaLin, js_min(ld<S>(s.stiffness, dir), ld<S>(w.P.penaltyMax, dir)));
+  __syncwarp(mask);
+  set_dir(s.peak, peak, dir);
+  set_dir(s.penalty, penalty, dir);
+  if (torn && dir == 0) s.broken = 1;
 }
 
 // Bounded grid barrier of the cooperative iterate kernel (ctl[4] arrivals,
@@ -1354,11 +1394,23 @@ __global__ void __launch_bounds__(kBodyThreads, 1) iterate_kernel(TWorld w) {
   const int total_it = P.iterations + (P.postStabilize ? 1 : 0);
   // thread index spread so that consecutive items land on different SMs
   const int g = blockIdx.x + gridDim.x * threadIdx.x, gs = gridDim.x * blockDim.x;
-  // the inertial terms from the top of the thread range (the dual updates
-  // take it from the bottom)
-  const int gi = gs - 1 - g;
-  for (int q = gi; q < w.n * kTangentDims; q += gs)
-    if (w.bs[q / kTangentDims].mass > 0) inertial_terms(w, q / kTangentDims, q % kTangentDims);
+  // The per-force phases run on five-lane groups, one tangent direction a
+  // lane, six groups a warp. Warps are numbered across the SMs first, and
+  // each kind of item (contacts, joints, springs, inertial terms) starts a
+  // quarter of the warps further on, so that the kinds run on different
+  // warps and their instruction streams side by side.
+  const int lane = threadIdx.x & 31, dir = lane % kTangentDims, slot = lane / kTangentDims;
+  const int nWarps = gridDim.x * (blockDim.x >> 5), wg = blockIdx.x + gridDim.x * (threadIdx.x >> 5);
+  const bool grouped = slot < kGroupsPerWarp;
+  const unsigned mask = grouped ? 0x1fu << (slot * kTangentDims) : 0u;
+  const int nGroups = nWarps * kGroupsPerWarp;
+  const int gContact = ((wg + 0 * (nWarps / 4)) % nWarps) * kGroupsPerWarp + slot;
+  const int gJoint = ((wg + 1 * (nWarps / 4)) % nWarps) * kGroupsPerWarp + slot;
+  const int gSpring = ((wg + 2 * (nWarps / 4)) % nWarps) * kGroupsPerWarp + slot;
+  const int gInert = ((wg + 3 * (nWarps / 4)) % nWarps) * kGroupsPerWarp + slot;
+  if (grouped)
+    for (int q = gInert; q < w.n; q += nGroups)
+      if (w.bs[q].mass > 0) inertial_terms(w, q, dir);
   if (!tg_grid_sync(w)) return;
   for (int it = 0; it < total_it; it++) {
     const R alpha = P.postStabilize ? (it < P.iterations ? 1.0 : 0.0) : P.alpha;
@@ -1368,17 +1420,19 @@ __global__ void __launch_bounds__(kBodyThreads, 1) iterate_kernel(TWorld w) {
       if (!tg_grid_sync(w)) return;
     }
     if (it < P.iterations) {
-      for (int k = g; k < total * kMaxContacts; k += gs) {
-        TManifold &m = w.cur[k / kMaxContacts];
-        const int i = k % kMaxContacts;
-        if (i < m.count) contact_dual(w, m, i, alpha);
+      if (grouped) {
+        for (int k = gContact; k < total * kMaxContacts; k += nGroups) {
+          TManifold &m = w.cur[k / kMaxContacts];
+          const int i = k % kMaxContacts;
+          if (i < m.count) contact_dual_dir(w, m, i, alpha, dir, mask);
+        }
+        for (int k = gJoint; k < w.nj; k += nGroups)
+          if (!w.j[k].removed) joint_dual_dir(w, w.j[k], alpha, dir, mask);
+        for (int k = gSpring; k < w.ns; k += nGroups) spring_dual_dir(w, w.s[k], dir, mask);
+        if (it + 1 < total_it)  // the next iteration's inertial terms (the iterates are final for this one)
+          for (int q = gInert; q < w.n; q += nGroups)
+            if (w.bs[q].mass > 0) inertial_terms(w, q, dir);
       }
-      for (int k = g; k < w.nj; k += gs)
-        if (!w.j[k].removed) joint_dual(w, w.j[k], alpha);
-      for (int k = g; k < w.ns; k += gs) spring_dual(w, w.s[k]);
-      if (it + 1 < total_it)  // the next iteration's inertial terms (the iterates are final for this one)
-        for (int q = gi; q < w.n * kTangentDims; q += gs)
-          if (w.bs[q / kTangentDims].mass > 0) inertial_terms(w, q / kTangentDims, q % kTangentDims);
       if (!tg_grid_sync(w)) return;
     }
     if (it == P.iterations - 1) {
