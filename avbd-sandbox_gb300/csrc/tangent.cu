@@ -1081,6 +1081,7 @@ struct BodySmem {
   R acc[kSysEntries];                                             // the entries, summed so far
   uint32_t items[kRowsPerPass];                                   // (force entry << 3) | contact, force order
   signed char groupRow[kRowsPerPass];                             // the row of a thread group, or -1
+  Dual1 ldl[kTangentDims][6][6];                                  // L of the 6x6 solve, per direction
   int nItems, cursorE, cursorC;
 };
 
@@ -1125,6 +1126,68 @@ __device__ void next_rows(const TWorld &w, int i, BodySmem &sm) {
   sm.nItems = n;
   sm.cursorE = e;
   sm.cursorC = c;
+}
+
+// The lanes of the six-lane row groups: 30 of warp 0's lanes, one row of
+// the 6x6 system and one tangent direction each.
+constexpr unsigned kSolveLanes = 0x3fffffffu;
+static_assert(kTangentDims * 6 <= 32, "the row groups fit one warp");
+__device__ __forceinline__ Dual1 shfl_dual(const Dual1 &a, int src) {
+  Dual1 o(__shfl_sync(kSolveLanes, a.v, src));
+  o.d[0] = __shfl_sync(kSolveLanes, a.d[0], src);
+  return o;
+}
+
+// solve6 above spread over the six rows of the system: lane r of direction
+// dir's group holds row r and forms L(r, j) as soon as D(j) is known, the
+// rows' divisions of one column at once. Every L, D, y, z and x is formed by
+// the same operations in the same order as in solve6 (the terms of a sum
+// left to right, a product's factors commuting exactly), so the values are
+// the serial solve's. acc: the 33 entries; returns x(r).
+__device__ Dual1 solve6_lanes(const R *acc, int dir, int r, Dual1 (&Lsm)[6][6]) {
+  using S = Dual1;
+  const int base = dir * 6;
+  S A[6], L[6], num[6];
+  for (int c = 0; c < 6; c++) {  // A(r, c), c <= r: lin, then cross and ang below the diagonal
+    const int e = r < 3 ? r * 3 + c : (c < 3 ? 18 + (r - 3) * 3 + c : 9 + (r - 3) * 3 + (c - 3));
+    A[c] = c <= r ? dir_of(acc[e], dir) : S(0.0);
+    L[c] = S(0.0);
+    num[c] = A[c];
+  }
+  const S b = -(r < 3 ? dir_of(acc[27 + r], dir) : dir_of(acc[30 + (r - 3)], dir));  // -bl, -ba
+  S D[6], dacc(0.0), Dr(0.0);
+#pragma unroll
+  for (int j = 0; j < 6; j++) {
+    const S Dj = j == 0 ? A[0] : A[j] - dacc;  // meaningful in lane j: D1 = A11, Dj = Ajj - (sum)
+    if (r == j) Dr = Dj;
+    D[j] = shfl_dual(Dj, base + j);
+    if (r > j) L[j] = num[j] / D[j];
+#pragma unroll
+    for (int c = j + 1; c < 6; c++) {  // column j of L from the lanes below
+      const S Lcj = shfl_dual(L[j], base + c);
+      if (r > c) num[c] = num[c] - (Lcj * L[j]) * D[j];
+    }
+    if (r > j) dacc = j == 0 ? (L[0] * L[0]) * D[0] : dacc + (L[j] * L[j]) * D[j];
+  }
+  // forward substitution: y(r) = b(r) - L(r,0) y(0) - L(r,1) y(1) - ...
+  S y = b;
+#pragma unroll
+  for (int j = 0; j < 5; j++) {
+    const S yj = shfl_dual(y, base + j);
+    if (r > j) y = y - L[j] * yj;
+  }
+  const S z = y / Dr;
+  // back substitution: x(r) = z(r) - L(r+1,r) x(r+1) - L(r+2,r) x(r+2) - ...
+  for (int c = 0; c < r; c++) Lsm[r][c] = L[c];
+  __syncwarp(kSolveLanes);
+  S x = z, xs[6];
+#pragma unroll
+  for (int c = 5; c > 0; c--) {
+    xs[c] = shfl_dual(x, base + c);  // final: its lane finished in the round before
+    if (r == c - 1)
+      for (int m = c; m < 6; m++) x = x - Lsm[m][r] * xs[m];
+  }
+  return x;
 }
 
 // solver.js:425-433: the inertial terms M/dt^2 and M (x - y)/dt^2 of body
@@ -1207,40 +1270,40 @@ __device__ void body_update_block(const TWorld &w, int i, R alpha, BodySmem &sm)
     if (t == nt - 1) next_rows(w, i, sm);  // the rows are recorded; the replay reads only rec and cnt
     __syncthreads();
   }
-  if (t < kTangentDims) {  // the 6x6 solve and the update, one tangent direction per thread
+  if (t < kTangentDims * 6) {  // the 6x6 solve over six lanes a direction, then the update
     using S = Dual1;
-    const int k = t;
-    TBody &b = w.b[i];
-    Sys6T<S> s;
-    S *e = &s.lin[0];
-    for (int c = 0; c < kSysEntries; c++) e[c] = dir_of(sm.acc[c], k);
-    S p[3], p0[3], q[4], q0[4];
+    const int k = t / 6, r = t % 6;
+    S x = solve6_lanes(sm.acc, k, r, sm.ldl[k]);
+    S xl[3], xa[3];
     for (int c = 0; c < 3; c++) {
-      p[c] = dir_of(b.p[c], k);
-      p0[c] = dir_of(b.p0[c], k);
+      xl[c] = shfl_dual(x, k * 6 + c);
+      xa[c] = shfl_dual(x, k * 6 + 3 + c);
     }
-    for (int c = 0; c < 4; c++) {
-      q[c] = dir_of(b.q[c], k);
-      q0[c] = dir_of(b.q0[c], k);
+    if (r == 0) {
+      constexpr unsigned kFirstLanes = 0x01041041u;  // lane 0 of each direction's six
+      TBody &b = w.b[i];
+      S p[3], p0[3], q[4], q0[4];
+      for (int c = 0; c < 3; c++) {
+        p[c] = dir_of(b.p[c], k);
+        p0[c] = dir_of(b.p0[c], k);
+      }
+      for (int c = 0; c < 4; c++) {
+        q[c] = dir_of(b.q[c], k);
+        q0[c] = dir_of(b.q0[c], k);
+      }
+      __syncwarp(kFirstLanes);  // every direction has read the body before any writes it
+      v3_add(p, p, xl);
+      S q1[4], dqL[3], dqA[3];
+      q_integrate(q1, q, xa);
+      v3_sub(dqL, p, p0);
+      q_subtract(dqA, q1, q0);
+      for (int c = 0; c < 3; c++) {
+        set_dir(b.p[c], p[c], k);
+        set_dir(b.dqL[c], dqL[c], k);
+        set_dir(b.dqA[c], dqA[c], k);
+      }
+      for (int c = 0; c < 4; c++) set_dir(b.q[c], q1[c], k);
     }
-    __syncwarp(0x1fu);  // every direction has read the body before any writes it
-    S xl[3], xa[3], nl[3], na[3];
-    for (int c = 0; c < 3; c++) {
-      nl[c] = -s.bl[c];
-      na[c] = -s.ba[c];
-    }
-    solve6(s.lin, s.ang, s.cross, nl, na, xl, xa);
-    v3_add(p, p, xl);
-    S q1[4], dqL[3], dqA[3];
-    q_integrate(q1, q, xa);
-    v3_sub(dqL, p, p0);
-    q_subtract(dqA, q1, q0);
-    for (int c = 0; c < 3; c++) {
-      set_dir(b.p[c], p[c], k);
-      set_dir(b.dqL[c], dqL[c], k);
-      set_dir(b.dqA[c], dqA[c], k);
-    }
-    for (int c = 0; c < 4; c++) set_dir(b.q[c], q1[c], k);
   }
   __syncthreads();
 }
