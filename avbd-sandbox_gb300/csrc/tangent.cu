@@ -54,6 +54,7 @@ struct TBody {
   R v[3], w[3];    // velocity, angular velocity
   R pv[3];         // previous velocity
   R p0[3], q0[4];  // x_t (initialLin / initialAng)
+  R q0i[4];        // q0's inverse q0* / |q0|^2, the right factor of every q_subtract(., q0) of the step
   R yl[3], yq[4];  // inertial target y
 };
 struct TBodyStatic {
@@ -706,6 +707,13 @@ __global__ void bodies_init_kernel(TWorld w) {
     if (!isfinite(weight)) weight = 0.0;
     for (int k = 0; k < 3; k++) b.p0[k] = b.p[k];
     for (int k = 0; k < 4; k++) b.q0[k] = b.q[k];
+    {  // q_subtract's inverse of q0, the same operations
+      const R lsq = b.q0[0] * b.q0[0] + b.q0[1] * b.q0[1] + b.q0[2] * b.q0[2] + b.q0[3] * b.q0[3];
+      b.q0i[0] = -b.q0[0] / lsq;
+      b.q0i[1] = -b.q0[1] / lsq;
+      b.q0i[2] = -b.q0[2] / lsq;
+      b.q0i[3] = b.q0[3] / lsq;
+    }
     if (dyn) {
       v3_add_scaled(b.p, b.v, R(dt));
       v3_add_scaled(b.p, g, weight * dt * dt);
@@ -1138,6 +1146,11 @@ __device__ __forceinline__ Dual1 shfl_dual(const Dual1 &a, int src) {
   return o;
 }
 
+// a[i] of four values, i in [0, 4), by selects (no local memory)
+__device__ __forceinline__ Dual1 pick4(const Dual1 *a, int i) {
+  return i == 0 ? a[0] : (i == 1 ? a[1] : (i == 2 ? a[2] : a[3]));
+}
+
 // solve6 above spread over the six rows of the system: lane r of direction
 // dir's group holds row r and forms L(r, j) as soon as D(j) is known, the
 // rows' divisions of one column at once. Every L, D, y, z and x is formed by
@@ -1274,36 +1287,58 @@ __device__ void body_update_block(const TWorld &w, int i, R alpha, BodySmem &sm)
     using S = Dual1;
     const int k = t / 6, r = t % 6;
     S x = solve6_lanes(sm.acc, k, r, sm.ldl[k]);
-    S xl[3], xa[3];
-    for (int c = 0; c < 3; c++) {
-      xl[c] = shfl_dual(x, k * 6 + c);
-      xa[c] = shfl_dual(x, k * 6 + 3 + c);
+    // the update (solver.js:450-457), one component a lane: rows 0-2 the
+    // position, 0-3 the orientation (q_integrate, then q_subtract against
+    // q0 with its inverse formed at the step's start); each component by the
+    // operations of the serial functions, a - b written a + (-b), which is
+    // exact
+    S xa[3];
+    for (int c = 0; c < 3; c++) xa[c] = shfl_dual(x, k * 6 + 3 + c);
+    TBody &b = w.b[i];
+    const int c3 = r < 3 ? r : 0, c4 = r < 4 ? r : 0;
+    S q[4], qi[4];
+    for (int c = 0; c < 4; c++) {
+      q[c] = dir_of(b.q[c], k);
+      qi[c] = dir_of(b.q0i[c], k);
     }
-    if (r == 0) {
-      constexpr unsigned kFirstLanes = 0x01041041u;  // lane 0 of each direction's six
-      TBody &b = w.b[i];
-      S p[3], p0[3], q[4], q0[4];
-      for (int c = 0; c < 3; c++) {
-        p[c] = dir_of(b.p[c], k);
-        p0[c] = dir_of(b.p0[c], k);
-      }
-      for (int c = 0; c < 4; c++) {
-        q[c] = dir_of(b.q[c], k);
-        q0[c] = dir_of(b.q0[c], k);
-      }
-      __syncwarp(kFirstLanes);  // every direction has read the body before any writes it
-      v3_add(p, p, xl);
-      S q1[4], dqL[3], dqA[3];
-      q_integrate(q1, q, xa);
-      v3_sub(dqL, p, p0);
-      q_subtract(dqA, q1, q0);
-      for (int c = 0; c < 3; c++) {
-        set_dir(b.p[c], p[c], k);
-        set_dir(b.dqL[c], dqL[c], k);
-        set_dir(b.dqA[c], dqA[c], k);
-      }
-      for (int c = 0; c < 4; c++) set_dir(b.q[c], q1[c], k);
+    const S p = dir_of(b.p[c3], k), p0 = dir_of(b.p0[c3], k);
+    __syncwarp(kSolveLanes);  // every lane has read the body before any writes it
+    // q_integrate: p_c = 0 q_c + wx q_. + wy q_. + wz q_. (quaternion product
+    // signs), r_c = q_c + p_c / 2, q1_c = r_c / |r|
+    constexpr unsigned kIntIdx = (3u << 0) | (2u << 2) | (1u << 4) | (2u << 6) | (3u << 8) | (0u << 10) |
+                                 (1u << 12) | (0u << 14) | (3u << 16) | (0u << 18) | (1u << 20) | (2u << 22);
+    constexpr unsigned kIntNeg = (1u << 2) | (1u << 3) | (1u << 7) | (1u << 9) | (1u << 10) | (1u << 11);
+    S pc = 0.0 * pick4(q, c4);
+    for (int m = 0; m < 3; m++) {
+      const int bit = 3 * c4 + m;
+      const S wm = (kIntNeg >> bit) & 1u ? -xa[m] : xa[m];
+      pc = pc + wm * pick4(q, (int)((kIntIdx >> (2 * bit)) & 3u));
     }
+    const S rc = pick4(q, c4) + pc * 0.5;
+    S rq[4];
+    for (int m = 0; m < 4; m++) rq[m] = shfl_dual(rc, k * 6 + m);
+    const S len = sqrt(rq[0] * rq[0] + rq[1] * rq[1] + rq[2] * rq[2] + rq[3] * rq[3]);
+    const S q1 = rc / len;
+    S a[4];  // q1 (x, y, z, w)
+    for (int m = 0; m < 4; m++) a[m] = shfl_dual(q1, k * 6 + m);
+    // q_subtract(q1, q0) = 2 (q1 * q0^-1).xyz: terms aw, ax, ay, az in order
+    constexpr unsigned kSubIdx = (0u << 0) | (3u << 2) | (2u << 4) | (1u << 6) | (1u << 8) | (2u << 10) |
+                                 (3u << 12) | (0u << 14) | (2u << 16) | (1u << 18) | (0u << 20) | (3u << 22);
+    constexpr unsigned kSubNeg = (1u << 3) | (1u << 5) | (1u << 10);
+    S dqa = a[3] * pick4(qi, (int)(kSubIdx >> (8 * c3)) & 3);
+    for (int m = 1; m < 4; m++) {
+      const int bit = 4 * c3 + m;
+      const S am = (kSubNeg >> bit) & 1u ? -a[m - 1] : a[m - 1];
+      dqa = dqa + am * pick4(qi, (int)((kSubIdx >> (2 * bit)) & 3u));
+    }
+    dqa = dqa * 2.0;
+    if (r < 3) {
+      const S pn = p + x;
+      set_dir(b.p[r], pn, k);
+      set_dir(b.dqL[r], pn - p0, k);
+      set_dir(b.dqA[r], dqa, k);
+    }
+    if (r < 4) set_dir(b.q[r], q1, k);
   }
   __syncthreads();
 }
