@@ -55,6 +55,7 @@ struct TBody {
   R pv[3];         // previous velocity
   R p0[3], q0[4];  // x_t (initialLin / initialAng)
   R q0i[4];        // q0's inverse q0* / |q0|^2, the right factor of every q_subtract(., q0) of the step
+  R yqi[4];        // yq's inverse, likewise for the inertial terms
   R yl[3], yq[4];  // inertial target y
 };
 struct TBodyStatic {
@@ -217,14 +218,29 @@ __device__ __forceinline__ void m3_add_into(O &&o, const S *a) {
   for (int i = 0; i < 9; i++) o[i] += a[i];
 }
 // Eq. 20 (maths.js:541-555)
+// q_subtract's second half: 2 (a * b^-1).xyz with b^-1 = (ix, iy, iz, iw)
 template <class S>
-__device__ void q_subtract(S *o, const S *a, const S *b) {
-  const S lsq = b[0] * b[0] + b[1] * b[1] + b[2] * b[2] + b[3] * b[3];
-  const S ix = -b[0] / lsq, iy = -b[1] / lsq, iz = -b[2] / lsq, iw = b[3] / lsq;
+__device__ __forceinline__ void q_mul_inv(S *o, const S *a, const S *inv) {
+  const S ix = inv[0], iy = inv[1], iz = inv[2], iw = inv[3];
   const S ax = a[0], ay = a[1], az = a[2], aw = a[3];
   o[0] = (aw * ix + ax * iw + ay * iz - az * iy) * 2.0;
   o[1] = (aw * iy - ax * iz + ay * iw + az * ix) * 2.0;
   o[2] = (aw * iz + ax * iy - ay * ix + az * iw) * 2.0;
+}
+// b^-1 = b* / |b|^2
+template <class S>
+__device__ __forceinline__ void q_inverse(S *o, const S *b) {
+  const S lsq = b[0] * b[0] + b[1] * b[1] + b[2] * b[2] + b[3] * b[3];
+  o[0] = -b[0] / lsq;
+  o[1] = -b[1] / lsq;
+  o[2] = -b[2] / lsq;
+  o[3] = b[3] / lsq;
+}
+template <class S>
+__device__ void q_subtract(S *o, const S *a, const S *b) {
+  S inv[4];
+  q_inverse(inv, b);
+  q_mul_inv(o, a, inv);
 }
 // Eq. 21 (maths.js:568-592), its "0 * q" terms kept
 template <class S>
@@ -707,13 +723,8 @@ __global__ void bodies_init_kernel(TWorld w) {
     if (!isfinite(weight)) weight = 0.0;
     for (int k = 0; k < 3; k++) b.p0[k] = b.p[k];
     for (int k = 0; k < 4; k++) b.q0[k] = b.q[k];
-    {  // q_subtract's inverse of q0, the same operations
-      const R lsq = b.q0[0] * b.q0[0] + b.q0[1] * b.q0[1] + b.q0[2] * b.q0[2] + b.q0[3] * b.q0[3];
-      b.q0i[0] = -b.q0[0] / lsq;
-      b.q0i[1] = -b.q0[1] / lsq;
-      b.q0i[2] = -b.q0[2] / lsq;
-      b.q0i[3] = b.q0[3] / lsq;
-    }
+    q_inverse(b.q0i, b.q0);  // q_subtract's inverses of the step's constant quaternions
+    q_inverse(b.yqi, b.yq);
     if (dyn) {
       v3_add_scaled(b.p, b.v, R(dt));
       v3_add_scaled(b.p, g, weight * dt * dt);
@@ -1212,14 +1223,14 @@ __device__ void inertial_terms(const TWorld &w, int i, int k) {
   const TBody &b = w.b[i];
   const TBodyStatic &st = w.bs[i];
   const double dt2 = P.dt * P.dt;
-  S p[3], yl[3], q[4], yq[4];
+  S p[3], yl[3], q[4], yqi[4];
   for (int c = 0; c < 3; c++) {
     p[c] = dir_of(b.p[c], k);
     yl[c] = dir_of(b.yl[c], k);
   }
   for (int c = 0; c < 4; c++) {
     q[c] = dir_of(b.q[c], k);
-    yq[c] = dir_of(b.yq[c], k);
+    yqi[c] = dir_of(b.yqi[c], k);
   }
   Sys6T<S> s;
   S MAng[9], tmp[3], dq[3];
@@ -1229,7 +1240,7 @@ __device__ void inertial_terms(const TWorld &w, int i, int k) {
   m3_zero(s.cross);
   v3_sub(tmp, p, yl);
   m3_mul_vec(s.bl, s.lin, tmp);
-  q_subtract(dq, q, yq);
+  q_mul_inv(dq, q, yqi);  // q_subtract(dq, q, yq)
   m3_mul_vec(s.ba, s.ang, dq);
   const S *e = &s.lin[0];
   R *o = &w.inert[(size_t)i * kSysEntries];
@@ -1493,19 +1504,22 @@ __global__ void __launch_bounds__(kBodyThreads, 1) iterate_kernel(TWorld w) {
   // thread index spread so that consecutive items land on different SMs
   const int g = blockIdx.x + gridDim.x * threadIdx.x, gs = gridDim.x * blockDim.x;
   // The per-force phases run on five-lane groups, one tangent direction a
-  // lane, six groups a warp. Warps are numbered across the SMs first, and
-  // each kind of item (contacts, joints, springs, inertial terms) starts a
-  // quarter of the warps further on, so that the kinds run on different
-  // warps and their instruction streams side by side.
+  // lane, six groups a warp, each kind of item (contacts, joints, springs,
+  // inertial terms) from its own warps so that their instruction streams run
+  // side by side.
   const int lane = threadIdx.x & 31, dir = lane % kTangentDims, slot = lane / kTangentDims;
-  const int nWarps = gridDim.x * (blockDim.x >> 5), wg = blockIdx.x + gridDim.x * (threadIdx.x >> 5);
+  const int rows = blockDim.x >> 5, v = threadIdx.x >> 5;  // a block's warps
   const bool grouped = slot < kGroupsPerWarp;
   const unsigned mask = grouped ? 0x1fu << (slot * kTangentDims) : 0u;
-  const int nGroups = nWarps * kGroupsPerWarp;
-  const int gContact = ((wg + 0 * (nWarps / 4)) % nWarps) * kGroupsPerWarp + slot;
-  const int gJoint = ((wg + 1 * (nWarps / 4)) % nWarps) * kGroupsPerWarp + slot;
-  const int gSpring = ((wg + 2 * (nWarps / 4)) % nWarps) * kGroupsPerWarp + slot;
-  const int gInert = ((wg + 3 * (nWarps / 4)) % nWarps) * kGroupsPerWarp + slot;
+  const int nGroups = rows * gridDim.x * kGroupsPerWarp;
+  // a kind's n-th warp: warp rho(v) of block n % gridDim.x; contacts fill the
+  // blocks' warps from the first, joints, inertial terms and springs from
+  // the last three (warp v runs on sub-partition v % 4)
+  auto group_of = [&](int rho) { return (rho * (int)gridDim.x + (int)blockIdx.x) * kGroupsPerWarp + slot; };
+  const int gContact = group_of(v);
+  const int gJoint = group_of(rows - 1 - v);
+  const int gInert = group_of((2 * rows - 2 - v) % rows);
+  const int gSpring = group_of((2 * rows - 3 - v) % rows);
   if (grouped)
     for (int q = gInert; q < w.n; q += nGroups)
       if (w.bs[q].mass > 0) inertial_terms(w, q, dir);
