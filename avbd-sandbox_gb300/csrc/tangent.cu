@@ -642,15 +642,23 @@ __device__ void joint_eval_ang(const TWorld &w, const TJoint &j, S *out, int dir
   for (int k = 0; k < 3; k++) out[k] = out[k] * j.torqueArm;
 }
 // spring.js:447-458: C = |d| - rest, n = d / |d| (NaN C when |d| <= 1e-6)
+// (rW: if given, the rotated anchor of end `side`)
 template <class S>
-__device__ S spring_eval(const TWorld &w, const TSpring &s, S *d, S *n, int dir = 0) {
+__device__ S spring_eval(const TWorld &w, const TSpring &s, S *d, S *n, int dir = 0, int side = 0,
+                         S *rW = nullptr) {
   S pA[3], pB[3], p[3], q[4], r[3];
   ldn(r, s.rA, 3, dir);
   body_pose(w, s.a, p, q, dir);
-  transform_point(pA, p, q, r);
+  q_rotate(pA, q, r);
+  if (rW && side == 0)
+    for (int k = 0; k < 3; k++) rW[k] = pA[k];
+  for (int k = 0; k < 3; k++) pA[k] += p[k];
   ldn(r, s.rB, 3, dir);
   body_pose(w, s.b, p, q, dir);
-  transform_point(pB, p, q, r);
+  q_rotate(pB, q, r);
+  if (rW && side == 1)
+    for (int k = 0; k < 3; k++) rW[k] = pB[k];
+  for (int k = 0; k < 3; k++) pB[k] += p[k];
   v3_sub(d, pA, pB);
   const S len = sqrt(v3_len_sq(d));
   if (len <= 1.0e-6) return S(NAN);
@@ -964,29 +972,37 @@ template <class S, class Sink>
 __device__ void joint_primal(const TWorld &w, const TJoint &j, int side, R alpha, Sink &s, int dir) {
   S C[3], F[3], pen[3];
   if (nonzero3(j.penLin)) {
-    joint_eval_lin(w, j, C, dir);
+    // joint_eval_lin, keeping the rotated anchors (the rows' lever arms)
+    S rAW[3], rBW[3], pA[3], pB[3], p[3], q[4], rl[3];
+    ldn(rl, j.rA, 3, dir);
+    if (j.a >= 0) {
+      body_pose(w, j.a, p, q, dir);
+      q_rotate(rAW, q, rl);
+      for (int k = 0; k < 3; k++) pA[k] = rAW[k] + p[k];
+    } else {
+      for (int k = 0; k < 3; k++) pA[k] = rl[k];
+    }
+    ldn(rl, j.rB, 3, dir);
+    body_pose(w, j.b, p, q, dir);
+    q_rotate(rBW, q, rl);
+    for (int k = 0; k < 3; k++) pB[k] = rBW[k] + p[k];
+    v3_sub(C, pA, pB);
     if (j.stiffLin.v == INFINITY) {
       const S na = -ld<S>(alpha, dir);
       for (int k = 0; k < 3; k++) C[k] = C[k] + ld<S>(j.C0Lin[k], dir) * na;
     }
     ldn(pen, j.penLin, 3, dir);
     for (int k = 0; k < 3; k++) F[k] = pen[k] * C[k] + ld<S>(j.lamLin[k], dir);
-    S jLin[9], jAng[9], rW[3], r[3], q[4], rl[3];
-    if (!side) {
+    S jLin[9], jAng[9], r[3];
+    if (!side) {  // body a (j.a >= 0)
       m3_diag(jLin, S(1.0), S(1.0), S(1.0));
-      ldn(q, w.b[j.a].q, 4, dir);
-      ldn(rl, j.rA, 3, dir);
-      q_rotate(rW, q, rl);
-      for (int k = 0; k < 3; k++) r[k] = -rW[k];
+      for (int k = 0; k < 3; k++) r[k] = -rAW[k];
       m3_skew(jAng, r);
-      for (int k = 0; k < 3; k++) r[k] = rW[k];
+      for (int k = 0; k < 3; k++) r[k] = rAW[k];
     } else {
       m3_diag(jLin, S(-1.0), S(-1.0), S(-1.0));
-      ldn(q, w.b[j.b].q, 4, dir);
-      ldn(rl, j.rB, 3, dir);
-      q_rotate(rW, q, rl);
-      m3_skew(jAng, rW);
-      for (int k = 0; k < 3; k++) r[k] = -rW[k];
+      m3_skew(jAng, rBW);
+      for (int k = 0; k < 3; k++) r[k] = -rBW[k];
     }
     stamp_rows(s, jLin, jAng, pen, F);
     S G[9];
@@ -1014,22 +1030,16 @@ __device__ void joint_primal(const TWorld &w, const TJoint &j, int side, R alpha
 template <class S, class Sink>
 __device__ void spring_primal(const TWorld &w, const TSpring &sp, int side, Sink &s, const TParams &P, int dir) {
   if (sp.broken) return;
-  S d[3], n[3];
-  const S Cv = spring_eval(w, sp, d, n, dir);
+  S d[3], n[3], rW[3];
+  const S Cv = spring_eval(w, sp, d, n, dir, side, rW);
   if (Cv != Cv) return;
   const S k = ld<S>(sp.penalty, dir);
   const S f = k * Cv;
-  S rW[3], jLin[3], jAng[3], q[4], rl[3];
+  S jLin[3], jAng[3];
   if (!side) {
-    ldn(q, w.b[sp.a].q, 4, dir);
-    ldn(rl, sp.rA, 3, dir);
-    q_rotate(rW, q, rl);
     for (int c = 0; c < 3; c++) jLin[c] = n[c];
     v3_cross(jAng, rW, n);
   } else {
-    ldn(q, w.b[sp.b].q, 4, dir);
-    ldn(rl, sp.rB, 3, dir);
-    q_rotate(rW, q, rl);
     for (int c = 0; c < 3; c++) jLin[c] = -n[c];
     v3_cross(jAng, rW, n);
     for (int c = 0; c < 3; c++) jAng[c] = -jAng[c];
@@ -1277,6 +1287,7 @@ __device__ void body_update_block(const TWorld &w, int i, R alpha, BodySmem &sm)
       else if (type == kRefJoint) joint_primal<Dual1>(w, w.j[idx], (int)side, alpha, rs, dir);
       else spring_primal<Dual1>(w, w.s[idx], (int)side, rs, P, dir);
     }
+    __syncwarp();  // each warp whole again (its lanes took different rows) before the block barrier
     __syncthreads();
     for (int q = t; q < kSysEntries * kDualDoubles; q += nt) {  // one double of one entry per thread
       const int entry = q / kDualDoubles, part = q % kDualDoubles;
