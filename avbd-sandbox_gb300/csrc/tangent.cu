@@ -121,6 +121,7 @@ struct TWorld {
   uint64_t *key;               // current candidates (mcap)
   TManifold *cur, *prev;
   uint64_t *prevKey;
+  int *commitAt;  // per candidate: its slot among the step's live manifolds, or -1
   int *ctl;  // [0] candidates, [1] previous candidates, [2] overflow, [3] colours
   // adjacency of the solve (per dynamic body: its forces) and the colouring
   int *fStart, *fCount;  // n + 1
@@ -542,7 +543,9 @@ __device__ void contact_jacobians(S *out, const S *basis, const S *qA, const S *
 __global__ void narrow_kernel(TWorld w) {
   const int total = w.ctl[0], prevCount = w.ctl[1];
   const TParams &P = w.P;
-  for (int c = blockIdx.x * blockDim.x + threadIdx.x; c < total; c += gridDim.x * blockDim.x) {
+  // pairs spread over the blocks first (few pairs a warp: less divergence,
+  // more sub-partitions on the FP64 work)
+  for (int c = blockIdx.x + gridDim.x * threadIdx.x; c < total; c += gridDim.x * blockDim.x) {
     const uint64_t key = w.key[c];
     const int ia = (int)(key >> 32), ib = (int)(key & 0xffffffffu);
     TManifold &m = w.cur[c];
@@ -751,59 +754,116 @@ __global__ void bodies_init_kernel(TWorld w) {
 // The forces of the step after initialisation (solver.js:346-360): live
 // manifolds, joints that did not leave, every spring (a broken one stays and
 // does nothing). Per dynamic body its list of (type, index, side).
-template <class F>
-__device__ void for_each_force(const TWorld &w, int total, F &&f) {
-  for (int c = 0; c < total; c++)
-    if (w.cur[c].count > 0) f(0u, c, w.cur[c].a, w.cur[c].b, false);
-  for (int k = 0; k < w.nj; k++)
-    if (!w.j[k].removed) f((uint32_t)kRefJoint, k, w.j[k].a, w.j[k].b, false);
-  for (int k = 0; k < w.ns; k++) f((uint32_t)kRefSpring, k, w.s[k].a, w.s[k].b, w.s[k].broken != 0);
+// Slot g of the force list - the manifolds with contacts, then the live
+// joints, then every spring - or false for a slot that holds no force;
+// base: the force's reference without its side bit.
+__device__ bool force_at(const TWorld &w, int total, int g, uint32_t &base, int &a, int &b) {
+  if (g < total) {
+    const TManifold &m = w.cur[g];
+    if (m.count <= 0) return false;
+    base = (uint32_t)g << 1;
+    a = m.a;
+    b = m.b;
+    return true;
+  }
+  g -= total;
+  if (g < w.nj) {
+    const TJoint &j = w.j[g];
+    if (j.removed) return false;
+    base = (kRefJoint << 30) | ((uint32_t)g << 1);
+    a = j.a;
+    b = j.b;
+    return true;
+  }
+  g -= w.nj;
+  const TSpring &sp = w.s[g];
+  base = (kRefSpring << 30) | ((uint32_t)g << 1);
+  a = sp.a;
+  b = sp.b;
+  return true;
+}
+
+// Exclusive prefix sum of cnt[0, n) into start[0, n] by one block, in
+// chunks of its threads (Hillis-Steele in shared memory).
+__device__ void block_exclusive_scan(const int *cnt, int *start, int n, int *scan, int &carry) {
+  const int t = threadIdx.x, bd = blockDim.x;
+  if (t == 0) carry = 0;
+  for (int base = 0; base < n; base += bd) {
+    __syncthreads();
+    const int i = base + t, v = i < n ? cnt[i] : 0;
+    scan[t] = v;
+    __syncthreads();
+    for (int off = 1; off < bd; off <<= 1) {
+      const int x = t >= off ? scan[t - off] : 0;
+      __syncthreads();
+      scan[t] += x;
+      __syncthreads();
+    }
+    if (i < n) start[i] = carry + scan[t] - v;
+    __syncthreads();
+    if (t == bd - 1) carry += scan[t];
+  }
+  __syncthreads();
+  if (t == 0) start[n] = carry;
+  __syncthreads();
 }
 
 // The integer-priority greedy colouring (statics -1), computed as the fixed
 // point of Jacobi rounds (the CUDA step's colouring; the oracle's
 // priority_coloring); colour edges: forces between two dynamic bodies,
-// broken ones excluded (oracle constraint_edges).
+// broken ones excluded (oracle constraint_edges). One block: the per-body
+// force lists are filled stably (force-list order) a chunk of forces at a
+// time, each force's rank among its chunk's earlier forces on the same body
+// counted in shared memory; the (colour, index) order likewise.
 __global__ void __launch_bounds__(kBlock) adjacency_coloring_kernel(TWorld w) {
-  const int n = w.n, total = w.ctl[0];
-  const int t = threadIdx.x;
-  for (int i = t; i <= n; i += blockDim.x) w.fCount[i] = 0;
+  const int n = w.n, total = w.ctl[0], nForces = total + w.nj + w.ns;
+  const int t = threadIdx.x, bd = blockDim.x;
+  __shared__ int scan[kBlock], ea[kBlock], eb[kBlock], carry;
+  __shared__ int colorCount[kMaxColors], colorRun[kMaxColors], numColors, changed;
+  for (int i = t; i <= n; i += bd) w.fCount[i] = 0;
   __syncthreads();
-  if (t == 0) {
-    // per-body force lists in force-list order (single thread: small scenes)
-    for_each_force(w, total, [&](uint32_t type, int idx, int a, int b, bool) {
-      if (a >= 0 && w.bs[a].mass > 0) w.fCount[a]++;
-      if (w.bs[b].mass > 0) w.fCount[b]++;
-    });
-    int run = 0;
-    for (int i = 0; i < n; i++) {
-      w.fStart[i] = run;
-      run += w.fCount[i];
-      w.fCount[i] = 0;
-    }
-    w.fStart[n] = run;
-    if (run > w.fcap) w.ctl[2] = 1;
-    for_each_force(w, total, [&](uint32_t type, int idx, int a, int b, bool) {
-      const uint32_t base = (type << 30) | ((uint32_t)idx << 1);
-      if (a >= 0 && w.bs[a].mass > 0) {
-        const int at = w.fStart[a] + w.fCount[a]++;
-        if (at < w.fcap) w.fRef[at] = base | 0u;
-      }
-      if (w.bs[b].mass > 0) {
-        const int at = w.fStart[b] + w.fCount[b]++;
-        if (at < w.fcap) w.fRef[at] = base | 1u;
-      }
-    });
+  for (int g = t; g < nForces; g += bd) {  // forces per body
+    uint32_t fb;
+    int a, b;
+    if (!force_at(w, total, g, fb, a, b)) continue;
+    if (a >= 0 && w.bs[a].mass > 0) atomicAdd(&w.fCount[a], 1);
+    if (w.bs[b].mass > 0) atomicAdd(&w.fCount[b], 1);
   }
   __syncthreads();
+  block_exclusive_scan(w.fCount, w.fStart, n, scan, carry);
+  for (int i = t; i < n; i += bd) w.fCount[i] = 0;  // now the forces placed so far
+  if (t == 0 && w.fStart[n] > w.fcap) w.ctl[2] = 1;
+  __syncthreads();
   if (w.ctl[2]) return;
-  for (int i = t; i < n; i += blockDim.x) w.color[i] = is_dynamic(w, i) ? 0 : -1;
-  __shared__ int changed;
+  for (int base = 0; base < nForces; base += bd) {
+    const int g = base + t;
+    uint32_t fb = 0;
+    int a = -1, b = -1;
+    const bool has = g < nForces && force_at(w, total, g, fb, a, b);
+    const int xa = has && a >= 0 && w.bs[a].mass > 0 ? a : -1;
+    const int xb = has && w.bs[b].mass > 0 ? b : -1;
+    ea[t] = xa;
+    eb[t] = xb;
+    __syncthreads();
+    int ra = 0, rb = 0;  // earlier forces of the chunk on the same body
+    for (int k = 0; k < t; k++) {
+      const int pa = ea[k], pb = eb[k];
+      ra += xa >= 0 && (pa == xa || pb == xa);
+      rb += xb >= 0 && (pa == xb || pb == xb);
+    }
+    if (xa >= 0) w.fRef[w.fStart[xa] + w.fCount[xa] + ra] = fb | 0u;
+    if (xb >= 0) w.fRef[w.fStart[xb] + w.fCount[xb] + rb] = fb | 1u;
+    __syncthreads();
+    if (xa >= 0) atomicAdd(&w.fCount[xa], 1);
+    if (xb >= 0) atomicAdd(&w.fCount[xb], 1);
+    __syncthreads();
+  }
+  for (int i = t; i < n; i += bd) w.color[i] = is_dynamic(w, i) ? 0 : -1;
   for (int round = 0; round < 4096; round++) {
     __syncthreads();
     if (t == 0) changed = 0;
     __syncthreads();
-    for (int i = t; i < n; i += blockDim.x) {
+    for (int i = t; i < n; i += bd) {
       if (!is_dynamic(w, i)) continue;
       const uint32_t pi = w.prio[i];
       int c = -1;
@@ -835,19 +895,32 @@ __global__ void __launch_bounds__(kBlock) adjacency_coloring_kernel(TWorld w) {
     __syncthreads();
     if (!changed) break;
   }
+  // bodies in (colour, index) order
+  for (int c = t; c < kMaxColors; c += bd) colorCount[c] = colorRun[c] = 0;
+  if (t == 0) numColors = 0;
   __syncthreads();
-  if (t == 0) {  // bodies in (colour, index) order
-    int numColors = 0;
-    for (int i = 0; i < n; i++) numColors = max(numColors, w.color[i] + 1);
-    int at = 0;
-    for (int c = 0; c < numColors; c++) {
-      w.colorStart[c] = at;
-      for (int i = 0; i < n; i++)
-        if (w.color[i] == c) w.order[at++] = i;
-    }
-    w.colorStart[numColors] = at;
-    w.ctl[3] = numColors;
+  for (int i = t; i < n; i += bd) {
+    const int c = w.color[i];
+    if (c < 0) continue;
+    atomicAdd(&colorCount[c], 1);
+    atomicMax(&numColors, c + 1);
   }
+  __syncthreads();
+  block_exclusive_scan(colorCount, w.colorStart, numColors, scan, carry);
+  for (int base = 0; base < n; base += bd) {
+    const int i = base + t, c = i < n ? w.color[i] : -1;
+    ea[t] = c;
+    __syncthreads();
+    if (c >= 0) {
+      int r = 0;
+      for (int k = 0; k < t; k++) r += ea[k] == c;
+      w.order[w.colorStart[c] + colorRun[c] + r] = i;
+    }
+    __syncthreads();
+    if (c >= 0) atomicAdd(&colorRun[c], 1);
+    __syncthreads();
+  }
+  if (t == 0) w.ctl[3] = numColors;
 }
 
 // ---------------------------------------------------------------------------
@@ -1576,7 +1649,7 @@ __global__ void __launch_bounds__(kBodyThreads, 1) iterate_kernel(TWorld w) {
 
 // This step's manifolds become the next step's previous ones: keys of the
 // live ones, in key order (candidates are in key order already).
-__global__ void __launch_bounds__(kBlock) commit_kernel(TWorld w) {
+__global__ void __launch_bounds__(kBlock) commit_index_kernel(TWorld w) {
   if (w.ctl[2]) return;
   const int total = w.ctl[0];
   __shared__ int base;
@@ -1589,15 +1662,28 @@ __global__ void __launch_bounds__(kBlock) commit_kernel(TWorld w) {
     const int live = c < total && w.cur[c].count > 0 ? 1 : 0;
     int at, tot;
     Scan(tmp).ExclusiveSum(live, at, tot);
-    if (live) {
-      w.prev[base + at] = w.cur[c];
-      w.prevKey[base + at] = w.key[c];
-    }
+    if (c < total) w.commitAt[c] = live ? base + at : -1;
     __syncthreads();
     if (threadIdx.x == 0) base += tot;
     __syncthreads();
   }
   if (threadIdx.x == 0) w.ctl[1] = base;
+}
+// The live manifolds into the previous-step arrays, a warp per manifold.
+__global__ void commit_copy_kernel(TWorld w) {
+  if (w.ctl[2]) return;
+  const int total = w.ctl[0], lane = threadIdx.x & 31;
+  const int warps = gridDim.x * (blockDim.x >> 5);
+  static_assert(sizeof(TManifold) % sizeof(unsigned long long) == 0, "a manifold is whole words");
+  constexpr int kWords = (int)(sizeof(TManifold) / sizeof(unsigned long long));
+  for (int c = blockIdx.x + gridDim.x * (threadIdx.x >> 5); c < total; c += warps) {
+    const int at = w.commitAt[c];
+    if (at < 0) continue;
+    const unsigned long long *src = reinterpret_cast<const unsigned long long *>(&w.cur[c]);
+    unsigned long long *dst = reinterpret_cast<unsigned long long *>(&w.prev[at]);
+    for (int k = lane; k < kWords; k += 32) dst[k] = src[k];
+    if (lane == 0) w.prevKey[at] = w.key[c];
+  }
 }
 
 // grad[d] = sum over bodies and components of g[i][k] * dx_i,k / d theta_d
@@ -1804,7 +1890,8 @@ int tangent_pack(TangentCtx **out, const avbd_world *world, const avbd_params &P
   if ((e = t->alloc(&w.b, n)) || (e = t->alloc(&w.bs, n)) || (e = t->alloc(&cRefD, cRef.size())) ||
       (e = t->alloc(&w.j, nj)) || (e = t->alloc(&w.s, ns)) || (e = t->alloc(&w.pairCount, n + 1)) ||
       (e = t->alloc(&w.pairStart, n + 1)) || (e = t->alloc(&w.key, w.mcap)) || (e = t->alloc(&w.cur, w.mcap)) ||
-      (e = t->alloc(&w.prev, w.mcap)) || (e = t->alloc(&w.prevKey, w.mcap)) || (e = t->alloc(&w.ctl, 8)) ||
+      (e = t->alloc(&w.prev, w.mcap)) || (e = t->alloc(&w.prevKey, w.mcap)) || (e = t->alloc(&w.commitAt, w.mcap)) ||
+      (e = t->alloc(&w.ctl, 8)) ||
       (e = t->alloc(&w.fStart, n + 1)) || (e = t->alloc(&w.fCount, n + 1)) || (e = t->alloc(&w.fRef, w.fcap)) ||
       (e = t->alloc(&w.color, n)) || (e = t->alloc(&w.order, n)) || (e = t->alloc(&w.colorStart, kMaxColors + 1)) ||
       (e = t->alloc(&prioD, n)) || (e = t->alloc(&w.jac, (size_t)w.mcap * K8 * 18)) ||
@@ -1857,7 +1944,7 @@ int tangent_step(TangentCtx *t, int steps, void *temp, size_t tempBytes, char *m
     size_t tb = tempBytes;
     cub::DeviceScan::ExclusiveSum(temp, tb, w.pairCount, w.pairStart, w.n + 1, st);
     pairs_write_kernel<<<blocks, 128, 0, st>>>(w);
-    narrow_kernel<<<std::max(1, std::min((w.mcap + 63) / 64, t->smCount * 4)), 64, 0, st>>>(w);
+    narrow_kernel<<<t->smCount * 4, 32, 0, st>>>(w);
     forces_init_kernel<<<blocks, 128, 0, st>>>(w);
     bodies_init_kernel<<<blocks, 128, 0, st>>>(w);
     adjacency_coloring_kernel<<<1, kBlock, 0, st>>>(w);
@@ -1870,7 +1957,8 @@ int tangent_step(TangentCtx *t, int steps, void *temp, size_t tempBytes, char *m
         return AVBD_ERR_CUDA;
       }
     }
-    commit_kernel<<<1, kBlock, 0, st>>>(w);
+    commit_index_kernel<<<1, kBlock, 0, st>>>(w);
+    commit_copy_kernel<<<t->smCount, 128, 0, st>>>(w);
   }
   cudaError_t e = cudaStreamSynchronize(st);
   if (e == cudaSuccess) e = cudaGetLastError();
