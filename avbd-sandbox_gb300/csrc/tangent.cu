@@ -56,6 +56,7 @@ struct TBody {
   R p0[3], q0[4];  // x_t (initialLin / initialAng)
   R q0i[4];        // q0's inverse q0* / |q0|^2, the right factor of every q_subtract(., q0) of the step
   R yqi[4];        // yq's inverse, likewise for the inertial terms
+  R qi[4];         // q's inverse, kept with q during the iterations (the joints' angular rows)
   R yl[3], yq[4];  // inertial target y
 };
 struct TBodyStatic {
@@ -644,6 +645,15 @@ __device__ void joint_eval_ang(const TWorld &w, const TJoint &j, S *out, int dir
   q_subtract(out, qA, qB);
   for (int k = 0; k < 3; k++) out[k] = out[k] * j.torqueArm;
 }
+// the same during the iterations, with body b's inverse kept beside its q
+template <class S>
+__device__ void joint_eval_ang_iter(const TWorld &w, const TJoint &j, S *out, int dir) {
+  S qA[4] = {S(0.0), S(0.0), S(0.0), S(1.0)}, qBi[4];
+  if (j.a >= 0) ldn(qA, w.b[j.a].q, 4, dir);
+  ldn(qBi, w.b[j.b].qi, 4, dir);
+  q_mul_inv(out, qA, qBi);  // q_subtract(out, qA, qB)
+  for (int k = 0; k < 3; k++) out[k] = out[k] * j.torqueArm;
+}
 // spring.js:447-458: C = |d| - rest, n = d / |d| (NaN C when |d| <= 1e-6)
 // (rW: if given, the rotated anchor of end `side`)
 template <class S>
@@ -745,6 +755,7 @@ __global__ void bodies_init_kernel(TWorld w) {
     }
     v3_sub(b.dqL, b.p, b.p0);
     q_subtract(b.dqA, b.q, b.q0);
+    q_inverse(b.qi, b.q);
   }
 }
 
@@ -1083,7 +1094,7 @@ __device__ void joint_primal(const TWorld &w, const TJoint &j, int side, R alpha
     m3_add_into(s.ang, G);
   }
   if (nonzero3(j.penAng)) {
-    joint_eval_ang(w, j, C, dir);
+    joint_eval_ang_iter(w, j, C, dir);
     if (j.stiffAng.v == INFINITY) {
       const S na = -ld<S>(alpha, dir);
       for (int k = 0; k < 3; k++) C[k] = C[k] + ld<S>(j.C0Ang[k], dir) * na;
@@ -1433,7 +1444,11 @@ __device__ void body_update_block(const TWorld &w, int i, R alpha, BodySmem &sm)
       set_dir(b.dqL[r], pn - p0, k);
       set_dir(b.dqA[r], dqa, k);
     }
-    if (r < 4) set_dir(b.q[r], q1, k);
+    if (r < 4) {
+      const S lsq = a[0] * a[0] + a[1] * a[1] + a[2] * a[2] + a[3] * a[3];  // q_inverse of q1
+      set_dir(b.q[r], q1, k);
+      set_dir(b.qi[r], (r < 3 ? -pick4(a, r) : a[3]) / lsq, k);
+    }
   }
   __syncthreads();
 }
@@ -1491,7 +1506,7 @@ __device__ void joint_dual_dir(const TWorld &w, TJoint &j, R alpha, int dir, uns
     for (int k = 0; k < 3; k++) penL[k] = js_min(penL[k] + fabs(C[k]) * P.betaLin, cap);
   }
   if (nonzero3(j.penAng)) {
-    joint_eval_ang(w, j, C, dir);
+    joint_eval_ang_iter(w, j, C, dir);
     if (j.stiffAng.v == INFINITY) {
       const S na = -ld<S>(alpha, dir);
       for (int k = 0; k < 3; k++) C[k] = C[k] + ld<S>(j.C0Ang[k], dir) * na;
