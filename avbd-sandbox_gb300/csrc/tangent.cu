@@ -357,6 +357,15 @@ template <class S>
 __device__ __forceinline__ void ldn(S *o, const R *x, int n, int k) {
   for (int c = 0; c < n; c++) o[c] = ld<S>(x[c], k);
 }
+// A body's iterate (p, q) as seen in S by direction k.
+template <class S>
+__device__ __forceinline__ void body_pose(const TWorld &w, int i, S *p, S *q, int k) {
+  ldn(p, w.b[i].p, 3, k);
+  ldn(q, w.b[i].q, 4, k);
+}
+// Per-item work of the kernels below runs on five-lane groups, a tangent
+// direction a lane, six groups a warp (30 of its 32 lanes).
+constexpr int kGroupsPerWarp = 6;
 
 // The recording form of a body's system: one constraint's contribution as
 // the sequence of addends it adds to each entry, so that the addends of many
@@ -490,9 +499,10 @@ __global__ void pairs_write_kernel(TWorld w) {
 }
 
 // manifold.js:222-270, the sphere pairs' transport of lambda and k into the new basis
-__device__ void transport(R *lam, R *pen, const R *oldB, const R *newB) {
-  const R x = lam[0], y = lam[1], z = lam[2];
-  R o[3];
+template <class S>
+__device__ void transport(S *lam, S *pen, const S *oldB, const S *newB) {
+  const S x = lam[0], y = lam[1], z = lam[2];
+  S o[3];
   for (int r = 0; r < 3; r++) {
     const int n = r * 3;
     o[r] = x * (newB[n] * oldB[0] + newB[n + 1] * oldB[1] + newB[n + 2] * oldB[2]) +
@@ -500,24 +510,25 @@ __device__ void transport(R *lam, R *pen, const R *oldB, const R *newB) {
            z * (newB[n] * oldB[6] + newB[n + 1] * oldB[7] + newB[n + 2] * oldB[8]);
   }
   lam[0] = o[0]; lam[1] = o[1]; lam[2] = o[2];
-  const R px = pen[0], py = pen[1], pz = pen[2];
+  const S px = pen[0], py = pen[1], pz = pen[2];
   for (int r = 0; r < 3; r++) {
     const int n = r * 3;
-    const R dx = newB[n] * oldB[0] + newB[n + 1] * oldB[1] + newB[n + 2] * oldB[2];
-    const R dy = newB[n] * oldB[3] + newB[n + 1] * oldB[4] + newB[n + 2] * oldB[5];
-    const R dz = newB[n] * oldB[6] + newB[n + 1] * oldB[7] + newB[n + 2] * oldB[8];
+    const S dx = newB[n] * oldB[0] + newB[n + 1] * oldB[1] + newB[n + 2] * oldB[2];
+    const S dy = newB[n] * oldB[3] + newB[n + 1] * oldB[4] + newB[n + 2] * oldB[5];
+    const S dz = newB[n] * oldB[6] + newB[n + 1] * oldB[7] + newB[n + 2] * oldB[8];
     o[r] = px * dx * dx + py * dy * dy + pz * dz * dz;
   }
   pen[0] = o[0]; pen[1] = o[1]; pen[2] = o[2];
 }
 
-__device__ geo::BodyT<R> body_geo(const TWorld &w, int i) {
-  geo::BodyT<R> g;
+// body i's collision geometry as tangent direction dir sees it
+__device__ geo::BodyT<Dual1> body_geo(const TWorld &w, int i, int dir) {
+  geo::BodyT<Dual1> g;
   const TBody &b = w.b[i];
   const TBodyStatic &s = w.bs[i];
-  g.p = geo::D3T<R>{b.p[0], b.p[1], b.p[2]};
-  g.q = geo::QDT<R>{b.q[0], b.q[1], b.q[2], b.q[3]};
-  g.half = geo::D3T<R>{R(s.half[0]), R(s.half[1]), R(s.half[2])};
+  g.p = geo::D3T<Dual1>{dir_of(b.p[0], dir), dir_of(b.p[1], dir), dir_of(b.p[2], dir)};
+  g.q = geo::QDT<Dual1>{dir_of(b.q[0], dir), dir_of(b.q[1], dir), dir_of(b.q[2], dir), dir_of(b.q[3], dir)};
+  g.half = geo::D3T<Dual1>{Dual1(s.half[0]), Dual1(s.half[1]), Dual1(s.half[2])};
   g.radius = s.radius;
   g.sphere = s.shape == AVBD_SHAPE_SPHERE;
   return g;
@@ -541,87 +552,100 @@ __device__ void contact_jacobians(S *out, const S *basis, const S *qA, const S *
   }
 }
 
+// One candidate pair per five-lane group, a tangent direction per lane
+// (each lane also computes the values, so every lane takes the same
+// branches); lane 0 writes the value parts and the integers. Nothing the
+// kernel writes is read back: the manifold's data stay in registers.
 __global__ void narrow_kernel(TWorld w) {
+  using S = Dual1;
   const int total = w.ctl[0], prevCount = w.ctl[1];
   const TParams &P = w.P;
-  // pairs spread over the blocks first (few pairs a warp: less divergence,
-  // more sub-partitions on the FP64 work)
-  for (int c = blockIdx.x + gridDim.x * threadIdx.x; c < total; c += gridDim.x * blockDim.x) {
+  const int lane = threadIdx.x & 31, slot = lane / kTangentDims, dir = lane % kTangentDims;
+  if (slot >= kGroupsPerWarp) return;
+  const int nWarps = gridDim.x * (blockDim.x >> 5), wg = blockIdx.x + gridDim.x * (threadIdx.x >> 5);
+  // pairs spread over the warps (and SMs) first, then over a warp's groups
+  for (int c = slot * nWarps + wg; c < total; c += nWarps * kGroupsPerWarp) {
     const uint64_t key = w.key[c];
     const int ia = (int)(key >> 32), ib = (int)(key & 0xffffffffu);
     TManifold &m = w.cur[c];
-    m.a = ia;
-    m.b = ib;
     const int pi = find_key(w.prevKey, prevCount, key);
     const TManifold *old = pi >= 0 ? &w.prev[pi] : nullptr;
     const int oldNum = old ? old->count : 0;
     const bool hasSphere = w.bs[ia].shape == AVBD_SHAPE_SPHERE || w.bs[ib].shape == AVBD_SHAPE_SPHERE;
-    m.friction = sqrt(w.bs[ia].friction * w.bs[ib].friction);
-    const geo::BodyT<R> A = body_geo(w, ia), B = body_geo(w, ib);
-    geo::NewContactT<R> nc[K8];
-    R basis[9];
+    set_dir(m.friction, sqrt(dir_of(w.bs[ia].friction, dir) * dir_of(w.bs[ib].friction, dir)), dir);
+    const geo::BodyT<S> A = body_geo(w, ia, dir), B = body_geo(w, ib, dir);
+    geo::NewContactT<S> nc[K8];
+    S basis[9];
     for (int k = 0; k < 9; k++) basis[k] = 0.0;
-    geo::ColliderT<R> col(A, B, nc);
+    geo::ColliderT<S> col(A, B, nc);
     const int num = col.collide(basis);
     bool compatible = true;
     if (hasSphere && oldNum > 0)
-      compatible = (old->basis[0] * basis[0] + old->basis[1] * basis[1] + old->basis[2] * basis[2]) > 0.85;
+      compatible = (old->basis[0].v * basis[0].v + old->basis[1].v * basis[1].v + old->basis[2].v * basis[2].v) > 0.85;
+    for (int k = 0; k < 9; k++) set_dir(m.basis[k], basis[k], dir);
+    if (dir == 0) {
+      m.a = ia;
+      m.b = ib;
+      m.count = num;
+    }
+    S pA[3], qA[4], pB[3], qB[4];
+    body_pose(w, ia, pA, qA, dir);
+    body_pose(w, ib, pB, qB, dir);
     for (int i = 0; i < num; i++) {
       TContact &t = m.c[i];
-      for (int k = 0; k < 3; k++) {
-        t.rA[k] = k == 0 ? nc[i].rA.x : (k == 1 ? nc[i].rA.y : nc[i].rA.z);
-        t.rB[k] = k == 0 ? nc[i].rB.x : (k == 1 ? nc[i].rB.y : nc[i].rB.z);
-        t.pen[k] = 0.0;
-        t.lam[k] = 0.0;
-      }
-      t.feature = nc[i].feature;
-      t.stick = 0;
+      S rA[3] = {nc[i].rA.x, nc[i].rA.y, nc[i].rA.z}, rB[3] = {nc[i].rB.x, nc[i].rB.y, nc[i].rB.z};
+      S pen[3] = {S(0.0), S(0.0), S(0.0)}, lam[3] = {S(0.0), S(0.0), S(0.0)};
+      int stick = 0;
       for (int j = 0; j < oldNum; j++) {
         const TContact &o = old->c[j];
         if (compatible && nc[i].feature == o.feature) {
-          for (int k = 0; k < 3; k++) {
-            t.pen[k] = o.pen[k];
-            t.lam[k] = o.lam[k];
+          ldn(pen, o.pen, 3, dir);
+          ldn(lam, o.lam, 3, dir);
+          stick = o.stick;
+          if (hasSphere) {
+            S ob[9];
+            ldn(ob, old->basis, 9, dir);
+            transport(lam, pen, ob, basis);
           }
-          t.stick = o.stick;
-          if (hasSphere) transport(t.lam, t.pen, old->basis, basis);
-          if (o.stick && !hasSphere)  // a stuck box contact keeps its anchors (manifold.js:279-282)
-            for (int k = 0; k < 3; k++) {
-              t.rA[k] = o.rA[k];
-              t.rB[k] = o.rB[k];
-            }
+          if (o.stick && !hasSphere) {  // a stuck box contact keeps its anchors (manifold.js:279-282)
+            ldn(rA, o.rA, 3, dir);
+            ldn(rB, o.rB, 3, dir);
+          }
           break;
         }
       }
-    }
-    m.count = num;
-    for (int k = 0; k < 9; k++) m.basis[k] = basis[k];
-    const TBody &bA = w.b[ia], &bB = w.b[ib];
-    for (int i = 0; i < num; i++) {  // C*(x_t) + margin, warm start (manifold.js:292-315)
-      TContact &t = m.c[i];
-      R xA[3], xB[3], d[3];
-      transform_point(xA, bA.p, bA.q, t.rA);
-      transform_point(xB, bB.p, bB.q, t.rB);
+      // C*(x_t) + margin, warm start (manifold.js:292-315)
+      S xA[3], xB[3], d[3], C0[3];
+      transform_point(xA, pA, qA, rA);
+      transform_point(xB, pB, qB, rB);
       v3_sub(d, xA, xB);
-      m3_mul_vec(t.C0, m.basis, d);
-      t.C0[0] = t.C0[0] + P.margin;
+      m3_mul_vec(C0, basis, d);
+      C0[0] = C0[0] + P.margin;
+      const S pMax = dir_of(P.penaltyMax, dir);
       for (int k = 0; k < 3; k++) {
-        if (!P.postStabilize) t.lam[k] = (t.lam[k] * P.alpha) * P.gamma;
-        t.pen[k] = clampR(t.pen[k] * P.gamma, R(P.penaltyMin), P.penaltyMax);
+        if (!P.postStabilize) lam[k] = (lam[k] * P.alpha) * P.gamma;
+        pen[k] = clampR(pen[k] * P.gamma, S(P.penaltyMin), pMax);
+        set_dir(t.rA[k], rA[k], dir);
+        set_dir(t.rB[k], rB[k], dir);
+        set_dir(t.C0[k], C0[k], dir);
+        set_dir(t.pen[k], pen[k], dir);
+        set_dir(t.lam[k], lam[k], dir);
       }
-      if (P.cachedJacobians)  // the orientations here are the step's x_t ones
-        contact_jacobians(&w.jac[((size_t)c * K8 + i) * 18], m.basis, bA.q, bB.q, t.rA, t.rB);
+      if (dir == 0) {
+        t.feature = nc[i].feature;
+        t.stick = stick;
+      }
+      if (P.cachedJacobians) {  // the orientations here are the step's x_t ones
+        S jc[18];
+        contact_jacobians(jc, basis, qA, qB, rA, rB);
+        R *out = &w.jac[((size_t)c * K8 + i) * 18];
+        for (int q = 0; q < 18; q++) set_dir(out[q], jc[q], dir);
+      }
     }
   }
 }
 
 // Joint.initialize (joint.js:131-160) and Spring.initialize (spring.js:472-507).
-// A body's iterate (p, q) as seen in S by direction k.
-template <class S>
-__device__ __forceinline__ void body_pose(const TWorld &w, int i, S *p, S *q, int k) {
-  ldn(p, w.b[i].p, 3, k);
-  ldn(q, w.b[i].q, 4, k);
-}
 template <class S>
 __device__ void joint_eval_lin(const TWorld &w, const TJoint &j, S *out, int dir = 0) {
   S pA[3], pB[3], p[3], q[4], r[3];
@@ -1183,7 +1207,6 @@ __device__ void spring_primal(const TWorld &w, const TSpring &sp, int side, Sink
 // update's. The inertial terms (the entries' first values) were formed in
 // the phase before (inertial_terms).
 constexpr int kBodyThreads = 256;  // two warps per SM sub-partition: 255 registers a thread
-constexpr int kGroupsPerWarp = 6;  // 30 of a warp's 32 lanes
 constexpr int kRowsPerPass = kBodyThreads / 32 * kGroupsPerWarp;
 constexpr int kDualDoubles = kTangentDims + 1;
 static_assert(kGroupsPerWarp * kTangentDims <= 32, "a row's five threads in one warp");
@@ -1959,7 +1982,7 @@ int tangent_step(TangentCtx *t, int steps, void *temp, size_t tempBytes, char *m
     size_t tb = tempBytes;
     cub::DeviceScan::ExclusiveSum(temp, tb, w.pairCount, w.pairStart, w.n + 1, st);
     pairs_write_kernel<<<blocks, 128, 0, st>>>(w);
-    narrow_kernel<<<t->smCount * 4, 32, 0, st>>>(w);
+    narrow_kernel<<<t->smCount * 2, 64, 0, st>>>(w);
     forces_init_kernel<<<blocks, 128, 0, st>>>(w);
     bodies_init_kernel<<<blocks, 128, 0, st>>>(w);
     adjacency_coloring_kernel<<<1, kBlock, 0, st>>>(w);
