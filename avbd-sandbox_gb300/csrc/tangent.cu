@@ -466,30 +466,45 @@ __device__ bool constrained(const TWorld &w, int a, int b) {
 __device__ bool is_candidate(const TWorld &w, int a, int b, int prevCount) {
   if (!(w.bs[a].mass > 0 || w.bs[b].mass > 0)) return false;
   if (find_key(w.prevKey, prevCount, pair_key(a, b)) >= 0) return true;
-  const R dx = w.b[a].p[0] - w.b[b].p[0], dy = w.b[a].p[1] - w.b[b].p[1], dz = w.b[a].p[2] - w.b[b].p[2];
+  // the values of the dual positions' difference (the test reads values only)
+  const double dx = w.b[a].p[0].v - w.b[b].p[0].v, dy = w.b[a].p[1].v - w.b[b].p[1].v,
+               dz = w.b[a].p[2].v - w.b[b].p[2].v;
   const double r = w.bs[a].radius + w.bs[b].radius;
   if (!(dx * dx + dy * dy + dz * dz <= r * r)) return false;
   return !constrained(w, a, b);
 }
 
+// The candidate pairs (a, b), b < a, a warp per body a, its lanes over b in
+// rounds of 32: a ballot counts them, and its prefix places them in
+// increasing b.
 __global__ void pairs_count_kernel(TWorld w) {
-  const int prevCount = w.ctl[1];
-  for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < w.n; a += gridDim.x * blockDim.x) {
+  const int prevCount = w.ctl[1], lane = threadIdx.x & 31;
+  const int warps = gridDim.x * (blockDim.x >> 5);
+  for (int a = blockIdx.x + gridDim.x * (threadIdx.x >> 5); a < w.n; a += warps) {
     int c = 0;
-    for (int b = 0; b < a; b++) c += is_candidate(w, a, b, prevCount) ? 1 : 0;
-    w.pairCount[a] = c;
+    for (int b0 = 0; b0 < a; b0 += 32) {
+      const int b = b0 + lane;
+      c += __popc(__ballot_sync(0xffffffffu, b < a && is_candidate(w, a, b, prevCount)));
+    }
+    if (lane == 0) w.pairCount[a] = c;
   }
 }
 
 __global__ void pairs_write_kernel(TWorld w) {
-  const int prevCount = w.ctl[1];
-  for (int a = blockIdx.x * blockDim.x + threadIdx.x; a < w.n; a += gridDim.x * blockDim.x) {
+  const int prevCount = w.ctl[1], lane = threadIdx.x & 31;
+  const int warps = gridDim.x * (blockDim.x >> 5);
+  for (int a = blockIdx.x + gridDim.x * (threadIdx.x >> 5); a < w.n; a += warps) {
     int at = w.pairStart[a];
-    for (int b = 0; b < a; b++)
-      if (is_candidate(w, a, b, prevCount)) {
-        if (at < w.mcap) w.key[at] = pair_key(a, b);
-        at++;
+    for (int b0 = 0; b0 < a; b0 += 32) {
+      const int b = b0 + lane;
+      const bool cand = b < a && is_candidate(w, a, b, prevCount);
+      const unsigned ballot = __ballot_sync(0xffffffffu, cand);
+      if (cand) {
+        const int k = at + __popc(ballot & ((1u << lane) - 1u));
+        if (k < w.mcap) w.key[k] = pair_key(a, b);
       }
+      at += __popc(ballot);
+    }
   }
   if (blockIdx.x == 0 && threadIdx.x == 0) {
     const int total = w.pairStart[w.n];
@@ -702,84 +717,148 @@ __device__ S spring_eval(const TWorld &w, const TSpring &s, S *d, S *n, int dir 
   for (int k = 0; k < 3; k++) n[k] = d[k] / len;
   return len - s.rest;
 }
-// spring.js:461-470
-__device__ bool spring_tear(TSpring &s, R Cv) {
-  if (s.rest <= 1.0e-6) return false;
-  const R strain = js_max(R(0.0), Cv / s.rest);
-  s.peak = js_max(s.peak, strain);
-  if (strain <= s.tear) return false;
-  s.broken = 1;
-  s.penalty = 0.0;
-  return true;
-}
 
+// The per-item kernels below run an item on a five-lane group, a tangent
+// direction a lane: every lane reads the item, the group synchronises, and
+// then each lane writes its direction (lane 0 the value parts and flags).
+struct GroupLane {
+  int dir, first, stride;
+  unsigned mask;
+  bool on;
+  __device__ GroupLane() {
+    const int lane = threadIdx.x & 31, slot = lane / kTangentDims;
+    const int nWarps = gridDim.x * (blockDim.x >> 5), wg = blockIdx.x + gridDim.x * (threadIdx.x >> 5);
+    dir = lane % kTangentDims;
+    on = slot < kGroupsPerWarp;
+    mask = on ? 0x1fu << (slot * kTangentDims) : 0u;
+    first = slot * nWarps + wg;  // items over the warps (and SMs) first
+    stride = nWarps * kGroupsPerWarp;
+  }
+};
+
+// Joint.initialize (joint.js:131-160) and Spring.initialize (spring.js:472-507).
 __global__ void forces_init_kernel(TWorld w) {
+  using S = Dual1;
   const TParams &P = w.P;
-  const int tid = blockIdx.x * blockDim.x + threadIdx.x, stride = gridDim.x * blockDim.x;
-  for (int k = tid; k < w.nj; k += stride) {
-    TJoint &j = w.j[k];
+  const GroupLane g;
+  if (!g.on) return;
+  const int k = g.dir;
+  const S pMin(P.penaltyMin), pMax = dir_of(P.penaltyMax, k);
+  for (int idx = g.first; idx < w.nj; idx += g.stride) {
+    TJoint &j = w.j[idx];
     if (j.removed) continue;
-    joint_eval_lin(w, j, j.C0Lin);
-    joint_eval_ang(w, j, j.C0Ang);
+    S C0L[3], C0A[3], lamL[3], lamA[3], penL[3], penA[3];
+    joint_eval_lin(w, j, C0L, k);
+    joint_eval_ang(w, j, C0A, k);
+    ldn(lamL, j.lamLin, 3, k);
+    ldn(lamA, j.lamAng, 3, k);
+    ldn(penL, j.penLin, 3, k);
+    ldn(penA, j.penAng, 3, k);
+    const S stiffL = dir_of(j.stiffLin, k), stiffA = dir_of(j.stiffAng, k);
+    const bool broken = j.broken != 0;
+    __syncwarp(g.mask);
     for (int c = 0; c < 3; c++) {
       if (!P.postStabilize) {
-        j.lamLin[c] = (j.lamLin[c] * P.alpha) * P.gamma;
-        j.lamAng[c] = (j.lamAng[c] * P.alpha) * P.gamma;
+        lamL[c] = (lamL[c] * P.alpha) * P.gamma;
+        lamA[c] = (lamA[c] * P.alpha) * P.gamma;
       }
-      j.penLin[c] = js_min(clampR(j.penLin[c] * P.gamma, R(P.penaltyMin), P.penaltyMax), j.stiffLin);
-      j.penAng[c] = js_min(clampR(j.penAng[c] * P.gamma, R(P.penaltyMin), P.penaltyMax), j.stiffAng);
+      penL[c] = js_min(clampR(penL[c] * P.gamma, pMin, pMax), stiffL);
+      penA[c] = js_min(clampR(penA[c] * P.gamma, pMin, pMax), stiffA);
+      set_dir(j.C0Lin[c], C0L[c], k);
+      set_dir(j.C0Ang[c], C0A[c], k);
+      set_dir(j.lamLin[c], lamL[c], k);
+      set_dir(j.lamAng[c], lamA[c], k);
+      set_dir(j.penLin[c], penL[c], k);
+      set_dir(j.penAng[c], penA[c], k);
     }
-    if (j.broken) j.removed = 1;  // returns !broken: leaves the force list
+    if (broken && k == 0) j.removed = 1;  // returns !broken: leaves the force list
   }
-  for (int k = tid; k < w.ns; k += stride) {
-    TSpring &s = w.s[k];
-    if (s.broken) {
-      s.penalty = 0.0;
-      continue;
+  for (int idx = g.first; idx < w.ns; idx += g.stride) {
+    TSpring &sp = w.s[idx];
+    const bool broken = sp.broken != 0;
+    S penalty = dir_of(sp.penalty, k), peak = dir_of(sp.peak, k);
+    const S stiffness = dir_of(sp.stiffness, k);
+    bool torn = false;
+    if (!broken && isfinite(sp.tear)) {
+      S d[3], n[3];
+      const S Cv = spring_eval(w, sp, d, n, k);
+      if (!(Cv != Cv) && sp.rest > 1.0e-6) {  // the tear test (spring.js:461-470)
+        const S strain = js_max(S(0.0), Cv / sp.rest);
+        peak = js_max(peak, strain);
+        torn = !(strain <= sp.tear);
+      }
     }
-    if (isfinite(s.tear)) {
-      R d[3], n[3];
-      const R Cv = spring_eval(w, s, d, n);
-      if (!(Cv != Cv) && spring_tear(s, Cv)) continue;
-    }
-    if (!P.springRamp) s.penalty = s.stiffness;
-    else s.penalty = js_min(clampR(s.penalty * P.gamma, R(P.penaltyMin), P.penaltyMax), s.stiffness);
+    __syncwarp(g.mask);
+    if (broken || torn) penalty = S(0.0);
+    else if (!P.springRamp) penalty = stiffness;
+    else penalty = js_min(clampR(penalty * P.gamma, pMin, pMax), stiffness);
+    set_dir(sp.penalty, penalty, k);
+    set_dir(sp.peak, peak, k);
+    if (torn && k == 0) sp.broken = 1;
   }
 }
 
 // solver.js:366-401: y = x + v dt + g dt^2 (z), the adaptive initial guess.
 __global__ void bodies_init_kernel(TWorld w) {
+  using S = Dual1;
   const TParams &P = w.P;
   const double dt = P.dt;
-  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < w.n; i += gridDim.x * blockDim.x) {
+  const GroupLane g;
+  if (!g.on) return;
+  const int k = g.dir;
+  for (int i = g.first; i < w.n; i += g.stride) {
     TBody &b = w.b[i];
     const bool dyn = w.bs[i].mass > 0;
-    const R g[3] = {R(0.0), R(0.0), R(P.gravity)};
-    R tmp[3];
-    for (int k = 0; k < 3; k++) b.yl[k] = b.p[k];
-    v3_add_scaled(b.yl, b.v, R(dt));
-    if (dyn) v3_add_scaled(b.yl, g, R(dt * dt));
-    for (int k = 0; k < 3; k++) tmp[k] = b.w[k] * dt;
-    q_integrate(b.yq, b.q, tmp);
-    const R accelZ = (b.v[2] - b.pv[2]) / dt;
+    S p[3], q[4], v[3], om[3];
+    ldn(p, b.p, 3, k);
+    ldn(q, b.q, 4, k);
+    ldn(v, b.v, 3, k);
+    ldn(om, b.w, 3, k);
+    const S pv2 = dir_of(b.pv[2], k);
+    __syncwarp(g.mask);
+    const S gv[3] = {S(0.0), S(0.0), S(P.gravity)};
+    S yl[3], yq[4], tmp[3];
+    for (int c = 0; c < 3; c++) yl[c] = p[c];
+    v3_add_scaled(yl, v, S(dt));
+    if (dyn) v3_add_scaled(yl, gv, S(dt * dt));
+    for (int c = 0; c < 3; c++) tmp[c] = om[c] * dt;
+    q_integrate(yq, q, tmp);
+    const S accelZ = (v[2] - pv2) / dt;
     const double sgn = P.gravity < 0 ? -1.0 : (P.gravity > 0 ? 1.0 : 0.0);
-    const R accelExt = accelZ * sgn;
-    R weight = clampR(accelExt / ::fabs(P.gravity), R(0.0), R(1.0));
+    const S accelExt = accelZ * sgn;
+    S weight = clampR(accelExt / ::fabs(P.gravity), S(0.0), S(1.0));
     if (!isfinite(weight)) weight = 0.0;
-    for (int k = 0; k < 3; k++) b.p0[k] = b.p[k];
-    for (int k = 0; k < 4; k++) b.q0[k] = b.q[k];
-    q_inverse(b.q0i, b.q0);  // q_subtract's inverses of the step's constant quaternions
-    q_inverse(b.yqi, b.yq);
+    S p0[3], q0[4], q0i[4], yqi[4];
+    for (int c = 0; c < 3; c++) p0[c] = p[c];
+    for (int c = 0; c < 4; c++) q0[c] = q[c];
+    q_inverse(q0i, q0);  // q_subtract's inverses of the step's constant quaternions
+    q_inverse(yqi, yq);
     if (dyn) {
-      v3_add_scaled(b.p, b.v, R(dt));
-      v3_add_scaled(b.p, g, weight * dt * dt);
-      R q1[4];
-      q_integrate(q1, b.q, tmp);
-      for (int k = 0; k < 4; k++) b.q[k] = q1[k];
+      v3_add_scaled(p, v, S(dt));
+      v3_add_scaled(p, gv, weight * dt * dt);
+      S q1[4];
+      q_integrate(q1, q, tmp);
+      for (int c = 0; c < 4; c++) q[c] = q1[c];
     }
-    v3_sub(b.dqL, b.p, b.p0);
-    q_subtract(b.dqA, b.q, b.q0);
-    q_inverse(b.qi, b.q);
+    S dqL[3], dqA[3], qi[4];
+    v3_sub(dqL, p, p0);
+    q_subtract(dqA, q, q0);
+    q_inverse(qi, q);
+    for (int c = 0; c < 3; c++) {
+      set_dir(b.yl[c], yl[c], k);
+      set_dir(b.p0[c], p0[c], k);
+      set_dir(b.p[c], p[c], k);
+      set_dir(b.dqL[c], dqL[c], k);
+      set_dir(b.dqA[c], dqA[c], k);
+    }
+    for (int c = 0; c < 4; c++) {
+      set_dir(b.yq[c], yq[c], k);
+      set_dir(b.q0[c], q0[c], k);
+      set_dir(b.q0i[c], q0i[c], k);
+      set_dir(b.yqi[c], yqi[c], k);
+      set_dir(b.q[c], q[c], k);
+      set_dir(b.qi[c], qi[c], k);
+    }
   }
 }
 
@@ -1560,7 +1639,7 @@ __device__ void spring_dual_dir(const TWorld &w, TSpring &s, int dir, unsigned m
   if (Cv != Cv) return;
   S peak = ld<S>(s.peak, dir), penalty = ld<S>(s.penalty, dir);
   bool torn = false;
-  if (isfinite(s.tear) && s.rest > 1.0e-6) {  // spring_tear
+  if (isfinite(s.tear) && s.rest > 1.0e-6) {  // the tear test (spring.js:461-470)
     const S strain = js_max(S(0.0), Cv / s.rest);
     peak = js_max(peak, strain);
     if (!(strain <= s.tear)) {
@@ -1976,15 +2055,16 @@ int tangent_step(TangentCtx *t, int steps, void *temp, size_t tempBytes, char *m
   using namespace tg;
   TWorld &w = t->w;
   const int blocks = std::max(1, std::min((w.n + 127) / 128, t->smCount * 4));
+  const int pairBlocks = std::max(1, std::min((w.n + 3) / 4, t->smCount * 8));  // a warp per body
   for (int s = 0; s < steps; s++) {
     cudaMemsetAsync(w.pairCount + w.n, 0, sizeof(int), st);
-    pairs_count_kernel<<<blocks, 128, 0, st>>>(w);
+    pairs_count_kernel<<<pairBlocks, 128, 0, st>>>(w);
     size_t tb = tempBytes;
     cub::DeviceScan::ExclusiveSum(temp, tb, w.pairCount, w.pairStart, w.n + 1, st);
-    pairs_write_kernel<<<blocks, 128, 0, st>>>(w);
+    pairs_write_kernel<<<pairBlocks, 128, 0, st>>>(w);
     narrow_kernel<<<t->smCount * 2, 64, 0, st>>>(w);
-    forces_init_kernel<<<blocks, 128, 0, st>>>(w);
-    bodies_init_kernel<<<blocks, 128, 0, st>>>(w);
+    forces_init_kernel<<<t->smCount * 2, 64, 0, st>>>(w);
+    bodies_init_kernel<<<t->smCount * 2, 64, 0, st>>>(w);
     adjacency_coloring_kernel<<<1, kBlock, 0, st>>>(w);
     {
       void *args[] = {(void *)&w};
