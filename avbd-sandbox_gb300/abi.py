@@ -316,7 +316,16 @@ class World:
         return len(self.scene_start) - 1
 
     def c(self, with_manifolds: bool = True) -> WorldC:
-        """The ctypes view. Rebuilt on every call so array replacement is safe."""
+        """The ctypes view, cached per `with_manifolds` while every array
+        attribute is the same array and every other attribute has the same
+        value (an array replaced or a count changed rebuilds it; the cached
+        pointers keep their arrays alive, so an array's id is not reused
+        while cached)."""
+        d = self.__dict__
+        sig = tuple((k, id(v)) if isinstance(v, np.ndarray) else (k, v) for k, v in d.items() if k != "_c")
+        cache = d.get("_c")
+        if isinstance(cache, dict) and with_manifolds in cache and cache[with_manifolds][0] == sig:
+            return cache[with_manifolds][1]
         w = WorldC()
         b = w.bodies
         b.count = self.n_bodies
@@ -350,7 +359,10 @@ class World:
             m.restitution_bias = _ptr(self.m_restitution_bias, _d)
         w.num_scenes = self.num_scenes
         w.scene_start = _ptr(self.scene_start, _i)
-        self._c = w
+        if not isinstance(cache, dict):
+            cache = {}
+        cache[with_manifolds] = (sig, w)
+        self._c = cache
         return w
 
     def copy(self) -> "World":

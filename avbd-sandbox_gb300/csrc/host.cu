@@ -11,15 +11,11 @@
 // Manifold arenas are double-buffered and swapped on the host after each step.
 #include <algorithm>
 #include <cmath>
-#include <condition_variable>
 #include <cstdarg>
 #include <cstdio>
 #include <cstring>
-#include <functional>
 #include <memory>
-#include <mutex>
 #include <string>
-#include <thread>
 #include <vector>
 
 #include "../../include/avbd_cuda.h"
@@ -44,72 +40,6 @@ struct DevBuf {
 
 }  // namespace
 
-// Host worker threads for the per-body conversions of avbd_write_state and
-// avbd_read_state (memory-bound loops over every body's f64 arrays). Started
-// with the context, joined when it is destroyed; one call at a time (a
-// context is not thread-safe).
-class HostPool {
- public:
-  explicit HostPool(int workers) {
-    for (int k = 1; k <= workers; k++) threads_.emplace_back([this, k] { loop(k); });
-  }
-  ~HostPool() {
-    {
-      std::lock_guard<std::mutex> g(m_);
-      stop_ = true;
-    }
-    wake_.notify_all();
-    for (auto &t : threads_) t.join();
-  }
-  int parts() const { return (int)threads_.size() + 1; }
-  // fn(part, begin, end) over [0, n) split into parts(); the caller runs part 0
-  void run(int n, const std::function<void(int, int, int)> &fn) {
-    {
-      std::lock_guard<std::mutex> g(m_);
-      fn_ = &fn;
-      n_ = n;
-      pending_ = (int)threads_.size();
-      gen_++;
-    }
-    wake_.notify_all();
-    fn(0, 0, range(0));
-    std::unique_lock<std::mutex> g(m_);
-    done_.wait(g, [this] { return pending_ == 0; });
-    fn_ = nullptr;
-  }
-
- private:
-  int range(int part) const { return (int)((long long)n_ * (part + 1) / parts()); }
-  void loop(int k) {
-    uint64_t seen = 0;
-    for (;;) {
-      std::unique_lock<std::mutex> g(m_);
-      wake_.wait(g, [&] { return stop_ || gen_ != seen; });
-      if (stop_) return;
-      seen = gen_;
-      const auto *fn = fn_;
-      const int b = (int)((long long)n_ * k / parts()), e = range(k);
-      g.unlock();
-      (*fn)(k, b, e);
-      g.lock();
-      if (--pending_ == 0) done_.notify_one();
-    }
-  }
-  std::vector<std::thread> threads_;
-  std::mutex m_;
-  std::condition_variable wake_, done_;
-  const std::function<void(int, int, int)> *fn_ = nullptr;
-  int n_ = 0, pending_ = 0;
-  uint64_t gen_ = 0;
-  bool stop_ = false;
-};
-
-// fn(part, begin, end) over [0, n): in parts on the pool for large n.
-constexpr int kParallelBodies = 8192;
-void for_bodies(HostPool *pool, int n, const std::function<void(int, int, int)> &fn) {
-  if (pool && n >= kParallelBodies) pool->run(n, fn);
-  else fn(0, 0, n);
-}
 
 struct avbd_ctx {
   avbd_params params{};
@@ -135,9 +65,11 @@ struct avbd_ctx {
   int curIsA = 1;
   avbd_profile prof{};
   cudaEvent_t ev[8]{};
-  // pinned staging of the per-step body state (upload / readback)
-  D4 *hPos = nullptr;
-  float4 *hQuat = nullptr, *hVel = nullptr, *hOmega = nullptr, *hPrev = nullptr;
+  // the per-step body state as the caller's f64 arrays, on the device: pos
+  // (3n), quat (4n), vel, omega, prev_vel (3n each), and the first body with
+  // a non-finite position of an upload (hBad: its pinned copy)
+  double *d64 = nullptr;
+  int *dBad = nullptr, *hBad = nullptr;
   // of the latest completed step (pinned, written by the stream): [0] steps
   // skipped for a candidate overflow since the last regrow, [1] candidates
   int *hCand = nullptr;
@@ -149,7 +81,6 @@ struct avbd_ctx {
   // The host runs at most kRunAhead steps ahead of the device, so the
   // candidate count the regrow check reads is at most that many steps old.
   static constexpr int kRunAhead = 4;
-  std::unique_ptr<HostPool> pool;  // per-body host conversions
   cudaEvent_t stepEv[8]{};
   int64_t stepSeq = 0;
   // CUDA graphs of one step, one per manifold-arena parity (the arenas swap
@@ -225,11 +156,10 @@ void free_all(avbd_ctx *ctx) {
   ctx->growable.clear();
   if (ctx->hCand) cudaFreeHost(ctx->hCand);
   ctx->hCand = nullptr;
-  void *pinned[5] = {ctx->hPos, ctx->hQuat, ctx->hVel, ctx->hOmega, ctx->hPrev};
-  for (void *p : pinned)
-    if (p) cudaFreeHost(p);
-  ctx->hPos = nullptr;
-  ctx->hQuat = ctx->hVel = ctx->hOmega = ctx->hPrev = nullptr;
+  if (ctx->hBad) cudaFreeHost(ctx->hBad);
+  ctx->hBad = nullptr;
+  ctx->d64 = nullptr;  // (in allocs)
+  ctx->dBad = nullptr;
   ctx->packed = false;
 }
 
@@ -375,38 +305,69 @@ int record(avbd_ctx *ctx, int k) {
 
 // Upload the dynamic state (bodies, joints, springs, and manifolds when
 // given) of `world` into already-sized arenas.
+// The body state between the caller's f64 arrays (copied as they are) and
+// the device layout: positions D4, the rest float4 (round to nearest, as a
+// host (float) cast), absent arrays as the host path defaulted them.
+__global__ void state_check_kernel(const double *pos, int n, int *bad) {
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x)
+    if (!(isfinite(pos[i * 3]) && isfinite(pos[i * 3 + 1]) && isfinite(pos[i * 3 + 2]))) atomicMin(bad, i);
+}
+__global__ void state_in_kernel(const double *d64, int n, unsigned present, const int *bad, D4 *pos, float4 *quat,
+                                float4 *vel, float4 *omega, float4 *prev) {
+  if (*bad < n) return;  // a non-finite position: the state stays as it was
+  const double *p = d64, *q = d64 + 3 * (size_t)n, *v = q + 4 * (size_t)n, *om = v + 3 * (size_t)n,
+               *pv = om + 3 * (size_t)n;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    pos[i] = mkd4(p[i * 3], p[i * 3 + 1], p[i * 3 + 2], 0.0);
+    quat[i] = present & 1u ? make_float4((float)q[i * 4], (float)q[i * 4 + 1], (float)q[i * 4 + 2], (float)q[i * 4 + 3])
+                           : make_float4(0.f, 0.f, 0.f, 1.f);
+    const float4 vv = present & 2u ? make_float4((float)v[i * 3], (float)v[i * 3 + 1], (float)v[i * 3 + 2], 0.f)
+                                   : make_float4(0.f, 0.f, 0.f, 0.f);
+    vel[i] = vv;
+    omega[i] = present & 4u ? make_float4((float)om[i * 3], (float)om[i * 3 + 1], (float)om[i * 3 + 2], 0.f)
+                            : make_float4(0.f, 0.f, 0.f, 0.f);
+    prev[i] = present & 8u ? make_float4((float)pv[i * 3], (float)pv[i * 3 + 1], (float)pv[i * 3 + 2], 0.f) : vv;
+  }
+}
+__global__ void state_out_kernel(const D4 *pos, const float4 *quat, const float4 *vel, const float4 *omega,
+                                 const float4 *prev, int n, double *d64) {
+  double *p = d64, *q = d64 + 3 * (size_t)n, *v = q + 4 * (size_t)n, *om = v + 3 * (size_t)n, *pv = om + 3 * (size_t)n;
+  for (int i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
+    const D4 a = pos[i];
+    p[i * 3] = a.x; p[i * 3 + 1] = a.y; p[i * 3 + 2] = a.z;
+    const float4 b = quat[i];
+    q[i * 4] = b.x; q[i * 4 + 1] = b.y; q[i * 4 + 2] = b.z; q[i * 4 + 3] = b.w;
+    const float4 c = vel[i], d = omega[i], e = prev[i];
+    v[i * 3] = c.x; v[i * 3 + 1] = c.y; v[i * 3 + 2] = c.z;
+    om[i * 3] = d.x; om[i * 3 + 1] = d.y; om[i * 3 + 2] = d.z;
+    pv[i * 3] = e.x; pv[i * 3 + 1] = e.y; pv[i * 3 + 2] = e.z;
+  }
+}
+
 int write_state(avbd_ctx *ctx, const avbd_world *world, bool keepManifolds) {
   const avbd_body_soa &B = world->bodies;
   const int n = ctx->n;
-  std::vector<int> bad(ctx->pool ? ctx->pool->parts() : 1, n);  // first non-finite body per part
-  for_bodies(ctx->pool.get(), n, [&](int part, int b, int e) {
-    for (int i = b; i < e; i++) {
-      const double *p = &B.pos[i * 3];
-      if (!finite3(p)) {
-        bad[part] = i;
-        return;
-      }
-      ctx->hPos[i] = mkd4(p[0], p[1], p[2], 0.0);
-      const double *q = B.quat ? &B.quat[i * 4] : nullptr;
-      ctx->hQuat[i] = q ? make_float4((float)q[0], (float)q[1], (float)q[2], (float)q[3]) : make_float4(0, 0, 0, 1);
-      auto v3 = [&](const double *a) {
-        return a ? make_float4((float)a[i * 3], (float)a[i * 3 + 1], (float)a[i * 3 + 2], 0.f) : make_float4(0, 0, 0, 0);
-      };
-      ctx->hVel[i] = v3(B.vel);
-      ctx->hOmega[i] = v3(B.omega);
-      ctx->hPrev[i] = B.prev_vel ? v3(B.prev_vel) : ctx->hVel[i];
-    }
-  });
-  const int firstBad = *std::min_element(bad.begin(), bad.end());
-  if (firstBad < n) return fail(ctx, AVBD_ERR_NAN, "body %d: non-finite position", firstBad);
   World &w = ctx->w;
   cudaStream_t st = ctx->stream;
-  CK(cudaMemcpyAsync(w.b.pos, ctx->hPos, n * sizeof(D4), cudaMemcpyHostToDevice, st));
-  CK(cudaMemcpyAsync(w.b.quat, ctx->hQuat, n * sizeof(float4), cudaMemcpyHostToDevice, st));
-  CK(cudaMemcpyAsync(w.b.vel, ctx->hVel, n * sizeof(float4), cudaMemcpyHostToDevice, st));
-  CK(cudaMemcpyAsync(w.b.omega, ctx->hOmega, n * sizeof(float4), cudaMemcpyHostToDevice, st));
-  CK(cudaMemcpyAsync(w.b.prevVel, ctx->hPrev, n * sizeof(float4), cudaMemcpyHostToDevice, st));
-  CK(cudaStreamSynchronize(st));
+  {  // the caller's arrays straight to the device (GB300: host memory over NVLink-C2C), converted there
+    const size_t N = (size_t)n;
+    double *p = ctx->d64, *q = p + 3 * N, *v = q + 4 * N, *om = v + 3 * N, *pv = om + 3 * N;
+    const unsigned present = (B.quat ? 1u : 0u) | (B.vel ? 2u : 0u) | (B.omega ? 4u : 0u) | (B.prev_vel ? 8u : 0u);
+    CK(cudaMemcpyAsync(p, B.pos, 3 * N * sizeof(double), cudaMemcpyHostToDevice, st));
+    if (B.quat) CK(cudaMemcpyAsync(q, B.quat, 4 * N * sizeof(double), cudaMemcpyHostToDevice, st));
+    if (B.vel) CK(cudaMemcpyAsync(v, B.vel, 3 * N * sizeof(double), cudaMemcpyHostToDevice, st));
+    if (B.omega) CK(cudaMemcpyAsync(om, B.omega, 3 * N * sizeof(double), cudaMemcpyHostToDevice, st));
+    if (B.prev_vel) CK(cudaMemcpyAsync(pv, B.prev_vel, 3 * N * sizeof(double), cudaMemcpyHostToDevice, st));
+    CK(cudaMemsetAsync(ctx->dBad, 0x7f, sizeof(int), st));  // 0x7f7f7f7f: above any body index
+    const int grid = std::max(1, std::min((n + 255) / 256, ctx->smCount * 4));
+    state_check_kernel<<<grid, 256, 0, st>>>(p, n, ctx->dBad);
+    state_in_kernel<<<grid, 256, 0, st>>>(ctx->d64, n, present, ctx->dBad, w.b.pos, w.b.quat, w.b.vel, w.b.omega,
+                                          w.b.prevVel);
+    CK(cudaMemcpyAsync(ctx->hBad, ctx->dBad, sizeof(int), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    CK(cudaGetLastError());
+    if (*ctx->hBad < n) return fail(ctx, AVBD_ERR_NAN, "body %d: non-finite position", *ctx->hBad);
+  }
 
   const avbd_joint_soa &J = world->joints;
   if (ctx->nj) {
@@ -1148,10 +1109,6 @@ int avbd_pack(avbd_ctx *ctx, const avbd_world *world) {
   // launch shape of the persistent solve
   const int maxPerSm = solve_max_blocks_per_sm(ctx->lanes);
   ctx->autoLanes = P.lanes_per_body <= 0;
-  if (n >= kParallelBodies && !ctx->pool) {
-    const int hc = (int)std::thread::hardware_concurrency();
-    ctx->pool.reset(new HostPool(std::max(1, std::min(7, hc - 1))));
-  }
   ctx->lanes = P.lanes_per_body > 0 ? P.lanes_per_body : 32;
   ctx->nDyn = 0;
   for (int i = 0; i < n; i++) ctx->nDyn += B.mass[i] > 0 ? 1 : 0;
@@ -1163,11 +1120,11 @@ int avbd_pack(avbd_ctx *ctx, const avbd_world *world) {
   w.p.solveBlocksPerSm = ctx->blocksPerSm;
   // colours start at 0 for dynamic bodies
   CK(cudaMemset(w.b.color, 0, sizeof(int) * n));
-  CK(cudaMallocHost((void **)&ctx->hPos, sizeof(D4) * n));
-  CK(cudaMallocHost((void **)&ctx->hQuat, sizeof(float4) * n));
-  CK(cudaMallocHost((void **)&ctx->hVel, sizeof(float4) * n));
-  CK(cudaMallocHost((void **)&ctx->hOmega, sizeof(float4) * n));
-  CK(cudaMallocHost((void **)&ctx->hPrev, sizeof(float4) * n));
+  if ((rc = dalloc(ctx, &ctx->d64, (size_t)16 * n)) || (rc = dalloc(ctx, &ctx->dBad, 1))) return rc;
+  CK(cudaMallocHost((void **)&ctx->hBad, sizeof(int)));
+  // dalloc's zero fills run on the legacy default stream, which the context's
+  // non-blocking stream does not wait for: finish them before the upload
+  CK(cudaDeviceSynchronize());
   ctx->packed = true;
   ctx->stepSeq = 0;
   ctx->steps = 0;
@@ -1209,23 +1166,19 @@ int avbd_read_state(avbd_ctx *ctx, avbd_world *out) {
   avbd_body_soa &B = out->bodies;
   if (B.count < n) return fail(ctx, AVBD_ERR_ARG, "avbd_read_state: body arrays hold %d < %d", B.count, n);
   cudaStream_t st = ctx->stream;
-  CK(cudaMemcpyAsync(ctx->hPos, w.b.pos, n * sizeof(D4), cudaMemcpyDeviceToHost, st));
-  CK(cudaMemcpyAsync(ctx->hQuat, w.b.quat, n * sizeof(float4), cudaMemcpyDeviceToHost, st));
-  CK(cudaMemcpyAsync(ctx->hVel, w.b.vel, n * sizeof(float4), cudaMemcpyDeviceToHost, st));
-  CK(cudaMemcpyAsync(ctx->hOmega, w.b.omega, n * sizeof(float4), cudaMemcpyDeviceToHost, st));
-  CK(cudaMemcpyAsync(ctx->hPrev, w.b.prevVel, n * sizeof(float4), cudaMemcpyDeviceToHost, st));
-  CK(cudaStreamSynchronize(st));
-  const D4 *pos = ctx->hPos;
-  const float4 *q = ctx->hQuat, *v = ctx->hVel, *om = ctx->hOmega, *pv = ctx->hPrev;
-  for_bodies(ctx->pool.get(), n, [&](int, int b, int e) {
-    for (int i = b; i < e; i++) {
-      if (B.pos) { B.pos[i * 3] = pos[i].x; B.pos[i * 3 + 1] = pos[i].y; B.pos[i * 3 + 2] = pos[i].z; }
-      if (B.quat) { B.quat[i * 4] = q[i].x; B.quat[i * 4 + 1] = q[i].y; B.quat[i * 4 + 2] = q[i].z; B.quat[i * 4 + 3] = q[i].w; }
-      if (B.vel) { B.vel[i * 3] = v[i].x; B.vel[i * 3 + 1] = v[i].y; B.vel[i * 3 + 2] = v[i].z; }
-      if (B.omega) { B.omega[i * 3] = om[i].x; B.omega[i * 3 + 1] = om[i].y; B.omega[i * 3 + 2] = om[i].z; }
-      if (B.prev_vel) { B.prev_vel[i * 3] = pv[i].x; B.prev_vel[i * 3 + 1] = pv[i].y; B.prev_vel[i * 3 + 2] = pv[i].z; }
-    }
-  });
+  {  // converted on the device, then straight into the caller's arrays
+    const size_t N = (size_t)n;
+    const double *p = ctx->d64, *q = p + 3 * N, *v = q + 4 * N, *om = v + 3 * N, *pv = om + 3 * N;
+    const int grid = std::max(1, std::min((n + 255) / 256, ctx->smCount * 4));
+    state_out_kernel<<<grid, 256, 0, st>>>(w.b.pos, w.b.quat, w.b.vel, w.b.omega, w.b.prevVel, n, ctx->d64);
+    if (B.pos) CK(cudaMemcpyAsync(B.pos, p, 3 * N * sizeof(double), cudaMemcpyDeviceToHost, st));
+    if (B.quat) CK(cudaMemcpyAsync(B.quat, q, 4 * N * sizeof(double), cudaMemcpyDeviceToHost, st));
+    if (B.vel) CK(cudaMemcpyAsync(B.vel, v, 3 * N * sizeof(double), cudaMemcpyDeviceToHost, st));
+    if (B.omega) CK(cudaMemcpyAsync(B.omega, om, 3 * N * sizeof(double), cudaMemcpyDeviceToHost, st));
+    if (B.prev_vel) CK(cudaMemcpyAsync(B.prev_vel, pv, 3 * N * sizeof(double), cudaMemcpyDeviceToHost, st));
+    CK(cudaStreamSynchronize(st));
+    CK(cudaGetLastError());
+  }
   avbd_joint_soa &J = out->joints;
   if (ctx->nj && J.count >= ctx->nj) {
     std::vector<float4> kl(ctx->nj), ka(ctx->nj);
