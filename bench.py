@@ -329,14 +329,15 @@ def run_gpu(args):
     abi = pkg().abi
     backend = importlib.import_module("avbd-sandbox_gb300.backend")
     s = make_scene(args.layers)
-    params = params_for(abi, s)
+    params = params_for(abi, s)  # direct launches: the per-phase events (phases, roofline)
     world = s.world()
-    gpu = backend.GpuBackend(params)
+    # the headline: every step replayed as one CUDA graph (the same kernels)
+    gpu = backend.GpuBackend(params_for(abi, s, graph=1))
     gpu.pack(world)
     n_dyn = int((world.mass > 0).sum())
     n = world.n_bodies
     K = args.steps
-    per_body = 32 + 4 * 16  # f64 position (D4) + quaternion, velocity, angular velocity, previous velocity (float4)
+    per_body = 8 * 16  # the caller's f64 arrays: position 3, quaternion 4, velocity, angular and previous velocity 3
 
     gpu.step(args.warmup)
     gpu.idle()
@@ -346,14 +347,22 @@ def run_gpu(args):
         torch.distributed.barrier()
     torch.cuda.synchronize()
     t0 = time.perf_counter()
-    trace = open(args.trace, "w") if args.trace and rank == 0 else None
     with ClockSampler(local) as clk:
-        rec = timed_window(gpu, K, flush, n_dyn, params.iterations, trace)
-    if trace:
-        trace.close()
+        rec = timed_window(gpu, K, flush, n_dyn, params.iterations)
     torch.cuda.synchronize()
     wall = time.perf_counter() - t0
     dev_s = slowest_rank(sum(rec["step_ms"]) / 1e3, ws)
+    # the same steps launched directly, for the split by phase and the roofline
+    direct = backend.GpuBackend(params)
+    direct.pack(world)
+    direct.step(args.warmup)
+    direct.idle()
+    direct.pack(world)
+    trace = open(args.trace, "w") if args.trace and rank == 0 else None
+    prec = timed_window(direct, K, flush, n_dyn, params.iterations, trace)
+    if trace:
+        trace.close()
+    direct.destroy()
 
     # end to end over the same K steps; states for the CPU baseline on the way
     cpu = rank == 0 and not args.no_cpu_baseline
@@ -379,14 +388,17 @@ def run_gpu(args):
         "dtype": "f32 (f64 narrowphase geometry, f64 positions and joint multipliers)",
         "data": "synthetic",
         "config": bench_config(args, n, ws),
-        "roofline": roofline(rec, K, "sparse" if K <= 60 else "run"),
+        "roofline": roofline(prec, K, "sparse" if K <= 60 else "run"),
         "e2e": {"value": replica_rate(K, ws, e2e_s), "unit": UNIT, "h2d_bytes_per_step": n * per_body,
                 "d2h_bytes_per_step": n * per_body,
-                "how": "avbd_write_state + avbd_step(1) + avbd_read_state every step over the same steps, pinned "
-                       "staging, host f64 arrays"},
+                "how": "avbd_write_state + avbd_step(1) + avbd_read_state every step over the same steps: the "
+                       "caller's f64 arrays copied to and from the device as they are, converted there"},
+        "step_launch": "each timed step one CUDA graph (params.graph = 1); phases_ms and the roofline from the "
+                       "same steps launched directly, with events between the phases",
         "gpu_launches": rec["launches"],
         "clocks": clocks,
-        "phases_ms": {k: v / K for k, v in rec["phases"].items()},
+        "phases_ms": {k: v / K for k, v in prec["phases"].items()},
+        "phases_total_ms": sum(prec["step_ms"]) / K,
         "wall_s": wall,
         "mean_work_per_step": {k: v / K for k, v in rec["work"].items()},
         "peak_work": rec["peak"],
@@ -430,7 +442,7 @@ def run_dense(abi, backend, args, s, world, params, flush, n_dyn, ws, rank):
     snap_at = sorted({int(round(k * (K - 1) / 5.0)) - 1 for k in range(6)} - {-1}) if cpu else []
     e2e_s, snaps = e2e_window(gpu, start, K, snap_at)
     e2e_s = slowest_rank(e2e_s, ws)
-    per_body = 32 + 4 * 16
+    per_body = 8 * 16  # the caller's f64 body arrays, each way
     out = {"value": replica_rate(K, ws, dev_s), "unit": UNIT, "steps": K, "start_step": D,
            "ms_per_step": dev_s * 1e3 / K,
            "timed_steps": f"steps {D + 1}..{D + K} of the run (the state after step {D} reached on the device "
