@@ -67,7 +67,7 @@ struct SolverParams {
   int lanes;     // lanes per body of the colour-phase solve; 0: per body, from its constraint count
   int solveBlocksPerSm;  // resident blocks per SM of the solve launch (grid = this x SMs)
   long long barrierLimit, waitLimit;  // polls before a grid barrier / a neighbour wait gives up
-  int tailDiv;   // colours of at most (grid / tailDiv) chunks form the tail segment
+  int tailDiv;   // colours of at most (grid / tailDiv) chunks form the tail segment; 0 automatic, < 0 none
   // AVBD_CONTACT_MATERIALS (the WebGPU engine's contact extensions) when 1
   int contactModel;
   double restitutionThreshold, contactPersistence;

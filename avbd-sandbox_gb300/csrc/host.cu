@@ -708,7 +708,7 @@ void apply_config(avbd_ctx *ctx, const TuneConfig &c) {
   P.blocks_per_sm = c.blocksPerSm;
   ctx->w.p.schedule = c.schedule == 1 ? 1 : 0;
   ctx->w.p.lanes = c.lanes > 0 ? c.lanes : 0;
-  ctx->w.p.tailDiv = c.tailDiv > 0 ? c.tailDiv : 8;
+  ctx->w.p.tailDiv = c.tailDiv;
   ctx->autoLanes = c.lanes <= 0;
   ctx->lanes = c.lanes > 0 ? c.lanes : 32;
   ctx->blocksPerSm = c.blocksPerSm;
@@ -984,7 +984,7 @@ int avbd_pack(avbd_ctx *ctx, const avbd_world *world) {
                      P.wait_limit > 0 ? (long long)P.wait_limit : 20000000LL,
                      P.neighbor_wait_limit > 0 ? (long long)P.neighbor_wait_limit
                                                : (P.wait_limit > 0 ? (long long)P.wait_limit : 4000000LL),
-                     P.tail_div > 0 ? P.tail_div : 8, P.contact_model == AVBD_CONTACT_MATERIALS ? 1 : 0,
+                     P.tail_div, P.contact_model == AVBD_CONTACT_MATERIALS ? 1 : 0,
                      P.restitution_threshold, P.contact_persistence};
   int rc = 0;
   D4 *sizeP, *massDP;
@@ -1607,13 +1607,13 @@ int avbd_autotune(avbd_ctx *ctx, int32_t trial_steps, avbd_tuning *out) {
   Snapshot snap;
   int rc = take_snapshot(ctx, snap);
   if (rc) return rc;
-  const TuneConfig start{ctx->params.schedule == 1 ? 1 : 0, ctx->autoLanes ? 0 : ctx->lanes,
-                         ctx->params.tail_div > 0 ? ctx->params.tail_div : 8, ctx->blocksPerSm};
+  const TuneConfig start{ctx->params.schedule == 1 ? 1 : 0, ctx->autoLanes ? 0 : ctx->lanes, ctx->params.tail_div,
+                         ctx->blocksPerSm};
   std::vector<TuneConfig> cands = {start};
   const int maxB = ctx->maxBlocksPerSm;
   for (int b = maxB; b >= std::max(1, maxB - 1); b--) {
     for (int lanes : {0, 32})
-      for (int td : {4, 8, 16}) cands.push_back({0, lanes, td, b});
+      for (int td : {0, -1, 4, 8, 16}) cands.push_back({0, lanes, td, b});  // automatic, no tail, explicit
     for (int lanes : {16, 32}) cands.push_back({1, lanes, 8, b});
   }
   std::memset(out, 0, sizeof(*out));

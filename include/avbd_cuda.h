@@ -121,7 +121,9 @@ typedef struct avbd_params {
   int32_t neighbor_wait_limit;
   /* Colour-phase schedule: colours of at most (solve blocks / tail_div) lane
      chunks run as one dependency-driven tail segment per iteration instead
-     of one grid barrier each; 0 = 8. Does not change results. */
+     of one grid barrier each. 0 (automatic): tail_div 8 for steps of at
+     least 16 colours, no tail segment for fewer; > 0: that tail_div every
+     step; < 0: no tail segment. Does not change results. */
   int32_t tail_div;
   /* 1: each step is replayed as a CUDA graph (captured on first use, once
      per manifold-arena parity; rebuilt after a pack, an arena regrow, an

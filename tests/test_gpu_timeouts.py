@@ -39,12 +39,14 @@ def test_wait_gives_up_and_reports_timeout(abi, scenes, backend_mod, schedule):
 
 @pytest.mark.parametrize("schedule", [0, 1])
 def test_neighbour_wait_gives_up_and_reports_timeout(abi, scenes, backend_mod, schedule):
-    """A hanging chain (links in two thin colours, so that the colour-phase
-    schedule runs them in its tail segment) and a spring chain: a body of the
-    second colour reaches its wait while its first-colour neighbour is still
-    being solved, and one poll is not enough."""
+    """A hanging chain (links in two thin colours, which the colour-phase
+    schedule with an explicit tail_div runs in its tail segment; the
+    automatic rule keeps a barrier per colour for so few colours) and a spring
+    chain: a body of the second colour reaches its wait while its
+    first-colour neighbour is still being solved, and one poll is not
+    enough."""
     s = scenes.heavy_chain(links=8, springs=10)
-    gpu = backend_mod.GpuBackend(abi.default_params(**s.params, schedule=schedule, neighbor_wait_limit=1))
+    gpu = backend_mod.GpuBackend(abi.default_params(**s.params, schedule=schedule, neighbor_wait_limit=1, tail_div=8))
     gpu.pack(s.world())
     gpu.step(5)
     with pytest.raises(backend_mod.AvbdError) as e:
