@@ -1,5 +1,6 @@
 """The C-ABI library builds for sm_103a, loads, and exports every function
-declared in include/avbd_cuda.h (no GPU needed)."""
+declared in include/avbd_cuda.h (no GPU needed); the host side's ctypes
+view of a world."""
 import ctypes
 import importlib
 import os
@@ -55,3 +56,24 @@ def test_default_params_match_reference(abi):
     assert (p.penalty_min, p.penalty_max, p.collision_margin, p.stick_threshold) == (1.0, 1e10, 0.01, 1e-5)
     assert (p.rotated_inertia, p.spring_stiffness_ramp, p.spring_geometric_stiffness,
             p.cached_contact_jacobians, p.post_stabilize) == (1, 0, 1, 1, 0)
+
+
+def test_world_ctypes_view_is_cached_until_an_array_or_count_changes(abi, scenes):
+    """World.c() keeps its ctypes view while the world's arrays are the same
+    objects and its counts the same values (the per-step write_state /
+    read_state calls reuse it); replacing an array or changing a count gives
+    a fresh view with the new pointer or count."""
+    w = scenes.pyramid(layers=4).world()
+    a = w.c()
+    assert w.c() is a
+    b = w.c(with_manifolds=False)
+    assert b is not a and w.c(with_manifolds=False) is b and w.c() is a
+    w.pos[0, 0] += 1.0  # in place: the same buffer, the same view
+    assert w.c() is a
+    w.pos = w.pos.copy()
+    c = w.c()
+    assert c is not a
+    assert ctypes.cast(c.bodies.pos, ctypes.c_void_p).value == w.pos.ctypes.data
+    w.m_count = w.m_count + 1
+    d = w.c()
+    assert d is not c and d.manifolds.count == w.m_count

@@ -225,3 +225,55 @@ def test_uniform_grab_matches_oracle(abi, scenes, backend_mod, schedule):
     gpu.step(3)
     gpu.idle()
     assert np.max(np.abs(gpu.read_state().pos[dyn] - ref.state().pos[dyn])) < 5e-3
+
+
+def test_state_upload_round_trip_and_non_finite_rejection(abi, scenes, backend_mod):
+    """avbd_write_state copies the caller's f64 arrays to the device as they
+    are and converts them there: reading the state back gives the positions
+    exactly and the f32-held fields rounded to f32. A position that is not
+    finite is caught on the device: AVBD_ERR_NAN naming the first such body,
+    and the device state stays what it was."""
+    s = scenes.pyramid(layers=6)
+    gpu = backend_mod.GpuBackend(abi.default_params(**s.params))
+    gpu.pack(s.world())
+    gpu.step(4)
+    host = gpu.read_state()
+    rng = np.random.default_rng(7)
+    host.pos = host.pos + rng.normal(0.0, 1e-3, host.pos.shape)
+    host.vel = rng.normal(0.0, 1.0, host.vel.shape)
+    gpu.write_state(host)
+    back = gpu.read_state()
+    f32 = lambda a: a.astype(np.float32).astype(np.float64)
+    assert np.array_equal(back.pos, host.pos)
+    assert np.array_equal(back.vel, f32(host.vel))
+    assert np.array_equal(back.quat, f32(host.quat))
+    bad = host.copy()
+    bad.pos[5, 1] = np.nan
+    bad.pos[9, 0] = np.inf
+    with pytest.raises(backend_mod.AvbdError) as e:
+        gpu.write_state(bad)
+    assert e.value.code == abi.AVBD_ERR_NAN and "body 5" in str(e.value)
+    after = gpu.read_state()
+    assert np.array_equal(after.pos, back.pos) and np.array_equal(after.vel, back.vel)
+    gpu.step(1)
+    gpu.idle()
+
+
+@pytest.mark.parametrize("name", ["pyramid", "joint_clique"])
+def test_tail_segment_rule_does_not_change_results(abi, scenes, backend_mod, name):
+    """The colour-phase schedule's tail segment - automatic (tail_div 0: only
+    for steps of at least 16 colours), forced (8) or off (-1) - orders the
+    same body updates, so the states are bit-identical; the pyramid has a few
+    colours a step, the joint clique 72."""
+    s = scenes.pyramid(layers=8) if name == "pyramid" else scenes.joint_clique()
+    states = []
+    for td in (0, 8, -1):
+        gpu = backend_mod.GpuBackend(abi.default_params(**s.params, body_order=abi.ORDER_PRIORITY, tail_div=td))
+        gpu.pack(s.world())
+        gpu.step(12)
+        gpu.idle()
+        states.append(gpu.read_state())
+        gpu.destroy()
+    for other in states[1:]:
+        assert np.array_equal(other.pos, states[0].pos) and np.array_equal(other.quat, states[0].quat)
+        assert np.array_equal(other.vel, states[0].vel)
