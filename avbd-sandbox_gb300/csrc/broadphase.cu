@@ -682,10 +682,19 @@ extern "C" int avbd_overlap_pairs_static(int32_t n, const double *pos, const dou
              e != cudaSuccess ? cudaGetErrorString(e) : "device ordinal out of range");
     return set_context_free_error(AVBD_ERR_CUDA, msg);
   }
+  cudaStream_t st = (cudaStream_t)stream;
+  // The array's address, looked up again on every call outside a stream
+  // capture (a module reloaded after cudaDeviceReset, or another context
+  // current on the device, moves it); a capture uses the last address seen.
+  cudaStreamCaptureStatus capturing = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(st, &capturing) != cudaSuccess) {
+    cudaGetLastError();
+    capturing = cudaStreamCaptureStatusNone;
+  }
   unsigned char *base = nullptr;
   {
     std::lock_guard<std::mutex> lock(g_static_mutex);
-    if (!g_static_ptr[dev]) {
+    if (!g_static_ptr[dev] || capturing == cudaStreamCaptureStatusNone) {
       void *p = nullptr;
       e = cudaGetSymbolAddress(&p, g_static_scratch);
       if (e != cudaSuccess) {
@@ -696,7 +705,6 @@ extern "C" int avbd_overlap_pairs_static(int32_t n, const double *pos, const dou
     }
     base = (unsigned char *)g_static_ptr[dev];
   }
-  cudaStream_t st = (cudaStream_t)stream;
   if (n == 0) {
     e = cudaMemsetAsync(count, 0, sizeof(int32_t), st);
     if (e != cudaSuccess) {

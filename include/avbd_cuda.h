@@ -518,14 +518,13 @@ const char *avbd_last_error(const avbd_ctx *ctx);
  *              non-finite or beyond 1e9 cells from the origin
  *   stream     a cudaStream_t (NULL = the legacy default stream)
  *
- * The results are ready when the stream reaches the end of the call. The
- * first call on each device looks up the scratch array's address
- * (cudaGetSymbolAddress) with that device current; when a call may happen
- * while its stream is being captured, make one call on that device before.
- * The address is kept per device ordinal for the life of the process, so it
- * belongs to the device's primary context: after cudaDeviceReset of that
- * device, or from a different (driver-API) context current on it, do not
- * call this function again in the same process.
+ * The results are ready when the stream reaches the end of the call. Every
+ * call outside a stream capture looks up the scratch array's address
+ * (cudaGetSymbolAddress, allocation-free) with the calling context current;
+ * a call while its stream is being captured (the call allocates nothing, so
+ * it can be captured into a CUDA graph) uses the address of the last call
+ * on that device, so make one call outside the capture first, with the
+ * context the graph will run in.
  * All calls on a device share the one scratch array, and every call resets
  * the parts that must start at zero: two calls whose executions overlap (on
  * different streams, or from different host threads without ordering) race

@@ -112,3 +112,42 @@ def test_static_pairs_rejects_too_many_bodies(backend_mod):
     with pytest.raises(backend_mod.AvbdError) as e:
         backend_mod.overlap_pairs_static(backend_mod.STATIC_PAIRS_MAX_BODIES + 1, 1, 1, 0, 1.0, 1, 1, 1, 0)
     assert "at most 65000" in str(e.value)
+
+
+def test_static_pairs_capture_into_a_graph(abi, scenes, backend_mod):
+    """The call allocates nothing and never waits on the host, so it can be
+    captured into a CUDA graph (a cudaMalloc inside a capture would fail it);
+    replaying the graph gives the pairs of a direct call."""
+    torch = pytest.importorskip("torch")
+    s = scenes.random_pile(300, seed=11)
+    w = s.world()
+    expect = step_pairs(abi, backend_mod, s)
+    dev = torch.device("cuda", torch.cuda.current_device())
+    pos = torch.tensor(np.ascontiguousarray(w.pos), dtype=torch.float64, device=dev)
+    rad = torch.tensor(np.ascontiguousarray(w.radius), dtype=torch.float64, device=dev)
+    dyn = torch.tensor((w.mass > 0).astype(np.int32), device=dev)
+    cap = len(expect) + 64
+    r = np.asarray(w.radius)
+    cell = 2.0 * float(r[r <= 2 * np.median(r)].max()) * (1 + 1e-6) + 1e-9
+    keys = torch.full((cap,), -1, dtype=torch.int64, device=dev)
+    count = torch.full((1,), -7, dtype=torch.int32, device=dev)
+    side = torch.cuda.Stream()
+    with torch.cuda.stream(side):  # one call outside the capture: the array's address
+        backend_mod.overlap_pairs_static(w.n_bodies, pos.data_ptr(), rad.data_ptr(), dyn.data_ptr(), cell,
+                                         keys.data_ptr(), cap, count.data_ptr(), side.cuda_stream)
+    torch.cuda.synchronize()
+    keys.fill_(-1)
+    count.fill_(-7)
+    torch.cuda.synchronize()
+    g = torch.cuda.CUDAGraph()
+    with torch.cuda.graph(g):
+        backend_mod.overlap_pairs_static(w.n_bodies, pos.data_ptr(), rad.data_ptr(), dyn.data_ptr(), cell,
+                                         keys.data_ptr(), cap, count.data_ptr(),
+                                         torch.cuda.current_stream().cuda_stream)
+    torch.cuda.synchronize()
+    assert int(count.item()) == -7  # captured, not run
+    g.replay()
+    torch.cuda.synchronize()
+    n = int(count.item())
+    got = keys[:n].cpu().numpy().view(np.uint64)
+    assert np.array_equal(got, expect)
