@@ -548,20 +548,41 @@ __device__ void coloring_finish(const World &w) {
   if (!grid_barrier(ctl, w.p.barrierLimit)) return;
   if (blockIdx.x == 0) {
     // per colour: the blocks' offsets (a scan over blocks), then the colours'
-    // starts (a block-wide scan over colours, in rounds of blockDim colours)
+    // starts (a block-wide scan over colours, in rounds of blockDim colours).
+    // A round's colours share the block's threads: `parts` threads a colour,
+    // each summing, then offsetting, a contiguous run of blocks (the counts
+    // are integers: any grouping gives the same offsets).
     __shared__ int scan[256];
+    __shared__ int partSum[256];
     __shared__ int carry;
     if (threadIdx.x == 0) carry = 0;
     __syncthreads();
     for (int c0 = 0; c0 < numColors; c0 += blockDim.x) {
-      const int c = c0 + threadIdx.x;
-      int run = 0;
-      if (c < numColors)
-        for (int b = 0; b < (int)gridDim.x; b++) {
-          const int h = w.a.blockHist[b * kMaxColors + c];
-          w.a.blockHist[b * kMaxColors + c] = run;
+      const int round = min((int)blockDim.x, numColors - c0);
+      const int parts = max(1, (int)blockDim.x / round);
+      const int cl = (int)threadIdx.x / parts, part = (int)threadIdx.x % parts;
+      const int len = ((int)gridDim.x + parts - 1) / parts, bb = part * len, be = min((int)gridDim.x, bb + len);
+      const bool mine = cl < round;
+      const int cc = c0 + cl;
+      int sum = 0;
+      if (mine)
+        for (int b = bb; b < be; b++) sum += w.a.blockHist[b * kMaxColors + cc];
+      partSum[threadIdx.x] = sum;
+      __syncthreads();
+      if (mine) {
+        int run = 0;
+        for (int q = 0; q < part; q++) run += partSum[cl * parts + q];
+        for (int b = bb; b < be; b++) {
+          const int h = w.a.blockHist[b * kMaxColors + cc];
+          w.a.blockHist[b * kMaxColors + cc] = run;
           run += h;
         }
+      }
+      const int c = c0 + threadIdx.x;
+      int run = 0;  // colour c's total
+      if (threadIdx.x < round)
+        for (int q = 0; q < parts; q++) run += partSum[threadIdx.x * parts + q];
+      __syncthreads();
       scan[threadIdx.x] = run;
       __syncthreads();
       for (int d = 1; d < (int)blockDim.x; d <<= 1) {  // inclusive scan
