@@ -1117,6 +1117,32 @@ __device__ void stamp_rows(Sink &s, const S *jLin, const S *jAng, const S *Kd, c
   }
 }
 
+// stamp_rows for a ball socket's rows, J_lin = sgn I and J_ang = the skew J
+// (zero diagonal): each entry's nonzero terms in stamp_rows's order and no
+// products with the zeros and ones (the sums lose only exact zero terms, so
+// the values are stamp_rows's); every entry still gets its one addend.
+template <class S, class Sink>
+__device__ void stamp_joint_rows(Sink &s, double sgn, const S *J, const S *Kd, const S *F) {
+  const S one(sgn), zero(0.0);
+  for (int r = 0; r < 3; r++)
+    for (int c = 0; c < 3; c++) {
+      s.lin[r * 3 + c] += r == c ? (one * Kd[r]) * one : zero;
+      if (r == c) {
+        const int k1 = r == 0 ? 1 : 0, k2 = r == 2 ? 1 : 2;
+        s.ang[r * 3 + c] += (J[k1 * 3 + r] * Kd[k1]) * J[k1 * 3 + c] + (J[k2 * 3 + r] * Kd[k2]) * J[k2 * 3 + c];
+      } else {
+        const int k = 3 - r - c;
+        s.ang[r * 3 + c] += (J[k * 3 + r] * Kd[k]) * J[k * 3 + c];
+      }
+      s.cross[r * 3 + c] += (J[c * 3 + r] * Kd[c]) * one;
+    }
+  for (int r = 0; r < 3; r++) {
+    const int k1 = r == 0 ? 1 : 0, k2 = r == 2 ? 1 : 2;
+    s.bl[r] += one * F[r];
+    s.ba[r] += J[k1 * 3 + r] * F[k1] + J[k2 * 3 + r] * F[k2];
+  }
+}
+
 // manifold.js:411-445, contact i of the manifold
 template <class S, class Sink>
 __device__ void contact_primal(const TWorld &w, const TManifold &m, int i, int side, R alpha, Sink &s, int dir) {
@@ -1180,18 +1206,16 @@ __device__ void joint_primal(const TWorld &w, const TJoint &j, int side, R alpha
     }
     ldn(pen, j.penLin, 3, dir);
     for (int k = 0; k < 3; k++) F[k] = pen[k] * C[k] + ld<S>(j.lamLin[k], dir);
-    S jLin[9], jAng[9], r[3];
+    S jAng[9], r[3];  // J_lin = I (body a) or -I (body b)
     if (!side) {  // body a (j.a >= 0)
-      m3_diag(jLin, S(1.0), S(1.0), S(1.0));
       for (int k = 0; k < 3; k++) r[k] = -rAW[k];
       m3_skew(jAng, r);
       for (int k = 0; k < 3; k++) r[k] = rAW[k];
     } else {
-      m3_diag(jLin, S(-1.0), S(-1.0), S(-1.0));
       m3_skew(jAng, rBW);
       for (int k = 0; k < 3; k++) r[k] = -rBW[k];
     }
-    stamp_rows(s, jLin, jAng, pen, F);
+    stamp_joint_rows(s, side ? -1.0 : 1.0, jAng, pen, F);
     S G[9];
     ball_socket_geometric(G, r, F);
     m3_add_into(s.ang, G);
