@@ -29,8 +29,16 @@
 // colouring (src/physics/gpu/layout.js:50-66), as the CUDA backend's step.
 //
 // Layout: small scenes (the differentiable workloads: hundreds of bodies),
-// structure of records, one thread per pair / force / body; the iterations
-// run in one block (colour phases separated by __syncthreads).
+// structure of records. GB300's FP64 issue costs an SM sub-partition the same
+// per warp instruction however few of its lanes are active, so the kernels
+// compute in Dual1 - the value and one tangent direction - on five lanes per
+// item, one direction a lane (every lane also computes the value and takes
+// the same branches), and give each kind of work its own warps: the narrow
+// phase, the force and body initialisations and the dual updates an item per
+// five-lane group; the iterations one cooperative block per SM, a body
+// update per block (its constraint rows on five-lane groups by kind, their
+// addends summed in the f64 engine's order, the 6x6 LDL^T on six lanes a
+// direction), bounded grid barriers between colour phases.
 #include <cub/cub.cuh>
 
 #include <cstdio>
