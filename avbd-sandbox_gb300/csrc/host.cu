@@ -248,6 +248,9 @@ int one_step(avbd_ctx *ctx);
 int resolve_skips(avbd_ctx *ctx) {
   for (int round = 0; round < 4; round++) {
     CK(cudaStreamSynchronize(ctx->stream));
+    // the stream copied each step's skip count to hCand[0] (pinned): nothing
+    // skipped, nothing to read back
+    if (round == 0 && ctx->hCand[0] <= 0) return AVBD_OK;
     Control c{};
     CK(cudaMemcpy(&c, ctx->w.ctl, sizeof(Control), cudaMemcpyDeviceToHost));
     ctx->hCand[0] = 0;
